@@ -1,0 +1,628 @@
+"""ctypes binding of libaleator_gb300.so and the reference-shaped Python API."""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libaleator_gb300.so"
+
+TRUNCATED, SHIFTED, LINEAR_FORCE_SHIFTED = 0, 1, 2
+LORENTZ_BERTHELOT, GEOMETRIC = 0, 1
+FP64, FP32 = 0, 1
+ALEA_DRAWS_RIGHT_TO_LEFT, ALEA_DRAWS_LEFT_TO_RIGHT = 0, 1
+
+_STATUS_EXC = {1: ValueError, 2: IndexError, 3: RuntimeError}
+
+
+class AleatorError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+_D = ctypes.POINTER(ctypes.c_double)
+_U32 = ctypes.POINTER(ctypes.c_uint32)
+_U64 = ctypes.POINTER(ctypes.c_uint64)
+_I32 = ctypes.POINTER(ctypes.c_int32)
+_VP = ctypes.c_void_p
+
+
+class _Lattice(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_double * 9)]
+
+
+class _LJ(ctypes.Structure):
+    _fields_ = [("n_species", ctypes.c_uint32), ("epsilon", _D), ("sigma", _D),
+                ("cutoff", ctypes.c_double), ("truncation", ctypes.c_int32),
+                ("mixing", ctypes.c_int32)]
+
+
+class _Ewald(ctypes.Structure):
+    _fields_ = [("alpha", ctypes.c_double), ("real_space_cutoff", ctypes.c_double),
+                ("kmax", ctypes.c_int32)]
+
+
+class _Particles(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint64), ("x", _D), ("y", _D), ("z", _D), ("charge", _D),
+                ("species", _U32)]
+
+
+class _Species(ctypes.Structure):
+    _fields_ = [("n_sites", ctypes.c_uint32), ("x", _D), ("y", _D), ("z", _D),
+                ("lj_species", _U32), ("charge", _D)]
+
+
+class _GridStats(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_uint64), ("algorithmic_pairs", ctypes.c_uint64),
+                ("executed_pairs", ctypes.c_uint64), ("images", ctypes.c_uint64),
+                ("bricks", ctypes.c_uint64), ("last_kernel_ms", ctypes.c_float)]
+
+
+class _WidomResult(ctypes.Structure):
+    _fields_ = [("henry", ctypes.c_double), ("log_mean_weight", ctypes.c_double),
+                ("rel_std_error", ctypes.c_double), ("n_trials", ctypes.c_uint64),
+                ("kernel_ms", ctypes.c_float)]
+
+
+_SIGNATURES = {
+    "alea_last_error": (ctypes.c_size_t, [ctypes.c_char_p, ctypes.c_size_t]),
+    "alea_status_string": (ctypes.c_char_p, [ctypes.c_int32]),
+    "alea_version": (ctypes.c_int32, [_I32, _I32, _I32]),
+    "alea_device_info": (ctypes.c_int32, [ctypes.c_char_p, ctypes.c_size_t, _I32, _I32, _I32]),
+    "alea_probe_fp32_fma_tflops": (ctypes.c_int32, [_D]),
+    "alea_philox4x32_10": (ctypes.c_int32, [_U32, _U32, _U32, ctypes.c_uint64]),
+    "alea_philox_fill_u64": (ctypes.c_int32, [ctypes.c_uint64] * 4 + [_U64]),
+    "alea_philox_fill_uniform": (ctypes.c_int32, [ctypes.c_uint64] * 4 + [_D]),
+    "alea_philox_fill_u64_device": (ctypes.c_int32, [ctypes.c_uint64] * 4 + [_VP, _VP]),
+    "alea_philox_fill_uniform_device": (ctypes.c_int32, [ctypes.c_uint64] * 4 + [_VP, _VP]),
+    "alea_grid_build": (ctypes.c_int32, [ctypes.POINTER(_LJ), ctypes.POINTER(_Particles),
+                                         ctypes.POINTER(_Lattice), _U32, ctypes.c_uint32,
+                                         ctypes.c_double, ctypes.c_int32, ctypes.POINTER(_VP)]),
+    "alea_grid_point_counts": (ctypes.c_int32, [_VP, _I32]),
+    "alea_grid_spacing": (ctypes.c_int32, [_VP, _D]),
+    "alea_grid_species": (ctypes.c_int32, [_VP, _U32, ctypes.c_uint32, _U32]),
+    "alea_grid_interpolate": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D, ctypes.c_uint64, _D]),
+    "alea_grid_interpolate_device": (ctypes.c_int32, [_VP, ctypes.c_uint32, _VP, ctypes.c_uint64,
+                                                      _VP, _VP]),
+    "alea_grid_download": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D, ctypes.c_uint64]),
+    "alea_grid_table_device": (ctypes.c_int32, [_VP, ctypes.c_uint32, ctypes.POINTER(_VP)]),
+    "alea_grid_rebuild": (ctypes.c_int32, [_VP, _VP]),
+    "alea_grid_stats_get": (ctypes.c_int32, [_VP, ctypes.POINTER(_GridStats)]),
+    "alea_grid_serialize": (ctypes.c_int32, [_VP, ctypes.c_char_p, ctypes.POINTER(_LJ),
+                                             ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
+                                             _U32, ctypes.c_uint32]),
+    "alea_grid_cache_file_name": (ctypes.c_int32, [ctypes.POINTER(_LJ), ctypes.POINTER(_Particles),
+                                                   ctypes.POINTER(_Lattice), _U32, ctypes.c_uint32,
+                                                   ctypes.c_double, ctypes.c_char_p,
+                                                   ctypes.c_size_t]),
+    "alea_grid_load_cache": (ctypes.c_int32, [ctypes.c_char_p, ctypes.POINTER(_LJ),
+                                              ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
+                                              _U32, ctypes.c_uint32, ctypes.c_double,
+                                              ctypes.POINTER(_VP)]),
+    "alea_grid_destroy": (ctypes.c_int32, [_VP]),
+    "alea_lj_particle_energy": (ctypes.c_int32, [ctypes.POINTER(_LJ), ctypes.POINTER(_Particles),
+                                                 ctypes.POINTER(_Lattice), _U64, ctypes.c_uint64,
+                                                 _U64, ctypes.c_uint64, _D]),
+    "alea_lj_tail_correction": (ctypes.c_int32, [ctypes.POINTER(_LJ), ctypes.POINTER(_Particles),
+                                                 ctypes.POINTER(_Lattice), _D]),
+    "alea_ewald_reciprocal_terms": (ctypes.c_int32, [ctypes.POINTER(_Lattice), ctypes.c_double,
+                                                     ctypes.c_int32, _D, _D, ctypes.c_uint64,
+                                                     _U64]),
+    "alea_ewald_real_space_particle_energy": (ctypes.c_int32, [
+        ctypes.POINTER(_Ewald), ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice), _U64,
+        ctypes.c_uint64, _U64, ctypes.c_uint64, _D]),
+    "alea_ewald_energy_breakdown": (ctypes.c_int32, [ctypes.POINTER(_Ewald),
+                                                     ctypes.POINTER(_Particles),
+                                                     ctypes.POINTER(_Lattice), _U64,
+                                                     ctypes.c_uint64, _D]),
+    "alea_ewald_state_create": (ctypes.c_int32, [ctypes.POINTER(_Ewald), ctypes.POINTER(_Particles),
+                                                 ctypes.POINTER(_Lattice), ctypes.POINTER(_VP)]),
+    "alea_ewald_state_committed_energy": (ctypes.c_int32, [_VP, _D]),
+    "alea_ewald_state_propose": (ctypes.c_int32, [_VP, _D, ctypes.c_uint64, _D, ctypes.c_uint64,
+                                                  _D]),
+    "alea_ewald_state_commit": (ctypes.c_int32, [_VP, _D, ctypes.c_uint64, _D, ctypes.c_uint64]),
+    "alea_ewald_state_recompute": (ctypes.c_int32, [_VP, ctypes.POINTER(_Particles),
+                                                    ctypes.c_uint64, _U64, _U64, _D]),
+    "alea_ewald_state_resync": (ctypes.c_int32, [_VP, ctypes.POINTER(_Particles), ctypes.c_uint64,
+                                                 _U64, _U64]),
+    "alea_ewald_state_raw": (ctypes.c_int32, [_VP, _D, ctypes.c_uint64, _U64]),
+    "alea_ewald_state_term_count": (ctypes.c_int32, [_VP, _U64]),
+    "alea_ewald_state_destroy": (ctypes.c_int32, [_VP]),
+    "alea_widom_create": (ctypes.c_int32, [ctypes.POINTER(_LJ), ctypes.POINTER(_Ewald),
+                                           ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
+                                           ctypes.POINTER(_Species), ctypes.c_double,
+                                           ctypes.c_int32, ctypes.POINTER(_VP)]),
+    "alea_widom_run": (ctypes.c_int32, [_VP, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                        ctypes.c_uint64, ctypes.c_int32,
+                                        ctypes.POINTER(_WidomResult), _D]),
+    "alea_widom_destroy": (ctypes.c_int32, [_VP]),
+    "alea_insertion_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                               ctypes.c_double, ctypes.c_double]),
+    "alea_deletion_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                              ctypes.c_double, ctypes.c_double]),
+    "alea_metropolis_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
+    "alea_swap_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                          ctypes.c_uint64, ctypes.c_double, ctypes.c_double]),
+    "alea_peng_robinson_fugacity": (ctypes.c_int32, [ctypes.c_double] * 5 + [_D]),
+}
+
+_LIB = None
+
+
+def load_library(path: str | os.PathLike | None = None, build_if_missing: bool = False):
+    """Loads libaleator_gb300.so (raising if absent) and declares every signature."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else LIB_PATH
+    if not p.exists() and build_if_missing:
+        from .build import build
+        build()
+    if not p.exists():
+        raise FileNotFoundError(
+            f"{p} is not built; run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(str(p))
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def library():
+    return load_library()
+
+
+def _check(status: int):
+    if status == 0:
+        return
+    lib = library()
+    buf = ctypes.create_string_buffer(4096)
+    lib.alea_last_error(buf, 4096)
+    msg = buf.value.decode(errors="replace")
+    exc = _STATUS_EXC.get(status)
+    if exc is not None:
+        raise exc(msg)
+    raise AleatorError(status, msg)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def _u32p(a):
+    return None if a is None else a.ctypes.data_as(_U32)
+
+
+def _u64p(a):
+    return None if a is None else a.ctypes.data_as(_U64)
+
+
+def _lattice(m) -> _Lattice:
+    arr = _f64(np.asarray(m, dtype=np.float64).reshape(9))
+    out = _Lattice()
+    for i in range(9):
+        out.m[i] = arr[i]
+    return out
+
+
+class ParticleData:
+    """core::ParticleData SoA (core/math/particle_data.hpp:20-25)."""
+
+    def __init__(self, x, y, z, charge=None, species=None):
+        self.x, self.y, self.z = _f64(x), _f64(y), _f64(z)
+        n = self.x.shape[0]
+        self.charge = _f64(charge) if charge is not None else np.zeros(n)
+        self.species = (np.ascontiguousarray(species, dtype=np.uint32) if species is not None
+                        else np.zeros(n, np.uint32))
+
+    @classmethod
+    def from_framework(cls, fw):
+        return cls(fw.x, fw.y, fw.z, fw.charge, fw.species)
+
+    def __len__(self):
+        return int(self.x.shape[0])
+
+    def c(self) -> _Particles:
+        return _Particles(len(self), _dp(self.x), _dp(self.y), _dp(self.z), _dp(self.charge),
+                          _u32p(self.species))
+
+
+class LennardJones:
+    """LennardJones(perSpecies, cutoff, truncation, mixing) (lennard_jones.hpp:64-66)."""
+
+    def __init__(self, epsilon, sigma, cutoff, truncation=TRUNCATED, mixing=LORENTZ_BERTHELOT):
+        self.epsilon = _f64(epsilon)
+        self.sigma = _f64(sigma)
+        self.cutoff = float(cutoff)
+        self.truncation = int(truncation)
+        self.mixing = int(mixing)
+
+    def c(self) -> _LJ:
+        return _LJ(len(self.epsilon), _dp(self.epsilon), _dp(self.sigma), self.cutoff,
+                   self.truncation, self.mixing)
+
+
+class Ewald:
+    """Ewald(alpha, realSpaceCutoff, kMax) (ewald.hpp:76-77)."""
+
+    def __init__(self, alpha, real_space_cutoff, kmax):
+        self.alpha = float(alpha)
+        self.real_space_cutoff = float(real_space_cutoff)
+        self.kmax = int(kmax)
+
+    def c(self) -> _Ewald:
+        return _Ewald(self.alpha, self.real_space_cutoff, self.kmax)
+
+
+# ---------------------------------------------------------------- Philox
+def philox4x32_10(ctr, key):
+    ctr = np.ascontiguousarray(np.asarray(ctr, dtype=np.uint32).reshape(-1, 4))
+    key = np.ascontiguousarray(np.asarray(key, dtype=np.uint32).reshape(-1, 2))
+    out = np.zeros_like(ctr)
+    _check(library().alea_philox4x32_10(_u32p(ctr), _u32p(key), _u32p(out), ctr.shape[0]))
+    return out
+
+
+def philox_u64(seed, stream, first, n):
+    out = np.zeros(n, np.uint64)
+    _check(library().alea_philox_fill_u64(seed, stream, first, n, _u64p(out)))
+    return out
+
+
+def philox_uniform(seed, stream, first, n):
+    out = np.zeros(n, np.float64)
+    _check(library().alea_philox_fill_uniform(seed, stream, first, n, _dp(out)))
+    return out
+
+
+def device_info():
+    name = ctypes.create_string_buffer(256)
+    sms, ma, mi = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    _check(library().alea_device_info(name, 256, ctypes.byref(sms), ctypes.byref(ma),
+                                      ctypes.byref(mi)))
+    return {"name": name.value.decode(), "sm_count": sms.value, "cc": (ma.value, mi.value)}
+
+
+def fp32_fma_tflops():
+    """Sustained FP32 FFMA throughput measured on the current device."""
+    v = ctypes.c_double()
+    _check(library().alea_probe_fp32_fma_tflops(ctypes.byref(v)))
+    return v.value
+
+
+# ---------------------------------------------------------------- grid
+class FrameworkEnergyGrid:
+    """FrameworkEnergyGrid (engines/monte_carlo/framework_energy_grid.hpp:94-200) on the GPU."""
+
+    def __init__(self, force_field: LennardJones, framework: ParticleData, lattice,
+                 guest_species_ids, spacing_angstrom: float, precision: int = FP64, *,
+                 _handle=None):
+        self._lib = library()
+        self._keep = (force_field, framework)
+        self.lattice = np.asarray(lattice, dtype=np.float64).reshape(3, 3).copy()
+        self._ff = force_field
+        self._fw = framework
+        self._guests = np.ascontiguousarray(guest_species_ids, dtype=np.uint32)
+        self._h = _VP()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            lj = force_field.c()
+            p = framework.c()
+            lat = _lattice(lattice)
+            _check(self._lib.alea_grid_build(ctypes.byref(lj), ctypes.byref(p), ctypes.byref(lat),
+                                             _u32p(self._guests), len(self._guests),
+                                             float(spacing_angstrom), int(precision),
+                                             ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                self._lib.alea_grid_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def point_counts(self):
+        out = np.zeros(3, np.int32)
+        _check(self._lib.alea_grid_point_counts(self._h, out.ctypes.data_as(_I32)))
+        return tuple(int(v) for v in out)
+
+    def spacing_angstrom(self):
+        v = ctypes.c_double()
+        _check(self._lib.alea_grid_spacing(self._h, ctypes.byref(v)))
+        return v.value
+
+    def species(self):
+        n = ctypes.c_uint32()
+        _check(self._lib.alea_grid_species(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, np.uint32)
+        _check(self._lib.alea_grid_species(self._h, _u32p(out), n.value, ctypes.byref(n)))
+        return [int(v) for v in out]
+
+    def interpolate(self, species: int, positions):
+        xyz = _f64(np.asarray(positions, dtype=np.float64).reshape(-1, 3))
+        out = np.zeros(xyz.shape[0])
+        _check(self._lib.alea_grid_interpolate(self._h, int(species), _dp(xyz), xyz.shape[0],
+                                               _dp(out)))
+        return out
+
+    def interpolate_device(self, species: int, xyz_ptr: int, n: int, out_ptr: int, stream=0):
+        _check(self._lib.alea_grid_interpolate_device(self._h, int(species), xyz_ptr, n, out_ptr,
+                                                      stream))
+
+    def table(self, species: int):
+        nx, ny, nz = self.point_counts()
+        out = np.zeros(nx * ny * nz)
+        _check(self._lib.alea_grid_download(self._h, int(species), _dp(out), out.size))
+        return out
+
+    def download_into(self, species: int, out: np.ndarray):
+        _check(self._lib.alea_grid_download(self._h, int(species), _dp(out), out.size))
+
+    def rebuild(self, stream=0):
+        _check(self._lib.alea_grid_rebuild(self._h, stream))
+
+    def stats(self):
+        s = _GridStats()
+        _check(self._lib.alea_grid_stats_get(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def serialize(self, path):
+        lj = self._ff.c()
+        p = self._fw.c()
+        lat = _lattice(self.lattice)
+        _check(self._lib.alea_grid_serialize(self._h, str(path).encode(), ctypes.byref(lj),
+                                             ctypes.byref(p), ctypes.byref(lat),
+                                             _u32p(self._guests), len(self._guests)))
+
+    @staticmethod
+    def cache_file_name(force_field, framework, lattice, guest_species_ids, spacing):
+        g = np.ascontiguousarray(guest_species_ids, dtype=np.uint32)
+        lj = force_field.c()
+        p = framework.c()
+        lat = _lattice(lattice)
+        buf = ctypes.create_string_buffer(512)
+        _check(library().alea_grid_cache_file_name(ctypes.byref(lj), ctypes.byref(p),
+                                                   ctypes.byref(lat), _u32p(g), len(g),
+                                                   float(spacing), buf, 512))
+        return buf.value.decode()
+
+    @classmethod
+    def load_from_cache(cls, cache_dir, force_field, framework, lattice, guest_species_ids,
+                        spacing):
+        g = np.ascontiguousarray(guest_species_ids, dtype=np.uint32)
+        lj = force_field.c()
+        p = framework.c()
+        lat = _lattice(lattice)
+        h = _VP()
+        _check(library().alea_grid_load_cache(str(cache_dir).encode(), ctypes.byref(lj),
+                                              ctypes.byref(p), ctypes.byref(lat), _u32p(g), len(g),
+                                              float(spacing), ctypes.byref(h)))
+        if not h:
+            return None
+        return cls(force_field, framework, lattice, g, spacing, _handle=h)
+
+
+# ---------------------------------------------------------------- LJ / Ewald free functions
+def lj_particle_energy(force_field: LennardJones, particles: ParticleData, lattice, queries,
+                       excluded=()):
+    q = np.ascontiguousarray(queries, dtype=np.uint64)
+    ex = np.ascontiguousarray(excluded, dtype=np.uint64)
+    out = np.zeros(len(q))
+    lj = force_field.c()
+    p = particles.c()
+    lat = _lattice(lattice)
+    _check(library().alea_lj_particle_energy(ctypes.byref(lj), ctypes.byref(p), ctypes.byref(lat),
+                                             _u64p(q), len(q), _u64p(ex), len(ex), _dp(out)))
+    return out
+
+
+def lj_tail_correction(force_field: LennardJones, particles: ParticleData, lattice):
+    v = ctypes.c_double()
+    lj = force_field.c()
+    p = particles.c()
+    lat = _lattice(lattice)
+    _check(library().alea_lj_tail_correction(ctypes.byref(lj), ctypes.byref(p), ctypes.byref(lat),
+                                             ctypes.byref(v)))
+    return v.value
+
+
+def ewald_reciprocal_terms(lattice, alpha, kmax):
+    lat = _lattice(lattice)
+    n = ctypes.c_uint64()
+    _check(library().alea_ewald_reciprocal_terms(ctypes.byref(lat), alpha, kmax, None, None, 0,
+                                                 ctypes.byref(n)))
+    k = np.zeros(3 * n.value)
+    w = np.zeros(n.value)
+    _check(library().alea_ewald_reciprocal_terms(ctypes.byref(lat), alpha, kmax, _dp(k), _dp(w),
+                                                 n.value, ctypes.byref(n)))
+    return k.reshape(-1, 3), w
+
+
+def ewald_real_space_particle_energy(ewald: Ewald, particles: ParticleData, lattice, queries,
+                                     excluded=()):
+    q = np.ascontiguousarray(queries, dtype=np.uint64)
+    ex = np.ascontiguousarray(excluded, dtype=np.uint64)
+    out = np.zeros(len(q))
+    e = ewald.c()
+    p = particles.c()
+    lat = _lattice(lattice)
+    _check(library().alea_ewald_real_space_particle_energy(ctypes.byref(e), ctypes.byref(p),
+                                                           ctypes.byref(lat), _u64p(q), len(q),
+                                                           _u64p(ex), len(ex), _dp(out)))
+    return out
+
+
+def ewald_energy_breakdown(ewald: Ewald, particles: ParticleData, lattice, exclusions=()):
+    ex = np.ascontiguousarray(np.asarray(exclusions, dtype=np.uint64).reshape(-1))
+    out = np.zeros(5)
+    e = ewald.c()
+    p = particles.c()
+    lat = _lattice(lattice)
+    _check(library().alea_ewald_energy_breakdown(ctypes.byref(e), ctypes.byref(p),
+                                                 ctypes.byref(lat), _u64p(ex), len(ex) // 2,
+                                                 _dp(out)))
+    return out
+
+
+def _sites(s):
+    s = _f64(np.asarray(s, dtype=np.float64).reshape(-1))
+    if s.size % 4:
+        raise ValueError("sites must be packed {x, y, z, q}")
+    return s, s.size // 4
+
+
+class EwaldIncrementalState:
+    """EwaldIncrementalState (ewald_incremental_state.hpp:70-171) with S(k) in HBM."""
+
+    def __init__(self, ewald: Ewald, particles: ParticleData, lattice):
+        self._lib = library()
+        self._h = _VP()
+        e = ewald.c()
+        p = particles.c()
+        lat = _lattice(lattice)
+        _check(self._lib.alea_ewald_state_create(ctypes.byref(e), ctypes.byref(p),
+                                                 ctypes.byref(lat), ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                self._lib.alea_ewald_state_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def committed_energy(self):
+        v = ctypes.c_double()
+        _check(self._lib.alea_ewald_state_committed_energy(self._h, ctypes.byref(v)))
+        return v.value
+
+    def propose(self, removed, added):
+        r, nr = _sites(removed)
+        a, na = _sites(added)
+        v = ctypes.c_double()
+        _check(self._lib.alea_ewald_state_propose(self._h, _dp(r), nr, _dp(a), na,
+                                                  ctypes.byref(v)))
+        return v.value
+
+    def commit(self, removed, added):
+        r, nr = _sites(removed)
+        a, na = _sites(added)
+        _check(self._lib.alea_ewald_state_commit(self._h, _dp(r), nr, _dp(a), na))
+
+    def propose_move(self, old, new):
+        return self.propose(old, new)
+
+    def propose_insertion(self, new):
+        return self.propose(np.zeros((0, 4)), new)
+
+    def propose_deletion(self, existing):
+        return self.propose(existing, np.zeros((0, 4)))
+
+    def commit_move(self, old, new):
+        self.commit(old, new)
+
+    def commit_insertion(self, new):
+        self.commit(np.zeros((0, 4)), new)
+
+    def commit_deletion(self, existing):
+        self.commit(existing, np.zeros((0, 4)))
+
+    @staticmethod
+    def _csr(molecules):
+        offs = np.zeros(len(molecules) + 1, np.uint64)
+        for i, m in enumerate(molecules):
+            offs[i + 1] = offs[i] + len(m)
+        idx = np.array([j for m in molecules for j in m], dtype=np.uint64)
+        return offs, (idx if idx.size else np.zeros(1, np.uint64))
+
+    def recompute_from_scratch(self, particles: ParticleData, molecules):
+        offs, idx = self._csr(molecules)
+        p = particles.c()
+        v = ctypes.c_double()
+        _check(self._lib.alea_ewald_state_recompute(self._h, ctypes.byref(p), len(molecules),
+                                                    _u64p(offs), _u64p(idx), ctypes.byref(v)))
+        return v.value
+
+    def resync(self, particles: ParticleData, molecules):
+        offs, idx = self._csr(molecules)
+        p = particles.c()
+        _check(self._lib.alea_ewald_state_resync(self._h, ctypes.byref(p), len(molecules),
+                                                 _u64p(offs), _u64p(idx)))
+
+    def raw_state_for_testing(self):
+        n = ctypes.c_uint64()
+        _check(self._lib.alea_ewald_state_raw(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        _check(self._lib.alea_ewald_state_raw(self._h, _dp(out), n.value, ctypes.byref(n)))
+        return out
+
+    def term_count(self):
+        n = ctypes.c_uint64()
+        _check(self._lib.alea_ewald_state_term_count(self._h, ctypes.byref(n)))
+        return n.value
+
+
+# ---------------------------------------------------------------- Widom
+class Widom:
+    """Device context for MonteCarloEngine::widomInsertionHenryCoefficient
+    (monte_carlo_engine.cc:850-917)."""
+
+    def __init__(self, force_field: LennardJones, framework: ParticleData, lattice, guest: dict,
+                 temperature: float, ewald: Ewald | None = None, precision: int = FP64):
+        self._lib = library()
+        self._h = _VP()
+        self._g = {k: (_f64(guest[k]) if k != "lj_species" else
+                       np.ascontiguousarray(guest[k], dtype=np.uint32))
+                   for k in ("x", "y", "z", "lj_species", "charge")}
+        sp = _Species(len(self._g["x"]), _dp(self._g["x"]), _dp(self._g["y"]), _dp(self._g["z"]),
+                      _u32p(self._g["lj_species"]), _dp(self._g["charge"]))
+        lj = force_field.c()
+        p = framework.c()
+        lat = _lattice(lattice)
+        e = ewald.c() if ewald is not None else None
+        _check(self._lib.alea_widom_create(ctypes.byref(lj), ctypes.byref(e) if e else None,
+                                           ctypes.byref(p), ctypes.byref(lat), ctypes.byref(sp),
+                                           float(temperature), int(precision),
+                                           ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                self._lib.alea_widom_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def run(self, seed, stream, n_trials, first_trial=0, draw_order=ALEA_DRAWS_RIGHT_TO_LEFT,
+            per_trial=False):
+        res = _WidomResult()
+        out = np.zeros(n_trials) if per_trial else None
+        _check(self._lib.alea_widom_run(self._h, seed, stream, first_trial, n_trials, draw_order,
+                                        ctypes.byref(res), _dp(out)))
+        r = {f: getattr(res, f) for f, _ in res._fields_}
+        return (r, out) if per_trial else r
+
+    def henry_coefficient(self, seed, stream, n_trials, draw_order=ALEA_DRAWS_RIGHT_TO_LEFT):
+        return self.run(seed, stream, n_trials, draw_order=draw_order)["henry"]
+
+
+def peng_robinson_fugacity(tc, pc, omega, t, p):
+    v = ctypes.c_double()
+    _check(library().alea_peng_robinson_fugacity(tc, pc, omega, t, p, ctypes.byref(v)))
+    return v.value

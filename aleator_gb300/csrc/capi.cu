@@ -1,0 +1,626 @@
+// extern "C" entry points of libaleator_gb300.so (declared in
+// include/aleator_gb300.h). Each call converts exceptions into an
+// alea_status and records the message for alea_last_error().
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "grid.cuh"
+
+struct alea_grid {
+    alea::GridImpl* impl;
+};
+struct alea_ewald_state {
+    alea::EwaldStateImpl* impl;
+};
+struct alea_widom {
+    alea::WidomImpl* impl;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F>
+alea_status guarded(F&& f) {
+    try {
+        f();
+        g_last_error.clear();
+        return ALEA_OK;
+    } catch (const alea::Error& e) {
+        g_last_error = e.what();
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return ALEA_ERR_RUNTIME;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return ALEA_ERR_RUNTIME;
+    } catch (...) {
+        g_last_error = "unknown error";
+        return ALEA_ERR_RUNTIME;
+    }
+}
+
+void need(const void* p, const char* what) {
+    if (!p) throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, std::string(what) + " is NULL");
+}
+
+alea_particles particles_or_empty(const alea_particles* p) {
+    need(p, "particles");
+    return *p;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* alea_status_string(alea_status s) {
+    switch (s) {
+        case ALEA_OK: return "ok";
+        case ALEA_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case ALEA_ERR_OUT_OF_RANGE: return "out of range";
+        case ALEA_ERR_RUNTIME: return "runtime error";
+        case ALEA_ERR_CUDA: return "CUDA error";
+        case ALEA_ERR_NO_DEVICE: return "no CUDA device";
+        case ALEA_ERR_DEVICE_CHECK: return "device-side check failed";
+        default: return "unknown status";
+    }
+}
+
+size_t alea_last_error(char* buf, size_t cap) {
+    if (buf && cap) {
+        const size_t n = std::min(cap - 1, g_last_error.size());
+        std::memcpy(buf, g_last_error.data(), n);
+        buf[n] = '\0';
+    }
+    return g_last_error.size();
+}
+
+alea_status alea_version(int32_t* major, int32_t* minor, int32_t* arch) {
+    return guarded([&] {
+        if (major) *major = 0;
+        if (minor) *minor = 1;
+        if (arch) *arch = 103;
+    });
+}
+
+alea_status alea_device_info(char* name, size_t cap, int32_t* sm_count, int32_t* cc_major,
+                             int32_t* cc_minor) {
+    return guarded([&] {
+        alea::require_device();
+        int dev = 0;
+        ALEA_CUDA(cudaGetDevice(&dev));
+        cudaDeviceProp prop{};
+        ALEA_CUDA(cudaGetDeviceProperties(&prop, dev));
+        if (name && cap) {
+            std::strncpy(name, prop.name, cap - 1);
+            name[cap - 1] = '\0';
+        }
+        if (sm_count) *sm_count = prop.multiProcessorCount;
+        if (cc_major) *cc_major = prop.major;
+        if (cc_minor) *cc_minor = prop.minor;
+    });
+}
+
+// ---------------------------------------------------------------- Philox
+alea_status alea_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out, uint64_t n) {
+    return guarded([&] {
+        if (n == 0) return;
+        need(ctr, "ctr");
+        need(key, "key");
+        need(out, "out");
+        alea::philox_raw(ctr, key, out, n);
+    });
+}
+
+alea_status alea_philox_fill_u64(uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+                                 uint64_t* out) {
+    return guarded([&] {
+        if (n == 0) return;
+        need(out, "out");
+        alea::require_device();
+        alea::DevBuf<uint64_t> d(n);
+        alea::philox_fill_u64_device(seed, stream, first, n, d.p, 0);
+        d.download(out, n);
+        ALEA_CUDA(cudaDeviceSynchronize());
+    });
+}
+
+alea_status alea_philox_fill_uniform(uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+                                     double* out) {
+    return guarded([&] {
+        if (n == 0) return;
+        need(out, "out");
+        alea::require_device();
+        alea::DevBuf<double> d(n);
+        alea::philox_fill_uniform_device(seed, stream, first, n, d.p, 0);
+        d.download(out, n);
+        ALEA_CUDA(cudaDeviceSynchronize());
+    });
+}
+
+alea_status alea_philox_fill_u64_device(uint64_t seed, uint64_t stream_index, uint64_t first,
+                                        uint64_t n, uint64_t* out, void* cuda_stream) {
+    return guarded([&] {
+        if (n) need(out, "out");
+        alea::philox_fill_u64_device(seed, stream_index, first, n, out, (cudaStream_t)cuda_stream);
+    });
+}
+
+alea_status alea_philox_fill_uniform_device(uint64_t seed, uint64_t stream_index, uint64_t first,
+                                            uint64_t n, double* out, void* cuda_stream) {
+    return guarded([&] {
+        if (n) need(out, "out");
+        alea::philox_fill_uniform_device(seed, stream_index, first, n, out, (cudaStream_t)cuda_stream);
+    });
+}
+
+// ---------------------------------------------------------------- grid
+alea_status alea_grid_build(const alea_lennard_jones* lj, const alea_particles* framework,
+                            const alea_lattice* lattice, const uint32_t* guest_species,
+                            uint32_t n_guest, double spacing, int32_t precision, alea_grid** out) {
+    return guarded([&] {
+        need(lj, "lj");
+        need(lattice, "lattice");
+        need(out, "out");
+        if (n_guest) need(guest_species, "guest_species");
+        *out = nullptr;
+        auto* g = new alea_grid{nullptr};
+        try {
+            g->impl = alea::grid_build(*lj, particles_or_empty(framework), *lattice,
+                                       guest_species, n_guest, spacing, precision);
+        } catch (...) {
+            delete g;
+            throw;
+        }
+        *out = g;
+    });
+}
+
+alea_status alea_grid_point_counts(const alea_grid* g, int32_t out[3]) {
+    return guarded([&] {
+        need(g, "grid");
+        need(out, "out");
+        alea::grid_counts(g->impl, out);
+    });
+}
+
+alea_status alea_grid_spacing(const alea_grid* g, double* out) {
+    return guarded([&] {
+        need(g, "grid");
+        need(out, "out");
+        *out = alea::grid_spacing(g->impl);
+    });
+}
+
+alea_status alea_grid_species(const alea_grid* g, uint32_t* out, uint32_t cap, uint32_t* n_out) {
+    return guarded([&] {
+        need(g, "grid");
+        const auto& sp = alea::grid_species(g->impl);
+        if (n_out) *n_out = (uint32_t)sp.size();
+        for (uint32_t i = 0; out && i < cap && i < sp.size(); ++i) out[i] = sp[i];
+    });
+}
+
+alea_status alea_grid_interpolate(const alea_grid* g, uint32_t species, const double* xyz,
+                                  uint64_t n, double* out) {
+    return guarded([&] {
+        need(g, "grid");
+        if (n) {
+            need(xyz, "xyz");
+            need(out, "out");
+        }
+        alea::grid_interpolate_host(g->impl, species, xyz, n, out);
+    });
+}
+
+alea_status alea_grid_interpolate_device(const alea_grid* g, uint32_t species, const double* xyz,
+                                         uint64_t n, double* out, void* cuda_stream) {
+    return guarded([&] {
+        need(g, "grid");
+        alea::grid_interpolate_device(g->impl, species, xyz, n, out, (cudaStream_t)cuda_stream);
+    });
+}
+
+alea_status alea_grid_download(const alea_grid* g, uint32_t species, double* out, uint64_t n) {
+    return guarded([&] {
+        need(g, "grid");
+        need(out, "out");
+        alea::grid_download(g->impl, species, out, n);
+    });
+}
+
+alea_status alea_grid_table_device(const alea_grid* g, uint32_t species, const double** out) {
+    return guarded([&] {
+        need(g, "grid");
+        need(out, "out");
+        *out = alea::grid_table(g->impl, species);
+    });
+}
+
+alea_status alea_grid_rebuild(alea_grid* g, void* cuda_stream) {
+    return guarded([&] {
+        need(g, "grid");
+        alea::grid_rebuild(g->impl, (cudaStream_t)cuda_stream);
+    });
+}
+
+alea_status alea_grid_stats_get(const alea_grid* g, alea_grid_stats* out) {
+    return guarded([&] {
+        need(g, "grid");
+        need(out, "out");
+        alea::grid_stats(g->impl, out);
+    });
+}
+
+alea_status alea_grid_serialize(const alea_grid* g, const char* path, const alea_lennard_jones* lj,
+                                const alea_particles* framework, const alea_lattice* lattice,
+                                const uint32_t* guest_species, uint32_t n_guest) {
+    return guarded([&] {
+        need(g, "grid");
+        need(path, "path");
+        need(lj, "lj");
+        need(lattice, "lattice");
+        const auto& sp = alea::grid_species(g->impl);
+        int32_t counts[3];
+        alea::grid_counts(g->impl, counts);
+        const uint64_t nodes = (uint64_t)counts[0] * counts[1] * counts[2];
+        std::vector<std::vector<double>> tables(sp.size(), std::vector<double>(nodes));
+        for (size_t i = 0; i < sp.size(); ++i) alea::grid_download(g->impl, sp[i], tables[i].data(), nodes);
+        alea::grid_cache_write(path, *lj, particles_or_empty(framework), *lattice, guest_species,
+                               n_guest, alea::grid_spacing(g->impl), counts, sp, tables);
+    });
+}
+
+alea_status alea_grid_cache_file_name(const alea_lennard_jones* lj, const alea_particles* framework,
+                                      const alea_lattice* lattice, const uint32_t* guest_species,
+                                      uint32_t n_guest, double spacing, char* out, size_t cap) {
+    return guarded([&] {
+        need(lj, "lj");
+        need(lattice, "lattice");
+        need(out, "out");
+        const std::string s = alea::grid_cache_file_name(*lj, particles_or_empty(framework),
+                                                         *lattice, guest_species, n_guest, spacing);
+        if (s.size() + 1 > cap)
+            throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, "alea_grid_cache_file_name: buffer too small");
+        std::memcpy(out, s.c_str(), s.size() + 1);
+    });
+}
+
+alea_status alea_grid_load_cache(const char* cache_dir, const alea_lennard_jones* lj,
+                                 const alea_particles* framework, const alea_lattice* lattice,
+                                 const uint32_t* guest_species, uint32_t n_guest, double spacing,
+                                 alea_grid** out) {
+    return guarded([&] {
+        need(cache_dir, "cache_dir");
+        need(lj, "lj");
+        need(lattice, "lattice");
+        need(out, "out");
+        *out = nullptr;
+        int32_t counts[3];
+        std::vector<uint32_t> sp;
+        std::vector<std::vector<double>> tables;
+        if (!alea::grid_cache_read(cache_dir, *lj, particles_or_empty(framework), *lattice,
+                                   guest_species, n_guest, spacing, counts, sp, tables))
+            return;
+        auto* g = new alea_grid{nullptr};
+        try {
+            g->impl = alea::grid_from_tables(*lattice, spacing, counts, sp, tables);
+        } catch (...) {
+            delete g;
+            throw;
+        }
+        *out = g;
+    });
+}
+
+alea_status alea_grid_destroy(alea_grid* g) {
+    return guarded([&] {
+        if (!g) return;
+        alea::grid_destroy(g->impl);
+        delete g;
+    });
+}
+
+// ---------------------------------------------------------------- Lennard-Jones
+alea_status alea_lj_particle_energy(const alea_lennard_jones* lj, const alea_particles* particles,
+                                    const alea_lattice* lattice, const uint64_t* query,
+                                    uint64_t n_query, const uint64_t* excluded, uint64_t n_excluded,
+                                    double* out) {
+    return guarded([&] {
+        need(lj, "lj");
+        need(lattice, "lattice");
+        if (n_query) {
+            need(query, "query");
+            need(out, "out");
+        }
+        if (n_excluded) need(excluded, "excluded");
+        alea::lj_particle_energy(*lj, particles_or_empty(particles), *lattice, query, n_query,
+                                 excluded, n_excluded, out);
+    });
+}
+
+// LennardJones::tailEnergyCorrection (lennard_jones.cc:217-257): an
+// O(species^2) host formula over the species counts.
+alea_status alea_lj_tail_correction(const alea_lennard_jones* lj, const alea_particles* particles,
+                                    const alea_lattice* lattice, double* out) {
+    return guarded([&] {
+        need(lj, "lj");
+        need(lattice, "lattice");
+        need(out, "out");
+        const alea_particles p = particles_or_empty(particles);
+        const alea::Lattice L = alea::make_lattice(lattice->m);
+        const double volume = std::fabs(L.volume);
+        const double rc = lj->cutoff;
+        std::vector<uint64_t> counts(lj->n_species, 0);
+        for (uint64_t i = 0; i < p.n; ++i) {
+            const uint32_t s = p.species ? p.species[i] : 0u;
+            if (s >= lj->n_species)
+                throw alea::Error(ALEA_ERR_OUT_OF_RANGE, "tailEnergyCorrection: species out of range");
+            counts[s] += 1;
+        }
+        std::vector<alea::PairParams> table((size_t)lj->n_species * lj->n_species);
+        alea::mixed_table(*lj, table.data());
+        double total = 0.0;
+        for (uint32_t a = 0; a < lj->n_species; ++a) {
+            if (!counts[a]) continue;
+            for (uint32_t b = 0; b < lj->n_species; ++b) {
+                if (!counts[b]) continue;
+                const alea::PairParams& pp = table[(size_t)a * lj->n_species + b];
+                const double sr3 = pp.sigma * pp.sigma * pp.sigma;
+                const double sr9 = sr3 * sr3 * sr3 / (rc * rc * rc * rc * rc * rc * rc * rc * rc);
+                const double sr3rc3 = sr3 / (rc * rc * rc);
+                total += (double)counts[a] * (double)counts[b] *
+                         (pp.eps * sr3 * ((4.0 / 9.0) * sr9 - (4.0 / 3.0) * sr3rc3));
+            }
+        }
+        *out = (2.0 * alea::kPi / volume) * total;
+    });
+}
+
+// ---------------------------------------------------------------- Ewald
+alea_status alea_ewald_reciprocal_terms(const alea_lattice* lattice, double alpha, int32_t kmax,
+                                        double* k, double* weight, uint64_t cap, uint64_t* n_out) {
+    return guarded([&] {
+        need(lattice, "lattice");
+        if (!(alpha > 0.0)) throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, "Ewald: alpha must be positive");
+        if (kmax < 1) throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, "Ewald: kMax must be at least 1");
+        const alea::Lattice L = alea::make_lattice(lattice->m);
+        const uint64_t n = alea::ewald_terms_host(L, alpha, kmax, k, weight, nullptr, (k || weight) ? cap : 0);
+        if (n_out) *n_out = n;
+    });
+}
+
+alea_status alea_ewald_real_space_particle_energy(const alea_ewald* ewald,
+                                                  const alea_particles* particles,
+                                                  const alea_lattice* lattice,
+                                                  const uint64_t* query, uint64_t n_query,
+                                                  const uint64_t* excluded, uint64_t n_excluded,
+                                                  double* out) {
+    return guarded([&] {
+        need(ewald, "ewald");
+        need(lattice, "lattice");
+        if (n_query) {
+            need(query, "query");
+            need(out, "out");
+        }
+        if (n_excluded) need(excluded, "excluded");
+        alea::ewald_real_space_particle_energy(*ewald, particles_or_empty(particles), *lattice, query,
+                                               n_query, excluded, n_excluded, out);
+    });
+}
+
+alea_status alea_ewald_energy_breakdown(const alea_ewald* ewald, const alea_particles* particles,
+                                        const alea_lattice* lattice, const uint64_t* exclusions,
+                                        uint64_t n_exclusions, double out[5]) {
+    return guarded([&] {
+        need(ewald, "ewald");
+        need(lattice, "lattice");
+        need(out, "out");
+        if (n_exclusions) need(exclusions, "exclusions");
+        alea::ewald_breakdown(*ewald, particles_or_empty(particles), *lattice, exclusions,
+                              n_exclusions, out);
+    });
+}
+
+alea_status alea_ewald_state_create(const alea_ewald* ewald, const alea_particles* particles,
+                                    const alea_lattice* lattice, alea_ewald_state** out) {
+    return guarded([&] {
+        need(ewald, "ewald");
+        need(lattice, "lattice");
+        need(out, "out");
+        *out = nullptr;
+        auto* s = new alea_ewald_state{nullptr};
+        try {
+            s->impl = alea::ewald_state_create(*ewald, particles_or_empty(particles), *lattice);
+        } catch (...) {
+            delete s;
+            throw;
+        }
+        *out = s;
+    });
+}
+
+alea_status alea_ewald_state_committed_energy(const alea_ewald_state* s, double* out) {
+    return guarded([&] {
+        need(s, "state");
+        need(out, "out");
+        *out = alea::ewald_state_energy(s->impl);
+    });
+}
+
+alea_status alea_ewald_state_propose(const alea_ewald_state* s, const double* removed,
+                                     uint64_t n_removed, const double* added, uint64_t n_added,
+                                     double* delta) {
+    return guarded([&] {
+        need(s, "state");
+        need(delta, "delta");
+        if (n_removed) need(removed, "removed");
+        if (n_added) need(added, "added");
+        *delta = alea::ewald_state_propose(s->impl, removed, n_removed, added, n_added);
+    });
+}
+
+alea_status alea_ewald_state_commit(alea_ewald_state* s, const double* removed, uint64_t n_removed,
+                                    const double* added, uint64_t n_added) {
+    return guarded([&] {
+        need(s, "state");
+        if (n_removed) need(removed, "removed");
+        if (n_added) need(added, "added");
+        alea::ewald_state_commit(s->impl, removed, n_removed, added, n_added);
+    });
+}
+
+alea_status alea_ewald_state_recompute(const alea_ewald_state* s, const alea_particles* particles,
+                                       uint64_t n_molecules, const uint64_t* offsets,
+                                       const uint64_t* indices, double* out) {
+    return guarded([&] {
+        need(s, "state");
+        need(out, "out");
+        if (n_molecules) {
+            need(offsets, "offsets");
+            need(indices, "indices");
+        }
+        *out = alea::ewald_state_recompute(s->impl, particles_or_empty(particles), n_molecules,
+                                           offsets, indices);
+    });
+}
+
+alea_status alea_ewald_state_resync(alea_ewald_state* s, const alea_particles* particles,
+                                    uint64_t n_molecules, const uint64_t* offsets,
+                                    const uint64_t* indices) {
+    return guarded([&] {
+        need(s, "state");
+        if (n_molecules) {
+            need(offsets, "offsets");
+            need(indices, "indices");
+        }
+        alea::ewald_state_resync(s->impl, particles_or_empty(particles), n_molecules, offsets,
+                                 indices);
+    });
+}
+
+alea_status alea_ewald_state_raw(const alea_ewald_state* s, double* out, uint64_t cap,
+                                 uint64_t* n_out) {
+    return guarded([&] {
+        need(s, "state");
+        const auto raw = alea::ewald_state_raw(s->impl);
+        if (n_out) *n_out = raw.size();
+        for (uint64_t i = 0; out && i < cap && i < raw.size(); ++i) out[i] = raw[i];
+    });
+}
+
+alea_status alea_ewald_state_term_count(const alea_ewald_state* s, uint64_t* out) {
+    return guarded([&] {
+        need(s, "state");
+        need(out, "out");
+        *out = alea::ewald_state_nk(s->impl);
+    });
+}
+
+alea_status alea_ewald_state_destroy(alea_ewald_state* s) {
+    return guarded([&] {
+        if (!s) return;
+        alea::ewald_state_destroy(s->impl);
+        delete s;
+    });
+}
+
+// ---------------------------------------------------------------- Widom
+alea_status alea_widom_create(const alea_lennard_jones* lj, const alea_ewald* ewald,
+                              const alea_particles* framework, const alea_lattice* lattice,
+                              const alea_molecule_species* guest, double temperature,
+                              int32_t precision, alea_widom** out) {
+    return guarded([&] {
+        need(lj, "lj");
+        need(lattice, "lattice");
+        need(guest, "guest");
+        need(out, "out");
+        *out = nullptr;
+        auto* w = new alea_widom{nullptr};
+        try {
+            w->impl = alea::widom_create(*lj, ewald, particles_or_empty(framework), *lattice, *guest,
+                                         temperature, precision);
+        } catch (...) {
+            delete w;
+            throw;
+        }
+        *out = w;
+    });
+}
+
+alea_status alea_widom_run(alea_widom* w, uint64_t seed, uint64_t stream, uint64_t first_trial,
+                           uint64_t n_trials, int32_t draw_order, alea_widom_result* out,
+                           double* per_trial_du) {
+    return guarded([&] {
+        need(w, "widom");
+        need(out, "out");
+        alea::widom_run(w->impl, seed, stream, first_trial, n_trials, draw_order, out, per_trial_du);
+    });
+}
+
+alea_status alea_widom_destroy(alea_widom* w) {
+    return guarded([&] {
+        if (!w) return;
+        alea::widom_destroy(w->impl);
+        delete w;
+    });
+}
+
+// ---------------------------------------------------------------- acceptance / EOS
+double alea_insertion_ratio(double f, double v, uint64_t n_before, double t, double du) {
+    return (f * v / t) / (double)(n_before + 1) * std::exp(-du / t);
+}
+double alea_deletion_ratio(double f, double v, uint64_t n_before, double t, double du) {
+    return (double)n_before / (f * v / t) * std::exp(-du / t);
+}
+double alea_metropolis_ratio(double t, double du) { return std::exp(-du / t); }
+double alea_swap_ratio(double f_from, double f_to, uint64_t n_from, uint64_t n_to, double t,
+                       double du) {
+    return (f_to / f_from) * ((double)n_from / (double)(n_to + 1)) * std::exp(-du / t);
+}
+
+// PengRobinson (peng_robinson.cc:10-110): a scalar Newton solve, host side.
+alea_status alea_peng_robinson_fugacity(double tc, double pc, double omega, double t, double p,
+                                        double* out) {
+    return guarded([&] {
+        need(out, "out");
+        if (!(tc > 0.0)) throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, "PengRobinson: criticalTemperatureKelvin must be positive");
+        if (!(pc > 0.0)) throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, "PengRobinson: criticalPressurePascal must be positive");
+        if (!(t > 0.0)) throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, "PengRobinson: temperatureKelvin must be positive");
+        if (!(p > 0.0)) throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, "PengRobinson: pressurePascal must be positive");
+        const double R = 8.31446261815324;
+        const double a = 0.45724 * R * R * tc * tc / pc;
+        const double b = 0.07780 * R * tc / pc;
+        const double kappa = 0.37464 + 1.54226 * omega - 0.26992 * omega * omega;
+        const double term = 1.0 + kappa * (1.0 - std::sqrt(t / tc));
+        const double aa = a * (term * term);
+        const double A = aa * p / (R * R * t * t);
+        const double B = b * p / (R * t);
+        const double c2 = -(1.0 - B), c1 = A - 3.0 * B * B - 2.0 * B, c0 = -(A * B - B * B - B * B * B);
+        double z = 1.0;
+        bool converged = false;
+        for (int it = 0; it < 100; ++it) {
+            const double fz = z * z * z + c2 * z * z + c1 * z + c0;
+            if (std::fabs(fz) < 1e-14) {
+                converged = true;
+                break;
+            }
+            const double fp = 3.0 * z * z + 2.0 * c2 * z + c1;
+            if (fp == 0.0) break;
+            z -= fz / fp;
+            if (!(z > B)) z = B + 0.5 * (1.0 - B > 0 ? 1.0 - B : 1.0);
+        }
+        if (!converged && std::fabs(z * z * z + c2 * z * z + c1 * z + c0) > 1e-8)
+            throw alea::Error(ALEA_ERR_RUNTIME, "PengRobinson::compressibilityFactor: Newton-Raphson did not converge");
+        const double s2 = 1.41421356237309504880;
+        const double lnphi = (z - 1.0) - std::log(z - B) -
+                             (A / (2.0 * s2 * B)) * std::log((z + (1.0 + s2) * B) / (z + (1.0 - s2) * B));
+        *out = std::exp(lnphi) * p;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,104 @@
+// Internal declarations shared between the kernels and the C-ABI layer.
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace alea {
+
+struct GridImpl;
+GridImpl* grid_build(const alea_lennard_jones& lj, const alea_particles& fw,
+                     const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
+                     double spacing, int precision);
+GridImpl* grid_from_tables(const alea_lattice& lat, double spacing, const int32_t counts[3],
+                           const std::vector<uint32_t>& species,
+                           const std::vector<std::vector<double>>& tables);
+void grid_rebuild(GridImpl* g, cudaStream_t s);
+void grid_destroy(GridImpl* g);
+const double* grid_table(const GridImpl* g, uint32_t species);
+void grid_interpolate_device(const GridImpl* g, uint32_t species, const double* xyz, uint64_t n,
+                             double* out, cudaStream_t s);
+void grid_interpolate_host(const GridImpl* g, uint32_t species, const double* xyz, uint64_t n,
+                           double* out);
+void grid_download(const GridImpl* g, uint32_t species, double* out, uint64_t n);
+void grid_counts(const GridImpl* g, int32_t* out);
+double grid_spacing(const GridImpl* g);
+const std::vector<uint32_t>& grid_species(const GridImpl* g);
+void grid_stats(const GridImpl* g, alea_grid_stats* out);
+
+// grid_cache.cpp: the reference's on-disk cache format (version 1).
+void grid_cache_write(const char* path, const alea_lennard_jones& lj, const alea_particles& fw,
+                      const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
+                      double spacing, const int32_t counts[3], const std::vector<uint32_t>& species,
+                      const std::vector<std::vector<double>>& tables);
+std::string grid_cache_file_name(const alea_lennard_jones& lj, const alea_particles& fw,
+                                 const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
+                                 double spacing);
+// Returns false on a plain miss; throws Error(ALEA_ERR_RUNTIME) on a bad file.
+bool grid_cache_read(const char* dir, const alea_lennard_jones& lj, const alea_particles& fw,
+                     const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
+                     double spacing, int32_t counts[3], std::vector<uint32_t>& species,
+                     std::vector<std::vector<double>>& tables);
+
+// philox.cu
+void philox_raw(const uint32_t* ctr, const uint32_t* key, uint32_t* out, uint64_t n);
+void philox_fill_u64_device(uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+                            uint64_t* out, cudaStream_t s);
+void philox_fill_uniform_device(uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+                                double* out, cudaStream_t s);
+
+// lj.cu / ewald.cu
+void lj_particle_energy(const alea_lennard_jones& lj, const alea_particles& p,
+                        const alea_lattice& lat, const uint64_t* query, uint64_t nq,
+                        const uint64_t* excluded, uint64_t nex, double* out);
+void ewald_real_space_particle_energy(const alea_ewald& ew, const alea_particles& p,
+                                      const alea_lattice& lat, const uint64_t* query, uint64_t nq,
+                                      const uint64_t* excluded, uint64_t nex, double* out);
+void ewald_breakdown(const alea_ewald& ew, const alea_particles& p, const alea_lattice& lat,
+                     const uint64_t* excl, uint64_t n_excl, double* out);
+uint64_t ewald_terms_host(const Lattice& L, double alpha, int kmax, double* k, double* w,
+                          int32_t* nidx, uint64_t cap);
+
+struct EwaldStateImpl;
+EwaldStateImpl* ewald_state_create(const alea_ewald& ew, const alea_particles& p,
+                                   const alea_lattice& lat);
+void ewald_state_destroy(EwaldStateImpl* s);
+double ewald_state_energy(const EwaldStateImpl* s);
+double ewald_state_propose(const EwaldStateImpl* s, const double* removed, uint64_t nr,
+                           const double* added, uint64_t na);
+void ewald_state_commit(EwaldStateImpl* s, const double* removed, uint64_t nr, const double* added,
+                        uint64_t na);
+double ewald_state_recompute(const EwaldStateImpl* s, const alea_particles& p, uint64_t n_mol,
+                             const uint64_t* offsets, const uint64_t* indices);
+void ewald_state_resync(EwaldStateImpl* s, const alea_particles& p, uint64_t n_mol,
+                        const uint64_t* offsets, const uint64_t* indices);
+std::vector<double> ewald_state_raw(const EwaldStateImpl* s);
+uint64_t ewald_state_nk(const EwaldStateImpl* s);
+// Device views for kernels that read the committed cache (Widom).
+struct EwaldDeviceView {
+    uint64_t nk;
+    const double* k;     // 3 per term
+    const double* w;
+    const double* sre;
+    const double* sim;
+    const int32_t* nidx; // (n0, n1, n2) per term
+    double alpha;
+    double volume;
+    double self_pref;    // -kC * alpha / sqrt(pi)
+    double rec_pref;     // kC * 2 pi / V
+    int kmax;
+    double b[9];         // reciprocal vectors (rows)
+};
+EwaldDeviceView ewald_state_view(const EwaldStateImpl* s);
+
+// widom.cu
+struct WidomImpl;
+WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
+                        const alea_particles& fw, const alea_lattice& lat,
+                        const alea_molecule_species& guest, double temperature, int precision);
+void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+               int draw_order, alea_widom_result* out, double* per_trial);
+void widom_destroy(WidomImpl* w);
+
+}  // namespace alea

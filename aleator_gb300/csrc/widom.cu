@@ -1,0 +1,494 @@
+// Widom test-particle insertion on sm_103a.
+//
+// Reference: MonteCarloEngine::widomInsertionHenryCoefficient
+// (engines/monte_carlo/monte_carlo_engine.cc:850-917). Trial t of a freshly
+// seeded engine consumes Philox call indices 3t..3t+2 (position) and, for a
+// multi-site species, 3t+3..3t+5 (orientation, Shoemake quaternion,
+// monte_carlo_engine.cc:56-72), so each thread computes its own trial
+// directly from the counter. deltaU = sum over sites of the LJ energy against
+// every framework atom (lennard_jones.cc:158-182) + the real-space Ewald
+// energy (ewald.cc:223-249) + EwaldIncrementalState::proposeInsertion against
+// the framework's S(k) (ewald_incremental_state.cc:95-136, 152-154).
+//
+// One thread per trial; the framework is streamed through shared memory in
+// tiles (every thread reads the same atom: a broadcast). The reciprocal delta
+// walks the reference's term order row by row (n0, n1) and advances
+// exp(i k.r) along n2 by one complex multiply per term and site, instead of
+// one sincos per term and site. Boltzmann weights are reduced as an FP64
+// log-sum-exp: per block (max, sum exp(l - max), sum exp(2(l - max))), then
+// across blocks in block order.
+
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "grid.cuh"
+
+namespace alea {
+
+namespace {
+
+constexpr int WT = 128;        // trials per block
+constexpr int ATILE = 512;     // framework atoms per shared-memory tile
+constexpr int MAXS = 8;        // sites per guest molecule
+constexpr int MAXT = 64;       // LJ species
+
+struct GuestSite {
+    double x, y, z, q;
+    uint32_t lj;
+};
+
+struct WidomParams {
+    Lattice L;
+    uint64_t n_atoms;
+    int n_sites;
+    GuestSite site[MAXS];
+    uint32_t n_species;
+    double rc, rc2;
+    int trunc;
+    double temperature;
+    // electrostatics (charged == 0: none)
+    int charged;
+    double alpha, rc_ewald;
+    uint64_t nk;
+    int n_rows;
+    double b[9];
+    double self_pref, rec_pref;
+};
+
+struct KRow {
+    int n0, n1, m, t0;
+};
+
+// cross(qv, v) with non-contracted arithmetic (monte_carlo_engine.cc:25-27)
+__device__ __forceinline__ void cross_rn(const double* a, const double* b, double* o) {
+    o[0] = sub_rn(mul_rn(a[1], b[2]), mul_rn(a[2], b[1]));
+    o[1] = sub_rn(mul_rn(a[2], b[0]), mul_rn(a[0], b[2]));
+    o[2] = sub_rn(mul_rn(a[0], b[1]), mul_rn(a[1], b[0]));
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(WT)
+widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
+             const uint32_t* __restrict__ types, const PairParams* __restrict__ table,
+             const KRow* __restrict__ rows, const double* __restrict__ w,
+             const double* __restrict__ sre, const double* __restrict__ sim, uint64_t seed,
+             uint64_t stream, uint64_t first, uint64_t n, int draw_order,
+             double* __restrict__ per_trial, double* __restrict__ partial) {
+    __shared__ double4 tile[ATILE];
+    __shared__ uint32_t ttype[ATILE];
+    __shared__ PairParams pp[MAXS * MAXT];
+    __shared__ double red[WT];
+
+    const int ns = P.n_sites;
+    for (int i = threadIdx.x; i < ns * (int)P.n_species; i += WT) {
+        const int s = i / P.n_species, t = i % P.n_species;
+        pp[s * MAXT + t] = table[(size_t)P.site[s].lj * P.n_species + t];
+    }
+
+    const uint64_t local = (uint64_t)blockIdx.x * WT + threadIdx.x;
+    const bool active = local < n;
+    const uint64_t trial = first + local;
+    const double* M = P.L.m;
+
+    // ---- position and orientation (monte_carlo_engine.cc:882-901)
+    const uint64_t per = ns > 1 ? 6 : 3;
+    const uint64_t c0 = per * trial;
+    double u[3] = {philox_uniform(seed, stream, c0), philox_uniform(seed, stream, c0 + 1),
+                   philox_uniform(seed, stream, c0 + 2)};
+    if (draw_order == ALEA_DRAWS_RIGHT_TO_LEFT) {
+        const double tmp = u[0];
+        u[0] = u[2];
+        u[2] = tmp;
+    }
+    double ref[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        ref[c] = add_rn(add_rn(mul_rn(M[c], u[0]), mul_rn(M[3 + c], u[1])), mul_rn(M[6 + c], u[2]));
+    double q[4] = {1.0, 0.0, 0.0, 0.0};
+    if (ns > 1) {
+        double v[3] = {philox_uniform(seed, stream, c0 + 3), philox_uniform(seed, stream, c0 + 4),
+                       philox_uniform(seed, stream, c0 + 5)};
+        if (draw_order == ALEA_DRAWS_RIGHT_TO_LEFT) {
+            const double tmp = v[0];
+            v[0] = v[2];
+            v[2] = tmp;
+        }
+        const double r1 = __dsqrt_rn(sub_rn(1.0, v[0]));
+        const double r2 = __dsqrt_rn(v[0]);
+        const double t1 = mul_rn(2.0 * kPi, v[1]);
+        const double t2 = mul_rn(2.0 * kPi, v[2]);
+        q[0] = mul_rn(r2, cos(t2));
+        q[1] = mul_rn(r1, sin(t1));
+        q[2] = mul_rn(r1, cos(t1));
+        q[3] = mul_rn(r2, sin(t2));
+    }
+    double sx[MAXS], sy[MAXS], sz[MAXS];
+#pragma unroll
+    for (int s = 0; s < MAXS; ++s) {
+        if (s >= ns) break;
+        double loc[3] = {P.site[s].x, P.site[s].y, P.site[s].z};
+        double rot[3] = {loc[0], loc[1], loc[2]};
+        if (ns > 1) {  // rotateByQuaternion (monte_carlo_engine.cc:68-72)
+            const double qv[3] = {q[1], q[2], q[3]};
+            double c[3], t[3], c2[3];
+            cross_rn(qv, loc, c);
+            for (int i = 0; i < 3; ++i) t[i] = mul_rn(c[i], 2.0);
+            cross_rn(qv, t, c2);
+            for (int i = 0; i < 3; ++i) rot[i] = add_rn(add_rn(loc[i], mul_rn(t[i], q[0])), c2[i]);
+        }
+        sx[s] = add_rn(ref[0], rot[0]);
+        sy[s] = add_rn(ref[1], rot[1]);
+        sz[s] = add_rn(ref[2], rot[2]);
+    }
+
+    // ---- LJ and real-space sums against the framework, atom tiles in smem
+    double lj_site[MAXS], es_site[MAXS];
+#pragma unroll
+    for (int s = 0; s < MAXS; ++s) {
+        lj_site[s] = 0.0;
+        es_site[s] = 0.0;
+    }
+    for (uint64_t base = 0; base < P.n_atoms; base += ATILE) {
+        __syncthreads();
+        const int cnt = (int)min((uint64_t)ATILE, P.n_atoms - base);
+        for (int i = threadIdx.x; i < cnt; i += WT) {
+            tile[i] = atoms[base + i];
+            ttype[i] = types[base + i];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int s = 0; s < MAXS; ++s) {
+            if (s >= ns) break;
+            Real lj_acc = 0, es_acc = 0;
+            const PairParams* row = pp + s * MAXT;
+            for (int j = 0; j < cnt; ++j) {
+                const double4 a = tile[j];
+                double dx, dy, dz;
+                min_image(P.L, a.x - sx[s], a.y - sy[s], a.z - sz[s], dx, dy, dz);
+                const double r2 = dx * dx + dy * dy + dz * dz;
+                if (sizeof(Real) == 8) {
+                    const double r = sqrt(r2);
+                    lj_acc += lj_pair_rt(P.trunc, r, P.rc, row[ttype[j]]);
+                    if (P.charged && r <= P.rc_ewald) es_acc += a.w * (erfc(P.alpha * r) / r);
+                } else {
+                    const float rf = sqrtf((float)r2);
+                    if (r2 <= P.rc2) {
+                        const PairParams& p = row[ttype[j]];
+                        const float sr = (float)p.sigma / rf;
+                        const float sr2 = sr * sr;
+                        const float sr6 = sr2 * sr2 * sr2;
+                        float e = 4.0f * (float)p.eps * (sr6 * sr6 - sr6);
+                        if (P.trunc != ALEA_TRUNCATED) e -= (float)p.shift;
+                        if (P.trunc == ALEA_LINEAR_FORCE_SHIFTED)
+                            e -= (rf - (float)P.rc) * (float)p.dvdrc;
+                        lj_acc += e;
+                    }
+                    if (P.charged && rf <= (float)P.rc_ewald)
+                        es_acc += (float)a.w * (erfcf((float)P.alpha * rf) / rf);
+                }
+            }
+            lj_site[s] += (double)lj_acc;
+            es_site[s] += (double)es_acc;
+        }
+    }
+    double du = 0.0;
+#pragma unroll
+    for (int s = 0; s < MAXS; ++s)
+        if (s < ns) du += lj_site[s];
+
+    if (P.charged) {
+        double e = 0.0;
+#pragma unroll
+        for (int s = 0; s < MAXS; ++s)
+            if (s < ns) e += (P.site[s].q * es_site[s]) * kCoulomb;
+        du += e;
+        // ---- reciprocal delta against the framework S(k)
+        double th[MAXS][3], cs2[MAXS], sn2[MAXS];
+#pragma unroll
+        for (int s = 0; s < MAXS; ++s) {
+            if (s >= ns) break;
+            for (int i = 0; i < 3; ++i)
+                th[s][i] = P.b[3 * i] * sx[s] + P.b[3 * i + 1] * sy[s] + P.b[3 * i + 2] * sz[s];
+            sincos(th[s][2], &sn2[s], &cs2[s]);
+        }
+        double acc = 0.0;
+        for (int r = 0; r < P.n_rows; ++r) {
+            const KRow kr = rows[r];
+            double pc[MAXS], ps[MAXS];
+#pragma unroll
+            for (int s = 0; s < MAXS; ++s) {
+                if (s >= ns) break;
+                const double ph = kr.n0 * th[s][0] + kr.n1 * th[s][1] - kr.m * th[s][2];
+                sincos(ph, &ps[s], &pc[s]);
+            }
+            int t = kr.t0;
+            for (int n2 = -kr.m; n2 <= kr.m; ++n2) {
+                if (!(kr.n0 == 0 && kr.n1 == 0 && n2 == 0)) {
+                    double re = 0.0, im = 0.0;
+#pragma unroll
+                    for (int s = 0; s < MAXS; ++s) {
+                        if (s >= ns) break;
+                        re += P.site[s].q * pc[s];
+                        im += P.site[s].q * ps[s];
+                    }
+                    const double o_re = __ldg(&sre[t]), o_im = __ldg(&sim[t]);
+                    const double n_re = o_re + re, n_im = o_im + im;
+                    acc += __ldg(&w[t]) * ((n_re * n_re + n_im * n_im) - (o_re * o_re + o_im * o_im));
+                    ++t;
+                }
+#pragma unroll
+                for (int s = 0; s < MAXS; ++s) {
+                    if (s >= ns) break;
+                    const double c = pc[s] * cs2[s] - ps[s] * sn2[s];
+                    ps[s] = ps[s] * cs2[s] + pc[s] * sn2[s];
+                    pc[s] = c;
+                }
+            }
+        }
+        double q2 = 0.0, ex = 0.0;
+        for (int i = 0; i < ns; ++i) {
+            q2 += P.site[i].q * P.site[i].q;
+            for (int j = i + 1; j < ns; ++j) {
+                double dx, dy, dz;
+                min_image(P.L, sx[j] - sx[i], sy[j] - sy[i], sz[j] - sz[i], dx, dy, dz);
+                const double r = sqrt(dx * dx + dy * dy + dz * dz);
+                ex += P.site[i].q * P.site[j].q *
+                      (r < 1e-8 ? 2.0 * P.alpha / sqrt(kPi) : erf(P.alpha * r) / r);
+            }
+        }
+        du += (P.rec_pref * acc + P.self_pref * q2) + (-kCoulomb * ex);
+    }
+
+    if (active && per_trial) per_trial[local] = du;
+
+    // ---- log-sum-exp of -du/T over the block (fixed order)
+    const double lw = active ? (-du) / P.temperature : -INFINITY;
+    red[threadIdx.x] = lw;
+    __syncthreads();
+    for (int s = WT / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    const double mx = red[0];
+    __syncthreads();
+    const bool finite = mx > -INFINITY;
+    red[threadIdx.x] = (active && finite) ? exp(lw - mx) : 0.0;
+    __syncthreads();
+    for (int s = WT / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    const double s1 = red[0];
+    __syncthreads();
+    red[threadIdx.x] = (active && finite) ? exp(2.0 * (lw - mx)) : 0.0;
+    __syncthreads();
+    for (int s = WT / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[3 * blockIdx.x] = mx;
+        partial[3 * blockIdx.x + 1] = s1;
+        partial[3 * blockIdx.x + 2] = red[0];
+    }
+}
+
+// Combines the per-block (max, s1, s2) in block order: out = {max, S1, S2}.
+__global__ void widom_combine_kernel(const double* __restrict__ partial, uint64_t nblocks,
+                                     double* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double mx = -INFINITY;
+    for (uint64_t b = 0; b < nblocks; ++b) mx = fmax(mx, partial[3 * b]);
+    double s1 = 0.0, s2 = 0.0;
+    if (mx > -INFINITY)
+        for (uint64_t b = 0; b < nblocks; ++b) {
+            const double m = partial[3 * b];
+            if (!(m > -INFINITY)) continue;
+            const double f = exp(m - mx);
+            s1 += partial[3 * b + 1] * f;
+            s2 += partial[3 * b + 2] * (f * f);
+        }
+    out[0] = mx;
+    out[1] = s1;
+    out[2] = s2;
+}
+
+}  // namespace
+
+struct WidomImpl {
+    WidomParams P{};
+    int precision = ALEA_FP64;
+    DevBuf<double4> atoms;
+    DevBuf<uint32_t> types;
+    DevBuf<PairParams> table;
+    DevBuf<KRow> rows;
+    EwaldStateImpl* ews = nullptr;
+    DevBuf<double> partial, result, per_trial;
+    ~WidomImpl() {
+        if (ews) ewald_state_destroy(ews);
+    }
+};
+
+WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
+                        const alea_particles& fw, const alea_lattice& lat,
+                        const alea_molecule_species& guest, double temperature, int precision) {
+    require(temperature > 0.0, ALEA_ERR_INVALID_ARGUMENT,
+            "MonteCarloEngine: temperatureKelvin must be positive");
+    require(guest.n_sites >= 1 && guest.n_sites <= MAXS, ALEA_ERR_INVALID_ARGUMENT,
+            "Widom: the guest species needs 1..8 sites");
+    require(lj.n_species >= 1 && lj.n_species <= MAXT, ALEA_ERR_INVALID_ARGUMENT,
+            "Widom: 1..64 LJ species supported");
+    require(lj.cutoff > 0.0, ALEA_ERR_INVALID_ARGUMENT, "LennardJones: cutoff must be positive");
+    require(precision == ALEA_FP64 || precision == ALEA_FP32, ALEA_ERR_INVALID_ARGUMENT,
+            "Widom: precision must be ALEA_FP64 or ALEA_FP32");
+    require(fw.n == 0 || (fw.x && fw.y && fw.z), ALEA_ERR_INVALID_ARGUMENT,
+            "Widom: framework coordinates missing");
+    auto* w = new WidomImpl();
+    try {
+        WidomParams& P = w->P;
+        P.L = make_lattice(lat.m);
+        validate_cutoff(P.L, lj.cutoff, "MonteCarloEngine (LJ)");
+        P.n_atoms = fw.n;
+        P.n_sites = (int)guest.n_sites;
+        for (uint32_t s = 0; s < guest.n_sites; ++s) {
+            require(guest.lj_species[s] < lj.n_species, ALEA_ERR_OUT_OF_RANGE,
+                    "Widom: guest site LJ species out of range");
+            P.site[s] = GuestSite{guest.x[s], guest.y[s], guest.z[s],
+                                  guest.charge ? guest.charge[s] : 0.0, guest.lj_species[s]};
+        }
+        P.n_species = lj.n_species;
+        P.rc = lj.cutoff;
+        P.rc2 = lj.cutoff * lj.cutoff;
+        P.trunc = lj.truncation;
+        P.temperature = temperature;
+        w->precision = precision;
+        require_device();
+        std::vector<double4> packed(fw.n);
+        std::vector<uint32_t> types(fw.n, 0);
+        for (uint64_t i = 0; i < fw.n; ++i) {
+            packed[i] = make_double4(fw.x[i], fw.y[i], fw.z[i], fw.charge ? fw.charge[i] : 0.0);
+            if (fw.species) {
+                require(fw.species[i] < lj.n_species, ALEA_ERR_OUT_OF_RANGE,
+                        "Widom: framework species out of range");
+                types[i] = fw.species[i];
+            }
+        }
+        w->atoms.alloc(std::max<size_t>(fw.n, 1));
+        w->types.alloc(std::max<size_t>(fw.n, 1));
+        w->atoms.upload(packed.data(), fw.n);
+        w->types.upload(types.data(), fw.n);
+        std::vector<PairParams> table((size_t)lj.n_species * lj.n_species);
+        mixed_table(lj, table.data());
+        w->table.alloc(table.size());
+        w->table.upload(table.data(), table.size());
+        std::vector<KRow> rows;
+        if (ew) {
+            // engine ctor checks (monte_carlo_engine.cc:273-293)
+            double qs = 0.0;
+            for (uint32_t s = 0; s < guest.n_sites; ++s) qs += guest.charge ? guest.charge[s] : 0.0;
+            require(std::fabs(qs) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
+                    "MonteCarloEngine: GCMC species 0 is not individually charge-neutral");
+            double qf = 0.0;
+            for (uint64_t i = 0; i < fw.n; ++i) qf += fw.charge ? fw.charge[i] : 0.0;
+            require(std::fabs(qf) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
+                    "MonteCarloEngine: framework is not charge-neutral");
+            validate_cutoff(P.L, ew->real_space_cutoff, "MonteCarloEngine (Ewald real space)");
+            w->ews = ewald_state_create(*ew, fw, lat);
+            const EwaldDeviceView v = ewald_state_view(w->ews);
+            P.charged = 1;
+            P.alpha = ew->alpha;
+            P.rc_ewald = ew->real_space_cutoff;
+            P.nk = v.nk;
+            for (int i = 0; i < 9; ++i) P.b[i] = v.b[i];
+            P.self_pref = v.self_pref;
+            P.rec_pref = v.rec_pref;
+            const int K = ew->kmax;
+            const int bound = K * K + 2;
+            int t = 0;
+            for (int n0 = -K; n0 <= K; ++n0)
+                for (int n1 = -K; n1 <= K; ++n1) {
+                    const int rem = bound - n0 * n0 - n1 * n1;  // n2^2 < rem
+                    if (rem <= 0) continue;
+                    int m = 0;
+                    while ((m + 1) * (m + 1) < rem) ++m;
+                    rows.push_back(KRow{n0, n1, m, t});
+                    t += 2 * m + 1 - ((n0 == 0 && n1 == 0) ? 1 : 0);
+                }
+            require((uint64_t)t == v.nk, ALEA_ERR_RUNTIME, "Widom: k-row table mismatch");
+            P.n_rows = (int)rows.size();
+        }
+        w->rows.alloc(std::max<size_t>(rows.size(), 1));
+        w->rows.upload(rows.data(), rows.size());
+        w->result.alloc(3);
+    } catch (...) {
+        delete w;
+        throw;
+    }
+    return w;
+}
+
+void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+               int draw_order, alea_widom_result* out, double* per_trial) {
+    require(n > 0, ALEA_ERR_INVALID_ARGUMENT, "Widom: numTrials must be positive");
+    require(draw_order == ALEA_DRAWS_RIGHT_TO_LEFT || draw_order == ALEA_DRAWS_LEFT_TO_RIGHT,
+            ALEA_ERR_INVALID_ARGUMENT, "Widom: unknown draw order");
+    const uint64_t nblocks = (n + WT - 1) / WT;
+    require(nblocks < (1ull << 31), ALEA_ERR_INVALID_ARGUMENT, "Widom: too many trials per call");
+    if (w->partial.n < 3 * nblocks) w->partial.alloc(3 * nblocks);
+    if (per_trial && w->per_trial.n < n) w->per_trial.alloc(n);
+    const double* w_ = nullptr;
+    const double *sre = nullptr, *sim = nullptr;
+    if (w->ews) {
+        const EwaldDeviceView v = ewald_state_view(w->ews);
+        w_ = v.w;
+        sre = v.sre;
+        sim = v.sim;
+    }
+    cudaEvent_t e0, e1;
+    ALEA_CUDA(cudaEventCreate(&e0));
+    ALEA_CUDA(cudaEventCreate(&e1));
+    ALEA_CUDA(cudaEventRecord(e0));
+    if (w->precision == ALEA_FP32)
+        widom_kernel<float><<<(unsigned)nblocks, WT>>>(w->P, w->atoms.p, w->types.p, w->table.p,
+                                                       w->rows.p, w_, sre, sim, seed, stream, first,
+                                                       n, draw_order, per_trial ? w->per_trial.p : nullptr,
+                                                       w->partial.p);
+    else
+        widom_kernel<double><<<(unsigned)nblocks, WT>>>(w->P, w->atoms.p, w->types.p, w->table.p,
+                                                        w->rows.p, w_, sre, sim, seed, stream, first,
+                                                        n, draw_order, per_trial ? w->per_trial.p : nullptr,
+                                                        w->partial.p);
+    ALEA_CUDA(cudaGetLastError());
+    widom_combine_kernel<<<1, 32>>>(w->partial.p, nblocks, w->result.p);
+    ALEA_CUDA(cudaGetLastError());
+    ALEA_CUDA(cudaEventRecord(e1));
+    ALEA_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    ALEA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    double r[3];
+    ALEA_CUDA(cudaMemcpy(r, w->result.p, sizeof r, cudaMemcpyDeviceToHost));
+    if (per_trial) {
+        ALEA_CUDA(cudaMemcpy(per_trial, w->per_trial.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    const double nn = (double)n;
+    const double mean_scaled = r[1] / nn;  // mean(exp(l - max))
+    out->n_trials = n;
+    out->kernel_ms = ms;
+    if (r[1] > 0.0) {
+        out->log_mean_weight = r[0] + std::log(mean_scaled);
+        out->henry = std::exp(out->log_mean_weight) / w->P.temperature;
+        const double var = r[2] / nn - mean_scaled * mean_scaled;  // in units of exp(2 max)
+        out->rel_std_error = std::sqrt(std::max(var, 0.0) / nn) / mean_scaled;
+    } else {
+        out->log_mean_weight = -INFINITY;
+        out->henry = 0.0;
+        out->rel_std_error = INFINITY;
+    }
+}
+
+void widom_destroy(WidomImpl* w) { delete w; }
+
+}  // namespace alea

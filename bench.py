@@ -1,0 +1,387 @@
+"""Benchmark of the GCMC energy hot path on GB300.
+
+Headline workload: the framework energy grid of the large triclinic
+supercell: a 24 Å base cell (angles 70/80/100 degrees, 422 atoms) replicated
+4x4x4 (27 008 atoms), 0.2 Å spacing (457 x 437 x 437 nodes), the two LJ site
+types of rigid CO2 as guest species, truncated-shifted LJ with rc = 12.8 Å,
+FP32 pair terms with FP64 accumulation. The metric is energy-grid pair
+evaluations per second, counted as the reference's loop counts them
+(framework_energy_grid.cc:221-242): nodes x framework atoms x guest species.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+* ``value``: K timed grid builds with every input resident in HBM
+  (alea_grid_rebuild), L2 flushed between steps; CUDA events on the launching
+  stream; max over ranks.
+* ``e2e``: the same metric through the public C-ABI call a user makes
+  (FrameworkEnergyGrid from host arrays, then both tables copied to pinned
+  host memory), host<->device copies inside the timed region.
+* ``roofline``: the build kernel against the FP32 FFMA peak measured in the
+  same run (the kernel is FP32-pipe bound; the peaks file has no FP32 figure).
+* ``cpu_baseline``: the CPU restatement of the reference's grid loop on a
+  bounded sample of the same nodes, on all host cores.
+* ``--impl reference``: the reference's CPU algorithm (the oracle port; the
+  reference tree is not present on the GPU host) on all host cores, the same
+  metric on a bounded node sample per step.
+Multi-GPU: one replica of the workload per rank (weak scaling, no data-path
+collective); the barrier and the max-over-ranks time reduction are control.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SPACING = 0.2
+CUTOFF = 12.8
+REPS = 4
+FLOPS_PER_NODE_IMAGE = 11      # displacement, r^2, clamp, rcp, cutoff test
+FLOPS_PER_SPECIES = 8          # s^2, s^6, s^12 - s^6, 4 eps (.) - shift, accumulate
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.gpu), "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() in ("active", "1", "0x1"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload():
+    from aleator_gb300 import workloads as W
+    fw = W.triclinic_supercell(reps=REPS)
+    guests = [fw.guest_species["CO2_C"], fw.guest_species["CO2_O"]]
+    return fw, guests
+
+
+def cpu_grid_rate(fw, guests, seconds_target=12.0, threads=None):
+    """Reference grid loop (CPU restatement) on a bounded node sample."""
+    import oracle as O
+    orc = O.Oracle()
+    threads = threads or os.cpu_count() or 1
+    ff = dict(eps=fw.eps, sigma=fw.sigma, cutoff=CUTOFF, truncation=O.SHIFTED)
+    counts = orc.grid_point_counts(fw.lattice, SPACING)
+    total = counts[0] * counts[1] * counts[2]
+    # calibrate on a small sample, then size the measured sample
+    probe = max(threads, 16)
+    t0 = time.perf_counter()
+    orc.grid_build(ff, fw.lattice, fw.x, fw.y, fw.z, fw.species, guests[0], SPACING, 0, probe,
+                   threads)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    per_node = dt / probe
+    nodes = int(min(total, max(probe, seconds_target / per_node / len(guests))))
+    start = (total // 2) - nodes // 2  # a slab through the middle of the cell
+    t0 = time.perf_counter()
+    for g in guests:
+        orc.grid_build(ff, fw.lattice, fw.x, fw.y, fw.z, fw.species, g, SPACING, start,
+                       start + nodes, threads)
+    dt = time.perf_counter() - t0
+    pairs = nodes * fw.n_atoms * len(guests)
+    return pairs / dt, dict(nodes=nodes, pairs=pairs, seconds=dt, threads=threads,
+                            sample=f"{nodes} grid nodes x {fw.n_atoms} atoms x {len(guests)} species "
+                                   f"(node range [{start}, {start + nodes}) of {total})")
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    fw, guests = make_workload()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_grid_rate(fw, guests, seconds_target=2.0, threads=threads)
+    t0 = time.perf_counter()
+    rates, info = [], None
+    for _ in range(args.steps):
+        r, info = cpu_grid_rate(fw, guests, seconds_target=8.0, threads=threads)
+        rates.append(r)
+    wall = time.perf_counter() - t0
+    value = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": "energy-grid pair evals/s", "value": value,
+        "unit": "pair evals/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": _config(fw, guests),
+        "cpu_baseline": {"value": value, "unit": "pair evals/s", "cores": threads, "kind": "port",
+                         "sample": info["sample"] + " per step"},
+        "e2e": {"value": value, "unit": "pair evals/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "the reference tree is not present on the GPU host, so its compiled code "
+                "(oracle/_ref) cannot be rebuilt there; this is the C restatement of the same "
+                "loop, checked bit-exact against the reference's own build in the test suite",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _config(fw, guests):
+    return {"workload": "framework energy grid, 4x4x4 triclinic supercell (a=b=c=24 Å, "
+                        "70/80/100 deg) of 422 atoms, CO2 guest site types, 0.2 Å spacing",
+            "framework_atoms": int(fw.n_atoms), "guest_species": len(guests),
+            "grid_points": "457x437x437", "cutoff_angstrom": CUTOFF, "spacing_angstrom": SPACING,
+            "truncation": "shifted", "l2": "256 MB buffer written between timed steps; each "
+                                          "step also writes 1.4 GB of tables (> L2)",
+            "parallelism": "replica per GPU"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import aleator_gb300 as A
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    A.load_library()
+
+    fw, guests = make_workload()
+    ff = A.LennardJones(fw.eps, fw.sigma, CUTOFF, A.SHIFTED)
+    parts = A.ParticleData.from_framework(fw)
+    grid = A.FrameworkEnergyGrid(ff, parts, fw.lattice, guests, SPACING, A.FP32)
+    st = grid.stats()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        grid.rebuild(sp)
+    torch.cuda.synchronize()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            starts[i].record(stream)
+            grid.rebuild(sp)
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        region_s = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    kernel_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    step_ms = float(np.mean(kernel_ms))
+    st = grid.stats()
+    total_ms = float(np.sum(kernel_ms))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    pairs_step = st["algorithmic_pairs"]
+    value = ws * pairs_step * args.steps / (total_ms * 1e-3)
+
+    # e2e through the public call with host buffers (pinned host output)
+    nodes = st["nodes"]
+    pinned = [torch.empty(nodes, dtype=torch.float64, pin_memory=True) for _ in guests]
+    h2d = st["images"] * 32 + (fw.n_atoms * (4 * 8 + 4))
+    d2h = nodes * 8 * len(guests)
+    e2e_steps = max(2, min(args.steps, 5))
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        g = A.FrameworkEnergyGrid(ff, parts, fw.lattice, guests, SPACING, A.FP32)
+        for i, s in enumerate(guests):
+            status = A.library().alea_grid_download(
+                g._h, s, ctypes.cast(pinned[i].data_ptr(), ctypes.POINTER(ctypes.c_double)), nodes)
+            if status != 0:
+                raise RuntimeError(f"alea_grid_download failed with status {status}")
+        del g
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = ws * pairs_step * e2e_steps / e2e_s
+
+    if rank == 0:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+            if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        fp32_peak = A.fp32_fma_tflops()
+        ng = len(guests)
+        node_image = st["executed_pairs"] / ng
+        flops = node_image * (FLOPS_PER_NODE_IMAGE + FLOPS_PER_SPECIES * ng)
+        achieved = flops / (step_ms * 1e-3) / 1e12
+        line = {
+            "metric": "energy-grid pair evals/s", "value": value, "unit": "pair evals/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 pair terms, fp64 accumulation", "data": "synthetic",
+            "config": _config(fw, guests),
+            "region_ms": region_s * 1e3,
+            "gpu_launches": args.steps,
+            "roofline": {
+                "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak,
+                "peak_source": "FP32 FFMA loop measured in this run (alea_probe_fp32_fma_tflops)",
+                "traffic": None,
+                "kernel": "grid_build_kernel<float,2,SHIFTED>",
+                "executed_node_image_pairs_per_step": int(node_image),
+                "flops_per_node_image_pair": FLOPS_PER_NODE_IMAGE + FLOPS_PER_SPECIES * ng,
+            },
+            "e2e": {"value": e2e_value, "unit": "pair evals/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+            "clocks": clocks.summary(),
+            "peaks_file": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops")},
+        }
+        if not args.no_cpu_baseline:
+            rate, info = cpu_grid_rate(fw, guests, seconds_target=12.0)
+            line["cpu_baseline"] = {"value": rate, "unit": "pair evals/s",
+                                    "cores": info["threads"], "kind": "port",
+                                    "sample": info["sample"]}
+        if not args.no_extras:
+            line["extra"] = extras(A, torch, peaks)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def extras(A, torch, peaks):
+    """Secondary measurements of the other hot-path kernels (not the headline)."""
+    from aleator_gb300 import workloads as W
+    out = {}
+    # 424-atom cubic cell, 52^3 grid at 0.5 Å, CH4 (the CPU-runnable configuration)
+    fw = W.cubic_framework()
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    for prec, name in ((A.FP64, "fp64"), (A.FP32, "fp32")):
+        g = A.FrameworkEnergyGrid(ff, p, fw.lattice, [fw.guest_species["CH4"]], 0.5, prec)
+        ms = []
+        for _ in range(5):
+            g.rebuild(0)
+            ms.append(g.stats()["last_kernel_ms"])
+        st = g.stats()
+        out[f"grid_424atoms_52cube_{name}_pair_evals_per_s"] = st["algorithmic_pairs"] / (min(ms) * 1e-3)
+    # Widom, CH4 and charged CO2 (kMax 10 from the 1e-6 rule), FP64
+    alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
+    fwq = W.cubic_framework(charged=True)
+    pq = A.ParticleData.from_framework(fwq)
+    w = A.Widom(ff, p, fw.lattice, W.ch4_guest(fw), 298.0)
+    w.run(42, 0, 10000)
+    r = w.run(42, 0, 1_000_000)
+    out["widom_ch4_trials_per_s"] = 1_000_000 / (r["kernel_ms"] * 1e-3)
+    wq = A.Widom(ff, pq, fwq.lattice, W.co2_guest(fwq), 298.0, ewald=A.Ewald(alpha, 12.0, kmax))
+    wq.run(42, 0, 2000)
+    r = wq.run(42, 0, 100_000)
+    out["widom_co2_kmax10_trials_per_s"] = 100_000 / (r["kernel_ms"] * 1e-3)
+    out["widom_co2_kmax10_terms"] = int(A.EwaldIncrementalState(A.Ewald(alpha, 12.0, kmax), pq,
+                                                                fwq.lattice).term_count())
+    # trilinear interpolation (HBM-bound gather) on the 0.2 Å supercell grid
+    big, guests = make_workload()
+    gi = A.FrameworkEnergyGrid(A.LennardJones(big.eps, big.sigma, CUTOFF, A.SHIFTED),
+                               A.ParticleData.from_framework(big), big.lattice, guests[:1],
+                               SPACING, A.FP32)
+    n = 64 * 1024 * 1024
+    u = torch.rand(n, 3, dtype=torch.float64, device="cuda")
+    xyz = (u @ torch.tensor(big.lattice, device="cuda")).contiguous()
+    res = torch.empty(n, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        gi.interpolate_device(guests[0], xyz.data_ptr(), n, res.data_ptr(), s.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    gi.interpolate_device(guests[0], xyz.data_ptr(), n, res.data_ptr(), s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    algo_bytes = n * (24 + 8 * 8 + 8)
+    gbs = algo_bytes / (ms * 1e-3) / 1e9
+    out["interpolate_queries_per_s"] = n / (ms * 1e-3)
+    out["interpolate_roofline"] = {"bound": "hbm", "achieved": gbs, "peak": peaks.get("hbm_gbs"),
+                                   "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None,
+                                   "bytes_per_query": 96, "note": "8 corner loads of 8 B + 24 B in + 8 B out; "
+                                   "random queries over a 0.7 GB table"}
+    return out
+
+
+if __name__ == "__main__":
+    sys.exit(main())

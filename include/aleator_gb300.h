@@ -1,0 +1,297 @@
+/*
+ * aleator_gb300 — C ABI of the GB300 (sm_103a) GCMC energy hot path.
+ *
+ * Plain C: pointers, sizes and status codes only. Every entry point names
+ * the reference interface it replaces (paths relative to the reference
+ * project's src/). Host pointers are borrowed for the duration of a call;
+ * opaque handles own their device memory. No exception crosses this
+ * boundary: each call returns an alea_status and the calling thread's last
+ * error message is available from alea_last_error(). The status codes map
+ * one-to-one onto the exception types the reference throws:
+ *   ALEA_ERR_INVALID_ARGUMENT -> std::invalid_argument
+ *   ALEA_ERR_OUT_OF_RANGE     -> std::out_of_range
+ *   ALEA_ERR_RUNTIME          -> std::runtime_error
+ *
+ * Units follow the reference: Å, K (energy / k_B), e, K/Å^3 for pressure.
+ * Lattices are row-major double[9], row i = lattice vector a_i
+ * (core/geometry/lattice.hpp:21-30).
+ *
+ * Every energy routine here requires cutoff <= L_perp/2 on every axis
+ * (Lattice::validateCutoff, core/geometry/lattice.cc:286-300): under that
+ * condition at most one periodic image of an atom lies within the cutoff,
+ * which is what makes the device kernels' image handling equal to the
+ * reference's minimum-image search.
+ */
+#ifndef ALEATOR_GB300_H
+#define ALEATOR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t alea_status;
+enum {
+    ALEA_OK = 0,
+    ALEA_ERR_INVALID_ARGUMENT = 1,
+    ALEA_ERR_OUT_OF_RANGE = 2,
+    ALEA_ERR_RUNTIME = 3,
+    ALEA_ERR_CUDA = 4,
+    ALEA_ERR_NO_DEVICE = 5,
+    ALEA_ERR_DEVICE_CHECK = 6 /* a kernel's own bounds / wait check fired */
+};
+
+/* LennardJonesTruncation (forcefield/pairwise/lennard_jones.hpp:21-38) */
+enum { ALEA_TRUNCATED = 0, ALEA_SHIFTED = 1, ALEA_LINEAR_FORCE_SHIFTED = 2 };
+/* MixingRule (forcefield/pairwise/lennard_jones.hpp:42-50) */
+enum { ALEA_LORENTZ_BERTHELOT = 0, ALEA_GEOMETRIC = 1 };
+/* Arithmetic of the pair sums. FP64 is the parity form; FP32 evaluates pair
+ * terms in FP32 and accumulates them into FP64 per atom tile. */
+enum { ALEA_FP64 = 0, ALEA_FP32 = 1 };
+/* Order in which the reference's nested RNG draws reach their arguments
+ * (monte_carlo_engine.cc:572-579, 882-888): C++ leaves it unspecified; GCC
+ * evaluates right to left (a2 gets the first uniform), clang left to right. */
+enum { ALEA_DRAWS_RIGHT_TO_LEFT = 0, ALEA_DRAWS_LEFT_TO_RIGHT = 1 };
+
+typedef struct {
+    double m[9];
+} alea_lattice;
+
+/* LennardJones(perSpecies, cutoff, truncation, mixingRule)
+ * (forcefield/pairwise/lennard_jones.hpp:64-66) */
+typedef struct {
+    uint32_t n_species;
+    const double* epsilon; /* K, per LJ species */
+    const double* sigma;   /* Å, per LJ species */
+    double cutoff;
+    int32_t truncation;
+    int32_t mixing;
+} alea_lennard_jones;
+
+/* Ewald(alpha, realSpaceCutoff, kMax) (forcefield/electrostatics/ewald.hpp:76-77) */
+typedef struct {
+    double alpha;
+    double real_space_cutoff;
+    int32_t kmax;
+} alea_ewald;
+
+/* core::ParticleData SoA (core/math/particle_data.hpp:20-25), host pointers.
+ * charge may be NULL (all zero); species may be NULL (all zero). */
+typedef struct {
+    uint64_t n;
+    const double* x;
+    const double* y;
+    const double* z;
+    const double* charge;
+    const uint32_t* species;
+} alea_particles;
+
+/* MoleculeSpecies / MoleculeSite (engines/monte_carlo/molecule_species.hpp:14-29) */
+typedef struct {
+    uint32_t n_sites;
+    const double* x;
+    const double* y;
+    const double* z;
+    const uint32_t* lj_species;
+    const double* charge;
+} alea_molecule_species;
+
+/* ------------------------------------------------------------------ errors / device */
+const char* alea_status_string(alea_status s);
+/* Copies the calling thread's last error message; returns its full length. */
+size_t alea_last_error(char* buf, size_t cap);
+/* Library build identification: compute capability compiled for, e.g. 103. */
+alea_status alea_version(int32_t* major, int32_t* minor, int32_t* arch);
+/* Device name and SM count of the current device. */
+alea_status alea_device_info(char* name, size_t cap, int32_t* sm_count, int32_t* cc_major,
+                             int32_t* cc_minor);
+
+/* Sustained FP32 FFMA throughput of the current device in TFLOP/s (a
+ * measurement helper: the roofline denominator of the FP32 pair kernels). */
+alea_status alea_probe_fp32_fma_tflops(double* out);
+
+/* ------------------------------------------------------------------ Philox4x32-10 */
+/* philox4x32_10 (core/math/counter_based_rng.hpp:43-44, .cc:42-54), evaluated
+ * on the device for n (counter, key) pairs: ctr 4n, key 2n, out 4n words. */
+alea_status alea_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out, uint64_t n);
+/* Philox4x32Rng::seed(seed, stream) then n x nextU64() starting at call
+ * index `first` (counter_based_rng.cc:56-71). Host output. */
+alea_status alea_philox_fill_u64(uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+                                 uint64_t* out);
+/* ... n x nextUniform() (counter_based_rng.cc:73-79). Host output. */
+alea_status alea_philox_fill_uniform(uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+                                     double* out);
+/* Device-resident variants (out is a device pointer; stream is a cudaStream_t). */
+alea_status alea_philox_fill_u64_device(uint64_t seed, uint64_t stream_index, uint64_t first,
+                                        uint64_t n, uint64_t* out, void* cuda_stream);
+alea_status alea_philox_fill_uniform_device(uint64_t seed, uint64_t stream_index, uint64_t first,
+                                            uint64_t n, double* out, void* cuda_stream);
+
+/* ------------------------------------------------------------------ framework energy grid */
+/* FrameworkEnergyGrid(forceField, frameworkParticles, lattice, guestSpeciesIds,
+ * spacingAngstrom) (engines/monte_carlo/framework_energy_grid.hpp:118-120,
+ * .cc:193-249): builds one table per distinct guest species on the device.
+ * Fails with ALEA_ERR_INVALID_ARGUMENT when spacing <= 0 (as the reference)
+ * or when cutoff > L_perp/2. */
+typedef struct alea_grid alea_grid;
+alea_status alea_grid_build(const alea_lennard_jones* lj, const alea_particles* framework,
+                            const alea_lattice* lattice, const uint32_t* guest_species,
+                            uint32_t n_guest, double spacing, int32_t precision, alea_grid** out);
+/* pointCounts() / spacingAngstrom() (framework_energy_grid.hpp:131-132) */
+alea_status alea_grid_point_counts(const alea_grid* g, int32_t out[3]);
+alea_status alea_grid_spacing(const alea_grid* g, double* out);
+/* Sorted distinct guest species with a table; n_out receives the count. */
+alea_status alea_grid_species(const alea_grid* g, uint32_t* out, uint32_t cap, uint32_t* n_out);
+/* interpolate(guestSpeciesId, position) (framework_energy_grid.hpp:128-129,
+ * .cc:251-288) for n positions (xyz interleaved, host). Unknown species ->
+ * ALEA_ERR_OUT_OF_RANGE, as the reference's tables_.at(). */
+alea_status alea_grid_interpolate(const alea_grid* g, uint32_t species, const double* xyz,
+                                  uint64_t n, double* out);
+/* Same with device pointers on a caller stream (the HBM-resident form). */
+alea_status alea_grid_interpolate_device(const alea_grid* g, uint32_t species, const double* xyz,
+                                         uint64_t n, double* out, void* cuda_stream);
+/* Copies one species' table (nx*ny*nz doubles, index (iz*ny+iy)*nx+ix,
+ * framework_energy_grid.hpp:186-194) to host memory. */
+alea_status alea_grid_download(const alea_grid* g, uint32_t species, double* out, uint64_t n);
+/* Device pointer of one species' table (owned by the grid). */
+alea_status alea_grid_table_device(const alea_grid* g, uint32_t species, const double** out);
+/* Re-runs the build kernels into the grid's own tables with inputs already
+ * resident in HBM; returns the kernel-only time. Used for measurement. */
+alea_status alea_grid_rebuild(alea_grid* g, void* cuda_stream);
+typedef struct {
+    uint64_t nodes;             /* nx*ny*nz */
+    uint64_t algorithmic_pairs; /* sum over species of nodes * framework atoms */
+    uint64_t executed_pairs;    /* node-image pairs the kernel evaluated (all species) */
+    uint64_t images;            /* periodic atom images staged */
+    uint64_t bricks;            /* thread-block tiles of nodes */
+    float last_kernel_ms;       /* duration of the last build, CUDA events */
+} alea_grid_stats;
+alea_status alea_grid_stats_get(const alea_grid* g, alea_grid_stats* out);
+/* Writes the reference's on-disk cache file for this grid (format version 1,
+ * framework_energy_grid.cc:290-316; key layout framework_energy_grid.cc:77-97).
+ * The key fields are passed explicitly as in makeFrameworkEnergyGridCacheKey
+ * (framework_energy_grid.cc:169-191). */
+alea_status alea_grid_serialize(const alea_grid* g, const char* path,
+                                const alea_lennard_jones* lj, const alea_particles* framework,
+                                const alea_lattice* lattice, const uint32_t* guest_species,
+                                uint32_t n_guest);
+/* cacheFilePath(cacheDirectory, key) (framework_energy_grid.cc:318-325). */
+alea_status alea_grid_cache_file_name(const alea_lennard_jones* lj,
+                                      const alea_particles* framework,
+                                      const alea_lattice* lattice, const uint32_t* guest_species,
+                                      uint32_t n_guest, double spacing, char* out, size_t cap);
+/* loadFromCache (framework_energy_grid.cc:354-409): reads the file named by
+ * the key in cache_dir; *out = NULL on a plain miss; ALEA_ERR_RUNTIME on a
+ * version mismatch, key mismatch or truncated file. */
+alea_status alea_grid_load_cache(const char* cache_dir, const alea_lennard_jones* lj,
+                                 const alea_particles* framework, const alea_lattice* lattice,
+                                 const uint32_t* guest_species, uint32_t n_guest, double spacing,
+                                 alea_grid** out);
+alea_status alea_grid_destroy(alea_grid* g);
+
+/* ------------------------------------------------------------------ Lennard-Jones */
+/* LennardJones::computeParticleEnergy(index, particles, lattice, excluded)
+ * (lennard_jones.cc:158-182) for n_query indices at once. */
+alea_status alea_lj_particle_energy(const alea_lennard_jones* lj, const alea_particles* particles,
+                                    const alea_lattice* lattice, const uint64_t* query,
+                                    uint64_t n_query, const uint64_t* excluded,
+                                    uint64_t n_excluded, double* out);
+/* LennardJones::tailEnergyCorrection (lennard_jones.cc:246-257). */
+alea_status alea_lj_tail_correction(const alea_lennard_jones* lj, const alea_particles* particles,
+                                    const alea_lattice* lattice, double* out);
+
+/* ------------------------------------------------------------------ Ewald */
+/* Ewald::reciprocalTerms(lattice) (ewald.hpp:137-138, ewald.cc:137-161):
+ * k (3 per term) and weight; n_out = total count even when cap is smaller. */
+alea_status alea_ewald_reciprocal_terms(const alea_lattice* lattice, double alpha, int32_t kmax,
+                                        double* k, double* weight, uint64_t cap, uint64_t* n_out);
+/* Ewald::realSpaceParticleEnergy (ewald.hpp:159-161, ewald.cc:223-249) for
+ * n_query indices. */
+alea_status alea_ewald_real_space_particle_energy(const alea_ewald* ewald,
+                                                  const alea_particles* particles,
+                                                  const alea_lattice* lattice,
+                                                  const uint64_t* query, uint64_t n_query,
+                                                  const uint64_t* excluded, uint64_t n_excluded,
+                                                  double* out);
+/* Ewald::computeEnergyBreakdown (ewald.cc:251-313): out = {real, reciprocal,
+ * self, exclusion, surface}; exclusions as index pairs (2 per pair).
+ * ALEA_ERR_INVALID_ARGUMENT for a non-neutral system (ewald.cc:181-195). */
+alea_status alea_ewald_energy_breakdown(const alea_ewald* ewald, const alea_particles* particles,
+                                        const alea_lattice* lattice, const uint64_t* exclusions,
+                                        uint64_t n_exclusions, double out[5]);
+
+/* EwaldIncrementalState (forcefield/electrostatics/ewald_incremental_state.hpp:70-171):
+ * the structure-factor cache lives in HBM. Sites are packed {x, y, z, q}. */
+typedef struct alea_ewald_state alea_ewald_state;
+/* EwaldIncrementalState(ewald, particles, lattice) (ewald_incremental_state.cc:55-83) */
+alea_status alea_ewald_state_create(const alea_ewald* ewald, const alea_particles* particles,
+                                    const alea_lattice* lattice, alea_ewald_state** out);
+/* committedEnergy() (ewald_incremental_state.cc:85-93) */
+alea_status alea_ewald_state_committed_energy(const alea_ewald_state* s, double* out);
+/* proposeMove / proposeInsertion / proposeDeletion (ewald_incremental_state.cc:147-159):
+ * removed -> added; never mutates the committed cache. */
+alea_status alea_ewald_state_propose(const alea_ewald_state* s, const double* removed,
+                                     uint64_t n_removed, const double* added, uint64_t n_added,
+                                     double* delta);
+/* commitMove / commitInsertion / commitDeletion (ewald_incremental_state.cc:161-172) */
+alea_status alea_ewald_state_commit(alea_ewald_state* s, const double* removed,
+                                    uint64_t n_removed, const double* added, uint64_t n_added);
+/* recomputeFromScratch (ewald_incremental_state.cc:174-212); molecules as
+ * CSR (offsets n_molecules+1, indices). */
+alea_status alea_ewald_state_recompute(const alea_ewald_state* s, const alea_particles* particles,
+                                       uint64_t n_molecules, const uint64_t* offsets,
+                                       const uint64_t* indices, double* out);
+/* resync (ewald_incremental_state.cc:214-247) */
+alea_status alea_ewald_state_resync(alea_ewald_state* s, const alea_particles* particles,
+                                    uint64_t n_molecules, const uint64_t* offsets,
+                                    const uint64_t* indices);
+/* rawStateForTesting (ewald_incremental_state.cc:249-257): sRe..., sIm...,
+ * self, exclusion; n_out = full length. */
+alea_status alea_ewald_state_raw(const alea_ewald_state* s, double* out, uint64_t cap,
+                                 uint64_t* n_out);
+alea_status alea_ewald_state_term_count(const alea_ewald_state* s, uint64_t* out);
+alea_status alea_ewald_state_destroy(alea_ewald_state* s);
+
+/* ------------------------------------------------------------------ Widom insertion */
+/* MonteCarloEngine::widomInsertionHenryCoefficient(numTrials, speciesIndex)
+ * (engines/monte_carlo/monte_carlo_engine.hpp:198-199, .cc:850-917) on the
+ * device: trial t of stream (seed, stream) uses Philox call indices 3t..3t+2
+ * (one site) or 6t..6t+5 (several sites), exactly the draws a freshly seeded
+ * engine makes. A context holds the framework, force field, optional Ewald
+ * S(k) of the framework and the guest template in HBM. */
+typedef struct alea_widom alea_widom;
+alea_status alea_widom_create(const alea_lennard_jones* lj, const alea_ewald* ewald /* nullable */,
+                              const alea_particles* framework, const alea_lattice* lattice,
+                              const alea_molecule_species* guest, double temperature,
+                              int32_t precision, alea_widom** out);
+typedef struct {
+    double henry;             /* K_H = mean(exp(-dU/T)) / T, 1/K */
+    double log_mean_weight;   /* log(mean(exp(-dU/T))), from the FP64 log-sum-exp */
+    double rel_std_error;     /* standard error of K_H / K_H over the trials */
+    uint64_t n_trials;
+    float kernel_ms;          /* device time of the trial + reduction kernels */
+} alea_widom_result;
+/* Trials [first_trial, first_trial + n_trials); per_trial_du (nullable, host)
+ * receives each trial's deltaU in K. */
+alea_status alea_widom_run(alea_widom* w, uint64_t seed, uint64_t stream, uint64_t first_trial,
+                           uint64_t n_trials, int32_t draw_order, alea_widom_result* out,
+                           double* per_trial_du);
+alea_status alea_widom_destroy(alea_widom* w);
+
+/* ------------------------------------------------------------------ acceptance / EOS (host) */
+/* gcmc::insertionRatio ... clampToProbability (engines/monte_carlo/gcmc_acceptance.hpp:28-101) */
+double alea_insertion_ratio(double f, double v, uint64_t n_before, double t, double du);
+double alea_deletion_ratio(double f, double v, uint64_t n_before, double t, double du);
+double alea_metropolis_ratio(double t, double du);
+double alea_swap_ratio(double f_from, double f_to, uint64_t n_from, uint64_t n_to, double t,
+                       double du);
+/* PengRobinson::fugacityPascal (engines/monte_carlo/peng_robinson.cc:108-110) */
+alea_status alea_peng_robinson_fugacity(double tc, double pc, double omega, double t, double p,
+                                        double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ALEATOR_GB300_H */

@@ -1,0 +1,211 @@
+"""Framework energy grid on the GPU against the reference (golden cache files,
+interpolations) and the oracle.
+
+Tolerances: FP64 form 1e-10 relative per node with a 1 K floor
+(|dE| <= 1e-10 * max(1 K, |E|)); FP32 form 1e-5 relative with the same floor,
+checked on nodes with E <= 1e4 K (deeper in the repulsive core the FP32 terms
+are clamped and every such node ends at the 1e5 K cap in both forms);
+interpolation on identical tables bit-exact."""
+import os
+import tempfile
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import golden, rel_err
+from test_oracle_golden import _cache_tables
+
+pytestmark = pytest.mark.gpu
+
+
+def _gc():
+    return golden("grid_cubic")
+
+
+def _build(A, g, spacing, precision, cutoff=None, guests=None):
+    ff = A.LennardJones(g["eps"], g["sigma"], float(g["cutoff"]) if cutoff is None else cutoff,
+                        A.SHIFTED)
+    p = A.ParticleData(g["x"], g["y"], g["z"], g["charge"], g["species"])
+    gg = [int(v) for v in g["guests"]] if guests is None else guests
+    return A.FrameworkEnergyGrid(ff, p, g["lattice"], gg, spacing, precision), ff, p
+
+
+def test_fp64_grid_matches_reference_tables(lib):
+    A, _ = lib
+    g = _gc()
+    grid, ff, p = _build(A, g, float(g["spacing"]), A.FP64)
+    counts, tables = _cache_tables(g["cache_file"])
+    assert grid.point_counts() == counts
+    assert grid.species() == sorted(tables)
+    for sid, ref_table in tables.items():
+        assert rel_err(grid.table(sid), ref_table).max() <= 1e-10
+
+
+def test_fp32_grid_within_1e5(lib):
+    A, _ = lib
+    g = _gc()
+    grid, ff, p = _build(A, g, float(g["spacing"]), A.FP32)
+    counts, tables = _cache_tables(g["cache_file"])
+    for sid, ref_table in tables.items():
+        mine = grid.table(sid)
+        keep = ref_table <= 1e4
+        assert keep.sum() > 0.5 * ref_table.size
+        assert rel_err(mine[keep], ref_table[keep]).max() <= 1e-5
+        assert (mine[ref_table >= 1e5] >= 1e4).all()
+
+
+def test_interpolation_bit_exact(lib):
+    A, _ = lib
+    g = _gc()
+    grid, ff, p = _build(A, g, float(g["spacing"]), A.FP64)
+    counts, tables = _cache_tables(g["cache_file"])
+    # identical tables -> identical interpolation: load the reference's file
+    with tempfile.TemporaryDirectory() as td:
+        (Path(td) / str(g["cache_name"])).write_bytes(g["cache_file"].tobytes())
+        loaded = A.FrameworkEnergyGrid.load_from_cache(td, ff, p, g["lattice"],
+                                                       [int(v) for v in g["guests"]],
+                                                       float(g["spacing"]))
+    assert loaded is not None
+    for i, sid in enumerate(g["guests"]):
+        assert np.array_equal(loaded.interpolate(int(sid), g["points"]), g["interp"][i])
+        # and the GPU-built tables interpolate to within the FP64 tolerance
+        assert rel_err(grid.interpolate(int(sid), g["points"]), g["interp"][i]).max() <= 1e-10
+    with pytest.raises(IndexError):
+        grid.interpolate(0, g["points"][:4])
+
+
+def test_cache_file_byte_identical_and_guards(lib):
+    """framework_energy_grid.cc:290-409 and test_framework_energy_grid_cache.cc:
+    the written file equals the reference's bytes (tables from the reference's
+    own file, so the comparison is of the format), names match, and a foreign
+    file at the hashed path is a hard error."""
+    A, _ = lib
+    g = _gc()
+    ff = A.LennardJones(g["eps"], g["sigma"], float(g["cutoff"]), A.SHIFTED)
+    p = A.ParticleData(g["x"], g["y"], g["z"], g["charge"], g["species"])
+    guests = [int(v) for v in g["guests"]]
+    name = A.FrameworkEnergyGrid.cache_file_name(ff, p, g["lattice"], guests, float(g["spacing"]))
+    assert name == str(g["cache_name"])
+    with tempfile.TemporaryDirectory() as td:
+        (Path(td) / name).write_bytes(g["cache_file"].tobytes())
+        loaded = A.FrameworkEnergyGrid.load_from_cache(td, ff, p, g["lattice"], guests,
+                                                       float(g["spacing"]))
+        out = Path(td) / "again.bin"
+        loaded.serialize(out)
+        assert out.read_bytes() == g["cache_file"].tobytes()
+        # miss -> None
+        assert A.FrameworkEnergyGrid.load_from_cache(td, ff, p, g["lattice"], guests, 1.0) is None
+        # version mismatch -> hard error
+        bad = bytearray(g["cache_file"].tobytes())
+        bad[0] = 2
+        (Path(td) / name).write_bytes(bytes(bad))
+        with pytest.raises(RuntimeError, match="format version"):
+            A.FrameworkEnergyGrid.load_from_cache(td, ff, p, g["lattice"], guests, float(g["spacing"]))
+        # truncated -> hard error
+        (Path(td) / name).write_bytes(g["cache_file"].tobytes()[:5000])
+        with pytest.raises(RuntimeError, match="truncated or corrupt"):
+            A.FrameworkEnergyGrid.load_from_cache(td, ff, p, g["lattice"], guests, float(g["spacing"]))
+        # GPU-built grid round-trips bit-identically through its own file
+        grid, _, _ = _build(A, g, float(g["spacing"]), A.FP64)
+        grid.serialize(Path(td) / name)
+        back = A.FrameworkEnergyGrid.load_from_cache(td, ff, p, g["lattice"], guests, float(g["spacing"]))
+        for sid in guests:
+            assert np.array_equal(back.table(sid), grid.table(sid))
+
+
+def test_triclinic_fp64(lib):
+    A, _ = lib
+    t = golden("triclinic")
+    counts, tables = _cache_tables(t["cache_file"])
+    sid = list(tables)[0]
+    ff = A.LennardJones(t["eps"], t["sigma"], 10.0, A.SHIFTED)
+    p = A.ParticleData(t["x"], t["y"], t["z"], t["charge"], t["species"])
+    grid = A.FrameworkEnergyGrid(ff, p, t["lattice"], [sid], 1.0, A.FP64)
+    assert grid.point_counts() == counts
+    assert rel_err(grid.table(sid), tables[sid]).max() <= 1e-10
+    g32 = A.FrameworkEnergyGrid(ff, p, t["lattice"], [sid], 1.0, A.FP32)
+    keep = tables[sid] <= 1e4
+    assert rel_err(g32.table(sid)[keep], tables[sid][keep]).max() <= 1e-5
+
+
+@pytest.mark.parametrize("trunc", [0, 2])
+def test_truncations_vs_oracle(lib, orc, trunc):
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    fw = W.cubic_framework(seed=7)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.0, trunc)
+    p = A.ParticleData.from_framework(fw)
+    grid = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4, 6], 1.7, A.FP64)
+    for sid in (4, 6):
+        ref = orc.grid_build(dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.0, truncation=trunc),
+                             fw.lattice, fw.x, fw.y, fw.z, fw.species, sid, 1.7, threads=8)
+        assert rel_err(grid.table(sid), ref).max() <= 1e-10
+
+
+def test_full_c1_grid_vs_oracle_sample(lib, orc):
+    """The 52^3 grid of the 424-atom cell at 0.5 Å: every node in FP64 and FP32
+    against the oracle on a strided sample of nodes."""
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    fw = W.cubic_framework()
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    g64 = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4], 0.5, A.FP64)
+    g32 = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4], 0.5, A.FP32)
+    assert g64.point_counts() == (52, 52, 52)
+    t64, t32 = g64.table(4), g32.table(4)
+    st = g64.stats()
+    assert st["algorithmic_pairs"] == 52 ** 3 * 424
+    odict = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.8, truncation=O.SHIFTED)
+    idx = np.arange(0, 52 ** 3, 97)
+    ref = np.concatenate([orc.grid_build(odict, fw.lattice, fw.x, fw.y, fw.z, fw.species, 4, 0.5,
+                                         node_begin=int(i), node_end=int(i) + 1) for i in idx])
+    assert rel_err(t64[idx], ref).max() <= 1e-10
+    keep = ref <= 1e4
+    assert rel_err(t32[idx][keep], ref[keep]).max() <= 1e-5
+
+
+def test_supercell_invariance_at_scale(lib):
+    """Size-independent property (test_supercell_energy_invariance.cc): the grid
+    of a 2x2x2 supercell with node spacing L/n equals the base cell's grid tiled,
+    node for node."""
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    base = W.cubic_framework(seed=3)
+    sup = W.replicate(base, (2, 2, 2))
+    ff = A.LennardJones(base.eps, base.sigma, 12.8, A.SHIFTED)
+    n = 40
+    spacing = 25.832 / n
+    gb = A.FrameworkEnergyGrid(ff, A.ParticleData.from_framework(base), base.lattice, [5], spacing, A.FP64)
+    gs = A.FrameworkEnergyGrid(ff, A.ParticleData.from_framework(sup), sup.lattice, [5], spacing, A.FP64)
+    assert gs.point_counts() == (2 * n, 2 * n, 2 * n)
+    tb = gb.table(5).reshape(n, n, n)
+    ts = gs.table(5).reshape(2 * n, 2 * n, 2 * n)
+    tiled = np.tile(tb, (2, 2, 2))
+    assert rel_err(ts, tiled).max() <= 1e-10
+    for prec in (A.FP32,):
+        g32 = A.FrameworkEnergyGrid(ff, A.ParticleData.from_framework(sup), sup.lattice, [5], spacing, prec)
+        t32 = g32.table(5)
+        keep = tiled.reshape(-1) <= 1e4
+        assert rel_err(t32[keep], tiled.reshape(-1)[keep]).max() <= 1e-5
+
+
+def test_edge_cases(lib):
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    fw = W.cubic_framework(seed=5)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.0, A.SHIFTED)
+    # empty framework: every node is 0
+    empty = A.ParticleData(np.zeros(0), np.zeros(0), np.zeros(0))
+    g = A.FrameworkEnergyGrid(ff, empty, fw.lattice, [4], 3.0)
+    assert (g.table(4) == 0).all()
+    # one atom, grid coarser than one node per axis is clamped to 1
+    one = A.ParticleData([1.0], [2.0], [3.0], None, [0])
+    g1 = A.FrameworkEnergyGrid(ff, one, fw.lattice, [4, 4, 4], 100.0)
+    assert g1.point_counts() == (1, 1, 1) and g1.species() == [4]
+    d = np.sqrt(1 + 4 + 9)
+    eps, sig = np.sqrt(fw.eps[4] * fw.eps[0]), 0.5 * (fw.sigma[4] + fw.sigma[0])
+    raw = lambda r: 4 * eps * ((sig / r) ** 12 - (sig / r) ** 6)
+    assert abs(g1.table(4)[0] - min(raw(d) - raw(12.0), 1e5)) <= 1e-10 * max(1, abs(raw(d)))
