@@ -54,6 +54,7 @@ struct GridGeom {
     int nb[3];             // bins per axis
     double binw[3];        // fractional bin width
     double G[9];           // metric tensor a_i . a_j
+    float Gf[9];           // the same in FP32 (bin culling)
     double rc, rc2;
     int bricks[3];
     int n_types;           // framework LJ species in the table
@@ -97,11 +98,6 @@ __device__ __forceinline__ void fence_barrier_init() {
 __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
-__device__ __forceinline__ float rcp_approx(float x) {
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
 
 // Waits for one phase of an mbarrier with an iteration limit; on timeout the
 // error flag is raised and false returned (the caller stops using the tile).
@@ -117,33 +113,35 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // Lower bound on min |D . M|^2 over the fractional box D = [dlo, dhi]:
 // a few coordinate-descent sweeps of the convex quadratic D^T G D, then the
 // first-order bound f(x) + min_{y in box} grad(x).(y - x), which never exceeds
-// the true minimum. Exact for orthorhombic cells.
-__device__ __forceinline__ double box_min_dist2_lb(const double* G, const double* dlo,
-                                                   const double* dhi) {
-    double x[3];
+// the true minimum. Exact for orthorhombic cells. FP32 (FP64 issues at a small
+// fraction of the FP32 rate on this part); the caller compares against rc^2
+// with a relative margin far above FP32 rounding, so culling stays conservative.
+__device__ __forceinline__ float box_min_dist2_lb(const float* G, const float* dlo,
+                                                  const float* dhi) {
+    float x[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) x[i] = fmin(fmax(0.0, dlo[i]), dhi[i]);
+    for (int i = 0; i < 3; ++i) x[i] = fminf(fmaxf(0.0f, dlo[i]), dhi[i]);
 #pragma unroll
     for (int sweep = 0; sweep < 4; ++sweep) {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            double s = 0.0;
+            float s = 0.0f;
 #pragma unroll
             for (int j = 0; j < 3; ++j)
                 if (j != i) s += G[3 * i + j] * x[j];
-            x[i] = fmin(fmax(-s / G[4 * i], dlo[i]), dhi[i]);
+            x[i] = fminf(fmaxf(-s / G[4 * i], dlo[i]), dhi[i]);
         }
     }
-    double g[3];
-    double f = 0.0;
+    float g[3];
+    float f = 0.0f;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        g[i] = 2.0 * (G[3 * i] * x[0] + G[3 * i + 1] * x[1] + G[3 * i + 2] * x[2]);
-        f += 0.5 * g[i] * x[i];
+        g[i] = 2.0f * (G[3 * i] * x[0] + G[3 * i + 1] * x[1] + G[3 * i + 2] * x[2]);
+        f += 0.5f * g[i] * x[i];
     }
-    double lb = f;
+    float lb = f;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) lb += fmin(g[i] * (dlo[i] - x[i]), g[i] * (dhi[i] - x[i]));
+    for (int i = 0; i < 3; ++i) lb += fminf(g[i] * (dlo[i] - x[i]), g[i] * (dhi[i] - x[i]));
     return lb;
 }
 
@@ -215,19 +213,20 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
         if (tid == 0) flag_error(flags, DEV_ERR_CAPACITY);
         return;
     }
+    const float keep2 = (float)(geo.rc2 * (1.0 + 1e-3) + 1e-2);
     for (int r = tid; r < total_rows; r += THREADS) {
         const int ry = blo[1] + r % rows_y, rz = blo[2] + r / rows_y;
         int first = -1, last = -1;
         for (int rx = blo[0]; rx <= bhi[0]; ++rx) {
-            double dlo[3], dhi[3];
+            float dlo[3], dhi[3];
             const int bi[3] = {rx, ry, rz};
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                const double b0 = geo.lo[a] + bi[a] * geo.binw[a];
-                dlo[a] = b0 - fhi[a];
-                dhi[a] = b0 + geo.binw[a] - flo[a];
+                const float b0 = (float)geo.lo[a] + bi[a] * (float)geo.binw[a];
+                dlo[a] = b0 - (float)fhi[a];
+                dhi[a] = b0 + (float)geo.binw[a] - (float)flo[a];
             }
-            if (box_min_dist2_lb(geo.G, dlo, dhi) <= geo.rc2 * (1.0 + 1e-9) + 1e-9) {
+            if (box_min_dist2_lb(geo.Gf, dlo, dhi) <= keep2) {
                 if (first < 0) first = rx;
                 last = rx;
             }
@@ -259,29 +258,35 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
 #pragma unroll
         for (int k = 0; k < NPT; ++k) acc[g][k] = 0.0;
 
-    // brick origin (FP32 form) and node coordinates
+    // Brick centre (origin of the FP32 form's local coordinates: the atoms
+    // that matter most, the close ones, then have the smallest coordinates and
+    // the smallest rounding) and node coordinates.
     const double* M = geo.L.m;
     double ox = 0, oy = 0, oz = 0;
     Real nxr[NPT], nyr[NPT], nzr[NPT];
     {
-        const double f0o = (double)x0 / nx, f1o = (double)y0 / ny, f2o = (double)z0 / nz;
+        const double cx = x0 + 0.5 * (BX - 1), cy = y0 + 0.5 * (BY - 1), cz = z0 + 0.5 * (BZ - 1);
+        const double f0o = cx / nx, f1o = cy / ny, f2o = cz / nz;
         ox = f0o * M[0] + f1o * M[3] + f2o * M[6];
         oy = f0o * M[1] + f1o * M[4] + f2o * M[7];
         oz = f0o * M[2] + f1o * M[5] + f2o * M[8];
 #pragma unroll
         for (int k = 0; k < NPT; ++k) {
             const int izn = z0 + tz + 2 * k;
+            if (sizeof(Real) == 4) {
+                const double d0 = (ixn - cx) / nx, d1 = (iyn - cy) / ny, d2 = (izn - cz) / nz;
+                nxr[k] = (Real)(d0 * M[0] + d1 * M[3] + d2 * M[6]);
+                nyr[k] = (Real)(d0 * M[1] + d1 * M[4] + d2 * M[7]);
+                nzr[k] = (Real)(d0 * M[2] + d1 * M[5] + d2 * M[8]);
+                continue;
+            }
             // framework_energy_grid.cc:227-231 node position
             const double f0 = (double)ixn / nx, f1 = (double)iyn / ny, f2 = (double)izn / nz;
             double c[3];
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc)
                 c[cc] = add_rn(add_rn(mul_rn(f0, M[cc]), mul_rn(f1, M[3 + cc])), mul_rn(f2, M[6 + cc]));
-            if (sizeof(Real) == 4) {
-                nxr[k] = (Real)(c[0] - ox);
-                nyr[k] = (Real)(c[1] - oy);
-                nzr[k] = (Real)(c[2] - oz);
-            } else {
+            {
                 nxr[k] = (Real)c[0];
                 nyr[k] = (Real)c[1];
                 nzr[k] = (Real)c[2];
@@ -362,7 +367,7 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
                     const float dy = a.y - (float)nyr[k];
                     const float dz = a.z - (float)nzr[k];
                     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const float inv = rcp_approx(fmaxf(r2, 1e-4f));
+                    const float inv = __frcp_rn(fmaxf(r2, 1e-4f));
                     const bool in = r2 <= rc2f;
 #pragma unroll
                     for (int g = 0; g < NG; ++g) {
@@ -575,6 +580,7 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
             g.geo.G[3 * i + j] = m[3 * i] * m[3 * j] + m[3 * i + 1] * m[3 * j + 1] + m[3 * i + 2] * m[3 * j + 2];
+    for (int i = 0; i < 9; ++i) g.geo.Gf[i] = (float)g.geo.G[i];
     g.geo.rc = lj.cutoff;
     g.geo.rc2 = lj.cutoff * lj.cutoff;
     // widen the bins until no brick can touch more than MAX_ROWS bin rows

@@ -114,9 +114,11 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_workload():
+def make_workload(reps: int = REPS):
+    """reps=4: the benchmark workload; reps=2: the same cell 2x2x2 (8x fewer
+    nodes and atoms, tables still larger than L2) used for profiler captures."""
     from aleator_gb300 import workloads as W
-    fw = W.triclinic_supercell(reps=REPS)
+    fw = W.triclinic_supercell(reps=reps)
     guests = [fw.guest_species["CO2_C"], fw.guest_species["CO2_O"]]
     return fw, guests
 
@@ -182,11 +184,13 @@ def run_reference(args):
     return 0
 
 
-def _config(fw, guests):
-    return {"workload": "framework energy grid, 4x4x4 triclinic supercell (a=b=c=24 Å, "
-                        "70/80/100 deg) of 422 atoms, CO2 guest site types, 0.2 Å spacing",
+def _config(fw, guests, counts=(457, 437, 437), reps=REPS):
+    return {"workload": f"framework energy grid, {reps}x{reps}x{reps} triclinic supercell "
+                        "(a=b=c=24 Å, 70/80/100 deg) of 422 atoms, CO2 guest site types, "
+                        "0.2 Å spacing" + ("" if reps == REPS else " [profiling case]"),
             "framework_atoms": int(fw.n_atoms), "guest_species": len(guests),
-            "grid_points": "457x437x437", "cutoff_angstrom": CUTOFF, "spacing_angstrom": SPACING,
+            "grid_points": "x".join(str(c) for c in counts), "cutoff_angstrom": CUTOFF,
+            "spacing_angstrom": SPACING,
             "truncation": "shifted", "l2": "256 MB buffer written between timed steps; each "
                                           "step also writes 1.4 GB of tables (> L2)",
             "parallelism": "replica per GPU"}
@@ -200,6 +204,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--workload", default="full", choices=["full", "small"],
+                    help="small: 2x2x2 supercell for profiler captures (not a bench line)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -216,7 +222,7 @@ def main():
         dist.init_process_group("nccl")
     A.load_library()
 
-    fw, guests = make_workload()
+    fw, guests = make_workload(REPS if args.workload == "full" else 2)
     ff = A.LennardJones(fw.eps, fw.sigma, CUTOFF, A.SHIFTED)
     parts = A.ParticleData.from_framework(fw)
     grid = A.FrameworkEnergyGrid(ff, parts, fw.lattice, guests, SPACING, A.FP32)
@@ -295,7 +301,8 @@ def main():
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32 pair terms, fp64 accumulation", "data": "synthetic",
-            "config": _config(fw, guests),
+            "config": _config(fw, guests, grid.point_counts(),
+                              REPS if args.workload == "full" else 2),
             "region_ms": region_s * 1e3,
             "gpu_launches": args.steps,
             "roofline": {

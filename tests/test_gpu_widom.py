@@ -1,13 +1,16 @@
 """Widom insertion on the GPU against the reference's per-trial energies
 (golden, made by the reference's own MonteCarloEngine primitives) and the
 oracle. FP64 per-trial dU within 1e-10 relative (1 K floor); K_H within
-1e-9 relative; FP32 form per-trial within 1e-5 relative (1 K floor) on trials
-that carry Boltzmann weight (dU <= 1e4 K)."""
+1e-9 relative; FP32 form per-trial within 1e-5 relative with a kT floor
+(|d dU| <= 1e-5 * max(kT, |dU|), kT = 298 K) on trials that carry Boltzmann
+weight (dU <= 1e4 K), and its K_H within 1e-5 relative."""
 import numpy as np
 import pytest
 
 import oracle as O
 from conftest import golden, rel_err
+
+KT = 298.0
 
 pytestmark = pytest.mark.gpu
 
@@ -36,7 +39,7 @@ def test_ch4_per_trial_and_henry(lib):
     w32 = A.Widom(ff, p, g["lattice"], guest, 298.0, precision=A.FP32)
     r32, per32 = w32.run(42, 0, len(w["per_trial"]), per_trial=True)
     keep = w["per_trial"] <= 1e4
-    assert rel_err(per32[keep], w["per_trial"][keep]).max() <= 1e-5
+    assert rel_err(per32[keep], w["per_trial"][keep], floor=KT).max() <= 1e-5
     assert abs(r32["henry"] / float(w["kh"]) - 1) <= 1e-5
 
 
@@ -52,7 +55,7 @@ def test_co2_charged_per_trial_and_henry(lib):
     w32 = A.Widom(ff, p, g["lattice"], guest, 298.0, ewald=ew, precision=A.FP32)
     _, per32 = w32.run(42, 0, len(c["per_trial"]), per_trial=True)
     keep = c["per_trial"] <= 1e4
-    assert rel_err(per32[keep], c["per_trial"][keep]).max() <= 1e-5
+    assert rel_err(per32[keep], c["per_trial"][keep], floor=KT).max() <= 1e-5
 
 
 def test_triclinic_charged(lib):
