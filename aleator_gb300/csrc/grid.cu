@@ -36,7 +36,7 @@ constexpr int BX = 16, BY = 8, BZ = 8;   // brick of nodes
 constexpr int THREADS = 256;
 constexpr int NPT = 4;                    // nodes per thread (along z)
 constexpr int TILE = 256;                 // image records per shared-memory stage
-constexpr int MAX_ROWS = 1024;            // bin rows a brick may touch
+constexpr int MAX_ROWS = 512;             // bin rows a brick may touch
 constexpr int MAX_NG = 4;                 // guest species per launch
 constexpr unsigned WAIT_LIMIT = 1u << 20; // bounded mbarrier polls (~0.1 s worst case)
 
@@ -55,6 +55,7 @@ struct GridGeom {
     double binw[3];        // fractional bin width
     double G[9];           // metric tensor a_i . a_j
     float Gf[9];           // the same in FP32 (bin culling)
+    float lof[3], binwf[3];  // lo and binw in FP32 (bin culling)
     double rc, rc2;
     int bricks[3];
     int n_types;           // framework LJ species in the table
@@ -145,6 +146,48 @@ __device__ __forceinline__ float box_min_dist2_lb(const float* G, const float* d
     return lb;
 }
 
+// ---------------------------------------------------------------- double-float
+// Two-float ("double-float") arithmetic for the rare close pairs of the FP32
+// form: the repulsive terms there reach 1e4 K, where FP32's ~1e-6 relative
+// rounding would leave ~1e-2 K of error in a node energy. Error-free
+// transformations (Knuth two-sum, FMA two-product); the _rn intrinsics keep
+// the compiler from contracting or reassociating them.
+struct ff {
+    float hi, lo;
+};
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+__device__ __forceinline__ ff ff_fast(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    ff s = ff_two_sum(a.hi, b.hi);
+    s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+    return ff_fast(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    return ff_fast(p, e);
+}
+__device__ __forceinline__ ff ff_rcp(ff a) {  // one Newton step from the FP32 reciprocal
+    const float y = __frcp_rn(a.hi);
+    const ff ay = ff_mul(a, ff{y, 0.f});
+    const ff r = ff_add(ff{1.f, 0.f}, ff{-ay.hi, -ay.lo});
+    const ff c = ff_mul(ff{y, 0.f}, r);
+    return ff_add(ff{y, 0.f}, c);
+}
+
+struct alignas(16) ParamFF {
+    float sig2_hi, sig2_lo, eps4_hi, eps4_lo, shift_hi, shift_lo, dvdrc, pad;
+};
+
 struct alignas(16) ParamF {
     float sig2, eps4, shift, dvdrc;
 };
@@ -162,13 +205,27 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
                   const uint32_t* __restrict__ bin_start, const PairParams* __restrict__ params,
                   const uint32_t* __restrict__ guests, double* __restrict__ tables,
                   unsigned long long* __restrict__ executed, unsigned* flags) {
-    __shared__ __align__(128) ImageRec raw[2][TILE];
-    __shared__ __align__(16) float4 conv[TILE];
-    __shared__ uint64_t bars[2];
-    __shared__ uint32_t row_begin[MAX_ROWS];
-    __shared__ uint32_t row_off[MAX_ROWS + 1];
-    __shared__ ParamF pf[64 * MAX_NG];
-    __shared__ PairParams pd[64 * MAX_NG];
+    // dynamic shared memory (above the 48 KB static limit), carved by hand;
+    // the layout is mirrored by grid_smem_bytes<Real>() on the host
+    extern __shared__ __align__(128) unsigned char smem[];
+    unsigned char* sp = smem;
+    auto take = [&](size_t bytes) {
+        unsigned char* q = sp;
+        sp += (bytes + 127) & ~(size_t)127;
+        return q;
+    };
+    ImageRec* raw = reinterpret_cast<ImageRec*>(take(2 * TILE * sizeof(ImageRec)));
+    float4* conv = reinterpret_cast<float4*>(take(TILE * sizeof(float4)));
+    float4* convlo = reinterpret_cast<float4*>(take((sizeof(Real) == 4 ? TILE : 1) * sizeof(float4)));
+    float* nlo = reinterpret_cast<float*>(take((sizeof(Real) == 4 ? NPT * 3 * THREADS : 1) * sizeof(float)));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(take(2 * sizeof(uint64_t)));
+    uint32_t* row_begin = reinterpret_cast<uint32_t*>(take(MAX_ROWS * sizeof(uint32_t)));
+    uint32_t* row_off = reinterpret_cast<uint32_t*>(take((MAX_ROWS + 1) * sizeof(uint32_t)));
+    uint32_t* warp_tot = reinterpret_cast<uint32_t*>(take((THREADS / 32) * sizeof(uint32_t)));
+    ParamF* pf = reinterpret_cast<ParamF*>(take(64 * MAX_NG * sizeof(ParamF)));
+    float* rcl2 = reinterpret_cast<float*>(take(64 * sizeof(float)));
+    PairParams* pd = reinterpret_cast<PairParams*>(take(64 * MAX_NG * sizeof(PairParams)));
+    ParamFF* pff = reinterpret_cast<ParamFF*>(pd);  // the FP32 form uses this slot instead
 
     const int tid = threadIdx.x;
     const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
@@ -181,10 +238,25 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
     for (int i = tid; i < geo.n_types * NG; i += THREADS) {
         const int t = i / NG, g = i % NG;
         const PairParams p = params[(size_t)guests[g] * geo.n_types + t];
-        pd[i] = p;
         const double s2 = p.sigma * p.sigma;
         pf[i] = ParamF{(float)s2, (float)(4.0 * p.eps), (float)p.shift, (float)p.dvdrc};
+        if (sizeof(Real) == 8) {
+            pd[i] = p;
+        } else {
+            const double e4 = 4.0 * p.eps;
+            const float s2h = (float)s2, e4h = (float)e4, shh = (float)p.shift;
+            pff[i] = ParamFF{s2h, (float)(s2 - s2h), e4h, (float)(e4 - e4h), shh,
+                             (float)(p.shift - shh), (float)p.dvdrc, 0.f};
+        }
     }
+    __syncthreads();
+    // close-pair radius per framework type: r < sigma for some guest (s^2 > 1)
+    if (sizeof(Real) == 4)
+        for (int t = tid; t < geo.n_types; t += THREADS) {
+            float m = 0.f;
+            for (int g = 0; g < NG; ++g) m = fmaxf(m, pf[t * NG + g].sig2);
+            rcl2[t] = m;
+        }
     if (tid == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
@@ -214,18 +286,23 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
         return;
     }
     const float keep2 = (float)(geo.rc2 * (1.0 + 1e-3) + 1e-2);
+    const float flof[3] = {(float)flo[0], (float)flo[1], (float)flo[2]};
+    const float fhif[3] = {(float)fhi[0], (float)fhi[1], (float)fhi[2]};
     for (int r = tid; r < total_rows; r += THREADS) {
         const int ry = blo[1] + r % rows_y, rz = blo[2] + r / rows_y;
         int first = -1, last = -1;
-        for (int rx = blo[0]; rx <= bhi[0]; ++rx) {
-            float dlo[3], dhi[3];
-            const int bi[3] = {rx, ry, rz};
+        float dlo[3], dhi[3];
+        const int byz[2] = {ry, rz};
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                const float b0 = (float)geo.lo[a] + bi[a] * (float)geo.binw[a];
-                dlo[a] = b0 - (float)fhi[a];
-                dhi[a] = b0 + (float)geo.binw[a] - (float)flo[a];
-            }
+        for (int a = 1; a < 3; ++a) {
+            const float b0 = geo.lof[a] + byz[a - 1] * geo.binwf[a];
+            dlo[a] = b0 - fhif[a];
+            dhi[a] = b0 + geo.binwf[a] - flof[a];
+        }
+        for (int rx = blo[0]; rx <= bhi[0]; ++rx) {
+            const float b0 = geo.lof[0] + rx * geo.binwf[0];
+            dlo[0] = b0 - fhif[0];
+            dhi[0] = b0 + geo.binwf[0] - flof[0];
             if (box_min_dist2_lb(geo.Gf, dlo, dhi) <= keep2) {
                 if (first < 0) first = rx;
                 last = rx;
@@ -241,10 +318,33 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
         row_off[r + 1] = e - s;
     }
     __syncthreads();
+    // exclusive scan of the row counts: each thread sums a run of rows, a
+    // warp scan over those sums, then a scan of the warp totals
     const int nr = total_rows;
-    if (tid == 0) {
-        row_off[0] = 0;
-        for (int r = 0; r < nr; ++r) row_off[r + 1] += row_off[r];
+    {
+        constexpr int PER = (MAX_ROWS + THREADS - 1) / THREADS;
+        const int r0 = tid * PER;
+        uint32_t run = 0;
+        for (int i = 0; i < PER; ++i)
+            if (r0 + i < nr) run += row_off[r0 + i + 1];
+        uint32_t incl = run;
+        const int lane = tid & 31, wid = tid >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) warp_tot[wid] = incl;
+        __syncthreads();
+        uint32_t base = 0;
+        for (int w = 0; w < wid; ++w) base += warp_tot[w];
+        uint32_t acc = base + incl - run;
+        for (int i = 0; i < PER; ++i)
+            if (r0 + i < nr) {
+                const uint32_t c = row_off[r0 + i + 1];
+                row_off[r0 + i + 1] = acc + c;
+                acc += c;
+            }
+        if (tid == 0) row_off[0] = 0;
     }
     __syncthreads();
     const uint32_t n_cand = row_off[nr];
@@ -275,9 +375,15 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
             const int izn = z0 + tz + 2 * k;
             if (sizeof(Real) == 4) {
                 const double d0 = (ixn - cx) / nx, d1 = (iyn - cy) / ny, d2 = (izn - cz) / nz;
-                nxr[k] = (Real)(d0 * M[0] + d1 * M[3] + d2 * M[6]);
-                nyr[k] = (Real)(d0 * M[1] + d1 * M[4] + d2 * M[7]);
-                nzr[k] = (Real)(d0 * M[2] + d1 * M[5] + d2 * M[8]);
+                const double lx = d0 * M[0] + d1 * M[3] + d2 * M[6];
+                const double ly = d0 * M[1] + d1 * M[4] + d2 * M[7];
+                const double lz = d0 * M[2] + d1 * M[5] + d2 * M[8];
+                nxr[k] = (Real)lx;
+                nyr[k] = (Real)ly;
+                nzr[k] = (Real)lz;
+                nlo[(k * 3 + 0) * THREADS + tid] = (float)(lx - (double)nxr[k]);
+                nlo[(k * 3 + 1) * THREADS + tid] = (float)(ly - (double)nyr[k]);
+                nlo[(k * 3 + 2) * THREADS + tid] = (float)(lz - (double)nzr[k]);
                 continue;
             }
             // framework_energy_grid.cc:227-231 node position
@@ -312,7 +418,7 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
         for (; r < nr && row_off[r] < b; ++r) {
             const uint32_t s = max(row_off[r], a), e = min(row_off[r + 1], b);
             if (e > s)
-                bulk_g2s(&raw[buf][s - a], images + row_begin[r] + (s - row_off[r]),
+                bulk_g2s(&raw[buf * TILE + (s - a)], images + row_begin[r] + (s - row_off[r]),
                          (e - s) * (uint32_t)sizeof(ImageRec), &bars[buf]);
         }
     };
@@ -339,9 +445,11 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
         }
         if (sizeof(Real) == 4) {
             for (uint32_t i = tid; i < cnt; i += THREADS) {
-                const ImageRec r = raw[buf][i];
-                conv[i] = make_float4((float)(r.x - ox), (float)(r.y - oy), (float)(r.z - oz),
-                                      __int_as_float((int)r.type));
+                const ImageRec r = raw[buf * TILE + i];
+                const double lx = r.x - ox, ly = r.y - oy, lz = r.z - oz;
+                const float hx = (float)lx, hy = (float)ly, hz = (float)lz;
+                conv[i] = make_float4(hx, hy, hz, __int_as_float((int)r.type));
+                convlo[i] = make_float4((float)(lx - hx), (float)(ly - hy), (float)(lz - hz), 0.f);
             }
             __syncthreads();
             // raw[buf] is free again: prefetch tile t + 2 while computing
@@ -358,6 +466,7 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
             for (uint32_t j = 0; j < cnt; ++j) {
                 const float4 a = conv[j];
                 const int type = __float_as_int(a.w);
+                const float close2 = rcl2[type];
                 ParamF p[NG];
 #pragma unroll
                 for (int g = 0; g < NG; ++g) p[g] = pf[type * NG + g];
@@ -368,7 +477,8 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
                     const float dz = a.z - (float)nzr[k];
                     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                     const float inv = __frcp_rn(fmaxf(r2, 1e-4f));
-                    const bool in = r2 <= rc2f;
+                    const bool close = r2 < close2;
+                    const bool in = (r2 <= rc2f) && !close;
 #pragma unroll
                     for (int g = 0; g < NG; ++g) {
                         const float s2 = p[g].sig2 * inv;
@@ -380,6 +490,29 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
                         }
                         part[g][k] += in ? e : 0.f;
                     }
+                    if (close) {
+                        // rare: r < sigma; double-float term straight into FP64
+                        const float4 al = convlo[j];
+                        const ff ddx = ff_add(ff{a.x, al.x}, ff{-(float)nxr[k], -nlo[(k * 3 + 0) * THREADS + tid]});
+                        const ff ddy = ff_add(ff{a.y, al.y}, ff{-(float)nyr[k], -nlo[(k * 3 + 1) * THREADS + tid]});
+                        const ff ddz = ff_add(ff{a.z, al.z}, ff{-(float)nzr[k], -nlo[(k * 3 + 2) * THREADS + tid]});
+                        ff rr = ff_add(ff_add(ff_mul(ddx, ddx), ff_mul(ddy, ddy)), ff_mul(ddz, ddz));
+                        if (rr.hi < 1e-4f) rr = ff{1e-4f, 0.f};
+                        const ff iv = ff_rcp(rr);
+#pragma unroll
+                        for (int g = 0; g < NG; ++g) {
+                            const ParamFF q = pff[type * NG + g];
+                            const ff s2 = ff_mul(ff{q.sig2_hi, q.sig2_lo}, iv);
+                            const ff s6 = ff_mul(ff_mul(s2, s2), s2);
+                            const ff t = ff_mul(s6, ff_add(s6, ff{-1.f, 0.f}));
+                            ff e = ff_add(ff_mul(ff{q.eps4_hi, q.eps4_lo}, t), ff{-q.shift_hi, -q.shift_lo});
+                            if (TRUNC == ALEA_LINEAR_FORCE_SHIFTED) {
+                                const float r = sqrtf(rr.hi);
+                                e = ff_add(e, ff{-(r - rcf) * q.dvdrc, 0.f});
+                            }
+                            acc[g][k] += (double)e.hi + (double)e.lo;
+                        }
+                    }
                 }
             }
 #pragma unroll
@@ -389,7 +522,7 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
             __syncthreads();  // conv reused by the next tile
         } else {
             for (uint32_t j = 0; j < cnt; ++j) {
-                const ImageRec a = raw[buf][j];
+                const ImageRec a = raw[buf * TILE + j];
                 const PairParams* pp = &pd[a.type * NG];
 #pragma unroll
                 for (int k = 0; k < NPT; ++k) {
@@ -487,20 +620,40 @@ __global__ void grid_interpolate_kernel(Lattice L, int nx, int ny, int nz,
     out[i] = add_rn(mul_rn(c0, sub_rn(1.0, t[2])), mul_rn(c1, t[2]));
 }
 
+template <typename Real>
+constexpr size_t grid_smem_bytes() {
+    auto up = [](size_t b) { return (b + 127) & ~(size_t)127; };
+    return up(2 * TILE * sizeof(ImageRec)) + up(TILE * sizeof(float4)) +
+           up((sizeof(Real) == 4 ? TILE : 1) * sizeof(float4)) +
+           up((sizeof(Real) == 4 ? NPT * 3 * THREADS : 1) * sizeof(float)) + up(2 * sizeof(uint64_t)) +
+           up(MAX_ROWS * sizeof(uint32_t)) + up((MAX_ROWS + 1) * sizeof(uint32_t)) +
+           up((THREADS / 32) * sizeof(uint32_t)) + up(64 * MAX_NG * sizeof(ParamF)) +
+           up(64 * sizeof(float)) + up(64 * MAX_NG * sizeof(PairParams));
+}
+
+template <typename Real, int NG, int TRUNC>
+void launch_one(dim3 grid, cudaStream_t s, const GridGeom& geo, const ImageRec* images,
+                const uint32_t* bins, const PairParams* params, const uint32_t* guests,
+                double* tables, unsigned long long* executed, unsigned* flags) {
+    constexpr size_t bytes = grid_smem_bytes<Real>();
+    // opt in to more than 48 KB of dynamic shared memory (per device, cheap)
+    ALEA_CUDA(cudaFuncSetAttribute(grid_build_kernel<Real, NG, TRUNC>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    grid_build_kernel<Real, NG, TRUNC>
+        <<<grid, THREADS, bytes, s>>>(geo, images, bins, params, guests, tables, executed, flags);
+}
+
 template <typename Real, int NG>
 void launch_build_t(int trunc, dim3 grid, cudaStream_t s, const GridGeom& geo,
                     const ImageRec* images, const uint32_t* bins, const PairParams* params,
                     const uint32_t* guests, double* tables, unsigned long long* executed,
                     unsigned* flags) {
     if (trunc == ALEA_TRUNCATED)
-        grid_build_kernel<Real, NG, ALEA_TRUNCATED>
-            <<<grid, THREADS, 0, s>>>(geo, images, bins, params, guests, tables, executed, flags);
+        launch_one<Real, NG, ALEA_TRUNCATED>(grid, s, geo, images, bins, params, guests, tables, executed, flags);
     else if (trunc == ALEA_SHIFTED)
-        grid_build_kernel<Real, NG, ALEA_SHIFTED>
-            <<<grid, THREADS, 0, s>>>(geo, images, bins, params, guests, tables, executed, flags);
+        launch_one<Real, NG, ALEA_SHIFTED>(grid, s, geo, images, bins, params, guests, tables, executed, flags);
     else
-        grid_build_kernel<Real, NG, ALEA_LINEAR_FORCE_SHIFTED>
-            <<<grid, THREADS, 0, s>>>(geo, images, bins, params, guests, tables, executed, flags);
+        launch_one<Real, NG, ALEA_LINEAR_FORCE_SHIFTED>(grid, s, geo, images, bins, params, guests, tables, executed, flags);
 }
 
 template <typename Real>
@@ -604,6 +757,8 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
         const double span = g.geo.hi[a] - g.geo.lo[a];
         g.geo.nb[a] = std::max(1, (int)std::ceil(span * g.geo.L.perp[a] / bin_width));
         g.geo.binw[a] = span / g.geo.nb[a];
+        g.geo.lof[a] = (float)g.geo.lo[a];
+        g.geo.binwf[a] = (float)g.geo.binw[a];
         g.geo.bricks[a] = (g.geo.n[a] + (a == 0 ? BX : a == 1 ? BY : BZ) - 1) /
                           (a == 0 ? BX : a == 1 ? BY : BZ);
     }

@@ -161,6 +161,7 @@ widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
         for (int s = 0; s < MAXS; ++s) {
             if (s >= ns) break;
             Real lj_acc = 0, es_acc = 0;
+            double lj_close = 0.0;
             const PairParams* row = pp + s * MAXT;
             for (int j = 0; j < cnt; ++j) {
                 const double4 a = tile[j];
@@ -173,8 +174,13 @@ widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
                     if (P.charged && r <= P.rc_ewald) es_acc += a.w * (erfc(P.alpha * r) / r);
                 } else {
                     const float rf = sqrtf((float)r2);
-                    if (r2 <= P.rc2) {
-                        const PairParams& p = row[ttype[j]];
+                    const PairParams& pc = row[ttype[j]];
+                    if (r2 < pc.sigma * pc.sigma) {
+                        // rare close pair (r < sigma): its repulsive term reaches
+                        // 1e4 K, kept in FP64 so its rounding stays below 1e-6 K
+                        lj_close += lj_pair_rt(P.trunc, sqrt(r2), P.rc, pc);
+                    } else if (r2 <= P.rc2) {
+                        const PairParams& p = pc;
                         const float sr = (float)p.sigma / rf;
                         const float sr2 = sr * sr;
                         const float sr6 = sr2 * sr2 * sr2;
@@ -188,7 +194,7 @@ widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
                         es_acc += (float)a.w * (erfcf((float)P.alpha * rf) / rf);
                 }
             }
-            lj_site[s] += (double)lj_acc;
+            lj_site[s] += (double)lj_acc + lj_close;
             es_site[s] += (double)es_acc;
         }
     }

@@ -37,13 +37,15 @@ PASCAL_TO_INTERNAL = 1.0 / (1.380649e-23 * 1.0e30)
 
 def build_oracle(force: bool = False) -> Path:
     """Compile the C restatement (gcc, no FMA contraction, pthreads)."""
-    src = HERE / "aleator_oracle.c"
-    if ORACLE_SO.exists() and not force and ORACLE_SO.stat().st_mtime >= src.stat().st_mtime:
+    srcs = [HERE / "aleator_oracle.c", HERE / "aleator_oracle_gcmc.c"]
+    deps = srcs + [HERE / "aleator_oracle.h", HERE / "aleator_oracle_gcmc.h"]
+    if ORACLE_SO.exists() and not force and all(
+            ORACLE_SO.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return ORACLE_SO
     BUILD.mkdir(exist_ok=True)
     tmp = ORACLE_SO.with_suffix(f".so.{os.getpid()}")
     subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
-                    "-o", str(tmp), str(src), "-lm"], check=True)
+                    "-o", str(tmp), *map(str, srcs), "-lm"], check=True)
     os.replace(tmp, ORACLE_SO)
     return ORACLE_SO
 
@@ -305,6 +307,78 @@ class Oracle:
 
     def pr_fugacity(self, tc, pc, omega, t, p):
         return self.lib.orc_pr_fugacity(tc, pc, omega, t, p)
+
+    def gcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature, fugacity_pa, seed,
+             stream, max_translation=1.5, max_rotation=0.5, draw_order=DRAWS_RIGHT_TO_LEFT):
+        return OracleGcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature,
+                          fugacity_pa, seed, stream, max_translation, max_rotation, draw_order)
+
+
+class OracleGcmc:
+    """Single-species GCMC chain (MonteCarloEngine::run restated in C)."""
+
+    def __init__(self, orc, ff, ewald, m, x, y, z, q, species, guest, temperature, fugacity_pa,
+                 seed, stream, max_translation, max_rotation, draw_order):
+        L = orc.lib
+        self.L = L
+        L.orc_gcmc_new.restype = ctypes.c_void_p
+        L.orc_gcmc_new.argtypes = [ctypes.POINTER(_LJ), ctypes.POINTER(_EwaldParams), _D,
+                                   ctypes.c_uint64, _D, _D, _D, _D, _U32, ctypes.POINTER(_Species),
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]
+        L.orc_gcmc_run.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.orc_gcmc_delete.argtypes = [ctypes.c_void_p]
+        L.orc_gcmc_molecules.restype = ctypes.c_uint64
+        L.orc_gcmc_molecules.argtypes = [ctypes.c_void_p]
+        L.orc_gcmc_particles.restype = ctypes.c_uint64
+        L.orc_gcmc_particles.argtypes = [ctypes.c_void_p, _D, ctypes.c_uint64]
+        L.orc_gcmc_calls.restype = ctypes.c_uint64
+        L.orc_gcmc_calls.argtypes = [ctypes.c_void_p]
+        L.orc_gcmc_ewald_energy.restype = ctypes.c_double
+        L.orc_gcmc_ewald_energy.argtypes = [ctypes.c_void_p]
+        L.orc_gcmc_counters.argtypes = [ctypes.c_void_p, _U64]
+        lj, keep = orc._lj(ff)
+        self._keep = keep
+        ew = _EwaldParams(ewald["alpha"], ewald["rc"], ewald["kmax"]) if ewald else _EwaldParams(0, 0, 0)
+        g = {k: _f64(guest[k]) for k in ("x", "y", "z", "charge")}
+        gs = np.ascontiguousarray(guest["lj_species"], dtype=np.uint32)
+        sp = _Species(len(g["x"]), _dp(g["x"]), _dp(g["y"]), _dp(g["z"]), _u32(gs), _dp(g["charge"]))
+        x, y, z = _f64(x), _f64(y), _f64(z)
+        q = _f64(q if q is not None else np.zeros(len(x)))
+        fs = np.ascontiguousarray(species, dtype=np.uint32)
+        self.h = L.orc_gcmc_new(ctypes.byref(lj), ctypes.byref(ew), _dp(_mat(m)), len(x), _dp(x),
+                                _dp(y), _dp(z), _dp(q), _u32(fs), ctypes.byref(sp), temperature,
+                                fugacity_pa, max_translation, max_rotation, seed, stream,
+                                draw_order)
+
+    def __del__(self):
+        try:
+            self.L.orc_gcmc_delete(self.h)
+        except Exception:
+            pass
+
+    def run(self, steps):
+        self.L.orc_gcmc_run(self.h, steps)
+
+    def molecules(self):
+        return int(self.L.orc_gcmc_molecules(self.h))
+
+    def positions(self):
+        n = self.L.orc_gcmc_particles(self.h, None, 0)
+        out = np.zeros(3 * n)
+        self.L.orc_gcmc_particles(self.h, _dp(out), n)
+        return out.reshape(n, 3)
+
+    def calls(self):
+        return int(self.L.orc_gcmc_calls(self.h))
+
+    def ewald_energy(self):
+        return self.L.orc_gcmc_ewald_energy(self.h)
+
+    def counters(self):
+        out = np.zeros(8, np.uint64)
+        self.L.orc_gcmc_counters(self.h, _u64(out))
+        return out
 
 
 class OracleEwaldState:
@@ -574,6 +648,57 @@ class Reference:
 
     def pr_fugacity(self, tc, pc, omega, t, p):
         return self.lib.ref_pr_fugacity(tc, pc, omega, t, p)
+
+    def gcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature, fugacity_pa, seed,
+             stream, max_translation=1.5, max_rotation=0.5):
+        return ReferenceGcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature,
+                             fugacity_pa, seed, stream, max_translation, max_rotation)
+
+
+class ReferenceGcmc:
+    """MonteCarloEngine (the reference's own class) driven through the shim."""
+
+    def __init__(self, ref, ff, ewald, m, x, y, z, q, species, guest, temperature, fugacity_pa,
+                 seed, stream, max_translation, max_rotation):
+        self.ref = ref
+        eps, sig = _f64(ff["eps"]), _f64(ff["sigma"])
+        x, y, z = _f64(x), _f64(y), _f64(z)
+        q = _f64(q if q is not None else np.zeros(len(x)))
+        sp = np.ascontiguousarray(species, dtype=np.uint32)
+        gx, gy, gz = _f64(guest["x"]), _f64(guest["y"]), _f64(guest["z"])
+        gs = np.ascontiguousarray(guest["lj_species"], dtype=np.uint32)
+        gq = _f64(guest["charge"])
+        alpha = ewald["alpha"] if ewald else 0.0
+        erc = ewald["rc"] if ewald else 0.0
+        kmax = ewald["kmax"] if ewald else 0
+        self.h = ref.lib.ref_gcmc_create(_dp(_mat(m)), len(x), _dp(x), _dp(y), _dp(z), _dp(q),
+                                         _u32(sp), len(eps), _dp(eps), _dp(sig), ff["cutoff"],
+                                         ff.get("truncation", SHIFTED),
+                                         ff.get("mixing", LORENTZ_BERTHELOT), alpha, erc, kmax,
+                                         len(gx), _dp(gx), _dp(gy), _dp(gz), _u32(gs), _dp(gq),
+                                         temperature, fugacity_pa, max_translation, max_rotation,
+                                         seed, stream)
+
+    def __del__(self):
+        try:
+            self.ref.lib.ref_gcmc_destroy(self.h)
+        except Exception:
+            pass
+
+    def run(self, steps):
+        self.ref.lib.ref_gcmc_run(self.h, steps)
+
+    def molecules(self):
+        return int(self.ref.lib.ref_gcmc_molecules(self.h))
+
+    def positions(self):
+        n = self.ref.lib.ref_gcmc_particles(self.h, None, 0)
+        out = np.zeros(3 * n)
+        self.ref.lib.ref_gcmc_particles(self.h, _dp(out), n)
+        return out.reshape(n, 3)
+
+    def ewald_energy(self):
+        return self.ref.lib.ref_gcmc_ewald_energy(self.h)
 
 
 class ReferenceGrid:

@@ -389,3 +389,35 @@ void orc_gcmc_run(orc_gcmc* g, uint64_t steps) {
 }
 
 double orc_gcmc_ewald_energy(const orc_gcmc* g) { return g->charged ? orc_ews_energy(&g->ews) : 0.0; }
+
+/* Heap handles for the Python binding. */
+orc_gcmc* orc_gcmc_new(const orc_lj* lj, const orc_ewald_params* ew, const double m[9], uint64_t n,
+                       const double* x, const double* y, const double* z, const double* q,
+                       const uint32_t* species, const orc_species* guest, double temperature,
+                       double fugacity_pa, double max_translation, double max_rotation,
+                       uint64_t seed, uint64_t stream, int draw_order) {
+    orc_gcmc* g = (orc_gcmc*)malloc(sizeof(orc_gcmc));
+    orc_gcmc_create(g, lj, ew, m, n, x, y, z, q, species, guest, temperature, fugacity_pa,
+                    max_translation, max_rotation, seed, stream, draw_order);
+    return g;
+}
+void orc_gcmc_delete(orc_gcmc* g) {
+    orc_gcmc_free(g);
+    free(g);
+}
+uint64_t orc_gcmc_molecules(const orc_gcmc* g) { return g->n_mol; }
+uint64_t orc_gcmc_particles(const orc_gcmc* g, double* xyz, uint64_t cap) {
+    for (uint64_t i = 0; i < g->n && i < cap; ++i) {
+        xyz[3 * i] = g->x[i];
+        xyz[3 * i + 1] = g->y[i];
+        xyz[3 * i + 2] = g->z[i];
+    }
+    return g->n;
+}
+uint64_t orc_gcmc_calls(const orc_gcmc* g) { return g->call; }
+void orc_gcmc_counters(const orc_gcmc* g, uint64_t* out8) {
+    for (int i = 0; i < 4; ++i) {
+        out8[i] = g->attempted[i];
+        out8[4 + i] = g->accepted[i];
+    }
+}

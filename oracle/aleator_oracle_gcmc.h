@@ -44,6 +44,16 @@ int orc_gcmc_create(orc_gcmc* g, const orc_lj* lj, const orc_ewald_params* ew, c
 void orc_gcmc_run(orc_gcmc* g, uint64_t steps);
 double orc_gcmc_ewald_energy(const orc_gcmc* g);
 void orc_gcmc_free(orc_gcmc* g);
+orc_gcmc* orc_gcmc_new(const orc_lj* lj, const orc_ewald_params* ew, const double m[9], uint64_t n,
+                       const double* x, const double* y, const double* z, const double* q,
+                       const uint32_t* species, const orc_species* guest, double temperature,
+                       double fugacity_pa, double max_translation, double max_rotation,
+                       uint64_t seed, uint64_t stream, int draw_order);
+void orc_gcmc_delete(orc_gcmc* g);
+uint64_t orc_gcmc_molecules(const orc_gcmc* g);
+uint64_t orc_gcmc_particles(const orc_gcmc* g, double* xyz, uint64_t cap);
+uint64_t orc_gcmc_calls(const orc_gcmc* g);
+void orc_gcmc_counters(const orc_gcmc* g, uint64_t* out8);
 
 #ifdef __cplusplus
 }
