@@ -21,6 +21,7 @@ from ._lib import (  # noqa: F401
     Ewald,
     EwaldIncrementalState,
     FrameworkEnergyGrid,
+    GcmcChains,
     LennardJones,
     ParticleData,
     Widom,

@@ -62,6 +62,15 @@ class _GridStats(ctypes.Structure):
                 ("bricks", ctypes.c_uint64), ("last_kernel_ms", ctypes.c_float)]
 
 
+class _ChainInfo(ctypes.Structure):
+    _fields_ = [("molecules", ctypes.c_uint64), ("guest_sites", ctypes.c_uint64),
+                ("call_index", ctypes.c_uint64), ("steps", ctypes.c_uint64),
+                ("resyncs", ctypes.c_uint64), ("attempted", ctypes.c_uint64 * 4),
+                ("accepted", ctypes.c_uint64 * 4), ("sum_molecules", ctypes.c_double),
+                ("sum_molecules_sq", ctypes.c_double), ("last_du", ctypes.c_double),
+                ("last_kernel_ms", ctypes.c_float)]
+
+
 class _WidomResult(ctypes.Structure):
     _fields_ = [("henry", ctypes.c_double), ("log_mean_weight", ctypes.c_double),
                 ("rel_std_error", ctypes.c_double), ("n_trials", ctypes.c_uint64),
@@ -140,6 +149,16 @@ _SIGNATURES = {
                                         ctypes.c_uint64, ctypes.c_int32,
                                         ctypes.POINTER(_WidomResult), _D]),
     "alea_widom_destroy": (ctypes.c_int32, [_VP]),
+    "alea_gcmc_create": (ctypes.c_int32, [ctypes.POINTER(_LJ), ctypes.POINTER(_Ewald),
+                                          ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
+                                          ctypes.POINTER(_Species), ctypes.c_double, _D, _U64, _U64,
+                                          ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_int32, ctypes.c_uint32, ctypes.POINTER(_VP)]),
+    "alea_gcmc_run": (ctypes.c_int32, [_VP, ctypes.c_uint64, _VP]),
+    "alea_gcmc_chain_info_get": (ctypes.c_int32, [_VP, ctypes.c_uint32, ctypes.POINTER(_ChainInfo)]),
+    "alea_gcmc_particles": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D, ctypes.c_uint64, _U64]),
+    "alea_gcmc_ewald_energy": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D]),
+    "alea_gcmc_destroy": (ctypes.c_int32, [_VP]),
     "alea_insertion_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                                ctypes.c_double, ctypes.c_double]),
     "alea_deletion_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
@@ -620,6 +639,74 @@ class Widom:
 
     def henry_coefficient(self, seed, stream, n_trials, draw_order=ALEA_DRAWS_RIGHT_TO_LEFT):
         return self.run(seed, stream, n_trials, draw_order=draw_order)["henry"]
+
+
+class GcmcChains:
+    """MonteCarloEngine (monte_carlo_engine.hpp:76-83, single species) for many
+    independent chains advanced together on the GPU."""
+
+    def __init__(self, force_field: LennardJones, framework: ParticleData, lattice, guest: dict,
+                 temperature: float, fugacities_pa, seeds, streams, ewald: Ewald | None = None,
+                 max_translation=1.5, max_rotation=0.5, draw_order=ALEA_DRAWS_RIGHT_TO_LEFT,
+                 max_molecules=256):
+        self._lib = library()
+        self._h = _VP()
+        self._g = {k: (_f64(guest[k]) if k != "lj_species" else
+                       np.ascontiguousarray(guest[k], dtype=np.uint32))
+                   for k in ("x", "y", "z", "lj_species", "charge")}
+        sp = _Species(len(self._g["x"]), _dp(self._g["x"]), _dp(self._g["y"]), _dp(self._g["z"]),
+                      _u32p(self._g["lj_species"]), _dp(self._g["charge"]))
+        f = _f64(np.atleast_1d(fugacities_pa))
+        se = np.ascontiguousarray(np.atleast_1d(seeds), dtype=np.uint64)
+        st = np.ascontiguousarray(np.atleast_1d(streams), dtype=np.uint64)
+        self.n_chains = len(f)
+        if len(se) != self.n_chains or len(st) != self.n_chains:
+            raise ValueError("one fugacity, seed and stream per chain")
+        lj = force_field.c()
+        p = framework.c()
+        lat = _lattice(lattice)
+        e = ewald.c() if ewald is not None else None
+        _check(self._lib.alea_gcmc_create(ctypes.byref(lj), ctypes.byref(e) if e else None,
+                                          ctypes.byref(p), ctypes.byref(lat), ctypes.byref(sp),
+                                          float(temperature), _dp(f), _u64p(se), _u64p(st),
+                                          self.n_chains, float(max_translation),
+                                          float(max_rotation), int(draw_order), int(max_molecules),
+                                          ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                self._lib.alea_gcmc_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def run(self, steps, stream=0):
+        _check(self._lib.alea_gcmc_run(self._h, int(steps), stream))
+
+    def info(self, chain=0):
+        s = _ChainInfo()
+        _check(self._lib.alea_gcmc_chain_info_get(self._h, chain, ctypes.byref(s)))
+        d = {f: getattr(s, f) for f, _ in s._fields_}
+        d["attempted"] = list(s.attempted)
+        d["accepted"] = list(s.accepted)
+        return d
+
+    def molecules(self, chain=0):
+        return int(self.info(chain)["molecules"])
+
+    def positions(self, chain=0):
+        n = ctypes.c_uint64()
+        _check(self._lib.alea_gcmc_particles(self._h, chain, None, 0, ctypes.byref(n)))
+        out = np.zeros(3 * n.value)
+        _check(self._lib.alea_gcmc_particles(self._h, chain, _dp(out), n.value, ctypes.byref(n)))
+        return out.reshape(-1, 3)
+
+    def ewald_energy(self, chain=0):
+        v = ctypes.c_double()
+        _check(self._lib.alea_gcmc_ewald_energy(self._h, chain, ctypes.byref(v)))
+        return v.value
 
 
 def peng_robinson_fugacity(tc, pc, omega, t, p):

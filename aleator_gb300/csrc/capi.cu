@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "gcmc.cuh"
 #include "grid.cuh"
 
 struct alea_grid {
@@ -17,6 +18,9 @@ struct alea_ewald_state {
 };
 struct alea_widom {
     alea::WidomImpl* impl;
+};
+struct alea_gcmc {
+    alea::GcmcImpl* impl;
 };
 
 namespace {
@@ -54,6 +58,10 @@ alea_particles particles_or_empty(const alea_particles* p) {
 }
 
 }  // namespace
+
+namespace alea {
+void record_last_error(const char* message) { g_last_error = message ? message : ""; }
+}  // namespace alea
 
 extern "C" {
 
@@ -567,6 +575,93 @@ alea_status alea_widom_destroy(alea_widom* w) {
         if (!w) return;
         alea::widom_destroy(w->impl);
         delete w;
+    });
+}
+
+// ---------------------------------------------------------------- GCMC chains
+alea_status alea_gcmc_create(const alea_lennard_jones* lj, const alea_ewald* ewald,
+                             const alea_particles* framework, const alea_lattice* lattice,
+                             const alea_molecule_species* species, double temperature,
+                             const double* fugacity_pa, const uint64_t* seeds,
+                             const uint64_t* streams, uint32_t n_chains, double max_translation,
+                             double max_rotation, int32_t draw_order, uint32_t max_molecules,
+                             alea_gcmc** out) {
+    return guarded([&] {
+        need(lj, "lj");
+        need(lattice, "lattice");
+        need(species, "species");
+        need(fugacity_pa, "fugacity_pa");
+        need(seeds, "seeds");
+        need(streams, "streams");
+        need(out, "out");
+        *out = nullptr;
+        auto* g = new alea_gcmc{nullptr};
+        try {
+            g->impl = alea::gcmc_create(*lj, ewald, particles_or_empty(framework), *lattice, *species,
+                                        temperature, fugacity_pa, seeds, streams, n_chains,
+                                        max_translation, max_rotation, draw_order, max_molecules);
+        } catch (...) {
+            delete g;
+            throw;
+        }
+        *out = g;
+    });
+}
+
+alea_status alea_gcmc_run(alea_gcmc* g, uint64_t steps, void* cuda_stream) {
+    return guarded([&] {
+        need(g, "gcmc");
+        alea::gcmc_run(g->impl, steps, (cudaStream_t)cuda_stream);
+    });
+}
+
+alea_status alea_gcmc_chain_info_get(const alea_gcmc* g, uint32_t chain, alea_gcmc_chain_info* out) {
+    return guarded([&] {
+        need(g, "gcmc");
+        need(out, "out");
+        const unsigned n = alea::gcmc_chains(g->impl);
+        if (chain >= n) throw alea::Error(ALEA_ERR_OUT_OF_RANGE, "GCMC: chain index");
+        std::vector<alea::ChainState> st(n);
+        alea::gcmc_states(g->impl, st.data());
+        const alea::ChainState& c = st[chain];
+        out->molecules = c.n_mol;
+        out->guest_sites = c.n_guest;
+        out->call_index = c.call;
+        out->steps = c.steps;
+        out->resyncs = c.resyncs;
+        for (int i = 0; i < 4; ++i) {
+            out->attempted[i] = c.attempted[i];
+            out->accepted[i] = c.accepted[i];
+        }
+        out->sum_molecules = c.sum_n;
+        out->sum_molecules_sq = c.sum_n2;
+        out->last_du = c.last_du;
+        out->last_kernel_ms = alea::gcmc_last_ms(g->impl);
+    });
+}
+
+alea_status alea_gcmc_particles(const alea_gcmc* g, uint32_t chain, double* xyz, uint64_t cap,
+                                uint64_t* n_out) {
+    return guarded([&] {
+        need(g, "gcmc");
+        const uint64_t n = alea::gcmc_particles(g->impl, chain, xyz, cap);
+        if (n_out) *n_out = n;
+    });
+}
+
+alea_status alea_gcmc_ewald_energy(const alea_gcmc* g, uint32_t chain, double* out) {
+    return guarded([&] {
+        need(g, "gcmc");
+        need(out, "out");
+        *out = alea::gcmc_ewald_energy(g->impl, chain);
+    });
+}
+
+alea_status alea_gcmc_destroy(alea_gcmc* g) {
+    return guarded([&] {
+        if (!g) return;
+        alea::gcmc_destroy(g->impl);
+        delete g;
     });
 }
 

@@ -241,6 +241,10 @@ struct DevBuf {
 // Checks and clears a device error-flag word after a kernel sequence.
 void check_device_flags(unsigned* d_flags, cudaStream_t s, const char* what);
 
+// Records the calling thread's last error message (capi.cu) for entry points
+// that do not go through the C-ABI wrapper.
+void record_last_error(const char* message);
+
 // Ensures a CUDA device exists (throws ALEA_ERR_NO_DEVICE otherwise).
 void require_device();
 

@@ -1,0 +1,835 @@
+// Single-species GCMC chains on sm_103a, one CTA per chain, every move of a
+// launch in one persistent loop.
+//
+// Reference: MonteCarloEngine (engines/monte_carlo/monte_carlo_engine.cc):
+//   run                      :405-439   25 % each translate / rotate / insert / delete
+//   attemptTranslation       :441-484
+//   attemptRotation          :486-554   (rotateAboutAxis :40-44)
+//   attemptInsertion         :556-619   (randomUnitQuaternion :56-63, rotateByQuaternion :68-72)
+//   attemptDeletion          :621-671   (removeMolecule :814-823, removeParticleIndices :825-848)
+//   moleculeDispersionEnergy :341-374   (direct scan form; the guest-guest cell-list
+//                                        candidates are a superset visited in ascending order)
+//   moleculeElectrostaticRealSpaceEnergy :299-314
+//   maybeResyncEwald         :380-403   (every 100 accepted moves)
+// and EwaldIncrementalState's propose / commit / resync
+// (forcefield/electrostatics/ewald_incremental_state.cc:95-247).
+//
+// Per move: thread 0 draws from the chain's Philox stream in the reference's
+// order and builds the trial sites; the block sums the LJ and real-space
+// Ewald energies of the old and new sites against every particle in one pass
+// (FP64); the reciprocal delta runs one thread per k-term, each site's phase
+// exp(i k.r) assembled from per-site tables of exp(i n theta_a) in shared
+// memory (two complex products per term and site instead of an FP64 sincos),
+// and the per-term delta is kept for the commit; thread 0 applies the
+// acceptance rule and the bookkeeping (molecule erase, swap-with-last
+// removal). Every 100 accepted moves S(k) is rebuilt as the framework's S(k)
+// plus the guest sites in index order, the reference's summation order.
+//
+// Layout in HBM: read-only framework (x, y, z, q as double4 + LJ type), mixed
+// LJ table, k-term table (k, weight, index triple, framework S(k)); per chain:
+// guest sites SoA (x, y, z, q, type), molecule -> particle index table, the
+// committed S(k), a per-term delta scratch, and a ChainState record.
+
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "gcmc.cuh"
+#include "grid.cuh"
+
+namespace alea {
+
+namespace {
+
+constexpr int GT = 256;     // threads per chain
+constexpr int MAXS = 8;     // sites per molecule
+constexpr int KMAXC = 20;   // largest kMax the per-site phase tables hold
+constexpr int RSTRIDE = 4 * MAXS + 1;
+
+struct GcmcConst {
+    Lattice L;
+    int ns;
+    double sx[MAXS], sy[MAXS], sz[MAXS], sq[MAXS];
+    uint32_t slj[MAXS];
+    uint32_t n_species;
+    double rc, rc2;
+    int trunc;
+    double temperature;
+    double max_trans, max_rot;
+    int draw_order;
+    uint64_t n_fw;
+    uint32_t max_mol, max_sites;
+    double volume;
+    int charged;
+    double alpha, rc_ew, rc_ew2;
+    int kmax;
+    uint64_t nk;
+    double b[9];
+    double self_pref, rec_pref;
+    double fw_q2;
+};
+
+struct GcmcPtrs {
+    const double4* fw;
+    const uint32_t* fw_type;
+    const PairParams* table;
+    const double* k;
+    const double* w;
+    const int* nidx;
+    const double* sfw_re;
+    const double* sfw_im;
+    ChainState* st;
+    double *gx, *gy, *gz, *gq;
+    uint32_t* gt;
+    uint32_t* mol;
+    double *sre, *sim, *dre, *dim;
+    unsigned* flags;
+};
+
+struct StepShared {
+    int move, valid, accept, do_resync;
+    uint32_t mi;
+    int n_old, n_new;
+    uint64_t ng;        // guest sites while the move is evaluated
+    uint64_t ng_after;  // guest sites after the bookkeeping
+    double op[MAXS][3];
+    double np_[MAXS][3];
+    uint32_t ex[MAXS];
+    double e_lj[2 * MAXS], e_el[2 * MAXS];
+    double rec_sum, dself, dexcl;
+};
+
+__device__ __forceinline__ double u01(ChainState& c) {
+    return philox_uniform(c.seed, c.stream, c.call++);
+}
+
+// Fixed-order block sum of n values per thread (n <= 4*MAXS).
+__device__ void block_sum_n(double* v, int n, double* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = 0; i < n; ++i) {
+        double x = v[i];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[wid * RSTRIDE + i] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < n) {
+        double s = 0.0;
+        for (int w = 0; w < GT / 32; ++w) s += red[w * RSTRIDE + threadIdx.x];
+        red[(GT / 32) * RSTRIDE + threadIdx.x] = s;
+    }
+    __syncthreads();
+    for (int i = 0; i < n; ++i) v[i] = red[(GT / 32) * RSTRIDE + i];
+    __syncthreads();
+}
+
+__device__ __forceinline__ double erf_over_r_d(double r, double alpha) {
+    if (r < 1e-8) return 2.0 * alpha / sqrt(kPi);
+    return erf(alpha * r) / r;
+}
+
+// pairExclusionSum (ewald_incremental_state.cc:32-43)
+__device__ double exclusion_sum(const Lattice& L, const double (*p)[3], const double* q, int n,
+                                double alpha) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j) {
+            double dx, dy, dz;
+            min_image(L, p[j][0] - p[i][0], p[j][1] - p[i][1], p[j][2] - p[i][2], dx, dy, dz);
+            s += q[i] * q[j] * erf_over_r_d(sqrt(dx * dx + dy * dy + dz * dz), alpha);
+        }
+    return s;
+}
+
+// rotateAboutAxis (monte_carlo_engine.cc:40-44)
+__device__ void rotate_about_axis(const double* v, const double* a, double th, double* o) {
+    const double c = cos(th), s = sin(th);
+    const double cr[3] = {sub_rn(mul_rn(a[1], v[2]), mul_rn(a[2], v[1])),
+                          sub_rn(mul_rn(a[2], v[0]), mul_rn(a[0], v[2])),
+                          sub_rn(mul_rn(a[0], v[1]), mul_rn(a[1], v[0]))};
+    const double ad = mul_rn(add_rn(add_rn(mul_rn(a[0], v[0]), mul_rn(a[1], v[1])), mul_rn(a[2], v[2])),
+                             sub_rn(1.0, c));
+    for (int i = 0; i < 3; ++i) o[i] = add_rn(add_rn(mul_rn(v[i], c), mul_rn(cr[i], s)), mul_rn(a[i], ad));
+}
+
+// Thread 0: the draws and trial geometry of one move.
+__device__ void plan_move(const GcmcConst& C, ChainState& c, const double* gx, const double* gy,
+                          const double* gz, const uint32_t* mol, StepShared& S) {
+    const double pick = u01(c);
+    S.move = pick < 0.25 ? 0 : pick < 0.5 ? 1 : pick < 0.75 ? 2 : 3;
+    S.valid = 1;
+    S.accept = 0;
+    S.do_resync = 0;
+    S.n_old = S.n_new = 0;
+    S.ng = c.n_guest;
+    const int ns = C.ns;
+    if (S.move == 2) {  // monte_carlo_engine.cc:568-590
+        double u[3];
+        u[0] = u01(c);
+        u[1] = u01(c);
+        u[2] = u01(c);
+        if (C.draw_order == ALEA_DRAWS_RIGHT_TO_LEFT) {
+            const double t = u[0];
+            u[0] = u[2];
+            u[2] = t;
+        }
+        const double* M = C.L.m;
+        double ref[3];
+        for (int k = 0; k < 3; ++k)
+            ref[k] = add_rn(add_rn(mul_rn(M[k], u[0]), mul_rn(M[3 + k], u[1])), mul_rn(M[6 + k], u[2]));
+        double q[4] = {1.0, 0.0, 0.0, 0.0};
+        if (ns > 1) {
+            double v[3];
+            v[0] = u01(c);
+            v[1] = u01(c);
+            v[2] = u01(c);
+            if (C.draw_order == ALEA_DRAWS_RIGHT_TO_LEFT) {
+                const double t = v[0];
+                v[0] = v[2];
+                v[2] = t;
+            }
+            const double r1 = __dsqrt_rn(sub_rn(1.0, v[0])), r2 = __dsqrt_rn(v[0]);
+            const double t1 = mul_rn(2.0 * kPi, v[1]), t2 = mul_rn(2.0 * kPi, v[2]);
+            q[0] = mul_rn(r2, cos(t2));
+            q[1] = mul_rn(r1, sin(t1));
+            q[2] = mul_rn(r1, cos(t1));
+            q[3] = mul_rn(r2, sin(t2));
+        }
+        for (int s = 0; s < ns; ++s) {
+            const double loc[3] = {C.sx[s], C.sy[s], C.sz[s]};
+            double rot[3] = {loc[0], loc[1], loc[2]};
+            if (ns > 1) {
+                const double qv[3] = {q[1], q[2], q[3]};
+                const double cr[3] = {sub_rn(mul_rn(qv[1], loc[2]), mul_rn(qv[2], loc[1])),
+                                      sub_rn(mul_rn(qv[2], loc[0]), mul_rn(qv[0], loc[2])),
+                                      sub_rn(mul_rn(qv[0], loc[1]), mul_rn(qv[1], loc[0]))};
+                const double t[3] = {mul_rn(cr[0], 2.0), mul_rn(cr[1], 2.0), mul_rn(cr[2], 2.0)};
+                const double c2[3] = {sub_rn(mul_rn(qv[1], t[2]), mul_rn(qv[2], t[1])),
+                                      sub_rn(mul_rn(qv[2], t[0]), mul_rn(qv[0], t[2])),
+                                      sub_rn(mul_rn(qv[0], t[1]), mul_rn(qv[1], t[0]))};
+                for (int i = 0; i < 3; ++i) rot[i] = add_rn(add_rn(loc[i], mul_rn(t[i], q[0])), c2[i]);
+            }
+            for (int i = 0; i < 3; ++i) S.np_[s][i] = add_rn(ref[i], rot[i]);
+        }
+        S.n_new = ns;
+        return;
+    }
+    // nothing to act on, or a single-site rotation: no further draws
+    if (c.n_mol == 0 || (S.move == 1 && ns < 2)) {
+        S.valid = 0;
+        return;
+    }
+    const uint32_t mi = (uint32_t)(u01(c) * (double)c.n_mol);
+    S.mi = mi;
+    for (int s = 0; s < ns; ++s) {
+        const uint32_t gi = mol[(size_t)mi * ns + s];
+        S.ex[s] = gi;
+        const uint32_t slot = gi - (uint32_t)C.n_fw;
+        S.op[s][0] = gx[slot];
+        S.op[s][1] = gy[slot];
+        S.op[s][2] = gz[slot];
+    }
+    S.n_old = ns;
+    if (S.move == 3) return;
+    if (S.move == 0) {  // braced initializer: left-to-right draws (:454-456)
+        double d[3];
+        for (int i = 0; i < 3; ++i) d[i] = mul_rn(sub_rn(mul_rn(2.0, u01(c)), 1.0), C.max_trans);
+        for (int s = 0; s < ns; ++s)
+            for (int i = 0; i < 3; ++i) S.np_[s][i] = add_rn(S.op[s][i], d[i]);
+    } else {  // :512-532
+        double cen[3] = {0.0, 0.0, 0.0};
+        for (int s = 0; s < ns; ++s)
+            for (int i = 0; i < 3; ++i) cen[i] = add_rn(cen[i], S.op[s][i]);
+        const double inv = 1.0 / (double)ns;
+        for (int i = 0; i < 3; ++i) cen[i] = mul_rn(cen[i], inv);
+        const double ct = sub_rn(mul_rn(2.0, u01(c)), 1.0);
+        const double st = __dsqrt_rn(fmax(0.0, sub_rn(1.0, mul_rn(ct, ct))));
+        const double phi = mul_rn(2.0 * kPi, u01(c));
+        const double axis[3] = {mul_rn(st, cos(phi)), mul_rn(st, sin(phi)), ct};
+        const double ang = mul_rn(sub_rn(mul_rn(2.0, u01(c)), 1.0), C.max_rot);
+        for (int s = 0; s < ns; ++s) {
+            const double v[3] = {sub_rn(S.op[s][0], cen[0]), sub_rn(S.op[s][1], cen[1]),
+                                 sub_rn(S.op[s][2], cen[2])};
+            double r[3];
+            rotate_about_axis(v, axis, ang, r);
+            for (int i = 0; i < 3; ++i) S.np_[s][i] = add_rn(cen[i], r[i]);
+        }
+    }
+    S.n_new = ns;
+}
+
+template <int NS>
+__global__ void __launch_bounds__(GT)
+gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
+    __shared__ StepShared S;
+    __shared__ double red[(GT / 32 + 1) * RSTRIDE];
+    __shared__ double2 etab[2 * NS][3][2 * KMAXC + 1];
+    __shared__ double eq[2 * NS];
+    __shared__ PairParams srow[NS][64];
+
+    const int chain = blockIdx.x;
+    ChainState c = P.st[chain];  // thread 0's copy is the authoritative one
+    const size_t so = (size_t)chain * C.max_sites;
+    double* gx = P.gx + so;
+    double* gy = P.gy + so;
+    double* gz = P.gz + so;
+    double* gq = P.gq + so;
+    uint32_t* gt = P.gt + so;
+    uint32_t* mol = P.mol + (size_t)chain * C.max_mol * NS;
+    double* sre = P.sre + (size_t)chain * C.nk;
+    double* sim = P.sim + (size_t)chain * C.nk;
+    double* dre = P.dre + (size_t)chain * C.nk;
+    double* dim = P.dim + (size_t)chain * C.nk;
+    const int K = C.kmax;
+    for (int i = threadIdx.x; i < NS * (int)C.n_species; i += GT)
+        srow[i / C.n_species][i % C.n_species] =
+            P.table[(size_t)C.slj[i / C.n_species] * C.n_species + i % C.n_species];
+    __syncthreads();
+
+    for (uint64_t step = 0; step < steps; ++step) {
+        if (threadIdx.x == 0) {
+            if (c.err == 0) {
+                plan_move(C, c, gx, gy, gz, mol, S);
+            } else {
+                S.valid = 0;
+            }
+        }
+        __syncthreads();
+        if (S.valid) {
+            const int n_old = S.n_old, n_new = S.n_new;
+            const uint64_t n_all = C.n_fw + S.ng;
+            // ---- LJ and real-space sums of old sites (e < NS) and new sites (e >= NS)
+            double acc[4 * NS];
+#pragma unroll
+            for (int e = 0; e < 4 * NS; ++e) acc[e] = 0.0;
+            for (uint64_t j = threadIdx.x; j < n_all; j += GT) {
+                bool skip = false;
+                if (n_old)
+#pragma unroll
+                    for (int x = 0; x < NS; ++x) skip |= (S.ex[x] == (uint32_t)j);
+                if (skip) continue;
+                double4 a;
+                uint32_t ta;
+                if (j < C.n_fw) {
+                    a = P.fw[j];
+                    ta = P.fw_type[j];
+                } else {
+                    const uint64_t g = j - C.n_fw;
+                    a = make_double4(gx[g], gy[g], gz[g], gq[g]);
+                    ta = gt[g];
+                }
+#pragma unroll
+                for (int e = 0; e < 2 * NS; ++e) {
+                    const bool is_old = e < NS;
+                    if (is_old ? (n_old == 0) : (n_new == 0)) continue;
+                    const int s = is_old ? e : e - NS;
+                    const double* p = is_old ? S.op[s] : S.np_[s];
+                    double dx, dy, dz;
+                    min_image(C.L, a.x - p[0], a.y - p[1], a.z - p[2], dx, dy, dz);
+                    const double r2 = dx * dx + dy * dy + dz * dz;
+                    const bool lj_in = r2 <= C.rc2 * (1.0 + 1e-12);
+                    const bool el_in = C.charged && r2 <= C.rc_ew2 * (1.0 + 1e-12);
+                    if (!lj_in && !el_in) continue;
+                    const double r = sqrt(r2);
+                    if (lj_in) acc[2 * e] += lj_pair_rt(C.trunc, r, C.rc, srow[s][ta]);
+                    if (el_in && r <= C.rc_ew) acc[2 * e + 1] += a.w * (erfc(C.alpha * r) / r);
+                }
+            }
+            block_sum_n(acc, 4 * NS, red);
+            if (threadIdx.x == 0)
+#pragma unroll
+                for (int e = 0; e < 2 * NS; ++e) {
+                    const int s = e < NS ? e : e - NS;
+                    S.e_lj[e] = acc[2 * e];
+                    S.e_el[e] = (C.sq[s] * acc[2 * e + 1]) * kCoulomb;
+                }
+
+            // ---- reciprocal delta: removed = old sites, added = new sites
+            if (C.charged) {
+                const int tw = 2 * K + 1;
+                for (int i = threadIdx.x; i < 2 * NS * 3 * tw; i += GT) {
+                    const int e = i / (3 * tw), a = (i / tw) % 3, n = i % tw - K;
+                    const bool is_old = e < NS;
+                    if (is_old ? (n_old == 0) : (n_new == 0)) continue;
+                    const int s = is_old ? e : e - NS;
+                    const double* p = is_old ? S.op[s] : S.np_[s];
+                    const double th = C.b[3 * a] * p[0] + C.b[3 * a + 1] * p[1] + C.b[3 * a + 2] * p[2];
+                    double sn, cs;
+                    sincos((double)n * th, &sn, &cs);
+                    etab[e][a][n + K] = make_double2(cs, sn);
+                }
+                if (threadIdx.x < 2 * NS) eq[threadIdx.x] = C.sq[threadIdx.x % NS];
+                __syncthreads();
+                double racc = 0.0;
+                for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
+                    const int n0 = P.nidx[3 * t] + K, n1 = P.nidx[3 * t + 1] + K, n2 = P.nidx[3 * t + 2] + K;
+                    double re = 0.0, im = 0.0;
+                    if (n_new)  // added first (ewald_incremental_state.cc:107-111)
+#pragma unroll
+                        for (int s = 0; s < NS; ++s) {
+                            const double2 A = etab[NS + s][0][n0], B = etab[NS + s][1][n1], Cc = etab[NS + s][2][n2];
+                            const double abr = A.x * B.x - A.y * B.y, abi = A.x * B.y + A.y * B.x;
+                            re += eq[NS + s] * (abr * Cc.x - abi * Cc.y);
+                            im += eq[NS + s] * (abr * Cc.y + abi * Cc.x);
+                        }
+                    if (n_old)  // then removed (:112-116)
+#pragma unroll
+                        for (int s = 0; s < NS; ++s) {
+                            const double2 A = etab[s][0][n0], B = etab[s][1][n1], Cc = etab[s][2][n2];
+                            const double abr = A.x * B.x - A.y * B.y, abi = A.x * B.y + A.y * B.x;
+                            re -= eq[s] * (abr * Cc.x - abi * Cc.y);
+                            im -= eq[s] * (abr * Cc.y + abi * Cc.x);
+                        }
+                    const double o_re = sre[t], o_im = sim[t];
+                    const double n_re = o_re + re, n_im = o_im + im;
+                    racc += P.w[t] * ((n_re * n_re + n_im * n_im) - (o_re * o_re + o_im * o_im));
+                    dre[t] = re;
+                    dim[t] = im;
+                }
+                double v[1] = {racc};
+                block_sum_n(v, 1, red);
+                if (threadIdx.x == 0) {
+                    S.rec_sum = C.rec_pref * v[0];
+                    double q2a = 0.0, q2r = 0.0;
+                    for (int s = 0; s < n_new; ++s) q2a += C.sq[s] * C.sq[s];
+                    for (int s = 0; s < n_old; ++s) q2r += C.sq[s] * C.sq[s];
+                    S.dself = C.self_pref * (q2a - q2r);
+                    S.dexcl = -kCoulomb * (exclusion_sum(C.L, S.np_, C.sq, n_new, C.alpha) -
+                                           exclusion_sum(C.L, S.op, C.sq, n_old, C.alpha));
+                }
+            }
+
+            // ---- acceptance (gcmc_acceptance.hpp:28-101)
+            if (threadIdx.x == 0) {
+                double u_old = 0.0, u_new = 0.0, e_old = 0.0, e_new = 0.0;
+                for (int s = 0; s < n_old; ++s) {
+                    u_old += S.e_lj[s];
+                    e_old += S.e_el[s];
+                }
+                for (int s = 0; s < n_new; ++s) {
+                    u_new += S.e_lj[NS + s];
+                    e_new += S.e_el[NS + s];
+                }
+                const double rec = C.charged ? (S.rec_sum + S.dself) + S.dexcl : 0.0;
+                const double T = C.temperature;
+                double du, ratio;
+                if (S.move <= 1) {
+                    du = (u_new - u_old) + (e_new - e_old) + rec;
+                    ratio = exp(-du / T);
+                } else if (S.move == 2) {
+                    du = u_new + e_new + rec;
+                    ratio = (c.fugacity * C.volume / T) / (double)(c.n_mol + 1) * exp(-du / T);
+                } else {
+                    du = -(u_old + e_old) + rec;
+                    ratio = (double)c.n_mol / (c.fugacity * C.volume / T) * exp(-du / T);
+                }
+                c.attempted[S.move]++;
+                const double prob = ratio < 1.0 ? ratio : 1.0;
+                S.accept = u01(c) < prob ? 1 : 0;
+                if (S.accept && S.move == 2 && c.n_mol + 1 > C.max_mol) {
+                    c.err |= DEV_ERR_CAPACITY;  // the chain stops; the host reports it
+                    S.accept = 0;
+                }
+                c.last_du = du;
+            }
+            __syncthreads();
+
+            if (S.accept) {
+                if (C.charged)
+                    for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
+                        sre[t] += dre[t];
+                        sim[t] += dim[t];
+                    }
+                if (threadIdx.x == 0) {
+                    c.accepted[S.move]++;
+                    if (C.charged) {
+                        c.self_e += S.dself;
+                        c.excl_e += S.dexcl;
+                    }
+                    if (S.move <= 1) {
+                        for (int s = 0; s < NS; ++s) {
+                            const uint32_t slot = S.ex[s] - (uint32_t)C.n_fw;
+                            gx[slot] = S.np_[s][0];
+                            gy[slot] = S.np_[s][1];
+                            gz[slot] = S.np_[s][2];
+                        }
+                    } else if (S.move == 2) {
+                        for (int s = 0; s < NS; ++s) {
+                            const uint32_t slot = (uint32_t)c.n_guest + s;
+                            gx[slot] = S.np_[s][0];
+                            gy[slot] = S.np_[s][1];
+                            gz[slot] = S.np_[s][2];
+                            gq[slot] = C.sq[s];
+                            gt[slot] = C.slj[s];
+                            mol[(size_t)c.n_mol * NS + s] = (uint32_t)C.n_fw + slot;
+                        }
+                        c.n_guest += NS;
+                        c.n_mol += 1;
+                    } else {
+                        uint32_t idx[NS];
+                        for (int s = 0; s < NS; ++s) idx[s] = S.ex[s];
+                        for (uint32_t m = S.mi; m + 1 < c.n_mol; ++m)
+                            for (int s = 0; s < NS; ++s) mol[(size_t)m * NS + s] = mol[(size_t)(m + 1) * NS + s];
+                        c.n_mol -= 1;
+                        for (int k = 0; k < NS; ++k) {
+                            const uint32_t site = idx[k];
+                            const uint32_t last = (uint32_t)(C.n_fw + c.n_guest - 1);
+                            if (site != last) {
+                                const uint32_t ds = site - (uint32_t)C.n_fw, ls = last - (uint32_t)C.n_fw;
+                                gx[ds] = gx[ls];
+                                gy[ds] = gy[ls];
+                                gz[ds] = gz[ls];
+                                gq[ds] = gq[ls];
+                                gt[ds] = gt[ls];
+                                for (uint64_t m = 0; m < (uint64_t)c.n_mol * NS; ++m)
+                                    if (mol[m] == last) mol[m] = site;
+                                for (int k2 = k + 1; k2 < NS; ++k2)
+                                    if (idx[k2] == last) idx[k2] = site;
+                            }
+                            c.n_guest -= 1;
+                        }
+                    }
+                    if (C.charged) {
+                        c.moves_since_resync++;
+                        if (c.moves_since_resync >= 100) {
+                            S.do_resync = 1;
+                            c.moves_since_resync = 0;
+                            c.resyncs++;
+                        }
+                    }
+                    S.ng_after = c.n_guest;
+                }
+                __syncthreads();
+                if (S.do_resync) {
+                    const uint64_t ng = S.ng_after;
+                    for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
+                        const double k0 = P.k[3 * t], k1 = P.k[3 * t + 1], k2 = P.k[3 * t + 2];
+                        double re = P.sfw_re[t], im = P.sfw_im[t];
+                        for (uint64_t g = 0; g < ng; ++g) {
+                            double sn, cs;
+                            sincos(k0 * gx[g] + k1 * gy[g] + k2 * gz[g], &sn, &cs);
+                            re += gq[g] * cs;
+                            im += gq[g] * sn;
+                        }
+                        sre[t] = re;
+                        sim[t] = im;
+                    }
+                    if (threadIdx.x == 0) {
+                        double q2 = C.fw_q2;
+                        for (uint64_t g = 0; g < ng; ++g) q2 += gq[g] * gq[g];
+                        c.self_e = C.self_pref * q2;
+                        double ex = 0.0;
+                        for (uint32_t m = 0; m < c.n_mol; ++m) {
+                            double p[MAXS][3], q[MAXS];
+                            for (int s = 0; s < NS; ++s) {
+                                const uint32_t slot = mol[(size_t)m * NS + s] - (uint32_t)C.n_fw;
+                                p[s][0] = gx[slot];
+                                p[s][1] = gy[slot];
+                                p[s][2] = gz[slot];
+                                q[s] = gq[slot];
+                            }
+                            ex += exclusion_sum(C.L, p, q, NS, C.alpha);
+                        }
+                        c.excl_e = -kCoulomb * ex;
+                    }
+                }
+            }
+        }
+        if (threadIdx.x == 0) {
+            c.steps++;
+            c.sum_n += (double)c.n_mol;
+            c.sum_n2 += (double)c.n_mol * (double)c.n_mol;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        P.st[chain] = c;
+        if (c.err) atomicOr(P.flags, c.err);
+    }
+}
+
+template <int NS>
+void launch_chains(unsigned n_chains, const GcmcConst& C, const GcmcPtrs& P, uint64_t steps,
+                   cudaStream_t s) {
+    gcmc_kernel<NS><<<n_chains, GT, 0, s>>>(C, P, steps);
+}
+
+__global__ void gather_sfw_kernel(uint64_t nk, const double* re, const double* im, double* out_re,
+                                  double* out_im, unsigned n_chains) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nk) return;
+    for (unsigned c = 0; c < n_chains; ++c) {
+        out_re[(size_t)c * nk + t] = re[t];
+        out_im[(size_t)c * nk + t] = im[t];
+    }
+}
+
+}  // namespace
+
+struct GcmcImpl {
+    GcmcConst C{};
+    unsigned n_chains = 0;
+    DevBuf<double4> fw;
+    DevBuf<uint32_t> fw_type;
+    DevBuf<PairParams> table;
+    DevBuf<double> k, w, sfw_re, sfw_im;
+    DevBuf<int> nidx;
+    DevBuf<ChainState> st;
+    DevBuf<double> gx, gy, gz, gq, sre, sim, dre, dim;
+    DevBuf<uint32_t> gt, mol;
+    DevBuf<unsigned> flags;
+    float last_ms = 0.f;
+};
+
+GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const alea_particles& fw,
+                      const alea_lattice& lat, const alea_molecule_species& guest,
+                      double temperature, const double* fugacity_pa, const uint64_t* seeds,
+                      const uint64_t* streams, uint32_t n_chains, double max_translation,
+                      double max_rotation, int draw_order, uint32_t max_molecules) {
+    require(n_chains >= 1, ALEA_ERR_INVALID_ARGUMENT, "GCMC: at least one chain");
+    require(guest.n_sites >= 1 && guest.n_sites <= MAXS, ALEA_ERR_INVALID_ARGUMENT,
+            "GCMC: the species needs 1..8 sites");
+    require(guest.n_sites == 1 || guest.n_sites == 2 || guest.n_sites == 3 || guest.n_sites == 4 ||
+                guest.n_sites == 5,
+            ALEA_ERR_INVALID_ARGUMENT, "GCMC: 1..5 sites per molecule are compiled");
+    require(temperature > 0.0, ALEA_ERR_INVALID_ARGUMENT,
+            "MonteCarloEngine: temperatureKelvin must be positive");
+    require(lj.cutoff > 0.0 && lj.n_species >= 1 && lj.n_species <= 64, ALEA_ERR_INVALID_ARGUMENT,
+            "GCMC: LJ cutoff > 0 and 1..64 species");
+    require(max_molecules >= 1, ALEA_ERR_INVALID_ARGUMENT, "GCMC: max_molecules >= 1");
+    require(draw_order == ALEA_DRAWS_RIGHT_TO_LEFT || draw_order == ALEA_DRAWS_LEFT_TO_RIGHT,
+            ALEA_ERR_INVALID_ARGUMENT, "GCMC: unknown draw order");
+    require(fw.n == 0 || (fw.x && fw.y && fw.z), ALEA_ERR_INVALID_ARGUMENT,
+            "GCMC: framework coordinates missing");
+    for (uint32_t c = 0; c < n_chains; ++c)
+        require(fugacity_pa[c] * (1.0 / (1.380649e-23 * 1.0e30)) > 0.0, ALEA_ERR_INVALID_ARGUMENT,
+                "MonteCarloEngine: every fugacityPascal must be positive");
+    auto* g = new GcmcImpl();
+    try {
+        GcmcConst& C = g->C;
+        C.L = make_lattice(lat.m);
+        validate_cutoff(C.L, lj.cutoff, "MonteCarloEngine (LJ)");
+        C.ns = (int)guest.n_sites;
+        double qs = 0.0;
+        for (uint32_t s = 0; s < guest.n_sites; ++s) {
+            require(guest.lj_species[s] < lj.n_species, ALEA_ERR_OUT_OF_RANGE,
+                    "GCMC: site LJ species out of range");
+            C.sx[s] = guest.x[s];
+            C.sy[s] = guest.y[s];
+            C.sz[s] = guest.z[s];
+            C.sq[s] = guest.charge ? guest.charge[s] : 0.0;
+            C.slj[s] = guest.lj_species[s];
+            qs += C.sq[s];
+        }
+        C.n_species = lj.n_species;
+        C.rc = lj.cutoff;
+        C.rc2 = lj.cutoff * lj.cutoff;
+        C.trunc = lj.truncation;
+        C.temperature = temperature;
+        C.max_trans = max_translation;
+        C.max_rot = max_rotation;
+        C.draw_order = draw_order;
+        C.n_fw = fw.n;
+        C.max_mol = max_molecules;
+        C.max_sites = max_molecules * guest.n_sites;
+        C.volume = std::fabs(C.L.volume);
+        std::vector<double4> packed(fw.n);
+        std::vector<uint32_t> types(fw.n, 0);
+        double fwq = 0.0, fwq2 = 0.0;
+        for (uint64_t i = 0; i < fw.n; ++i) {
+            const double q = fw.charge ? fw.charge[i] : 0.0;
+            packed[i] = make_double4(fw.x[i], fw.y[i], fw.z[i], q);
+            if (fw.species) {
+                require(fw.species[i] < lj.n_species, ALEA_ERR_OUT_OF_RANGE,
+                        "GCMC: framework species out of range");
+                types[i] = fw.species[i];
+            }
+            fwq += q;
+            fwq2 += q * q;
+        }
+        C.fw_q2 = fwq2;
+        EwaldStateImpl* ews = nullptr;
+        if (ew) {
+            // monte_carlo_engine.cc:273-293
+            require(std::fabs(qs) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
+                    "MonteCarloEngine: GCMC species 0 is not individually charge-neutral");
+            require(std::fabs(fwq) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
+                    "MonteCarloEngine: framework is not charge-neutral");
+            require(ew->kmax <= KMAXC, ALEA_ERR_INVALID_ARGUMENT, "GCMC: kMax <= 20 supported");
+            validate_cutoff(C.L, ew->real_space_cutoff, "MonteCarloEngine (Ewald real space)");
+        }
+        require_device();
+        g->n_chains = n_chains;
+        g->fw.alloc(std::max<size_t>(fw.n, 1));
+        g->fw_type.alloc(std::max<size_t>(fw.n, 1));
+        g->fw.upload(packed.data(), fw.n);
+        g->fw_type.upload(types.data(), fw.n);
+        std::vector<PairParams> table((size_t)lj.n_species * lj.n_species);
+        mixed_table(lj, table.data());
+        g->table.alloc(table.size());
+        g->table.upload(table.data(), table.size());
+        uint64_t nk = 0;
+        if (ew) {
+            ews = ewald_state_create(*ew, fw, lat);
+            const EwaldDeviceView v = ewald_state_view(ews);
+            nk = v.nk;
+            C.charged = 1;
+            C.alpha = ew->alpha;
+            C.rc_ew = ew->real_space_cutoff;
+            C.rc_ew2 = C.rc_ew * C.rc_ew;
+            C.kmax = ew->kmax;
+            C.nk = nk;
+            for (int i = 0; i < 9; ++i) C.b[i] = v.b[i];
+            C.self_pref = v.self_pref;
+            C.rec_pref = v.rec_pref;
+            g->k.alloc(3 * nk);
+            g->w.alloc(nk);
+            g->nidx.alloc(3 * nk);
+            g->sfw_re.alloc(nk);
+            g->sfw_im.alloc(nk);
+            ALEA_CUDA(cudaMemcpy(g->k.p, v.k, 3 * nk * sizeof(double), cudaMemcpyDeviceToDevice));
+            ALEA_CUDA(cudaMemcpy(g->w.p, v.w, nk * sizeof(double), cudaMemcpyDeviceToDevice));
+            ALEA_CUDA(cudaMemcpy(g->nidx.p, v.nidx, 3 * nk * sizeof(int), cudaMemcpyDeviceToDevice));
+            ALEA_CUDA(cudaMemcpy(g->sfw_re.p, v.sre, nk * sizeof(double), cudaMemcpyDeviceToDevice));
+            ALEA_CUDA(cudaMemcpy(g->sfw_im.p, v.sim, nk * sizeof(double), cudaMemcpyDeviceToDevice));
+        }
+        const size_t nkc = std::max<uint64_t>(nk, 1);
+        g->sre.alloc(nkc * n_chains);
+        g->sim.alloc(nkc * n_chains);
+        g->dre.alloc(nkc * n_chains);
+        g->dim.alloc(nkc * n_chains);
+        if (ews) {
+            gather_sfw_kernel<<<(unsigned)((nk + 255) / 256), 256>>>(nk, g->sfw_re.p, g->sfw_im.p,
+                                                                   g->sre.p, g->sim.p, n_chains);
+            ALEA_CUDA(cudaGetLastError());
+        }
+        const size_t sites = (size_t)C.max_sites * n_chains;
+        g->gx.alloc(sites);
+        g->gy.alloc(sites);
+        g->gz.alloc(sites);
+        g->gq.alloc(sites);
+        g->gt.alloc(sites);
+        g->mol.alloc(sites);
+        std::vector<ChainState> st(n_chains);
+        const double self0 = ews ? ewald_state_view(ews).self_pref * fwq2 : 0.0;
+        for (uint32_t c = 0; c < n_chains; ++c) {
+            ChainState& s = st[c];
+            s = ChainState{};
+            s.seed = seeds[c];
+            s.stream = streams[c];
+            s.fugacity = fugacity_pa[c] * (1.0 / (1.380649e-23 * 1.0e30));
+            s.self_e = self0;
+        }
+        if (ews) {
+            // the committed self energy is the framework's (ewald_incremental_state.cc:77-81)
+            const auto raw = ewald_state_raw(ews);
+            for (auto& s : st) s.self_e = raw[2 * nk];
+            ewald_state_destroy(ews);
+        }
+        g->st.alloc(n_chains);
+        g->st.upload(st.data(), n_chains);
+        g->flags.alloc(1);
+        ALEA_CUDA(cudaMemset(g->flags.p, 0, sizeof(unsigned)));
+        ALEA_CUDA(cudaDeviceSynchronize());
+    } catch (...) {
+        delete g;
+        throw;
+    }
+    return g;
+}
+
+void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s) {
+    GcmcPtrs P{};
+    P.fw = g->fw.p;
+    P.fw_type = g->fw_type.p;
+    P.table = g->table.p;
+    P.k = g->k.p;
+    P.w = g->w.p;
+    P.nidx = g->nidx.p;
+    P.sfw_re = g->sfw_re.p;
+    P.sfw_im = g->sfw_im.p;
+    P.st = g->st.p;
+    P.gx = g->gx.p;
+    P.gy = g->gy.p;
+    P.gz = g->gz.p;
+    P.gq = g->gq.p;
+    P.gt = g->gt.p;
+    P.mol = g->mol.p;
+    P.sre = g->sre.p;
+    P.sim = g->sim.p;
+    P.dre = g->dre.p;
+    P.dim = g->dim.p;
+    P.flags = g->flags.p;
+    cudaEvent_t e0, e1;
+    ALEA_CUDA(cudaEventCreate(&e0));
+    ALEA_CUDA(cudaEventCreate(&e1));
+    ALEA_CUDA(cudaEventRecord(e0, s));
+    switch (g->C.ns) {
+        case 1: launch_chains<1>(g->n_chains, g->C, P, steps, s); break;
+        case 2: launch_chains<2>(g->n_chains, g->C, P, steps, s); break;
+        case 3: launch_chains<3>(g->n_chains, g->C, P, steps, s); break;
+        case 4: launch_chains<4>(g->n_chains, g->C, P, steps, s); break;
+        default: launch_chains<5>(g->n_chains, g->C, P, steps, s); break;
+    }
+    ALEA_CUDA(cudaGetLastError());
+    ALEA_CUDA(cudaEventRecord(e1, s));
+    ALEA_CUDA(cudaEventSynchronize(e1));
+    ALEA_CUDA(cudaEventElapsedTime(&g->last_ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    check_device_flags(g->flags.p, s, "GCMC chains (capacity: raise max_molecules)");
+}
+
+void gcmc_states(const GcmcImpl* g, ChainState* out) {
+    g->st.download(out, g->n_chains);
+    ALEA_CUDA(cudaDeviceSynchronize());
+}
+
+uint64_t gcmc_particles(const GcmcImpl* g, uint32_t chain, double* xyz, uint64_t cap) {
+    require(chain < g->n_chains, ALEA_ERR_OUT_OF_RANGE, "GCMC: chain index");
+    ChainState s;
+    ALEA_CUDA(cudaMemcpy(&s, g->st.p + chain, sizeof s, cudaMemcpyDeviceToHost));
+    const uint64_t n = g->C.n_fw + s.n_guest;
+    if (xyz && cap >= n) {
+        std::vector<double4> f(g->C.n_fw);
+        g->fw.download(f.data(), g->C.n_fw);
+        std::vector<double> x(s.n_guest), y(s.n_guest), z(s.n_guest);
+        const size_t so = (size_t)chain * g->C.max_sites;
+        ALEA_CUDA(cudaMemcpy(x.data(), g->gx.p + so, s.n_guest * 8, cudaMemcpyDeviceToHost));
+        ALEA_CUDA(cudaMemcpy(y.data(), g->gy.p + so, s.n_guest * 8, cudaMemcpyDeviceToHost));
+        ALEA_CUDA(cudaMemcpy(z.data(), g->gz.p + so, s.n_guest * 8, cudaMemcpyDeviceToHost));
+        ALEA_CUDA(cudaDeviceSynchronize());
+        for (uint64_t i = 0; i < g->C.n_fw; ++i) {
+            xyz[3 * i] = f[i].x;
+            xyz[3 * i + 1] = f[i].y;
+            xyz[3 * i + 2] = f[i].z;
+        }
+        for (uint64_t i = 0; i < s.n_guest; ++i) {
+            xyz[3 * (g->C.n_fw + i)] = x[i];
+            xyz[3 * (g->C.n_fw + i) + 1] = y[i];
+            xyz[3 * (g->C.n_fw + i) + 2] = z[i];
+        }
+    }
+    return n;
+}
+
+// committedEnergy() of one chain's cache (ewald_incremental_state.cc:85-93)
+double gcmc_ewald_energy(const GcmcImpl* g, uint32_t chain) {
+    require(chain < g->n_chains, ALEA_ERR_OUT_OF_RANGE, "GCMC: chain index");
+    if (!g->C.charged) return 0.0;
+    const uint64_t nk = g->C.nk;
+    std::vector<double> re(nk), im(nk), w(nk);
+    ALEA_CUDA(cudaMemcpy(re.data(), g->sre.p + (size_t)chain * nk, nk * 8, cudaMemcpyDeviceToHost));
+    ALEA_CUDA(cudaMemcpy(im.data(), g->sim.p + (size_t)chain * nk, nk * 8, cudaMemcpyDeviceToHost));
+    ALEA_CUDA(cudaMemcpy(w.data(), g->w.p, nk * 8, cudaMemcpyDeviceToHost));
+    ChainState s;
+    ALEA_CUDA(cudaMemcpy(&s, g->st.p + chain, sizeof s, cudaMemcpyDeviceToHost));
+    double sum = 0.0;
+    for (uint64_t t = 0; t < nk; ++t) sum += w[t] * (re[t] * re[t] + im[t] * im[t]);
+    return sum * kCoulomb * (2.0 * kPi / g->C.volume) + s.self_e + s.excl_e;
+}
+
+unsigned gcmc_chains(const GcmcImpl* g) { return g->n_chains; }
+float gcmc_last_ms(const GcmcImpl* g) { return g->last_ms; }
+void gcmc_destroy(GcmcImpl* g) { delete g; }
+
+}  // namespace alea

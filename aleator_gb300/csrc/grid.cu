@@ -56,6 +56,7 @@ struct GridGeom {
     double G[9];           // metric tensor a_i . a_j
     float Gf[9];           // the same in FP32 (bin culling)
     float lof[3], binwf[3];  // lo and binw in FP32 (bin culling)
+    float near2;           // (largest sigma + brick half-diagonal)^2: close-pass reach
     double rc, rc2;
     int bricks[3];
     int n_types;           // framework LJ species in the table
@@ -224,6 +225,7 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
     uint32_t* warp_tot = reinterpret_cast<uint32_t*>(take((THREADS / 32) * sizeof(uint32_t)));
     ParamF* pf = reinterpret_cast<ParamF*>(take(64 * MAX_NG * sizeof(ParamF)));
     float* rcl2 = reinterpret_cast<float*>(take(64 * sizeof(float)));
+    uint16_t* close_idx = reinterpret_cast<uint16_t*>(take(TILE * sizeof(uint16_t)));
     PairParams* pd = reinterpret_cast<PairParams*>(take(64 * MAX_NG * sizeof(PairParams)));
     ParamFF* pff = reinterpret_cast<ParamFF*>(pd);  // the FP32 form uses this slot instead
 
@@ -444,13 +446,29 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
             break;
         }
         if (sizeof(Real) == 4) {
-            for (uint32_t i = tid; i < cnt; i += THREADS) {
-                const ImageRec r = raw[buf * TILE + i];
+            // convert to brick-centred FP32 (hi + lo parts) and list, in atom
+            // order, the atoms that can be closer than sigma to a node of this
+            // brick (within reach of the brick centre)
+            static_assert(TILE == THREADS, "one atom per thread in the conversion pass");
+            bool near = false;
+            if ((uint32_t)tid < cnt) {
+                const ImageRec r = raw[buf * TILE + tid];
                 const double lx = r.x - ox, ly = r.y - oy, lz = r.z - oz;
                 const float hx = (float)lx, hy = (float)ly, hz = (float)lz;
-                conv[i] = make_float4(hx, hy, hz, __int_as_float((int)r.type));
-                convlo[i] = make_float4((float)(lx - hx), (float)(ly - hy), (float)(lz - hz), 0.f);
+                conv[tid] = make_float4(hx, hy, hz, __int_as_float((int)r.type));
+                convlo[tid] = make_float4((float)(lx - hx), (float)(ly - hy), (float)(lz - hz), 0.f);
+                near = fmaf(hx, hx, fmaf(hy, hy, hz * hz)) < geo.near2;
             }
+            const unsigned ballot = __ballot_sync(0xffffffffu, near);
+            if ((tid & 31) == 0) warp_tot[tid >> 5] = __popc(ballot);
+            __syncthreads();
+            if (near) {
+                uint32_t off = __popc(ballot & ((1u << (tid & 31)) - 1u));
+                for (int w = 0; w < (tid >> 5); ++w) off += warp_tot[w];
+                close_idx[off] = (uint16_t)tid;
+            }
+            uint32_t n_close = 0;
+            for (int w = 0; w < THREADS / 32; ++w) n_close += warp_tot[w];
             __syncthreads();
             // raw[buf] is free again: prefetch tile t + 2 while computing
             if (tid == 0 && t + 2 < n_tiles) {
@@ -477,8 +495,8 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
                     const float dz = a.z - (float)nzr[k];
                     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                     const float inv = __frcp_rn(fmaxf(r2, 1e-4f));
-                    const bool close = r2 < close2;
-                    const bool in = (r2 <= rc2f) && !close;
+                    // pairs closer than sigma are left to the close pass below
+                    const bool in = (r2 <= rc2f) && (r2 >= close2);
 #pragma unroll
                     for (int g = 0; g < NG; ++g) {
                         const float s2 = p[g].sig2 * inv;
@@ -490,8 +508,22 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
                         }
                         part[g][k] += in ? e : 0.f;
                     }
-                    if (close) {
-                        // rare: r < sigma; double-float term straight into FP64
+                }
+            }
+            // close pass: the few listed atoms, pairs closer than sigma in
+            // double-float, straight into the FP64 accumulators
+            for (uint32_t c = 0; c < n_close; ++c) {
+                const uint32_t j = close_idx[c];
+                const float4 a = conv[j];
+                const int type = __float_as_int(a.w);
+                const float close2 = rcl2[type];
+#pragma unroll
+                for (int k = 0; k < NPT; ++k) {
+                    const float dx = a.x - (float)nxr[k];
+                    const float dy = a.y - (float)nyr[k];
+                    const float dz = a.z - (float)nzr[k];
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    if (r2 < close2) {
                         const float4 al = convlo[j];
                         const ff ddx = ff_add(ff{a.x, al.x}, ff{-(float)nxr[k], -nlo[(k * 3 + 0) * THREADS + tid]});
                         const ff ddy = ff_add(ff{a.y, al.y}, ff{-(float)nyr[k], -nlo[(k * 3 + 1) * THREADS + tid]});
@@ -628,7 +660,8 @@ constexpr size_t grid_smem_bytes() {
            up((sizeof(Real) == 4 ? NPT * 3 * THREADS : 1) * sizeof(float)) + up(2 * sizeof(uint64_t)) +
            up(MAX_ROWS * sizeof(uint32_t)) + up((MAX_ROWS + 1) * sizeof(uint32_t)) +
            up((THREADS / 32) * sizeof(uint32_t)) + up(64 * MAX_NG * sizeof(ParamF)) +
-           up(64 * sizeof(float)) + up(64 * MAX_NG * sizeof(PairParams));
+           up(64 * sizeof(float)) + up(TILE * sizeof(uint16_t)) +
+           up(64 * MAX_NG * sizeof(PairParams));
 }
 
 template <typename Real, int NG, int TRUNC>
@@ -816,6 +849,22 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
 
     std::vector<PairParams> table((size_t)lj.n_species * lj.n_species);
     mixed_table(lj, table.data());
+    // reach of the FP32 form's close pass: largest mixed sigma of these guests
+    // plus the half-diagonal of a brick (triangle inequality bound)
+    {
+        double smax = 0.0;
+        for (uint32_t gs : sp)
+            for (uint32_t t = 0; t < lj.n_species; ++t)
+                smax = std::max(smax, table[(size_t)gs * lj.n_species + t].sigma);
+        double half = 0.0;
+        const int bd[3] = {BX, BY, BZ};
+        for (int a = 0; a < 3; ++a) {
+            const double f = (double)(bd[a] - 1) / g.geo.n[a];
+            half += 0.5 * f * std::sqrt(m[3 * a] * m[3 * a] + m[3 * a + 1] * m[3 * a + 1] + m[3 * a + 2] * m[3 * a + 2]);
+        }
+        const double reach = smax * (1.0 + 1e-5) + half + 1e-3;
+        g.geo.near2 = (float)(reach * reach);
+    }
     g.params.alloc(table.size());
     g.params.upload(table.data(), table.size());
     g.guests.alloc(std::max(ng, 1));

@@ -101,4 +101,20 @@ void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uin
                int draw_order, alea_widom_result* out, double* per_trial);
 void widom_destroy(WidomImpl* w);
 
+// gcmc.cu
+struct GcmcImpl;
+struct ChainState;
+GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const alea_particles& fw,
+                      const alea_lattice& lat, const alea_molecule_species& guest,
+                      double temperature, const double* fugacity_pa, const uint64_t* seeds,
+                      const uint64_t* streams, uint32_t n_chains, double max_translation,
+                      double max_rotation, int draw_order, uint32_t max_molecules);
+void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s);
+void gcmc_states(const GcmcImpl* g, ChainState* out);
+uint64_t gcmc_particles(const GcmcImpl* g, uint32_t chain, double* xyz, uint64_t cap);
+double gcmc_ewald_energy(const GcmcImpl* g, uint32_t chain);
+unsigned gcmc_chains(const GcmcImpl* g);
+float gcmc_last_ms(const GcmcImpl* g);
+void gcmc_destroy(GcmcImpl* g);
+
 }  // namespace alea

@@ -280,6 +280,44 @@ alea_status alea_widom_run(alea_widom* w, uint64_t seed, uint64_t stream, uint64
                            double* per_trial_du);
 alea_status alea_widom_destroy(alea_widom* w);
 
+/* ------------------------------------------------------------------ GCMC chains */
+/* MonteCarloEngine (engines/monte_carlo/monte_carlo_engine.hpp:76-83, single
+ * species, direct-scan dispersion) for n_chains independent chains at once:
+ * chain c uses Philox stream (seeds[c], streams[c]) and fugacity_pa[c]
+ * (PengRobinson::fugacityPascal output). ewald may be NULL (LJ only).
+ * max_molecules bounds each chain's molecule count (device storage). */
+typedef struct alea_gcmc alea_gcmc;
+alea_status alea_gcmc_create(const alea_lennard_jones* lj, const alea_ewald* ewald,
+                             const alea_particles* framework, const alea_lattice* lattice,
+                             const alea_molecule_species* species, double temperature,
+                             const double* fugacity_pa, const uint64_t* seeds,
+                             const uint64_t* streams, uint32_t n_chains, double max_translation,
+                             double max_rotation, int32_t draw_order, uint32_t max_molecules,
+                             alea_gcmc** out);
+/* run(numSteps) (monte_carlo_engine.hpp:163, .cc:405-439) on every chain. */
+alea_status alea_gcmc_run(alea_gcmc* g, uint64_t steps, void* cuda_stream);
+typedef struct {
+    uint64_t molecules;      /* moleculeCount() (monte_carlo_engine.hpp:168) */
+    uint64_t guest_sites;
+    uint64_t call_index;     /* Philox draws consumed so far */
+    uint64_t steps;
+    uint64_t resyncs;        /* S(k) rebuilds (maybeResyncEwald) */
+    uint64_t attempted[4];   /* translate, rotate, insert, delete */
+    uint64_t accepted[4];
+    double sum_molecules;    /* sum over moves of the molecule count after the move */
+    double sum_molecules_sq;
+    double last_du;
+    float last_kernel_ms;
+} alea_gcmc_chain_info;
+alea_status alea_gcmc_chain_info_get(const alea_gcmc* g, uint32_t chain, alea_gcmc_chain_info* out);
+/* particles() positions (monte_carlo_engine.hpp:165): framework then guest
+ * sites in the engine's particle order; n_out = count. */
+alea_status alea_gcmc_particles(const alea_gcmc* g, uint32_t chain, double* xyz, uint64_t cap,
+                                uint64_t* n_out);
+/* electrostaticEnergyForTesting() (monte_carlo_engine.hpp:214, .cc:928-930). */
+alea_status alea_gcmc_ewald_energy(const alea_gcmc* g, uint32_t chain, double* out);
+alea_status alea_gcmc_destroy(alea_gcmc* g);
+
 /* ------------------------------------------------------------------ acceptance / EOS (host) */
 /* gcmc::insertionRatio ... clampToProbability (engines/monte_carlo/gcmc_acceptance.hpp:28-101) */
 double alea_insertion_ratio(double f, double v, uint64_t n_before, double t, double du);

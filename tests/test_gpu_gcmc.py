@@ -1,0 +1,96 @@
+"""GCMC chains on the GPU against the oracle's restatement of
+MonteCarloEngine::run (itself bit-exact to the reference engine, see
+tests/test_oracle_gcmc.py): the same Philox stream drives both, so the move
+sequence, acceptances, molecule counts and particle order must agree;
+positions and the committed Ewald energy within FP64 rounding (1e-9 Å and
+1e-10 relative; the GPU sums pair energies in a tree order)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from aleator_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(A, orc, fw, guest, ewald, fug, seed, stream, T=298.0):
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    ew = A.Ewald(ewald["alpha"], ewald["rc"], ewald["kmax"]) if ewald else None
+    gpu = A.GcmcChains(ff, p, fw.lattice, guest, T, [fug], [seed], [stream], ewald=ew)
+    od = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.8, truncation=O.SHIFTED)
+    cpu = orc.gcmc(od, ewald, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guest, T, fug,
+                   seed, stream)
+    return gpu, cpu
+
+
+def _compare(gpu, cpu, chain=0, charged=False):
+    info = gpu.info(chain)
+    assert info["molecules"] == cpu.molecules()
+    assert info["call_index"] == cpu.calls()
+    ctr = cpu.counters()
+    assert list(info["attempted"]) == [int(v) for v in ctr[:4]]
+    assert list(info["accepted"]) == [int(v) for v in ctr[4:]]
+    pg, pc = gpu.positions(chain), cpu.positions()
+    assert pg.shape == pc.shape
+    assert np.abs(pg - pc).max() <= 1e-9
+    if charged:
+        eg, ec = gpu.ewald_energy(chain), cpu.ewald_energy()
+        assert abs(eg - ec) <= 1e-10 * max(1.0, abs(ec))
+
+
+def test_ch4_chain_matches_oracle(lib, orc):
+    A, _ = lib
+    fw = W.cubic_framework(seed=11)
+    fug = orc.pr_fugacity(*W.METHANE_CRITICAL, 298.0, 5e6)
+    gpu, cpu = _pair(A, orc, fw, W.ch4_guest(fw), None, fug, 5, 1)
+    for _ in range(4):
+        gpu.run(400)
+        cpu.run(400)
+        _compare(gpu, cpu)
+    assert gpu.info()["accepted"][2] > 0
+
+
+def test_co2_charged_chain_with_resync(lib, orc):
+    A, _ = lib
+    fw = W.cubic_framework(seed=12, charged=True)
+    fw.charge = fw.charge * 0.15  # weaker framework field: many accepted moves, several resyncs
+    ew = dict(alpha=0.31, rc=12.0, kmax=5)
+    fug = orc.pr_fugacity(*W.CO2_CRITICAL, 298.0, 1e6)
+    gpu, cpu = _pair(A, orc, fw, W.co2_guest(fw), ew, fug, 3, 7)
+    for _ in range(6):
+        gpu.run(500)
+        cpu.run(500)
+        _compare(gpu, cpu, charged=True)
+    assert gpu.info()["resyncs"] >= 1
+
+
+def test_many_chains_independent(lib, orc):
+    A, _ = lib
+    fw = W.cubic_framework(seed=13, charged=True)
+    fw.charge = fw.charge * 0.15
+    ew = dict(alpha=0.31, rc=12.0, kmax=4)
+    pressures = [1e4, 1e5, 1e6, 3e6]
+    fugs = [orc.pr_fugacity(*W.CO2_CRITICAL, 298.0, P) for P in pressures]
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    chains = A.GcmcChains(ff, p, fw.lattice, W.co2_guest(fw), 298.0, fugs, [21] * 4,
+                          [0, 1, 2, 3], ewald=A.Ewald(0.31, 12.0, 4))
+    chains.run(600)
+    od = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.8, truncation=O.SHIFTED)
+    for c in range(4):
+        cpu = orc.gcmc(od, ew, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species,
+                       W.co2_guest(fw), 298.0, fugs[c], 21, c)
+        cpu.run(600)
+        _compare(chains, cpu, chain=c, charged=True)
+
+
+def test_capacity_is_reported(lib):
+    A, _ = lib
+    fw = W.cubic_framework(seed=14)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    chains = A.GcmcChains(ff, A.ParticleData.from_framework(fw), fw.lattice, W.ch4_guest(fw), 298.0,
+                          [1e9], [1], [0], max_molecules=2)
+    with pytest.raises(A.AleatorError) as e:
+        chains.run(2000)
+    assert e.value.status == 6

@@ -56,7 +56,7 @@ def test_fp32_grid_within_1e5(lib):
     for sid, ref_table in tables.items():
         mine = grid.table(sid)
         keep = ref_table <= 1e4
-        assert keep.sum() > 0.2 * ref_table.size
+        assert keep.sum() > 500
         assert rel_err(mine[keep], ref_table[keep], floor=KT).max() <= 1e-5
         assert (mine[ref_table >= 1e5] >= 1e4).all()
 
