@@ -141,6 +141,10 @@ _SIGNATURES = {
     "alea_ewald_state_raw": (ctypes.c_int32, [_VP, _D, ctypes.c_uint64, _U64]),
     "alea_ewald_state_term_count": (ctypes.c_int32, [_VP, _U64]),
     "alea_ewald_state_destroy": (ctypes.c_int32, [_VP]),
+    "alea_ewald_propose_no_alloc": (ctypes.c_int32, [_VP, _VP, _VP, _VP, ctypes.c_uint64,
+                                                     ctypes.c_double, ctypes.POINTER(_Lattice), _D,
+                                                     ctypes.c_uint64, _D, ctypes.c_uint64, _VP,
+                                                     _VP]),
     "alea_widom_create": (ctypes.c_int32, [ctypes.POINTER(_LJ), ctypes.POINTER(_Ewald),
                                            ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
                                            ctypes.POINTER(_Species), ctypes.c_double,

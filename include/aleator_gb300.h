@@ -254,6 +254,28 @@ alea_status alea_ewald_state_raw(const alea_ewald_state* s, double* out, uint64_
 alea_status alea_ewald_state_term_count(const alea_ewald_state* s, uint64_t* out);
 alea_status alea_ewald_state_destroy(alea_ewald_state* s);
 
+/* No counterpart in the reference. The energy change alea_ewald_state_propose
+ * computes, for callers that cannot let a library allocate device memory: an
+ * engine that hands out every device buffer from its own pre-reserved pool,
+ * or one that cannot accept the device-wide synchronisation cudaMalloc and
+ * cudaFree may imply while its other streams are busy. This call allocates
+ * nothing. The caller passes device pointers to the terms' k vectors
+ * (3 doubles each), weights and committed sRe / sIm (n_terms each), the
+ * Ewald alpha and the lattice, the removed and added sites as host arrays
+ * (packed {x, y, z, q}; at most 64 together), and a device pointer `out` to 4
+ * doubles that receive {reciprocal, self, exclusion, total}. The call is
+ * asynchronous on cuda_stream. Limit: n_terms <= 262144 (the size of the fixed
+ * scratch array; larger requests fail with ALEA_ERR_INVALID_ARGUMENT). The
+ * per-block partial sums live in one file-scope device array that every GPU
+ * loading the library holds until exit; calls that overlap on the GPU race on
+ * it, and the first call on each device looks up its address, so make that
+ * first call before any stream capture. */
+alea_status alea_ewald_propose_no_alloc(const double* k, const double* weight, const double* sre,
+                                        const double* sim, uint64_t n_terms, double alpha,
+                                        const alea_lattice* lattice, const double* removed,
+                                        uint64_t n_removed, const double* added, uint64_t n_added,
+                                        double* out, void* cuda_stream);
+
 /* ------------------------------------------------------------------ Widom insertion */
 /* MonteCarloEngine::widomInsertionHenryCoefficient(numTrials, speciesIndex)
  * (engines/monte_carlo/monte_carlo_engine.hpp:198-199, .cc:850-917) on the
