@@ -18,6 +18,9 @@
 // parallelepiped distance, merges each bin row into one contiguous atom
 // range, and streams the ranges through shared memory in 256-record tiles
 // with cp.async.bulk (TMA) copies completed on an mbarrier, double-buffered.
+// The FP32 form then groups each tile by framework type, skips per warp the
+// atoms beyond reach of the warp's 8x4x4 sub-box, and evaluates the rest as
+// r^-6 (A r^-6 - B) with the shift terms applied per same-type run.
 
 #include <algorithm>
 #include <cmath>
@@ -47,19 +50,36 @@ struct __align__(16) ImageRec {
 };
 static_assert(sizeof(ImageRec) == 32, "image record must stay 32 bytes");
 
+// The FP32 form's copy of an image: the position as double-float
+// (x = xh + xl, ...), also 32 bytes so that both forms share the staging code.
+struct __align__(16) ImageRecF {
+    float xh, yh, zh;
+    uint32_t type;
+    float xl, yl, zl;
+    float pad;
+};
+static_assert(sizeof(ImageRecF) == 32, "image record must stay 32 bytes");
+
 struct GridGeom {
     Lattice L;
     int n[3];
-    double lo[3], hi[3];   // fractional extent of the binned image range
-    int nb[3];             // bins per axis
-    double binw[3];        // fractional bin width
-    double G[9];           // metric tensor a_i . a_j
-    float Gf[9];           // the same in FP32 (bin culling)
-    float lof[3], binwf[3];  // lo and binw in FP32 (bin culling)
-    float near2;           // (largest sigma + brick half-diagonal)^2: close-pass reach
+    double lo[3], hi[3];     // fractional extent of the binned image range
+    int nb[3];               // bins per axis
+    double binw[3];          // fractional bin width
+    float Gf[9];             // metric tensor a_i . a_j in FP32 (bin culling)
+    float Ginvf[3];          // 1 / G_ii
+    float lof[3], binwf[3], inv_binwf[3];  // lo, binw and 1 / binw in FP32
+    float inv_nf[3];         // 1 / n per axis
+    float hf[3];             // rc / L_perp per axis: the cutoff in fractional units
+    float keep2f;            // rc^2 plus the bin-culling margin
+    float hf_near[3];        // smax / L_perp: reach of the close-pair correction
+    float keep2_near;        // smax^2 plus the bin-culling margin
+    float rcf, rc2f, irc2f;  // rc, rc^2 and 1 / rc^2 in FP32
+    float smaxf;             // largest mixed sigma of the grid's guests (close-pair reach)
+    float sh[9], sl[9];      // row a: lattice vector a / n[a] as double-float (hi, lo)
     double rc, rc2;
     int bricks[3];
-    int n_types;           // framework LJ species in the table
+    int n_types;             // framework LJ species in the table
 };
 
 // ---------------------------------------------------------------- PTX helpers
@@ -115,11 +135,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // Lower bound on min |D . M|^2 over the fractional box D = [dlo, dhi]:
 // a few coordinate-descent sweeps of the convex quadratic D^T G D, then the
 // first-order bound f(x) + min_{y in box} grad(x).(y - x), which never exceeds
-// the true minimum. Exact for orthorhombic cells. FP32 (FP64 issues at a small
+// the true minimum whatever point x of the box the sweeps end on (so Ginv,
+// the reciprocal diagonal of G, need not be exact). Exact for orthorhombic cells. FP32 (FP64 issues at a small
 // fraction of the FP32 rate on this part); the caller compares against rc^2
 // with a relative margin far above FP32 rounding, so culling stays conservative.
-__device__ __forceinline__ float box_min_dist2_lb(const float* G, const float* dlo,
-                                                  const float* dhi) {
+__device__ __forceinline__ float box_min_dist2_lb(const float* G, const float* Ginv,
+                                                  const float* dlo, const float* dhi) {
     float x[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) x[i] = fminf(fmaxf(0.0f, dlo[i]), dhi[i]);
@@ -131,7 +152,7 @@ __device__ __forceinline__ float box_min_dist2_lb(const float* G, const float* d
 #pragma unroll
             for (int j = 0; j < 3; ++j)
                 if (j != i) s += G[3 * i + j] * x[j];
-            x[i] = fminf(fmaxf(-s / G[4 * i], dlo[i]), dhi[i]);
+            x[i] = fminf(fmaxf(-s * Ginv[i], dlo[i]), dhi[i]);
         }
     }
     float g[3];
@@ -189,108 +210,89 @@ struct alignas(16) ParamFF {
     float sig2_hi, sig2_lo, eps4_hi, eps4_lo, shift_hi, shift_lo, dvdrc, pad;
 };
 
-struct alignas(16) ParamF {
-    float sig2, eps4, shift, dvdrc;
+// The FP32 main loop's pair term: 4 eps ((sigma/r)^12 - (sigma/r)^6) =
+// r^-6 (A r^-6 - B) with A = 4 eps sigma^12 and B = 4 eps sigma^6: two FMAs
+// per guest species once r^-6 is known.
+struct alignas(16) ParamAB {
+    float a, b, shift, dvdrc;
 };
 
-template <typename Real>
-struct KernelSmem;
+// Approximate reciprocal (MUFU, relative error within 1 ulp; ftz).
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
-// ---------------------------------------------------------------- build kernel
-// Real = float: pair terms in FP32 on brick-local coordinates, per-tile FP32
-// partial sums folded into FP64. Real = double: the FP64 parity form on the
-// reference's global Cartesian coordinates.
-template <typename Real, int NG, int TRUNC>
-__global__ void __launch_bounds__(THREADS)
-grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
-                  const uint32_t* __restrict__ bin_start, const PairParams* __restrict__ params,
-                  const uint32_t* __restrict__ guests, double* __restrict__ tables,
-                  unsigned long long* __restrict__ executed, unsigned* flags) {
-    // dynamic shared memory (above the 48 KB static limit), carved by hand;
-    // the layout is mirrored by grid_smem_bytes<Real>() on the host
-    extern __shared__ __align__(128) unsigned char smem[];
-    unsigned char* sp = smem;
-    auto take = [&](size_t bytes) {
-        unsigned char* q = sp;
-        sp += (bytes + 127) & ~(size_t)127;
+// s * v for an FP32 scalar s and a double-float v.
+__device__ __forceinline__ ff ff_scale(float s, ff v) { return ff_mul(ff{s, 0.f}, v); }
+// a + b for a double-float a and an FP32 b.
+__device__ __forceinline__ ff ff_add_f(ff a, float b) {
+    ff s = ff_two_sum(a.hi, b);
+    s.lo = __fadd_rn(s.lo, a.lo);
+    return ff_fast(s.hi, s.lo);
+}
+
+// Node ownership inside a 16x8x8 brick: warp w covers the 8x4x4 sub-box
+// ((w&1)*8, ((w>>1)&1)*4, (w>>2)*4); lane l the column (l%8, l/8) of it and
+// NPT consecutive nodes along z. A compact sub-box keeps the warp's bounding
+// sphere small for the per-warp atom cull.
+__device__ __forceinline__ void thread_nodes(int tid, int& tx, int& ty, int& tz0) {
+    const int w = tid >> 5, l = tid & 31;
+    tx = (w & 1) * 8 + (l & 7);
+    ty = ((w >> 1) & 1) * 4 + (l >> 3);
+    tz0 = (w >> 2) * 4;
+}
+
+// Shared memory carved by hand (dynamic, above the 48 KB static limit); the
+// host mirrors each kernel's layout to size the launch.
+__host__ __device__ constexpr size_t carve(size_t bytes) { return (bytes + 127) & ~(size_t)127; }
+struct SmemCarve {
+    unsigned char* p;
+    template <typename T>
+    __device__ T* take(size_t n) {
+        T* q = reinterpret_cast<T*>(p);
+        p += carve(n * sizeof(T));
         return q;
-    };
-    ImageRec* raw = reinterpret_cast<ImageRec*>(take(2 * TILE * sizeof(ImageRec)));
-    float4* conv = reinterpret_cast<float4*>(take(TILE * sizeof(float4)));
-    float4* convlo = reinterpret_cast<float4*>(take((sizeof(Real) == 4 ? TILE : 1) * sizeof(float4)));
-    float* nlo = reinterpret_cast<float*>(take((sizeof(Real) == 4 ? NPT * 3 * THREADS : 1) * sizeof(float)));
-    uint64_t* bars = reinterpret_cast<uint64_t*>(take(2 * sizeof(uint64_t)));
-    uint32_t* row_begin = reinterpret_cast<uint32_t*>(take(MAX_ROWS * sizeof(uint32_t)));
-    uint32_t* row_off = reinterpret_cast<uint32_t*>(take((MAX_ROWS + 1) * sizeof(uint32_t)));
-    uint32_t* warp_tot = reinterpret_cast<uint32_t*>(take((THREADS / 32) * sizeof(uint32_t)));
-    ParamF* pf = reinterpret_cast<ParamF*>(take(64 * MAX_NG * sizeof(ParamF)));
-    float* rcl2 = reinterpret_cast<float*>(take(64 * sizeof(float)));
-    uint16_t* close_idx = reinterpret_cast<uint16_t*>(take(TILE * sizeof(uint16_t)));
-    PairParams* pd = reinterpret_cast<PairParams*>(take(64 * MAX_NG * sizeof(PairParams)));
-    ParamFF* pff = reinterpret_cast<ParamFF*>(pd);  // the FP32 form uses this slot instead
+    }
+};
 
+// ---------------------------------------------------------------- brick plan
+// The bin rows a brick can reach: one thread per (by, bz) row finds the first
+// and last bins within reach of the brick's nodes (FP32 lower bound on the
+// parallelepiped distance against keep2 = reach^2 plus a margin; reach_frac =
+// reach / L_perp per axis bounds the bin range), then an exclusive scan turns the
+// row lengths into offsets of one concatenated candidate list. Row slots
+// follow the row enumeration, so the candidate order (and the floating-point
+// summation order) is the same on every run. Returns the number of rows, or
+// -1 with the error flag raised when the brick touches more than MAX_ROWS
+// rows (the same on every thread). Every thread of the block calls it.
+__device__ int plan_rows(const GridGeom& geo, const float* reach_frac, float keep2,
+                         const uint32_t* __restrict__ bin_start, int x0, int y0, int z0,
+                         uint32_t* row_begin, uint32_t* row_off, uint32_t* warp_tot,
+                         unsigned* flags) {
     const int tid = threadIdx.x;
-    const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
-    const int brick = blockIdx.x;
-    const int bxn = geo.bricks[0], byn = geo.bricks[1];
-    const int bx = brick % bxn, by = (brick / bxn) % byn, bz = brick / (bxn * byn);
-    const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
-
-    // pair parameters for (framework type, guest g)
-    for (int i = tid; i < geo.n_types * NG; i += THREADS) {
-        const int t = i / NG, g = i % NG;
-        const PairParams p = params[(size_t)guests[g] * geo.n_types + t];
-        const double s2 = p.sigma * p.sigma;
-        pf[i] = ParamF{(float)s2, (float)(4.0 * p.eps), (float)p.shift, (float)p.dvdrc};
-        if (sizeof(Real) == 8) {
-            pd[i] = p;
-        } else {
-            const double e4 = 4.0 * p.eps;
-            const float s2h = (float)s2, e4h = (float)e4, shh = (float)p.shift;
-            pff[i] = ParamFF{s2h, (float)(s2 - s2h), e4h, (float)(e4 - e4h), shh,
-                             (float)(p.shift - shh), (float)p.dvdrc, 0.f};
-        }
-    }
-    __syncthreads();
-    // close-pair radius per framework type: r < sigma for some guest (s^2 > 1)
-    if (sizeof(Real) == 4)
-        for (int t = tid; t < geo.n_types; t += THREADS) {
-            float m = 0.f;
-            for (int g = 0; g < NG; ++g) m = fmaxf(m, pf[t * NG + g].sig2);
-            rcl2[t] = m;
-        }
-    if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_barrier_init();
-    }
-
-    // fractional extent of the brick's nodes
-    const int xe = min(x0 + BX, nx) - 1, ye = min(y0 + BY, ny) - 1, ze = min(z0 + BZ, nz) - 1;
-    double flo[3] = {(double)x0 / nx, (double)y0 / ny, (double)z0 / nz};
-    double fhi[3] = {(double)xe / nx, (double)ye / ny, (double)ze / nz};
+    const int lo_i[3] = {x0, y0, z0};
+    const int hi_i[3] = {min(x0 + BX, geo.n[0]) - 1, min(y0 + BY, geo.n[1]) - 1,
+                         min(z0 + BZ, geo.n[2]) - 1};
+    float flof[3], fhif[3];
     int blo[3], bhi[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const double h = geo.rc / geo.L.perp[a];
-        blo[a] = max(0, (int)floor((flo[a] - h - geo.lo[a]) / geo.binw[a]) - 1);
-        bhi[a] = min(geo.nb[a] - 1, (int)floor((fhi[a] + h - geo.lo[a]) / geo.binw[a]) + 1);
+        flof[a] = lo_i[a] * geo.inv_nf[a];
+        fhif[a] = hi_i[a] * geo.inv_nf[a];
+        // one bin of margin on each side covers the FP32 rounding here
+        blo[a] = max(0, (int)floorf((flof[a] - reach_frac[a] - geo.lof[a]) * geo.inv_binwf[a]) - 1);
+        bhi[a] = min(geo.nb[a] - 1,
+                     (int)floorf((fhif[a] + reach_frac[a] - geo.lof[a]) * geo.inv_binwf[a]) + 1);
     }
     const int rows_y = bhi[1] - blo[1] + 1, rows_z = bhi[2] - blo[2] + 1;
-    const int total_rows = rows_y * rows_z;
-    __syncthreads();
-
-    // one thread per bin row: find the first and last bins within reach.
-    // Row slots follow the row enumeration, so the candidate order (and the
-    // floating-point summation order) is the same on every run.
-    if (total_rows > MAX_ROWS) {
+    const int nr = rows_y * rows_z;
+    if (nr > MAX_ROWS) {
         if (tid == 0) flag_error(flags, DEV_ERR_CAPACITY);
-        return;
+        return -1;
     }
-    const float keep2 = (float)(geo.rc2 * (1.0 + 1e-3) + 1e-2);
-    const float flof[3] = {(float)flo[0], (float)flo[1], (float)flo[2]};
-    const float fhif[3] = {(float)fhi[0], (float)fhi[1], (float)fhi[2]};
-    for (int r = tid; r < total_rows; r += THREADS) {
+    for (int r = tid; r < nr; r += THREADS) {
         const int ry = blo[1] + r % rows_y, rz = blo[2] + r / rows_y;
         int first = -1, last = -1;
         float dlo[3], dhi[3];
@@ -305,7 +307,7 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
             const float b0 = geo.lof[0] + rx * geo.binwf[0];
             dlo[0] = b0 - fhif[0];
             dhi[0] = b0 + geo.binwf[0] - flof[0];
-            if (box_min_dist2_lb(geo.Gf, dlo, dhi) <= keep2) {
+            if (box_min_dist2_lb(geo.Gf, geo.Ginvf, dlo, dhi) <= keep2) {
                 if (first < 0) first = rx;
                 last = rx;
             }
@@ -322,7 +324,6 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
     __syncthreads();
     // exclusive scan of the row counts: each thread sums a run of rows, a
     // warp scan over those sums, then a scan of the warp totals
-    const int nr = total_rows;
     {
         constexpr int PER = (MAX_ROWS + THREADS - 1) / THREADS;
         const int r0 = tid * PER;
@@ -349,244 +350,143 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
         if (tid == 0) row_off[0] = 0;
     }
     __syncthreads();
+    return nr;
+}
+
+// Stages tile t of the brick's concatenated candidate list (32-byte records)
+// into dst: one bulk copy per overlapping row range, completing on bar.
+__device__ void issue_tile(uint32_t t, uint32_t n_cand, int nr, const uint32_t* row_begin,
+                           const uint32_t* row_off, const unsigned char* images,
+                           unsigned char* dst, uint64_t* bar) {
+    constexpr uint32_t REC = 32;
+    const uint32_t a = t * TILE;
+    const uint32_t b = min(a + (uint32_t)TILE, n_cand);
+    mbar_expect_tx(bar, (b - a) * REC);
+    int lo = 0, hi = nr - 1;  // last row with row_off[r] <= a
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (row_off[mid] <= a) lo = mid; else hi = mid - 1;
+    }
+    for (int r = lo; r < nr && row_off[r] < b; ++r) {
+        const uint32_t s = max(row_off[r], a), e = min(row_off[r + 1], b);
+        if (e > s)
+            bulk_g2s(dst + (size_t)(s - a) * REC,
+                     images + (size_t)(row_begin[r] + (s - row_off[r])) * REC, (e - s) * REC, bar);
+    }
+}
+
+// After a timed-out wait: tiles failed_tile and failed_tile + 1 are the only
+// ones issued and not consumed; wait for each (again bounded) before exit.
+__device__ void drain_tiles(uint32_t failed_tile, uint32_t n_tiles, uint64_t* bars) {
+    if (threadIdx.x == 0)
+        for (uint32_t t = failed_tile; t < failed_tile + 2 && t < n_tiles; ++t)
+            for (unsigned it = 0; it < WAIT_LIMIT && !mbar_try_wait(&bars[t & 1], (t >> 1) & 1); ++it)
+                __nanosleep(64);
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- FP64 build kernel
+// The parity form: the reference's node positions and pairEnergy in FP64 on
+// global Cartesian coordinates, candidates in a fixed order.
+template <int NG, int TRUNC>
+__global__ void __launch_bounds__(THREADS, 2)
+grid_build_f64_kernel(GridGeom geo, const ImageRec* __restrict__ images,
+                      const uint32_t* __restrict__ bin_start, const PairParams* __restrict__ params,
+                      const uint32_t* __restrict__ guests, double* __restrict__ tables,
+                      unsigned long long* __restrict__ executed, unsigned* flags) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    SmemCarve sc{smem};
+    ImageRec* raw = sc.take<ImageRec>(2 * TILE);
+    uint64_t* bars = sc.take<uint64_t>(2);
+    uint32_t* row_begin = sc.take<uint32_t>(MAX_ROWS);
+    uint32_t* row_off = sc.take<uint32_t>(MAX_ROWS + 1);
+    uint32_t* warp_tot = sc.take<uint32_t>(THREADS / 32);
+    PairParams* pd = sc.take<PairParams>(64 * NG);
+
+    const int tid = threadIdx.x;
+    const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
+    const int brick = blockIdx.x;
+    const int bxn = geo.bricks[0], byn = geo.bricks[1];
+    const int bx = brick % bxn, by = (brick / bxn) % byn, bz = brick / (bxn * byn);
+    const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
+
+    for (int i = tid; i < geo.n_types * NG; i += THREADS) {
+        const int t = i / NG, g = i % NG;
+        pd[i] = params[(size_t)guests[g] * geo.n_types + t];
+    }
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    const int nr = plan_rows(geo, geo.hf, geo.keep2f, bin_start, x0, y0, z0, row_begin, row_off,
+                             warp_tot, flags);
+    if (nr < 0) return;
     const uint32_t n_cand = row_off[nr];
 
-    // this thread's nodes
-    const int tx = tid % BX, ty = (tid / BX) % BY, tz = tid / (BX * BY);
+    int tx, ty, tz0;
+    thread_nodes(tid, tx, ty, tz0);
     const int ixn = x0 + tx, iyn = y0 + ty;
+    const double* M = geo.L.m;
+    double nxr[NPT], nyr[NPT], nzr[NPT];
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) {
+        // framework_energy_grid.cc:227-231 node position
+        const int izn = z0 + tz0 + k;
+        const double f0 = (double)ixn / nx, f1 = (double)iyn / ny, f2 = (double)izn / nz;
+        double c[3];
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc)
+            c[cc] = add_rn(add_rn(mul_rn(f0, M[cc]), mul_rn(f1, M[3 + cc])), mul_rn(f2, M[6 + cc]));
+        nxr[k] = c[0];
+        nyr[k] = c[1];
+        nzr[k] = c[2];
+    }
     double acc[NG][NPT];
 #pragma unroll
     for (int g = 0; g < NG; ++g)
 #pragma unroll
         for (int k = 0; k < NPT; ++k) acc[g][k] = 0.0;
 
-    // Brick centre (origin of the FP32 form's local coordinates: the atoms
-    // that matter most, the close ones, then have the smallest coordinates and
-    // the smallest rounding) and node coordinates.
-    const double* M = geo.L.m;
-    double ox = 0, oy = 0, oz = 0;
-    Real nxr[NPT], nyr[NPT], nzr[NPT];
-    {
-        const double cx = x0 + 0.5 * (BX - 1), cy = y0 + 0.5 * (BY - 1), cz = z0 + 0.5 * (BZ - 1);
-        const double f0o = cx / nx, f1o = cy / ny, f2o = cz / nz;
-        ox = f0o * M[0] + f1o * M[3] + f2o * M[6];
-        oy = f0o * M[1] + f1o * M[4] + f2o * M[7];
-        oz = f0o * M[2] + f1o * M[5] + f2o * M[8];
-#pragma unroll
-        for (int k = 0; k < NPT; ++k) {
-            const int izn = z0 + tz + 2 * k;
-            if (sizeof(Real) == 4) {
-                const double d0 = (ixn - cx) / nx, d1 = (iyn - cy) / ny, d2 = (izn - cz) / nz;
-                const double lx = d0 * M[0] + d1 * M[3] + d2 * M[6];
-                const double ly = d0 * M[1] + d1 * M[4] + d2 * M[7];
-                const double lz = d0 * M[2] + d1 * M[5] + d2 * M[8];
-                nxr[k] = (Real)lx;
-                nyr[k] = (Real)ly;
-                nzr[k] = (Real)lz;
-                nlo[(k * 3 + 0) * THREADS + tid] = (float)(lx - (double)nxr[k]);
-                nlo[(k * 3 + 1) * THREADS + tid] = (float)(ly - (double)nyr[k]);
-                nlo[(k * 3 + 2) * THREADS + tid] = (float)(lz - (double)nzr[k]);
-                continue;
-            }
-            // framework_energy_grid.cc:227-231 node position
-            const double f0 = (double)ixn / nx, f1 = (double)iyn / ny, f2 = (double)izn / nz;
-            double c[3];
-#pragma unroll
-            for (int cc = 0; cc < 3; ++cc)
-                c[cc] = add_rn(add_rn(mul_rn(f0, M[cc]), mul_rn(f1, M[3 + cc])), mul_rn(f2, M[6 + cc]));
-            {
-                nxr[k] = (Real)c[0];
-                nyr[k] = (Real)c[1];
-                nzr[k] = (Real)c[2];
-            }
-        }
-    }
-
-    // stage tile `t` of the concatenated candidate list into raw[buf]
-    auto issue = [&](uint32_t t, int buf) {
-        const uint32_t a = t * TILE;
-        const uint32_t b = min(a + (uint32_t)TILE, n_cand);
-        mbar_expect_tx(&bars[buf], (b - a) * (uint32_t)sizeof(ImageRec));
-        // rows overlapping [a, b)
-        int r = 0;
-        {
-            int lo = 0, hi = nr - 1;  // last row with row_off[r] <= a
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) / 2;
-                if (row_off[mid] <= a) lo = mid; else hi = mid - 1;
-            }
-            r = lo;
-        }
-        for (; r < nr && row_off[r] < b; ++r) {
-            const uint32_t s = max(row_off[r], a), e = min(row_off[r + 1], b);
-            if (e > s)
-                bulk_g2s(&raw[buf * TILE + (s - a)], images + row_begin[r] + (s - row_off[r]),
-                         (e - s) * (uint32_t)sizeof(ImageRec), &bars[buf]);
-        }
-    };
-
+    const unsigned char* img = reinterpret_cast<const unsigned char*>(images);
+    unsigned char* rawb = reinterpret_cast<unsigned char*>(raw);
     const uint32_t n_tiles = (n_cand + TILE - 1) / TILE;
     if (tid == 0) {
-        if (n_tiles > 0) issue(0, 0);
-        if (n_tiles > 1) issue(1, 1);
+        if (n_tiles > 0) issue_tile(0, n_cand, nr, row_begin, row_off, img, rawb, &bars[0]);
+        if (n_tiles > 1)
+            issue_tile(1, n_cand, nr, row_begin, row_off, img, rawb + TILE * sizeof(ImageRec), &bars[1]);
     }
-    const float rc2f = (float)geo.rc2;
-    const float rcf = (float)geo.rc;
-    bool ok = true;
-    uint32_t failed_tile = 0;
-
     for (uint32_t t = 0; t < n_tiles; ++t) {
         const int buf = t & 1;
         const uint32_t cnt = min((uint32_t)TILE, n_cand - t * TILE);
         // block-wide vote so that every thread takes the same path on a timeout
         const bool got = mbar_wait_bounded(&bars[buf], (t >> 1) & 1, flags);
         if (!__syncthreads_and(got)) {
-            ok = false;
-            failed_tile = t;
-            break;
+            drain_tiles(t, n_tiles, bars);
+            return;
         }
-        if (sizeof(Real) == 4) {
-            // convert to brick-centred FP32 (hi + lo parts) and list, in atom
-            // order, the atoms that can be closer than sigma to a node of this
-            // brick (within reach of the brick centre)
-            static_assert(TILE == THREADS, "one atom per thread in the conversion pass");
-            bool near = false;
-            if ((uint32_t)tid < cnt) {
-                const ImageRec r = raw[buf * TILE + tid];
-                const double lx = r.x - ox, ly = r.y - oy, lz = r.z - oz;
-                const float hx = (float)lx, hy = (float)ly, hz = (float)lz;
-                conv[tid] = make_float4(hx, hy, hz, __int_as_float((int)r.type));
-                convlo[tid] = make_float4((float)(lx - hx), (float)(ly - hy), (float)(lz - hz), 0.f);
-                near = fmaf(hx, hx, fmaf(hy, hy, hz * hz)) < geo.near2;
-            }
-            const unsigned ballot = __ballot_sync(0xffffffffu, near);
-            if ((tid & 31) == 0) warp_tot[tid >> 5] = __popc(ballot);
-            __syncthreads();
-            if (near) {
-                uint32_t off = __popc(ballot & ((1u << (tid & 31)) - 1u));
-                for (int w = 0; w < (tid >> 5); ++w) off += warp_tot[w];
-                close_idx[off] = (uint16_t)tid;
-            }
-            uint32_t n_close = 0;
-            for (int w = 0; w < THREADS / 32; ++w) n_close += warp_tot[w];
-            __syncthreads();
-            // raw[buf] is free again: prefetch tile t + 2 while computing
-            if (tid == 0 && t + 2 < n_tiles) {
-                fence_proxy_async();
-                issue(t + 2, buf);
-            }
-            float part[NG][NPT];
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const ImageRec a = raw[buf * TILE + j];
+            const PairParams* pp = &pd[a.type * NG];
 #pragma unroll
-            for (int g = 0; g < NG; ++g)
+            for (int k = 0; k < NPT; ++k) {
+                const double dx = a.x - nxr[k];
+                const double dy = a.y - nyr[k];
+                const double dz = a.z - nzr[k];
+                const double r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 > geo.rc2 * (1.0 + 1e-12)) continue;
+                const double r = sqrt(r2);
 #pragma unroll
-                for (int k = 0; k < NPT; ++k) part[g][k] = 0.f;
-#pragma unroll 2
-            for (uint32_t j = 0; j < cnt; ++j) {
-                const float4 a = conv[j];
-                const int type = __float_as_int(a.w);
-                const float close2 = rcl2[type];
-                ParamF p[NG];
-#pragma unroll
-                for (int g = 0; g < NG; ++g) p[g] = pf[type * NG + g];
-#pragma unroll
-                for (int k = 0; k < NPT; ++k) {
-                    const float dx = a.x - (float)nxr[k];
-                    const float dy = a.y - (float)nyr[k];
-                    const float dz = a.z - (float)nzr[k];
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const float inv = __frcp_rn(fmaxf(r2, 1e-4f));
-                    // pairs closer than sigma are left to the close pass below
-                    const bool in = (r2 <= rc2f) && (r2 >= close2);
-#pragma unroll
-                    for (int g = 0; g < NG; ++g) {
-                        const float s2 = p[g].sig2 * inv;
-                        const float s6 = s2 * s2 * s2;
-                        float e = fmaf(p[g].eps4, fmaf(s6, s6, -s6), -p[g].shift);
-                        if (TRUNC == ALEA_LINEAR_FORCE_SHIFTED) {
-                            const float r = r2 * rsqrtf(fmaxf(r2, 1e-4f));
-                            e = fmaf(-(r - rcf), p[g].dvdrc, e);
-                        }
-                        part[g][k] += in ? e : 0.f;
-                    }
-                }
-            }
-            // close pass: the few listed atoms, pairs closer than sigma in
-            // double-float, straight into the FP64 accumulators
-            for (uint32_t c = 0; c < n_close; ++c) {
-                const uint32_t j = close_idx[c];
-                const float4 a = conv[j];
-                const int type = __float_as_int(a.w);
-                const float close2 = rcl2[type];
-#pragma unroll
-                for (int k = 0; k < NPT; ++k) {
-                    const float dx = a.x - (float)nxr[k];
-                    const float dy = a.y - (float)nyr[k];
-                    const float dz = a.z - (float)nzr[k];
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    if (r2 < close2) {
-                        const float4 al = convlo[j];
-                        const ff ddx = ff_add(ff{a.x, al.x}, ff{-(float)nxr[k], -nlo[(k * 3 + 0) * THREADS + tid]});
-                        const ff ddy = ff_add(ff{a.y, al.y}, ff{-(float)nyr[k], -nlo[(k * 3 + 1) * THREADS + tid]});
-                        const ff ddz = ff_add(ff{a.z, al.z}, ff{-(float)nzr[k], -nlo[(k * 3 + 2) * THREADS + tid]});
-                        ff rr = ff_add(ff_add(ff_mul(ddx, ddx), ff_mul(ddy, ddy)), ff_mul(ddz, ddz));
-                        if (rr.hi < 1e-4f) rr = ff{1e-4f, 0.f};
-                        const ff iv = ff_rcp(rr);
-#pragma unroll
-                        for (int g = 0; g < NG; ++g) {
-                            const ParamFF q = pff[type * NG + g];
-                            const ff s2 = ff_mul(ff{q.sig2_hi, q.sig2_lo}, iv);
-                            const ff s6 = ff_mul(ff_mul(s2, s2), s2);
-                            const ff t = ff_mul(s6, ff_add(s6, ff{-1.f, 0.f}));
-                            ff e = ff_add(ff_mul(ff{q.eps4_hi, q.eps4_lo}, t), ff{-q.shift_hi, -q.shift_lo});
-                            if (TRUNC == ALEA_LINEAR_FORCE_SHIFTED) {
-                                const float r = sqrtf(rr.hi);
-                                e = ff_add(e, ff{-(r - rcf) * q.dvdrc, 0.f});
-                            }
-                            acc[g][k] += (double)e.hi + (double)e.lo;
-                        }
-                    }
-                }
-            }
-#pragma unroll
-            for (int g = 0; g < NG; ++g)
-#pragma unroll
-                for (int k = 0; k < NPT; ++k) acc[g][k] += (double)part[g][k];
-            __syncthreads();  // conv reused by the next tile
-        } else {
-            for (uint32_t j = 0; j < cnt; ++j) {
-                const ImageRec a = raw[buf * TILE + j];
-                const PairParams* pp = &pd[a.type * NG];
-#pragma unroll
-                for (int k = 0; k < NPT; ++k) {
-                    const double dx = a.x - (double)nxr[k];
-                    const double dy = a.y - (double)nyr[k];
-                    const double dz = a.z - (double)nzr[k];
-                    const double r2 = dx * dx + dy * dy + dz * dz;
-                    if (r2 > geo.rc2 * (1.0 + 1e-12)) continue;
-                    const double r = sqrt(r2);
-#pragma unroll
-                    for (int g = 0; g < NG; ++g) acc[g][k] += lj_pair<TRUNC>(r, geo.rc, pp[g]);
-                }
-            }
-            __syncthreads();
-            if (tid == 0 && t + 2 < n_tiles) {
-                fence_proxy_async();
-                issue(t + 2, buf);
+                for (int g = 0; g < NG; ++g) acc[g][k] += lj_pair<TRUNC>(r, geo.rc, pp[g]);
             }
         }
-    }
-    if (!ok) {
-        // Drain this block's copies still in flight (tiles failed_tile and
-        // failed_tile + 1 are the only ones issued and not yet consumed),
-        // each wait again bounded, before the block exits.
-        if (tid == 0)
-            for (uint32_t t = failed_tile; t < failed_tile + 2 && t < n_tiles; ++t)
-                for (unsigned it = 0; it < WAIT_LIMIT && !mbar_try_wait(&bars[t & 1], (t >> 1) & 1);
-                     ++it) {
-                    __nanosleep(64);
-                }
         __syncthreads();
-        return;
+        if (tid == 0 && t + 2 < n_tiles) {
+            fence_proxy_async();
+            issue_tile(t + 2, n_cand, nr, row_begin, row_off, img, rawb + buf * TILE * sizeof(ImageRec),
+                       &bars[buf]);
+        }
     }
 
     // store min(E, cap) (framework_energy_grid.cc:22, 243)
@@ -594,7 +494,7 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
     const size_t per_table = plane * nz;
 #pragma unroll
     for (int k = 0; k < NPT; ++k) {
-        const int izn = z0 + tz + 2 * k;
+        const int izn = z0 + tz0 + k;
         if (ixn < nx && iyn < ny && izn < nz) {
             const size_t idx = (size_t)izn * plane + (size_t)iyn * nx + ixn;
 #pragma unroll
@@ -605,10 +505,665 @@ grid_build_kernel(GridGeom geo, const ImageRec* __restrict__ images,
         }
     }
     if (tid == 0) {
-        const unsigned long long active =
-            (unsigned long long)(xe - x0 + 1) * (ye - y0 + 1) * (ze - z0 + 1);
+        const unsigned long long active = (unsigned long long)(min(x0 + BX, nx) - x0) *
+                                          (min(y0 + BY, ny) - y0) * (min(z0 + BZ, nz) - z0);
         atomicAdd(executed, active * n_cand);
     }
+}
+
+template <int NG>
+constexpr size_t f64_smem_bytes() {
+    return carve(2 * TILE * sizeof(ImageRec)) + carve(2 * sizeof(uint64_t)) +
+           carve(MAX_ROWS * sizeof(uint32_t)) + carve((MAX_ROWS + 1) * sizeof(uint32_t)) +
+           carve((THREADS / 32) * sizeof(uint32_t)) + carve(64 * NG * sizeof(PairParams));
+}
+
+// ---------------------------------------------------------------- packed FP32
+// Two FP32 lanes in one 64-bit register (PTX .f32x2, sm_100 family): one
+// instruction adds, multiplies or fuses two lanes, each rounded exactly as the
+// scalar instruction would round it. The FP32 kernel keeps the nodes k and
+// k + 1 of a thread in the two lanes.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 f2_pack(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// ---------------------------------------------------------------- FP32 build: shared pieces
+// The FP32 form runs in two kernels, the sweep and the close-pair correction,
+// which must classify every (atom, node) pair identically. Both therefore
+// build positions and r^2 with the same explicitly rounded operations below
+// (no contraction can differ between them).
+
+// Per (framework type t, guest g) parameters in shared memory, and per type
+// the FP32 window's inner edge sigma_t^2 (the largest sigma^2 over the
+// guests) with the value the sweep adds for a pair clamped to it.
+template <int NG, int TRUNC>
+struct F32Params {
+    ulonglong2 ab[64 * NG];  // {A, A}, {-B, -B}
+    float shift[64 * NG];
+    float dvdrc[64 * NG];
+    float vclose[64 * NG];
+    ParamFF pff[64 * NG];
+    float close2[64];
+};
+
+template <int NG, int TRUNC>
+__device__ void load_f32_params(F32Params<NG, TRUNC>& P, const ParamAB* __restrict__ pab_g,
+                                const ParamFF* __restrict__ pff_g, int nt, float rcf) {
+    const int tid = threadIdx.x;
+    for (int i = tid; i < nt * NG; i += THREADS) {
+        const int t = i / NG, g = i % NG;
+        const ParamAB p = pab_g[(size_t)g * nt + t];
+        P.ab[i] = make_ulonglong2(f2_pack(p.a, p.a), f2_pack(-p.b, -p.b));
+        P.shift[i] = TRUNC == ALEA_TRUNCATED ? 0.f : p.shift;
+        P.dvdrc[i] = p.dvdrc;
+        P.pff[i] = pff_g[(size_t)g * nt + t];
+    }
+    __syncthreads();
+    // the sweep's operations, in its order, at r^2 = sigma_t^2
+    for (int t = tid; t < nt; t += THREADS) {
+        float m = 0.f;
+        for (int g = 0; g < NG; ++g) m = fmaxf(m, P.pff[t * NG + g].sig2_hi);
+        P.close2[t] = m;
+        const float ir2 = rcp_approx(m);
+        const float ir6 = __fmul_rn(ir2, __fmul_rn(ir2, ir2));
+        for (int g = 0; g < NG; ++g) {
+            float a, nb, dummy;
+            f2_unpack(P.ab[t * NG + g].x, a, dummy);
+            f2_unpack(P.ab[t * NG + g].y, nb, dummy);
+            float v = __fmul_rn(ir6, __fmaf_rn(a, ir6, nb));
+            if (TRUNC == ALEA_LINEAR_FORCE_SHIFTED)
+                v = __fmaf_rn(-P.dvdrc[t * NG + g], __fsub_rn(__fmul_rn(m, rsqrtf(m)), rcf), v);
+            P.vclose[t * NG + g] = v;
+        }
+    }
+    __syncthreads();
+}
+
+// The brick centre (x0 + 7.5, y0 + 3.5, z0 + 3.5 in node units) in
+// double-float: sum over axes of (centre index) x (lattice vector / n).
+__device__ __forceinline__ void brick_origin(const GridGeom& geo, int x0, int y0, int z0, ff* org) {
+    const float cen[3] = {x0 + 0.5f * (BX - 1), y0 + 0.5f * (BY - 1), z0 + 0.5f * (BZ - 1)};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        ff v = ff_scale(cen[0], ff{geo.sh[c], geo.sl[c]});
+        v = ff_add(v, ff_scale(cen[1], ff{geo.sh[3 + c], geo.sl[3 + c]}));
+        org[c] = ff_add(v, ff_scale(cen[2], ff{geo.sh[6 + c], geo.sl[6 + c]}));
+    }
+}
+
+// A node relative to the brick centre, from its offsets (small half-integers,
+// exact in FP32), as double-float components.
+__device__ __forceinline__ void node_local(const GridGeom& geo, float dxi, float dyi, float dzi,
+                                           ff* v) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        ff w = ff_scale(dxi, ff{geo.sh[c], geo.sl[c]});
+        w = ff_add(w, ff_scale(dyi, ff{geo.sh[3 + c], geo.sl[3 + c]}));
+        v[c] = ff_add(w, ff_scale(dzi, ff{geo.sh[6 + c], geo.sl[6 + c]}));
+    }
+}
+
+// An image relative to the brick centre, as double-float components.
+__device__ __forceinline__ void atom_local(const ImageRecF& r, const ff* org, ff* v) {
+    v[0] = ff_add(ff{r.xh, r.xl}, ff{-org[0].hi, -org[0].lo});
+    v[1] = ff_add(ff{r.yh, r.yl}, ff{-org[1].hi, -org[1].lo});
+    v[2] = ff_add(ff{r.zh, r.zl}, ff{-org[2].hi, -org[2].lo});
+}
+
+// FP32 r^2 from the hi parts, rounded exactly as the packed sweep rounds it.
+__device__ __forceinline__ float r2_f32(float ax, float ay, float az, float nx, float ny, float nz) {
+    const float dx = __fsub_rn(ax, nx), dy = __fsub_rn(ay, ny), dz = __fsub_rn(az, nz);
+    return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+}
+
+// Double-float energy of one close pair for one guest, shift (and the linear
+// force shift) included, minus what the sweep adds for it (vclose) and plus
+// the -V(rc) the sweep charges every pair: the correction that turns the
+// sweep's value for this pair into the exact one.
+template <int NG, int TRUNC>
+__device__ __forceinline__ ff close_pair(const F32Params<NG, TRUNC>& P, int type, int g, ff ddx,
+                                         ff ddy, ff ddz, float rcf) {
+    ff rr = ff_add(ff_add(ff_mul(ddx, ddx), ff_mul(ddy, ddy)), ff_mul(ddz, ddz));
+    if (rr.hi < 1e-4f) rr = ff{1e-4f, 0.f};
+    const ff iv = ff_rcp(rr);
+    const ParamFF q = P.pff[type * NG + g];
+    const ff s2 = ff_mul(ff{q.sig2_hi, q.sig2_lo}, iv);
+    const ff s6 = ff_mul(ff_mul(s2, s2), s2);
+    const ff tt = ff_mul(s6, ff_add(s6, ff{-1.f, 0.f}));
+    ff e = ff_add(ff_mul(ff{q.eps4_hi, q.eps4_lo}, tt), ff{-q.shift_hi, -q.shift_lo});
+    if (TRUNC == ALEA_LINEAR_FORCE_SHIFTED) {
+        const float rs = sqrtf(rr.hi);
+        e = ff_add(e, ff{-(rs - rcf) * q.dvdrc, 0.f});
+    }
+    e = ff_add_f(e, -P.vclose[type * NG + g]);
+    return ff_add_f(e, P.shift[type * NG + g]);
+}
+
+// Nodes whose FP32 close-pair estimate |ce| stays within this multiple of
+// max(floor, |E|) keep the FP32 sum; the others get the double-float
+// correction. The estimate's FP32 error stays within about 1.5e-6 |ce|, so
+// within 3e-6 x max(floor, |E|) here. (On dense frameworks about 1-2% of the
+// nodes exceed the ratio: nodes near 0 K with a few strongly repulsive pairs.)
+constexpr float CLOSE_FP32_RATIO = 2.0f;
+constexpr float CLOSE_FP32_FLOOR = 300.0f;  // K
+
+// ---------------------------------------------------------------- FP32 sweep kernel
+// Pair terms in FP32 on brick-centred coordinates, double-float where a
+// rounding error would reach the result (image and node positions, the
+// per-node accumulators). FP64 issues at a small fraction of the FP32 rate on
+// this part, so the only FP64 operations left are the final stores.
+//
+// Per tile of 256 candidates each thread converts one record to brick-centred
+// FP32 (hi + lo parts); then every warp walks the tile, skipping atoms beyond
+// rc + (its sub-box radius) of its sub-box centre (a warp-uniform branch).
+// For each remaining atom and node:
+//   * r^2 is clamped to [sigma_t^2, rc^2] (sigma_t: the atom type's largest
+//     sigma over the guests) and r^-6 (A r^-6 - B) evaluated in FP32 at the
+//     clamped value, two nodes per instruction;
+//   * every evaluated pair is charged -V(rc) (the shift; summed per atom, not
+//     per pair), so a pair beyond rc contributes V(rc) - V(rc) = 0 to FP32
+//     rounding and a pair within the window V(r) - V(rc);
+//   * for a pair closer than sigma_t (only atoms within sigma_t + radius of
+//     the warp centre can have one: a warp-uniform branch) the exact value
+//     minus the clamped one is estimated in FP32 into a separate per-node sum.
+// Per node and guest the result is then: the sweep's sum when there is no
+// close pair; the cap when sum + estimate exceeds it by 1%; sum + estimate
+// when the estimate is small against max(300 K, |E|); otherwise the sweep's
+// sum is stored and the node flagged for grid_close_fix_kernel.
+// With plain truncation a pair beyond rc gets r^-2 = 0 instead (no shift).
+// Linear force shifting adds -(r - rc) V'(rc) per pair at the clamped r.
+template <int NG, int TRUNC>
+__global__ void __launch_bounds__(THREADS, 4)
+grid_build_f32_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
+                      const uint32_t* __restrict__ bin_start, const ParamAB* __restrict__ pab_g,
+                      const ParamFF* __restrict__ pff_g, double* __restrict__ tables,
+                      uint8_t* __restrict__ fix, unsigned long long* __restrict__ executed,
+                      unsigned* flags) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    SmemCarve sc{smem};
+    ImageRecF* raw = sc.take<ImageRecF>(2 * TILE);
+    ulonglong2* cxy = sc.take<ulonglong2>(TILE);   // {x, x}, {y, y}
+    ulonglong2* czt = sc.take<ulonglong2>(TILE);   // {z, z}, {type, 0}
+    uint64_t* bars = sc.take<uint64_t>(2);
+    uint32_t* row_begin = sc.take<uint32_t>(MAX_ROWS);
+    uint32_t* row_off = sc.take<uint32_t>(MAX_ROWS + 1);
+    uint32_t* warp_tot = sc.take<uint32_t>(THREADS / 32);
+    F32Params<NG, TRUNC>& P = *sc.take<F32Params<NG, TRUNC>>(1);
+    // double-float sweep sums (touched once per tile): hi at [(g NPT + k) 2 + 0]
+    // x THREADS + tid, lo at [... + 1]
+    float* accs = sc.take<float>(2 * NG * NPT * THREADS);
+
+    const int tid = threadIdx.x;
+    const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
+    const int brick = blockIdx.x;
+    const int bxn = geo.bricks[0], byn = geo.bricks[1];
+    const int bx = brick % bxn, by = (brick / bxn) % byn, bz = brick / (bxn * byn);
+    const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
+    const float rc2f = geo.rc2f, rcf = geo.rcf;
+    auto acc_hi = [&](int g, int k) -> float& { return accs[((g * NPT + k) * 2) * THREADS + tid]; };
+    auto acc_lo = [&](int g, int k) -> float& { return accs[((g * NPT + k) * 2 + 1) * THREADS + tid]; };
+
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_barrier_init();
+    }
+    load_f32_params(P, pab_g, pff_g, geo.n_types, rcf);
+    const int nr = plan_rows(geo, geo.hf, geo.keep2f, bin_start, x0, y0, z0, row_begin, row_off,
+                             warp_tot, flags);
+    if (nr < 0) return;
+    const uint32_t n_cand = row_off[nr];
+
+    int tx, ty, tz0;
+    thread_nodes(tid, tx, ty, tz0);
+    const int ixn = x0 + tx, iyn = y0 + ty;
+    ff org[3];
+    brick_origin(geo, x0, y0, z0, org);
+    constexpr int NP = NPT / 2;  // node pairs per thread: nodes 2q and 2q + 1
+    f2 NX[NP], NY[NP], NZ[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        ff v0[3], v1[3];
+        node_local(geo, tx - 0.5f * (BX - 1), ty - 0.5f * (BY - 1), tz0 + 2 * q - 0.5f * (BZ - 1), v0);
+        node_local(geo, tx - 0.5f * (BX - 1), ty - 0.5f * (BY - 1), tz0 + 2 * q + 1 - 0.5f * (BZ - 1), v1);
+        NX[q] = f2_pack(v0[0].hi, v1[0].hi);
+        NY[q] = f2_pack(v0[1].hi, v1[1].hi);
+        NZ[q] = f2_pack(v0[2].hi, v1[2].hi);
+    }
+    // the warp's bounding sphere: centre of its 8x4x4 sub-box, radius over its
+    // nodes; 1e-3 A of margin covers FP32 rounding in the two reach tests
+    float wcx, wcy, wcz, cull2, near2;
+    {
+        const int w = tid >> 5;
+        const float wd0 = (w & 1) * 8 + 3.5f - 0.5f * (BX - 1);
+        const float wd1 = ((w >> 1) & 1) * 4 + 1.5f - 0.5f * (BY - 1);
+        const float wd2 = (w >> 2) * 4 + 1.5f - 0.5f * (BZ - 1);
+        wcx = wd0 * geo.sh[0] + wd1 * geo.sh[3] + wd2 * geo.sh[6];
+        wcy = wd0 * geo.sh[1] + wd1 * geo.sh[4] + wd2 * geo.sh[7];
+        wcz = wd0 * geo.sh[2] + wd1 * geo.sh[5] + wd2 * geo.sh[8];
+        float r2max = 0.f;
+#pragma unroll
+        for (int k = 0; k < NPT; ++k) {
+            float px, py, pz, d0, d1, d2;
+            f2_unpack(NX[k / 2], d0, px);
+            f2_unpack(NY[k / 2], d1, py);
+            f2_unpack(NZ[k / 2], d2, pz);
+            if ((k & 1) == 0) {
+                px = d0;
+                py = d1;
+                pz = d2;
+            }
+            const float ex = px - wcx, ey = py - wcy, ez = pz - wcz;
+            r2max = fmaxf(r2max, fmaf(ex, ex, fmaf(ey, ey, ez * ez)));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r2max = fmaxf(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
+        const float rad = sqrtf(r2max) + 1e-3f;
+        cull2 = (geo.rcf + rad) * (geo.rcf + rad) * (1.0f + 1e-5f);
+        near2 = (geo.smaxf + rad) * (geo.smaxf + rad) * (1.0f + 1e-5f);
+    }
+
+    float ce[NG][NPT];               // FP32 close-pair estimates
+    uint32_t has_close = 0;          // bit k: node k has a close pair
+#pragma unroll
+    for (int g = 0; g < NG; ++g)
+#pragma unroll
+        for (int k = 0; k < NPT; ++k) {
+            acc_hi(g, k) = acc_lo(g, k) = 0.f;
+            ce[g][k] = 0.f;
+        }
+    uint32_t passes = 0;  // atoms this warp evaluated
+
+    const unsigned char* img = reinterpret_cast<const unsigned char*>(images);
+    unsigned char* rawb = reinterpret_cast<unsigned char*>(raw);
+    const uint32_t n_tiles = (n_cand + TILE - 1) / TILE;
+    if (tid == 0) {
+        if (n_tiles > 0) issue_tile(0, n_cand, nr, row_begin, row_off, img, rawb, &bars[0]);
+        if (n_tiles > 1)
+            issue_tile(1, n_cand, nr, row_begin, row_off, img, rawb + TILE * sizeof(ImageRecF), &bars[1]);
+    }
+    for (uint32_t t = 0; t < n_tiles; ++t) {
+        const int buf = t & 1;
+        const uint32_t cnt = min((uint32_t)TILE, n_cand - t * TILE);
+        // block-wide vote so that every thread takes the same path on a timeout
+        const bool got = mbar_wait_bounded(&bars[buf], (t >> 1) & 1, flags);
+        if (!__syncthreads_and(got)) {
+            drain_tiles(t, n_tiles, bars);
+            return;
+        }
+        static_assert(TILE == THREADS, "one record per thread in the conversion pass");
+        if ((uint32_t)tid < cnt) {
+            ff v[3];
+            const ImageRecF r = raw[buf * TILE + tid];
+            atom_local(r, org, v);
+            cxy[tid] = make_ulonglong2(f2_pack(v[0].hi, v[0].hi), f2_pack(v[1].hi, v[1].hi));
+            czt[tid] = make_ulonglong2(f2_pack(v[2].hi, v[2].hi), (unsigned long long)r.type);
+        }
+        __syncthreads();
+        // raw[buf] is free again: prefetch tile t + 2 while computing
+        if (tid == 0 && t + 2 < n_tiles) {
+            fence_proxy_async();
+            issue_tile(t + 2, n_cand, nr, row_begin, row_off, img,
+                       rawb + buf * TILE * sizeof(ImageRecF), &bars[buf]);
+        }
+        f2 part[NG][NP];
+        float shift_sum[NG];
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+            shift_sum[g] = 0.f;
+#pragma unroll
+            for (int q = 0; q < NP; ++q) part[g][q] = 0ull;  // {+0, +0}
+        }
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const ulonglong2 xy = cxy[j];
+            const ulonglong2 zt = czt[j];
+            float ax, ay, az, dummy;
+            f2_unpack(xy.x, ax, dummy);
+            f2_unpack(xy.y, ay, dummy);
+            f2_unpack(zt.x, az, dummy);
+            float d2w;
+            {
+                const float ex = ax - wcx, ey = ay - wcy, ez = az - wcz;
+                d2w = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+            }
+            if (d2w > cull2) continue;  // warp-uniform
+            ++passes;
+            const int type = (int)(uint32_t)zt.y;
+            const float close2 = P.close2[type];
+            ulonglong2 AB[NG];
+#pragma unroll
+            for (int g = 0; g < NG; ++g) {
+                AB[g] = P.ab[type * NG + g];
+                shift_sum[g] += P.shift[type * NG + g];
+            }
+            if (d2w < near2) {  // warp-uniform: this atom may be closer than sigma_t
+#pragma unroll
+                for (int k = 0; k < NPT; ++k) {
+                    float p[2][3];
+                    f2_unpack(NX[k / 2], p[0][0], p[1][0]);
+                    f2_unpack(NY[k / 2], p[0][1], p[1][1]);
+                    f2_unpack(NZ[k / 2], p[0][2], p[1][2]);
+                    const float r2 = r2_f32(ax, ay, az, p[k & 1][0], p[k & 1][1], p[k & 1][2]);
+                    if (r2 < close2) {
+                        has_close |= 1u << k;
+                        const float ir2 = rcp_approx(fmaxf(r2, 1e-4f));
+                        const float ir6 = ir2 * ir2 * ir2;
+#pragma unroll
+                        for (int g = 0; g < NG; ++g) {
+                            float a, nb, dm;
+                            f2_unpack(AB[g].x, a, dm);
+                            f2_unpack(AB[g].y, nb, dm);
+                            float v = ir6 * fmaf(a, ir6, nb) - P.vclose[type * NG + g];
+                            if (TRUNC == ALEA_LINEAR_FORCE_SHIFTED)
+                                v -= (sqrtf(fmaxf(r2, 1e-4f)) - rcf) * P.dvdrc[type * NG + g];
+                            ce[g][k] += v;
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < NP; ++q) {
+                const f2 dx = f2_sub(xy.x, NX[q]);
+                const f2 dy = f2_sub(xy.y, NY[q]);
+                const f2 dz = f2_sub(zt.x, NZ[q]);
+                const f2 r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
+                float r2a, r2b;
+                f2_unpack(r2, r2a, r2b);
+                float ia, ib;
+                if (TRUNC == ALEA_TRUNCATED) {
+                    ia = r2a > rc2f ? 0.f : rcp_approx(fmaxf(r2a, close2));
+                    ib = r2b > rc2f ? 0.f : rcp_approx(fmaxf(r2b, close2));
+                } else {
+                    r2a = fminf(fmaxf(r2a, close2), rc2f);
+                    r2b = fminf(fmaxf(r2b, close2), rc2f);
+                    ia = rcp_approx(r2a);
+                    ib = rcp_approx(r2b);
+                }
+                const f2 ir2 = f2_pack(ia, ib);
+                const f2 ir6 = f2_mul(ir2, f2_mul(ir2, ir2));
+#pragma unroll
+                for (int g = 0; g < NG; ++g) part[g][q] = f2_fma(ir6, f2_fma(AB[g].x, ir6, AB[g].y), part[g][q]);
+                if (TRUNC == ALEA_LINEAR_FORCE_SHIFTED) {
+                    const f2 dr = f2_pack(__fsub_rn(__fmul_rn(r2a, rsqrtf(r2a)), rcf),
+                                          __fsub_rn(__fmul_rn(r2b, rsqrtf(r2b)), rcf));
+#pragma unroll
+                    for (int g = 0; g < NG; ++g) {
+                        const float md = -P.dvdrc[type * NG + g];
+                        part[g][q] = f2_fma(f2_pack(md, md), dr, part[g][q]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < NG; ++g)
+#pragma unroll
+            for (int q = 0; q < NP; ++q) {
+                float pa, pb;
+                f2_unpack(part[g][q], pa, pb);
+                const ff sa = ff_add_f(ff{acc_hi(g, 2 * q), acc_lo(g, 2 * q)}, pa - shift_sum[g]);
+                const ff sb = ff_add_f(ff{acc_hi(g, 2 * q + 1), acc_lo(g, 2 * q + 1)}, pb - shift_sum[g]);
+                acc_hi(g, 2 * q) = sa.hi;
+                acc_lo(g, 2 * q) = sa.lo;
+                acc_hi(g, 2 * q + 1) = sb.hi;
+                acc_lo(g, 2 * q + 1) = sb.lo;
+            }
+        __syncthreads();  // the staged tile is rewritten by the next one
+    }
+
+    // per node and guest: sweep sum, cap, sweep sum + FP32 estimate, or the
+    // sweep sum flagged for the double-float correction
+    // (the cap: framework_energy_grid.cc:22, 243)
+    const size_t plane = (size_t)nx * ny;
+    const size_t per_table = plane * nz;
+    uint32_t mine = 0;
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) {
+        const int izn = z0 + tz0 + k;
+        if (ixn < nx && iyn < ny && izn < nz) {
+            const size_t idx = (size_t)izn * plane + (size_t)iyn * nx + ixn;
+#pragma unroll
+            for (int g = 0; g < NG; ++g) {
+                const double e = (double)acc_hi(g, k) + (double)acc_lo(g, k);
+                double out = e;
+                uint8_t f = 0;
+                if (has_close & (1u << k)) {
+                    const double est = e + (double)ce[g][k];
+                    if (est > 1.01 * kEnergyCap)
+                        out = kEnergyCap;
+                    else if (fabsf(ce[g][k]) <= CLOSE_FP32_RATIO * fmaxf(CLOSE_FP32_FLOOR, (float)fabs(est)))
+                        out = est;
+                    else
+                        f = 1;
+                }
+                tables[(size_t)g * per_table + idx] = (!f && kEnergyCap < out) ? kEnergyCap : out;
+                fix[(size_t)g * per_table + idx] = f;
+            }
+            mine += passes;
+        }
+    }
+    // node-image pairs evaluated: atoms past the warp cull x nodes in the grid
+    mine = __reduce_add_sync(0xffffffffu, mine);
+    __syncthreads();  // warp_tot is free after the tile loop
+    if ((tid & 31) == 0) warp_tot[tid >> 5] = mine;
+    __syncthreads();
+    if (tid == 0) {
+        unsigned long long sum = 0;
+        for (int w = 0; w < THREADS / 32; ++w) sum += warp_tot[w];
+        atomicAdd(executed, sum);
+    }
+}
+
+template <int NG, int TRUNC>
+constexpr size_t f32_smem_bytes() {
+    return carve(2 * TILE * sizeof(ImageRecF)) + carve(TILE * sizeof(ulonglong2)) +
+           carve(TILE * sizeof(ulonglong2)) + carve(2 * sizeof(uint64_t)) +
+           carve(MAX_ROWS * sizeof(uint32_t)) + carve((MAX_ROWS + 1) * sizeof(uint32_t)) +
+           carve((THREADS / 32) * sizeof(uint32_t)) + carve(sizeof(F32Params<NG, TRUNC>)) +
+           carve(2 * NG * NPT * THREADS * sizeof(float));
+}
+
+// ---------------------------------------------------------------- FP32 close-pair correction
+// For the nodes the sweep flagged: the pairs closer than sigma_t, exactly as
+// the sweep classified them, evaluated in double-float; their correction is
+// added to the stored sweep sum and the cap applied. One CTA per brick; a
+// brick without flagged nodes returns after reading its flags. The images
+// within reach (smax of the brick's nodes) are converted once into shared
+// memory, in chunks. Per chunk, phase A gives each flagged node a thread that
+// lists the node's close images (a uniform scan); phase B gives each flagged
+// (node, guest) a thread that evaluates just those pairs, so the expensive
+// double-float work runs without divergence.
+constexpr int NEAR_CHUNK = 512;
+constexpr int MAX_CLOSE = 16;  // listed close images per node and chunk
+
+template <int NG, int TRUNC>
+__global__ void __launch_bounds__(THREADS)
+grid_close_fix_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
+                      const uint32_t* __restrict__ bin_start, const ParamAB* __restrict__ pab_g,
+                      const ParamFF* __restrict__ pff_g, const uint8_t* __restrict__ fix,
+                      double* __restrict__ tables, unsigned* flags) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    SmemCarve sc{smem};
+    float4* ahi = sc.take<float4>(NEAR_CHUNK);  // x, y, z hi, type
+    float4* alo = sc.take<float4>(NEAR_CHUNK);  // x, y, z lo
+    uint32_t* row_begin = sc.take<uint32_t>(MAX_ROWS);
+    uint32_t* row_off = sc.take<uint32_t>(MAX_ROWS + 1);
+    uint32_t* warp_tot = sc.take<uint32_t>(THREADS / 32);
+    uint16_t* fnode = sc.take<uint16_t>(THREADS * NPT);       // (thread << 2) | k
+    uint8_t* fmask = sc.take<uint8_t>(THREADS * NPT);         // flagged guests
+    float4* fpos = sc.take<float4>(2 * THREADS * NPT);        // node hi, lo
+    uint16_t* clist = sc.take<uint16_t>(THREADS * NPT * MAX_CLOSE);
+    uint16_t* ccount = sc.take<uint16_t>(THREADS * NPT);
+    F32Params<NG, TRUNC>& P = *sc.take<F32Params<NG, TRUNC>>(1);
+    static_assert(NPT == 4 && NG <= 8, "node and guest bits");
+
+    const int tid = threadIdx.x;
+    const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
+    const int brick = blockIdx.x;
+    const int bxn = geo.bricks[0], byn = geo.bricks[1];
+    const int bx = brick % bxn, by = (brick / bxn) % byn, bz = brick / (bxn * byn);
+    const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
+    const size_t plane = (size_t)nx * ny;
+    const size_t per_table = plane * nz;
+
+    int tx, ty, tz0;
+    thread_nodes(tid, tx, ty, tz0);
+    uint32_t gm[NPT];
+    uint32_t cnt_nodes = 0;
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) {
+        gm[k] = 0;
+        const int ixn = x0 + tx, iyn = y0 + ty, izn = z0 + tz0 + k;
+        if (ixn < nx && iyn < ny && izn < nz) {
+            const size_t idx = (size_t)izn * plane + (size_t)iyn * nx + ixn;
+#pragma unroll
+            for (int g = 0; g < NG; ++g)
+                if (fix[(size_t)g * per_table + idx]) gm[k] |= 1u << g;
+        }
+        cnt_nodes += gm[k] != 0;
+    }
+    if (!__syncthreads_or(cnt_nodes != 0)) return;
+
+    // compact the flagged nodes: exclusive scan of the per-thread counts
+    uint32_t n_fn;
+    {
+        const int lane = tid & 31, wid = tid >> 5;
+        uint32_t incl = cnt_nodes;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) warp_tot[wid] = incl;
+        __syncthreads();
+        uint32_t base = 0;
+        n_fn = 0;
+        for (int w = 0; w < THREADS / 32; ++w) {
+            if (w < wid) base += warp_tot[w];
+            n_fn += warp_tot[w];
+        }
+        uint32_t off = base + incl - cnt_nodes;
+#pragma unroll
+        for (int k = 0; k < NPT; ++k)
+            if (gm[k]) {
+                fnode[off] = (uint16_t)((tid << 2) | k);
+                fmask[off] = (uint8_t)gm[k];
+                ff v[3];
+                node_local(geo, tx - 0.5f * (BX - 1), ty - 0.5f * (BY - 1), tz0 + k - 0.5f * (BZ - 1), v);
+                fpos[2 * off] = make_float4(v[0].hi, v[1].hi, v[2].hi, 0.f);
+                fpos[2 * off + 1] = make_float4(v[0].lo, v[1].lo, v[2].lo, 0.f);
+                ++off;
+            }
+    }
+    load_f32_params(P, pab_g, pff_g, geo.n_types, geo.rcf);  // synchronises
+    const int nr = plan_rows(geo, geo.hf_near, geo.keep2_near, bin_start, x0, y0, z0, row_begin,
+                             row_off, warp_tot, flags);
+    if (nr < 0) return;
+    const uint32_t n_near = row_off[nr];
+    ff org[3];
+    brick_origin(geo, x0, y0, z0, org);
+
+    for (uint32_t c0 = 0; c0 < n_near; c0 += NEAR_CHUNK) {
+        const uint32_t cnt = min((uint32_t)NEAR_CHUNK, n_near - c0);
+        for (uint32_t i = tid; i < cnt; i += THREADS) {
+            const uint32_t q = c0 + i;
+            int lo = 0, hi = nr - 1;  // last row with row_off[r] <= q
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) / 2;
+                if (row_off[mid] <= q) lo = mid; else hi = mid - 1;
+            }
+            const ImageRecF r = images[row_begin[lo] + (q - row_off[lo])];
+            ff v[3];
+            atom_local(r, org, v);
+            ahi[i] = make_float4(v[0].hi, v[1].hi, v[2].hi, __int_as_float((int)r.type));
+            alo[i] = make_float4(v[0].lo, v[1].lo, v[2].lo, 0.f);
+        }
+        __syncthreads();
+        // phase A: each flagged node lists its close images in this chunk
+        for (uint32_t f = tid; f < n_fn; f += THREADS) {
+            const float4 p = fpos[2 * f];
+            uint32_t c = 0;
+            for (uint32_t i = 0; i < cnt; ++i) {
+                const float4 a = ahi[i];
+                if (r2_f32(a.x, a.y, a.z, p.x, p.y, p.z) < P.close2[__float_as_int(a.w)]) {
+                    if (c < MAX_CLOSE) clist[f * MAX_CLOSE + c] = (uint16_t)i;
+                    ++c;
+                }
+            }
+            ccount[f] = (uint16_t)min(c, 65535u);
+        }
+        __syncthreads();
+        // phase B: each flagged (node, guest) sums its close pairs
+        for (uint32_t jb = tid; jb < n_fn * NG; jb += THREADS) {
+            const uint32_t f = jb / NG;
+            const int g = (int)(jb % NG);
+            if (!(fmask[f] & (1u << g))) continue;
+            const float4 p = fpos[2 * f], pl = fpos[2 * f + 1];
+            const uint32_t c = ccount[f];
+            ff acc{0.f, 0.f};
+            // more close images than slots: scan the chunk again (rare)
+            const uint32_t n_it = c <= MAX_CLOSE ? c : cnt;
+            for (uint32_t u = 0; u < n_it; ++u) {
+                const uint32_t i = c <= MAX_CLOSE ? clist[f * MAX_CLOSE + u] : u;
+                const float4 a = ahi[i];
+                const int type = __float_as_int(a.w);
+                if (c > MAX_CLOSE && !(r2_f32(a.x, a.y, a.z, p.x, p.y, p.z) < P.close2[type])) continue;
+                const float4 l = alo[i];
+                const ff ddx = ff_add(ff{a.x, l.x}, ff{-p.x, -pl.x});
+                const ff ddy = ff_add(ff{a.y, l.y}, ff{-p.y, -pl.y});
+                const ff ddz = ff_add(ff{a.z, l.z}, ff{-p.z, -pl.z});
+                acc = ff_add(acc, close_pair(P, type, g, ddx, ddy, ddz, geo.rcf));
+            }
+            if (c) {
+                const uint32_t node = fnode[f];
+                int jx, jy, jz0;
+                thread_nodes((int)(node >> 2), jx, jy, jz0);
+                const size_t idx = (size_t)(z0 + jz0 + (node & 3)) * plane + (size_t)(y0 + jy) * nx + (x0 + jx);
+                tables[(size_t)g * per_table + idx] += (double)acc.hi + (double)acc.lo;
+            }
+        }
+        __syncthreads();
+    }
+    for (uint32_t jb = tid; jb < n_fn * NG; jb += THREADS) {
+        const uint32_t f = jb / NG;
+        const int g = (int)(jb % NG);
+        if (!(fmask[f] & (1u << g))) continue;
+        const uint32_t node = fnode[f];
+        int jx, jy, jz0;
+        thread_nodes((int)(node >> 2), jx, jy, jz0);
+        const size_t idx = (size_t)(z0 + jz0 + (node & 3)) * plane + (size_t)(y0 + jy) * nx + (x0 + jx);
+        double& e = tables[(size_t)g * per_table + idx];
+        if (kEnergyCap < e) e = kEnergyCap;
+    }
+}
+
+template <int NG, int TRUNC>
+constexpr size_t fix_smem_bytes() {
+    return 2 * carve(NEAR_CHUNK * sizeof(float4)) + carve(MAX_ROWS * sizeof(uint32_t)) +
+           carve((MAX_ROWS + 1) * sizeof(uint32_t)) + carve((THREADS / 32) * sizeof(uint32_t)) +
+           carve(THREADS * NPT * sizeof(uint16_t)) + carve(THREADS * NPT * sizeof(uint8_t)) +
+           carve(2 * THREADS * NPT * sizeof(float4)) +
+           carve(THREADS * NPT * MAX_CLOSE * sizeof(uint16_t)) +
+           carve(THREADS * NPT * sizeof(uint16_t)) + carve(sizeof(F32Params<NG, TRUNC>));
 }
 
 // ---------------------------------------------------------------- interpolation
@@ -652,53 +1207,62 @@ __global__ void grid_interpolate_kernel(Lattice L, int nx, int ny, int nz,
     out[i] = add_rn(mul_rn(c0, sub_rn(1.0, t[2])), mul_rn(c1, t[2]));
 }
 
-template <typename Real>
-constexpr size_t grid_smem_bytes() {
-    auto up = [](size_t b) { return (b + 127) & ~(size_t)127; };
-    return up(2 * TILE * sizeof(ImageRec)) + up(TILE * sizeof(float4)) +
-           up((sizeof(Real) == 4 ? TILE : 1) * sizeof(float4)) +
-           up((sizeof(Real) == 4 ? NPT * 3 * THREADS : 1) * sizeof(float)) + up(2 * sizeof(uint64_t)) +
-           up(MAX_ROWS * sizeof(uint32_t)) + up((MAX_ROWS + 1) * sizeof(uint32_t)) +
-           up((THREADS / 32) * sizeof(uint32_t)) + up(64 * MAX_NG * sizeof(ParamF)) +
-           up(64 * sizeof(float)) + up(TILE * sizeof(uint16_t)) +
-           up(64 * MAX_NG * sizeof(PairParams));
+struct BuildArgs {
+    const ImageRec* images;      // FP64 form
+    const ImageRecF* images_f;   // FP32 form
+    const uint32_t* bins;
+    const PairParams* params;    // FP64 form: mixed table, indexed through guests
+    const uint32_t* guests;
+    const ParamAB* pab;          // FP32 form: [guest of this launch][type]
+    const ParamFF* pff;
+    double* tables;
+    uint8_t* fix;                // FP32 form: per node and guest, 1 = close-pair correction due
+    unsigned long long* executed;
+    unsigned* flags;
+};
+
+template <int NG, int TRUNC>
+void launch_one(bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo, const BuildArgs& a) {
+    if (f32) {
+        constexpr size_t bytes = f32_smem_bytes<NG, TRUNC>();
+        // opt in to more than 48 KB of dynamic shared memory (per device, cheap)
+        ALEA_CUDA(cudaFuncSetAttribute(grid_build_f32_kernel<NG, TRUNC>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        grid_build_f32_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(
+            geo, a.images_f, a.bins, a.pab, a.pff, a.tables, a.fix, a.executed, a.flags);
+        ALEA_CUDA(cudaGetLastError());
+        constexpr size_t fbytes = fix_smem_bytes<NG, TRUNC>();
+        ALEA_CUDA(cudaFuncSetAttribute(grid_close_fix_kernel<NG, TRUNC>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fbytes));
+        grid_close_fix_kernel<NG, TRUNC><<<grid, THREADS, fbytes, s>>>(
+            geo, a.images_f, a.bins, a.pab, a.pff, a.fix, a.tables, a.flags);
+    } else {
+        constexpr size_t bytes = f64_smem_bytes<NG>();
+        ALEA_CUDA(cudaFuncSetAttribute(grid_build_f64_kernel<NG, TRUNC>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        grid_build_f64_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(
+            geo, a.images, a.bins, a.params, a.guests, a.tables, a.executed, a.flags);
+    }
 }
 
-template <typename Real, int NG, int TRUNC>
-void launch_one(dim3 grid, cudaStream_t s, const GridGeom& geo, const ImageRec* images,
-                const uint32_t* bins, const PairParams* params, const uint32_t* guests,
-                double* tables, unsigned long long* executed, unsigned* flags) {
-    constexpr size_t bytes = grid_smem_bytes<Real>();
-    // opt in to more than 48 KB of dynamic shared memory (per device, cheap)
-    ALEA_CUDA(cudaFuncSetAttribute(grid_build_kernel<Real, NG, TRUNC>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    grid_build_kernel<Real, NG, TRUNC>
-        <<<grid, THREADS, bytes, s>>>(geo, images, bins, params, guests, tables, executed, flags);
-}
-
-template <typename Real, int NG>
-void launch_build_t(int trunc, dim3 grid, cudaStream_t s, const GridGeom& geo,
-                    const ImageRec* images, const uint32_t* bins, const PairParams* params,
-                    const uint32_t* guests, double* tables, unsigned long long* executed,
-                    unsigned* flags) {
+template <int NG>
+void launch_trunc(int trunc, bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo,
+                  const BuildArgs& a) {
     if (trunc == ALEA_TRUNCATED)
-        launch_one<Real, NG, ALEA_TRUNCATED>(grid, s, geo, images, bins, params, guests, tables, executed, flags);
+        launch_one<NG, ALEA_TRUNCATED>(f32, grid, s, geo, a);
     else if (trunc == ALEA_SHIFTED)
-        launch_one<Real, NG, ALEA_SHIFTED>(grid, s, geo, images, bins, params, guests, tables, executed, flags);
+        launch_one<NG, ALEA_SHIFTED>(f32, grid, s, geo, a);
     else
-        launch_one<Real, NG, ALEA_LINEAR_FORCE_SHIFTED>(grid, s, geo, images, bins, params, guests, tables, executed, flags);
+        launch_one<NG, ALEA_LINEAR_FORCE_SHIFTED>(f32, grid, s, geo, a);
 }
 
-template <typename Real>
-void launch_build(int ng, int trunc, dim3 grid, cudaStream_t s, const GridGeom& geo,
-                  const ImageRec* images, const uint32_t* bins, const PairParams* params,
-                  const uint32_t* guests, double* tables, unsigned long long* executed,
-                  unsigned* flags) {
+void launch_build(int ng, int trunc, bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo,
+                  const BuildArgs& a) {
     switch (ng) {
-        case 1: launch_build_t<Real, 1>(trunc, grid, s, geo, images, bins, params, guests, tables, executed, flags); break;
-        case 2: launch_build_t<Real, 2>(trunc, grid, s, geo, images, bins, params, guests, tables, executed, flags); break;
-        case 3: launch_build_t<Real, 3>(trunc, grid, s, geo, images, bins, params, guests, tables, executed, flags); break;
-        default: launch_build_t<Real, 4>(trunc, grid, s, geo, images, bins, params, guests, tables, executed, flags); break;
+        case 1: launch_trunc<1>(trunc, f32, grid, s, geo, a); break;
+        case 2: launch_trunc<2>(trunc, f32, grid, s, geo, a); break;
+        case 3: launch_trunc<3>(trunc, f32, grid, s, geo, a); break;
+        default: launch_trunc<4>(trunc, f32, grid, s, geo, a); break;
     }
 }
 
@@ -712,7 +1276,11 @@ struct GridImpl {
     double spacing = 0;
     uint64_t n_atoms = 0;
     std::vector<uint32_t> species;  // sorted distinct guest species
-    DevBuf<ImageRec> images;
+    DevBuf<ImageRec> images;     // FP64 form
+    DevBuf<ImageRecF> images_f;  // FP32 form
+    DevBuf<ParamAB> pab;         // FP32 form, [guest][type]
+    DevBuf<ParamFF> pff;
+    DevBuf<uint8_t> fix;         // FP32 form: close-pair correction flags, per guest and node
     DevBuf<uint32_t> bin_start;
     DevBuf<PairParams> params;
     DevBuf<uint32_t> guests;
@@ -765,10 +1333,24 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
     const double* m = g.geo.L.m;
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
-            g.geo.G[3 * i + j] = m[3 * i] * m[3 * j] + m[3 * i + 1] * m[3 * j + 1] + m[3 * i + 2] * m[3 * j + 2];
-    for (int i = 0; i < 9; ++i) g.geo.Gf[i] = (float)g.geo.G[i];
+            g.geo.Gf[3 * i + j] = (float)(m[3 * i] * m[3 * j] + m[3 * i + 1] * m[3 * j + 1] +
+                                          m[3 * i + 2] * m[3 * j + 2]);
+    for (int i = 0; i < 3; ++i) g.geo.Ginvf[i] = 1.0f / g.geo.Gf[4 * i];
     g.geo.rc = lj.cutoff;
     g.geo.rc2 = lj.cutoff * lj.cutoff;
+    g.geo.rcf = (float)lj.cutoff;
+    g.geo.rc2f = (float)g.geo.rc2;
+    g.geo.irc2f = (float)(1.0 / g.geo.rc2);
+    g.geo.keep2f = (float)(g.geo.rc2 * (1.0 + 1e-3) + 1e-2);
+    for (int a = 0; a < 3; ++a) {
+        g.geo.inv_nf[a] = (float)(1.0 / g.geo.n[a]);
+        g.geo.hf[a] = (float)(lj.cutoff / g.geo.L.perp[a]);
+        for (int c = 0; c < 3; ++c) {
+            const double v = m[3 * a + c] / g.geo.n[a];
+            g.geo.sh[3 * a + c] = (float)v;
+            g.geo.sl[3 * a + c] = (float)(v - (double)g.geo.sh[3 * a + c]);
+        }
+    }
     // widen the bins until no brick can touch more than MAX_ROWS bin rows
     for (int attempt = 0; attempt < 64; ++attempt) {
         int span_bins[3];
@@ -792,6 +1374,7 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
         g.geo.binw[a] = span / g.geo.nb[a];
         g.geo.lof[a] = (float)g.geo.lo[a];
         g.geo.binwf[a] = (float)g.geo.binw[a];
+        g.geo.inv_binwf[a] = (float)(1.0 / g.geo.binw[a]);
         g.geo.bricks[a] = (g.geo.n[a] + (a == 0 ? BX : a == 1 ? BY : BZ) - 1) /
                           (a == 0 ? BX : a == 1 ? BY : BZ);
     }
@@ -842,28 +1425,62 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
         for (size_t i = 0; i < recs.size(); ++i) sorted[fill[keys[i]]++] = recs[i];
     }
     g.n_images = sorted.size();
-    g.images.alloc(std::max<size_t>(sorted.size(), 1));
-    g.images.upload(sorted.data(), sorted.size());
+    if (precision == ALEA_FP32) {
+        std::vector<ImageRecF> sf(sorted.size());
+        for (size_t i = 0; i < sorted.size(); ++i) {
+            const ImageRec& r = sorted[i];
+            ImageRecF& q = sf[i];
+            q.xh = (float)r.x;
+            q.yh = (float)r.y;
+            q.zh = (float)r.z;
+            q.xl = (float)(r.x - (double)q.xh);
+            q.yl = (float)(r.y - (double)q.yh);
+            q.zl = (float)(r.z - (double)q.zh);
+            q.type = r.type;
+            q.pad = 0.f;
+        }
+        g.images_f.alloc(std::max<size_t>(sf.size(), 1));
+        g.images_f.upload(sf.data(), sf.size());
+    } else {
+        g.images.alloc(std::max<size_t>(sorted.size(), 1));
+        g.images.upload(sorted.data(), sorted.size());
+    }
     g.bin_start.alloc(start.size());
     g.bin_start.upload(start.data(), start.size());
 
     std::vector<PairParams> table((size_t)lj.n_species * lj.n_species);
     mixed_table(lj, table.data());
-    // reach of the FP32 form's close pass: largest mixed sigma of these guests
-    // plus the half-diagonal of a brick (triangle inequality bound)
+    // FP32 form: per (guest, framework type) the A/B coefficients and the
+    // shift terms, and the double-float parameters of the close pairs; the
+    // close-pair reach is the largest mixed sigma of these guests
     {
+        const uint32_t nt = lj.n_species;
+        std::vector<ParamAB> ab((size_t)ng * nt);
+        std::vector<ParamFF> pf((size_t)ng * nt);
         double smax = 0.0;
-        for (uint32_t gs : sp)
-            for (uint32_t t = 0; t < lj.n_species; ++t)
-                smax = std::max(smax, table[(size_t)gs * lj.n_species + t].sigma);
-        double half = 0.0;
-        const int bd[3] = {BX, BY, BZ};
-        for (int a = 0; a < 3; ++a) {
-            const double f = (double)(bd[a] - 1) / g.geo.n[a];
-            half += 0.5 * f * std::sqrt(m[3 * a] * m[3 * a] + m[3 * a + 1] * m[3 * a + 1] + m[3 * a + 2] * m[3 * a + 2]);
+        for (int gi = 0; gi < ng; ++gi)
+            for (uint32_t t = 0; t < nt; ++t) {
+                const PairParams& p = table[(size_t)sp[gi] * nt + t];
+                smax = std::max(smax, p.sigma);
+                const double s2 = p.sigma * p.sigma, s6 = s2 * s2 * s2, e4 = 4.0 * p.eps;
+                ab[(size_t)gi * nt + t] = ParamAB{(float)(e4 * s6 * s6), (float)(e4 * s6),
+                                                  (float)p.shift, (float)p.dvdrc};
+                const float s2h = (float)s2, e4h = (float)e4, shh = (float)p.shift;
+                pf[(size_t)gi * nt + t] = ParamFF{s2h, (float)(s2 - s2h), e4h, (float)(e4 - e4h), shh,
+                                                  (float)(p.shift - shh), (float)p.dvdrc, 0.f};
+            }
+        g.geo.smaxf = (float)(smax * (1.0 + 1e-5));
+        // reach of the close-pair correction: pairs closer than the largest
+        // sigma (FP32 classification, so a relative margin on top)
+        const double reach = smax * (1.0 + 1e-4) + 1e-3;
+        for (int a = 0; a < 3; ++a) g.geo.hf_near[a] = (float)(reach / g.geo.L.perp[a]);
+        g.geo.keep2_near = (float)(reach * reach * (1.0 + 1e-3) + 1e-2);
+        if (precision == ALEA_FP32) {
+            g.pab.alloc(std::max<size_t>(ab.size(), 1));
+            g.pab.upload(ab.data(), ab.size());
+            g.pff.alloc(std::max<size_t>(pf.size(), 1));
+            g.pff.upload(pf.data(), pf.size());
         }
-        const double reach = smax * (1.0 + 1e-5) + half + 1e-3;
-        g.geo.near2 = (float)(reach * reach);
     }
     g.params.alloc(table.size());
     g.params.upload(table.data(), table.size());
@@ -871,6 +1488,7 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
     g.guests.upload(sp.data(), sp.size());
     const size_t nodes = (size_t)g.geo.n[0] * g.geo.n[1] * g.geo.n[2];
     g.tables.alloc(nodes * std::max(ng, 1));
+    if (precision == ALEA_FP32) g.fix.alloc(nodes * std::max(ng, 1));
     g.executed.alloc(1);
     g.flags.alloc(1);
     ALEA_CUDA(cudaMemset(g.flags.p, 0, sizeof(unsigned)));
@@ -889,14 +1507,13 @@ static void run_build(GridImpl& g, cudaStream_t s) {
     for (int g0 = 0; g0 < ng; g0 += MAX_NG) {
         const int cnt = std::min(MAX_NG, ng - g0);
         dim3 grid((unsigned)nbricks);
-        if (g.precision == ALEA_FP32)
-            launch_build<float>(cnt, g.truncation, grid, s, g.geo, g.images.p, g.bin_start.p,
-                                g.params.p, g.guests.p + g0, g.tables.p + (size_t)g0 * nodes,
-                                g.executed.p, g.flags.p);
-        else
-            launch_build<double>(cnt, g.truncation, grid, s, g.geo, g.images.p, g.bin_start.p,
-                                 g.params.p, g.guests.p + g0, g.tables.p + (size_t)g0 * nodes,
-                                 g.executed.p, g.flags.p);
+        const size_t pofs = (size_t)g0 * g.geo.n_types;
+        const bool f32 = g.precision == ALEA_FP32;
+        const BuildArgs args{g.images.p, g.images_f.p, g.bin_start.p, g.params.p, g.guests.p + g0,
+                             f32 ? g.pab.p + pofs : nullptr, f32 ? g.pff.p + pofs : nullptr,
+                             g.tables.p + (size_t)g0 * nodes,
+                             f32 ? g.fix.p + (size_t)g0 * nodes : nullptr, g.executed.p, g.flags.p};
+        launch_build(cnt, g.truncation, f32, grid, s, g.geo, args);
         ALEA_CUDA(cudaGetLastError());
     }
     ALEA_CUDA(cudaEventRecord(e1, s));

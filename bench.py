@@ -47,8 +47,11 @@ sys.path.insert(0, str(ROOT))
 SPACING = 0.2
 CUTOFF = 12.8
 REPS = 4
-FLOPS_PER_NODE_IMAGE = 11      # displacement, r^2, clamp, rcp, cutoff test
-FLOPS_PER_SPECIES = 8          # s^2, s^6, s^12 - s^6, 4 eps (.) - shift, accumulate
+# FP32 build kernel, per evaluated node-image pair (an FMA counts 2):
+# displacement 3, r^2 5 (FMUL + 2 FFMA), reciprocal 1, r^-6 2
+FLOPS_PER_NODE_IMAGE = 11
+# per guest species: t = A r^-6 - B and part += r^-6 t, two FFMA
+FLOPS_PER_SPECIES = 4
 
 
 def _dist():
@@ -310,7 +313,7 @@ def main():
                 "frac": achieved / fp32_peak,
                 "peak_source": "FP32 FFMA loop measured in this run (alea_probe_fp32_fma_tflops)",
                 "traffic": None,
-                "kernel": "grid_build_kernel<float,2,SHIFTED>",
+                "kernel": "grid_build_f32_kernel<2,SHIFTED>",
                 "executed_node_image_pairs_per_step": int(node_image),
                 "flops_per_node_image_pair": FLOPS_PER_NODE_IMAGE + FLOPS_PER_SPECIES * ng,
             },
