@@ -1221,22 +1221,24 @@ struct BuildArgs {
     unsigned* flags;
 };
 
+// phase 0: the sweep (or the FP64 kernel); phase 1: the FP32 close-pair correction
 template <int NG, int TRUNC>
-void launch_one(bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo, const BuildArgs& a) {
-    if (f32) {
+void launch_one(bool f32, int phase, dim3 grid, cudaStream_t s, const GridGeom& geo,
+                const BuildArgs& a) {
+    if (f32 && phase == 0) {
         constexpr size_t bytes = f32_smem_bytes<NG, TRUNC>();
         // opt in to more than 48 KB of dynamic shared memory (per device, cheap)
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f32_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
         grid_build_f32_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(
             geo, a.images_f, a.bins, a.pab, a.pff, a.tables, a.fix, a.executed, a.flags);
-        ALEA_CUDA(cudaGetLastError());
+    } else if (f32) {
         constexpr size_t fbytes = fix_smem_bytes<NG, TRUNC>();
         ALEA_CUDA(cudaFuncSetAttribute(grid_close_fix_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fbytes));
         grid_close_fix_kernel<NG, TRUNC><<<grid, THREADS, fbytes, s>>>(
             geo, a.images_f, a.bins, a.pab, a.pff, a.fix, a.tables, a.flags);
-    } else {
+    } else if (phase == 0) {
         constexpr size_t bytes = f64_smem_bytes<NG>();
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f64_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -1246,23 +1248,23 @@ void launch_one(bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo, const 
 }
 
 template <int NG>
-void launch_trunc(int trunc, bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo,
+void launch_trunc(int trunc, bool f32, int phase, dim3 grid, cudaStream_t s, const GridGeom& geo,
                   const BuildArgs& a) {
     if (trunc == ALEA_TRUNCATED)
-        launch_one<NG, ALEA_TRUNCATED>(f32, grid, s, geo, a);
+        launch_one<NG, ALEA_TRUNCATED>(f32, phase, grid, s, geo, a);
     else if (trunc == ALEA_SHIFTED)
-        launch_one<NG, ALEA_SHIFTED>(f32, grid, s, geo, a);
+        launch_one<NG, ALEA_SHIFTED>(f32, phase, grid, s, geo, a);
     else
-        launch_one<NG, ALEA_LINEAR_FORCE_SHIFTED>(f32, grid, s, geo, a);
+        launch_one<NG, ALEA_LINEAR_FORCE_SHIFTED>(f32, phase, grid, s, geo, a);
 }
 
-void launch_build(int ng, int trunc, bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo,
-                  const BuildArgs& a) {
+void launch_build(int ng, int trunc, bool f32, int phase, dim3 grid, cudaStream_t s,
+                  const GridGeom& geo, const BuildArgs& a) {
     switch (ng) {
-        case 1: launch_trunc<1>(trunc, f32, grid, s, geo, a); break;
-        case 2: launch_trunc<2>(trunc, f32, grid, s, geo, a); break;
-        case 3: launch_trunc<3>(trunc, f32, grid, s, geo, a); break;
-        default: launch_trunc<4>(trunc, f32, grid, s, geo, a); break;
+        case 1: launch_trunc<1>(trunc, f32, phase, grid, s, geo, a); break;
+        case 2: launch_trunc<2>(trunc, f32, phase, grid, s, geo, a); break;
+        case 3: launch_trunc<3>(trunc, f32, phase, grid, s, geo, a); break;
+        default: launch_trunc<4>(trunc, f32, phase, grid, s, geo, a); break;
     }
 }
 
@@ -1290,6 +1292,9 @@ struct GridImpl {
     uint64_t n_images = 0;
     uint64_t executed_pairs = 0;
     float last_ms = 0.f;
+    float last_sweep_ms = 0.f;   // the FP32 sweep, or the FP64 kernel
+    float last_fix_ms = 0.f;     // the FP32 close-pair correction
+    int launches = 0;
 };
 
 static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_particles& fw,
@@ -1500,29 +1505,44 @@ static void run_build(GridImpl& g, cudaStream_t s) {
     const uint64_t nbricks = (uint64_t)g.geo.bricks[0] * g.geo.bricks[1] * g.geo.bricks[2];
     require(nbricks < (1ull << 31), ALEA_ERR_INVALID_ARGUMENT, "grid too large");
     ALEA_CUDA(cudaMemsetAsync(g.executed.p, 0, sizeof(unsigned long long), s));
-    cudaEvent_t e0, e1;
-    ALEA_CUDA(cudaEventCreate(&e0));
-    ALEA_CUDA(cudaEventCreate(&e1));
-    ALEA_CUDA(cudaEventRecord(e0, s));
-    for (int g0 = 0; g0 < ng; g0 += MAX_NG) {
+    const bool f32 = g.precision == ALEA_FP32;
+    // events around every launch on the launching stream: [chunk][phase]
+    const int chunks = (ng + MAX_NG - 1) / MAX_NG;
+    std::vector<cudaEvent_t> ev((size_t)chunks * 3);
+    for (auto& e : ev) ALEA_CUDA(cudaEventCreate(&e));
+    for (int c = 0; c < chunks; ++c) {
+        const int g0 = c * MAX_NG;
         const int cnt = std::min(MAX_NG, ng - g0);
         dim3 grid((unsigned)nbricks);
         const size_t pofs = (size_t)g0 * g.geo.n_types;
-        const bool f32 = g.precision == ALEA_FP32;
         const BuildArgs args{g.images.p, g.images_f.p, g.bin_start.p, g.params.p, g.guests.p + g0,
                              f32 ? g.pab.p + pofs : nullptr, f32 ? g.pff.p + pofs : nullptr,
                              g.tables.p + (size_t)g0 * nodes,
                              f32 ? g.fix.p + (size_t)g0 * nodes : nullptr, g.executed.p, g.flags.p};
-        launch_build(cnt, g.truncation, f32, grid, s, g.geo, args);
+        ALEA_CUDA(cudaEventRecord(ev[3 * c], s));
+        launch_build(cnt, g.truncation, f32, 0, grid, s, g.geo, args);
         ALEA_CUDA(cudaGetLastError());
+        ALEA_CUDA(cudaEventRecord(ev[3 * c + 1], s));
+        if (f32) {
+            launch_build(cnt, g.truncation, f32, 1, grid, s, g.geo, args);
+            ALEA_CUDA(cudaGetLastError());
+        }
+        ALEA_CUDA(cudaEventRecord(ev[3 * c + 2], s));
     }
-    ALEA_CUDA(cudaEventRecord(e1, s));
-    ALEA_CUDA(cudaEventSynchronize(e1));
-    float ms = 0;
-    ALEA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    g.last_ms = ms;
+    ALEA_CUDA(cudaEventSynchronize(ev.back()));
+    float sweep = 0.f, fix = 0.f;
+    for (int c = 0; c < chunks; ++c) {
+        float a = 0.f, b = 0.f;
+        ALEA_CUDA(cudaEventElapsedTime(&a, ev[3 * c], ev[3 * c + 1]));
+        ALEA_CUDA(cudaEventElapsedTime(&b, ev[3 * c + 1], ev[3 * c + 2]));
+        sweep += a;
+        fix += b;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    g.last_ms = sweep + fix;
+    g.last_sweep_ms = sweep;
+    g.last_fix_ms = fix;
+    g.launches = chunks * (f32 ? 2 : 1);
     unsigned long long ex = 0;
     ALEA_CUDA(cudaMemcpy(&ex, g.executed.p, sizeof(ex), cudaMemcpyDeviceToHost));
     g.executed_pairs = ex;
@@ -1602,6 +1622,9 @@ void grid_stats(const GridImpl* g, alea_grid_stats* out) {
     out->images = g->n_images;
     out->bricks = (uint64_t)g->geo.bricks[0] * g->geo.bricks[1] * g->geo.bricks[2];
     out->last_kernel_ms = g->last_ms;
+    out->last_sweep_ms = g->last_sweep_ms;
+    out->last_fix_ms = g->last_fix_ms;
+    out->launches = (uint32_t)g->launches;
 }
 
 GridImpl* grid_from_tables(const alea_lattice& lat, double spacing, const int32_t counts[3],

@@ -47,11 +47,19 @@ sys.path.insert(0, str(ROOT))
 SPACING = 0.2
 CUTOFF = 12.8
 REPS = 4
-# FP32 build kernel, per evaluated node-image pair (an FMA counts 2):
-# displacement 3, r^2 5 (FMUL + 2 FFMA), reciprocal 1, r^-6 2
-FLOPS_PER_NODE_IMAGE = 11
-# per guest species: t = A r^-6 - B and part += r^-6 t, two FFMA
-FLOPS_PER_SPECIES = 4
+# Roofline unit: the reference's operation count per pair evaluation (node,
+# atom image, guest species): 3 sub, 3 rint + 3 FMA min-image, 5 for r^2,
+# 1 rcp, 1 s^2, 2 s^6, 1 s^12, 3 for 4 eps (s^12 - s^6) - V(rc), 1 accumulate,
+# 1 compare/select = 24 FLOP, counted over the pairs the kernel evaluates.
+FLOPS_PER_PAIR = 24
+# What the FP32 sweep itself issues per evaluated node-image pair (an FMA
+# counts 2): displacement 3, r^2 5, reciprocal 1, r^-6 2, and per guest
+# species two FMAs (t = A r^-6 - B; sum += r^-6 t) = 4.
+KERNEL_FLOPS_PER_NODE_IMAGE = 11
+KERNEL_FLOPS_PER_SPECIES = 4
+# DRAM bytes (read + write) of one sweep launch on this workload, from a
+# single-pass ncu capture of the full workload (profiles/grid_build_f32_c5_dram.md)
+SWEEP_DRAM_BYTES_PER_LAUNCH = 1538254336
 
 
 def _dist():
@@ -243,6 +251,7 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    sweep_ms, launches = [], 0
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
         for i in range(args.steps):
@@ -250,6 +259,9 @@ def main():
             starts[i].record(stream)
             grid.rebuild(sp)
             ends[i].record(stream)
+            st_i = grid.stats()  # the build synchronises; per-kernel event times
+            sweep_ms.append(st_i["last_sweep_ms"])
+            launches += st_i["launches"]
         torch.cuda.synchronize()
         region_s = time.perf_counter() - t0
     if dist:
@@ -297,8 +309,10 @@ def main():
         fp32_peak = A.fp32_fma_tflops()
         ng = len(guests)
         node_image = st["executed_pairs"] / ng
-        flops = node_image * (FLOPS_PER_NODE_IMAGE + FLOPS_PER_SPECIES * ng)
-        achieved = flops / (step_ms * 1e-3) / 1e12
+        sweep = float(np.mean(sweep_ms))
+        achieved = st["executed_pairs"] * FLOPS_PER_PAIR / (sweep * 1e-3) / 1e12
+        kflops = node_image * (KERNEL_FLOPS_PER_NODE_IMAGE + KERNEL_FLOPS_PER_SPECIES * ng)
+        kachieved = kflops / (sweep * 1e-3) / 1e12
         line = {
             "metric": "energy-grid pair evals/s", "value": value, "unit": "pair evals/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
@@ -307,15 +321,21 @@ def main():
             "config": _config(fw, guests, grid.point_counts(),
                               REPS if args.workload == "full" else 2),
             "region_ms": region_s * 1e3,
-            "gpu_launches": args.steps,
+            "gpu_launches": launches,
             "roofline": {
                 "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak,
                 "peak_source": "FP32 FFMA loop measured in this run (alea_probe_fp32_fma_tflops)",
-                "traffic": None,
+                "traffic": SWEEP_DRAM_BYTES_PER_LAUNCH if args.workload == "full" else None,
                 "kernel": "grid_build_f32_kernel<2,SHIFTED>",
-                "executed_node_image_pairs_per_step": int(node_image),
-                "flops_per_node_image_pair": FLOPS_PER_NODE_IMAGE + FLOPS_PER_SPECIES * ng,
+                "kernel_ms": sweep,
+                "flops_per_pair": FLOPS_PER_PAIR,
+                "executed_pairs_per_step": int(st["executed_pairs"]),
+                "kernel_issued_flops_per_node_image_pair":
+                    KERNEL_FLOPS_PER_NODE_IMAGE + KERNEL_FLOPS_PER_SPECIES * ng,
+                "kernel_issued_achieved": kachieved,
+                "kernel_issued_frac": kachieved / fp32_peak,
+                "close_fix_ms": float(st["last_fix_ms"]),
             },
             "e2e": {"value": e2e_value, "unit": "pair evals/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
