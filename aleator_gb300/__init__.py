@@ -15,6 +15,7 @@ from ._lib import (  # noqa: F401
     GEOMETRIC,
     LINEAR_FORCE_SHIFTED,
     LORENTZ_BERTHELOT,
+    SAMPLE_ROW,
     SHIFTED,
     TRUNCATED,
     AleatorError,
@@ -24,6 +25,7 @@ from ._lib import (  # noqa: F401
     GcmcChains,
     LennardJones,
     ParticleData,
+    Proposal,
     Widom,
     device_info,
     ewald_energy_breakdown,

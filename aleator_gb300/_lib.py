@@ -31,6 +31,21 @@ _I32 = ctypes.POINTER(ctypes.c_int32)
 _VP = ctypes.c_void_p
 
 
+_F = ctypes.POINTER(ctypes.c_float)
+SAMPLE_ROW = 5  # floats per training row {s0, s1, s2, -dU/T, lq} (ALEA_SAMPLE_ROW)
+
+
+class _ProposalConfig(ctypes.Structure):
+    _fields_ = [("n_freq", ctypes.c_uint32), ("width", ctypes.c_uint32), ("depth", ctypes.c_uint32),
+                ("freq_max", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+
+
+class _TrainConfig(ctypes.Structure):
+    _fields_ = [("epochs", ctypes.c_uint32), ("batch", ctypes.c_uint32), ("lr", ctypes.c_double),
+                ("tau", ctypes.c_double), ("beta1", ctypes.c_double), ("beta2", ctypes.c_double),
+                ("eps", ctypes.c_double), ("seed", ctypes.c_uint64)]
+
+
 class _Lattice(ctypes.Structure):
     _fields_ = [("m", ctypes.c_double * 9)]
 
@@ -155,6 +170,25 @@ _SIGNATURES = {
                                         ctypes.c_uint64, ctypes.c_int32,
                                         ctypes.POINTER(_WidomResult), _D]),
     "alea_widom_destroy": (ctypes.c_int32, [_VP]),
+    "alea_widom_samples": (ctypes.c_int32, [_VP, _VP, ctypes.c_uint64, ctypes.c_uint64,
+                                            ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, _VP]),
+    "alea_widom_run_biased": (ctypes.c_int32, [_VP, _VP, ctypes.c_uint64, ctypes.c_uint64,
+                                               ctypes.c_uint64, ctypes.c_uint64,
+                                               ctypes.POINTER(_WidomResult), _D, _D]),
+    "alea_proposal_create": (ctypes.c_int32, [ctypes.POINTER(_ProposalConfig),
+                                              ctypes.POINTER(_VP)]),
+    "alea_proposal_param_count": (ctypes.c_int32, [_VP, _U64]),
+    "alea_proposal_wave_vectors": (ctypes.c_int32, [_VP, _I32, ctypes.c_uint64]),
+    "alea_proposal_get_params": (ctypes.c_int32, [_VP, _F, ctypes.c_uint64]),
+    "alea_proposal_set_params": (ctypes.c_int32, [_VP, _F, ctypes.c_uint64]),
+    "alea_proposal_forward": (ctypes.c_int32, [_VP, _F, ctypes.c_uint64, _F]),
+    "alea_proposal_loss_grad": (ctypes.c_int32, [_VP, _F, ctypes.c_uint64, ctypes.c_double, _D,
+                                                 _F, ctypes.c_uint64]),
+    "alea_proposal_train": (ctypes.c_int32, [_VP, _VP, ctypes.c_uint64,
+                                             ctypes.POINTER(_TrainConfig), _D, _VP]),
+    "alea_proposal_tabulate": (ctypes.c_int32, [_VP, ctypes.c_uint32, ctypes.c_double]),
+    "alea_proposal_log_density": (ctypes.c_int32, [_VP, _D, ctypes.c_uint64, _D]),
+    "alea_proposal_destroy": (ctypes.c_int32, [_VP]),
     "alea_gcmc_create": (ctypes.c_int32, [ctypes.POINTER(_LJ), ctypes.POINTER(_Ewald),
                                           ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
                                           ctypes.POINTER(_Species), ctypes.c_double, _D, _U64, _U64,
@@ -645,6 +679,122 @@ class Widom:
 
     def henry_coefficient(self, seed, stream, n_trials, draw_order=ALEA_DRAWS_RIGHT_TO_LEFT):
         return self.run(seed, stream, n_trials, draw_order=draw_order)["henry"]
+
+    def samples(self, seed, stream, n_trials, out_device_ptr, first_trial=0,
+                draw_order=ALEA_DRAWS_RIGHT_TO_LEFT, proposal=None):
+        """Trials as training rows {s0, s1, s2, -dU/T, lq} (float32, SAMPLE_ROW per
+        trial) written to a device buffer: uniform trials (lq = 0), or drawn from
+        a tabulated proposal (lq = its log density at the position)."""
+        _check(self._lib.alea_widom_samples(self._h, proposal._h if proposal else None, seed,
+                                            stream, first_trial, n_trials, draw_order,
+                                            out_device_ptr))
+
+    def run_biased(self, proposal, seed, stream, n_trials, first_trial=0, per_trial=False):
+        """Insertions drawn from the tabulated learned proposal; the weights are
+        exp(-dU/T)/p(s), so `henry` estimates the same K_H as run()."""
+        res = _WidomResult()
+        du = np.zeros(n_trials) if per_trial else None
+        fr = np.zeros((n_trials, 3)) if per_trial else None
+        _check(self._lib.alea_widom_run_biased(self._h, proposal._h, seed, stream, first_trial,
+                                               n_trials, ctypes.byref(res), _dp(du), _dp(fr)))
+        r = {f: getattr(res, f) for f, _ in res._fields_}
+        return (r, du, fr) if per_trial else r
+
+
+class Proposal:
+    """Learned insertion proposal: a Fourier-feature MLP log-density f(s) over
+    fractional positions, trained on the GPU, tabulated into the exact
+    piecewise-constant density that Widom (run_biased) and GCMC sample from."""
+
+    def __init__(self, n_freq=32, width=128, depth=3, freq_max=6, seed=7):
+        self._lib = library()
+        self._h = _VP()
+        cfg = _ProposalConfig(n_freq, width, depth, freq_max, seed)
+        _check(self._lib.alea_proposal_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+        self.n_freq, self.width, self.depth = n_freq, width, depth
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                self._lib.alea_proposal_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def param_count(self):
+        n = ctypes.c_uint64()
+        _check(self._lib.alea_proposal_param_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def wave_vectors(self):
+        k = np.zeros((self.n_freq, 3), np.int32)
+        _check(self._lib.alea_proposal_wave_vectors(self._h, k.ctypes.data_as(_I32), k.size))
+        return k
+
+    def get_params(self):
+        w = np.zeros(self.param_count(), np.float32)
+        _check(self._lib.alea_proposal_get_params(self._h, w.ctypes.data_as(_F), w.size))
+        return w
+
+    def set_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        _check(self._lib.alea_proposal_set_params(self._h, w.ctypes.data_as(_F), w.size))
+
+    def forward(self, s):
+        s = np.ascontiguousarray(s, dtype=np.float32).reshape(-1, 3)
+        out = np.zeros(len(s), np.float32)
+        _check(self._lib.alea_proposal_forward(self._h, s.ctypes.data_as(_F), len(s),
+                                               out.ctypes.data_as(_F)))
+        return out
+
+    def loss_grad(self, samples, tau=1.0):
+        """Loss and gradient for host rows {s, l} or {s, l, lq} (lq = 0 if absent)."""
+        samples = np.asarray(samples, dtype=np.float32)
+        if samples.shape[1] == 4:
+            samples = np.concatenate([samples, np.zeros((len(samples), 1), np.float32)], axis=1)
+        samples = np.ascontiguousarray(samples, dtype=np.float32).reshape(-1, SAMPLE_ROW)
+        g = np.zeros(self.param_count(), np.float32)
+        loss = ctypes.c_double()
+        _check(self._lib.alea_proposal_loss_grad(self._h, samples.ctypes.data_as(_F), len(samples),
+                                                 float(tau), ctypes.byref(loss),
+                                                 g.ctypes.data_as(_F), g.size))
+        return loss.value, g
+
+    def train(self, samples_device_ptr, n, epochs=20, batch=65536, lr=2e-3, tau=1.0,
+              beta1=0.9, beta2=0.999, eps=1e-8, seed=11, stream=None):
+        cfg = _TrainConfig(epochs, batch, lr, tau, beta1, beta2, eps, seed)
+        loss = ctypes.c_double()
+        _check(self._lib.alea_proposal_train(self._h, samples_device_ptr, n, ctypes.byref(cfg),
+                                             ctypes.byref(loss), stream))
+        return loss.value
+
+    def fit(self, widom, n_samples=1 << 18, rounds=2, epochs=30, batch=16384, lr=2e-3, tau=1.0,
+            cells=48, uniform_share=0.05, seed=1234, stream=7):
+        """Trains on the Widom context's own trials and tabulates: round 0 on
+        uniform trials, each further round on trials drawn from the previous
+        round's table (importance-weighted by its density). Returns the final loss.
+        Trial streams: (seed, stream + round)."""
+        import torch
+
+        rows = torch.empty((n_samples, SAMPLE_ROW), dtype=torch.float32, device="cuda")
+        loss = float("nan")
+        for r in range(rounds):
+            widom.samples(seed, stream + r, n_samples, rows.data_ptr(),
+                          proposal=self if r > 0 else None)
+            loss = self.train(rows.data_ptr(), n_samples, epochs=epochs, batch=batch, lr=lr,
+                              tau=tau, seed=seed + r)
+            self.tabulate(cells, uniform_share)
+        return loss
+
+    def tabulate(self, cells=64, uniform_share=0.05):
+        _check(self._lib.alea_proposal_tabulate(self._h, cells, float(uniform_share)))
+
+    def log_density(self, s):
+        s = _f64(np.asarray(s, dtype=np.float64).reshape(-1, 3))
+        out = np.zeros(len(s))
+        _check(self._lib.alea_proposal_log_density(self._h, _dp(s), len(s), _dp(out)))
+        return out
 
 
 class GcmcChains:

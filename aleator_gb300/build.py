@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libaleator_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["common.cu", "philox.cu", "grid.cu", "grid_cache.cpp", "lj.cu", "ewald.cu", "widom.cu",
-           "gcmc.cu", "capi.cu", "probe.cu", "noalloc.cu"]
+           "gcmc.cu", "proposal.cu", "capi.cu", "probe.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -1,6 +1,7 @@
 // extern "C" entry points of libaleator_gb300.so (declared in
 // include/aleator_gb300.h). Each call converts exceptions into an
 // alea_status and records the message for alea_last_error().
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -21,6 +22,9 @@ struct alea_widom {
 };
 struct alea_gcmc {
     alea::GcmcImpl* impl;
+};
+struct alea_proposal {
+    alea::ProposalImpl* impl;
 };
 
 namespace {
@@ -567,6 +571,143 @@ alea_status alea_widom_run(alea_widom* w, uint64_t seed, uint64_t stream, uint64
         need(w, "widom");
         need(out, "out");
         alea::widom_run(w->impl, seed, stream, first_trial, n_trials, draw_order, out, per_trial_du);
+    });
+}
+
+alea_status alea_widom_samples(alea_widom* w, const alea_proposal* proposal, uint64_t seed,
+                               uint64_t stream, uint64_t first_trial, uint64_t n_trials,
+                               int32_t draw_order, float* samples_device) {
+    return guarded([&] {
+        need(w, "widom");
+        alea::require(samples_device || n_trials == 0, ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_widom_samples: samples_device is required");
+        if (proposal) {
+            const alea::ProposalTable t = alea::proposal_table(proposal->impl);
+            alea::widom_samples(w->impl, seed, stream, first_trial, n_trials, draw_order,
+                                samples_device, &t);
+        } else {
+            alea::widom_samples(w->impl, seed, stream, first_trial, n_trials, draw_order,
+                                samples_device, nullptr);
+        }
+    });
+}
+
+alea_status alea_widom_run_biased(alea_widom* w, const alea_proposal* p, uint64_t seed,
+                                  uint64_t stream, uint64_t first_trial, uint64_t n_trials,
+                                  alea_widom_result* out, double* per_trial_du,
+                                  double* per_trial_frac) {
+    return guarded([&] {
+        need(w, "widom");
+        need(p, "proposal");
+        need(out, "out");
+        const alea::ProposalTable t = alea::proposal_table(p->impl);
+        alea::widom_run(w->impl, seed, stream, first_trial, n_trials, ALEA_DRAWS_RIGHT_TO_LEFT, out,
+                        per_trial_du, &t, per_trial_frac);
+    });
+}
+
+alea_status alea_proposal_create(const alea_proposal_config* config, alea_proposal** out) {
+    return guarded([&] {
+        need(config, "config");
+        need(out, "out");
+        *out = nullptr;
+        auto* impl = alea::proposal_create(*config);
+        *out = new alea_proposal{impl};
+    });
+}
+
+alea_status alea_proposal_param_count(const alea_proposal* p, uint64_t* out) {
+    return guarded([&] {
+        need(p, "proposal");
+        need(out, "out");
+        *out = alea::proposal_param_count(p->impl);
+    });
+}
+
+alea_status alea_proposal_wave_vectors(const alea_proposal* p, int32_t* out, uint64_t cap) {
+    return guarded([&] {
+        need(p, "proposal");
+        const auto& k = alea::proposal_wave_vectors(p->impl);
+        alea::require(out && cap >= k.size(), ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_proposal_wave_vectors: output too small");
+        std::copy(k.begin(), k.end(), out);
+    });
+}
+
+alea_status alea_proposal_get_params(const alea_proposal* p, float* out, uint64_t n) {
+    return guarded([&] {
+        need(p, "proposal");
+        alea::require(out && n >= alea::proposal_param_count(p->impl), ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_proposal_get_params: output too small");
+        alea::proposal_get_params(p->impl, out);
+    });
+}
+
+alea_status alea_proposal_set_params(alea_proposal* p, const float* in, uint64_t n) {
+    return guarded([&] {
+        need(p, "proposal");
+        alea::require(in && n == alea::proposal_param_count(p->impl), ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_proposal_set_params: wrong parameter count");
+        alea::proposal_set_params(p->impl, in);
+    });
+}
+
+alea_status alea_proposal_forward(alea_proposal* p, const float* s, uint64_t n, float* out) {
+    return guarded([&] {
+        need(p, "proposal");
+        alea::require((s && out) || n == 0, ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_proposal_forward: s and out are required");
+        alea::proposal_forward_host(p->impl, s, n, out);
+    });
+}
+
+alea_status alea_proposal_loss_grad(alea_proposal* p, const float* samples, uint64_t n,
+                                    double tau, double* loss, float* grad, uint64_t n_grad) {
+    return guarded([&] {
+        need(p, "proposal");
+        alea::require(samples && loss && grad, ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_proposal_loss_grad: samples, loss and grad are required");
+        alea::require(n_grad >= alea::proposal_param_count(p->impl), ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_proposal_loss_grad: gradient output too small");
+        *loss = alea::proposal_loss_grad_host(p->impl, samples, n, tau, grad);
+    });
+}
+
+alea_status alea_proposal_train(alea_proposal* p, const float* samples_device, uint64_t n,
+                                const alea_proposal_train_config* config, double* final_loss,
+                                void* cuda_stream) {
+    return guarded([&] {
+        need(p, "proposal");
+        alea::require(samples_device && config, ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_proposal_train: samples_device and config are required");
+        const double l = alea::proposal_train(p->impl, samples_device, n, *config,
+                                              (cudaStream_t)cuda_stream);
+        if (final_loss) *final_loss = l;
+    });
+}
+
+alea_status alea_proposal_tabulate(alea_proposal* p, uint32_t cells, double uniform_share) {
+    return guarded([&] {
+        need(p, "proposal");
+        alea::proposal_tabulate(p->impl, cells, uniform_share);
+    });
+}
+
+alea_status alea_proposal_log_density(const alea_proposal* p, const double* s, uint64_t n,
+                                      double* out) {
+    return guarded([&] {
+        need(p, "proposal");
+        alea::require((s && out) || n == 0, ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_proposal_log_density: s and out are required");
+        for (uint64_t i = 0; i < n; ++i) out[i] = alea::proposal_log_density_host(p->impl, s + 3 * i);
+    });
+}
+
+alea_status alea_proposal_destroy(alea_proposal* p) {
+    return guarded([&] {
+        if (!p) return;
+        alea::proposal_destroy(p->impl);
+        delete p;
     });
 }
 

@@ -92,13 +92,40 @@ struct EwaldDeviceView {
 };
 EwaldDeviceView ewald_state_view(const EwaldStateImpl* s);
 
+// proposal.cu: the learned insertion proposal and its tabulated density
+struct ProposalImpl;
+struct ProposalTable {
+    int cells;          // per axis; cell c = (iz cells + iy) cells + ix
+    const double* cdf;  // cumulative cell probabilities (device), last = 1
+    const double* logp; // log of the cell density relative to uniform (device)
+};
+ProposalImpl* proposal_create(const alea_proposal_config& c);
+void proposal_destroy(ProposalImpl* P);
+uint64_t proposal_param_count(const ProposalImpl* P);
+const std::vector<int32_t>& proposal_wave_vectors(const ProposalImpl* P);
+void proposal_get_params(const ProposalImpl* P, float* out);
+void proposal_set_params(ProposalImpl* P, const float* in);
+void proposal_forward_host(ProposalImpl* P, const float* s, uint64_t n, float* out);
+double proposal_loss_grad_host(ProposalImpl* P, const float* samples, uint64_t n, double tau,
+                               float* grad);
+double proposal_train(ProposalImpl* P, const float* samples_dev, uint64_t pool,
+                      const alea_proposal_train_config& c, cudaStream_t s);
+void proposal_tabulate(ProposalImpl* P, uint32_t cells, double uniform_share);
+ProposalTable proposal_table(const ProposalImpl* P);
+double proposal_log_density_host(const ProposalImpl* P, const double* s);
+
 // widom.cu
 struct WidomImpl;
 WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
                         const alea_particles& fw, const alea_lattice& lat,
                         const alea_molecule_species& guest, double temperature, int precision);
 void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
-               int draw_order, alea_widom_result* out, double* per_trial);
+               int draw_order, alea_widom_result* out, double* per_trial,
+               const ProposalTable* proposal = nullptr, double* per_trial_frac = nullptr);
+// Trials as training rows {s0, s1, s2, -dU/T, lq} (device): uniform when
+// proposal is null (lq = 0), else drawn from the proposal (lq = log density).
+void widom_samples(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+                   int draw_order, float* samples_dev, const ProposalTable* proposal);
 void widom_destroy(WidomImpl* w);
 
 // gcmc.cu

@@ -18,6 +18,7 @@
 // log-sum-exp: per block (max, sum exp(l - max), sum exp(2(l - max))), then
 // across blocks in block order.
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -74,7 +75,8 @@ widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
              const KRow* __restrict__ rows, const double* __restrict__ w,
              const double* __restrict__ sre, const double* __restrict__ sim, uint64_t seed,
              uint64_t stream, uint64_t first, uint64_t n, int draw_order,
-             double* __restrict__ per_trial, double* __restrict__ partial) {
+             double* __restrict__ per_trial, double* __restrict__ partial, const ProposalTable tab,
+             double* __restrict__ frac_out, float* __restrict__ samples_out) {
     __shared__ double4 tile[ATILE];
     __shared__ uint32_t ttype[ATILE];
     __shared__ PairParams pp[MAXS * MAXT];
@@ -92,14 +94,34 @@ widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
     const double* M = P.L.m;
 
     // ---- position and orientation (monte_carlo_engine.cc:882-901)
-    const uint64_t per = ns > 1 ? 6 : 3;
+    const uint64_t per = tab.cells > 0 ? 8 : ns > 1 ? 6 : 3;
     const uint64_t c0 = per * trial;
-    double u[3] = {philox_uniform(seed, stream, c0), philox_uniform(seed, stream, c0 + 1),
-                   philox_uniform(seed, stream, c0 + 2)};
-    if (draw_order == ALEA_DRAWS_RIGHT_TO_LEFT) {
-        const double tmp = u[0];
-        u[0] = u[2];
-        u[2] = tmp;
+    double u[3];
+    uint32_t cell = 0;
+    if (tab.cells > 0) {
+        // learned proposal: a cell from the tabulated CDF (first entry above
+        // the draw), then a uniform point inside it
+        const uint32_t C = (uint32_t)tab.cells;
+        const double uc = philox_uniform(seed, stream, c0);
+        uint32_t lo = 0, hi = C * C * C - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) / 2;
+            if (__ldg(&tab.cdf[mid]) > uc) hi = mid; else lo = mid + 1;
+        }
+        cell = lo;
+        const uint32_t ix = cell % C, iy = (cell / C) % C, iz = cell / (C * C);
+        u[0] = ((double)ix + philox_uniform(seed, stream, c0 + 1)) / (double)C;
+        u[1] = ((double)iy + philox_uniform(seed, stream, c0 + 2)) / (double)C;
+        u[2] = ((double)iz + philox_uniform(seed, stream, c0 + 3)) / (double)C;
+    } else {
+        u[0] = philox_uniform(seed, stream, c0);
+        u[1] = philox_uniform(seed, stream, c0 + 1);
+        u[2] = philox_uniform(seed, stream, c0 + 2);
+        if (draw_order == ALEA_DRAWS_RIGHT_TO_LEFT) {
+            const double tmp = u[0];
+            u[0] = u[2];
+            u[2] = tmp;
+        }
     }
     double ref[3];
 #pragma unroll
@@ -107,9 +129,10 @@ widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
         ref[c] = add_rn(add_rn(mul_rn(M[c], u[0]), mul_rn(M[3 + c], u[1])), mul_rn(M[6 + c], u[2]));
     double q[4] = {1.0, 0.0, 0.0, 0.0};
     if (ns > 1) {
-        double v[3] = {philox_uniform(seed, stream, c0 + 3), philox_uniform(seed, stream, c0 + 4),
-                       philox_uniform(seed, stream, c0 + 5)};
-        if (draw_order == ALEA_DRAWS_RIGHT_TO_LEFT) {
+        const uint64_t q0 = tab.cells > 0 ? c0 + 4 : c0 + 3;
+        double v[3] = {philox_uniform(seed, stream, q0), philox_uniform(seed, stream, q0 + 1),
+                       philox_uniform(seed, stream, q0 + 2)};
+        if (tab.cells == 0 && draw_order == ALEA_DRAWS_RIGHT_TO_LEFT) {
             const double tmp = v[0];
             v[0] = v[2];
             v[2] = tmp;
@@ -267,9 +290,19 @@ widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
     }
 
     if (active && per_trial) per_trial[local] = du;
+    if (active && frac_out)
+        for (int a = 0; a < 3; ++a) frac_out[3 * local + a] = u[a];
+    if (active && samples_out) {
+        float* o = samples_out + ALEA_SAMPLE_ROW * local;
+        for (int a = 0; a < 3; ++a) o[a] = (float)u[a];
+        o[3] = (float)((-du) / P.temperature);
+        o[4] = tab.cells > 0 ? (float)__ldg(&tab.logp[cell]) : 0.f;
+    }
 
-    // ---- log-sum-exp of -du/T over the block (fixed order)
-    const double lw = active ? (-du) / P.temperature : -INFINITY;
+    // ---- log-sum-exp of -du/T (minus log p(s) for the learned proposal)
+    // over the block (fixed order)
+    double lw = active ? (-du) / P.temperature : -INFINITY;
+    if (active && tab.cells > 0) lw -= __ldg(&tab.logp[cell]);
     red[threadIdx.x] = lw;
     __syncthreads();
     for (int s = WT / 2; s > 0; s >>= 1) {
@@ -330,7 +363,7 @@ struct WidomImpl {
     DevBuf<PairParams> table;
     DevBuf<KRow> rows;
     EwaldStateImpl* ews = nullptr;
-    DevBuf<double> partial, result, per_trial;
+    DevBuf<double> partial, result, per_trial, per_trial_frac;
     ~WidomImpl() {
         if (ews) ewald_state_destroy(ews);
     }
@@ -434,15 +467,10 @@ WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
     return w;
 }
 
-void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
-               int draw_order, alea_widom_result* out, double* per_trial) {
-    require(n > 0, ALEA_ERR_INVALID_ARGUMENT, "Widom: numTrials must be positive");
-    require(draw_order == ALEA_DRAWS_RIGHT_TO_LEFT || draw_order == ALEA_DRAWS_LEFT_TO_RIGHT,
-            ALEA_ERR_INVALID_ARGUMENT, "Widom: unknown draw order");
+static void widom_launch(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+                         int draw_order, bool per_trial, const ProposalTable& tab,
+                         double* frac_dev, float* samples_dev) {
     const uint64_t nblocks = (n + WT - 1) / WT;
-    require(nblocks < (1ull << 31), ALEA_ERR_INVALID_ARGUMENT, "Widom: too many trials per call");
-    if (w->partial.n < 3 * nblocks) w->partial.alloc(3 * nblocks);
-    if (per_trial && w->per_trial.n < n) w->per_trial.alloc(n);
     const double* w_ = nullptr;
     const double *sre = nullptr, *sim = nullptr;
     if (w->ews) {
@@ -451,21 +479,54 @@ void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uin
         sre = v.sre;
         sim = v.sim;
     }
-    cudaEvent_t e0, e1;
-    ALEA_CUDA(cudaEventCreate(&e0));
-    ALEA_CUDA(cudaEventCreate(&e1));
-    ALEA_CUDA(cudaEventRecord(e0));
     if (w->precision == ALEA_FP32)
         widom_kernel<float><<<(unsigned)nblocks, WT>>>(w->P, w->atoms.p, w->types.p, w->table.p,
                                                        w->rows.p, w_, sre, sim, seed, stream, first,
                                                        n, draw_order, per_trial ? w->per_trial.p : nullptr,
-                                                       w->partial.p);
+                                                       w->partial.p, tab, frac_dev, samples_dev);
     else
         widom_kernel<double><<<(unsigned)nblocks, WT>>>(w->P, w->atoms.p, w->types.p, w->table.p,
                                                         w->rows.p, w_, sre, sim, seed, stream, first,
                                                         n, draw_order, per_trial ? w->per_trial.p : nullptr,
-                                                        w->partial.p);
+                                                        w->partial.p, tab, frac_dev, samples_dev);
     ALEA_CUDA(cudaGetLastError());
+}
+
+void widom_samples(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+                   int draw_order, float* samples_dev, const ProposalTable* proposal) {
+    require(draw_order == ALEA_DRAWS_RIGHT_TO_LEFT || draw_order == ALEA_DRAWS_LEFT_TO_RIGHT,
+            ALEA_ERR_INVALID_ARGUMENT, "Widom: unknown draw order");
+    if (n == 0) return;
+    const uint64_t chunk = (uint64_t)WT << 20;  // trials per launch
+    for (uint64_t a = 0; a < n; a += chunk) {
+        const uint64_t m = std::min(chunk, n - a);
+        const uint64_t nblocks = (m + WT - 1) / WT;
+        if (w->partial.n < 3 * nblocks) w->partial.alloc(3 * nblocks);
+        widom_launch(w, seed, stream, first + a, m, draw_order, false,
+                     proposal ? *proposal : ProposalTable{0, nullptr, nullptr}, nullptr,
+                     samples_dev + ALEA_SAMPLE_ROW * a);
+    }
+    ALEA_CUDA(cudaDeviceSynchronize());
+}
+
+void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
+               int draw_order, alea_widom_result* out, double* per_trial,
+               const ProposalTable* proposal, double* per_trial_frac) {
+    require(n > 0, ALEA_ERR_INVALID_ARGUMENT, "Widom: numTrials must be positive");
+    require(draw_order == ALEA_DRAWS_RIGHT_TO_LEFT || draw_order == ALEA_DRAWS_LEFT_TO_RIGHT,
+            ALEA_ERR_INVALID_ARGUMENT, "Widom: unknown draw order");
+    const uint64_t nblocks = (n + WT - 1) / WT;
+    require(nblocks < (1ull << 31), ALEA_ERR_INVALID_ARGUMENT, "Widom: too many trials per call");
+    if (w->partial.n < 3 * nblocks) w->partial.alloc(3 * nblocks);
+    if (per_trial && w->per_trial.n < n) w->per_trial.alloc(n);
+    if (per_trial_frac && w->per_trial_frac.n < 3 * n) w->per_trial_frac.alloc(3 * n);
+    const ProposalTable tab = proposal ? *proposal : ProposalTable{0, nullptr, nullptr};
+    cudaEvent_t e0, e1;
+    ALEA_CUDA(cudaEventCreate(&e0));
+    ALEA_CUDA(cudaEventCreate(&e1));
+    ALEA_CUDA(cudaEventRecord(e0));
+    widom_launch(w, seed, stream, first, n, draw_order, per_trial != nullptr, tab,
+                 per_trial_frac ? w->per_trial_frac.p : nullptr, nullptr);
     widom_combine_kernel<<<1, 32>>>(w->partial.p, nblocks, w->result.p);
     ALEA_CUDA(cudaGetLastError());
     ALEA_CUDA(cudaEventRecord(e1));
@@ -478,6 +539,10 @@ void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uin
     ALEA_CUDA(cudaMemcpy(r, w->result.p, sizeof r, cudaMemcpyDeviceToHost));
     if (per_trial) {
         ALEA_CUDA(cudaMemcpy(per_trial, w->per_trial.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    if (per_trial_frac) {
+        ALEA_CUDA(cudaMemcpy(per_trial_frac, w->per_trial_frac.p, 3 * n * sizeof(double),
+                             cudaMemcpyDeviceToHost));
     }
     const double nn = (double)n;
     const double mean_scaled = r[1] / nn;  // mean(exp(l - max))

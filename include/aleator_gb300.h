@@ -305,6 +305,75 @@ alea_status alea_widom_run(alea_widom* w, uint64_t seed, uint64_t stream, uint64
                            double* per_trial_du);
 alea_status alea_widom_destroy(alea_widom* w);
 
+/* ------------------------------------------------------------------ learned insertion proposal */
+/* No counterpart in the reference, whose insertions are uniform
+ * (monte_carlo_engine.cc:572-574, 882-884). A Fourier-feature MLP log-density
+ * f(s) over fractional positions s in [0,1)^3 (2 n_freq periodic features
+ * (sin, cos)(2 pi k.s) with integer k, `depth` SiLU layers of `width`, one
+ * output; BF16 weights, FP32 accumulation), trained on the GPU on
+ * Boltzmann-weighted uniform Widom samples, then tabulated on cells^3 cells
+ * and mixed with a uniform share. Widom and GCMC sample from that table, so
+ * the proposal density that enters their weights is exact. */
+typedef struct alea_proposal alea_proposal;
+typedef struct {
+    uint32_t n_freq;   /* wave vectors: 2 n_freq features */
+    uint32_t width;    /* hidden width */
+    uint32_t depth;    /* hidden layers */
+    uint32_t freq_max; /* wave-vector components uniform in [-freq_max, freq_max] */
+    uint64_t seed;     /* wave vectors and initial weights (Philox streams 1, 2) */
+} alea_proposal_config;
+alea_status alea_proposal_create(const alea_proposal_config* config, alea_proposal** out);
+alea_status alea_proposal_param_count(const alea_proposal* p, uint64_t* out);
+/* n_freq x 3 integer wave vectors */
+alea_status alea_proposal_wave_vectors(const alea_proposal* p, int32_t* out, uint64_t cap);
+/* FP32 master weights: per layer W [out x in] row-major, then b [out] */
+alea_status alea_proposal_get_params(const alea_proposal* p, float* out, uint64_t n);
+alea_status alea_proposal_set_params(alea_proposal* p, const float* in, uint64_t n);
+/* f(s) at n host positions (3 floats each) */
+alea_status alea_proposal_forward(alea_proposal* p, const float* s, uint64_t n, float* out);
+/* Training rows are ALEA_SAMPLE_ROW floats {s0, s1, s2, l, lq}: a fractional
+ * position, its log-weight l = -dU/T and the log density lq (relative to
+ * uniform) of the proposal it was drawn from (0 for uniform trials). */
+#define ALEA_SAMPLE_ROW 5
+/* Loss L = -sum_i softmax(tau l - lq)_i f_i + log mean_i exp(f_i - lq_i)
+ * over one batch of host rows, and dL/dweights. */
+alea_status alea_proposal_loss_grad(alea_proposal* p, const float* samples, uint64_t n,
+                                    double tau, double* loss, float* grad, uint64_t n_grad);
+typedef struct {
+    uint32_t epochs;
+    uint32_t batch;
+    double lr, tau, beta1, beta2, eps;
+    uint64_t seed;     /* per-epoch sample order (Philox stream 3) */
+} alea_proposal_train_config;
+/* Adam over n device rows (as alea_widom_samples writes them). */
+alea_status alea_proposal_train(alea_proposal* p, const float* samples_device, uint64_t n,
+                                const alea_proposal_train_config* config, double* final_loss,
+                                void* cuda_stream);
+/* P_c = (1 - uniform_share) softmax(f(centre_c)) + uniform_share / cells^3 */
+alea_status alea_proposal_tabulate(alea_proposal* p, uint32_t cells, double uniform_share);
+/* log of the tabulated density relative to uniform at n fractional positions (3 doubles each) */
+alea_status alea_proposal_log_density(const alea_proposal* p, const double* s, uint64_t n,
+                                      double* out);
+alea_status alea_proposal_destroy(alea_proposal* p);
+
+/* Widom trials as training rows (ALEA_SAMPLE_ROW floats each) written to
+ * device memory: uniform trials as alea_widom_run draws them when proposal is
+ * NULL (lq = 0), else trials drawn as alea_widom_run_biased draws them (lq =
+ * log of the proposal's density at the position). */
+alea_status alea_widom_samples(alea_widom* w, const alea_proposal* proposal, uint64_t seed,
+                               uint64_t stream, uint64_t first_trial, uint64_t n_trials,
+                               int32_t draw_order, float* samples_device);
+/* Widom with insertion positions drawn from the tabulated proposal: trial t
+ * uses Philox calls 8t (cell, from the CDF), 8t+1..8t+3 (point in the cell)
+ * and 8t+4..8t+6 (orientation, several sites); its weight is
+ * exp(-dU/T) / p(s) with p the density relative to uniform, so
+ * henry = mean / T estimates the same K_H as the uniform method.
+ * per_trial_du and per_trial_frac (3 doubles per trial) are optional. */
+alea_status alea_widom_run_biased(alea_widom* w, const alea_proposal* p, uint64_t seed,
+                                  uint64_t stream, uint64_t first_trial, uint64_t n_trials,
+                                  alea_widom_result* out, double* per_trial_du,
+                                  double* per_trial_frac);
+
 /* ------------------------------------------------------------------ GCMC chains */
 /* MonteCarloEngine (engines/monte_carlo/monte_carlo_engine.hpp:76-83, single
  * species, direct-scan dispersion) for n_chains independent chains at once:
