@@ -199,6 +199,7 @@ _SIGNATURES = {
     "alea_gcmc_particles": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D, ctypes.c_uint64, _U64]),
     "alea_gcmc_ewald_energy": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D]),
     "alea_gcmc_destroy": (ctypes.c_int32, [_VP]),
+    "alea_gcmc_set_proposal": (ctypes.c_int32, [_VP, _VP]),
     "alea_insertion_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                                ctypes.c_double, ctypes.c_double]),
     "alea_deletion_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
@@ -840,6 +841,11 @@ class GcmcChains:
 
     def run(self, steps, stream=0):
         _check(self._lib.alea_gcmc_run(self._h, int(steps), stream))
+
+    def set_proposal(self, proposal):
+        """Insert and delete with a tabulated learned Proposal from now on (its
+        density enters the acceptance ratios); None restores uniform insertion."""
+        _check(self._lib.alea_gcmc_set_proposal(self._h, proposal._h if proposal else None))
 
     def info(self, chain=0):
         s = _ChainInfo()

@@ -606,6 +606,18 @@ alea_status alea_widom_run_biased(alea_widom* w, const alea_proposal* p, uint64_
     });
 }
 
+alea_status alea_gcmc_set_proposal(alea_gcmc* g, const alea_proposal* p) {
+    return guarded([&] {
+        need(g, "gcmc");
+        if (!p) {
+            alea::gcmc_set_proposal(g->impl, nullptr);
+            return;
+        }
+        const alea::ProposalTable t = alea::proposal_table(p->impl);
+        alea::gcmc_set_proposal(g->impl, &t);
+    });
+}
+
 alea_status alea_proposal_create(const alea_proposal_config* config, alea_proposal** out) {
     return guarded([&] {
         need(config, "config");

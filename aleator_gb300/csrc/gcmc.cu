@@ -67,6 +67,10 @@ struct GcmcConst {
     double b[9];
     double self_pref, rec_pref;
     double fw_q2;
+    // learned insertion proposal (prop_cells == 0: the reference's uniform
+    // insertion): the template centred on its centroid, and the table size
+    int prop_cells;
+    double tc[MAXS][3];
 };
 
 struct GcmcPtrs {
@@ -84,6 +88,8 @@ struct GcmcPtrs {
     uint32_t* mol;
     double *sre, *sim, *dre, *dim;
     unsigned* flags;
+    const double* pcdf;   // proposal cell CDF
+    const double* plogp;  // log of the cell density relative to uniform
 };
 
 struct StepShared {
@@ -97,6 +103,7 @@ struct StepShared {
     uint32_t ex[MAXS];
     double e_lj[2 * MAXS], e_el[2 * MAXS];
     double rec_sum, dself, dexcl;
+    double lq;  // learned proposal: log density at the inserted / deleted centroid
 };
 
 __device__ __forceinline__ double u01(ChainState& c) {
@@ -151,9 +158,70 @@ __device__ void rotate_about_axis(const double* v, const double* a, double th, d
     for (int i = 0; i < 3; ++i) o[i] = add_rn(add_rn(mul_rn(v[i], c), mul_rn(cr[i], s)), mul_rn(a[i], ad));
 }
 
+// Proposal cell of a fractional position (wrapped into [0, 1)).
+__device__ __forceinline__ uint32_t proposal_cell(int cells, const double* f) {
+    uint32_t idx[3];
+    for (int a = 0; a < 3; ++a) {
+        const double w = f[a] - floor(f[a]);
+        const int i = (int)(w * cells);
+        idx[a] = (uint32_t)min(max(i, 0), cells - 1);
+    }
+    return (idx[2] * (uint32_t)cells + idx[1]) * (uint32_t)cells + idx[0];
+}
+
+// Learned-proposal insertion: the centroid from the tabulated density (a cell
+// from the CDF, a uniform point inside it; draws 1 and 2..4), a uniform
+// orientation (draws 5..7, in order), the template centred on its centroid.
+__device__ void plan_biased_insertion(const GcmcConst& C, const GcmcPtrs& P, ChainState& c,
+                                      StepShared& S) {
+    const uint32_t cells = (uint32_t)C.prop_cells;
+    const double uc = u01(c);
+    uint32_t lo = 0, hi = cells * cells * cells - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (P.pcdf[mid] > uc) hi = mid; else lo = mid + 1;
+    }
+    const uint32_t idx[3] = {lo % cells, (lo / cells) % cells, lo / (cells * cells)};
+    double u[3];
+    for (int a = 0; a < 3; ++a) u[a] = ((double)idx[a] + u01(c)) / (double)cells;
+    S.lq = P.plogp[lo];
+    const double* M = C.L.m;
+    double ref[3];
+    for (int k = 0; k < 3; ++k)
+        ref[k] = add_rn(add_rn(mul_rn(M[k], u[0]), mul_rn(M[3 + k], u[1])), mul_rn(M[6 + k], u[2]));
+    const int ns = C.ns;
+    double q[4] = {1.0, 0.0, 0.0, 0.0};
+    if (ns > 1) {
+        const double v0 = u01(c), v1 = u01(c), v2 = u01(c);
+        const double r1 = __dsqrt_rn(sub_rn(1.0, v0)), r2 = __dsqrt_rn(v0);
+        const double t1 = mul_rn(2.0 * kPi, v1), t2 = mul_rn(2.0 * kPi, v2);
+        q[0] = mul_rn(r2, cos(t2));
+        q[1] = mul_rn(r1, sin(t1));
+        q[2] = mul_rn(r1, cos(t1));
+        q[3] = mul_rn(r2, sin(t2));
+    }
+    for (int s = 0; s < ns; ++s) {
+        const double* loc = C.tc[s];
+        double rot[3] = {loc[0], loc[1], loc[2]};
+        if (ns > 1) {
+            const double qv[3] = {q[1], q[2], q[3]};
+            const double cr[3] = {sub_rn(mul_rn(qv[1], loc[2]), mul_rn(qv[2], loc[1])),
+                                  sub_rn(mul_rn(qv[2], loc[0]), mul_rn(qv[0], loc[2])),
+                                  sub_rn(mul_rn(qv[0], loc[1]), mul_rn(qv[1], loc[0]))};
+            const double t[3] = {mul_rn(cr[0], 2.0), mul_rn(cr[1], 2.0), mul_rn(cr[2], 2.0)};
+            const double c2[3] = {sub_rn(mul_rn(qv[1], t[2]), mul_rn(qv[2], t[1])),
+                                  sub_rn(mul_rn(qv[2], t[0]), mul_rn(qv[0], t[2])),
+                                  sub_rn(mul_rn(qv[0], t[1]), mul_rn(qv[1], t[0]))};
+            for (int i = 0; i < 3; ++i) rot[i] = add_rn(add_rn(loc[i], mul_rn(t[i], q[0])), c2[i]);
+        }
+        for (int i = 0; i < 3; ++i) S.np_[s][i] = add_rn(ref[i], rot[i]);
+    }
+    S.n_new = ns;
+}
+
 // Thread 0: the draws and trial geometry of one move.
-__device__ void plan_move(const GcmcConst& C, ChainState& c, const double* gx, const double* gy,
-                          const double* gz, const uint32_t* mol, StepShared& S) {
+__device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, const double* gx,
+                          const double* gy, const double* gz, const uint32_t* mol, StepShared& S) {
     const double pick = u01(c);
     S.move = pick < 0.25 ? 0 : pick < 0.5 ? 1 : pick < 0.75 ? 2 : 3;
     S.valid = 1;
@@ -161,7 +229,12 @@ __device__ void plan_move(const GcmcConst& C, ChainState& c, const double* gx, c
     S.do_resync = 0;
     S.n_old = S.n_new = 0;
     S.ng = c.n_guest;
+    S.lq = 0.0;
     const int ns = C.ns;
+    if (S.move == 2 && C.prop_cells > 0) {
+        plan_biased_insertion(C, P, c, S);
+        return;
+    }
     if (S.move == 2) {  // monte_carlo_engine.cc:568-590
         double u[3];
         u[0] = u01(c);
@@ -229,7 +302,19 @@ __device__ void plan_move(const GcmcConst& C, ChainState& c, const double* gx, c
         S.op[s][2] = gz[slot];
     }
     S.n_old = ns;
-    if (S.move == 3) return;
+    if (S.move == 3) {
+        if (C.prop_cells > 0) {  // the proposal's density at the molecule's centroid
+            double cen[3] = {0.0, 0.0, 0.0};
+            for (int s = 0; s < ns; ++s)
+                for (int i = 0; i < 3; ++i) cen[i] += S.op[s][i];
+            for (int i = 0; i < 3; ++i) cen[i] /= (double)ns;
+            double f[3];
+            for (int a = 0; a < 3; ++a)
+                f[a] = cen[0] * C.L.inv[a] + cen[1] * C.L.inv[3 + a] + cen[2] * C.L.inv[6 + a];
+            S.lq = P.plogp[proposal_cell(C.prop_cells, f)];
+        }
+        return;
+    }
     if (S.move == 0) {  // braced initializer: left-to-right draws (:454-456)
         double d[3];
         for (int i = 0; i < 3; ++i) d[i] = mul_rn(sub_rn(mul_rn(2.0, u01(c)), 1.0), C.max_trans);
@@ -288,7 +373,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     for (uint64_t step = 0; step < steps; ++step) {
         if (threadIdx.x == 0) {
             if (c.err == 0) {
-                plan_move(C, c, gx, gy, gz, mol, S);
+                plan_move(C, P, c, gx, gy, gz, mol, S);
             } else {
                 S.valid = 0;
             }
@@ -418,9 +503,13 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 } else if (S.move == 2) {
                     du = u_new + e_new + rec;
                     ratio = (c.fugacity * C.volume / T) / (double)(c.n_mol + 1) * exp(-du / T);
+                    // learned proposal: divided by its density (relative to uniform)
+                    if (C.prop_cells > 0) ratio *= exp(-S.lq);
                 } else {
                     du = -(u_old + e_old) + rec;
                     ratio = (double)c.n_mol / (c.fugacity * C.volume / T) * exp(-du / T);
+                    // the reverse insertion's proposal density at this centroid
+                    if (C.prop_cells > 0) ratio *= exp(S.lq);
                 }
                 c.attempted[S.move]++;
                 const double prob = ratio < 1.0 ? ratio : 1.0;
@@ -577,6 +666,7 @@ struct GcmcImpl {
     DevBuf<double> gx, gy, gz, gq, sre, sim, dre, dim;
     DevBuf<uint32_t> gt, mol;
     DevBuf<unsigned> flags;
+    DevBuf<double> pcdf, plogp;  // the chains' copy of a tabulated proposal
     float last_ms = 0.f;
 };
 
@@ -618,7 +708,17 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
             C.sz[s] = guest.z[s];
             C.sq[s] = guest.charge ? guest.charge[s] : 0.0;
             C.slj[s] = guest.lj_species[s];
+            C.tc[s][0] = guest.x[s];
+            C.tc[s][1] = guest.y[s];
+            C.tc[s][2] = guest.z[s];
             qs += C.sq[s];
+        }
+        {  // the template about its centroid (the learned proposal's reference point)
+            double m[3] = {0.0, 0.0, 0.0};
+            for (int s = 0; s < C.ns; ++s)
+                for (int i = 0; i < 3; ++i) m[i] += C.tc[s][i];
+            for (int s = 0; s < C.ns; ++s)
+                for (int i = 0; i < 3; ++i) C.tc[s][i] -= m[i] / C.ns;
         }
         C.n_species = lj.n_species;
         C.rc = lj.cutoff;
@@ -759,6 +859,8 @@ void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s) {
     P.dre = g->dre.p;
     P.dim = g->dim.p;
     P.flags = g->flags.p;
+    P.pcdf = g->pcdf.p;
+    P.plogp = g->plogp.p;
     cudaEvent_t e0, e1;
     ALEA_CUDA(cudaEventCreate(&e0));
     ALEA_CUDA(cudaEventCreate(&e1));
@@ -826,6 +928,22 @@ double gcmc_ewald_energy(const GcmcImpl* g, uint32_t chain) {
     double sum = 0.0;
     for (uint64_t t = 0; t < nk; ++t) sum += w[t] * (re[t] * re[t] + im[t] * im[t]);
     return sum * kCoulomb * (2.0 * kPi / g->C.volume) + s.self_e + s.excl_e;
+}
+
+// Insertions and deletions from now on use the tabulated proposal (its
+// tables are copied), or the reference's uniform insertion when t is null.
+void gcmc_set_proposal(GcmcImpl* g, const ProposalTable* t) {
+    if (!t) {
+        g->C.prop_cells = 0;
+        return;
+    }
+    const uint64_t n = (uint64_t)t->cells * t->cells * t->cells;
+    g->pcdf.alloc(n);
+    g->plogp.alloc(n);
+    ALEA_CUDA(cudaMemcpy(g->pcdf.p, t->cdf, n * sizeof(double), cudaMemcpyDeviceToDevice));
+    ALEA_CUDA(cudaMemcpy(g->plogp.p, t->logp, n * sizeof(double), cudaMemcpyDeviceToDevice));
+    ALEA_CUDA(cudaDeviceSynchronize());
+    g->C.prop_cells = t->cells;
 }
 
 unsigned gcmc_chains(const GcmcImpl* g) { return g->n_chains; }

@@ -140,6 +140,7 @@ void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s);
 void gcmc_states(const GcmcImpl* g, ChainState* out);
 uint64_t gcmc_particles(const GcmcImpl* g, uint32_t chain, double* xyz, uint64_t cap);
 double gcmc_ewald_energy(const GcmcImpl* g, uint32_t chain);
+void gcmc_set_proposal(GcmcImpl* g, const ProposalTable* t);
 unsigned gcmc_chains(const GcmcImpl* g);
 float gcmc_last_ms(const GcmcImpl* g);
 void gcmc_destroy(GcmcImpl* g);

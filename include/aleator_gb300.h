@@ -411,6 +411,15 @@ alea_status alea_gcmc_particles(const alea_gcmc* g, uint32_t chain, double* xyz,
 /* electrostaticEnergyForTesting() (monte_carlo_engine.hpp:214, .cc:928-930). */
 alea_status alea_gcmc_ewald_energy(const alea_gcmc* g, uint32_t chain, double* out);
 alea_status alea_gcmc_destroy(alea_gcmc* g);
+/* Insertions and deletions of every chain from the next run on use the
+ * tabulated learned proposal (its table is copied): the insertion's centroid
+ * is drawn from it (Philox draws: move pick, cell, 3 in-cell, 3 orientation,
+ * accept) with the template centred on its centroid, and the acceptance
+ * ratios carry 1/p(centroid) (insertion) and p(centroid) (deletion), p the
+ * density relative to uniform, so detailed balance holds. NULL restores the
+ * reference's uniform insertion. Declared after alea_proposal below. */
+struct alea_proposal;
+alea_status alea_gcmc_set_proposal(alea_gcmc* g, const struct alea_proposal* p);
 
 /* ------------------------------------------------------------------ acceptance / EOS (host) */
 /* gcmc::insertionRatio ... clampToProbability (engines/monte_carlo/gcmc_acceptance.hpp:28-101) */

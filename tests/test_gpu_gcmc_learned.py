@@ -1,0 +1,90 @@
+"""GCMC chains inserting and deleting with the learned proposal.
+
+Detailed balance: for an ideal gas (every epsilon and charge zero) the
+stationary molecule count is Poisson with mean f V / T whatever the
+insertion density, so with a strongly non-uniform proposal the chains'
+mean count must still match f V / T (within 3 standard errors over
+independent chains) and their variance their mean (within 8 %); a density
+factor missing from either acceptance ratio would shift both.
+
+Loading: CH4 in the cubic test framework, chains with a proposal fitted to
+the framework's own Widom trials against chains with the reference's uniform
+insertion: equal mean loading within 3 combined standard errors (chain to
+chain)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from aleator_gb300 import workloads as W
+from oracle import proposal_oracle as PO
+
+pytestmark = pytest.mark.gpu
+
+T = 298.0
+
+
+def test_ideal_gas_poisson_with_biased_proposal(lib):
+    A, _ = lib
+    fw = W.cubic_framework(seed=11)
+    eps = np.zeros_like(fw.eps)
+    ff = A.LennardJones(eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData(fw.x, fw.y, fw.z, None, fw.species)
+    guest = W.ch4_guest(fw)
+    m = np.asarray(fw.lattice).reshape(3, 3)
+    V = abs(np.linalg.det(m))
+    lam = 12.0
+    f_int = lam * T / V
+    f_pa = f_int / O.PASCAL_TO_INTERNAL
+    n = 128
+    chains = A.GcmcChains(ff, p, fw.lattice, guest, T, [f_pa] * n, list(range(100, 100 + n)),
+                          [0] * n, max_molecules=200)
+    # a clearly non-uniform proposal: a random network, tabulated with a floor
+    P = A.Proposal(seed=21)
+    rng = np.random.default_rng(5)
+    w = P.get_params()
+    P.set_params((rng.normal(0, 1, w.size) * 0.25).astype(np.float32))
+    P.tabulate(16, 0.1)
+    lp = P.log_density(PO.cell_centres(16))
+    assert np.exp(lp).max() / np.exp(lp).min() > 8.0  # really non-uniform
+    chains.set_proposal(P)
+    chains.run(10000)  # equilibrate
+    before = [(chains.info(c)["sum_molecules"], chains.info(c)["sum_molecules_sq"]) for c in range(n)]
+    steps = 100000
+    chains.run(steps)
+    mean = np.array([(chains.info(c)["sum_molecules"] - before[c][0]) / steps for c in range(n)])
+    sq = np.array([(chains.info(c)["sum_molecules_sq"] - before[c][1]) / steps for c in range(n)])
+    se = mean.std(ddof=1) / np.sqrt(n)
+    assert abs(mean.mean() - lam) <= 3 * se + 1e-9, (mean.mean(), lam, se)
+    # variance pooled over all chains and steps (the within-chain variance
+    # alone misses the spread of the chain means: the count decorrelates over
+    # hundreds of moves when the proposal is far from the ideal gas's)
+    var = sq.mean() - mean.mean() ** 2
+    assert abs(var / lam - 1) <= 0.08, (var, lam)
+
+
+def test_learned_loading_matches_uniform(lib, orc):
+    A, _ = lib
+    fw = W.cubic_framework(seed=11)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    guest = W.ch4_guest(fw)
+    fug = orc.pr_fugacity(*W.METHANE_CRITICAL, T, 1e6)
+    n = 48
+    widom = A.Widom(ff, p, fw.lattice, guest, T)
+    P = A.Proposal(seed=2)
+    P.fit(widom, n_samples=1 << 17, rounds=2, epochs=20, cells=32)
+    out = {}
+    for name, prop in (("uniform", None), ("learned", P)):
+        ch = A.GcmcChains(ff, p, fw.lattice, guest, T, [fug] * n, list(range(500, 500 + n)),
+                          [1] * n, max_molecules=400)
+        if prop is not None:
+            ch.set_proposal(prop)
+        ch.run(20000)
+        before = [ch.info(c)["sum_molecules"] for c in range(n)]
+        steps = 40000
+        ch.run(steps)
+        out[name] = np.array([(ch.info(c)["sum_molecules"] - before[c]) / steps for c in range(n)])
+    mu, ml = out["uniform"], out["learned"]
+    se = np.hypot(mu.std(ddof=1), ml.std(ddof=1)) / np.sqrt(n)
+    assert mu.mean() > 0.5  # an adsorbing state point
+    assert abs(ml.mean() - mu.mean()) <= 3 * se, (ml.mean(), mu.mean(), se)
