@@ -23,6 +23,7 @@ from ._lib import (  # noqa: F401
     EwaldIncrementalState,
     FrameworkEnergyGrid,
     GcmcChains,
+    GridBatch,
     LennardJones,
     ParticleData,
     Proposal,

@@ -79,6 +79,13 @@ class _GridStats(ctypes.Structure):
                 ("launches", ctypes.c_uint32)]
 
 
+class _GridBatchStats(ctypes.Structure):
+    _fields_ = [("grids", ctypes.c_uint32), ("nodes", ctypes.c_uint64),
+                ("algorithmic_pairs", ctypes.c_uint64), ("executed_pairs", ctypes.c_uint64),
+                ("bricks", ctypes.c_uint64), ("last_ms", ctypes.c_float), ("variant", ctypes.c_int32),
+                ("tune_ms", ctypes.c_float * 2), ("graph_launches", ctypes.c_uint32)]
+
+
 class _ChainInfo(ctypes.Structure):
     _fields_ = [("molecules", ctypes.c_uint64), ("guest_sites", ctypes.c_uint64),
                 ("call_index", ctypes.c_uint64), ("steps", ctypes.c_uint64),
@@ -200,6 +207,16 @@ _SIGNATURES = {
     "alea_gcmc_ewald_energy": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D]),
     "alea_gcmc_destroy": (ctypes.c_int32, [_VP]),
     "alea_gcmc_set_proposal": (ctypes.c_int32, [_VP, _VP]),
+    "alea_grid_batch_create": (ctypes.c_int32, [ctypes.c_uint32, ctypes.POINTER(_LJ),
+                                                ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
+                                                _U32, ctypes.c_uint32, ctypes.c_double,
+                                                ctypes.POINTER(_VP)]),
+    "alea_grid_batch_build": (ctypes.c_int32, [_VP, _VP]),
+    "alea_grid_batch_stats_get": (ctypes.c_int32, [_VP, ctypes.POINTER(_GridBatchStats)]),
+    "alea_grid_batch_point_counts": (ctypes.c_int32, [_VP, ctypes.c_uint32, _I32]),
+    "alea_grid_batch_download": (ctypes.c_int32, [_VP, ctypes.c_uint32, ctypes.c_uint32, _D,
+                                                  ctypes.c_uint64]),
+    "alea_grid_batch_destroy": (ctypes.c_int32, [_VP]),
     "alea_insertion_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                                ctypes.c_double, ctypes.c_double]),
     "alea_deletion_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
@@ -700,6 +717,59 @@ class Widom:
                                                n_trials, ctypes.byref(res), _dp(du), _dp(fr)))
         r = {f: getattr(res, f) for f, _ in res._fields_}
         return (r, du, fr) if per_trial else r
+
+
+class GridBatch:
+    """Many independent FP32 energy grids (each framework with its own force
+    field, atoms and cell) built together: one persistent launch per kernel,
+    replayed from a CUDA graph captured after an autotuning first build."""
+
+    def __init__(self, force_fields, frameworks, lattices, guests, spacing):
+        self._lib = library()
+        self._h = _VP()
+        n = len(frameworks)
+        assert len(force_fields) == n and len(lattices) == n and len(guests) == n
+        self._keep = [ff for ff in force_fields] + list(frameworks)
+        ljs = (_LJ * n)(*[ff.c() for ff in force_fields])
+        ps = (_Particles * n)(*[p.c() for p in frameworks])
+        lats = (_Lattice * n)(*[_lattice(m) for m in lattices])
+        ng = len(guests[0])
+        g = np.ascontiguousarray(np.asarray(guests, dtype=np.uint32).reshape(n, ng))
+        self._lists = (ljs, ps, lats, g)
+        _check(self._lib.alea_grid_batch_create(n, ljs, ps, lats, _u32p(g), ng, float(spacing),
+                                                ctypes.byref(self._h)))
+        self.n = n
+        self.guests = g
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                self._lib.alea_grid_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def build(self, stream=None):
+        _check(self._lib.alea_grid_batch_build(self._h, stream))
+
+    def stats(self):
+        s = _GridBatchStats()
+        _check(self._lib.alea_grid_batch_stats_get(self._h, ctypes.byref(s)))
+        d = {f: getattr(s, f) for f, _ in s._fields_}
+        d["tune_ms"] = list(s.tune_ms)
+        return d
+
+    def point_counts(self, i):
+        out = np.zeros(3, np.int32)
+        _check(self._lib.alea_grid_batch_point_counts(self._h, i, out.ctypes.data_as(_I32)))
+        return tuple(int(v) for v in out)
+
+    def table(self, i, species):
+        nx, ny, nz = self.point_counts(i)
+        out = np.zeros(nx * ny * nz)
+        _check(self._lib.alea_grid_batch_download(self._h, i, species, _dp(out), out.size))
+        return out
 
 
 class Proposal:

@@ -26,6 +26,9 @@ struct alea_gcmc {
 struct alea_proposal {
     alea::ProposalImpl* impl;
 };
+struct alea_grid_batch {
+    alea::GridBatchImpl* impl;
+};
 
 namespace {
 
@@ -603,6 +606,61 @@ alea_status alea_widom_run_biased(alea_widom* w, const alea_proposal* p, uint64_
         const alea::ProposalTable t = alea::proposal_table(p->impl);
         alea::widom_run(w->impl, seed, stream, first_trial, n_trials, ALEA_DRAWS_RIGHT_TO_LEFT, out,
                         per_trial_du, &t, per_trial_frac);
+    });
+}
+
+alea_status alea_grid_batch_create(uint32_t n, const alea_lennard_jones* lj,
+                                   const alea_particles* frameworks, const alea_lattice* lattices,
+                                   const uint32_t* guest_species, uint32_t n_guest, double spacing,
+                                   alea_grid_batch** out) {
+    return guarded([&] {
+        need(out, "out");
+        *out = nullptr;
+        alea::require(lj && frameworks && lattices && guest_species, ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_grid_batch_create: lj, frameworks, lattices and guest_species are required");
+        auto* impl = alea::grid_batch_create(n, lj, frameworks, lattices, guest_species, n_guest,
+                                             spacing);
+        *out = new alea_grid_batch{impl};
+    });
+}
+
+alea_status alea_grid_batch_build(alea_grid_batch* b, void* cuda_stream) {
+    return guarded([&] {
+        need(b, "grid batch");
+        alea::grid_batch_build(b->impl, (cudaStream_t)cuda_stream);
+    });
+}
+
+alea_status alea_grid_batch_stats_get(const alea_grid_batch* b, alea_grid_batch_stats* out) {
+    return guarded([&] {
+        need(b, "grid batch");
+        need(out, "out");
+        alea::grid_batch_stats(b->impl, out);
+    });
+}
+
+alea_status alea_grid_batch_point_counts(const alea_grid_batch* b, uint32_t grid, int32_t out[3]) {
+    return guarded([&] {
+        need(b, "grid batch");
+        need(out, "out");
+        alea::grid_counts(alea::grid_batch_item(b->impl, grid), out);
+    });
+}
+
+alea_status alea_grid_batch_download(const alea_grid_batch* b, uint32_t grid, uint32_t species,
+                                     double* out, uint64_t n) {
+    return guarded([&] {
+        need(b, "grid batch");
+        need(out, "out");
+        alea::grid_download(alea::grid_batch_item(b->impl, grid), species, out, n);
+    });
+}
+
+alea_status alea_grid_batch_destroy(alea_grid_batch* b) {
+    return guarded([&] {
+        if (!b) return;
+        alea::grid_batch_destroy(b->impl);
+        delete b;
     });
 }
 

@@ -693,19 +693,29 @@ constexpr float CLOSE_FP32_FLOOR = 300.0f;  // K
 // sum is stored and the node flagged for grid_close_fix_kernel.
 // With plain truncation a pair beyond rc gets r^-2 = 0 instead (no shift).
 // Linear force shifting adds -(r - rc) V'(rc) per pair at the clamped r.
+// Pointers of one grid for the FP32 kernels.
+struct F32GridArgs {
+    const ImageRecF* images;
+    const uint32_t* bin_start;
+    const ParamAB* pab;  // [guest of this launch][type]
+    const ParamFF* pff;
+    double* tables;
+    uint8_t* fix;
+};
+
+// One brick of the sweep (the body of the sweep kernels). `tiles` counts the
+// tiles this CTA has staged so far: the two mbarriers alternate by it, so
+// their phases run on across bricks. Returns false when the CTA must stop (a
+// bounded wait ran out; the error flag is raised).
 template <int NG, int TRUNC>
-__global__ void __launch_bounds__(THREADS, 4)
-grid_build_f32_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
-                      const uint32_t* __restrict__ bin_start, const ParamAB* __restrict__ pab_g,
-                      const ParamFF* __restrict__ pff_g, double* __restrict__ tables,
-                      uint8_t* __restrict__ fix, unsigned long long* __restrict__ executed,
-                      unsigned* flags) {
-    extern __shared__ __align__(128) unsigned char smem[];
+__device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridArgs& A, int brick,
+                                            unsigned char* smem, uint64_t* bars, uint32_t& tiles,
+                                            unsigned long long* __restrict__ executed,
+                                            unsigned* flags) {
     SmemCarve sc{smem};
     ImageRecF* raw = sc.take<ImageRecF>(2 * TILE);
     ulonglong2* cxy = sc.take<ulonglong2>(TILE);   // {x, x}, {y, y}
     ulonglong2* czt = sc.take<ulonglong2>(TILE);   // {z, z}, {type, 0}
-    uint64_t* bars = sc.take<uint64_t>(2);
     uint32_t* row_begin = sc.take<uint32_t>(MAX_ROWS);
     uint32_t* row_off = sc.take<uint32_t>(MAX_ROWS + 1);
     uint32_t* warp_tot = sc.take<uint32_t>(THREADS / 32);
@@ -713,10 +723,13 @@ grid_build_f32_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
     // double-float sweep sums (touched once per tile): hi at [(g NPT + k) 2 + 0]
     // x THREADS + tid, lo at [... + 1]
     float* accs = sc.take<float>(2 * NG * NPT * THREADS);
+    const ImageRecF* __restrict__ images = A.images;
+    const uint32_t* __restrict__ bin_start = A.bin_start;
+    double* __restrict__ tables = A.tables;
+    uint8_t* __restrict__ fix = A.fix;
 
     const int tid = threadIdx.x;
     const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
-    const int brick = blockIdx.x;
     const int bxn = geo.bricks[0], byn = geo.bricks[1];
     const int bx = brick % bxn, by = (brick / bxn) % byn, bz = brick / (bxn * byn);
     const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
@@ -724,15 +737,10 @@ grid_build_f32_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
     auto acc_hi = [&](int g, int k) -> float& { return accs[((g * NPT + k) * 2) * THREADS + tid]; };
     auto acc_lo = [&](int g, int k) -> float& { return accs[((g * NPT + k) * 2 + 1) * THREADS + tid]; };
 
-    if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_barrier_init();
-    }
-    load_f32_params(P, pab_g, pff_g, geo.n_types, rcf);
+    load_f32_params(P, A.pab, A.pff, geo.n_types, rcf);
     const int nr = plan_rows(geo, geo.hf, geo.keep2f, bin_start, x0, y0, z0, row_begin, row_off,
                              warp_tot, flags);
-    if (nr < 0) return;
+    if (nr < 0) return true;  // capacity flag raised; the other bricks go on
     const uint32_t n_cand = row_off[nr];
 
     int tx, ty, tz0;
@@ -798,19 +806,22 @@ grid_build_f32_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
     const unsigned char* img = reinterpret_cast<const unsigned char*>(images);
     unsigned char* rawb = reinterpret_cast<unsigned char*>(raw);
     const uint32_t n_tiles = (n_cand + TILE - 1) / TILE;
+    const uint32_t T0 = tiles;  // tile t of this brick is the CTA's tile T0 + t
     if (tid == 0) {
-        if (n_tiles > 0) issue_tile(0, n_cand, nr, row_begin, row_off, img, rawb, &bars[0]);
-        if (n_tiles > 1)
-            issue_tile(1, n_cand, nr, row_begin, row_off, img, rawb + TILE * sizeof(ImageRecF), &bars[1]);
+        for (uint32_t t = 0; t < 2 && t < n_tiles; ++t) {
+            const int b = (T0 + t) & 1;
+            issue_tile(t, n_cand, nr, row_begin, row_off, img, rawb + b * TILE * sizeof(ImageRecF),
+                       &bars[b]);
+        }
     }
     for (uint32_t t = 0; t < n_tiles; ++t) {
-        const int buf = t & 1;
+        const int buf = (T0 + t) & 1;
         const uint32_t cnt = min((uint32_t)TILE, n_cand - t * TILE);
         // block-wide vote so that every thread takes the same path on a timeout
-        const bool got = mbar_wait_bounded(&bars[buf], (t >> 1) & 1, flags);
+        const bool got = mbar_wait_bounded(&bars[buf], ((T0 + t) >> 1) & 1, flags);
         if (!__syncthreads_and(got)) {
-            drain_tiles(t, n_tiles, bars);
-            return;
+            drain_tiles(T0 + t, T0 + n_tiles, bars);
+            return false;
         }
         static_assert(TILE == THREADS, "one record per thread in the conversion pass");
         if ((uint32_t)tid < cnt) {
@@ -930,6 +941,7 @@ grid_build_f32_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
             }
         __syncthreads();  // the staged tile is rewritten by the next one
     }
+    tiles = T0 + n_tiles;
 
     // per node and guest: sweep sum, cap, sweep sum + FP32 estimate, or the
     // sweep sum flagged for the double-float correction
@@ -972,15 +984,32 @@ grid_build_f32_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
         for (int w = 0; w < THREADS / 32; ++w) sum += warp_tot[w];
         atomicAdd(executed, sum);
     }
+    __syncthreads();  // shared memory is reused by the next brick
+    return true;
+}
+
+template <int NG, int TRUNC>
+__global__ void __launch_bounds__(THREADS, 4)
+grid_build_f32_kernel(GridGeom geo, F32GridArgs args, unsigned long long* __restrict__ executed,
+                      unsigned* flags) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    uint32_t tiles = 0;
+    sweep_brick<NG, TRUNC>(geo, args, (int)blockIdx.x, smem, bars, tiles, executed, flags);
 }
 
 template <int NG, int TRUNC>
 constexpr size_t f32_smem_bytes() {
     return carve(2 * TILE * sizeof(ImageRecF)) + carve(TILE * sizeof(ulonglong2)) +
-           carve(TILE * sizeof(ulonglong2)) + carve(2 * sizeof(uint64_t)) +
-           carve(MAX_ROWS * sizeof(uint32_t)) + carve((MAX_ROWS + 1) * sizeof(uint32_t)) +
-           carve((THREADS / 32) * sizeof(uint32_t)) + carve(sizeof(F32Params<NG, TRUNC>)) +
-           carve(2 * NG * NPT * THREADS * sizeof(float));
+           carve(TILE * sizeof(ulonglong2)) + carve(MAX_ROWS * sizeof(uint32_t)) +
+           carve((MAX_ROWS + 1) * sizeof(uint32_t)) + carve((THREADS / 32) * sizeof(uint32_t)) +
+           carve(sizeof(F32Params<NG, TRUNC>)) + carve(2 * NG * NPT * THREADS * sizeof(float));
 }
 
 // ---------------------------------------------------------------- FP32 close-pair correction
@@ -996,13 +1025,14 @@ constexpr size_t f32_smem_bytes() {
 constexpr int NEAR_CHUNK = 512;
 constexpr int MAX_CLOSE = 16;  // listed close images per node and chunk
 
+// One brick of the close-pair correction (the body of the correction kernels).
 template <int NG, int TRUNC>
-__global__ void __launch_bounds__(THREADS)
-grid_close_fix_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
-                      const uint32_t* __restrict__ bin_start, const ParamAB* __restrict__ pab_g,
-                      const ParamFF* __restrict__ pff_g, const uint8_t* __restrict__ fix,
-                      double* __restrict__ tables, unsigned* flags) {
-    extern __shared__ __align__(128) unsigned char smem[];
+__device__ __forceinline__ void fix_brick(const GridGeom& geo, const F32GridArgs& A, int brick,
+                                          unsigned char* smem, unsigned* flags) {
+    const ImageRecF* __restrict__ images = A.images;
+    const uint32_t* __restrict__ bin_start = A.bin_start;
+    const uint8_t* __restrict__ fix = A.fix;
+    double* __restrict__ tables = A.tables;
     SmemCarve sc{smem};
     float4* ahi = sc.take<float4>(NEAR_CHUNK);  // x, y, z hi, type
     float4* alo = sc.take<float4>(NEAR_CHUNK);  // x, y, z lo
@@ -1019,7 +1049,6 @@ grid_close_fix_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
 
     const int tid = threadIdx.x;
     const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
-    const int brick = blockIdx.x;
     const int bxn = geo.bricks[0], byn = geo.bricks[1];
     const int bx = brick % bxn, by = (brick / bxn) % byn, bz = brick / (bxn * byn);
     const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
@@ -1042,7 +1071,7 @@ grid_close_fix_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
         }
         cnt_nodes += gm[k] != 0;
     }
-    if (!__syncthreads_or(cnt_nodes != 0)) return;
+    if (!__syncthreads_or(cnt_nodes != 0)) return;  // (every thread: a uniform vote)
 
     // compact the flagged nodes: exclusive scan of the per-thread counts
     uint32_t n_fn;
@@ -1074,7 +1103,7 @@ grid_close_fix_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
                 ++off;
             }
     }
-    load_f32_params(P, pab_g, pff_g, geo.n_types, geo.rcf);  // synchronises
+    load_f32_params(P, A.pab, A.pff, geo.n_types, geo.rcf);  // synchronises
     const int nr = plan_rows(geo, geo.hf_near, geo.keep2_near, bin_start, x0, y0, z0, row_begin,
                              row_off, warp_tot, flags);
     if (nr < 0) return;
@@ -1154,6 +1183,14 @@ grid_close_fix_kernel(GridGeom geo, const ImageRecF* __restrict__ images,
         double& e = tables[(size_t)g * per_table + idx];
         if (kEnergyCap < e) e = kEnergyCap;
     }
+    __syncthreads();  // shared memory is reused by the next brick
+}
+
+template <int NG, int TRUNC>
+__global__ void __launch_bounds__(THREADS)
+grid_close_fix_kernel(GridGeom geo, F32GridArgs args, unsigned* flags) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    fix_brick<NG, TRUNC>(geo, args, (int)blockIdx.x, smem, flags);
 }
 
 template <int NG, int TRUNC>
@@ -1164,6 +1201,134 @@ constexpr size_t fix_smem_bytes() {
            carve(2 * THREADS * NPT * sizeof(float4)) +
            carve(THREADS * NPT * MAX_CLOSE * sizeof(uint16_t)) +
            carve(THREADS * NPT * sizeof(uint16_t)) + carve(sizeof(F32Params<NG, TRUNC>));
+}
+
+// ---------------------------------------------------------------- batched FP32 build
+// Many independent grids (uneven frameworks: their own cells, atoms, force
+// fields and node counts) in one persistent launch per kernel: every CTA takes
+// (grid, brick) work items from a global counter (dynamic, so uneven grids
+// balance) and runs the same per-brick code as the single-grid kernels, with
+// the item's geometry copied into shared memory. The results are those of
+// building each grid alone, bit for bit: every brick is computed the same way
+// whichever CTA takes it.
+struct BatchItem {
+    GridGeom geo;
+    F32GridArgs args;
+    uint64_t brick0;  // first work item of this grid
+};
+
+__device__ __forceinline__ bool next_item(const BatchItem* __restrict__ items, int n_items,
+                                          uint64_t total, unsigned long long* next,
+                                          unsigned long long& work, int& item, GridGeom& geo) {
+    if (threadIdx.x == 0) {
+        work = atomicAdd(next, 1ull);
+        if (work < total) {
+            int lo = 0, hi = n_items - 1;  // last grid with brick0 <= work
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) / 2;
+                if (items[mid].brick0 <= work) lo = mid; else hi = mid - 1;
+            }
+            item = lo;
+        }
+    }
+    __syncthreads();
+    if (work >= total) return false;
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&items[item].geo);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&geo);
+    for (int i = threadIdx.x; i < (int)(sizeof(GridGeom) / 4); i += THREADS) dst[i] = src[i];
+    __syncthreads();
+    return true;
+}
+
+template <int NG, int TRUNC, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
+grid_build_f32_batch_kernel(const BatchItem* __restrict__ items, int n_items, uint64_t total,
+                            unsigned long long* next, unsigned long long* __restrict__ executed,
+                            unsigned* flags) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ unsigned long long work;
+    __shared__ int item;
+    GridGeom& geo = *reinterpret_cast<GridGeom*>(smem);
+    unsigned char* body = smem + carve(sizeof(GridGeom));
+    static_assert(sizeof(GridGeom) % 4 == 0, "geometry copied as words");
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    uint32_t tiles = 0;
+    while (next_item(items, n_items, total, next, work, item, geo)) {
+        const BatchItem& it = items[item];
+        if (!sweep_brick<NG, TRUNC>(geo, it.args, (int)(work - it.brick0), body, bars, tiles,
+                                    executed, flags))
+            return;
+        __syncthreads();  // work, item and geo are rewritten next
+    }
+}
+
+template <int NG, int TRUNC>
+__global__ void __launch_bounds__(THREADS)
+grid_close_fix_batch_kernel(const BatchItem* __restrict__ items, int n_items, uint64_t total,
+                            unsigned long long* next, unsigned* flags) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ unsigned long long work;
+    __shared__ int item;
+    GridGeom& geo = *reinterpret_cast<GridGeom*>(smem);
+    unsigned char* body = smem + carve(sizeof(GridGeom));
+    while (next_item(items, n_items, total, next, work, item, geo)) {
+        const BatchItem& it = items[item];
+        fix_brick<NG, TRUNC>(geo, it.args, (int)(work - it.brick0), body, flags);
+        __syncthreads();
+    }
+}
+
+// The batched launch shapes the autotuner chooses between.
+constexpr int BATCH_VARIANTS = 2;  // 0: 3 sweep blocks per SM, 1: 4
+
+template <int NG, int TRUNC>
+void batch_launch_t(int variant, int sms, cudaStream_t s, const BatchItem* items, int n_items,
+                    uint64_t total, unsigned long long* counters, unsigned long long* executed,
+                    unsigned* flags) {
+    const size_t sb = carve(sizeof(GridGeom)) + f32_smem_bytes<NG, TRUNC>();
+    const size_t fb = carve(sizeof(GridGeom)) + fix_smem_bytes<NG, TRUNC>();
+    auto sweep = variant == 0 ? grid_build_f32_batch_kernel<NG, TRUNC, 3>
+                              : grid_build_f32_batch_kernel<NG, TRUNC, 4>;
+    ALEA_CUDA(cudaFuncSetAttribute(sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+    ALEA_CUDA(cudaFuncSetAttribute(grid_close_fix_batch_kernel<NG, TRUNC>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb));
+    int per_sm = 1, fix_per_sm = 1;
+    ALEA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep, THREADS, sb));
+    ALEA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &fix_per_sm, grid_close_fix_batch_kernel<NG, TRUNC>, THREADS, fb));
+    const unsigned gs = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(total, (uint64_t)sms * std::max(per_sm, 1)));
+    const unsigned gf = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(total, (uint64_t)sms * std::max(fix_per_sm, 1)));
+    ALEA_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), s));
+    sweep<<<gs, THREADS, sb, s>>>(items, n_items, total, counters, executed, flags);
+    ALEA_CUDA(cudaGetLastError());
+    grid_close_fix_batch_kernel<NG, TRUNC><<<gf, THREADS, fb, s>>>(items, n_items, total,
+                                                                     counters + 1, flags);
+    ALEA_CUDA(cudaGetLastError());
+}
+
+void batch_launch(int ng, int trunc, int variant, int sms, cudaStream_t s, const BatchItem* items,
+                  int n_items, uint64_t total, unsigned long long* counters,
+                  unsigned long long* executed, unsigned* flags) {
+#define ALEA_BATCH_T(NGV)                                                                          \
+    if (trunc == ALEA_TRUNCATED)                                                                   \
+        batch_launch_t<NGV, ALEA_TRUNCATED>(variant, sms, s, items, n_items, total, counters, executed, flags); \
+    else if (trunc == ALEA_SHIFTED)                                                                \
+        batch_launch_t<NGV, ALEA_SHIFTED>(variant, sms, s, items, n_items, total, counters, executed, flags);   \
+    else                                                                                           \
+        batch_launch_t<NGV, ALEA_LINEAR_FORCE_SHIFTED>(variant, sms, s, items, n_items, total, counters, executed, flags);
+    switch (ng) {
+        case 1: ALEA_BATCH_T(1) break;
+        case 2: ALEA_BATCH_T(2) break;
+        case 3: ALEA_BATCH_T(3) break;
+        default: ALEA_BATCH_T(4) break;
+    }
+#undef ALEA_BATCH_T
 }
 
 // ---------------------------------------------------------------- interpolation
@@ -1230,14 +1395,14 @@ void launch_one(bool f32, int phase, dim3 grid, cudaStream_t s, const GridGeom& 
         // opt in to more than 48 KB of dynamic shared memory (per device, cheap)
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f32_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-        grid_build_f32_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(
-            geo, a.images_f, a.bins, a.pab, a.pff, a.tables, a.fix, a.executed, a.flags);
+        const F32GridArgs fa{a.images_f, a.bins, a.pab, a.pff, a.tables, a.fix};
+        grid_build_f32_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(geo, fa, a.executed, a.flags);
     } else if (f32) {
         constexpr size_t fbytes = fix_smem_bytes<NG, TRUNC>();
         ALEA_CUDA(cudaFuncSetAttribute(grid_close_fix_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fbytes));
-        grid_close_fix_kernel<NG, TRUNC><<<grid, THREADS, fbytes, s>>>(
-            geo, a.images_f, a.bins, a.pab, a.pff, a.fix, a.tables, a.flags);
+        const F32GridArgs fa{a.images_f, a.bins, a.pab, a.pff, a.tables, a.fix};
+        grid_close_fix_kernel<NG, TRUNC><<<grid, THREADS, fbytes, s>>>(geo, fa, a.flags);
     } else if (phase == 0) {
         constexpr size_t bytes = f64_smem_bytes<NG>();
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f64_kernel<NG, TRUNC>,
@@ -1626,6 +1791,147 @@ void grid_stats(const GridImpl* g, alea_grid_stats* out) {
     out->last_fix_ms = g->last_fix_ms;
     out->launches = (uint32_t)g->launches;
 }
+
+// ---------------------------------------------------------------- batch of grids
+struct GridBatchImpl {
+    std::vector<GridImpl*> grids;
+    int ng = 0, truncation = ALEA_SHIFTED;
+    uint64_t total = 0;
+    DevBuf<BatchItem> items;
+    DevBuf<unsigned long long> counters, executed;
+    DevBuf<unsigned> flags;
+    cudaStream_t own = nullptr;  // capture stream (graphs cannot be captured on stream 0)
+    int sms = 0;
+    int variant = -1;            // chosen by the autotuner on the first build
+    float tune_ms[BATCH_VARIANTS] = {};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint32_t graph_launches = 0;
+    float last_ms = 0.f;
+    uint64_t executed_pairs = 0;
+    ~GridBatchImpl() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (own) cudaStreamDestroy(own);
+        for (auto* g : grids) delete g;
+    }
+};
+
+GridBatchImpl* grid_batch_create(uint32_t n, const alea_lennard_jones* lj, const alea_particles* fw,
+                                 const alea_lattice* lat, const uint32_t* guests, uint32_t n_guest,
+                                 double spacing) {
+    require(n >= 1, ALEA_ERR_INVALID_ARGUMENT, "alea_grid_batch_create: at least one grid");
+    require(n_guest >= 1 && n_guest <= (uint32_t)MAX_NG, ALEA_ERR_INVALID_ARGUMENT,
+            "alea_grid_batch_create: 1..4 guest species per grid");
+    auto* b = new GridBatchImpl();
+    try {
+        std::vector<BatchItem> items(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            auto* g = new GridImpl();
+            b->grids.push_back(g);
+            build_plan(*g, lj[i], fw[i], lat[i], guests + (size_t)i * n_guest, n_guest, spacing,
+                       ALEA_FP32, 2.0);
+            if (i == 0) {
+                b->ng = (int)g->species.size();
+                b->truncation = g->truncation;
+            }
+            require((int)g->species.size() == b->ng && g->truncation == b->truncation,
+                    ALEA_ERR_INVALID_ARGUMENT,
+                    "alea_grid_batch_create: every grid needs the same number of distinct guests "
+                    "and the same truncation");
+            const uint64_t nodes = (uint64_t)g->geo.n[0] * g->geo.n[1] * g->geo.n[2];
+            (void)nodes;
+            items[i].geo = g->geo;
+            items[i].args = F32GridArgs{g->images_f.p, g->bin_start.p, g->pab.p, g->pff.p,
+                                        g->tables.p, g->fix.p};
+            items[i].brick0 = b->total;
+            b->total += (uint64_t)g->geo.bricks[0] * g->geo.bricks[1] * g->geo.bricks[2];
+        }
+        b->items.alloc(n);
+        b->items.upload(items.data(), n);
+        b->counters.alloc(2);
+        b->executed.alloc(1);
+        b->flags.alloc(1);
+        ALEA_CUDA(cudaMemset(b->flags.p, 0, sizeof(unsigned)));
+        ALEA_CUDA(cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking));
+        int dev = 0;
+        ALEA_CUDA(cudaGetDevice(&dev));
+        ALEA_CUDA(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev));
+        ALEA_CUDA(cudaDeviceSynchronize());
+    } catch (...) {
+        delete b;
+        throw;
+    }
+    return b;
+}
+
+static void batch_sequence(GridBatchImpl* b, int variant, cudaStream_t s) {
+    ALEA_CUDA(cudaMemsetAsync(b->executed.p, 0, sizeof(unsigned long long), s));
+    batch_launch(b->ng, b->truncation, variant, b->sms, s, b->items.p, (int)b->grids.size(), b->total,
+                 b->counters.p, b->executed.p, b->flags.p);
+}
+
+// One build of every grid. The first call times each launch variant on the
+// whole batch (the autotuner; every variant writes the same tables), keeps the
+// fastest and captures its launch sequence into a CUDA graph; every call then
+// replays the graph on the caller's stream.
+void grid_batch_build(GridBatchImpl* b, cudaStream_t s) {
+    cudaStream_t run = s ? s : b->own;
+    cudaEvent_t e0, e1;
+    ALEA_CUDA(cudaEventCreate(&e0));
+    ALEA_CUDA(cudaEventCreate(&e1));
+    if (b->variant < 0) {
+        for (int v = 0; v < BATCH_VARIANTS; ++v) {
+            ALEA_CUDA(cudaEventRecord(e0, run));
+            batch_sequence(b, v, run);
+            ALEA_CUDA(cudaEventRecord(e1, run));
+            ALEA_CUDA(cudaEventSynchronize(e1));
+            ALEA_CUDA(cudaEventElapsedTime(&b->tune_ms[v], e0, e1));
+            check_device_flags(b->flags.p, run, "batched grid build");
+        }
+        b->variant = (int)(std::min_element(b->tune_ms, b->tune_ms + BATCH_VARIANTS) - b->tune_ms);
+        ALEA_CUDA(cudaStreamBeginCapture(b->own, cudaStreamCaptureModeThreadLocal));
+        batch_sequence(b, b->variant, b->own);
+        ALEA_CUDA(cudaStreamEndCapture(b->own, &b->graph));
+        ALEA_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    }
+    ALEA_CUDA(cudaEventRecord(e0, run));
+    ALEA_CUDA(cudaGraphLaunch(b->exec, run));
+    ALEA_CUDA(cudaEventRecord(e1, run));
+    ALEA_CUDA(cudaEventSynchronize(e1));
+    ALEA_CUDA(cudaEventElapsedTime(&b->last_ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ++b->graph_launches;
+    unsigned long long ex = 0;
+    ALEA_CUDA(cudaMemcpy(&ex, b->executed.p, sizeof(ex), cudaMemcpyDeviceToHost));
+    b->executed_pairs = ex;
+    check_device_flags(b->flags.p, run, "batched grid build");
+}
+
+void grid_batch_stats(const GridBatchImpl* b, alea_grid_batch_stats* out) {
+    out->grids = (uint32_t)b->grids.size();
+    out->nodes = 0;
+    out->algorithmic_pairs = 0;
+    for (const auto* g : b->grids) {
+        const uint64_t nodes = (uint64_t)g->geo.n[0] * g->geo.n[1] * g->geo.n[2];
+        out->nodes += nodes;
+        out->algorithmic_pairs += nodes * g->n_atoms * (uint64_t)g->species.size();
+    }
+    out->executed_pairs = b->executed_pairs * (uint64_t)b->ng;
+    out->bricks = b->total;
+    out->last_ms = b->last_ms;
+    out->variant = b->variant;
+    for (int v = 0; v < BATCH_VARIANTS && v < 2; ++v) out->tune_ms[v] = b->tune_ms[v];
+    out->graph_launches = b->graph_launches;
+}
+
+const GridImpl* grid_batch_item(const GridBatchImpl* b, uint32_t i) {
+    require(i < b->grids.size(), ALEA_ERR_OUT_OF_RANGE, "grid batch: grid index");
+    return b->grids[i];
+}
+
+void grid_batch_destroy(GridBatchImpl* b) { delete b; }
 
 GridImpl* grid_from_tables(const alea_lattice& lat, double spacing, const int32_t counts[3],
                            const std::vector<uint32_t>& species,

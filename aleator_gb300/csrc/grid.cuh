@@ -27,6 +27,15 @@ double grid_spacing(const GridImpl* g);
 const std::vector<uint32_t>& grid_species(const GridImpl* g);
 void grid_stats(const GridImpl* g, alea_grid_stats* out);
 
+struct GridBatchImpl;
+GridBatchImpl* grid_batch_create(uint32_t n, const alea_lennard_jones* lj, const alea_particles* fw,
+                                 const alea_lattice* lat, const uint32_t* guests, uint32_t n_guest,
+                                 double spacing);
+void grid_batch_build(GridBatchImpl* b, cudaStream_t s);
+void grid_batch_stats(const GridBatchImpl* b, alea_grid_batch_stats* out);
+const GridImpl* grid_batch_item(const GridBatchImpl* b, uint32_t i);
+void grid_batch_destroy(GridBatchImpl* b);
+
 // grid_cache.cpp: the reference's on-disk cache format (version 1).
 void grid_cache_write(const char* path, const alea_lennard_jones& lj, const alea_particles& fw,
                       const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,

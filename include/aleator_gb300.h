@@ -194,6 +194,40 @@ alea_status alea_grid_load_cache(const char* cache_dir, const alea_lennard_jones
                                  alea_grid** out);
 alea_status alea_grid_destroy(alea_grid* g);
 
+/* ------------------------------------------------------------------ batch of energy grids */
+/* No counterpart in the reference (one FrameworkEnergyGrid per framework,
+ * framework_energy_grid.cc:193-249). n independent frameworks, each with its
+ * own force field, atoms and cell (so their node counts differ), built in the
+ * FP32 form in one persistent launch per kernel: CTAs take (grid, brick) work
+ * items from a global counter. The first build times the launch variants on
+ * the batch (the autotuner) and captures the chosen launch sequence into a
+ * CUDA graph; every build replays it. Each grid equals a single
+ * alea_grid_build of that framework (FP32), bit for bit. guest_species holds
+ * n x n_guest ids; every grid must have the same number of distinct guests
+ * (1..4) and the same truncation. */
+typedef struct alea_grid_batch alea_grid_batch;
+alea_status alea_grid_batch_create(uint32_t n, const alea_lennard_jones* lj,
+                                   const alea_particles* frameworks, const alea_lattice* lattices,
+                                   const uint32_t* guest_species, uint32_t n_guest, double spacing,
+                                   alea_grid_batch** out);
+alea_status alea_grid_batch_build(alea_grid_batch* b, void* cuda_stream);
+typedef struct {
+    uint32_t grids;
+    uint64_t nodes;             /* over all grids */
+    uint64_t algorithmic_pairs; /* sum of nodes x atoms x guests */
+    uint64_t executed_pairs;    /* node-image pairs evaluated (all guests) */
+    uint64_t bricks;            /* work items */
+    float last_ms;              /* the last build (one graph launch), CUDA events */
+    int32_t variant;            /* launch variant the autotuner chose (-1 before the first build) */
+    float tune_ms[2];           /* the autotuner's timings of each variant */
+    uint32_t graph_launches;
+} alea_grid_batch_stats;
+alea_status alea_grid_batch_stats_get(const alea_grid_batch* b, alea_grid_batch_stats* out);
+alea_status alea_grid_batch_point_counts(const alea_grid_batch* b, uint32_t grid, int32_t out[3]);
+alea_status alea_grid_batch_download(const alea_grid_batch* b, uint32_t grid, uint32_t species,
+                                     double* out, uint64_t n);
+alea_status alea_grid_batch_destroy(alea_grid_batch* b);
+
 /* ------------------------------------------------------------------ Lennard-Jones */
 /* LennardJones::computeParticleEnergy(index, particles, lattice, excluded)
  * (lennard_jones.cc:158-182) for n_query indices at once. */
