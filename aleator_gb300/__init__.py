@@ -28,6 +28,7 @@ from ._lib import (  # noqa: F401
     ParticleData,
     Proposal,
     Widom,
+    WidomBatch,
     device_info,
     ewald_energy_breakdown,
     ewald_real_space_particle_energy,

@@ -217,6 +217,14 @@ _SIGNATURES = {
     "alea_grid_batch_download": (ctypes.c_int32, [_VP, ctypes.c_uint32, ctypes.c_uint32, _D,
                                                   ctypes.c_uint64]),
     "alea_grid_batch_destroy": (ctypes.c_int32, [_VP]),
+    "alea_widom_batch_create": (ctypes.c_int32, [ctypes.c_uint32, ctypes.POINTER(_LJ),
+                                                 ctypes.POINTER(_Ewald), ctypes.POINTER(_Particles),
+                                                 ctypes.POINTER(_Lattice), ctypes.POINTER(_Species),
+                                                 ctypes.c_double, ctypes.c_int32,
+                                                 ctypes.POINTER(_VP)]),
+    "alea_widom_batch_run": (ctypes.c_int32, [_VP, _U64, _U64, ctypes.c_uint64, ctypes.c_uint64,
+                                              ctypes.c_int32, ctypes.POINTER(_WidomResult), _VP]),
+    "alea_widom_batch_destroy": (ctypes.c_int32, [_VP]),
     "alea_insertion_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                                ctypes.c_double, ctypes.c_double]),
     "alea_deletion_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
@@ -770,6 +778,47 @@ class GridBatch:
         out = np.zeros(nx * ny * nz)
         _check(self._lib.alea_grid_batch_download(self._h, i, species, _dp(out), out.size))
         return out
+
+
+class WidomBatch:
+    """Widom contexts for many frameworks run together (one persistent launch
+    behind a captured CUDA graph); result i equals Widom.run on framework i."""
+
+    def __init__(self, force_fields, frameworks, lattices, guests, temperature, ewalds=None,
+                 precision=FP64):
+        self._lib = library()
+        self._h = _VP()
+        n = len(frameworks)
+        self.n = n
+        gd = [{k: (_f64(g[k]) if k != "lj_species" else np.ascontiguousarray(g[k], dtype=np.uint32))
+               for k in ("x", "y", "z", "lj_species", "charge")} for g in guests]
+        sps = (_Species * n)(*[_Species(len(g["x"]), _dp(g["x"]), _dp(g["y"]), _dp(g["z"]),
+                                        _u32p(g["lj_species"]), _dp(g["charge"])) for g in gd])
+        ljs = (_LJ * n)(*[ff.c() for ff in force_fields])
+        ps = (_Particles * n)(*[p.c() for p in frameworks])
+        lats = (_Lattice * n)(*[_lattice(m) for m in lattices])
+        ews = (_Ewald * n)(*[e.c() for e in ewalds]) if ewalds else None
+        self._keep = (list(force_fields), list(frameworks), gd, sps, ljs, ps, lats, ews)
+        _check(self._lib.alea_widom_batch_create(n, ljs, ews, ps, lats, sps, float(temperature),
+                                                 int(precision), ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                self._lib.alea_widom_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def run(self, seeds, streams, n_trials, first_trial=0, draw_order=ALEA_DRAWS_RIGHT_TO_LEFT,
+            stream=None):
+        sd = np.ascontiguousarray(seeds, dtype=np.uint64)
+        st = np.ascontiguousarray(streams, dtype=np.uint64)
+        res = (_WidomResult * self.n)()
+        _check(self._lib.alea_widom_batch_run(self._h, _u64p(sd), _u64p(st), first_trial, n_trials,
+                                              draw_order, res, stream))
+        return [{f: getattr(r, f) for f, _ in r._fields_} for r in res]
 
 
 class Proposal:

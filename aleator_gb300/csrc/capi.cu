@@ -29,6 +29,9 @@ struct alea_proposal {
 struct alea_grid_batch {
     alea::GridBatchImpl* impl;
 };
+struct alea_widom_batch {
+    alea::WidomBatchImpl* impl;
+};
 
 namespace {
 
@@ -653,6 +656,41 @@ alea_status alea_grid_batch_download(const alea_grid_batch* b, uint32_t grid, ui
         need(b, "grid batch");
         need(out, "out");
         alea::grid_download(alea::grid_batch_item(b->impl, grid), species, out, n);
+    });
+}
+
+alea_status alea_widom_batch_create(uint32_t n, const alea_lennard_jones* lj, const alea_ewald* ewald,
+                                    const alea_particles* frameworks, const alea_lattice* lattices,
+                                    const alea_molecule_species* guests, double temperature,
+                                    int32_t precision, alea_widom_batch** out) {
+    return guarded([&] {
+        need(out, "out");
+        *out = nullptr;
+        alea::require(lj && frameworks && lattices && guests, ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_widom_batch_create: lj, frameworks, lattices and guests are required");
+        auto* impl = alea::widom_batch_create(n, lj, ewald, frameworks, lattices, guests, temperature,
+                                              precision);
+        *out = new alea_widom_batch{impl};
+    });
+}
+
+alea_status alea_widom_batch_run(alea_widom_batch* b, const uint64_t* seeds, const uint64_t* streams,
+                                 uint64_t first_trial, uint64_t n_trials, int32_t draw_order,
+                                 alea_widom_result* out, void* cuda_stream) {
+    return guarded([&] {
+        need(b, "widom batch");
+        alea::require(seeds && streams && out, ALEA_ERR_INVALID_ARGUMENT,
+                      "alea_widom_batch_run: seeds, streams and out are required");
+        alea::widom_batch_run(b->impl, seeds, streams, first_trial, n_trials, draw_order, out,
+                              (cudaStream_t)cuda_stream);
+    });
+}
+
+alea_status alea_widom_batch_destroy(alea_widom_batch* b) {
+    return guarded([&] {
+        if (!b) return;
+        alea::widom_batch_destroy(b->impl);
+        delete b;
     });
 }
 

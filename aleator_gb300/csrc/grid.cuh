@@ -136,6 +136,15 @@ void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uin
 void widom_samples(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
                    int draw_order, float* samples_dev, const ProposalTable* proposal);
 void widom_destroy(WidomImpl* w);
+struct WidomBatchImpl;
+WidomBatchImpl* widom_batch_create(uint32_t n, const alea_lennard_jones* lj, const alea_ewald* ew,
+                                   const alea_particles* fw, const alea_lattice* lat,
+                                   const alea_molecule_species* guest, double temperature,
+                                   int precision);
+void widom_batch_run(WidomBatchImpl* b, const uint64_t* seeds, const uint64_t* streams,
+                     uint64_t first, uint64_t n, int draw_order, alea_widom_result* out,
+                     cudaStream_t s);
+void widom_batch_destroy(WidomBatchImpl* b);
 
 // gcmc.cu
 struct GcmcImpl;

@@ -68,15 +68,33 @@ __device__ __forceinline__ void cross_rn(const double* a, const double* b, doubl
     o[2] = sub_rn(mul_rn(a[0], b[1]), mul_rn(a[1], b[0]));
 }
 
+// Device data of one Widom context.
+struct WidomPtrs {
+    const double4* atoms;
+    const uint32_t* types;
+    const PairParams* table;
+    const KRow* rows;
+    const double* w;
+    const double* sre;
+    const double* sim;
+};
+
+// One block of WT trials: trials first + block WT + threadIdx.x; writes the
+// block's (max, s1, s2) to partial[3 block ..].
 template <typename Real>
-__global__ void __launch_bounds__(WT)
-widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
-             const uint32_t* __restrict__ types, const PairParams* __restrict__ table,
-             const KRow* __restrict__ rows, const double* __restrict__ w,
-             const double* __restrict__ sre, const double* __restrict__ sim, uint64_t seed,
-             uint64_t stream, uint64_t first, uint64_t n, int draw_order,
-             double* __restrict__ per_trial, double* __restrict__ partial, const ProposalTable tab,
-             double* __restrict__ frac_out, float* __restrict__ samples_out) {
+__device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtrs& D, uint64_t block,
+                                            uint64_t seed, uint64_t stream, uint64_t first,
+                                            uint64_t n, int draw_order, double* __restrict__ per_trial,
+                                            double* __restrict__ partial, const ProposalTable& tab,
+                                            double* __restrict__ frac_out,
+                                            float* __restrict__ samples_out) {
+    const double4* __restrict__ atoms = D.atoms;
+    const uint32_t* __restrict__ types = D.types;
+    const PairParams* __restrict__ table = D.table;
+    const KRow* __restrict__ rows = D.rows;
+    const double* __restrict__ w = D.w;
+    const double* __restrict__ sre = D.sre;
+    const double* __restrict__ sim = D.sim;
     __shared__ double4 tile[ATILE];
     __shared__ uint32_t ttype[ATILE];
     __shared__ PairParams pp[MAXS * MAXT];
@@ -88,7 +106,7 @@ widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
         pp[s * MAXT + t] = table[(size_t)P.site[s].lj * P.n_species + t];
     }
 
-    const uint64_t local = (uint64_t)blockIdx.x * WT + threadIdx.x;
+    const uint64_t local = block * WT + threadIdx.x;
     const bool active = local < n;
     const uint64_t trial = first + local;
     const double* M = P.L.m;
@@ -327,16 +345,19 @@ widom_kernel(const WidomParams P, const double4* __restrict__ atoms,
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        partial[3 * blockIdx.x] = mx;
-        partial[3 * blockIdx.x + 1] = s1;
-        partial[3 * blockIdx.x + 2] = red[0];
+        partial[3 * block] = mx;
+        partial[3 * block + 1] = s1;
+        partial[3 * block + 2] = red[0];
     }
+    __syncthreads();  // shared memory is reused by the next block of trials
 }
 
-// Combines the per-block (max, s1, s2) in block order: out = {max, S1, S2}.
-__global__ void widom_combine_kernel(const double* __restrict__ partial, uint64_t nblocks,
-                                     double* __restrict__ out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+
+// The per-block (max, s1, s2) combined in block order into {max, S1, S2},
+// every operation explicitly rounded so that every kernel calling it gives
+// the same bits.
+__device__ __forceinline__ void combine_partials(const double* __restrict__ partial,
+                                                 uint64_t nblocks, double* __restrict__ out) {
     double mx = -INFINITY;
     for (uint64_t b = 0; b < nblocks; ++b) mx = fmax(mx, partial[3 * b]);
     double s1 = 0.0, s2 = 0.0;
@@ -344,13 +365,67 @@ __global__ void widom_combine_kernel(const double* __restrict__ partial, uint64_
         for (uint64_t b = 0; b < nblocks; ++b) {
             const double m = partial[3 * b];
             if (!(m > -INFINITY)) continue;
-            const double f = exp(m - mx);
-            s1 += partial[3 * b + 1] * f;
-            s2 += partial[3 * b + 2] * (f * f);
+            const double f = exp(__dsub_rn(m, mx));
+            s1 = __dadd_rn(s1, __dmul_rn(partial[3 * b + 1], f));
+            s2 = __dadd_rn(s2, __dmul_rn(partial[3 * b + 2], __dmul_rn(f, f)));
         }
     out[0] = mx;
     out[1] = s1;
     out[2] = s2;
+}
+
+
+// ---- the Widom kernel: one or many contexts in one launch
+// One CTA per work item (context, block of WT trials), found by binary search
+// over the contexts' first items (the hardware schedules the uneven blocks);
+// each CTA copies the context's parameters into shared memory and runs the
+// block. A single context is a batch of one, so a framework's result in a
+// batch is its own alea_widom_run's, bit for bit (the same instructions).
+struct WidomItem {
+    WidomParams P;
+    WidomPtrs D;
+    uint64_t seed, stream, first, n;
+    double* partial;  // 3 per block of this context
+    double* result;   // combined {max, S1, S2}
+    uint64_t block0;  // first work item
+    uint64_t nblocks;
+    // optional per-trial outputs (single contexts) and the learned proposal
+    double* per_trial;
+    double* frac_out;
+    float* samples_out;
+    ProposalTable tab;
+};
+
+template <typename Real>
+__global__ void __launch_bounds__(WT)
+widom_batch_kernel(const WidomItem* __restrict__ items, int n_items, int draw_order) {
+    __shared__ WidomParams Ps;
+    __shared__ int item;
+    static_assert(sizeof(WidomParams) % 4 == 0, "parameters copied as words");
+    const uint64_t work = blockIdx.x;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = n_items - 1;  // last context with block0 <= work
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (items[mid].block0 <= work) lo = mid; else hi = mid - 1;
+        }
+        item = lo;
+    }
+    __syncthreads();
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&items[item].P);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&Ps);
+    for (int i = threadIdx.x; i < (int)(sizeof(WidomParams) / 4); i += WT) dst[i] = src[i];
+    __syncthreads();
+    const WidomItem& it = items[item];
+    widom_block<Real>(Ps, it.D, work - it.block0, it.seed, it.stream, it.first, it.n, draw_order,
+                      it.per_trial, it.partial, it.tab, it.frac_out, it.samples_out);
+}
+
+// One thread per framework: its blocks' partials combined in block order.
+__global__ void widom_batch_combine_kernel(const WidomItem* __restrict__ items, int n_items) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_items) return;
+    combine_partials(items[i].partial, items[i].nblocks, items[i].result);
 }
 
 }  // namespace
@@ -364,6 +439,8 @@ struct WidomImpl {
     DevBuf<KRow> rows;
     EwaldStateImpl* ews = nullptr;
     DevBuf<double> partial, result, per_trial, per_trial_frac;
+    WidomItem item_h{};
+    DevBuf<WidomItem> item;          // the context as a batch of one
     ~WidomImpl() {
         if (ews) ewald_state_destroy(ews);
     }
@@ -460,6 +537,7 @@ WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
         w->rows.alloc(std::max<size_t>(rows.size(), 1));
         w->rows.upload(rows.data(), rows.size());
         w->result.alloc(3);
+        w->item.alloc(1);
     } catch (...) {
         delete w;
         throw;
@@ -467,28 +545,58 @@ WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
     return w;
 }
 
+// K_H, log mean weight and relative standard error from the combined
+// {max, S1 = sum e^(l - max), S2 = sum e^(2 (l - max))} of n trials.
+static void summarise(const double* r, uint64_t n, double temperature, float ms,
+                      alea_widom_result* out) {
+    const double nn = (double)n;
+    const double mean_scaled = r[1] / nn;  // mean(exp(l - max))
+    out->n_trials = n;
+    out->kernel_ms = ms;
+    if (r[1] > 0.0) {
+        out->log_mean_weight = r[0] + std::log(mean_scaled);
+        out->henry = std::exp(out->log_mean_weight) / temperature;
+        const double var = r[2] / nn - mean_scaled * mean_scaled;  // in units of exp(2 max)
+        out->rel_std_error = std::sqrt(std::max(var, 0.0) / nn) / mean_scaled;
+    } else {
+        out->log_mean_weight = -INFINITY;
+        out->henry = 0.0;
+        out->rel_std_error = INFINITY;
+    }
+}
+
 static void widom_launch(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
                          int draw_order, bool per_trial, const ProposalTable& tab,
                          double* frac_dev, float* samples_dev) {
     const uint64_t nblocks = (n + WT - 1) / WT;
-    const double* w_ = nullptr;
+    WidomItem& it = w->item_h;
+    it.P = w->P;
+    const double* wk = nullptr;
     const double *sre = nullptr, *sim = nullptr;
     if (w->ews) {
         const EwaldDeviceView v = ewald_state_view(w->ews);
-        w_ = v.w;
+        wk = v.w;
         sre = v.sre;
         sim = v.sim;
     }
-    if (w->precision == ALEA_FP32)
-        widom_kernel<float><<<(unsigned)nblocks, WT>>>(w->P, w->atoms.p, w->types.p, w->table.p,
-                                                       w->rows.p, w_, sre, sim, seed, stream, first,
-                                                       n, draw_order, per_trial ? w->per_trial.p : nullptr,
-                                                       w->partial.p, tab, frac_dev, samples_dev);
-    else
-        widom_kernel<double><<<(unsigned)nblocks, WT>>>(w->P, w->atoms.p, w->types.p, w->table.p,
-                                                        w->rows.p, w_, sre, sim, seed, stream, first,
-                                                        n, draw_order, per_trial ? w->per_trial.p : nullptr,
-                                                        w->partial.p, tab, frac_dev, samples_dev);
+    it.D = WidomPtrs{w->atoms.p, w->types.p, w->table.p, w->rows.p, wk, sre, sim};
+    it.seed = seed;
+    it.stream = stream;
+    it.first = first;
+    it.n = n;
+    it.partial = w->partial.p;
+    it.result = w->result.p;
+    it.block0 = 0;
+    it.nblocks = nblocks;
+    it.per_trial = per_trial ? w->per_trial.p : nullptr;
+    it.frac_out = frac_dev;
+    it.samples_out = samples_dev;
+    it.tab = tab;
+    ALEA_CUDA(cudaMemcpy(w->item.p, &it, sizeof(WidomItem), cudaMemcpyHostToDevice));
+    auto kern = w->precision == ALEA_FP32 ? widom_batch_kernel<float> : widom_batch_kernel<double>;
+    kern<<<(unsigned)nblocks, WT>>>(w->item.p, 1, draw_order);
+    ALEA_CUDA(cudaGetLastError());
+    widom_batch_combine_kernel<<<1, 32>>>(w->item.p, 1);
     ALEA_CUDA(cudaGetLastError());
 }
 
@@ -527,8 +635,6 @@ void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uin
     ALEA_CUDA(cudaEventRecord(e0));
     widom_launch(w, seed, stream, first, n, draw_order, per_trial != nullptr, tab,
                  per_trial_frac ? w->per_trial_frac.p : nullptr, nullptr);
-    widom_combine_kernel<<<1, 32>>>(w->partial.p, nblocks, w->result.p);
-    ALEA_CUDA(cudaGetLastError());
     ALEA_CUDA(cudaEventRecord(e1));
     ALEA_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
@@ -544,22 +650,132 @@ void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uin
         ALEA_CUDA(cudaMemcpy(per_trial_frac, w->per_trial_frac.p, 3 * n * sizeof(double),
                              cudaMemcpyDeviceToHost));
     }
-    const double nn = (double)n;
-    const double mean_scaled = r[1] / nn;  // mean(exp(l - max))
-    out->n_trials = n;
-    out->kernel_ms = ms;
-    if (r[1] > 0.0) {
-        out->log_mean_weight = r[0] + std::log(mean_scaled);
-        out->henry = std::exp(out->log_mean_weight) / w->P.temperature;
-        const double var = r[2] / nn - mean_scaled * mean_scaled;  // in units of exp(2 max)
-        out->rel_std_error = std::sqrt(std::max(var, 0.0) / nn) / mean_scaled;
-    } else {
-        out->log_mean_weight = -INFINITY;
-        out->henry = 0.0;
-        out->rel_std_error = INFINITY;
-    }
+    summarise(r, n, w->P.temperature, ms, out);
 }
 
 void widom_destroy(WidomImpl* w) { delete w; }
+
+// ---- batch of Widom contexts
+struct WidomBatchImpl {
+    std::vector<WidomImpl*> ctx;
+    int precision = ALEA_FP64;
+    std::vector<WidomItem> items_h;
+    DevBuf<WidomItem> items;
+    DevBuf<double> partial, result;
+    cudaStream_t own = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t graph_total = 0;  // the work the captured graph was made for
+    int graph_order = -1;
+    int sms = 0;
+    ~WidomBatchImpl() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (own) cudaStreamDestroy(own);
+        for (auto* c : ctx) delete c;
+    }
+};
+
+WidomBatchImpl* widom_batch_create(uint32_t n, const alea_lennard_jones* lj, const alea_ewald* ew,
+                                   const alea_particles* fw, const alea_lattice* lat,
+                                   const alea_molecule_species* guest, double temperature,
+                                   int precision) {
+    require(n >= 1, ALEA_ERR_INVALID_ARGUMENT, "alea_widom_batch_create: at least one framework");
+    auto* b = new WidomBatchImpl();
+    try {
+        for (uint32_t i = 0; i < n; ++i)
+            b->ctx.push_back(widom_create(lj[i], ew ? &ew[i] : nullptr, fw[i], lat[i], guest[i],
+                                          temperature, precision));
+        b->precision = precision;
+        b->items.alloc(n);
+        b->result.alloc(3 * (size_t)n);
+        ALEA_CUDA(cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking));
+        int dev = 0;
+        ALEA_CUDA(cudaGetDevice(&dev));
+        ALEA_CUDA(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev));
+    } catch (...) {
+        delete b;
+        throw;
+    }
+    return b;
+}
+
+// Trials [first, first + n) of every framework (framework i on stream
+// (seeds[i], streams[i])), one persistent launch and the per-framework
+// combination replayed from a CUDA graph (captured again only when the total
+// work or the draw order changes).
+void widom_batch_run(WidomBatchImpl* b, const uint64_t* seeds, const uint64_t* streams,
+                     uint64_t first, uint64_t n, int draw_order, alea_widom_result* out,
+                     cudaStream_t s) {
+    require(n > 0, ALEA_ERR_INVALID_ARGUMENT, "Widom: numTrials must be positive");
+    require(draw_order == ALEA_DRAWS_RIGHT_TO_LEFT || draw_order == ALEA_DRAWS_LEFT_TO_RIGHT,
+            ALEA_ERR_INVALID_ARGUMENT, "Widom: unknown draw order");
+    const uint32_t m = (uint32_t)b->ctx.size();
+    const uint64_t nb = (n + WT - 1) / WT;
+    const uint64_t total = nb * m;
+    if (b->partial.n < 3 * total) b->partial.alloc(3 * total);
+    b->items_h.resize(m);
+    for (uint32_t i = 0; i < m; ++i) {
+        WidomImpl* w = b->ctx[i];
+        const double* wk = nullptr;
+        const double *sre = nullptr, *sim = nullptr;
+        if (w->ews) {
+            const EwaldDeviceView v = ewald_state_view(w->ews);
+            wk = v.w;
+            sre = v.sre;
+            sim = v.sim;
+        }
+        WidomItem& it = b->items_h[i];
+        it.P = w->P;
+        it.D = WidomPtrs{w->atoms.p, w->types.p, w->table.p, w->rows.p, wk, sre, sim};
+        it.seed = seeds[i];
+        it.stream = streams[i];
+        it.first = first;
+        it.n = n;
+        it.partial = b->partial.p + 3 * nb * i;
+        it.result = b->result.p + 3 * (size_t)i;
+        it.block0 = nb * i;
+        it.nblocks = nb;
+        it.per_trial = nullptr;
+        it.frac_out = nullptr;
+        it.samples_out = nullptr;
+        it.tab = ProposalTable{0, nullptr, nullptr};
+    }
+    cudaStream_t run = s ? s : b->own;
+    ALEA_CUDA(cudaMemcpyAsync(b->items.p, b->items_h.data(), m * sizeof(WidomItem),
+                              cudaMemcpyHostToDevice, run));
+    if (!b->exec || b->graph_total != total || b->graph_order != draw_order) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
+        auto kern = b->precision == ALEA_FP32 ? widom_batch_kernel<float> : widom_batch_kernel<double>;
+        require(total < (1ull << 31), ALEA_ERR_INVALID_ARGUMENT, "Widom batch: too many trials");
+        ALEA_CUDA(cudaStreamSynchronize(run));
+        ALEA_CUDA(cudaStreamBeginCapture(b->own, cudaStreamCaptureModeThreadLocal));
+        kern<<<(unsigned)total, WT, 0, b->own>>>(b->items.p, (int)m, draw_order);
+        widom_batch_combine_kernel<<<(m + 127) / 128, 128, 0, b->own>>>(b->items.p, (int)m);
+        ALEA_CUDA(cudaStreamEndCapture(b->own, &b->graph));
+        ALEA_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+        b->graph_total = total;
+        b->graph_order = draw_order;
+    }
+    cudaEvent_t e0, e1;
+    ALEA_CUDA(cudaEventCreate(&e0));
+    ALEA_CUDA(cudaEventCreate(&e1));
+    ALEA_CUDA(cudaEventRecord(e0, run));
+    ALEA_CUDA(cudaGraphLaunch(b->exec, run));
+    ALEA_CUDA(cudaEventRecord(e1, run));
+    ALEA_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    ALEA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::vector<double> r(3 * (size_t)m);
+    ALEA_CUDA(cudaMemcpy(r.data(), b->result.p, r.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < m; ++i) summarise(&r[3 * (size_t)i], n, b->ctx[i]->P.temperature, ms, &out[i]);
+}
+
+void widom_batch_destroy(WidomBatchImpl* b) { delete b; }
 
 }  // namespace alea

@@ -73,6 +73,10 @@ def perpendicular_widths(m: np.ndarray) -> np.ndarray:
                      for i in range(3)])
 
 
+_IMAGE_SHIFTS = np.array([n for n in np.array(np.meshgrid([-1, 0, 1], [-1, 0, 1], [-1, 0, 1])).T.reshape(-1, 3)
+                          if n.any()], dtype=np.float64)
+
+
 def _min_image_dist2(m: np.ndarray, minv: np.ndarray, p: np.ndarray, pts: np.ndarray) -> np.ndarray:
     if pts.shape[0] == 0:
         return np.zeros(0)
@@ -80,18 +84,20 @@ def _min_image_dist2(m: np.ndarray, minv: np.ndarray, p: np.ndarray, pts: np.nda
     df -= np.rint(df)
     d = df @ m
     best = np.einsum("ij,ij->i", d, d)
-    # small skewed cells: also look at the neighbouring images
-    for n in np.array(np.meshgrid([-1, 0, 1], [-1, 0, 1], [-1, 0, 1])).T.reshape(-1, 3):
-        if not n.any():
-            continue
-        dd = d + n @ m
-        best = np.minimum(best, np.einsum("ij,ij->i", dd, dd))
-    return best
+    # small skewed cells: also look at the 26 neighbouring images
+    dd = d[None, :, :] + (_IMAGE_SHIFTS @ m)[:, None, :]
+    return np.minimum(best, np.einsum("kij,kij->ki", dd, dd).min(axis=0))
 
 
 def _place_atoms(m: np.ndarray, n_atoms: int, seed: int, stream: int, min_sep: float = 1.0):
-    """Uniform positions with minimum-image rejection below ``min_sep`` Å."""
+    """Uniform positions with minimum-image rejection below ``min_sep`` Å.
+
+    Candidates are checked against the atoms of the 27 neighbouring fractional
+    bins only: a bin is at least ``min_sep`` wide across, so every atom closer
+    than that is among them and the decisions equal those of a full scan."""
     minv = np.linalg.inv(m)
+    nb = np.maximum(1, np.floor(perpendicular_widths(m) / min_sep).astype(int))
+    bins: dict = {}
     pos = np.zeros((n_atoms, 3))
     count = 0
     call = 0
@@ -101,9 +107,16 @@ def _place_atoms(m: np.ndarray, n_atoms: int, seed: int, stream: int, min_sep: f
         call += batch
         for f in u:
             p = f @ m
-            if count and _min_image_dist2(m, minv, p, pos[:count]).min() < min_sep * min_sep:
+            b = [min(int(f[a] * nb[a]), nb[a] - 1) for a in range(3)]
+            cand = []
+            for i in {(b[0] + d) % nb[0] for d in (-1, 0, 1)}:
+                for j in {(b[1] + d) % nb[1] for d in (-1, 0, 1)}:
+                    for k in {(b[2] + d) % nb[2] for d in (-1, 0, 1)}:
+                        cand.extend(bins.get((i, j, k), ()))
+            if cand and _min_image_dist2(m, minv, p, pos[cand]).min() < min_sep * min_sep:
                 continue
             pos[count] = p
+            bins.setdefault((b[0], b[1], b[2]), []).append(count)
             count += 1
             if count == n_atoms:
                 break

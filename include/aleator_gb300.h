@@ -408,6 +408,22 @@ alea_status alea_widom_run_biased(alea_widom* w, const alea_proposal* p, uint64_
                                   alea_widom_result* out, double* per_trial_du,
                                   double* per_trial_frac);
 
+/* A batch of Widom contexts (one per framework, each with its own force field,
+ * atoms, cell and guest template) run together: one persistent launch over
+ * (framework, block of 128 trials) work items and a per-framework combination,
+ * replayed from a captured CUDA graph. Framework i's result equals
+ * alea_widom_run on its own context with (seeds[i], streams[i]). ewald is
+ * NULL (LJ only) or n entries. out holds n results. */
+typedef struct alea_widom_batch alea_widom_batch;
+alea_status alea_widom_batch_create(uint32_t n, const alea_lennard_jones* lj, const alea_ewald* ewald,
+                                    const alea_particles* frameworks, const alea_lattice* lattices,
+                                    const alea_molecule_species* guests, double temperature,
+                                    int32_t precision, alea_widom_batch** out);
+alea_status alea_widom_batch_run(alea_widom_batch* b, const uint64_t* seeds, const uint64_t* streams,
+                                 uint64_t first_trial, uint64_t n_trials, int32_t draw_order,
+                                 alea_widom_result* out, void* cuda_stream);
+alea_status alea_widom_batch_destroy(alea_widom_batch* b);
+
 /* ------------------------------------------------------------------ GCMC chains */
 /* MonteCarloEngine (engines/monte_carlo/monte_carlo_engine.hpp:76-83, single
  * species, direct-scan dispersion) for n_chains independent chains at once:

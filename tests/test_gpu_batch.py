@@ -1,7 +1,8 @@
-"""Batched energy grids (uneven triclinic frameworks, each with its own force
-field, in one persistent launch per kernel behind a captured CUDA graph):
-every grid equals the single-grid FP32 build of its framework bit for bit,
-graph replays reproduce it, and the autotuner records its choice."""
+"""Batched energy grids and Widom runs (uneven triclinic frameworks, each with
+its own force field, in one persistent launch per kernel behind a captured
+CUDA graph): every grid equals the single-grid FP32 build of its framework bit
+for bit, graph replays reproduce it, the autotuner records its choice, and
+every framework's batched Widom result equals its own Widom run exactly."""
 import numpy as np
 import pytest
 
@@ -51,3 +52,22 @@ def test_batch_rejects_mixed_guest_counts(lib):
     g = fws[0].guest_species["CH4"]
     with pytest.raises(ValueError):
         A.GridBatch(ffs, ps, [fw.lattice for fw in fws], [[g, g], [g, 0]], 0.6)
+
+
+def test_widom_batch_equals_single_runs(lib):
+    A, _ = lib
+    fws = _frameworks(5, seed=7)
+    ffs = [A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED) for fw in fws]
+    ps = [A.ParticleData.from_framework(fw) for fw in fws]
+    guests = [W.ch4_guest(fw) for fw in fws]
+    seeds, streams = [11 + i for i in range(5)], [i for i in range(5)]
+    for prec in (A.FP64, A.FP32):
+        batch = A.WidomBatch(ffs, ps, [fw.lattice for fw in fws], guests, 298.0, precision=prec)
+        for n in (3000, 5000):  # a second size re-captures the graph
+            res = batch.run(seeds, streams, n, first_trial=17)
+            for i, fw in enumerate(fws):
+                w = A.Widom(ffs[i], ps[i], fw.lattice, guests[i], 298.0, precision=prec)
+                r = w.run(seeds[i], streams[i], n, first_trial=17)
+                assert res[i]["henry"] == r["henry"], (prec, n, i)
+                assert res[i]["rel_std_error"] == r["rel_std_error"], (prec, n, i)
+                assert res[i]["n_trials"] == n
