@@ -563,7 +563,6 @@ struct F32Params {
     float shift[64 * NG];
     float dvdrc[64 * NG];
     float vclose[64 * NG];
-    ParamFF pff[64 * NG];
     float close2[64];
 };
 
@@ -577,13 +576,12 @@ __device__ void load_f32_params(F32Params<NG, TRUNC>& P, const ParamAB* __restri
         P.ab[i] = make_ulonglong2(f2_pack(p.a, p.a), f2_pack(-p.b, -p.b));
         P.shift[i] = TRUNC == ALEA_TRUNCATED ? 0.f : p.shift;
         P.dvdrc[i] = p.dvdrc;
-        P.pff[i] = pff_g[(size_t)g * nt + t];
     }
     __syncthreads();
     // the sweep's operations, in its order, at r^2 = sigma_t^2
     for (int t = tid; t < nt; t += THREADS) {
         float m = 0.f;
-        for (int g = 0; g < NG; ++g) m = fmaxf(m, P.pff[t * NG + g].sig2_hi);
+        for (int g = 0; g < NG; ++g) m = fmaxf(m, pff_g[(size_t)g * nt + t].sig2_hi);
         P.close2[t] = m;
         const float ir2 = rcp_approx(m);
         const float ir6 = __fmul_rn(ir2, __fmul_rn(ir2, ir2));
@@ -642,12 +640,12 @@ __device__ __forceinline__ float r2_f32(float ax, float ay, float az, float nx, 
 // the -V(rc) the sweep charges every pair: the correction that turns the
 // sweep's value for this pair into the exact one.
 template <int NG, int TRUNC>
-__device__ __forceinline__ ff close_pair(const F32Params<NG, TRUNC>& P, int type, int g, ff ddx,
+__device__ __forceinline__ ff close_pair(const F32Params<NG, TRUNC>& P, const ParamFF* pff, int type, int g, ff ddx,
                                          ff ddy, ff ddz, float rcf) {
     ff rr = ff_add(ff_add(ff_mul(ddx, ddx), ff_mul(ddy, ddy)), ff_mul(ddz, ddz));
     if (rr.hi < 1e-4f) rr = ff{1e-4f, 0.f};
     const ff iv = ff_rcp(rr);
-    const ParamFF q = P.pff[type * NG + g];
+    const ParamFF q = pff[type * NG + g];
     const ff s2 = ff_mul(ff{q.sig2_hi, q.sig2_lo}, iv);
     const ff s6 = ff_mul(ff_mul(s2, s2), s2);
     const ff tt = ff_mul(s6, ff_add(s6, ff{-1.f, 0.f}));
@@ -723,6 +721,10 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     // double-float sweep sums (touched once per tile): hi at [(g NPT + k) 2 + 0]
     // x THREADS + tid, lo at [... + 1]
     float* accs = sc.take<float>(2 * NG * NPT * THREADS);
+    float4* wsph = sc.take<float4>(THREADS / 32);  // per warp: sphere centre, cull2
+    float* wnear = sc.take<float>(THREADS / 32);   // per warp: near2
+    uint16_t* amask = sc.take<uint16_t>(TILE);     // per atom: bit w culled in, bit 8 + w near
+    uint16_t* wlist = sc.take<uint16_t>((THREADS / 32) * TILE);  // per warp: (atom << 1) | near
     const ImageRecF* __restrict__ images = A.images;
     const uint32_t* __restrict__ bin_start = A.bin_start;
     double* __restrict__ tables = A.tables;
@@ -761,8 +763,8 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     }
     // the warp's bounding sphere: centre of its 8x4x4 sub-box, radius over its
     // nodes; 1e-3 A of margin covers FP32 rounding in the two reach tests
-    float wcx, wcy, wcz, cull2, near2;
     {
+        float wcx, wcy, wcz;
         const int w = tid >> 5;
         const float wd0 = (w & 1) * 8 + 3.5f - 0.5f * (BX - 1);
         const float wd1 = ((w >> 1) & 1) * 4 + 1.5f - 0.5f * (BY - 1);
@@ -788,8 +790,10 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) r2max = fmaxf(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
         const float rad = sqrtf(r2max) + 1e-3f;
-        cull2 = (geo.rcf + rad) * (geo.rcf + rad) * (1.0f + 1e-5f);
-        near2 = (geo.smaxf + rad) * (geo.smaxf + rad) * (1.0f + 1e-5f);
+        if ((tid & 31) == 0) {  // read after the first tile's barrier
+            wsph[w] = make_float4(wcx, wcy, wcz, (geo.rcf + rad) * (geo.rcf + rad) * (1.0f + 1e-5f));
+            wnear[w] = (geo.smaxf + rad) * (geo.smaxf + rad) * (1.0f + 1e-5f);
+        }
     }
 
     float ce[NG][NPT];               // FP32 close-pair estimates
@@ -824,14 +828,43 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
             return false;
         }
         static_assert(TILE == THREADS, "one record per thread in the conversion pass");
+        static_assert(TILE <= 32768 && THREADS / 32 <= 8, "list entry and mask widths");
         if ((uint32_t)tid < cnt) {
             ff v[3];
             const ImageRecF r = raw[buf * TILE + tid];
             atom_local(r, org, v);
             cxy[tid] = make_ulonglong2(f2_pack(v[0].hi, v[0].hi), f2_pack(v[1].hi, v[1].hi));
             czt[tid] = make_ulonglong2(f2_pack(v[2].hi, v[2].hi), (unsigned long long)r.type);
+            // which warps' spheres this atom reaches
+            uint32_t m = 0;
+#pragma unroll
+            for (int w = 0; w < THREADS / 32; ++w) {
+                const float4 c = wsph[w];
+                const float ex = v[0].hi - c.x, ey = v[1].hi - c.y, ez = v[2].hi - c.z;
+                const float d2w = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                if (!(d2w > c.w)) m |= (d2w < wnear[w] ? 0x101u : 0x1u) << w;
+            }
+            amask[tid] = (uint16_t)m;
         }
         __syncthreads();
+        // this warp's atoms, in tile order
+        uint32_t n_w = 0;
+        uint16_t* mine_list = wlist + (tid >> 5) * TILE;
+        {
+            const int w = tid >> 5, lane = tid & 31;
+            for (uint32_t c0 = 0; c0 < cnt; c0 += 32) {
+                const uint32_t j = c0 + lane;
+                const uint32_t m = j < cnt ? amask[j] : 0u;
+                const bool in = (m >> w) & 1u;
+                const uint32_t b = __ballot_sync(0xffffffffu, in);
+                if (in)
+                    mine_list[n_w + __popc(b & ((1u << lane) - 1u))] =
+                        (uint16_t)((j << 1) | ((m >> (8 + w)) & 1u));
+                n_w += __popc(b);
+            }
+            __syncwarp();
+        }
+        passes += n_w;
         // raw[buf] is free again: prefetch tile t + 2 while computing
         if (tid == 0 && t + 2 < n_tiles) {
             fence_proxy_async();
@@ -846,20 +879,11 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
 #pragma unroll
             for (int q = 0; q < NP; ++q) part[g][q] = 0ull;  // {+0, +0}
         }
-        for (uint32_t j = 0; j < cnt; ++j) {
+        for (uint32_t u = 0; u < n_w; ++u) {
+            const uint32_t e = mine_list[u];
+            const uint32_t j = e >> 1;
             const ulonglong2 xy = cxy[j];
             const ulonglong2 zt = czt[j];
-            float ax, ay, az, dummy;
-            f2_unpack(xy.x, ax, dummy);
-            f2_unpack(xy.y, ay, dummy);
-            f2_unpack(zt.x, az, dummy);
-            float d2w;
-            {
-                const float ex = ax - wcx, ey = ay - wcy, ez = az - wcz;
-                d2w = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-            }
-            if (d2w > cull2) continue;  // warp-uniform
-            ++passes;
             const int type = (int)(uint32_t)zt.y;
             const float close2 = P.close2[type];
             ulonglong2 AB[NG];
@@ -868,7 +892,11 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
                 AB[g] = P.ab[type * NG + g];
                 shift_sum[g] += P.shift[type * NG + g];
             }
-            if (d2w < near2) {  // warp-uniform: this atom may be closer than sigma_t
+            if (e & 1u) {  // warp-uniform: this atom may be closer than sigma_t
+                float ax, ay, az, dummy;
+                f2_unpack(xy.x, ax, dummy);
+                f2_unpack(xy.y, ay, dummy);
+                f2_unpack(zt.x, az, dummy);
 #pragma unroll
                 for (int k = 0; k < NPT; ++k) {
                     float p[2][3];
@@ -1009,7 +1037,9 @@ constexpr size_t f32_smem_bytes() {
     return carve(2 * TILE * sizeof(ImageRecF)) + carve(TILE * sizeof(ulonglong2)) +
            carve(TILE * sizeof(ulonglong2)) + carve(MAX_ROWS * sizeof(uint32_t)) +
            carve((MAX_ROWS + 1) * sizeof(uint32_t)) + carve((THREADS / 32) * sizeof(uint32_t)) +
-           carve(sizeof(F32Params<NG, TRUNC>)) + carve(2 * NG * NPT * THREADS * sizeof(float));
+           carve(sizeof(F32Params<NG, TRUNC>)) + carve(2 * NG * NPT * THREADS * sizeof(float)) +
+           carve((THREADS / 32) * sizeof(float4)) + carve((THREADS / 32) * sizeof(float)) +
+           carve(TILE * sizeof(uint16_t)) + carve((THREADS / 32) * TILE * sizeof(uint16_t));
 }
 
 // ---------------------------------------------------------------- FP32 close-pair correction
@@ -1045,6 +1075,7 @@ __device__ __forceinline__ void fix_brick(const GridGeom& geo, const F32GridArgs
     uint16_t* clist = sc.take<uint16_t>(THREADS * NPT * MAX_CLOSE);
     uint16_t* ccount = sc.take<uint16_t>(THREADS * NPT);
     F32Params<NG, TRUNC>& P = *sc.take<F32Params<NG, TRUNC>>(1);
+    ParamFF* pff = sc.take<ParamFF>(64 * NG);  // [type][guest], double-float
     static_assert(NPT == 4 && NG <= 8, "node and guest bits");
 
     const int tid = threadIdx.x;
@@ -1103,6 +1134,8 @@ __device__ __forceinline__ void fix_brick(const GridGeom& geo, const F32GridArgs
                 ++off;
             }
     }
+    for (int i = tid; i < geo.n_types * NG; i += THREADS)
+        pff[i] = A.pff[(size_t)(i % NG) * geo.n_types + i / NG];
     load_f32_params(P, A.pab, A.pff, geo.n_types, geo.rcf);  // synchronises
     const int nr = plan_rows(geo, geo.hf_near, geo.keep2_near, bin_start, x0, y0, z0, row_begin,
                              row_off, warp_tot, flags);
@@ -1160,7 +1193,7 @@ __device__ __forceinline__ void fix_brick(const GridGeom& geo, const F32GridArgs
                 const ff ddx = ff_add(ff{a.x, l.x}, ff{-p.x, -pl.x});
                 const ff ddy = ff_add(ff{a.y, l.y}, ff{-p.y, -pl.y});
                 const ff ddz = ff_add(ff{a.z, l.z}, ff{-p.z, -pl.z});
-                acc = ff_add(acc, close_pair(P, type, g, ddx, ddy, ddz, geo.rcf));
+                acc = ff_add(acc, close_pair(P, pff, type, g, ddx, ddy, ddz, geo.rcf));
             }
             if (c) {
                 const uint32_t node = fnode[f];
@@ -1200,7 +1233,8 @@ constexpr size_t fix_smem_bytes() {
            carve(THREADS * NPT * sizeof(uint16_t)) + carve(THREADS * NPT * sizeof(uint8_t)) +
            carve(2 * THREADS * NPT * sizeof(float4)) +
            carve(THREADS * NPT * MAX_CLOSE * sizeof(uint16_t)) +
-           carve(THREADS * NPT * sizeof(uint16_t)) + carve(sizeof(F32Params<NG, TRUNC>));
+           carve(THREADS * NPT * sizeof(uint16_t)) + carve(sizeof(F32Params<NG, TRUNC>)) +
+           carve(64 * NG * sizeof(ParamFF));
 }
 
 // ---------------------------------------------------------------- batched FP32 build
