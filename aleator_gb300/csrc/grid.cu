@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -722,9 +723,9 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     // x THREADS + tid, lo at [... + 1]
     float* accs = sc.take<float>(2 * NG * NPT * THREADS);
     float4* wsph = sc.take<float4>(THREADS / 32);  // per warp: sphere centre, cull2
-    float* wnear = sc.take<float>(THREADS / 32);   // per warp: near2
-    uint16_t* amask = sc.take<uint16_t>(TILE);     // per atom: bit w culled in, bit 8 + w near
-    uint16_t* wlist = sc.take<uint16_t>((THREADS / 32) * TILE);  // per warp: (atom << 1) | near
+    float2* wlim = sc.take<float2>(THREADS / 32);  // per warp: near2, inner2
+    uint16_t* amask = sc.take<uint16_t>(TILE);     // per atom: 2-bit class per warp
+    uint16_t* wlist = sc.take<uint16_t>((THREADS / 32) * TILE);  // per warp: atom lists
     const ImageRecF* __restrict__ images = A.images;
     const uint32_t* __restrict__ bin_start = A.bin_start;
     double* __restrict__ tables = A.tables;
@@ -792,7 +793,10 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
         const float rad = sqrtf(r2max) + 1e-3f;
         if ((tid & 31) == 0) {  // read after the first tile's barrier
             wsph[w] = make_float4(wcx, wcy, wcz, (geo.rcf + rad) * (geo.rcf + rad) * (1.0f + 1e-5f));
-            wnear[w] = (geo.smaxf + rad) * (geo.smaxf + rad) * (1.0f + 1e-5f);
+            // near: within sigma_max of some node; inner: every node within the cutoff
+            const float in = geo.rcf - rad;
+            wlim[w] = make_float2((geo.smaxf + rad) * (geo.smaxf + rad) * (1.0f + 1e-5f),
+                                  in > 0.f ? in * in * (1.0f - 1e-5f) : -1.f);
         }
     }
 
@@ -828,71 +832,89 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
             return false;
         }
         static_assert(TILE == THREADS, "one record per thread in the conversion pass");
-        static_assert(TILE <= 32768 && THREADS / 32 <= 8, "list entry and mask widths");
+        static_assert(TILE <= 32768 && THREADS / 32 <= 8, "list entry and class-mask widths");
         if ((uint32_t)tid < cnt) {
             ff v[3];
             const ImageRecF r = raw[buf * TILE + tid];
             atom_local(r, org, v);
             cxy[tid] = make_ulonglong2(f2_pack(v[0].hi, v[0].hi), f2_pack(v[1].hi, v[1].hi));
             czt[tid] = make_ulonglong2(f2_pack(v[2].hi, v[2].hi), (unsigned long long)r.type);
-            // which warps' spheres this atom reaches
+            // this atom's class for each warp (2 bits per warp): 0 beyond the
+            // warp's reach, 1 inner, 2 boundary, 3 near
             uint32_t m = 0;
 #pragma unroll
             for (int w = 0; w < THREADS / 32; ++w) {
                 const float4 c = wsph[w];
+                const float2 lim = wlim[w];
                 const float ex = v[0].hi - c.x, ey = v[1].hi - c.y, ez = v[2].hi - c.z;
                 const float d2w = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-                if (!(d2w > c.w)) m |= (d2w < wnear[w] ? 0x101u : 0x1u) << w;
+                const uint32_t cls = d2w > c.w ? 0u : d2w < lim.x ? 3u : d2w <= lim.y ? 1u : 2u;
+                m |= cls << (2 * w);
             }
             amask[tid] = (uint16_t)m;
         }
         __syncthreads();
-        // this warp's atoms, in tile order
-        uint32_t n_w = 0;
-        uint16_t* mine_list = wlist + (tid >> 5) * TILE;
-        {
-            const int w = tid >> 5, lane = tid & 31;
-            for (uint32_t c0 = 0; c0 < cnt; c0 += 32) {
-                const uint32_t j = c0 + lane;
-                const uint32_t m = j < cnt ? amask[j] : 0u;
-                const bool in = (m >> w) & 1u;
-                const uint32_t b = __ballot_sync(0xffffffffu, in);
-                if (in)
-                    mine_list[n_w + __popc(b & ((1u << lane) - 1u))] =
-                        (uint16_t)((j << 1) | ((m >> (8 + w)) & 1u));
-                n_w += __popc(b);
-            }
-            __syncwarp();
-        }
-        passes += n_w;
         // raw[buf] is free again: prefetch tile t + 2 while computing
         if (tid == 0 && t + 2 < n_tiles) {
             fence_proxy_async();
             issue_tile(t + 2, n_cand, nr, row_begin, row_off, img,
                        rawb + buf * TILE * sizeof(ImageRecF), &bars[buf]);
         }
-        f2 part[NG][NP];
+        // this warp's atoms: inner ones from the front of its list (tile
+        // order), the others from the back; the shift sum over both (every
+        // lane of the warp needs the same sum)
+        uint32_t n_in = 0, n_out = 0;
+        uint16_t* mine_list = wlist + (tid >> 5) * TILE;
         float shift_sum[NG];
+        {
+            const int w = tid >> 5, lane = tid & 31;
+            const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
-        for (int g = 0; g < NG; ++g) {
-            shift_sum[g] = 0.f;
+            for (int g = 0; g < NG; ++g) shift_sum[g] = 0.f;
+            for (uint32_t c0 = 0; c0 < cnt; c0 += 32) {
+                const uint32_t j = c0 + lane;
+                const uint32_t cls = j < cnt ? (amask[j] >> (2 * w)) & 3u : 0u;
+                const uint32_t b_in = __ballot_sync(0xffffffffu, cls == 1u);
+                const uint32_t b_out = __ballot_sync(0xffffffffu, cls >= 2u);
+                if (cls == 1u) mine_list[n_in + __popc(b_in & lt)] = (uint16_t)j;
+                if (cls >= 2u)
+                    mine_list[TILE - 1 - (n_out + __popc(b_out & lt))] = (uint16_t)((j << 1) | (cls & 1u));
+                if (TRUNC != ALEA_TRUNCATED && cls) {
+                    const int type = (int)(uint32_t)czt[j].y;
+#pragma unroll
+                    for (int g = 0; g < NG; ++g) shift_sum[g] += P.shift[type * NG + g];
+                }
+                n_in += __popc(b_in);
+                n_out += __popc(b_out);
+            }
+            if (TRUNC != ALEA_TRUNCATED) {
+#pragma unroll
+                for (int g = 0; g < NG; ++g)
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1)
+                        shift_sum[g] += __shfl_xor_sync(0xffffffffu, shift_sum[g], o);
+            }
+            __syncwarp();
+        }
+        passes += n_in + n_out;
+        f2 part[NG][NP];
+#pragma unroll
+        for (int g = 0; g < NG; ++g)
 #pragma unroll
             for (int q = 0; q < NP; ++q) part[g][q] = 0ull;  // {+0, +0}
-        }
-        for (uint32_t u = 0; u < n_w; ++u) {
-            const uint32_t e = mine_list[u];
-            const uint32_t j = e >> 1;
+        // one atom against this thread's nodes; LO: clamp r^2 from below at
+        // sigma_t^2, HI: clamp (or cut) at the cutoff
+        auto add_atom = [&](uint32_t j, auto lo_tag, auto hi_tag) {
+            constexpr bool LO = decltype(lo_tag)::value, HI = decltype(hi_tag)::value;
             const ulonglong2 xy = cxy[j];
             const ulonglong2 zt = czt[j];
             const int type = (int)(uint32_t)zt.y;
-            const float close2 = P.close2[type];
+            float close2 = 0.f;
+            if (LO) close2 = P.close2[type];
             ulonglong2 AB[NG];
 #pragma unroll
-            for (int g = 0; g < NG; ++g) {
-                AB[g] = P.ab[type * NG + g];
-                shift_sum[g] += P.shift[type * NG + g];
-            }
-            if (e & 1u) {  // warp-uniform: this atom may be closer than sigma_t
+            for (int g = 0; g < NG; ++g) AB[g] = P.ab[type * NG + g];
+            if (LO) {  // this atom may be closer than sigma_t to a node
                 float ax, ay, az, dummy;
                 f2_unpack(xy.x, ax, dummy);
                 f2_unpack(xy.y, ay, dummy);
@@ -931,11 +953,21 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
                 f2_unpack(r2, r2a, r2b);
                 float ia, ib;
                 if (TRUNC == ALEA_TRUNCATED) {
-                    ia = r2a > rc2f ? 0.f : rcp_approx(fmaxf(r2a, close2));
-                    ib = r2b > rc2f ? 0.f : rcp_approx(fmaxf(r2b, close2));
+                    ia = rcp_approx(LO ? fmaxf(r2a, close2) : r2a);
+                    ib = rcp_approx(LO ? fmaxf(r2b, close2) : r2b);
+                    if (HI) {
+                        ia = r2a > rc2f ? 0.f : ia;
+                        ib = r2b > rc2f ? 0.f : ib;
+                    }
                 } else {
-                    r2a = fminf(fmaxf(r2a, close2), rc2f);
-                    r2b = fminf(fmaxf(r2b, close2), rc2f);
+                    if (LO) {
+                        r2a = fmaxf(r2a, close2);
+                        r2b = fmaxf(r2b, close2);
+                    }
+                    if (HI) {
+                        r2a = fminf(r2a, rc2f);
+                        r2b = fminf(r2b, rc2f);
+                    }
                     ia = rcp_approx(r2a);
                     ib = rcp_approx(r2b);
                 }
@@ -953,6 +985,18 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
                     }
                 }
             }
+        };
+        using yes = std::true_type;
+        using no = std::false_type;
+        // inner atoms: every node of the warp within the cutoff and none
+        // closer than sigma_t, so neither clamp can act
+        for (uint32_t u = 0; u < n_in; ++u) add_atom(mine_list[u], no{}, no{});
+        for (uint32_t u = TILE - n_out; u < TILE; ++u) {
+            const uint32_t e = mine_list[u];
+            if (e & 1u)  // warp-uniform
+                add_atom(e >> 1, yes{}, yes{});
+            else
+                add_atom(e >> 1, no{}, yes{});
         }
 #pragma unroll
         for (int g = 0; g < NG; ++g)
@@ -1038,7 +1082,7 @@ constexpr size_t f32_smem_bytes() {
            carve(TILE * sizeof(ulonglong2)) + carve(MAX_ROWS * sizeof(uint32_t)) +
            carve((MAX_ROWS + 1) * sizeof(uint32_t)) + carve((THREADS / 32) * sizeof(uint32_t)) +
            carve(sizeof(F32Params<NG, TRUNC>)) + carve(2 * NG * NPT * THREADS * sizeof(float)) +
-           carve((THREADS / 32) * sizeof(float4)) + carve((THREADS / 32) * sizeof(float)) +
+           carve((THREADS / 32) * sizeof(float4)) + carve((THREADS / 32) * sizeof(float2)) +
            carve(TILE * sizeof(uint16_t)) + carve((THREADS / 32) * TILE * sizeof(uint16_t));
 }
 

@@ -149,6 +149,36 @@ def test_truncations_vs_oracle(lib, orc, trunc):
         assert rel_err(grid.table(sid), ref).max() <= 1e-10
 
 
+@pytest.mark.parametrize("trunc", [0, 1, 2])
+def test_fp32_truncations_vs_oracle(lib, orc, trunc):
+    """The FP32 sweep in every truncation, two guests, at a coarse spacing
+    (every node) and a fine one (a strided sample): the atoms of a warp's
+    tile take the clamp-free, cutoff-clamped and close-pair paths."""
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    fw = W.cubic_framework(seed=7)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.0, trunc)
+    p = A.ParticleData.from_framework(fw)
+    odict = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.0, truncation=trunc)
+    for spacing, stride in ((1.7, 1), (0.45, 131)):
+        grid = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4, 6], spacing, A.FP32)
+        nodes = int(np.prod(grid.point_counts()))
+        idx = np.arange(0, nodes, stride)
+        for sid in (4, 6):
+            if stride == 1:
+                ref = orc.grid_build(odict, fw.lattice, fw.x, fw.y, fw.z, fw.species, sid, spacing,
+                                     threads=8)
+            else:
+                ref = np.concatenate([orc.grid_build(odict, fw.lattice, fw.x, fw.y, fw.z, fw.species,
+                                                     sid, spacing, node_begin=int(i),
+                                                     node_end=int(i) + 1) for i in idx])
+            mine = grid.table(sid)[idx]
+            keep = ref <= 1e4
+            assert keep.sum() > 100
+            assert rel_err(mine[keep], ref[keep], floor=KT).max() <= 1e-5
+            assert (mine[ref >= 1e5] >= 1e4).all()
+
+
 def test_full_c1_grid_vs_oracle_sample(lib, orc):
     """The 52^3 grid of the 424-atom cell at 0.5 Å: every node in FP64 and FP32
     against the oracle on a strided sample of nodes."""
