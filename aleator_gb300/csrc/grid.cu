@@ -712,9 +712,9 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
                                             unsigned long long* __restrict__ executed,
                                             unsigned* flags) {
     SmemCarve sc{smem};
-    ImageRecF* raw = sc.take<ImageRecF>(2 * TILE);
-    ulonglong2* cxy = sc.take<ulonglong2>(TILE);   // {x, x}, {y, y}
-    ulonglong2* czt = sc.take<ulonglong2>(TILE);   // {z, z}, {type, 0}
+    ImageRecF* raw = sc.take<ImageRecF>(TILE);         // the staged tile (TMA)
+    ulonglong2* cxy = sc.take<ulonglong2>(2 * TILE);   // converted tiles: {x, x}, {y, y}
+    ulonglong2* czt = sc.take<ulonglong2>(2 * TILE);   // {z, z}, {type, 0}
     uint32_t* row_begin = sc.take<uint32_t>(MAX_ROWS);
     uint32_t* row_off = sc.take<uint32_t>(MAX_ROWS + 1);
     uint32_t* warp_tot = sc.take<uint32_t>(THREADS / 32);
@@ -724,7 +724,7 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     float* accs = sc.take<float>(2 * NG * NPT * THREADS);
     float4* wsph = sc.take<float4>(THREADS / 32);  // per warp: sphere centre, cull2
     float2* wlim = sc.take<float2>(THREADS / 32);  // per warp: near2, inner2
-    uint16_t* amask = sc.take<uint16_t>(TILE);     // per atom: 2-bit class per warp
+    uint16_t* amask = sc.take<uint16_t>(2 * TILE); // per atom: 2-bit class per warp
     uint16_t* wlist = sc.take<uint16_t>((THREADS / 32) * TILE);  // per warp: atom lists
     const ImageRecF* __restrict__ images = A.images;
     const uint32_t* __restrict__ bin_start = A.bin_start;
@@ -815,30 +815,25 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     unsigned char* rawb = reinterpret_cast<unsigned char*>(raw);
     const uint32_t n_tiles = (n_cand + TILE - 1) / TILE;
     const uint32_t T0 = tiles;  // tile t of this brick is the CTA's tile T0 + t
-    if (tid == 0) {
-        for (uint32_t t = 0; t < 2 && t < n_tiles; ++t) {
-            const int b = (T0 + t) & 1;
-            issue_tile(t, n_cand, nr, row_begin, row_off, img, rawb + b * TILE * sizeof(ImageRecF),
-                       &bars[b]);
-        }
-    }
+    // One staging buffer (bars[0]; its k-th phase is the CTA's tile k) and two
+    // converted-tile buffers: the conversion of tile t writes buffer t & 1,
+    // last read by the main loop of tile t - 2, which every warp finished
+    // before the barrier of tile t - 1; so one barrier per tile.
+    if (tid == 0 && n_tiles > 0) issue_tile(0, n_cand, nr, row_begin, row_off, img, rawb, &bars[0]);
     for (uint32_t t = 0; t < n_tiles; ++t) {
-        const int buf = (T0 + t) & 1;
         const uint32_t cnt = min((uint32_t)TILE, n_cand - t * TILE);
-        // block-wide vote so that every thread takes the same path on a timeout
-        const bool got = mbar_wait_bounded(&bars[buf], ((T0 + t) >> 1) & 1, flags);
-        if (!__syncthreads_and(got)) {
-            drain_tiles(T0 + t, T0 + n_tiles, bars);
-            return false;
-        }
+        ulonglong2* cxy_t = cxy + (t & 1) * TILE;
+        ulonglong2* czt_t = czt + (t & 1) * TILE;
+        uint16_t* amask_t = amask + (t & 1) * TILE;
+        const bool got = mbar_wait_bounded(&bars[0], (T0 + t) & 1, flags);
         static_assert(TILE == THREADS, "one record per thread in the conversion pass");
         static_assert(TILE <= 32768 && THREADS / 32 <= 8, "list entry and class-mask widths");
-        if ((uint32_t)tid < cnt) {
+        if (got && (uint32_t)tid < cnt) {
             ff v[3];
-            const ImageRecF r = raw[buf * TILE + tid];
+            const ImageRecF r = raw[tid];
             atom_local(r, org, v);
-            cxy[tid] = make_ulonglong2(f2_pack(v[0].hi, v[0].hi), f2_pack(v[1].hi, v[1].hi));
-            czt[tid] = make_ulonglong2(f2_pack(v[2].hi, v[2].hi), (unsigned long long)r.type);
+            cxy_t[tid] = make_ulonglong2(f2_pack(v[0].hi, v[0].hi), f2_pack(v[1].hi, v[1].hi));
+            czt_t[tid] = make_ulonglong2(f2_pack(v[2].hi, v[2].hi), (unsigned long long)r.type);
             // this atom's class for each warp (2 bits per warp): 0 beyond the
             // warp's reach, 1 inner, 2 boundary, 3 near
             uint32_t m = 0;
@@ -851,14 +846,20 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
                 const uint32_t cls = d2w > c.w ? 0u : d2w < lim.x ? 3u : d2w <= lim.y ? 1u : 2u;
                 m |= cls << (2 * w);
             }
-            amask[tid] = (uint16_t)m;
+            amask_t[tid] = (uint16_t)m;
         }
-        __syncthreads();
-        // raw[buf] is free again: prefetch tile t + 2 while computing
-        if (tid == 0 && t + 2 < n_tiles) {
+        // block-wide vote so that every thread takes the same path on a timeout
+        if (!__syncthreads_and(got)) {
+            if (tid == 0)  // the timed-out tile is the only one in flight
+                for (unsigned it = 0; it < WAIT_LIMIT && !mbar_try_wait(&bars[0], (T0 + t) & 1); ++it)
+                    __nanosleep(64);
+            __syncthreads();
+            return false;
+        }
+        // the staging buffer is free again: stage tile t + 1 while computing
+        if (tid == 0 && t + 1 < n_tiles) {
             fence_proxy_async();
-            issue_tile(t + 2, n_cand, nr, row_begin, row_off, img,
-                       rawb + buf * TILE * sizeof(ImageRecF), &bars[buf]);
+            issue_tile(t + 1, n_cand, nr, row_begin, row_off, img, rawb, &bars[0]);
         }
         // this warp's atoms: inner ones from the front of its list (tile
         // order), the others from the back; the shift sum over both (every
@@ -873,14 +874,14 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
             for (int g = 0; g < NG; ++g) shift_sum[g] = 0.f;
             for (uint32_t c0 = 0; c0 < cnt; c0 += 32) {
                 const uint32_t j = c0 + lane;
-                const uint32_t cls = j < cnt ? (amask[j] >> (2 * w)) & 3u : 0u;
+                const uint32_t cls = j < cnt ? (amask_t[j] >> (2 * w)) & 3u : 0u;
                 const uint32_t b_in = __ballot_sync(0xffffffffu, cls == 1u);
                 const uint32_t b_out = __ballot_sync(0xffffffffu, cls >= 2u);
                 if (cls == 1u) mine_list[n_in + __popc(b_in & lt)] = (uint16_t)j;
                 if (cls >= 2u)
                     mine_list[TILE - 1 - (n_out + __popc(b_out & lt))] = (uint16_t)((j << 1) | (cls & 1u));
                 if (TRUNC != ALEA_TRUNCATED && cls) {
-                    const int type = (int)(uint32_t)czt[j].y;
+                    const int type = (int)(uint32_t)czt_t[j].y;
 #pragma unroll
                     for (int g = 0; g < NG; ++g) shift_sum[g] += P.shift[type * NG + g];
                 }
@@ -906,8 +907,8 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
         // sigma_t^2, HI: clamp (or cut) at the cutoff
         auto add_atom = [&](uint32_t j, auto lo_tag, auto hi_tag) {
             constexpr bool LO = decltype(lo_tag)::value, HI = decltype(hi_tag)::value;
-            const ulonglong2 xy = cxy[j];
-            const ulonglong2 zt = czt[j];
+            const ulonglong2 xy = cxy_t[j];
+            const ulonglong2 zt = czt_t[j];
             const int type = (int)(uint32_t)zt.y;
             float close2 = 0.f;
             if (LO) close2 = P.close2[type];
@@ -1011,7 +1012,6 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
                 acc_hi(g, 2 * q + 1) = sb.hi;
                 acc_lo(g, 2 * q + 1) = sb.lo;
             }
-        __syncthreads();  // the staged tile is rewritten by the next one
     }
     tiles = T0 + n_tiles;
 
@@ -1060,8 +1060,9 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     return true;
 }
 
+// 4 CTAs per SM fit in shared memory up to two guests, 3 beyond
 template <int NG, int TRUNC>
-__global__ void __launch_bounds__(THREADS, 4)
+__global__ void __launch_bounds__(THREADS, NG <= 2 ? 4 : 3)
 grid_build_f32_kernel(GridGeom geo, F32GridArgs args, unsigned long long* __restrict__ executed,
                       unsigned* flags) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1078,12 +1079,12 @@ grid_build_f32_kernel(GridGeom geo, F32GridArgs args, unsigned long long* __rest
 
 template <int NG, int TRUNC>
 constexpr size_t f32_smem_bytes() {
-    return carve(2 * TILE * sizeof(ImageRecF)) + carve(TILE * sizeof(ulonglong2)) +
-           carve(TILE * sizeof(ulonglong2)) + carve(MAX_ROWS * sizeof(uint32_t)) +
+    return carve(TILE * sizeof(ImageRecF)) + carve(2 * TILE * sizeof(ulonglong2)) +
+           carve(2 * TILE * sizeof(ulonglong2)) + carve(MAX_ROWS * sizeof(uint32_t)) +
            carve((MAX_ROWS + 1) * sizeof(uint32_t)) + carve((THREADS / 32) * sizeof(uint32_t)) +
            carve(sizeof(F32Params<NG, TRUNC>)) + carve(2 * NG * NPT * THREADS * sizeof(float)) +
            carve((THREADS / 32) * sizeof(float4)) + carve((THREADS / 32) * sizeof(float2)) +
-           carve(TILE * sizeof(uint16_t)) + carve((THREADS / 32) * TILE * sizeof(uint16_t));
+           carve(2 * TILE * sizeof(uint16_t)) + carve((THREADS / 32) * TILE * sizeof(uint16_t));
 }
 
 // ---------------------------------------------------------------- FP32 close-pair correction
