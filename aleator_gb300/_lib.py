@@ -75,7 +75,6 @@ class _GridStats(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_uint64), ("algorithmic_pairs", ctypes.c_uint64),
                 ("executed_pairs", ctypes.c_uint64), ("images", ctypes.c_uint64),
                 ("bricks", ctypes.c_uint64), ("last_kernel_ms", ctypes.c_float),
-                ("last_sweep_ms", ctypes.c_float), ("last_fix_ms", ctypes.c_float),
                 ("launches", ctypes.c_uint32)]
 
 

@@ -640,17 +640,20 @@ __device__ __forceinline__ float r2_f32(float ax, float ay, float az, float nx, 
 // force shift) included, minus what the sweep adds for it (vclose) and plus
 // the -V(rc) the sweep charges every pair: the correction that turns the
 // sweep's value for this pair into the exact one.
+// 4 eps ((sigma^2/r^2)^6 - (sigma^2/r^2)^3) in double-float, from r^2.
+__device__ __forceinline__ ff pair_ff(const ParamFF& q, ff rr) {
+    const ff s2 = ff_mul(ff{q.sig2_hi, q.sig2_lo}, ff_rcp(rr));
+    const ff s6 = ff_mul(ff_mul(s2, s2), s2);
+    return ff_mul(ff{q.eps4_hi, q.eps4_lo}, ff_mul(s6, ff_add(s6, ff{-1.f, 0.f})));
+}
+
 template <int NG, int TRUNC>
 __device__ __forceinline__ ff close_pair(const F32Params<NG, TRUNC>& P, const ParamFF* pff, int type, int g, ff ddx,
                                          ff ddy, ff ddz, float rcf) {
     ff rr = ff_add(ff_add(ff_mul(ddx, ddx), ff_mul(ddy, ddy)), ff_mul(ddz, ddz));
     if (rr.hi < 1e-4f) rr = ff{1e-4f, 0.f};
-    const ff iv = ff_rcp(rr);
     const ParamFF q = pff[type * NG + g];
-    const ff s2 = ff_mul(ff{q.sig2_hi, q.sig2_lo}, iv);
-    const ff s6 = ff_mul(ff_mul(s2, s2), s2);
-    const ff tt = ff_mul(s6, ff_add(s6, ff{-1.f, 0.f}));
-    ff e = ff_add(ff_mul(ff{q.eps4_hi, q.eps4_lo}, tt), ff{-q.shift_hi, -q.shift_lo});
+    ff e = ff_add(pair_ff(q, rr), ff{-q.shift_hi, -q.shift_lo});
     if (TRUNC == ALEA_LINEAR_FORCE_SHIFTED) {
         const float rs = sqrtf(rr.hi);
         e = ff_add(e, ff{-(rs - rcf) * q.dvdrc, 0.f});
@@ -666,6 +669,14 @@ __device__ __forceinline__ ff close_pair(const F32Params<NG, TRUNC>& P, const Pa
 // nodes exceed the ratio: nodes near 0 K with a few strongly repulsive pairs.)
 constexpr float CLOSE_FP32_RATIO = 2.0f;
 constexpr float CLOSE_FP32_FLOOR = 300.0f;  // K
+
+// Plain truncation: V jumps by V(rc) at the cutoff, so a pair whose FP32 r^2
+// lies within this fraction of rc^2 may be on the wrong side of it (the FP32
+// r^2 of brick-centred positions is off by ~1e-4 A^2 at most, 6e-7 of rc^2
+// for rc = 12.8 A); the node goes to the correction, which redoes those
+// pairs' decisions in double-float.
+constexpr float CUT_AMBIGUITY = 4e-6f;
+constexpr uint32_t FIX_AT_CUTOFF = 0x80;  // flag-mask bit: pairs at rc to redo
 
 // ---------------------------------------------------------------- FP32 sweep kernel
 // Pair terms in FP32 on brick-centred coordinates, double-float where a
@@ -689,7 +700,8 @@ constexpr float CLOSE_FP32_FLOOR = 300.0f;  // K
 // Per node and guest the result is then: the sweep's sum when there is no
 // close pair; the cap when sum + estimate exceeds it by 1%; sum + estimate
 // when the estimate is small against max(300 K, |E|); otherwise the sweep's
-// sum is stored and the node flagged for grid_close_fix_kernel.
+// sum is stored and the node's close pairs redone in double-float at the end
+// of the brick (fix_flagged).
 // With plain truncation a pair beyond rc gets r^-2 = 0 instead (no shift).
 // Linear force shifting adds -(r - rc) V'(rc) per pair at the clamped r.
 // Pointers of one grid for the FP32 kernels.
@@ -697,10 +709,258 @@ struct F32GridArgs {
     const ImageRecF* images;
     const uint32_t* bin_start;
     const ParamAB* pab;  // [guest of this launch][type]
-    const ParamFF* pff;
+    const ParamFF* pff;  // [guest of this launch][type]
     double* tables;
-    uint8_t* fix;
 };
+
+// ---------------------------------------------------------------- FP32 close-pair correction
+// For the nodes the sweep flagged: the pairs closer than sigma_t, exactly as
+// the sweep classified them, evaluated in double-float; their correction is
+// added to the stored sweep sum and the cap applied. It runs at the end of
+// the flagged node's brick, in the sweep's CTA and shared memory (its stalls
+// are covered by the other CTAs on the SM, which are sweeping). The images
+// that can be that close to one of the brick's nodes are gathered and
+// converted into shared memory (in windows, in a fixed order); each flagged
+// node has a thread that walks them and evaluates its close pairs.
+constexpr int NEAR_CHUNK = 512;
+
+template <int NG>
+__host__ __device__ constexpr size_t fix_buf_bytes() {
+    return 2 * carve(NEAR_CHUNK * sizeof(float4)) + carve(THREADS * NPT * sizeof(uint16_t)) +
+           carve(THREADS * NPT * sizeof(uint8_t));
+}
+
+// gm[k]: this thread's node k, bit g set when guest g is flagged. fbuf and
+// pff are shared memory free at this point; row_begin, row_off and warp_tot
+// are the sweep's (free after its tile loop). Every thread of the CTA calls it.
+template <int NG, int TRUNC>
+__device__ __forceinline__ void fix_flagged(const GridGeom& geo, const F32GridArgs& A,
+                                            const F32Params<NG, TRUNC>& P, const ff (&org)[3],
+                                            int x0, int y0, int z0, const uint32_t (&gm)[NPT],
+                                            unsigned char* fbuf, ParamFF* pff, uint32_t* row_begin,
+                                            uint32_t* row_off, uint32_t* warp_tot, unsigned* flags) {
+    SmemCarve sc{fbuf};
+    float4* ahi = sc.take<float4>(NEAR_CHUNK);  // x, y, z hi, type
+    float4* alo = sc.take<float4>(NEAR_CHUNK);  // x, y, z lo
+    uint16_t* fnode = sc.take<uint16_t>(THREADS * NPT);  // (thread << 2) | k
+    uint8_t* fmask = sc.take<uint8_t>(THREADS * NPT);    // flagged guests
+    static_assert(NPT == 4 && NG <= 7, "node and guest bits (bit 7: FIX_AT_CUTOFF)");
+    const ImageRecF* __restrict__ images = A.images;
+    double* __restrict__ tables = A.tables;
+    const int tid = threadIdx.x;
+    const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
+    const size_t plane = (size_t)nx * ny;
+    const size_t per_table = plane * nz;
+
+    uint32_t cnt_nodes = 0;
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) cnt_nodes += gm[k] != 0;
+    if (!__syncthreads_or(cnt_nodes != 0)) return;  // (every thread: a uniform vote)
+
+    // compact the flagged nodes: exclusive scan of the per-thread counts
+    uint32_t n_fn;
+    {
+        const int lane = tid & 31, wid = tid >> 5;
+        uint32_t incl = cnt_nodes;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) warp_tot[wid] = incl;
+        __syncthreads();
+        uint32_t base = 0;
+        n_fn = 0;
+        for (int w = 0; w < THREADS / 32; ++w) {
+            if (w < wid) base += warp_tot[w];
+            n_fn += warp_tot[w];
+        }
+        uint32_t off = base + incl - cnt_nodes;
+#pragma unroll
+        for (int k = 0; k < NPT; ++k)
+            if (gm[k]) {
+                fnode[off] = (uint16_t)((tid << 2) | k);
+                fmask[off] = (uint8_t)gm[k];
+                ++off;
+            }
+    }
+    for (int i = tid; i < geo.n_types * NG; i += THREADS)
+        pff[i] = A.pff[(size_t)(i % NG) * geo.n_types + i / NG];
+    float rb2 = 0.f;  // the brick's bounding radius about its centre, squared
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const float d0 = (c & 1 ? 0.5f : -0.5f) * (BX - 1), d1 = (c & 2 ? 0.5f : -0.5f) * (BY - 1),
+                    d2 = (c & 4 ? 0.5f : -0.5f) * (BZ - 1);
+        float q2 = 0.f;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float w = d0 * geo.sh[a] + d1 * geo.sh[3 + a] + d2 * geo.sh[6 + a];
+            q2 = fmaf(w, w, q2);
+        }
+        rb2 = fmaxf(rb2, q2);
+    }
+    const float rb = sqrtf(rb2) + 1e-3f;  // 1e-3 A of margin for the FP32 tests below
+    const float4* __restrict__ img4 = reinterpret_cast<const float4*>(images);  // 2 per record
+    const int lane = tid & 31, wid = tid >> 5;
+
+    // Gathers the images of rows [0, nr) that pass keep(|p|^2, type) (p: the
+    // image from the brick centre, from the hi parts, off by ~1e-5 A at
+    // most) into ahi / alo and calls use(count) per window of NEAR_CHUNK.
+    // Warp w scans rows w, w + 8, ...: a count pass, then a pass that writes
+    // each warp's images after the earlier warps' (a fixed order).
+    auto gather = [&](int nr, auto keep, auto use) {
+        auto passes = [&](uint32_t rec) -> bool {
+            const float4 h = img4[2 * (size_t)rec];  // xh, yh, zh, type
+            const float px = h.x - org[0].hi, py = h.y - org[1].hi, pz = h.z - org[2].hi;
+            return keep(fmaf(px, px, fmaf(py, py, pz * pz)), __float_as_int(h.w));
+        };
+        uint32_t mine = 0;
+        for (int r = wid; r < nr; r += THREADS / 32) {
+            const uint32_t beg = row_begin[r], len = row_off[r + 1] - row_off[r];
+            for (uint32_t i0 = 0; i0 < len; i0 += 32) {
+                const bool k = i0 + lane < len && passes(beg + i0 + lane);
+                mine += __popc(__ballot_sync(0xffffffffu, k));
+            }
+        }
+        __syncthreads();  // earlier reads of warp_tot
+        if (lane == 0) warp_tot[wid] = mine;
+        __syncthreads();
+        uint32_t base = 0, n_cand = 0;
+        for (int w = 0; w < THREADS / 32; ++w) {
+            if (w < wid) base += warp_tot[w];
+            n_cand += warp_tot[w];
+        }
+        for (uint32_t c0 = 0; c0 < n_cand; c0 += NEAR_CHUNK) {
+            const uint32_t cnt = min((uint32_t)NEAR_CHUNK, n_cand - c0);
+            if (base < c0 + cnt && base + mine > c0) {  // this warp has images in the window
+                uint32_t o = base;
+                for (int r = wid; r < nr && o < c0 + cnt; r += THREADS / 32) {
+                    const uint32_t beg = row_begin[r], len = row_off[r + 1] - row_off[r];
+                    for (uint32_t i0 = 0; i0 < len; i0 += 32) {
+                        const bool k = i0 + lane < len && passes(beg + i0 + lane);
+                        const uint32_t b = __ballot_sync(0xffffffffu, k);
+                        const uint32_t at = o + __popc(b & ((1u << lane) - 1u));
+                        if (k && at >= c0 && at < c0 + cnt) {
+                            const ImageRecF rr = images[beg + i0 + lane];
+                            ff v[3];
+                            atom_local(rr, org, v);
+                            ahi[at - c0] = make_float4(v[0].hi, v[1].hi, v[2].hi, __int_as_float((int)rr.type));
+                            alo[at - c0] = make_float4(v[0].lo, v[1].lo, v[2].lo, 0.f);
+                        }
+                        o += __popc(b);
+                    }
+                }
+            }
+            __syncthreads();
+            use(cnt);
+            __syncthreads();
+        }
+    };
+    // a thread per flagged node (whose mask has any of the bits `need`):
+    // body(node position, image, its lo part, guest mask, acc) per image of
+    // the window, then the sums added to the node's table entries
+    auto per_node = [&](uint32_t cnt, uint32_t need, auto body) {
+        for (uint32_t f = tid; f < n_fn; f += THREADS) {
+            const uint32_t gmask = fmask[f];
+            if (!(gmask & need)) continue;
+            const uint32_t node = fnode[f];
+            int jx, jy, jz0;
+            thread_nodes((int)(node >> 2), jx, jy, jz0);
+            const int jz = jz0 + (int)(node & 3);
+            ff v[3];
+            node_local(geo, jx - 0.5f * (BX - 1), jy - 0.5f * (BY - 1), jz - 0.5f * (BZ - 1), v);
+            ff acc[NG];
+#pragma unroll
+            for (int g = 0; g < NG; ++g) acc[g] = ff{0.f, 0.f};
+            for (uint32_t i = 0; i < cnt; ++i) body(v, ahi[i], i, gmask, acc);
+            const size_t idx = (size_t)(z0 + jz) * plane + (size_t)(y0 + jy) * nx + (x0 + jx);
+#pragma unroll
+            for (int g = 0; g < NG; ++g)
+                if (gmask & (1u << g))
+                    tables[(size_t)g * per_table + idx] += (double)acc[g].hi + (double)acc[g].lo;
+        }
+    };
+    auto delta = [&](const float4& a, uint32_t i, const ff (&v)[3], ff& ddx, ff& ddy, ff& ddz) {
+        const float4 l = alo[i];
+        ddx = ff_add(ff{a.x, l.x}, ff{-v[0].hi, -v[0].lo});
+        ddy = ff_add(ff{a.y, l.y}, ff{-v[1].hi, -v[1].lo});
+        ddz = ff_add(ff{a.z, l.z}, ff{-v[2].hi, -v[2].lo});
+    };
+
+    // 1. the close pairs: images within rb + sigma_t of the brick centre
+    // (plan_rows writes warp_tot only after a barrier of its own)
+    int nr = plan_rows(geo, geo.hf_near, geo.keep2_near, A.bin_start, x0, y0, z0, row_begin,
+                       row_off, warp_tot, flags);
+    if (nr < 0) return;
+    gather(
+        nr,
+        [&](float p2, int type) {
+            const float reach = rb + sqrtf(P.close2[type]);
+            return p2 < reach * reach;
+        },
+        [&](uint32_t cnt) {
+            per_node(cnt, (1u << NG) - 1u, [&](const ff (&v)[3], const float4& a, uint32_t i, uint32_t gmask, ff (&acc)[NG]) {
+                const int type = __float_as_int(a.w);
+                if (!(r2_f32(a.x, a.y, a.z, v[0].hi, v[1].hi, v[2].hi) < P.close2[type])) return;
+                ff ddx, ddy, ddz;
+                delta(a, i, v, ddx, ddy, ddz);
+#pragma unroll
+                for (int g = 0; g < NG; ++g)
+                    if (gmask & (1u << g))
+                        acc[g] = ff_add(acc[g], close_pair(P, pff, type, g, ddx, ddy, ddz, geo.rcf));
+            });
+        });
+
+    // 2. (plain truncation) the pairs at rc of the nodes that have one:
+    // images within rb of the cutoff sphere about the brick centre; a pair
+    // whose FP32 r^2 was near rc^2 gets its decision redone on the
+    // double-float r^2, and where the sweep's differs its V is added or
+    // taken back
+    if (TRUNC == ALEA_TRUNCATED) {
+        uint32_t at_cut = 0;
+        for (uint32_t f = tid; f < n_fn; f += THREADS) at_cut |= fmask[f] & FIX_AT_CUTOFF;
+        if (__syncthreads_or(at_cut != 0)) {
+            nr = plan_rows(geo, geo.hf, geo.keep2f, A.bin_start, x0, y0, z0, row_begin, row_off,
+                           warp_tot, flags);
+            if (nr < 0) return;
+            const float inner = fmaxf(geo.rcf - rb, 0.f), outer = geo.rcf + rb;
+            const float amb2 = CUT_AMBIGUITY * geo.rc2f;
+            gather(
+                nr, [&](float p2, int) { return p2 > inner * inner && p2 < outer * outer; },
+                [&](uint32_t cnt) {
+                    per_node(cnt, FIX_AT_CUTOFF, [&](const ff (&v)[3], const float4& a, uint32_t i, uint32_t gmask, ff (&acc)[NG]) {
+                        const float r2 = r2_f32(a.x, a.y, a.z, v[0].hi, v[1].hi, v[2].hi);
+                        if (!(fabsf(r2 - geo.rc2f) <= amb2)) return;
+                        ff ddx, ddy, ddz;
+                        delta(a, i, v, ddx, ddy, ddz);
+                        const ff rr = ff_add(ff_add(ff_mul(ddx, ddx), ff_mul(ddy, ddy)), ff_mul(ddz, ddz));
+                        const bool in_exact = (double)rr.hi + (double)rr.lo <= geo.rc2;
+                        const bool in_sweep = !(r2 > geo.rc2f);
+                        if (in_exact == in_sweep) return;
+                        const int type = __float_as_int(a.w);
+#pragma unroll
+                        for (int g = 0; g < NG; ++g)
+                            if (gmask & (1u << g)) {
+                                const ff e = pair_ff(pff[type * NG + g], rr);
+                                acc[g] = ff_add(acc[g], in_exact ? e : ff{-e.hi, -e.lo});
+                            }
+                    });
+                });
+        }
+    }
+    // the cap, once every chunk's correction is in (the sweep wrote these
+    // nodes' sums, uncapped, before the CTA's barriers)
+    for (uint32_t jb = tid; jb < n_fn * NG; jb += THREADS) {
+        const uint32_t f = jb / NG;
+        const int g = (int)(jb % NG);
+        if (!(fmask[f] & (1u << g))) continue;
+        const uint32_t node = fnode[f];
+        int jx, jy, jz0;
+        thread_nodes((int)(node >> 2), jx, jy, jz0);
+        const size_t idx = (size_t)(z0 + jz0 + (node & 3)) * plane + (size_t)(y0 + jy) * nx + (x0 + jx);
+        double& e = tables[(size_t)g * per_table + idx];
+        if (kEnergyCap < e) e = kEnergyCap;
+    }
+}
 
 // One brick of the sweep (the body of the sweep kernels). `tiles` counts the
 // tiles this CTA has staged so far: the two mbarriers alternate by it, so
@@ -729,7 +989,6 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     const ImageRecF* __restrict__ images = A.images;
     const uint32_t* __restrict__ bin_start = A.bin_start;
     double* __restrict__ tables = A.tables;
-    uint8_t* __restrict__ fix = A.fix;
 
     const int tid = threadIdx.x;
     const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
@@ -801,7 +1060,8 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     }
 
     float ce[NG][NPT];               // FP32 close-pair estimates
-    uint32_t has_close = 0;          // bit k: node k has a close pair
+    uint32_t has_close = 0;  // bit k: node k has a close pair; bit NPT + k: a pair at rc (truncated)
+    const float amb2 = CUT_AMBIGUITY * geo.rc2f;
 #pragma unroll
     for (int g = 0; g < NG; ++g)
 #pragma unroll
@@ -959,6 +1219,10 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
                     if (HI) {
                         ia = r2a > rc2f ? 0.f : ia;
                         ib = r2b > rc2f ? 0.f : ib;
+                        // V jumps at rc: a pair this near it may lie on the
+                        // other side in exact arithmetic (node to correction)
+                        if (fabsf(r2a - rc2f) <= amb2) has_close |= 1u << (NPT + 2 * q);
+                        if (fabsf(r2b - rc2f) <= amb2) has_close |= 1u << (NPT + 2 * q + 1);
                     }
                 } else {
                     if (LO) {
@@ -1021,8 +1285,10 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     const size_t plane = (size_t)nx * ny;
     const size_t per_table = plane * nz;
     uint32_t mine = 0;
+    uint32_t gm[NPT];  // per node: guests flagged for the correction
 #pragma unroll
     for (int k = 0; k < NPT; ++k) {
+        gm[k] = 0;
         const int izn = z0 + tz0 + k;
         if (ixn < nx && iyn < ny && izn < nz) {
             const size_t idx = (size_t)izn * plane + (size_t)iyn * nx + ixn;
@@ -1030,18 +1296,24 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
             for (int g = 0; g < NG; ++g) {
                 const double e = (double)acc_hi(g, k) + (double)acc_lo(g, k);
                 double out = e;
-                uint8_t f = 0;
+                bool f = false;
+                // (truncated) a pair at rc: the correction redoes its cutoff
+                // decision, and the node's close pairs with it
+                const bool amb = TRUNC == ALEA_TRUNCATED && ((has_close >> (NPT + k)) & 1u);
                 if (has_close & (1u << k)) {
                     const double est = e + (double)ce[g][k];
                     if (est > 1.01 * kEnergyCap)
                         out = kEnergyCap;
-                    else if (fabsf(ce[g][k]) <= CLOSE_FP32_RATIO * fmaxf(CLOSE_FP32_FLOOR, (float)fabs(est)))
+                    else if (!amb && fabsf(ce[g][k]) <= CLOSE_FP32_RATIO * fmaxf(CLOSE_FP32_FLOOR, (float)fabs(est)))
                         out = est;
                     else
-                        f = 1;
+                        f = true;
+                } else {
+                    f = amb;
                 }
                 tables[(size_t)g * per_table + idx] = (!f && kEnergyCap < out) ? kEnergyCap : out;
-                fix[(size_t)g * per_table + idx] = f;
+                gm[k] |= (uint32_t)f << g;
+                if (f && amb) gm[k] |= FIX_AT_CUTOFF;
             }
             mine += passes;
         }
@@ -1056,6 +1328,15 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
         for (int w = 0; w < THREADS / 32; ++w) sum += warp_tot[w];
         atomicAdd(executed, sum);
     }
+    // the flagged nodes' close pairs; the staging and converted-tile buffers
+    // and the accumulators are free now (the vote in fix_flagged is the
+    // barrier after the last reads of warp_tot and the accumulators)
+    static_assert(fix_buf_bytes<NG>() <= carve(TILE * sizeof(ImageRecF)) + 2 * carve(2 * TILE * sizeof(ulonglong2)),
+                  "correction buffers fit the tile buffers");
+    static_assert(64 * NG * sizeof(ParamFF) <= 2 * NG * NPT * THREADS * sizeof(float),
+                  "double-float parameters fit the accumulators");
+    fix_flagged<NG, TRUNC>(geo, A, P, org, x0, y0, z0, gm, smem, reinterpret_cast<ParamFF*>(accs),
+                           row_begin, row_off, warp_tot, flags);
     __syncthreads();  // shared memory is reused by the next brick
     return true;
 }
@@ -1085,201 +1366,6 @@ constexpr size_t f32_smem_bytes() {
            carve(sizeof(F32Params<NG, TRUNC>)) + carve(2 * NG * NPT * THREADS * sizeof(float)) +
            carve((THREADS / 32) * sizeof(float4)) + carve((THREADS / 32) * sizeof(float2)) +
            carve(2 * TILE * sizeof(uint16_t)) + carve((THREADS / 32) * TILE * sizeof(uint16_t));
-}
-
-// ---------------------------------------------------------------- FP32 close-pair correction
-// For the nodes the sweep flagged: the pairs closer than sigma_t, exactly as
-// the sweep classified them, evaluated in double-float; their correction is
-// added to the stored sweep sum and the cap applied. One CTA per brick; a
-// brick without flagged nodes returns after reading its flags. The images
-// within reach (smax of the brick's nodes) are converted once into shared
-// memory, in chunks. Per chunk, phase A gives each flagged node a thread that
-// lists the node's close images (a uniform scan); phase B gives each flagged
-// (node, guest) a thread that evaluates just those pairs, so the expensive
-// double-float work runs without divergence.
-constexpr int NEAR_CHUNK = 512;
-constexpr int MAX_CLOSE = 16;  // listed close images per node and chunk
-
-// One brick of the close-pair correction (the body of the correction kernels).
-template <int NG, int TRUNC>
-__device__ __forceinline__ void fix_brick(const GridGeom& geo, const F32GridArgs& A, int brick,
-                                          unsigned char* smem, unsigned* flags) {
-    const ImageRecF* __restrict__ images = A.images;
-    const uint32_t* __restrict__ bin_start = A.bin_start;
-    const uint8_t* __restrict__ fix = A.fix;
-    double* __restrict__ tables = A.tables;
-    SmemCarve sc{smem};
-    float4* ahi = sc.take<float4>(NEAR_CHUNK);  // x, y, z hi, type
-    float4* alo = sc.take<float4>(NEAR_CHUNK);  // x, y, z lo
-    uint32_t* row_begin = sc.take<uint32_t>(MAX_ROWS);
-    uint32_t* row_off = sc.take<uint32_t>(MAX_ROWS + 1);
-    uint32_t* warp_tot = sc.take<uint32_t>(THREADS / 32);
-    uint16_t* fnode = sc.take<uint16_t>(THREADS * NPT);       // (thread << 2) | k
-    uint8_t* fmask = sc.take<uint8_t>(THREADS * NPT);         // flagged guests
-    float4* fpos = sc.take<float4>(2 * THREADS * NPT);        // node hi, lo
-    uint16_t* clist = sc.take<uint16_t>(THREADS * NPT * MAX_CLOSE);
-    uint16_t* ccount = sc.take<uint16_t>(THREADS * NPT);
-    F32Params<NG, TRUNC>& P = *sc.take<F32Params<NG, TRUNC>>(1);
-    ParamFF* pff = sc.take<ParamFF>(64 * NG);  // [type][guest], double-float
-    static_assert(NPT == 4 && NG <= 8, "node and guest bits");
-
-    const int tid = threadIdx.x;
-    const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
-    const int bxn = geo.bricks[0], byn = geo.bricks[1];
-    const int bx = brick % bxn, by = (brick / bxn) % byn, bz = brick / (bxn * byn);
-    const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
-    const size_t plane = (size_t)nx * ny;
-    const size_t per_table = plane * nz;
-
-    int tx, ty, tz0;
-    thread_nodes(tid, tx, ty, tz0);
-    uint32_t gm[NPT];
-    uint32_t cnt_nodes = 0;
-#pragma unroll
-    for (int k = 0; k < NPT; ++k) {
-        gm[k] = 0;
-        const int ixn = x0 + tx, iyn = y0 + ty, izn = z0 + tz0 + k;
-        if (ixn < nx && iyn < ny && izn < nz) {
-            const size_t idx = (size_t)izn * plane + (size_t)iyn * nx + ixn;
-#pragma unroll
-            for (int g = 0; g < NG; ++g)
-                if (fix[(size_t)g * per_table + idx]) gm[k] |= 1u << g;
-        }
-        cnt_nodes += gm[k] != 0;
-    }
-    if (!__syncthreads_or(cnt_nodes != 0)) return;  // (every thread: a uniform vote)
-
-    // compact the flagged nodes: exclusive scan of the per-thread counts
-    uint32_t n_fn;
-    {
-        const int lane = tid & 31, wid = tid >> 5;
-        uint32_t incl = cnt_nodes;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        if (lane == 31) warp_tot[wid] = incl;
-        __syncthreads();
-        uint32_t base = 0;
-        n_fn = 0;
-        for (int w = 0; w < THREADS / 32; ++w) {
-            if (w < wid) base += warp_tot[w];
-            n_fn += warp_tot[w];
-        }
-        uint32_t off = base + incl - cnt_nodes;
-#pragma unroll
-        for (int k = 0; k < NPT; ++k)
-            if (gm[k]) {
-                fnode[off] = (uint16_t)((tid << 2) | k);
-                fmask[off] = (uint8_t)gm[k];
-                ff v[3];
-                node_local(geo, tx - 0.5f * (BX - 1), ty - 0.5f * (BY - 1), tz0 + k - 0.5f * (BZ - 1), v);
-                fpos[2 * off] = make_float4(v[0].hi, v[1].hi, v[2].hi, 0.f);
-                fpos[2 * off + 1] = make_float4(v[0].lo, v[1].lo, v[2].lo, 0.f);
-                ++off;
-            }
-    }
-    for (int i = tid; i < geo.n_types * NG; i += THREADS)
-        pff[i] = A.pff[(size_t)(i % NG) * geo.n_types + i / NG];
-    load_f32_params(P, A.pab, A.pff, geo.n_types, geo.rcf);  // synchronises
-    const int nr = plan_rows(geo, geo.hf_near, geo.keep2_near, bin_start, x0, y0, z0, row_begin,
-                             row_off, warp_tot, flags);
-    if (nr < 0) return;
-    const uint32_t n_near = row_off[nr];
-    ff org[3];
-    brick_origin(geo, x0, y0, z0, org);
-
-    for (uint32_t c0 = 0; c0 < n_near; c0 += NEAR_CHUNK) {
-        const uint32_t cnt = min((uint32_t)NEAR_CHUNK, n_near - c0);
-        for (uint32_t i = tid; i < cnt; i += THREADS) {
-            const uint32_t q = c0 + i;
-            int lo = 0, hi = nr - 1;  // last row with row_off[r] <= q
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) / 2;
-                if (row_off[mid] <= q) lo = mid; else hi = mid - 1;
-            }
-            const ImageRecF r = images[row_begin[lo] + (q - row_off[lo])];
-            ff v[3];
-            atom_local(r, org, v);
-            ahi[i] = make_float4(v[0].hi, v[1].hi, v[2].hi, __int_as_float((int)r.type));
-            alo[i] = make_float4(v[0].lo, v[1].lo, v[2].lo, 0.f);
-        }
-        __syncthreads();
-        // phase A: each flagged node lists its close images in this chunk
-        for (uint32_t f = tid; f < n_fn; f += THREADS) {
-            const float4 p = fpos[2 * f];
-            uint32_t c = 0;
-            for (uint32_t i = 0; i < cnt; ++i) {
-                const float4 a = ahi[i];
-                if (r2_f32(a.x, a.y, a.z, p.x, p.y, p.z) < P.close2[__float_as_int(a.w)]) {
-                    if (c < MAX_CLOSE) clist[f * MAX_CLOSE + c] = (uint16_t)i;
-                    ++c;
-                }
-            }
-            ccount[f] = (uint16_t)min(c, 65535u);
-        }
-        __syncthreads();
-        // phase B: each flagged (node, guest) sums its close pairs
-        for (uint32_t jb = tid; jb < n_fn * NG; jb += THREADS) {
-            const uint32_t f = jb / NG;
-            const int g = (int)(jb % NG);
-            if (!(fmask[f] & (1u << g))) continue;
-            const float4 p = fpos[2 * f], pl = fpos[2 * f + 1];
-            const uint32_t c = ccount[f];
-            ff acc{0.f, 0.f};
-            // more close images than slots: scan the chunk again (rare)
-            const uint32_t n_it = c <= MAX_CLOSE ? c : cnt;
-            for (uint32_t u = 0; u < n_it; ++u) {
-                const uint32_t i = c <= MAX_CLOSE ? clist[f * MAX_CLOSE + u] : u;
-                const float4 a = ahi[i];
-                const int type = __float_as_int(a.w);
-                if (c > MAX_CLOSE && !(r2_f32(a.x, a.y, a.z, p.x, p.y, p.z) < P.close2[type])) continue;
-                const float4 l = alo[i];
-                const ff ddx = ff_add(ff{a.x, l.x}, ff{-p.x, -pl.x});
-                const ff ddy = ff_add(ff{a.y, l.y}, ff{-p.y, -pl.y});
-                const ff ddz = ff_add(ff{a.z, l.z}, ff{-p.z, -pl.z});
-                acc = ff_add(acc, close_pair(P, pff, type, g, ddx, ddy, ddz, geo.rcf));
-            }
-            if (c) {
-                const uint32_t node = fnode[f];
-                int jx, jy, jz0;
-                thread_nodes((int)(node >> 2), jx, jy, jz0);
-                const size_t idx = (size_t)(z0 + jz0 + (node & 3)) * plane + (size_t)(y0 + jy) * nx + (x0 + jx);
-                tables[(size_t)g * per_table + idx] += (double)acc.hi + (double)acc.lo;
-            }
-        }
-        __syncthreads();
-    }
-    for (uint32_t jb = tid; jb < n_fn * NG; jb += THREADS) {
-        const uint32_t f = jb / NG;
-        const int g = (int)(jb % NG);
-        if (!(fmask[f] & (1u << g))) continue;
-        const uint32_t node = fnode[f];
-        int jx, jy, jz0;
-        thread_nodes((int)(node >> 2), jx, jy, jz0);
-        const size_t idx = (size_t)(z0 + jz0 + (node & 3)) * plane + (size_t)(y0 + jy) * nx + (x0 + jx);
-        double& e = tables[(size_t)g * per_table + idx];
-        if (kEnergyCap < e) e = kEnergyCap;
-    }
-    __syncthreads();  // shared memory is reused by the next brick
-}
-
-template <int NG, int TRUNC>
-__global__ void __launch_bounds__(THREADS)
-grid_close_fix_kernel(GridGeom geo, F32GridArgs args, unsigned* flags) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    fix_brick<NG, TRUNC>(geo, args, (int)blockIdx.x, smem, flags);
-}
-
-template <int NG, int TRUNC>
-constexpr size_t fix_smem_bytes() {
-    return 2 * carve(NEAR_CHUNK * sizeof(float4)) + carve(MAX_ROWS * sizeof(uint32_t)) +
-           carve((MAX_ROWS + 1) * sizeof(uint32_t)) + carve((THREADS / 32) * sizeof(uint32_t)) +
-           carve(THREADS * NPT * sizeof(uint16_t)) + carve(THREADS * NPT * sizeof(uint8_t)) +
-           carve(2 * THREADS * NPT * sizeof(float4)) +
-           carve(THREADS * NPT * MAX_CLOSE * sizeof(uint16_t)) +
-           carve(THREADS * NPT * sizeof(uint16_t)) + carve(sizeof(F32Params<NG, TRUNC>)) +
-           carve(64 * NG * sizeof(ParamFF));
 }
 
 // ---------------------------------------------------------------- batched FP32 build
@@ -1347,22 +1433,6 @@ grid_build_f32_batch_kernel(const BatchItem* __restrict__ items, int n_items, ui
     }
 }
 
-template <int NG, int TRUNC>
-__global__ void __launch_bounds__(THREADS)
-grid_close_fix_batch_kernel(const BatchItem* __restrict__ items, int n_items, uint64_t total,
-                            unsigned long long* next, unsigned* flags) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ unsigned long long work;
-    __shared__ int item;
-    GridGeom& geo = *reinterpret_cast<GridGeom*>(smem);
-    unsigned char* body = smem + carve(sizeof(GridGeom));
-    while (next_item(items, n_items, total, next, work, item, geo)) {
-        const BatchItem& it = items[item];
-        fix_brick<NG, TRUNC>(geo, it.args, (int)(work - it.brick0), body, flags);
-        __syncthreads();
-    }
-}
-
 // The batched launch shapes the autotuner chooses between.
 constexpr int BATCH_VARIANTS = 2;  // 0: 3 sweep blocks per SM, 1: 4
 
@@ -1371,23 +1441,14 @@ void batch_launch_t(int variant, int sms, cudaStream_t s, const BatchItem* items
                     uint64_t total, unsigned long long* counters, unsigned long long* executed,
                     unsigned* flags) {
     const size_t sb = carve(sizeof(GridGeom)) + f32_smem_bytes<NG, TRUNC>();
-    const size_t fb = carve(sizeof(GridGeom)) + fix_smem_bytes<NG, TRUNC>();
     auto sweep = variant == 0 ? grid_build_f32_batch_kernel<NG, TRUNC, 3>
                               : grid_build_f32_batch_kernel<NG, TRUNC, 4>;
     ALEA_CUDA(cudaFuncSetAttribute(sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-    ALEA_CUDA(cudaFuncSetAttribute(grid_close_fix_batch_kernel<NG, TRUNC>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fb));
-    int per_sm = 1, fix_per_sm = 1;
+    int per_sm = 1;
     ALEA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep, THREADS, sb));
-    ALEA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &fix_per_sm, grid_close_fix_batch_kernel<NG, TRUNC>, THREADS, fb));
     const unsigned gs = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(total, (uint64_t)sms * std::max(per_sm, 1)));
-    const unsigned gf = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(total, (uint64_t)sms * std::max(fix_per_sm, 1)));
     ALEA_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), s));
     sweep<<<gs, THREADS, sb, s>>>(items, n_items, total, counters, executed, flags);
-    ALEA_CUDA(cudaGetLastError());
-    grid_close_fix_batch_kernel<NG, TRUNC><<<gf, THREADS, fb, s>>>(items, n_items, total,
-                                                                     counters + 1, flags);
     ALEA_CUDA(cudaGetLastError());
 }
 
@@ -1460,29 +1521,20 @@ struct BuildArgs {
     const ParamAB* pab;          // FP32 form: [guest of this launch][type]
     const ParamFF* pff;
     double* tables;
-    uint8_t* fix;                // FP32 form: per node and guest, 1 = close-pair correction due
     unsigned long long* executed;
     unsigned* flags;
 };
 
-// phase 0: the sweep (or the FP64 kernel); phase 1: the FP32 close-pair correction
 template <int NG, int TRUNC>
-void launch_one(bool f32, int phase, dim3 grid, cudaStream_t s, const GridGeom& geo,
-                const BuildArgs& a) {
-    if (f32 && phase == 0) {
+void launch_one(bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo, const BuildArgs& a) {
+    if (f32) {
         constexpr size_t bytes = f32_smem_bytes<NG, TRUNC>();
         // opt in to more than 48 KB of dynamic shared memory (per device, cheap)
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f32_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-        const F32GridArgs fa{a.images_f, a.bins, a.pab, a.pff, a.tables, a.fix};
+        const F32GridArgs fa{a.images_f, a.bins, a.pab, a.pff, a.tables};
         grid_build_f32_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(geo, fa, a.executed, a.flags);
-    } else if (f32) {
-        constexpr size_t fbytes = fix_smem_bytes<NG, TRUNC>();
-        ALEA_CUDA(cudaFuncSetAttribute(grid_close_fix_kernel<NG, TRUNC>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fbytes));
-        const F32GridArgs fa{a.images_f, a.bins, a.pab, a.pff, a.tables, a.fix};
-        grid_close_fix_kernel<NG, TRUNC><<<grid, THREADS, fbytes, s>>>(geo, fa, a.flags);
-    } else if (phase == 0) {
+    } else {
         constexpr size_t bytes = f64_smem_bytes<NG>();
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f64_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -1492,23 +1544,23 @@ void launch_one(bool f32, int phase, dim3 grid, cudaStream_t s, const GridGeom& 
 }
 
 template <int NG>
-void launch_trunc(int trunc, bool f32, int phase, dim3 grid, cudaStream_t s, const GridGeom& geo,
+void launch_trunc(int trunc, bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo,
                   const BuildArgs& a) {
     if (trunc == ALEA_TRUNCATED)
-        launch_one<NG, ALEA_TRUNCATED>(f32, phase, grid, s, geo, a);
+        launch_one<NG, ALEA_TRUNCATED>(f32, grid, s, geo, a);
     else if (trunc == ALEA_SHIFTED)
-        launch_one<NG, ALEA_SHIFTED>(f32, phase, grid, s, geo, a);
+        launch_one<NG, ALEA_SHIFTED>(f32, grid, s, geo, a);
     else
-        launch_one<NG, ALEA_LINEAR_FORCE_SHIFTED>(f32, phase, grid, s, geo, a);
+        launch_one<NG, ALEA_LINEAR_FORCE_SHIFTED>(f32, grid, s, geo, a);
 }
 
-void launch_build(int ng, int trunc, bool f32, int phase, dim3 grid, cudaStream_t s,
-                  const GridGeom& geo, const BuildArgs& a) {
+void launch_build(int ng, int trunc, bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo,
+                  const BuildArgs& a) {
     switch (ng) {
-        case 1: launch_trunc<1>(trunc, f32, phase, grid, s, geo, a); break;
-        case 2: launch_trunc<2>(trunc, f32, phase, grid, s, geo, a); break;
-        case 3: launch_trunc<3>(trunc, f32, phase, grid, s, geo, a); break;
-        default: launch_trunc<4>(trunc, f32, phase, grid, s, geo, a); break;
+        case 1: launch_trunc<1>(trunc, f32, grid, s, geo, a); break;
+        case 2: launch_trunc<2>(trunc, f32, grid, s, geo, a); break;
+        case 3: launch_trunc<3>(trunc, f32, grid, s, geo, a); break;
+        default: launch_trunc<4>(trunc, f32, grid, s, geo, a); break;
     }
 }
 
@@ -1526,7 +1578,6 @@ struct GridImpl {
     DevBuf<ImageRecF> images_f;  // FP32 form
     DevBuf<ParamAB> pab;         // FP32 form, [guest][type]
     DevBuf<ParamFF> pff;
-    DevBuf<uint8_t> fix;         // FP32 form: close-pair correction flags, per guest and node
     DevBuf<uint32_t> bin_start;
     DevBuf<PairParams> params;
     DevBuf<uint32_t> guests;
@@ -1536,8 +1587,6 @@ struct GridImpl {
     uint64_t n_images = 0;
     uint64_t executed_pairs = 0;
     float last_ms = 0.f;
-    float last_sweep_ms = 0.f;   // the FP32 sweep, or the FP64 kernel
-    float last_fix_ms = 0.f;     // the FP32 close-pair correction
     int launches = 0;
 };
 
@@ -1737,7 +1786,6 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
     g.guests.upload(sp.data(), sp.size());
     const size_t nodes = (size_t)g.geo.n[0] * g.geo.n[1] * g.geo.n[2];
     g.tables.alloc(nodes * std::max(ng, 1));
-    if (precision == ALEA_FP32) g.fix.alloc(nodes * std::max(ng, 1));
     g.executed.alloc(1);
     g.flags.alloc(1);
     ALEA_CUDA(cudaMemset(g.flags.p, 0, sizeof(unsigned)));
@@ -1750,10 +1798,11 @@ static void run_build(GridImpl& g, cudaStream_t s) {
     require(nbricks < (1ull << 31), ALEA_ERR_INVALID_ARGUMENT, "grid too large");
     ALEA_CUDA(cudaMemsetAsync(g.executed.p, 0, sizeof(unsigned long long), s));
     const bool f32 = g.precision == ALEA_FP32;
-    // events around every launch on the launching stream: [chunk][phase]
+    // one launch per chunk of up to MAX_NG guests, timed by events on the stream
     const int chunks = (ng + MAX_NG - 1) / MAX_NG;
-    std::vector<cudaEvent_t> ev((size_t)chunks * 3);
+    cudaEvent_t ev[2];
     for (auto& e : ev) ALEA_CUDA(cudaEventCreate(&e));
+    ALEA_CUDA(cudaEventRecord(ev[0], s));
     for (int c = 0; c < chunks; ++c) {
         const int g0 = c * MAX_NG;
         const int cnt = std::min(MAX_NG, ng - g0);
@@ -1761,32 +1810,17 @@ static void run_build(GridImpl& g, cudaStream_t s) {
         const size_t pofs = (size_t)g0 * g.geo.n_types;
         const BuildArgs args{g.images.p, g.images_f.p, g.bin_start.p, g.params.p, g.guests.p + g0,
                              f32 ? g.pab.p + pofs : nullptr, f32 ? g.pff.p + pofs : nullptr,
-                             g.tables.p + (size_t)g0 * nodes,
-                             f32 ? g.fix.p + (size_t)g0 * nodes : nullptr, g.executed.p, g.flags.p};
-        ALEA_CUDA(cudaEventRecord(ev[3 * c], s));
-        launch_build(cnt, g.truncation, f32, 0, grid, s, g.geo, args);
+                             g.tables.p + (size_t)g0 * nodes, g.executed.p, g.flags.p};
+        launch_build(cnt, g.truncation, f32, grid, s, g.geo, args);
         ALEA_CUDA(cudaGetLastError());
-        ALEA_CUDA(cudaEventRecord(ev[3 * c + 1], s));
-        if (f32) {
-            launch_build(cnt, g.truncation, f32, 1, grid, s, g.geo, args);
-            ALEA_CUDA(cudaGetLastError());
-        }
-        ALEA_CUDA(cudaEventRecord(ev[3 * c + 2], s));
     }
-    ALEA_CUDA(cudaEventSynchronize(ev.back()));
-    float sweep = 0.f, fix = 0.f;
-    for (int c = 0; c < chunks; ++c) {
-        float a = 0.f, b = 0.f;
-        ALEA_CUDA(cudaEventElapsedTime(&a, ev[3 * c], ev[3 * c + 1]));
-        ALEA_CUDA(cudaEventElapsedTime(&b, ev[3 * c + 1], ev[3 * c + 2]));
-        sweep += a;
-        fix += b;
-    }
+    ALEA_CUDA(cudaEventRecord(ev[1], s));
+    ALEA_CUDA(cudaEventSynchronize(ev[1]));
+    float ms = 0.f;
+    ALEA_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
     for (auto& e : ev) cudaEventDestroy(e);
-    g.last_ms = sweep + fix;
-    g.last_sweep_ms = sweep;
-    g.last_fix_ms = fix;
-    g.launches = chunks * (f32 ? 2 : 1);
+    g.last_ms = ms;
+    g.launches = chunks;
     unsigned long long ex = 0;
     ALEA_CUDA(cudaMemcpy(&ex, g.executed.p, sizeof(ex), cudaMemcpyDeviceToHost));
     g.executed_pairs = ex;
@@ -1866,8 +1900,6 @@ void grid_stats(const GridImpl* g, alea_grid_stats* out) {
     out->images = g->n_images;
     out->bricks = (uint64_t)g->geo.bricks[0] * g->geo.bricks[1] * g->geo.bricks[2];
     out->last_kernel_ms = g->last_ms;
-    out->last_sweep_ms = g->last_sweep_ms;
-    out->last_fix_ms = g->last_fix_ms;
     out->launches = (uint32_t)g->launches;
 }
 
@@ -1922,7 +1954,7 @@ GridBatchImpl* grid_batch_create(uint32_t n, const alea_lennard_jones* lj, const
             (void)nodes;
             items[i].geo = g->geo;
             items[i].args = F32GridArgs{g->images_f.p, g->bin_start.p, g->pab.p, g->pff.p,
-                                        g->tables.p, g->fix.p};
+                                        g->tables.p};
             items[i].brick0 = b->total;
             b->total += (uint64_t)g->geo.bricks[0] * g->geo.bricks[1] * g->geo.bricks[2];
         }

@@ -166,9 +166,7 @@ typedef struct {
     uint64_t executed_pairs;    /* node-image pairs the kernel evaluated (all species) */
     uint64_t images;            /* periodic atom images staged */
     uint64_t bricks;            /* thread-block tiles of nodes */
-    float last_kernel_ms;       /* duration of the last build, CUDA events */
-    float last_sweep_ms;        /* of which the pair sweep (the FP64 kernel in that form) */
-    float last_fix_ms;          /* and the FP32 form's close-pair correction */
+    float last_kernel_ms;       /* duration of the last build's launches, CUDA events */
     uint32_t launches;          /* kernel launches of the last build */
 } alea_grid_stats;
 alea_status alea_grid_stats_get(const alea_grid* g, alea_grid_stats* out);

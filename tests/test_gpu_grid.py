@@ -179,6 +179,27 @@ def test_fp32_truncations_vs_oracle(lib, orc, trunc):
             assert (mine[ref >= 1e5] >= 1e4).all()
 
 
+@pytest.mark.parametrize("trunc", [0, 1, 2])
+def test_fp32_every_node_vs_fp64(lib, trunc):
+    """Every node of a fine grid (0.3 Å, 636k nodes, the CO2 site guests) in
+    FP32 against the FP64 form (itself within 1e-10 of the oracle): the nodes
+    whose close pairs take the double-float correction are among them."""
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    fw = W.cubic_framework(seed=13)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, trunc)
+    p = A.ParticleData.from_framework(fw)
+    guests = [fw.guest_species["CO2_C"], fw.guest_species["CO2_O"]]
+    g64 = A.FrameworkEnergyGrid(ff, p, fw.lattice, guests, 0.3, A.FP64)
+    g32 = A.FrameworkEnergyGrid(ff, p, fw.lattice, guests, 0.3, A.FP32)
+    for sid in guests:
+        t64, t32 = g64.table(sid), g32.table(sid)
+        keep = t64 <= 1e4
+        assert keep.sum() > 100000
+        assert rel_err(t32[keep], t64[keep], floor=KT).max() <= 1e-5
+        assert (t32[t64 >= 1e5] >= 1e4).all()
+
+
 def test_full_c1_grid_vs_oracle_sample(lib, orc):
     """The 52^3 grid of the 424-atom cell at 0.5 Å: every node in FP64 and FP32
     against the oracle on a strided sample of nodes."""
