@@ -196,10 +196,10 @@ alea_status alea_grid_destroy(alea_grid* g);
 /* No counterpart in the reference (one FrameworkEnergyGrid per framework,
  * framework_energy_grid.cc:193-249). n independent frameworks, each with its
  * own force field, atoms and cell (so their node counts differ), built in the
- * FP32 form in one persistent launch per kernel: CTAs take (grid, brick) work
- * items from a global counter. The first build times the launch variants on
- * the batch (the autotuner) and captures the chosen launch sequence into a
- * CUDA graph; every build replays it. Each grid equals a single
+ * FP32 form in one persistent launch: CTAs take (grid, brick) work items from
+ * a global counter. The first build times the launch variants on the batch
+ * (the autotuner) and captures the chosen launch into a CUDA graph; every
+ * build replays it. Each grid equals a single
  * alea_grid_build of that framework (FP32), bit for bit. guest_species holds
  * n x n_guest ids; every grid must have the same number of distinct guests
  * (1..4) and the same truncation. */
