@@ -59,7 +59,7 @@ KERNEL_FLOPS_PER_NODE_IMAGE = 11
 KERNEL_FLOPS_PER_SPECIES = 4
 # DRAM bytes (read + write) of one sweep launch on this workload, from a
 # single-pass ncu capture of the full workload (profiles/grid_build_f32_c5_dram.md)
-SWEEP_DRAM_BYTES_PER_LAUNCH = 1538254336
+SWEEP_DRAM_BYTES_PER_LAUNCH = 1347673088
 
 
 def _dist():
