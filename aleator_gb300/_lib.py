@@ -206,6 +206,7 @@ _SIGNATURES = {
     "alea_gcmc_ewald_energy": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D]),
     "alea_gcmc_destroy": (ctypes.c_int32, [_VP]),
     "alea_gcmc_set_proposal": (ctypes.c_int32, [_VP, _VP]),
+    "alea_gcmc_set_precision": (ctypes.c_int32, [_VP, ctypes.c_int32]),
     "alea_grid_batch_create": (ctypes.c_int32, [ctypes.c_uint32, ctypes.POINTER(_LJ),
                                                 ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
                                                 _U32, ctypes.c_uint32, ctypes.c_double,
@@ -923,7 +924,7 @@ class GcmcChains:
     def __init__(self, force_field: LennardJones, framework: ParticleData, lattice, guest: dict,
                  temperature: float, fugacities_pa, seeds, streams, ewald: Ewald | None = None,
                  max_translation=1.5, max_rotation=0.5, draw_order=ALEA_DRAWS_RIGHT_TO_LEFT,
-                 max_molecules=256):
+                 max_molecules=256, precision=None):
         self._lib = library()
         self._h = _VP()
         self._g = {k: (_f64(guest[k]) if k != "lj_species" else
@@ -947,6 +948,13 @@ class GcmcChains:
                                           self.n_chains, float(max_translation),
                                           float(max_rotation), int(draw_order), int(max_molecules),
                                           ctypes.byref(self._h)))
+        if precision is not None:
+            self.set_precision(precision)
+
+    def set_precision(self, precision):
+        """FP64 (the reference's arithmetic) or FP32 (FP32 pair terms and
+        S(k) phases, FP64 sums) for the next runs."""
+        _check(self._lib.alea_gcmc_set_precision(self._h, int(precision)))
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -714,6 +714,13 @@ alea_status alea_gcmc_set_proposal(alea_gcmc* g, const alea_proposal* p) {
     });
 }
 
+alea_status alea_gcmc_set_precision(alea_gcmc* g, int32_t precision) {
+    return guarded([&] {
+        need(g, "gcmc");
+        alea::gcmc_set_precision(g->impl, precision);
+    });
+}
+
 alea_status alea_proposal_create(const alea_proposal_config* config, alea_proposal** out) {
     return guarded([&] {
         need(config, "config");

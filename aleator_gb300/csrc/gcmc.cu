@@ -34,6 +34,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "ff.cuh"
 #include "gcmc.cuh"
 #include "grid.cuh"
 
@@ -71,6 +72,9 @@ struct GcmcConst {
     // insertion): the template centred on its centroid, and the table size
     int prop_cells;
     double tc[MAXS][3];
+    int f32;  // ALEA_FP32 form: FP32 pair and real-space terms, FP32 per-term S(k) deltas
+    float lh[9], ll[9], linv[9];  // FP32 form: rows a_i as hi + lo; the inverse (f = d . inv)
+    double excl_tmpl;  // FP32 form: pairExclusionSum of the rigid template (any position)
 };
 
 struct GcmcPtrs {
@@ -90,6 +94,14 @@ struct GcmcPtrs {
     unsigned* flags;
     const double* pcdf;   // proposal cell CDF
     const double* plogp;  // log of the cell density relative to uniform
+    // FP32 form: positions as double-float, {x, y, z hi, charge} and {x, y, z lo, 0}
+    const float4* fwh;
+    const float4* fwl;
+    float4 *ghi, *glo;
+    // FP32 form: FP32 copies of the weights and of each chain's committed
+    // S(k) (refreshed on every commit and resync), FP32 per-term deltas
+    const float* w32;
+    float *sre32, *sim32, *dre32, *dim32;
 };
 
 struct StepShared {
@@ -105,6 +117,38 @@ struct StepShared {
     double rec_sum, dself, dexcl;
     double lq;  // learned proposal: log density at the inserted / deleted centroid
 };
+
+// FP32 form: a guest site's pair terms with one framework or guest type:
+// 4 eps sigma^12, 4 eps sigma^6, the shift terms, and sigma^2 below which the
+// pair stays in FP64 (its repulsive term reaches 1e4 K there).
+struct PairF32 {
+    float a, b, shift, dvdrc, sig2;
+};
+
+// A displacement (double-float per component) brought to its image within the
+// cutoff: the lattice shifts are chosen from the hi parts in FP32 (any pair
+// within rc <= L_perp/2 has a clear choice) and taken off in double-float, so
+// the result carries ~48 bits however far the image moved.
+__device__ __forceinline__ void wrap_ff(const GcmcConst& C, ff& x, ff& y, ff& z) {
+    if (C.L.ortho) {
+        const float n0 = rintf(x.hi * C.linv[0]), n1 = rintf(y.hi * C.linv[4]),
+                    n2 = rintf(z.hi * C.linv[8]);
+        x = ff_add(x, ff_scale(-n0, ff{C.lh[0], C.ll[0]}));
+        y = ff_add(y, ff_scale(-n1, ff{C.lh[4], C.ll[4]}));
+        z = ff_add(z, ff_scale(-n2, ff{C.lh[8], C.ll[8]}));
+        return;
+    }
+    float n[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        n[a] = rintf(fmaf(x.hi, C.linv[a], fmaf(y.hi, C.linv[3 + a], z.hi * C.linv[6 + a])));
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        x = ff_add(x, ff_scale(-n[a], ff{C.lh[3 * a], C.ll[3 * a]}));
+        y = ff_add(y, ff_scale(-n[a], ff{C.lh[3 * a + 1], C.ll[3 * a + 1]}));
+        z = ff_add(z, ff_scale(-n[a], ff{C.lh[3 * a + 2], C.ll[3 * a + 2]}));
+    }
+}
 
 __device__ __forceinline__ double u01(ChainState& c) {
     return philox_uniform(c.seed, c.stream, c.call++);
@@ -149,7 +193,8 @@ __device__ double exclusion_sum(const Lattice& L, const double (*p)[3], const do
 
 // rotateAboutAxis (monte_carlo_engine.cc:40-44)
 __device__ void rotate_about_axis(const double* v, const double* a, double th, double* o) {
-    const double c = cos(th), s = sin(th);
+    double s, c;
+    sincos(th, &s, &c);
     const double cr[3] = {sub_rn(mul_rn(a[1], v[2]), mul_rn(a[2], v[1])),
                           sub_rn(mul_rn(a[2], v[0]), mul_rn(a[0], v[2])),
                           sub_rn(mul_rn(a[0], v[1]), mul_rn(a[1], v[0]))};
@@ -195,10 +240,13 @@ __device__ void plan_biased_insertion(const GcmcConst& C, const GcmcPtrs& P, Cha
         const double v0 = u01(c), v1 = u01(c), v2 = u01(c);
         const double r1 = __dsqrt_rn(sub_rn(1.0, v0)), r2 = __dsqrt_rn(v0);
         const double t1 = mul_rn(2.0 * kPi, v1), t2 = mul_rn(2.0 * kPi, v2);
-        q[0] = mul_rn(r2, cos(t2));
-        q[1] = mul_rn(r1, sin(t1));
-        q[2] = mul_rn(r1, cos(t1));
-        q[3] = mul_rn(r2, sin(t2));
+        double s1, c1, s2, c2;
+        sincos(t1, &s1, &c1);
+        sincos(t2, &s2, &c2);
+        q[0] = mul_rn(r2, c2);
+        q[1] = mul_rn(r1, s1);
+        q[2] = mul_rn(r1, c1);
+        q[3] = mul_rn(r2, s2);
     }
     for (int s = 0; s < ns; ++s) {
         const double* loc = C.tc[s];
@@ -217,6 +265,14 @@ __device__ void plan_biased_insertion(const GcmcConst& C, const GcmcPtrs& P, Cha
         for (int i = 0; i < 3; ++i) S.np_[s][i] = add_rn(ref[i], rot[i]);
     }
     S.n_new = ns;
+}
+
+// The double-float copy of a guest site's position (the FP32 form's input).
+__device__ __forceinline__ void put_hilo(float4* ghi, float4* glo, uint32_t slot, const double* p,
+                                         double q) {
+    const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
+    ghi[slot] = make_float4(x.hi, y.hi, z.hi, (float)q);
+    glo[slot] = make_float4(x.lo, y.lo, z.lo, 0.f);
 }
 
 // Thread 0: the draws and trial geometry of one move.
@@ -262,10 +318,13 @@ __device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, 
             }
             const double r1 = __dsqrt_rn(sub_rn(1.0, v[0])), r2 = __dsqrt_rn(v[0]);
             const double t1 = mul_rn(2.0 * kPi, v[1]), t2 = mul_rn(2.0 * kPi, v[2]);
-            q[0] = mul_rn(r2, cos(t2));
-            q[1] = mul_rn(r1, sin(t1));
-            q[2] = mul_rn(r1, cos(t1));
-            q[3] = mul_rn(r2, sin(t2));
+            double s1, c1, s2, c2;
+            sincos(t1, &s1, &c1);
+            sincos(t2, &s2, &c2);
+            q[0] = mul_rn(r2, c2);
+            q[1] = mul_rn(r1, s1);
+            q[2] = mul_rn(r1, c1);
+            q[3] = mul_rn(r2, s2);
         }
         for (int s = 0; s < ns; ++s) {
             const double loc[3] = {C.sx[s], C.sy[s], C.sz[s]};
@@ -329,7 +388,9 @@ __device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, 
         const double ct = sub_rn(mul_rn(2.0, u01(c)), 1.0);
         const double st = __dsqrt_rn(fmax(0.0, sub_rn(1.0, mul_rn(ct, ct))));
         const double phi = mul_rn(2.0 * kPi, u01(c));
-        const double axis[3] = {mul_rn(st, cos(phi)), mul_rn(st, sin(phi)), ct};
+        double sp, cp;
+        sincos(phi, &sp, &cp);
+        const double axis[3] = {mul_rn(st, cp), mul_rn(st, sp), ct};
         const double ang = mul_rn(sub_rn(mul_rn(2.0, u01(c)), 1.0), C.max_rot);
         for (int s = 0; s < ns; ++s) {
             const double v[3] = {sub_rn(S.op[s][0], cen[0]), sub_rn(S.op[s][1], cen[1]),
@@ -342,14 +403,26 @@ __device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, 
     S.n_new = ns;
 }
 
+// F32: the FP32 form. Its per-site phase tables (FP32, in dynamic shared
+// memory): e^{i n theta_a} per slot, axis and n, then
+// q e^{i (n0 theta_0 + n1 theta_1)} per slot and (n0, n1).
 template <int NS>
+constexpr size_t f32_phase_bytes(int kmax) {
+    const size_t tw = 2 * (size_t)kmax + 1;
+    return 2 * NS * 3 * tw * sizeof(float2) + 2 * NS * tw * tw * sizeof(float2);
+}
+
+template <int NS, bool F32>
 __global__ void __launch_bounds__(GT)
 gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     __shared__ StepShared S;
     __shared__ double red[(GT / 32 + 1) * RSTRIDE];
-    __shared__ double2 etab[2 * NS][3][2 * KMAXC + 1];
+    __shared__ double2 etab[F32 ? 1 : 2 * NS][3][2 * KMAXC + 1];
     __shared__ double eq[2 * NS];
     __shared__ PairParams srow[NS][64];
+    __shared__ PairF32 srow32[F32 ? NS : 1][64];
+    __shared__ float4 sph[F32 ? 2 * NS : 1], spl[F32 ? 2 * NS : 1];  // trial sites, hi + lo
+    extern __shared__ __align__(16) unsigned char dyn[];
 
     const int chain = blockIdx.x;
     ChainState c = P.st[chain];  // thread 0's copy is the authoritative one
@@ -359,21 +432,45 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     double* gz = P.gz + so;
     double* gq = P.gq + so;
     uint32_t* gt = P.gt + so;
+    float4* ghi = P.ghi + so;
+    float4* glo = P.glo + so;
     uint32_t* mol = P.mol + (size_t)chain * C.max_mol * NS;
     double* sre = P.sre + (size_t)chain * C.nk;
     double* sim = P.sim + (size_t)chain * C.nk;
     double* dre = P.dre + (size_t)chain * C.nk;
     double* dim = P.dim + (size_t)chain * C.nk;
+    float* sre32 = F32 ? P.sre32 + (size_t)chain * C.nk : nullptr;
+    float* sim32 = F32 ? P.sim32 + (size_t)chain * C.nk : nullptr;
+    float* dre32 = F32 ? P.dre32 + (size_t)chain * C.nk : nullptr;
+    float* dim32 = F32 ? P.dim32 + (size_t)chain * C.nk : nullptr;
     const int K = C.kmax;
-    for (int i = threadIdx.x; i < NS * (int)C.n_species; i += GT)
-        srow[i / C.n_species][i % C.n_species] =
-            P.table[(size_t)C.slj[i / C.n_species] * C.n_species + i % C.n_species];
+    for (int i = threadIdx.x; i < NS * (int)C.n_species; i += GT) {
+        const PairParams pp = P.table[(size_t)C.slj[i / C.n_species] * C.n_species + i % C.n_species];
+        srow[i / C.n_species][i % C.n_species] = pp;
+        if constexpr (F32) {
+            const double s2 = pp.sigma * pp.sigma, s6 = s2 * s2 * s2;
+            srow32[i / C.n_species][i % C.n_species] =
+                PairF32{(float)(4.0 * pp.eps * s6 * s6), (float)(4.0 * pp.eps * s6), (float)pp.shift,
+                        (float)pp.dvdrc, (float)s2};
+        }
+    }
+    const int tw = 2 * C.kmax + 1;
+    float2* etab32 = reinterpret_cast<float2*>(dyn);               // [2NS][3][tw]
+    float2* ab32 = etab32 + (size_t)2 * NS * 3 * tw;                // [2NS][tw][tw]
     __syncthreads();
 
     for (uint64_t step = 0; step < steps; ++step) {
         if (threadIdx.x == 0) {
             if (c.err == 0) {
                 plan_move(C, P, c, gx, gy, gz, mol, S);
+                if constexpr (F32) {
+                    for (int e = 0; e < 2 * NS; ++e) {
+                        const double* p = e < NS ? S.op[e] : S.np_[e - NS];
+                        const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
+                        sph[e] = make_float4(x.hi, y.hi, z.hi, 0.f);
+                        spl[e] = make_float4(x.lo, y.lo, z.lo, 0.f);
+                    }
+                }
             } else {
                 S.valid = 0;
             }
@@ -386,6 +483,71 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
             double acc[4 * NS];
 #pragma unroll
             for (int e = 0; e < 4 * NS; ++e) acc[e] = 0.0;
+            if constexpr (F32) {
+                // FP64 displacement and image, then FP32 terms; this thread's
+                // few FP32 partials are added in FP64 by the block sum
+                float accf[4 * NS];
+#pragma unroll
+                for (int e = 0; e < 4 * NS; ++e) accf[e] = 0.f;
+                const float rc2f = (float)C.rc2, rcf = (float)C.rc, rce2f = (float)C.rc_ew2,
+                            alphaf = (float)C.alpha;
+                for (uint64_t j = threadIdx.x; j < n_all; j += GT) {
+                    bool skip = false;
+                    if (n_old)
+#pragma unroll
+                        for (int x = 0; x < NS; ++x) skip |= (S.ex[x] == (uint32_t)j);
+                    if (skip) continue;
+                    float4 ah, al;
+                    uint32_t ta;
+                    if (j < C.n_fw) {
+                        ah = P.fwh[j];
+                        al = P.fwl[j];
+                        ta = P.fw_type[j];
+                    } else {
+                        const uint64_t g = j - C.n_fw;
+                        ah = ghi[g];
+                        al = glo[g];
+                        ta = gt[g];
+                    }
+                    const float qa = ah.w;
+#pragma unroll
+                    for (int e = 0; e < 2 * NS; ++e) {
+                        const bool is_old = e < NS;
+                        if (is_old ? (n_old == 0) : (n_new == 0)) continue;
+                        const int s = is_old ? e : e - NS;
+                        const float4 ph = sph[e], pl = spl[e];
+                        ff dx = ff_add(ff{ah.x, al.x}, ff{-ph.x, -pl.x});
+                        ff dy = ff_add(ff{ah.y, al.y}, ff{-ph.y, -pl.y});
+                        ff dz = ff_add(ff{ah.z, al.z}, ff{-ph.z, -pl.z});
+                        wrap_ff(C, dx, dy, dz);
+                        const float r2 = fmaf(dx.hi, dx.hi, fmaf(dy.hi, dy.hi, dz.hi * dz.hi));
+                        const bool lj_in = r2 <= rc2f;
+                        const bool el_in = C.charged && r2 <= rce2f;
+                        if (!lj_in && !el_in) continue;
+                        if (lj_in) {
+                            const PairF32 q = srow32[s][ta];
+                            if (r2 < q.sig2) {
+                                const double ex = (double)dx.hi + dx.lo, ey = (double)dy.hi + dy.lo,
+                                             ez = (double)dz.hi + dz.lo;
+                                acc[2 * e] += lj_pair_rt(C.trunc, sqrt(ex * ex + ey * ey + ez * ez), C.rc,
+                                                         srow[s][ta]);
+                            } else {
+                                const float ir2 = 1.0f / r2;
+                                const float ir6 = ir2 * ir2 * ir2;
+                                float v = ir6 * fmaf(q.a, ir6, -q.b) - q.shift;
+                                if (C.trunc == ALEA_LINEAR_FORCE_SHIFTED) v -= (sqrtf(r2) - rcf) * q.dvdrc;
+                                accf[2 * e] += v;
+                            }
+                        }
+                        if (el_in) {
+                            const float r = sqrtf(r2);
+                            accf[2 * e + 1] += qa * (erfcf(alphaf * r) / r);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int e = 0; e < 4 * NS; ++e) acc[e] += (double)accf[e];
+            } else
             for (uint64_t j = threadIdx.x; j < n_all; j += GT) {
                 bool skip = false;
                 if (n_old)
@@ -429,8 +591,74 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 }
 
             // ---- reciprocal delta: removed = old sites, added = new sites
-            if (C.charged) {
-                const int tw = 2 * K + 1;
+            if constexpr (F32) {
+              if (C.charged) {
+                // FP32 phases (the angle reduced to [-pi, pi] in FP64 first)
+                for (int i = threadIdx.x; i < 2 * NS * 3 * tw; i += GT) {
+                    const int e = i / (3 * tw), a = (i / tw) % 3, n = i % tw - K;
+                    const bool is_old = e < NS;
+                    if (is_old ? (n_old == 0) : (n_new == 0)) continue;
+                    const int s = is_old ? e : e - NS;
+                    const double* p = is_old ? S.op[s] : S.np_[s];
+                    const double th = C.b[3 * a] * p[0] + C.b[3 * a + 1] * p[1] + C.b[3 * a + 2] * p[2];
+                    const double x = (double)n * th;
+                    const double r = x - (2.0 * kPi) * rint(x * (0.5 / kPi));
+                    float sn, cs;
+                    sincosf((float)r, &sn, &cs);
+                    etab32[i] = make_float2(cs, sn);
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < 2 * NS * tw * tw; i += GT) {
+                    const int e = i / (tw * tw), n0 = (i / tw) % tw, n1 = i % tw;
+                    const bool is_old = e < NS;
+                    if (is_old ? (n_old == 0) : (n_new == 0)) continue;
+                    const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1];
+                    const float q = (float)C.sq[is_old ? e : e - NS];
+                    ab32[i] = make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
+                }
+                __syncthreads();
+                // per term w (2 S.delta + |delta|^2) in FP32 from the FP32
+                // copy of S; this thread's ~nk/256 terms summed in FP32, the
+                // block's partials in FP64
+                float racc = 0.f;
+                for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
+                    const int n0 = P.nidx[3 * t] + K, n1 = P.nidx[3 * t + 1] + K, n2 = P.nidx[3 * t + 2] + K;
+                    float re = 0.f, im = 0.f;
+                    if (n_new)  // added first (ewald_incremental_state.cc:107-111)
+#pragma unroll
+                        for (int s = 0; s < NS; ++s) {
+                            const float2 Z = ab32[((NS + s) * tw + n0) * tw + n1];
+                            const float2 Cc = etab32[((NS + s) * 3 + 2) * tw + n2];
+                            re = fmaf(Z.x, Cc.x, fmaf(-Z.y, Cc.y, re));
+                            im = fmaf(Z.x, Cc.y, fmaf(Z.y, Cc.x, im));
+                        }
+                    if (n_old)  // then removed (:112-116)
+#pragma unroll
+                        for (int s = 0; s < NS; ++s) {
+                            const float2 Z = ab32[(s * tw + n0) * tw + n1];
+                            const float2 Cc = etab32[(s * 3 + 2) * tw + n2];
+                            re = fmaf(-Z.x, Cc.x, fmaf(Z.y, Cc.y, re));
+                            im = fmaf(-Z.x, Cc.y, fmaf(-Z.y, Cc.x, im));
+                        }
+                    const float o_re = sre32[t], o_im = sim32[t];
+                    const float dot = fmaf(o_re, re, o_im * im);
+                    racc = fmaf(P.w32[t], fmaf(2.f, dot, fmaf(re, re, im * im)), racc);
+                    dre32[t] = re;
+                    dim32[t] = im;
+                }
+                double v[1] = {(double)racc};
+                block_sum_n(v, 1, red);
+                if (threadIdx.x == 0) {
+                    S.rec_sum = C.rec_pref * v[0];
+                    double q2a = 0.0, q2r = 0.0;
+                    for (int s = 0; s < n_new; ++s) q2a += C.sq[s] * C.sq[s];
+                    for (int s = 0; s < n_old; ++s) q2r += C.sq[s] * C.sq[s];
+                    S.dself = C.self_pref * (q2a - q2r);
+                    // a rigid molecule's exclusion sum is the template's
+                    S.dexcl = -kCoulomb * ((n_new ? C.excl_tmpl : 0.0) - (n_old ? C.excl_tmpl : 0.0));
+                }
+              }
+            } else if (C.charged) {
                 for (int i = threadIdx.x; i < 2 * NS * 3 * tw; i += GT) {
                     const int e = i / (3 * tw), a = (i / tw) % 3, n = i % tw - K;
                     const bool is_old = e < NS;
@@ -523,11 +751,21 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
             __syncthreads();
 
             if (S.accept) {
-                if (C.charged)
-                    for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
-                        sre[t] += dre[t];
-                        sim[t] += dim[t];
+                if (C.charged) {
+                    if constexpr (F32) {
+                        for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
+                            sre[t] += (double)dre32[t];
+                            sim[t] += (double)dim32[t];
+                            sre32[t] = (float)sre[t];
+                            sim32[t] = (float)sim[t];
+                        }
+                    } else {
+                        for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
+                            sre[t] += dre[t];
+                            sim[t] += dim[t];
+                        }
                     }
+                }
                 if (threadIdx.x == 0) {
                     c.accepted[S.move]++;
                     if (C.charged) {
@@ -540,6 +778,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                             gx[slot] = S.np_[s][0];
                             gy[slot] = S.np_[s][1];
                             gz[slot] = S.np_[s][2];
+                            put_hilo(ghi, glo, slot, S.np_[s], C.sq[s]);
                         }
                     } else if (S.move == 2) {
                         for (int s = 0; s < NS; ++s) {
@@ -549,6 +788,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                             gz[slot] = S.np_[s][2];
                             gq[slot] = C.sq[s];
                             gt[slot] = C.slj[s];
+                            put_hilo(ghi, glo, slot, S.np_[s], C.sq[s]);
                             mol[(size_t)c.n_mol * NS + s] = (uint32_t)C.n_fw + slot;
                         }
                         c.n_guest += NS;
@@ -569,6 +809,8 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                                 gz[ds] = gz[ls];
                                 gq[ds] = gq[ls];
                                 gt[ds] = gt[ls];
+                                ghi[ds] = ghi[ls];
+                                glo[ds] = glo[ls];
                                 for (uint64_t m = 0; m < (uint64_t)c.n_mol * NS; ++m)
                                     if (mol[m] == last) mol[m] = site;
                                 for (int k2 = k + 1; k2 < NS; ++k2)
@@ -601,12 +843,19 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         }
                         sre[t] = re;
                         sim[t] = im;
+                        if constexpr (F32) {
+                            sre32[t] = (float)re;
+                            sim32[t] = (float)im;
+                        }
                     }
                     if (threadIdx.x == 0) {
                         double q2 = C.fw_q2;
                         for (uint64_t g = 0; g < ng; ++g) q2 += gq[g] * gq[g];
                         c.self_e = C.self_pref * q2;
                         double ex = 0.0;
+                        if constexpr (F32)
+                            ex = (double)c.n_mol * C.excl_tmpl;
+                        else
                         for (uint32_t m = 0; m < c.n_mol; ++m) {
                             double p[MAXS][3], q[MAXS];
                             for (int s = 0; s < NS; ++s) {
@@ -639,16 +888,29 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
 template <int NS>
 void launch_chains(unsigned n_chains, const GcmcConst& C, const GcmcPtrs& P, uint64_t steps,
                    cudaStream_t s) {
-    gcmc_kernel<NS><<<n_chains, GT, 0, s>>>(C, P, steps);
+    if (C.f32) {
+        const size_t bytes = C.charged ? f32_phase_bytes<NS>(C.kmax) : 0;
+        ALEA_CUDA(cudaFuncSetAttribute(gcmc_kernel<NS, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        gcmc_kernel<NS, true><<<n_chains, GT, bytes, s>>>(C, P, steps);
+    } else {
+        gcmc_kernel<NS, false><<<n_chains, GT, 0, s>>>(C, P, steps);
+    }
 }
 
-__global__ void gather_sfw_kernel(uint64_t nk, const double* re, const double* im, double* out_re,
-                                  double* out_im, unsigned n_chains) {
+// Every chain's committed S(k) starts as the framework's (and its FP32 copy;
+// the weights' FP32 copy too).
+__global__ void gather_sfw_kernel(uint64_t nk, const double* re, const double* im, const double* w,
+                                  double* out_re, double* out_im, float* out_re32, float* out_im32,
+                                  float* w32, unsigned n_chains) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nk) return;
+    w32[t] = (float)w[t];
     for (unsigned c = 0; c < n_chains; ++c) {
         out_re[(size_t)c * nk + t] = re[t];
         out_im[(size_t)c * nk + t] = im[t];
+        out_re32[(size_t)c * nk + t] = (float)re[t];
+        out_im32[(size_t)c * nk + t] = (float)im[t];
     }
 }
 
@@ -667,6 +929,8 @@ struct GcmcImpl {
     DevBuf<uint32_t> gt, mol;
     DevBuf<unsigned> flags;
     DevBuf<double> pcdf, plogp;  // the chains' copy of a tabulated proposal
+    DevBuf<float4> fwh, fwl, ghi, glo;  // FP32 form: double-float positions
+    DevBuf<float> w32, sre32, sim32, dre32, dim32;  // FP32 form: S(k) copies and deltas
     float last_ms = 0.f;
 };
 
@@ -712,6 +976,19 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
             C.tc[s][1] = guest.y[s];
             C.tc[s][2] = guest.z[s];
             qs += C.sq[s];
+        }
+        {  // pairExclusionSum of the template (ewald_incremental_state.cc:32-43): a rigid
+           // molecule's, wherever it is (its pairs are far shorter than half a cell)
+            double ex = 0.0;
+            for (int i = 0; i < (int)guest.n_sites; ++i)
+                for (int j = i + 1; j < (int)guest.n_sites; ++j) {
+                    const double dx = guest.x[j] - guest.x[i], dy = guest.y[j] - guest.y[i],
+                                 dz = guest.z[j] - guest.z[i];
+                    const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+                    const double qq = C.sq[i] * C.sq[j];
+                    if (ew) ex += qq * (r < 1e-8 ? 2.0 * ew->alpha / std::sqrt(kPi) : std::erf(ew->alpha * r) / r);
+                }
+            C.excl_tmpl = ex;
         }
         {  // the template about its centroid (the learned proposal's reference point)
             double m[3] = {0.0, 0.0, 0.0};
@@ -763,6 +1040,24 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         g->fw_type.alloc(std::max<size_t>(fw.n, 1));
         g->fw.upload(packed.data(), fw.n);
         g->fw_type.upload(types.data(), fw.n);
+        {
+            std::vector<float4> h(fw.n), l(fw.n);
+            for (uint64_t i = 0; i < fw.n; ++i) {
+                const ff x = ff_from(packed[i].x), y = ff_from(packed[i].y), z = ff_from(packed[i].z);
+                h[i] = make_float4(x.hi, y.hi, z.hi, (float)packed[i].w);
+                l[i] = make_float4(x.lo, y.lo, z.lo, 0.f);
+            }
+            g->fwh.alloc(std::max<size_t>(fw.n, 1));
+            g->fwl.alloc(std::max<size_t>(fw.n, 1));
+            g->fwh.upload(h.data(), fw.n);
+            g->fwl.upload(l.data(), fw.n);
+            for (int i = 0; i < 9; ++i) {
+                const ff m = ff_from(C.L.m[i]);
+                C.lh[i] = m.hi;
+                C.ll[i] = m.lo;
+                C.linv[i] = (float)C.L.inv[i];
+            }
+        }
         std::vector<PairParams> table((size_t)lj.n_species * lj.n_species);
         mixed_table(lj, table.data());
         g->table.alloc(table.size());
@@ -797,9 +1092,15 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         g->sim.alloc(nkc * n_chains);
         g->dre.alloc(nkc * n_chains);
         g->dim.alloc(nkc * n_chains);
+        g->w32.alloc(nkc);
+        g->sre32.alloc(nkc * n_chains);
+        g->sim32.alloc(nkc * n_chains);
+        g->dre32.alloc(nkc * n_chains);
+        g->dim32.alloc(nkc * n_chains);
         if (ews) {
-            gather_sfw_kernel<<<(unsigned)((nk + 255) / 256), 256>>>(nk, g->sfw_re.p, g->sfw_im.p,
-                                                                   g->sre.p, g->sim.p, n_chains);
+            gather_sfw_kernel<<<(unsigned)((nk + 255) / 256), 256>>>(
+                nk, g->sfw_re.p, g->sfw_im.p, g->w.p, g->sre.p, g->sim.p, g->sre32.p, g->sim32.p,
+                g->w32.p, n_chains);
             ALEA_CUDA(cudaGetLastError());
         }
         const size_t sites = (size_t)C.max_sites * n_chains;
@@ -809,6 +1110,8 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         g->gq.alloc(sites);
         g->gt.alloc(sites);
         g->mol.alloc(sites);
+        g->ghi.alloc(sites);
+        g->glo.alloc(sites);
         std::vector<ChainState> st(n_chains);
         const double self0 = ews ? ewald_state_view(ews).self_pref * fwq2 : 0.0;
         for (uint32_t c = 0; c < n_chains; ++c) {
@@ -861,6 +1164,15 @@ void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s) {
     P.flags = g->flags.p;
     P.pcdf = g->pcdf.p;
     P.plogp = g->plogp.p;
+    P.fwh = g->fwh.p;
+    P.fwl = g->fwl.p;
+    P.ghi = g->ghi.p;
+    P.glo = g->glo.p;
+    P.w32 = g->w32.p;
+    P.sre32 = g->sre32.p;
+    P.sim32 = g->sim32.p;
+    P.dre32 = g->dre32.p;
+    P.dim32 = g->dim32.p;
     cudaEvent_t e0, e1;
     ALEA_CUDA(cudaEventCreate(&e0));
     ALEA_CUDA(cudaEventCreate(&e1));
@@ -944,6 +1256,13 @@ void gcmc_set_proposal(GcmcImpl* g, const ProposalTable* t) {
     ALEA_CUDA(cudaMemcpy(g->plogp.p, t->logp, n * sizeof(double), cudaMemcpyDeviceToDevice));
     ALEA_CUDA(cudaDeviceSynchronize());
     g->C.prop_cells = t->cells;
+}
+
+// ALEA_FP64 (the parity form) or ALEA_FP32 for the next runs.
+void gcmc_set_precision(GcmcImpl* g, int precision) {
+    require(precision == ALEA_FP64 || precision == ALEA_FP32, ALEA_ERR_INVALID_ARGUMENT,
+            "GCMC: precision must be ALEA_FP64 or ALEA_FP32");
+    g->C.f32 = precision == ALEA_FP32;
 }
 
 unsigned gcmc_chains(const GcmcImpl* g) { return g->n_chains; }

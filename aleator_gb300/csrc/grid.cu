@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "ff.cuh"
 #include "grid.cuh"
 
 namespace alea {
@@ -169,44 +170,6 @@ __device__ __forceinline__ float box_min_dist2_lb(const float* G, const float* G
     return lb;
 }
 
-// ---------------------------------------------------------------- double-float
-// Two-float ("double-float") arithmetic for the rare close pairs of the FP32
-// form: the repulsive terms there reach 1e4 K, where FP32's ~1e-6 relative
-// rounding would leave ~1e-2 K of error in a node energy. Error-free
-// transformations (Knuth two-sum, FMA two-product); the _rn intrinsics keep
-// the compiler from contracting or reassociating them.
-struct ff {
-    float hi, lo;
-};
-__device__ __forceinline__ ff ff_two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-    return {s, e};
-}
-__device__ __forceinline__ ff ff_fast(float a, float b) {  // |a| >= |b|
-    const float s = __fadd_rn(a, b);
-    return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ ff ff_add(ff a, ff b) {
-    ff s = ff_two_sum(a.hi, b.hi);
-    s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
-    return ff_fast(s.hi, s.lo);
-}
-__device__ __forceinline__ ff ff_mul(ff a, ff b) {
-    const float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);
-    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
-    return ff_fast(p, e);
-}
-__device__ __forceinline__ ff ff_rcp(ff a) {  // one Newton step from the FP32 reciprocal
-    const float y = __frcp_rn(a.hi);
-    const ff ay = ff_mul(a, ff{y, 0.f});
-    const ff r = ff_add(ff{1.f, 0.f}, ff{-ay.hi, -ay.lo});
-    const ff c = ff_mul(ff{y, 0.f}, r);
-    return ff_add(ff{y, 0.f}, c);
-}
-
 struct alignas(16) ParamFF {
     float sig2_hi, sig2_lo, eps4_hi, eps4_lo, shift_hi, shift_lo, dvdrc, pad;
 };
@@ -225,14 +188,6 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return y;
 }
 
-// s * v for an FP32 scalar s and a double-float v.
-__device__ __forceinline__ ff ff_scale(float s, ff v) { return ff_mul(ff{s, 0.f}, v); }
-// a + b for a double-float a and an FP32 b.
-__device__ __forceinline__ ff ff_add_f(ff a, float b) {
-    ff s = ff_two_sum(a.hi, b);
-    s.lo = __fadd_rn(s.lo, a.lo);
-    return ff_fast(s.hi, s.lo);
-}
 
 // Node ownership inside a 16x8x8 brick: warp w covers the 8x4x4 sub-box
 // ((w&1)*8, ((w>>1)&1)*4, (w>>2)*4); lane l the column (l%8, l/8) of it and

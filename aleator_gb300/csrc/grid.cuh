@@ -159,6 +159,7 @@ void gcmc_states(const GcmcImpl* g, ChainState* out);
 uint64_t gcmc_particles(const GcmcImpl* g, uint32_t chain, double* xyz, uint64_t cap);
 double gcmc_ewald_energy(const GcmcImpl* g, uint32_t chain);
 void gcmc_set_proposal(GcmcImpl* g, const ProposalTable* t);
+void gcmc_set_precision(GcmcImpl* g, int precision);
 unsigned gcmc_chains(const GcmcImpl* g);
 float gcmc_last_ms(const GcmcImpl* g);
 void gcmc_destroy(GcmcImpl* g);

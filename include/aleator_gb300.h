@@ -468,6 +468,13 @@ alea_status alea_gcmc_destroy(alea_gcmc* g);
  * reference's uniform insertion. Declared after alea_proposal below. */
 struct alea_proposal;
 alea_status alea_gcmc_set_proposal(alea_gcmc* g, const struct alea_proposal* p);
+/* The chains' energy form from the next run on: ALEA_FP64 (default; the
+ * reference's arithmetic, trajectories equal to the reference's) or ALEA_FP32
+ * (LJ and real-space pair terms in FP32 after an FP64 minimum image, pairs
+ * closer than sigma in FP64, per-term S(k) deltas from FP32 phases; every sum,
+ * S(k), the self and exclusion terms and the acceptance in FP64). No
+ * counterpart in the reference. */
+alea_status alea_gcmc_set_precision(alea_gcmc* g, int32_t precision);
 
 /* ------------------------------------------------------------------ acceptance / EOS (host) */
 /* gcmc::insertionRatio ... clampToProbability (engines/monte_carlo/gcmc_acceptance.hpp:28-101) */
