@@ -125,6 +125,43 @@ struct PairF32 {
     float a, b, shift, dvdrc, sig2;
 };
 
+// FP32 form, pairs closer than sigma: sigma^2, 4 eps and the shift as
+// double-float (their repulsive terms reach 1e4 K)
+struct PairCloseFF {
+    float sig2h, sig2l, eps4h, eps4l, shifth, shiftl, dvdrc, pad;
+};
+
+// pairEnergy (lennard_jones.cc:70-86) in double-float from r^2
+__device__ __forceinline__ ff lj_close_ff(const PairCloseFF& q, ff rr, float rcf, int trunc) {
+    const ff s2 = ff_mul(ff{q.sig2h, q.sig2l}, ff_rcp(rr));
+    const ff s6 = ff_mul(ff_mul(s2, s2), s2);
+    ff e = ff_mul(ff{q.eps4h, q.eps4l}, ff_mul(s6, ff_add(s6, ff{-1.f, 0.f})));
+    e = ff_add(e, ff{-q.shifth, -q.shiftl});
+    if (trunc == ALEA_LINEAR_FORCE_SHIFTED) e = ff_add_f(e, -(sqrtf(rr.hi) - rcf) * q.dvdrc);
+    return e;
+}
+
+// Block sum of n double-float values per thread (n <= 4*MAXS), in a fixed
+// order on the FP32 pipe (a warp tree, then the warps in order), rounded to
+// double: out[i] (shared memory, read after the call).
+__device__ void block_sum_ff(ff* v, int n, double* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    ff* rf = reinterpret_cast<ff*>(red);
+    for (int i = 0; i < n; ++i) {
+        ff x = v[i];
+        for (int o = 16; o > 0; o >>= 1)
+            x = ff_add(x, ff{__shfl_down_sync(0xffffffffu, x.hi, o), __shfl_down_sync(0xffffffffu, x.lo, o)});
+        if (lane == 0) rf[wid * RSTRIDE + i] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < n) {
+        ff t{0.f, 0.f};
+        for (int w = 0; w < GT / 32; ++w) t = ff_add(t, rf[w * RSTRIDE + threadIdx.x]);
+        red[(GT / 32) * RSTRIDE + threadIdx.x] = (double)t.hi + (double)t.lo;
+    }
+    __syncthreads();
+}
+
 // A displacement (double-float per component) brought to its image within the
 // cutoff: the lattice shifts are chosen from the hi parts in FP32 (any pair
 // within rc <= L_perp/2 has a clear choice) and taken off in double-float, so
@@ -421,6 +458,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     __shared__ double eq[2 * NS];
     __shared__ PairParams srow[NS][64];
     __shared__ PairF32 srow32[F32 ? NS : 1][64];
+    __shared__ PairCloseFF srowff[F32 ? NS : 1][64];
     __shared__ float4 sph[F32 ? 2 * NS : 1], spl[F32 ? 2 * NS : 1];  // trial sites, hi + lo
     extern __shared__ __align__(16) unsigned char dyn[];
 
@@ -452,6 +490,9 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
             srow32[i / C.n_species][i % C.n_species] =
                 PairF32{(float)(4.0 * pp.eps * s6 * s6), (float)(4.0 * pp.eps * s6), (float)pp.shift,
                         (float)pp.dvdrc, (float)s2};
+            const ff fs2 = ff_from(s2), fe4 = ff_from(4.0 * pp.eps), fsh = ff_from(pp.shift);
+            srowff[i / C.n_species][i % C.n_species] =
+                PairCloseFF{fs2.hi, fs2.lo, fe4.hi, fe4.lo, fsh.hi, fsh.lo, (float)pp.dvdrc, 0.f};
         }
     }
     const int tw = 2 * C.kmax + 1;
@@ -487,8 +528,11 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 // FP64 displacement and image, then FP32 terms; this thread's
                 // few FP32 partials are added in FP64 by the block sum
                 float accf[4 * NS];
+                ff closef[2 * NS];  // pairs closer than sigma, double-float
 #pragma unroll
                 for (int e = 0; e < 4 * NS; ++e) accf[e] = 0.f;
+#pragma unroll
+                for (int e = 0; e < 2 * NS; ++e) closef[e] = ff{0.f, 0.f};
                 const float rc2f = (float)C.rc2, rcf = (float)C.rc, rce2f = (float)C.rc_ew2,
                             alphaf = (float)C.alpha;
                 for (uint64_t j = threadIdx.x; j < n_all; j += GT) {
@@ -527,10 +571,8 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         if (lj_in) {
                             const PairF32 q = srow32[s][ta];
                             if (r2 < q.sig2) {
-                                const double ex = (double)dx.hi + dx.lo, ey = (double)dy.hi + dy.lo,
-                                             ez = (double)dz.hi + dz.lo;
-                                acc[2 * e] += lj_pair_rt(C.trunc, sqrt(ex * ex + ey * ey + ez * ez), C.rc,
-                                                         srow[s][ta]);
+                                const ff rr = ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
+                                closef[e] = ff_add(closef[e], lj_close_ff(srowff[s][ta], rr, rcf, C.trunc));
                             } else {
                                 const float ir2 = 1.0f / r2;
                                 const float ir6 = ir2 * ir2 * ir2;
@@ -545,8 +587,17 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         }
                     }
                 }
+                // this thread's sums as double-float, added over the block
+                ff v[4 * NS];
 #pragma unroll
-                for (int e = 0; e < 4 * NS; ++e) acc[e] += (double)accf[e];
+                for (int e = 0; e < 2 * NS; ++e) {
+                    v[2 * e] = ff_add_f(closef[e], accf[2 * e]);
+                    v[2 * e + 1] = ff{accf[2 * e + 1], 0.f};
+                }
+                block_sum_ff(v, 4 * NS, red);
+#pragma unroll
+                for (int e = 0; e < 4 * NS; ++e) acc[e] = red[(GT / 32) * RSTRIDE + e];
+                __syncthreads();
             } else
             for (uint64_t j = threadIdx.x; j < n_all; j += GT) {
                 bool skip = false;
@@ -581,7 +632,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     if (el_in && r <= C.rc_ew) acc[2 * e + 1] += a.w * (erfc(C.alpha * r) / r);
                 }
             }
-            block_sum_n(acc, 4 * NS, red);
+            if constexpr (!F32) block_sum_n(acc, 4 * NS, red);
             if (threadIdx.x == 0)
 #pragma unroll
                 for (int e = 0; e < 2 * NS; ++e) {
@@ -646,10 +697,10 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     dre32[t] = re;
                     dim32[t] = im;
                 }
-                double v[1] = {(double)racc};
-                block_sum_n(v, 1, red);
+                ff v[1] = {ff{racc, 0.f}};
+                block_sum_ff(v, 1, red);
                 if (threadIdx.x == 0) {
-                    S.rec_sum = C.rec_pref * v[0];
+                    S.rec_sum = C.rec_pref * red[(GT / 32) * RSTRIDE];
                     double q2a = 0.0, q2r = 0.0;
                     for (int s = 0; s < n_new; ++s) q2a += C.sq[s] * C.sq[s];
                     for (int s = 0; s < n_old; ++s) q2r += C.sq[s] * C.sq[s];
@@ -835,11 +886,27 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
                         const double k0 = P.k[3 * t], k1 = P.k[3 * t + 1], k2 = P.k[3 * t + 2];
                         double re = P.sfw_re[t], im = P.sfw_im[t];
-                        for (uint64_t g = 0; g < ng; ++g) {
-                            double sn, cs;
-                            sincos(k0 * gx[g] + k1 * gy[g] + k2 * gz[g], &sn, &cs);
-                            re += gq[g] * cs;
-                            im += gq[g] * sn;
+                        if constexpr (F32) {
+                            // FP32 phases from the angle reduced in FP64, summed in double-float
+                            ff rf{0.f, 0.f}, imf{0.f, 0.f};
+                            for (uint64_t g = 0; g < ng; ++g) {
+                                const double x = k0 * gx[g] + k1 * gy[g] + k2 * gz[g];
+                                const double r = x - (2.0 * kPi) * rint(x * (0.5 / kPi));
+                                float sn, cs;
+                                sincosf((float)r, &sn, &cs);
+                                const float q = ghi[g].w;
+                                rf = ff_add_f(rf, q * cs);
+                                imf = ff_add_f(imf, q * sn);
+                            }
+                            re += (double)rf.hi + (double)rf.lo;
+                            im += (double)imf.hi + (double)imf.lo;
+                        } else {
+                            for (uint64_t g = 0; g < ng; ++g) {
+                                double sn, cs;
+                                sincos(k0 * gx[g] + k1 * gy[g] + k2 * gz[g], &sn, &cs);
+                                re += gq[g] * cs;
+                                im += gq[g] * sn;
+                            }
                         }
                         sre[t] = re;
                         sim[t] = im;
