@@ -207,6 +207,8 @@ _SIGNATURES = {
     "alea_gcmc_destroy": (ctypes.c_int32, [_VP]),
     "alea_gcmc_set_proposal": (ctypes.c_int32, [_VP, _VP]),
     "alea_gcmc_set_precision": (ctypes.c_int32, [_VP, ctypes.c_int32]),
+    "alea_gcmc_guest_sites": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D, ctypes.POINTER(ctypes.c_uint32),
+                                               ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
     "alea_grid_batch_create": (ctypes.c_int32, [ctypes.c_uint32, ctypes.POINTER(_LJ),
                                                 ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
                                                 _U32, ctypes.c_uint32, ctypes.c_double,
@@ -909,6 +911,42 @@ class Proposal:
 
     def tabulate(self, cells=64, uniform_share=0.05):
         _check(self._lib.alea_proposal_tabulate(self._h, cells, float(uniform_share)))
+        self.tabulated = True
+
+    def fit_at_loading(self, chains, force_field, framework, lattice, guest, temperature,
+                       ewald=None, chain_ids=(0,), n_samples=1 << 17, rounds=1, epochs=20,
+                       batch=16384, lr=2e-3, tau=1.0, cells=48, uniform_share=0.2, seed=4321,
+                       stream=100):
+        """Refits on Widom trials in the loaded state: one Widom context per
+        listed chain, whose framework is the framework plus that chain's guest
+        sites now (so the trial energies include the guests already adsorbed).
+        Rows are drawn from the current table when there is one (their log
+        density enters the loss), else uniformly. Returns the final loss."""
+        import torch
+
+        ids = list(chain_ids)
+        per = n_samples // len(ids)
+        widoms = []
+        for c in ids:
+            sites, sp = chains.guest_sites(c)
+            pd = ParticleData(np.concatenate([framework.x, sites[:, 0]]),
+                              np.concatenate([framework.y, sites[:, 1]]),
+                              np.concatenate([framework.z, sites[:, 2]]),
+                              np.concatenate([framework.charge, sites[:, 3]]),
+                              np.concatenate([framework.species, sp]))
+            widoms.append(Widom(force_field, pd, lattice, guest, temperature, ewald=ewald))
+        n = per * len(ids)
+        rows = torch.empty((n, SAMPLE_ROW), dtype=torch.float32, device="cuda")
+        row_bytes = SAMPLE_ROW * 4
+        loss = float("nan")
+        for r in range(rounds):
+            for i, w in enumerate(widoms):
+                w.samples(seed, stream + r * len(ids) + i, per, rows.data_ptr() + i * per * row_bytes,
+                          proposal=self if getattr(self, "tabulated", False) else None)
+            loss = self.train(rows.data_ptr(), n, epochs=epochs, batch=batch, lr=lr, tau=tau,
+                              seed=seed + r)
+            self.tabulate(cells, uniform_share)
+        return loss
 
     def log_density(self, s):
         s = _f64(np.asarray(s, dtype=np.float64).reshape(-1, 3))
@@ -990,6 +1028,16 @@ class GcmcChains:
         out = np.zeros(3 * n.value)
         _check(self._lib.alea_gcmc_particles(self._h, chain, _dp(out), n.value, ctypes.byref(n)))
         return out.reshape(-1, 3)
+
+    def guest_sites(self, chain=0):
+        """This chain's guest sites: (n, 4) x, y, z, charge and (n,) LJ species."""
+        n = ctypes.c_uint64()
+        _check(self._lib.alea_gcmc_guest_sites(self._h, chain, None, None, 0, ctypes.byref(n)))
+        xyzq = np.zeros(4 * max(n.value, 1))
+        sp = np.zeros(max(n.value, 1), dtype=np.uint32)
+        _check(self._lib.alea_gcmc_guest_sites(self._h, chain, _dp(xyzq), _u32p(sp), n.value,
+                                               ctypes.byref(n)))
+        return xyzq[:4 * n.value].reshape(-1, 4), sp[:n.value]
 
     def ewald_energy(self, chain=0):
         v = ctypes.c_double()

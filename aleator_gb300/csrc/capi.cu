@@ -905,6 +905,15 @@ alea_status alea_gcmc_particles(const alea_gcmc* g, uint32_t chain, double* xyz,
     });
 }
 
+alea_status alea_gcmc_guest_sites(const alea_gcmc* g, uint32_t chain, double* xyzq,
+                                  uint32_t* lj_species, uint64_t cap, uint64_t* n_out) {
+    return guarded([&] {
+        need(g, "gcmc");
+        const uint64_t n = alea::gcmc_guest_sites(g->impl, chain, xyzq, lj_species, cap);
+        if (n_out) *n_out = n;
+    });
+}
+
 alea_status alea_gcmc_ewald_energy(const alea_gcmc* g, uint32_t chain, double* out) {
     return guarded([&] {
         need(g, "gcmc");

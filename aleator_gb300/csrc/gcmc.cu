@@ -1293,6 +1293,31 @@ uint64_t gcmc_particles(const GcmcImpl* g, uint32_t chain, double* xyz, uint64_t
     return n;
 }
 
+// One chain's guest sites (engine order): x, y, z, charge and LJ species.
+uint64_t gcmc_guest_sites(const GcmcImpl* g, uint32_t chain, double* xyzq, uint32_t* lj_species,
+                          uint64_t cap) {
+    require(chain < g->n_chains, ALEA_ERR_OUT_OF_RANGE, "GCMC: chain index");
+    ChainState s;
+    ALEA_CUDA(cudaMemcpy(&s, g->st.p + chain, sizeof s, cudaMemcpyDeviceToHost));
+    const uint64_t n = s.n_guest;
+    if (xyzq && lj_species && cap >= n && n > 0) {
+        const size_t so = (size_t)chain * g->C.max_sites;
+        std::vector<double> x(n), y(n), z(n), q(n);
+        ALEA_CUDA(cudaMemcpy(x.data(), g->gx.p + so, n * 8, cudaMemcpyDeviceToHost));
+        ALEA_CUDA(cudaMemcpy(y.data(), g->gy.p + so, n * 8, cudaMemcpyDeviceToHost));
+        ALEA_CUDA(cudaMemcpy(z.data(), g->gz.p + so, n * 8, cudaMemcpyDeviceToHost));
+        ALEA_CUDA(cudaMemcpy(q.data(), g->gq.p + so, n * 8, cudaMemcpyDeviceToHost));
+        ALEA_CUDA(cudaMemcpy(lj_species, g->gt.p + so, n * 4, cudaMemcpyDeviceToHost));
+        for (uint64_t i = 0; i < n; ++i) {
+            xyzq[4 * i] = x[i];
+            xyzq[4 * i + 1] = y[i];
+            xyzq[4 * i + 2] = z[i];
+            xyzq[4 * i + 3] = q[i];
+        }
+    }
+    return n;
+}
+
 // committedEnergy() of one chain's cache (ewald_incremental_state.cc:85-93)
 double gcmc_ewald_energy(const GcmcImpl* g, uint32_t chain) {
     require(chain < g->n_chains, ALEA_ERR_OUT_OF_RANGE, "GCMC: chain index");

@@ -157,6 +157,8 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
 void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s);
 void gcmc_states(const GcmcImpl* g, ChainState* out);
 uint64_t gcmc_particles(const GcmcImpl* g, uint32_t chain, double* xyz, uint64_t cap);
+uint64_t gcmc_guest_sites(const GcmcImpl* g, uint32_t chain, double* xyzq, uint32_t* lj_species,
+                          uint64_t cap);
 double gcmc_ewald_energy(const GcmcImpl* g, uint32_t chain);
 void gcmc_set_proposal(GcmcImpl* g, const ProposalTable* t);
 void gcmc_set_precision(GcmcImpl* g, int precision);

@@ -456,6 +456,12 @@ alea_status alea_gcmc_chain_info_get(const alea_gcmc* g, uint32_t chain, alea_gc
  * sites in the engine's particle order; n_out = count. */
 alea_status alea_gcmc_particles(const alea_gcmc* g, uint32_t chain, double* xyz, uint64_t cap,
                                 uint64_t* n_out);
+/* One chain's guest sites in the engine's order: 4 doubles each (x, y, z,
+ * charge) and the LJ species; when cap is below the count only n_out is set.
+ * (No single reference call: the engine's particles() restricted to guests,
+ * with their charges and species.) */
+alea_status alea_gcmc_guest_sites(const alea_gcmc* g, uint32_t chain, double* xyzq,
+                                  uint32_t* lj_species, uint64_t cap, uint64_t* n_out);
 /* electrostaticEnergyForTesting() (monte_carlo_engine.hpp:214, .cc:928-930). */
 alea_status alea_gcmc_ewald_energy(const alea_gcmc* g, uint32_t chain, double* out);
 alea_status alea_gcmc_destroy(alea_gcmc* g);

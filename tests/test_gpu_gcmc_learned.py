@@ -88,3 +88,60 @@ def test_learned_loading_matches_uniform(lib, orc):
     se = np.hypot(mu.std(ddof=1), ml.std(ddof=1)) / np.sqrt(n)
     assert mu.mean() > 0.5  # an adsorbing state point
     assert abs(ml.mean() - mu.mean()) <= 3 * se, (ml.mean(), mu.mean(), se)
+
+
+def test_guest_sites_export(lib):
+    """Each chain's guest sites: the tail of particles(), with the template's
+    charges and LJ species."""
+    A, _ = lib
+    fw = W.cubic_framework(seed=12, charged=True)
+    fw.charge = fw.charge * 0.15
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    guest = W.co2_guest(fw)
+    fug = A.peng_robinson_fugacity(*W.CO2_CRITICAL, T, 1e6)
+    ch = A.GcmcChains(ff, p, fw.lattice, guest, T, [fug] * 2, [3, 4], [0, 0],
+                      ewald=A.Ewald(0.31, 12.0, 5), precision=A.FP32)
+    ch.run(3000)
+    for c in range(2):
+        sites, sp = ch.guest_sites(c)
+        nm = ch.molecules(c)
+        assert nm > 0 and sites.shape == (3 * nm, 4) and sp.shape == (3 * nm,)
+        assert np.array_equal(sites[:, :3], ch.positions(c)[len(fw.x):])
+        qs = dict(zip(np.asarray(guest["lj_species"]).tolist(), np.asarray(guest["charge"]).tolist()))
+        assert np.allclose(sites[:, 3], [qs[int(t)] for t in sp])
+        assert sorted(np.unique(sp).tolist()) == sorted(set(qs))
+
+
+def test_fit_at_loading_keeps_the_loading(lib, orc):
+    """A proposal refitted on Widom trials in the loaded state (framework plus
+    the chains' adsorbed guests): chains inserting with it keep the uniform
+    chains' mean loading (within 3 combined standard errors)."""
+    A, _ = lib
+    fw = W.cubic_framework(seed=11)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    guest = W.ch4_guest(fw)
+    fug = orc.pr_fugacity(*W.METHANE_CRITICAL, T, 1e6)
+    n = 48
+    out = {}
+    for name in ("uniform", "learned"):
+        ch = A.GcmcChains(ff, p, fw.lattice, guest, T, [fug] * n, list(range(700, 700 + n)),
+                          [1] * n, max_molecules=400, precision=A.FP32)
+        ch.run(10000)
+        if name == "learned":
+            P = A.Proposal(seed=3)
+            P.fit_at_loading(ch, ff, p, fw.lattice, guest, T, chain_ids=range(4), n_samples=1 << 16,
+                             rounds=2, epochs=15, cells=32)
+            lp = P.log_density(PO.cell_centres(32))
+            assert abs(np.exp(lp).mean() - 1.0) <= 1e-9
+            ch.set_proposal(P)
+        ch.run(10000)
+        before = [ch.info(c)["sum_molecules"] for c in range(n)]
+        steps = 30000
+        ch.run(steps)
+        out[name] = np.array([(ch.info(c)["sum_molecules"] - before[c]) / steps for c in range(n)])
+    mu, ml = out["uniform"], out["learned"]
+    se = np.hypot(mu.std(ddof=1), ml.std(ddof=1)) / np.sqrt(n)
+    assert mu.mean() > 0.5
+    assert abs(ml.mean() - mu.mean()) <= 3 * se, (ml.mean(), mu.mean(), se)
