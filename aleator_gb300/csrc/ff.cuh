@@ -52,4 +52,30 @@ __host__ __device__ __forceinline__ ff ff_from(double v) {
     return ff{h, (float)(v - (double)h)};
 }
 
+// A displacement (double-float per component) brought to its image within a
+// cutoff rc <= L_perp/2: the lattice shifts are chosen from the hi parts in
+// FP32 (any pair within rc has a clear choice) and taken off in double-float,
+// so the result keeps ~48 bits however far the image moved. lh/ll: the rows
+// a_i as hi + lo (row-major 3x3), inv: the inverse (f = d . inv), ortho: the
+// cell is orthorhombic.
+__device__ __forceinline__ void ff_min_image(const float* lh, const float* ll, const float* inv,
+                                             int ortho, ff& x, ff& y, ff& z) {
+    if (ortho) {
+        const float n0 = rintf(x.hi * inv[0]), n1 = rintf(y.hi * inv[4]), n2 = rintf(z.hi * inv[8]);
+        x = ff_add(x, ff_scale(-n0, ff{lh[0], ll[0]}));
+        y = ff_add(y, ff_scale(-n1, ff{lh[4], ll[4]}));
+        z = ff_add(z, ff_scale(-n2, ff{lh[8], ll[8]}));
+        return;
+    }
+    float n[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) n[a] = rintf(fmaf(x.hi, inv[a], fmaf(y.hi, inv[3 + a], z.hi * inv[6 + a])));
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        x = ff_add(x, ff_scale(-n[a], ff{lh[3 * a], ll[3 * a]}));
+        y = ff_add(y, ff_scale(-n[a], ff{lh[3 * a + 1], ll[3 * a + 1]}));
+        z = ff_add(z, ff_scale(-n[a], ff{lh[3 * a + 2], ll[3 * a + 2]}));
+    }
+}
+
 }  // namespace alea

@@ -162,31 +162,6 @@ __device__ void block_sum_ff(ff* v, int n, double* red) {
     __syncthreads();
 }
 
-// A displacement (double-float per component) brought to its image within the
-// cutoff: the lattice shifts are chosen from the hi parts in FP32 (any pair
-// within rc <= L_perp/2 has a clear choice) and taken off in double-float, so
-// the result carries ~48 bits however far the image moved.
-__device__ __forceinline__ void wrap_ff(const GcmcConst& C, ff& x, ff& y, ff& z) {
-    if (C.L.ortho) {
-        const float n0 = rintf(x.hi * C.linv[0]), n1 = rintf(y.hi * C.linv[4]),
-                    n2 = rintf(z.hi * C.linv[8]);
-        x = ff_add(x, ff_scale(-n0, ff{C.lh[0], C.ll[0]}));
-        y = ff_add(y, ff_scale(-n1, ff{C.lh[4], C.ll[4]}));
-        z = ff_add(z, ff_scale(-n2, ff{C.lh[8], C.ll[8]}));
-        return;
-    }
-    float n[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-        n[a] = rintf(fmaf(x.hi, C.linv[a], fmaf(y.hi, C.linv[3 + a], z.hi * C.linv[6 + a])));
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        x = ff_add(x, ff_scale(-n[a], ff{C.lh[3 * a], C.ll[3 * a]}));
-        y = ff_add(y, ff_scale(-n[a], ff{C.lh[3 * a + 1], C.ll[3 * a + 1]}));
-        z = ff_add(z, ff_scale(-n[a], ff{C.lh[3 * a + 2], C.ll[3 * a + 2]}));
-    }
-}
-
 __device__ __forceinline__ double u01(ChainState& c) {
     return philox_uniform(c.seed, c.stream, c.call++);
 }
@@ -563,7 +538,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         ff dx = ff_add(ff{ah.x, al.x}, ff{-ph.x, -pl.x});
                         ff dy = ff_add(ff{ah.y, al.y}, ff{-ph.y, -pl.y});
                         ff dz = ff_add(ff{ah.z, al.z}, ff{-ph.z, -pl.z});
-                        wrap_ff(C, dx, dy, dz);
+                        ff_min_image(C.lh, C.ll, C.linv, C.L.ortho, dx, dy, dz);
                         const float r2 = fmaf(dx.hi, dx.hi, fmaf(dy.hi, dy.hi, dz.hi * dz.hi));
                         const bool lj_in = r2 <= rc2f;
                         const bool el_in = C.charged && r2 <= rce2f;

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "ff.cuh"
 #include "grid.cuh"
 
 namespace alea {
@@ -55,10 +56,17 @@ struct WidomParams {
     int n_rows;
     double b[9];
     double self_pref, rec_pref;
+    float lh[9], ll[9], linv[9];  // FP32 form: rows a_i as hi + lo; the inverse
 };
 
 struct KRow {
     int n0, n1, m, t0;
+};
+
+// FP32 form: a site's pair terms with one framework type: 4 eps sigma^12,
+// 4 eps sigma^6, the shift terms, and sigma^2 below which the pair stays FP64.
+struct PairF32W {
+    float a, b, shift, dvdrc, sig2;
 };
 
 // cross(qv, v) with non-contracted arithmetic (monte_carlo_engine.cc:25-27)
@@ -98,12 +106,20 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
     __shared__ double4 tile[ATILE];
     __shared__ uint32_t ttype[ATILE];
     __shared__ PairParams pp[MAXS * MAXT];
+    __shared__ PairF32W ppf[sizeof(Real) == 4 ? MAXS * MAXT : 1];
     __shared__ double red[WT];
 
     const int ns = P.n_sites;
     for (int i = threadIdx.x; i < ns * (int)P.n_species; i += WT) {
         const int s = i / P.n_species, t = i % P.n_species;
-        pp[s * MAXT + t] = table[(size_t)P.site[s].lj * P.n_species + t];
+        const PairParams q = table[(size_t)P.site[s].lj * P.n_species + t];
+        pp[s * MAXT + t] = q;
+        if constexpr (sizeof(Real) == 4) {
+            const double s2 = q.sigma * q.sigma, s6 = s2 * s2 * s2;
+            ppf[s * MAXT + t] = PairF32W{(float)(4.0 * q.eps * s6 * s6), (float)(4.0 * q.eps * s6),
+                                         P.trunc != ALEA_TRUNCATED ? (float)q.shift : 0.f,
+                                         (float)q.dvdrc, (float)s2};
+        }
     }
 
     const uint64_t local = block * WT + threadIdx.x;
@@ -194,7 +210,15 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
         __syncthreads();
         const int cnt = (int)min((uint64_t)ATILE, P.n_atoms - base);
         for (int i = threadIdx.x; i < cnt; i += WT) {
-            tile[i] = atoms[base + i];
+            const double4 a = atoms[base + i];
+            if (sizeof(Real) == 8) {
+                tile[i] = a;
+            } else {  // {x, y, z hi, charge}, {x, y, z lo, 0} as double-float
+                const ff x = ff_from(a.x), y = ff_from(a.y), z = ff_from(a.z);
+                float4* t4 = reinterpret_cast<float4*>(&tile[i]);
+                t4[0] = make_float4(x.hi, y.hi, z.hi, (float)a.w);
+                t4[1] = make_float4(x.lo, y.lo, z.lo, 0.f);
+            }
             ttype[i] = types[base + i];
         }
         __syncthreads();
@@ -204,35 +228,50 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
             Real lj_acc = 0, es_acc = 0;
             double lj_close = 0.0;
             const PairParams* row = pp + s * MAXT;
-            for (int j = 0; j < cnt; ++j) {
-                const double4 a = tile[j];
-                double dx, dy, dz;
-                min_image(P.L, a.x - sx[s], a.y - sy[s], a.z - sz[s], dx, dy, dz);
-                const double r2 = dx * dx + dy * dy + dz * dz;
-                if (sizeof(Real) == 8) {
+            if constexpr (sizeof(Real) == 8) {
+                for (int j = 0; j < cnt; ++j) {
+                    const double4 a = tile[j];
+                    double dx, dy, dz;
+                    min_image(P.L, a.x - sx[s], a.y - sy[s], a.z - sz[s], dx, dy, dz);
+                    const double r2 = dx * dx + dy * dy + dz * dz;
                     const double r = sqrt(r2);
                     lj_acc += lj_pair_rt(P.trunc, r, P.rc, row[ttype[j]]);
                     if (P.charged && r <= P.rc_ewald) es_acc += a.w * (erfc(P.alpha * r) / r);
-                } else {
-                    const float rf = sqrtf((float)r2);
-                    const PairParams& pc = row[ttype[j]];
-                    if (r2 < pc.sigma * pc.sigma) {
+                }
+            } else {
+                // the displacement formed and brought to its image in
+                // double-float, rounded to FP32 once; FP32 pair terms
+                const ff px = ff_from(sx[s]), py = ff_from(sy[s]), pz = ff_from(sz[s]);
+                const float rc2f = (float)P.rc2, rcf = (float)P.rc, alphaf = (float)P.alpha,
+                            rce2f = (float)(P.rc_ewald * P.rc_ewald);
+                const PairF32W* rowf = ppf + s * MAXT;
+                for (int j = 0; j < cnt; ++j) {
+                    const float4* t4 = reinterpret_cast<const float4*>(&tile[j]);
+                    const float4 ah = t4[0], al = t4[1];
+                    ff dx = ff_add(ff{ah.x, al.x}, ff{-px.hi, -px.lo});
+                    ff dy = ff_add(ff{ah.y, al.y}, ff{-py.hi, -py.lo});
+                    ff dz = ff_add(ff{ah.z, al.z}, ff{-pz.hi, -pz.lo});
+                    ff_min_image(P.lh, P.ll, P.linv, P.L.ortho, dx, dy, dz);
+                    const float r2 = fmaf(dx.hi, dx.hi, fmaf(dy.hi, dy.hi, dz.hi * dz.hi));
+                    const uint32_t ty = ttype[j];
+                    const PairF32W q = rowf[ty];
+                    if (r2 < q.sig2) {
                         // rare close pair (r < sigma): its repulsive term reaches
                         // 1e4 K, kept in FP64 so its rounding stays below 1e-6 K
-                        lj_close += lj_pair_rt(P.trunc, sqrt(r2), P.rc, pc);
-                    } else if (r2 <= P.rc2) {
-                        const PairParams& p = pc;
-                        const float sr = (float)p.sigma / rf;
-                        const float sr2 = sr * sr;
-                        const float sr6 = sr2 * sr2 * sr2;
-                        float e = 4.0f * (float)p.eps * (sr6 * sr6 - sr6);
-                        if (P.trunc != ALEA_TRUNCATED) e -= (float)p.shift;
-                        if (P.trunc == ALEA_LINEAR_FORCE_SHIFTED)
-                            e -= (rf - (float)P.rc) * (float)p.dvdrc;
+                        const double ex = (double)dx.hi + dx.lo, ey = (double)dy.hi + dy.lo,
+                                     ez = (double)dz.hi + dz.lo;
+                        lj_close += lj_pair_rt(P.trunc, sqrt(ex * ex + ey * ey + ez * ez), P.rc, row[ty]);
+                    } else if (r2 <= rc2f) {
+                        const float ir2 = 1.0f / r2;
+                        const float ir6 = ir2 * ir2 * ir2;
+                        float e = ir6 * fmaf(q.a, ir6, -q.b) - q.shift;
+                        if (P.trunc == ALEA_LINEAR_FORCE_SHIFTED) e -= (sqrtf(r2) - rcf) * q.dvdrc;
                         lj_acc += e;
                     }
-                    if (P.charged && rf <= (float)P.rc_ewald)
-                        es_acc += (float)a.w * (erfcf((float)P.alpha * rf) / rf);
+                    if (P.charged && r2 <= rce2f) {
+                        const float rf = sqrtf(r2);
+                        es_acc += ah.w * (erfcf(alphaf * rf) / rf);
+                    }
                 }
             }
             lj_site[s] += (double)lj_acc + lj_close;
@@ -464,6 +503,12 @@ WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
     try {
         WidomParams& P = w->P;
         P.L = make_lattice(lat.m);
+        for (int i = 0; i < 9; ++i) {
+            const ff m = ff_from(P.L.m[i]);
+            P.lh[i] = m.hi;
+            P.ll[i] = m.lo;
+            P.linv[i] = (float)P.L.inv[i];
+        }
         validate_cutoff(P.L, lj.cutoff, "MonteCarloEngine (LJ)");
         P.n_atoms = fw.n;
         P.n_sites = (int)guest.n_sites;
