@@ -1467,6 +1467,42 @@ __global__ void grid_interpolate_kernel(Lattice L, int nx, int ny, int nz,
     out[i] = add_rn(mul_rn(c0, sub_rn(1.0, t[2])), mul_rn(c1, t[2]));
 }
 
+// Grids built in the FP32 form: the same trilinear interpolation with the
+// fractional transform as multiplies by the inverse cell (no IEEE divisions)
+// and fused lerps: about 40 FP64 operations per query instead of about 100,
+// within ~1e-12 relative of the reference form's value (not bit-equal).
+__global__ void grid_interpolate_fast_kernel(Lattice L, int nx, int ny, int nz,
+                                             const double* __restrict__ table,
+                                             const double* __restrict__ xyz, uint64_t n,
+                                             double* __restrict__ out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double px = xyz[3 * i], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
+    const int cnt[3] = {nx, ny, nz};
+    int i0[3], i1[3];
+    double t[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double f = fma(px, L.inv[a], fma(py, L.inv[3 + a], pz * L.inv[6 + a]));
+        f -= floor(f);
+        const double g = f * (double)cnt[a];
+        int base = (int)g;  // g >= 0
+        t[a] = g - (double)base;
+        if (base >= cnt[a]) base -= cnt[a];  // f rounded up to 1
+        i0[a] = base;
+        i1[a] = base + 1 == cnt[a] ? 0 : base + 1;
+    }
+    auto V = [&](int ix, int iy, int iz) {
+        return __ldg(&table[((size_t)iz * ny + iy) * nx + ix]);
+    };
+    auto lerp = [](double a, double b, double w) { return fma(w, b - a, a); };
+    const double c00 = lerp(V(i0[0], i0[1], i0[2]), V(i1[0], i0[1], i0[2]), t[0]);
+    const double c10 = lerp(V(i0[0], i1[1], i0[2]), V(i1[0], i1[1], i0[2]), t[0]);
+    const double c01 = lerp(V(i0[0], i0[1], i1[2]), V(i1[0], i0[1], i1[2]), t[0]);
+    const double c11 = lerp(V(i0[0], i1[1], i1[2]), V(i1[0], i1[1], i1[2]), t[0]);
+    out[i] = lerp(lerp(c00, c10, t[1]), lerp(c01, c11, t[1]), t[2]);
+}
+
 struct BuildArgs {
     const ImageRec* images;      // FP64 form
     const ImageRecF* images_f;   // FP32 form
@@ -1818,8 +1854,13 @@ void grid_interpolate_device(const GridImpl* g, uint32_t species, const double* 
     const double* tab = grid_table(g, species);
     if (n == 0) return;
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    grid_interpolate_kernel<<<blocks, 256, 0, s>>>(g->geo.L, g->geo.n[0], g->geo.n[1], g->geo.n[2],
-                                                  tab, xyz, n, out);
+    // the FP64 form reproduces the reference's arithmetic bit for bit
+    if (g->precision == ALEA_FP32)
+        grid_interpolate_fast_kernel<<<blocks, 256, 0, s>>>(g->geo.L, g->geo.n[0], g->geo.n[1],
+                                                           g->geo.n[2], tab, xyz, n, out);
+    else
+        grid_interpolate_kernel<<<blocks, 256, 0, s>>>(g->geo.L, g->geo.n[0], g->geo.n[1],
+                                                      g->geo.n[2], tab, xyz, n, out);
     ALEA_CUDA(cudaGetLastError());
 }
 

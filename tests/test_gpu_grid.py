@@ -81,6 +81,29 @@ def test_interpolation_bit_exact(lib):
         grid.interpolate(0, g["points"][:4])
 
 
+def test_fp32_form_interpolation_vs_oracle(lib, orc):
+    """Grids built in the FP32 form interpolate with multiplies by the inverse
+    cell and fused lerps: within 1e-10 x max(1 K, |E|) of the oracle's
+    reference-order interpolation of the same table (triclinic cell, points
+    inside and outside the cell, on nodes and on cell faces)."""
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    fw = W.triclinic_supercell(reps=1)
+    ff = A.LennardJones(fw.eps, fw.sigma, 10.0, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    sid = fw.guest_species["CH4"]
+    g32 = A.FrameworkEnergyGrid(ff, p, fw.lattice, [sid], 0.7, A.FP32)
+    m = np.asarray(fw.lattice).reshape(3, 3)
+    rng = np.random.default_rng(3)
+    f = np.concatenate([rng.uniform(-1.5, 2.5, (4000, 3)),
+                        np.floor(rng.uniform(0, 8, (200, 3))) / np.array(g32.point_counts())])
+    xyz = f @ m
+    ref = orc.grid_interpolate(m, g32.point_counts(), g32.table(sid), xyz)
+    got = g32.interpolate(sid, xyz)
+    assert np.isfinite(got).all()
+    assert rel_err(got, ref).max() <= 1e-10
+
+
 def test_cache_file_byte_identical_and_guards(lib):
     """framework_energy_grid.cc:290-409 and test_framework_energy_grid_cache.cc:
     the written file equals the reference's bytes (tables from the reference's
