@@ -52,6 +52,24 @@ __host__ __device__ __forceinline__ ff ff_from(double v) {
     return ff{h, (float)(v - (double)h)};
 }
 
+// FP32 forms, LJ pairs closer than sigma: sigma^2, 4 eps and the shift as
+// double-float (the repulsive term reaches 1e4 K there, where FP32 rounding
+// would leave ~1e-2 K).
+struct PairCloseFF {
+    float sig2h, sig2l, eps4h, eps4l, shifth, shiftl, dvdrc, pad;
+};
+
+// pairEnergy (lennard_jones.cc:70-86) in double-float from r^2 (trunc: the
+// alea truncation code; the shift is 0 for plain truncation).
+__device__ __forceinline__ ff lj_close_ff(const PairCloseFF& q, ff rr, float rcf, int trunc) {
+    const ff s2 = ff_mul(ff{q.sig2h, q.sig2l}, ff_rcp(rr));
+    const ff s6 = ff_mul(ff_mul(s2, s2), s2);
+    ff e = ff_mul(ff{q.eps4h, q.eps4l}, ff_mul(s6, ff_add(s6, ff{-1.f, 0.f})));
+    e = ff_add(e, ff{-q.shifth, -q.shiftl});
+    if (trunc == ALEA_LINEAR_FORCE_SHIFTED) e = ff_add_f(e, -(sqrtf(rr.hi) - rcf) * q.dvdrc);
+    return e;
+}
+
 // A displacement (double-float per component) brought to its image within a
 // cutoff rc <= L_perp/2: the lattice shifts are chosen from the hi parts in
 // FP32 (any pair within rc has a clear choice) and taken off in double-float,

@@ -125,21 +125,6 @@ struct PairF32 {
     float a, b, shift, dvdrc, sig2;
 };
 
-// FP32 form, pairs closer than sigma: sigma^2, 4 eps and the shift as
-// double-float (their repulsive terms reach 1e4 K)
-struct PairCloseFF {
-    float sig2h, sig2l, eps4h, eps4l, shifth, shiftl, dvdrc, pad;
-};
-
-// pairEnergy (lennard_jones.cc:70-86) in double-float from r^2
-__device__ __forceinline__ ff lj_close_ff(const PairCloseFF& q, ff rr, float rcf, int trunc) {
-    const ff s2 = ff_mul(ff{q.sig2h, q.sig2l}, ff_rcp(rr));
-    const ff s6 = ff_mul(ff_mul(s2, s2), s2);
-    ff e = ff_mul(ff{q.eps4h, q.eps4l}, ff_mul(s6, ff_add(s6, ff{-1.f, 0.f})));
-    e = ff_add(e, ff{-q.shifth, -q.shiftl});
-    if (trunc == ALEA_LINEAR_FORCE_SHIFTED) e = ff_add_f(e, -(sqrtf(rr.hi) - rcf) * q.dvdrc);
-    return e;
-}
 
 // Block sum of n double-float values per thread (n <= 4*MAXS), in a fixed
 // order on the FP32 pipe (a warp tree, then the warps in order), rounded to

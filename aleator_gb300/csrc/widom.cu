@@ -105,20 +105,25 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
     const double* __restrict__ sim = D.sim;
     __shared__ double4 tile[ATILE];
     __shared__ uint32_t ttype[ATILE];
-    __shared__ PairParams pp[MAXS * MAXT];
+    __shared__ PairParams pp[sizeof(Real) == 8 ? MAXS * MAXT : 1];
     __shared__ PairF32W ppf[sizeof(Real) == 4 ? MAXS * MAXT : 1];
+    __shared__ PairCloseFF ppc[sizeof(Real) == 4 ? MAXS * MAXT : 1];
     __shared__ double red[WT];
 
     const int ns = P.n_sites;
     for (int i = threadIdx.x; i < ns * (int)P.n_species; i += WT) {
         const int s = i / P.n_species, t = i % P.n_species;
         const PairParams q = table[(size_t)P.site[s].lj * P.n_species + t];
-        pp[s * MAXT + t] = q;
-        if constexpr (sizeof(Real) == 4) {
+        if constexpr (sizeof(Real) == 8) {
+            pp[s * MAXT + t] = q;
+        } else {
             const double s2 = q.sigma * q.sigma, s6 = s2 * s2 * s2;
+            const double sh = P.trunc != ALEA_TRUNCATED ? q.shift : 0.0;
             ppf[s * MAXT + t] = PairF32W{(float)(4.0 * q.eps * s6 * s6), (float)(4.0 * q.eps * s6),
-                                         P.trunc != ALEA_TRUNCATED ? (float)q.shift : 0.f,
-                                         (float)q.dvdrc, (float)s2};
+                                         (float)sh, (float)q.dvdrc, (float)s2};
+            const ff fs2 = ff_from(s2), fe4 = ff_from(4.0 * q.eps), fsh = ff_from(sh);
+            ppc[s * MAXT + t] = PairCloseFF{fs2.hi, fs2.lo, fe4.hi, fe4.lo, fsh.hi, fsh.lo,
+                                            (float)q.dvdrc, 0.f};
         }
     }
 
@@ -227,7 +232,6 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
             if (s >= ns) break;
             Real lj_acc = 0, es_acc = 0;
             double lj_close = 0.0;
-            const PairParams* row = pp + s * MAXT;
             if constexpr (sizeof(Real) == 8) {
                 for (int j = 0; j < cnt; ++j) {
                     const double4 a = tile[j];
@@ -235,7 +239,7 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                     min_image(P.L, a.x - sx[s], a.y - sy[s], a.z - sz[s], dx, dy, dz);
                     const double r2 = dx * dx + dy * dy + dz * dz;
                     const double r = sqrt(r2);
-                    lj_acc += lj_pair_rt(P.trunc, r, P.rc, row[ttype[j]]);
+                    lj_acc += lj_pair_rt(P.trunc, r, P.rc, pp[s * MAXT + ttype[j]]);
                     if (P.charged && r <= P.rc_ewald) es_acc += a.w * (erfc(P.alpha * r) / r);
                 }
             } else {
@@ -245,6 +249,7 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                 const float rc2f = (float)P.rc2, rcf = (float)P.rc, alphaf = (float)P.alpha,
                             rce2f = (float)(P.rc_ewald * P.rc_ewald);
                 const PairF32W* rowf = ppf + s * MAXT;
+                ff close_acc{0.f, 0.f};
                 for (int j = 0; j < cnt; ++j) {
                     const float4* t4 = reinterpret_cast<const float4*>(&tile[j]);
                     const float4 ah = t4[0], al = t4[1];
@@ -256,11 +261,10 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                     const uint32_t ty = ttype[j];
                     const PairF32W q = rowf[ty];
                     if (r2 < q.sig2) {
-                        // rare close pair (r < sigma): its repulsive term reaches
-                        // 1e4 K, kept in FP64 so its rounding stays below 1e-6 K
-                        const double ex = (double)dx.hi + dx.lo, ey = (double)dy.hi + dy.lo,
-                                     ez = (double)dz.hi + dz.lo;
-                        lj_close += lj_pair_rt(P.trunc, sqrt(ex * ex + ey * ey + ez * ez), P.rc, row[ty]);
+                        // close pair (r < sigma): its repulsive term reaches 1e4 K,
+                        // in double-float so its rounding stays below 1e-6 K
+                        const ff rr = ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
+                        close_acc = ff_add(close_acc, lj_close_ff(ppc[s * MAXT + ty], rr, rcf, P.trunc));
                     } else if (r2 <= rc2f) {
                         const float ir2 = 1.0f / r2;
                         const float ir6 = ir2 * ir2 * ir2;
@@ -273,6 +277,7 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                         es_acc += ah.w * (erfcf(alphaf * rf) / rf);
                     }
                 }
+                lj_close = (double)close_acc.hi + (double)close_acc.lo;
             }
             lj_site[s] += (double)lj_acc + lj_close;
             es_site[s] += (double)es_acc;
@@ -435,8 +440,9 @@ struct WidomItem {
     ProposalTable tab;
 };
 
+// FP32: 3 CTAs per SM (at most 170 registers a thread)
 template <typename Real>
-__global__ void __launch_bounds__(WT)
+__global__ void __launch_bounds__(WT, sizeof(Real) == 4 ? 3 : 1)
 widom_batch_kernel(const WidomItem* __restrict__ items, int n_items, int draw_order) {
     __shared__ WidomParams Ps;
     __shared__ int item;

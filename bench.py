@@ -217,9 +217,14 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--workload", default="full", choices=["full", "small"],
                     help="small: 2x2x2 supercell for profiler captures (not a bench line)")
+    ap.add_argument("--kernel-case", default=None, choices=["gcmc", "widom", "interp"],
+                    help="one small case of a non-grid kernel for profiler captures, then exit "
+                         "(no bench line)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.kernel_case:
+        return kernel_case(args.kernel_case)
 
     import torch
     import aleator_gb300 as A
@@ -487,6 +492,55 @@ def gcmc_loading(A, torch, ff, p, fw, guest, ew, T, n=152, block=15000, blocks=2
                    "loading an insertion is accepted for few orientations, which a position-only "
                    "proposal cannot raise, so the learned proposal does not speed up the loading")
     return res
+
+
+def kernel_case(case):
+    """Small cases of the non-grid kernels for ncu captures (each a few
+    launches, tens of milliseconds):
+      gcmc:   152 FP32 charged-CO2 chains (kMax 10) in the charged 424-atom cell,
+              1 bar, a 2000-move launch then a 300-move launch;
+      widom:  2^20 FP32 CH4 trials (424-atom cell), then 2^16 FP64 charged-CO2
+              trials (kMax 10);
+      interp: 2^24 random queries on the FP32-form grid of the 2x2x2 supercell
+              (0.2 A, 174 MB table), then the same on its FP64-form grid."""
+    import torch
+    import aleator_gb300 as A
+    from aleator_gb300 import workloads as W
+    A.load_library()
+    if case == "gcmc":
+        fw = W.cubic_framework(charged=True)
+        alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
+        ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+        fug = A.peng_robinson_fugacity(*W.CO2_CRITICAL, 298.0, 1e5)
+        ch = A.GcmcChains(ff, A.ParticleData.from_framework(fw), fw.lattice, W.co2_guest(fw), 298.0,
+                          [fug] * 152, list(range(152)), [0] * 152, ewald=A.Ewald(alpha, 12.0, kmax),
+                          max_molecules=600, precision=A.FP32)
+        ch.run(2000)
+        ch.run(300)
+    elif case == "widom":
+        fw = W.cubic_framework()
+        ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+        A.Widom(ff, A.ParticleData.from_framework(fw), fw.lattice, W.ch4_guest(fw), 298.0,
+                precision=A.FP32).run(42, 0, 1 << 20)
+        fq = W.cubic_framework(charged=True)
+        alpha, kmax = W.ewald_parameters(fq.lattice, 12.0)
+        A.Widom(A.LennardJones(fq.eps, fq.sigma, 12.8, A.SHIFTED), A.ParticleData.from_framework(fq),
+                fq.lattice, W.co2_guest(fq), 298.0, ewald=A.Ewald(alpha, 12.0, kmax)).run(42, 0, 1 << 16)
+    else:
+        fw, guests = make_workload(2)
+        ff = A.LennardJones(fw.eps, fw.sigma, CUTOFF, A.SHIFTED)
+        n = 1 << 24
+        xyz = (torch.rand(n, 3, dtype=torch.float64, device="cuda")
+               @ torch.tensor(fw.lattice, device="cuda")).contiguous()
+        res = torch.empty(n, dtype=torch.float64, device="cuda")
+        for prec in (A.FP32, A.FP64):
+            g = A.FrameworkEnergyGrid(ff, A.ParticleData.from_framework(fw), fw.lattice, guests[:1],
+                                      SPACING, prec)
+            g.interpolate_device(guests[0], xyz.data_ptr(), n, res.data_ptr(), 0)
+            del g
+    torch.cuda.synchronize()
+    print(f"kernel case {case}: done")
+    return 0
 
 
 def batched_screening(A, torch, n_frameworks=256, trials=100_000):
