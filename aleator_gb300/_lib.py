@@ -207,6 +207,7 @@ _SIGNATURES = {
     "alea_gcmc_destroy": (ctypes.c_int32, [_VP]),
     "alea_gcmc_set_proposal": (ctypes.c_int32, [_VP, _VP]),
     "alea_gcmc_set_precision": (ctypes.c_int32, [_VP, ctypes.c_int32]),
+    "alea_gcmc_set_grid": (ctypes.c_int32, [_VP, _VP]),
     "alea_gcmc_guest_sites": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D, ctypes.POINTER(ctypes.c_uint32),
                                                ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
     "alea_grid_batch_create": (ctypes.c_int32, [ctypes.c_uint32, ctypes.POINTER(_LJ),
@@ -988,6 +989,13 @@ class GcmcChains:
                                           ctypes.byref(self._h)))
         if precision is not None:
             self.set_precision(precision)
+
+    def set_grid(self, grid):
+        """Dispersion from a FrameworkEnergyGrid of this cell (kept alive here)
+        plus the guests' LJ, as the reference engine with its grid; None
+        restores the direct scan."""
+        _check(self._lib.alea_gcmc_set_grid(self._h, grid._h if grid is not None else None))
+        self._grid = grid
 
     def set_precision(self, precision):
         """FP64 (the reference's arithmetic) or FP32 (FP32 pair terms and

@@ -714,6 +714,13 @@ alea_status alea_gcmc_set_proposal(alea_gcmc* g, const alea_proposal* p) {
     });
 }
 
+alea_status alea_gcmc_set_grid(alea_gcmc* g, const alea_grid* grid) {
+    return guarded([&] {
+        need(g, "gcmc");
+        alea::gcmc_set_grid(g->impl, grid ? grid->impl : nullptr);
+    });
+}
+
 alea_status alea_gcmc_set_precision(alea_gcmc* g, int32_t precision) {
     return guarded([&] {
         need(g, "gcmc");

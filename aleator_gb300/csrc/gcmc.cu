@@ -75,6 +75,10 @@ struct GcmcConst {
     int f32;  // ALEA_FP32 form: FP32 pair and real-space terms, FP32 per-term S(k) deltas
     float lh[9], ll[9], linv[9];  // FP32 form: rows a_i as hi + lo; the inverse (f = d . inv)
     double excl_tmpl;  // FP32 form: pairExclusionSum of the rigid template (any position)
+    // the engine's frameworkEnergyGrid (grid == 0: none): a site's dispersion
+    // is its species' interpolated table plus the LJ with the guests
+    int grid, grid_fast;
+    int gn[3];
 };
 
 struct GcmcPtrs {
@@ -102,6 +106,7 @@ struct GcmcPtrs {
     // S(k) (refreshed on every commit and resync), FP32 per-term deltas
     const float* w32;
     float *sre32, *sim32, *dre32, *dim32;
+    const double* gtab[MAXS];  // per site: its LJ species' grid table
 };
 
 struct StepShared {
@@ -400,6 +405,18 @@ __device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, 
     S.n_new = ns;
 }
 
+// The grid's value at site slot e (old sites first, then new): its LJ
+// species' table interpolated at the site (frameworkEnergyGrid_->interpolate,
+// monte_carlo_engine.cc:353-356).
+template <int NS>
+__device__ __forceinline__ double site_grid_energy(const GcmcConst& C, const GcmcPtrs& P,
+                                                   const StepShared& S, int e) {
+    const int s = e < NS ? e : e - NS;
+    const double* p = e < NS ? S.op[s] : S.np_[s];
+    return C.grid_fast ? grid_interp_fast(C.L, C.gn[0], C.gn[1], C.gn[2], P.gtab[s], p[0], p[1], p[2])
+                       : grid_interp_ref(C.L, C.gn[0], C.gn[1], C.gn[2], P.gtab[s], p[0], p[1], p[2]);
+}
+
 // F32: the FP32 form. Its per-site phase tables (FP32, in dynamic shared
 // memory): e^{i n theta_a} per slot, axis and n, then
 // q e^{i (n0 theta_0 + n1 theta_1)} per slot and (n0, n1).
@@ -480,6 +497,9 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
         if (S.valid) {
             const int n_old = S.n_old, n_new = S.n_new;
             const uint64_t n_all = C.n_fw + S.ng;
+            // with a grid the framework's LJ comes from the tables: its atoms
+            // are visited only for the real-space Ewald terms
+            const uint64_t j0 = (C.grid && !C.charged) ? C.n_fw : 0;
             // ---- LJ and real-space sums of old sites (e < NS) and new sites (e >= NS)
             double acc[4 * NS];
 #pragma unroll
@@ -495,7 +515,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 for (int e = 0; e < 2 * NS; ++e) closef[e] = ff{0.f, 0.f};
                 const float rc2f = (float)C.rc2, rcf = (float)C.rc, rce2f = (float)C.rc_ew2,
                             alphaf = (float)C.alpha;
-                for (uint64_t j = threadIdx.x; j < n_all; j += GT) {
+                for (uint64_t j = j0 + threadIdx.x; j < n_all; j += GT) {
                     bool skip = false;
                     if (n_old)
 #pragma unroll
@@ -525,7 +545,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         ff dz = ff_add(ff{ah.z, al.z}, ff{-ph.z, -pl.z});
                         ff_min_image(C.lh, C.ll, C.linv, C.L.ortho, dx, dy, dz);
                         const float r2 = fmaf(dx.hi, dx.hi, fmaf(dy.hi, dy.hi, dz.hi * dz.hi));
-                        const bool lj_in = r2 <= rc2f;
+                        const bool lj_in = !(C.grid && j < C.n_fw) && r2 <= rc2f;
                         const bool el_in = C.charged && r2 <= rce2f;
                         if (!lj_in && !el_in) continue;
                         if (lj_in) {
@@ -554,12 +574,18 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     v[2 * e] = ff_add_f(closef[e], accf[2 * e]);
                     v[2 * e + 1] = ff{accf[2 * e + 1], 0.f};
                 }
+                if (C.grid) {  // thread e adds site slot e's interpolated table
+#pragma unroll
+                    for (int e = 0; e < 2 * NS; ++e)
+                        if (threadIdx.x == e && (e < NS ? n_old : n_new))
+                            v[2 * e] = ff_add(v[2 * e], ff_from(site_grid_energy<NS>(C, P, S, e)));
+                }
                 block_sum_ff(v, 4 * NS, red);
 #pragma unroll
                 for (int e = 0; e < 4 * NS; ++e) acc[e] = red[(GT / 32) * RSTRIDE + e];
                 __syncthreads();
             } else
-            for (uint64_t j = threadIdx.x; j < n_all; j += GT) {
+            for (uint64_t j = j0 + threadIdx.x; j < n_all; j += GT) {
                 bool skip = false;
                 if (n_old)
 #pragma unroll
@@ -584,7 +610,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     double dx, dy, dz;
                     min_image(C.L, a.x - p[0], a.y - p[1], a.z - p[2], dx, dy, dz);
                     const double r2 = dx * dx + dy * dy + dz * dz;
-                    const bool lj_in = r2 <= C.rc2 * (1.0 + 1e-12);
+                    const bool lj_in = !(C.grid && j < C.n_fw) && r2 <= C.rc2 * (1.0 + 1e-12);
                     const bool el_in = C.charged && r2 <= C.rc_ew2 * (1.0 + 1e-12);
                     if (!lj_in && !el_in) continue;
                     const double r = sqrt(r2);
@@ -592,7 +618,15 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     if (el_in && r <= C.rc_ew) acc[2 * e + 1] += a.w * (erfc(C.alpha * r) / r);
                 }
             }
-            if constexpr (!F32) block_sum_n(acc, 4 * NS, red);
+            if constexpr (!F32) {
+                if (C.grid) {
+#pragma unroll
+                    for (int e = 0; e < 2 * NS; ++e)
+                        if (threadIdx.x == e && (e < NS ? n_old : n_new))
+                            acc[2 * e] += site_grid_energy<NS>(C, P, S, e);
+                }
+                block_sum_n(acc, 4 * NS, red);
+            }
             if (threadIdx.x == 0)
 #pragma unroll
                 for (int e = 0; e < 2 * NS; ++e) {
@@ -958,6 +992,7 @@ struct GcmcImpl {
     DevBuf<double> pcdf, plogp;  // the chains' copy of a tabulated proposal
     DevBuf<float4> fwh, fwl, ghi, glo;  // FP32 form: double-float positions
     DevBuf<float> w32, sre32, sim32, dre32, dim32;  // FP32 form: S(k) copies and deltas
+    const double* gtab[MAXS] = {};  // the borrowed grid's tables, per site
     float last_ms = 0.f;
 };
 
@@ -1196,6 +1231,7 @@ void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s) {
     P.ghi = g->ghi.p;
     P.glo = g->glo.p;
     P.w32 = g->w32.p;
+    for (int s = 0; s < MAXS; ++s) P.gtab[s] = g->gtab[s];
     P.sre32 = g->sre32.p;
     P.sim32 = g->sim32.p;
     P.dre32 = g->dre32.p;
@@ -1308,6 +1344,24 @@ void gcmc_set_proposal(GcmcImpl* g, const ProposalTable* t) {
     ALEA_CUDA(cudaMemcpy(g->plogp.p, t->logp, n * sizeof(double), cudaMemcpyDeviceToDevice));
     ALEA_CUDA(cudaDeviceSynchronize());
     g->C.prop_cells = t->cells;
+}
+
+// The engine's frameworkEnergyGrid (borrowed: it must outlive the chains'
+// runs), or none. Its cell must be the chains' and it must hold a table for
+// every site's LJ species.
+void gcmc_set_grid(GcmcImpl* g, const GridImpl* grid) {
+    if (!grid) {
+        g->C.grid = 0;
+        return;
+    }
+    const GridView v0 = grid_view(grid, g->C.slj[0]);
+    for (int i = 0; i < 9; ++i)
+        require(v0.L.m[i] == g->C.L.m[i], ALEA_ERR_INVALID_ARGUMENT,
+                "GCMC: the energy grid is for another cell");
+    for (int s = 0; s < g->C.ns; ++s) g->gtab[s] = grid_view(grid, g->C.slj[s]).table;
+    for (int a = 0; a < 3; ++a) g->C.gn[a] = v0.n[a];
+    g->C.grid_fast = v0.fast;
+    g->C.grid = 1;
 }
 
 // ALEA_FP64 (the parity form) or ALEA_FP32 for the next runs.

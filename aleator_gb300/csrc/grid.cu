@@ -1435,36 +1435,7 @@ __global__ void grid_interpolate_kernel(Lattice L, int nx, int ny, int nz,
                                         double* __restrict__ out) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double px = xyz[3 * i], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
-    double f[3];
-    f[0] = __ddiv_rn(dot_rn(L.c12, px, py, pz), L.volume);
-    f[1] = __ddiv_rn(dot_rn(L.c20, px, py, pz), L.volume);
-    f[2] = __ddiv_rn(dot_rn(L.c01, px, py, pz), L.volume);
-    const int cnt[3] = {nx, ny, nz};
-    int i0[3], i1[3];
-    double t[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        f[a] = sub_rn(f[a], floor(f[a]));
-        const double g = mul_rn(f[a], (double)cnt[a]);
-        const int base = (int)floor(g);
-        t[a] = sub_rn(g, (double)base);
-        const int w = ((base % cnt[a]) + cnt[a]) % cnt[a];
-        i0[a] = w;
-        i1[a] = (w + 1) % cnt[a];
-    }
-    auto V = [&](int ix, int iy, int iz) {
-        return __ldg(&table[((size_t)iz * ny + iy) * nx + ix]);
-    };
-    const double u0 = sub_rn(1.0, t[0]);
-    const double c00 = add_rn(mul_rn(V(i0[0], i0[1], i0[2]), u0), mul_rn(V(i1[0], i0[1], i0[2]), t[0]));
-    const double c10 = add_rn(mul_rn(V(i0[0], i1[1], i0[2]), u0), mul_rn(V(i1[0], i1[1], i0[2]), t[0]));
-    const double c01 = add_rn(mul_rn(V(i0[0], i0[1], i1[2]), u0), mul_rn(V(i1[0], i0[1], i1[2]), t[0]));
-    const double c11 = add_rn(mul_rn(V(i0[0], i1[1], i1[2]), u0), mul_rn(V(i1[0], i1[1], i1[2]), t[0]));
-    const double u1 = sub_rn(1.0, t[1]);
-    const double c0 = add_rn(mul_rn(c00, u1), mul_rn(c10, t[1]));
-    const double c1 = add_rn(mul_rn(c01, u1), mul_rn(c11, t[1]));
-    out[i] = add_rn(mul_rn(c0, sub_rn(1.0, t[2])), mul_rn(c1, t[2]));
+    out[i] = grid_interp_ref(L, nx, ny, nz, table, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
 }
 
 // Grids built in the FP32 form: the same trilinear interpolation with the
@@ -1477,30 +1448,7 @@ __global__ void grid_interpolate_fast_kernel(Lattice L, int nx, int ny, int nz,
                                              double* __restrict__ out) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double px = xyz[3 * i], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
-    const int cnt[3] = {nx, ny, nz};
-    int i0[3], i1[3];
-    double t[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        double f = fma(px, L.inv[a], fma(py, L.inv[3 + a], pz * L.inv[6 + a]));
-        f -= floor(f);
-        const double g = f * (double)cnt[a];
-        int base = (int)g;  // g >= 0
-        t[a] = g - (double)base;
-        if (base >= cnt[a]) base -= cnt[a];  // f rounded up to 1
-        i0[a] = base;
-        i1[a] = base + 1 == cnt[a] ? 0 : base + 1;
-    }
-    auto V = [&](int ix, int iy, int iz) {
-        return __ldg(&table[((size_t)iz * ny + iy) * nx + ix]);
-    };
-    auto lerp = [](double a, double b, double w) { return fma(w, b - a, a); };
-    const double c00 = lerp(V(i0[0], i0[1], i0[2]), V(i1[0], i0[1], i0[2]), t[0]);
-    const double c10 = lerp(V(i0[0], i1[1], i0[2]), V(i1[0], i1[1], i0[2]), t[0]);
-    const double c01 = lerp(V(i0[0], i0[1], i1[2]), V(i1[0], i0[1], i1[2]), t[0]);
-    const double c11 = lerp(V(i0[0], i1[1], i1[2]), V(i1[0], i1[1], i1[2]), t[0]);
-    out[i] = lerp(lerp(c00, c10, t[1]), lerp(c01, c11, t[1]), t[2]);
+    out[i] = grid_interp_fast(L, nx, ny, nz, table, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
 }
 
 struct BuildArgs {
@@ -1847,6 +1795,15 @@ static int table_index(const GridImpl* g, uint32_t species) {
 const double* grid_table(const GridImpl* g, uint32_t species) {
     const size_t nodes = (size_t)g->geo.n[0] * g->geo.n[1] * g->geo.n[2];
     return g->tables.p + (size_t)table_index(g, species) * nodes;
+}
+
+GridView grid_view(const GridImpl* g, uint32_t species) {
+    GridView v{};
+    v.L = g->geo.L;
+    for (int a = 0; a < 3; ++a) v.n[a] = g->geo.n[a];
+    v.table = grid_table(g, species);  // out_of_range as FrameworkEnergyGrid::interpolate
+    v.fast = g->precision == ALEA_FP32;
+    return v;
 }
 
 void grid_interpolate_device(const GridImpl* g, uint32_t species, const double* xyz, uint64_t n,

@@ -481,6 +481,14 @@ alea_status alea_gcmc_set_proposal(alea_gcmc* g, const struct alea_proposal* p);
  * S(k), the self and exclusion terms and the acceptance in FP64). No
  * counterpart in the reference. */
 alea_status alea_gcmc_set_precision(alea_gcmc* g, int32_t precision);
+/* MonteCarloEngine's frameworkEnergyGrid (monte_carlo_engine.hpp:76-83,
+ * .cc:341-374): from the next run on, a site's dispersion energy is its LJ
+ * species' table interpolated at the site plus the LJ with the guests (the
+ * framework atoms are then visited only for real-space Ewald). The grid is
+ * borrowed: it must stay alive while the chains run. Its cell must be the
+ * chains', with a table for every site species (else ALEA_ERR_OUT_OF_RANGE).
+ * NULL restores the direct scan. */
+alea_status alea_gcmc_set_grid(alea_gcmc* g, const alea_grid* grid);
 
 /* ------------------------------------------------------------------ acceptance / EOS (host) */
 /* gcmc::insertionRatio ... clampToProbability (engines/monte_carlo/gcmc_acceptance.hpp:28-101) */

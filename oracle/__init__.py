@@ -309,16 +309,20 @@ class Oracle:
         return self.lib.orc_pr_fugacity(tc, pc, omega, t, p)
 
     def gcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature, fugacity_pa, seed,
-             stream, max_translation=1.5, max_rotation=0.5, draw_order=DRAWS_RIGHT_TO_LEFT):
+             stream, max_translation=1.5, max_rotation=0.5, draw_order=DRAWS_RIGHT_TO_LEFT,
+             grid=None):
+        """grid: None, or {"counts": (nx, ny, nz), "tables": {species: table}}
+        on this cell (the engine's frameworkEnergyGrid)."""
         return OracleGcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature,
-                          fugacity_pa, seed, stream, max_translation, max_rotation, draw_order)
+                          fugacity_pa, seed, stream, max_translation, max_rotation, draw_order,
+                          grid)
 
 
 class OracleGcmc:
     """Single-species GCMC chain (MonteCarloEngine::run restated in C)."""
 
     def __init__(self, orc, ff, ewald, m, x, y, z, q, species, guest, temperature, fugacity_pa,
-                 seed, stream, max_translation, max_rotation, draw_order):
+                 seed, stream, max_translation, max_rotation, draw_order, grid=None):
         L = orc.lib
         self.L = L
         L.orc_gcmc_new.restype = ctypes.c_void_p
@@ -350,6 +354,15 @@ class OracleGcmc:
                                 _dp(y), _dp(z), _dp(q), _u32(fs), ctypes.byref(sp), temperature,
                                 fugacity_pa, max_translation, max_rotation, seed, stream,
                                 draw_order)
+        if grid is not None:
+            L.orc_gcmc_set_grid.argtypes = [ctypes.c_void_p, _I32, ctypes.c_uint32, _U32,
+                                            ctypes.POINTER(_D)]
+            self._tables = [(int(s), _f64(t)) for s, t in grid["tables"].items()]
+            ids = np.array([s for s, _ in self._tables], dtype=np.uint32)
+            ptrs = (_D * len(self._tables))(*[_dp(t) for _, t in self._tables])
+            counts = np.ascontiguousarray(grid["counts"], dtype=np.int32)
+            self._grid_keep = (ids, ptrs, counts)
+            L.orc_gcmc_set_grid(self.h, counts.ctypes.data_as(_I32), len(ids), _u32(ids), ptrs)
 
     def __del__(self):
         try:
@@ -514,6 +527,9 @@ class Reference:
                                       ctypes.c_uint32, _D, _D, _D, _U32, _D, ctypes.c_double,
                                       ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_uint64, ctypes.c_uint64]
+        L.ref_gcmc_create_grid.restype = ctypes.c_void_p
+        L.ref_gcmc_create_grid.argtypes = L.ref_gcmc_create.argtypes + [ctypes.c_double,
+                                                                          ctypes.c_uint32, _U32]
         L.ref_gcmc_run.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
         L.ref_gcmc_molecules.restype = ctypes.c_uint64
         L.ref_gcmc_molecules.argtypes = [ctypes.c_void_p]
@@ -650,16 +666,18 @@ class Reference:
         return self.lib.ref_pr_fugacity(tc, pc, omega, t, p)
 
     def gcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature, fugacity_pa, seed,
-             stream, max_translation=1.5, max_rotation=0.5):
+             stream, max_translation=1.5, max_rotation=0.5, grid=None):
+        """grid: None, or {"spacing": s, "species": [...]}: the engine gets the
+        reference's FrameworkEnergyGrid of those guest species."""
         return ReferenceGcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature,
-                             fugacity_pa, seed, stream, max_translation, max_rotation)
+                             fugacity_pa, seed, stream, max_translation, max_rotation, grid)
 
 
 class ReferenceGcmc:
     """MonteCarloEngine (the reference's own class) driven through the shim."""
 
     def __init__(self, ref, ff, ewald, m, x, y, z, q, species, guest, temperature, fugacity_pa,
-                 seed, stream, max_translation, max_rotation):
+                 seed, stream, max_translation, max_rotation, grid=None):
         self.ref = ref
         eps, sig = _f64(ff["eps"]), _f64(ff["sigma"])
         x, y, z = _f64(x), _f64(y), _f64(z)
@@ -671,13 +689,16 @@ class ReferenceGcmc:
         alpha = ewald["alpha"] if ewald else 0.0
         erc = ewald["rc"] if ewald else 0.0
         kmax = ewald["kmax"] if ewald else 0
-        self.h = ref.lib.ref_gcmc_create(_dp(_mat(m)), len(x), _dp(x), _dp(y), _dp(z), _dp(q),
-                                         _u32(sp), len(eps), _dp(eps), _dp(sig), ff["cutoff"],
-                                         ff.get("truncation", SHIFTED),
-                                         ff.get("mixing", LORENTZ_BERTHELOT), alpha, erc, kmax,
-                                         len(gx), _dp(gx), _dp(gy), _dp(gz), _u32(gs), _dp(gq),
-                                         temperature, fugacity_pa, max_translation, max_rotation,
-                                         seed, stream)
+        args = [_dp(_mat(m)), len(x), _dp(x), _dp(y), _dp(z), _dp(q), _u32(sp), len(eps), _dp(eps),
+                _dp(sig), ff["cutoff"], ff.get("truncation", SHIFTED),
+                ff.get("mixing", LORENTZ_BERTHELOT), alpha, erc, kmax, len(gx), _dp(gx), _dp(gy),
+                _dp(gz), _u32(gs), _dp(gq), temperature, fugacity_pa, max_translation,
+                max_rotation, seed, stream]
+        if grid is None:
+            self.h = ref.lib.ref_gcmc_create(*args)
+        else:
+            ids = np.ascontiguousarray(grid["species"], dtype=np.uint32)
+            self.h = ref.lib.ref_gcmc_create_grid(*args, grid["spacing"], len(ids), _u32(ids))
 
     def __del__(self):
         try:

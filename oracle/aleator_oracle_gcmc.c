@@ -3,12 +3,14 @@
  *
  * Plain-C restatement of MonteCarloEngine's single-species GCMC chain
  * (engines/monte_carlo/monte_carlo_engine.cc:159-439 run, :441-671 moves,
- * :814-848 removal), FP64, in the reference's operation order. No energy grid
- * (the direct-scan form): the reference's guest-guest cell-list candidates are
- * a superset of the guests within the cutoff visited in ascending index order
- * (monte_carlo_engine.cc:316-374), and pairEnergy beyond the cutoff is exactly
- * 0.0, so a full ascending scan over all particles gives the same sums bit for
- * bit; this port uses the full scan.
+ * :814-848 removal), FP64, in the reference's operation order. The
+ * reference's guest-guest cell-list candidates are a superset of the guests
+ * within the cutoff visited in ascending index order (monte_carlo_engine.cc:
+ * 316-374), and pairEnergy beyond the cutoff is exactly 0.0, so an ascending
+ * scan gives the same sums bit for bit; this port scans. Without an energy
+ * grid the scan covers every particle (framework first); with one, a site's
+ * dispersion is the grid's interpolation plus the scan over guests only
+ * (monte_carlo_engine.cc:353-372).
  */
 #include <math.h>
 #include <stdlib.h>
@@ -100,13 +102,49 @@ void orc_gcmc_free(orc_gcmc* g) {
     memset(g, 0, sizeof(*g));
 }
 
-/* moleculeDispersionEnergy (no grid) + moleculeElectrostaticRealSpaceEnergy
+/* computeParticleEnergyOverCandidates over the guests (indices from n_fw),
+ * ascending (lennard_jones.cc:179-209) */
+static double lj_over_guests(orc_gcmc* g, uint64_t index, const uint64_t* excluded, uint32_t n_ex) {
+    double energy = 0.0;
+    const double pi[3] = {g->x[index], g->y[index], g->z[index]};
+    for (uint64_t j = g->n_fw; j < g->n; ++j) {
+        if (j == index) continue;
+        int ex = 0;
+        for (uint32_t k = 0; k < n_ex; ++k) ex |= excluded[k] == j;
+        if (ex) continue;
+        double eps, sigma;
+        orc_lj_mixed(&g->lj, g->sp[index], g->sp[j], &eps, &sigma);
+        const double pj[3] = {g->x[j], g->y[j], g->z[j]};
+        double d[3];
+        orc_min_image(g->m, pi, pj, d);
+        energy += orc_lj_pair_energy(&g->lj, sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]), eps, sigma);
+    }
+    return energy;
+}
+
+/* moleculeDispersionEnergy + moleculeElectrostaticRealSpaceEnergy
  * (monte_carlo_engine.cc:299-314, 341-374) */
 static double dispersion(orc_gcmc* g, const uint64_t* idx) {
     double e = 0.0;
-    for (uint32_t s = 0; s < g->ns; ++s)
-        e += orc_lj_particle_energy(&g->lj, g->m, g->n, g->x, g->y, g->z, g->sp, idx[s], idx, g->ns);
+    for (uint32_t s = 0; s < g->ns; ++s) {
+        if (g->grid) {
+            const double p[3] = {g->x[idx[s]], g->y[idx[s]], g->z[idx[s]]};
+            e += orc_grid_interpolate(g->m, g->gcounts, g->gtab[g->sp[idx[s]]], p);
+            e += lj_over_guests(g, idx[s], idx, g->ns);
+        } else {
+            e += orc_lj_particle_energy(&g->lj, g->m, g->n, g->x, g->y, g->z, g->sp, idx[s], idx, g->ns);
+        }
+    }
     return e;
+}
+
+void orc_gcmc_set_grid(orc_gcmc* g, const int counts[3], uint32_t n_tables, const uint32_t* species,
+                       const double* const* tables) {
+    g->grid = n_tables > 0;
+    for (int i = 0; i < 64; ++i) g->gtab[i] = NULL;
+    for (int a = 0; a < 3; ++a) g->gcounts[a] = counts ? counts[a] : 0;
+    for (uint32_t i = 0; i < n_tables; ++i)
+        if (species[i] < 64) g->gtab[species[i]] = tables[i];
 }
 
 static double electro_real(orc_gcmc* g, const uint64_t* idx) {

@@ -34,6 +34,10 @@ typedef struct {
     uint64_t moves_since_resync, resyncs, steps;
     uint64_t attempted[4], accepted[4];
     double last_du;
+    /* optional energy grid (tables borrowed, one per LJ species or NULL) */
+    int grid;
+    int gcounts[3];
+    const double* gtab[64];
 } orc_gcmc;
 
 int orc_gcmc_create(orc_gcmc* g, const orc_lj* lj, const orc_ewald_params* ew, const double m[9],
@@ -54,6 +58,11 @@ uint64_t orc_gcmc_molecules(const orc_gcmc* g);
 uint64_t orc_gcmc_particles(const orc_gcmc* g, double* xyz, uint64_t cap);
 uint64_t orc_gcmc_calls(const orc_gcmc* g);
 void orc_gcmc_counters(const orc_gcmc* g, uint64_t* out8);
+/* MonteCarloEngine's frameworkEnergyGrid: per-species tables of a grid with
+ * `counts` nodes on the chain's cell (borrowed; NULL entries for species
+ * without a table); n_tables == 0 removes it. */
+void orc_gcmc_set_grid(orc_gcmc* g, const int counts[3], uint32_t n_tables, const uint32_t* species,
+                       const double* const* tables);
 
 #ifdef __cplusplus
 }

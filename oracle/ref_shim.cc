@@ -471,6 +471,31 @@ void* ref_gcmc_create(const double* m, uint64_t n, const double* x, const double
     return g;
 }
 
+// The same chain with the engine's shared FrameworkEnergyGrid built by the
+// reference from the same inputs (monte_carlo_engine.hpp:76-83).
+void* ref_gcmc_create_grid(const double* m, uint64_t n, const double* x, const double* y,
+                           const double* z, const double* q, const uint32_t* sp, uint32_t nSpecies,
+                           const double* eps, const double* sigma, double cutoff, int trunc,
+                           int mixing, double alpha, double ewaldRc, int kMax, uint32_t nSites,
+                           const double* sx, const double* sy, const double* sz, const uint32_t* sLj,
+                           const double* sq, double temperature, double fugacityPa, double maxTrans,
+                           double maxRot, uint64_t seed, uint64_t stream, double spacing,
+                           uint32_t nGrid, const uint32_t* gridSpecies) {
+    auto* g = new RefGcmc{latticeOf(m), nullptr};
+    const auto fw = particlesOf(n, x, y, z, q, sp);
+    auto lj = ljOf(nSpecies, eps, sigma, cutoff, trunc, mixing);
+    std::shared_ptr<forcefield::Ewald> ewald;
+    if (alpha > 0.0) ewald = std::make_shared<forcefield::Ewald>(alpha, ewaldRc, kMax);
+    const std::vector<uint32_t> ids(gridSpecies, gridSpecies + nGrid);
+    auto grid = std::make_shared<const engines::FrameworkEnergyGrid>(*lj, fw, g->lattice, ids, spacing);
+    auto rng = std::make_unique<core::Philox4x32Rng>();
+    rng->seed(seed, stream);
+    g->engine = std::make_unique<engines::MonteCarloEngine>(
+        fw, g->lattice, lj, std::move(rng), temperature, speciesOf(nSites, sx, sy, sz, sLj, sq),
+        fugacityPa, maxTrans, maxRot, ewald, grid);
+    return g;
+}
+
 void ref_gcmc_run(void* h, uint64_t steps) { static_cast<RefGcmc*>(h)->engine->run(steps); }
 
 uint64_t ref_gcmc_molecules(void* h) { return static_cast<RefGcmc*>(h)->engine->moleculeCount(); }

@@ -94,3 +94,56 @@ def test_capacity_is_reported(lib):
     with pytest.raises(A.AleatorError) as e:
         chains.run(2000)
     assert e.value.status == 6
+
+
+@pytest.mark.parametrize("charged", [False, True])
+def test_chain_with_energy_grid_matches_oracle(lib, orc, charged):
+    """The engine with its frameworkEnergyGrid (monte_carlo_engine.cc:341-374):
+    the GPU chain reads a GPU-built FP64 grid (within 1e-10 of the reference's
+    tables), the oracle the oracle's grid (bit-identical to the reference's,
+    tests/test_oracle_gcmc.py); same moves and decisions, positions within
+    1e-9 Å."""
+    A, _ = lib
+    fw = W.cubic_framework(seed=21, charged=charged)
+    if charged:
+        fw.charge = fw.charge * 0.15
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    ewd = dict(alpha=0.31, rc=12.0, kmax=5) if charged else None
+    ew = A.Ewald(0.31, 12.0, 5) if charged else None
+    guest = W.co2_guest(fw) if charged else W.ch4_guest(fw)
+    fug = orc.pr_fugacity(*(W.CO2_CRITICAL if charged else W.METHANE_CRITICAL), 298.0, 1e6)
+    species = sorted(set(int(s) for s in guest["lj_species"]))
+    grid = A.FrameworkEnergyGrid(ff, p, fw.lattice, species, 0.5, A.FP64)
+    od = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.8, truncation=O.SHIFTED)
+    tables = {s: orc.grid_build(od, fw.lattice, fw.x, fw.y, fw.z, fw.species, s, 0.5, threads=8)
+              for s in species}
+    gpu = A.GcmcChains(ff, p, fw.lattice, guest, 298.0, [fug], [9], [4], ewald=ew)
+    gpu.set_grid(grid)
+    cpu = orc.gcmc(od, ewd, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guest, 298.0, fug,
+                   9, 4, grid={"counts": grid.point_counts(), "tables": tables})
+    for _ in range(4):
+        gpu.run(300)
+        cpu.run(300)
+        _compare(gpu, cpu, charged=charged)
+    assert gpu.molecules() > 0
+
+
+def test_energy_grid_guards(lib):
+    A, _ = lib
+    fw = W.cubic_framework(seed=21)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    guest = W.ch4_guest(fw)
+    chains = A.GcmcChains(ff, p, fw.lattice, guest, 298.0, [1e5], [1], [0])
+    # a grid without the guest's species: out_of_range, as interpolate
+    g_wrong = A.FrameworkEnergyGrid(ff, p, fw.lattice, [fw.guest_species["CO2_C"]], 2.0, A.FP64)
+    with pytest.raises(IndexError):
+        chains.set_grid(g_wrong)
+    # a grid on another cell: invalid_argument
+    m2 = np.asarray(fw.lattice, dtype=float) * 1.01
+    g_cell = A.FrameworkEnergyGrid(ff, p, m2, [guest["lj_species"][0]], 2.0, A.FP64)
+    with pytest.raises(ValueError):
+        chains.set_grid(g_cell)
+    chains.set_grid(None)
+    chains.run(10)

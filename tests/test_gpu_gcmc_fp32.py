@@ -99,3 +99,28 @@ def test_fp32_loading_statistics_match_fp64(lib, orc):
     se = np.hypot(m64.std(ddof=1), m32.std(ddof=1)) / np.sqrt(n)
     assert m64.mean() > 1.0
     assert abs(m32.mean() - m64.mean()) <= 3 * se, (m32.mean(), m64.mean(), se)
+
+
+def test_fp32_with_energy_grid_matches_fp64_loading(lib, orc):
+    """Both forms reading an energy grid (FP32-form grid for the FP32 chains,
+    FP64-form grid for the FP64 chains): equal mean loadings."""
+    A, _ = lib
+    n = 64
+    fw = W.cubic_framework(seed=11)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    guest = W.ch4_guest(fw)
+    fug = orc.pr_fugacity(*W.METHANE_CRITICAL, KT, 5e6)
+    out = {}
+    for prec in (A.FP64, A.FP32):
+        grid = A.FrameworkEnergyGrid(ff, p, fw.lattice, [guest["lj_species"][0]], 0.3, prec)
+        ch = _chains(A, fw, guest, None, [fug] * n, list(range(40, 40 + n)), [3] * n, prec)
+        ch.set_grid(grid)
+        ch.run(5000)
+        before = [ch.info(c)["sum_molecules"] for c in range(n)]
+        ch.run(10000)
+        out[prec] = np.array([(ch.info(c)["sum_molecules"] - before[c]) / 10000 for c in range(n)])
+    m64, m32 = out[A.FP64], out[A.FP32]
+    se = np.hypot(m64.std(ddof=1), m32.std(ddof=1)) / np.sqrt(n)
+    assert m64.mean() > 1.0
+    assert abs(m32.mean() - m64.mean()) <= 3 * se, (m32.mean(), m64.mean(), se)

@@ -25,3 +25,34 @@ def test_chain_bit_identical_to_reference(orc, ref, charged):
         assert a.molecules() == b.molecules()
         assert np.array_equal(a.positions(), b.positions())
         assert a.ewald_energy() == b.ewald_energy()
+
+
+@pytest.mark.parametrize("charged", [False, True])
+def test_chain_with_energy_grid_bit_identical_to_reference(orc, ref, charged):
+    """The engine with its shared FrameworkEnergyGrid (monte_carlo_engine.cc:353-372):
+    a site's dispersion is the grid's interpolation plus the guests' LJ. The
+    oracle is given the oracle's own grid tables (bit-identical to the
+    reference's, test_oracle_vs_reference.py)."""
+    fw = W.cubic_framework(seed=21, charged=charged)
+    if charged:
+        fw.charge = fw.charge * 0.15
+    ff = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.8, truncation=O.SHIFTED)
+    ew = dict(alpha=0.31, rc=12.0, kmax=5) if charged else None
+    guest = W.co2_guest(fw) if charged else W.ch4_guest(fw)
+    fug = ref.pr_fugacity(*(W.CO2_CRITICAL if charged else W.METHANE_CRITICAL), 298.0, 1e6)
+    species = sorted(set(int(s) for s in guest["lj_species"]))
+    spacing = 0.5
+    tables = {s: orc.grid_build(ff, fw.lattice, fw.x, fw.y, fw.z, fw.species, s, spacing, threads=8)
+              for s in species}
+    counts = orc.grid_point_counts(fw.lattice, spacing)
+    a = ref.gcmc(ff, ew, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guest, 298.0, fug, 9, 4,
+                 grid={"spacing": spacing, "species": species})
+    b = orc.gcmc(ff, ew, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guest, 298.0, fug, 9, 4,
+                 grid={"counts": counts, "tables": tables})
+    for _ in range(4):
+        a.run(300)
+        b.run(300)
+        assert a.molecules() == b.molecules()
+        assert np.array_equal(a.positions(), b.positions())
+        assert a.ewald_energy() == b.ewald_energy()
+    assert a.molecules() > 0
