@@ -44,7 +44,10 @@ namespace {
 
 constexpr int GT = 256;     // threads per chain
 constexpr int MAXS = 8;     // sites per molecule
-constexpr int KMAXC = 20;   // largest kMax the per-site phase tables hold
+constexpr int KMAXC = 64;   // largest kMax the per-site phase tables hold
+// the FP32 form's (n0, n1) product table is used while it fits this budget
+// of dynamic shared memory; beyond, the products are formed per term
+constexpr size_t AB_TABLE_BUDGET = 160 * 1024;
 constexpr int RSTRIDE = 4 * MAXS + 1;
 
 struct GcmcConst {
@@ -417,13 +420,21 @@ __device__ __forceinline__ double site_grid_energy(const GcmcConst& C, const Gcm
                        : grid_interp_ref(C.L, C.gn[0], C.gn[1], C.gn[2], P.gtab[s], p[0], p[1], p[2]);
 }
 
-// F32: the FP32 form. Its per-site phase tables (FP32, in dynamic shared
-// memory): e^{i n theta_a} per slot, axis and n, then
-// q e^{i (n0 theta_0 + n1 theta_1)} per slot and (n0, n1).
+// Per-site phase tables in dynamic shared memory. FP64 form: e^{i n theta_a}
+// per slot (old sites, then new), axis and n. FP32 form: the same in FP32,
+// then (when it fits AB_TABLE_BUDGET) q e^{i (n0 theta_0 + n1 theta_1)} per
+// slot and (n0, n1).
 template <int NS>
-constexpr size_t f32_phase_bytes(int kmax) {
+__host__ __device__ size_t f32_ab_bytes(int kmax) {
     const size_t tw = 2 * (size_t)kmax + 1;
-    return 2 * NS * 3 * tw * sizeof(float2) + 2 * NS * tw * tw * sizeof(float2);
+    return 2 * NS * tw * tw * sizeof(float2);
+}
+template <int NS>
+size_t phase_bytes(int kmax, bool f32) {
+    const size_t tw = 2 * (size_t)kmax + 1;
+    if (!f32) return 2 * NS * 3 * tw * sizeof(double2);
+    const size_t ab = f32_ab_bytes<NS>(kmax);
+    return 2 * NS * 3 * tw * sizeof(float2) + (ab <= AB_TABLE_BUDGET ? ab : 0);
 }
 
 template <int NS, bool F32>
@@ -431,7 +442,6 @@ __global__ void __launch_bounds__(GT)
 gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     __shared__ StepShared S;
     __shared__ double red[(GT / 32 + 1) * RSTRIDE];
-    __shared__ double2 etab[F32 ? 1 : 2 * NS][3][2 * KMAXC + 1];
     __shared__ double eq[2 * NS];
     __shared__ PairParams srow[NS][64];
     __shared__ PairF32 srow32[F32 ? NS : 1][64];
@@ -473,8 +483,10 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
         }
     }
     const int tw = 2 * C.kmax + 1;
-    float2* etab32 = reinterpret_cast<float2*>(dyn);               // [2NS][3][tw]
+    double2* etab = reinterpret_cast<double2*>(dyn);               // FP64 form: [2NS][3][tw]
+    float2* etab32 = reinterpret_cast<float2*>(dyn);               // FP32 form: [2NS][3][tw]
     float2* ab32 = etab32 + (size_t)2 * NS * 3 * tw;                // [2NS][tw][tw]
+    const bool ab_table = F32 && f32_ab_bytes<NS>(C.kmax) <= AB_TABLE_BUDGET;
     __syncthreads();
 
     for (uint64_t step = 0; step < steps; ++step) {
@@ -653,7 +665,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     etab32[i] = make_float2(cs, sn);
                 }
                 __syncthreads();
-                for (int i = threadIdx.x; i < 2 * NS * tw * tw; i += GT) {
+                for (int i = threadIdx.x; ab_table && i < 2 * NS * tw * tw; i += GT) {
                     const int e = i / (tw * tw), n0 = (i / tw) % tw, n1 = i % tw;
                     const bool is_old = e < NS;
                     if (is_old ? (n_old == 0) : (n_new == 0)) continue;
@@ -669,10 +681,17 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
                     const int n0 = P.nidx[3 * t] + K, n1 = P.nidx[3 * t + 1] + K, n2 = P.nidx[3 * t + 2] + K;
                     float re = 0.f, im = 0.f;
+                    // q e^{i(n0 th0 + n1 th1)} of slot e: from the table, or formed here
+                    auto zq = [&](int e) -> float2 {
+                        if (ab_table) return ab32[(e * tw + n0) * tw + n1];
+                        const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1];
+                        const float q = (float)C.sq[e < NS ? e : e - NS];
+                        return make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
+                    };
                     if (n_new)  // added first (ewald_incremental_state.cc:107-111)
 #pragma unroll
                         for (int s = 0; s < NS; ++s) {
-                            const float2 Z = ab32[((NS + s) * tw + n0) * tw + n1];
+                            const float2 Z = zq(NS + s);
                             const float2 Cc = etab32[((NS + s) * 3 + 2) * tw + n2];
                             re = fmaf(Z.x, Cc.x, fmaf(-Z.y, Cc.y, re));
                             im = fmaf(Z.x, Cc.y, fmaf(Z.y, Cc.x, im));
@@ -680,7 +699,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     if (n_old)  // then removed (:112-116)
 #pragma unroll
                         for (int s = 0; s < NS; ++s) {
-                            const float2 Z = ab32[(s * tw + n0) * tw + n1];
+                            const float2 Z = zq(s);
                             const float2 Cc = etab32[(s * 3 + 2) * tw + n2];
                             re = fmaf(-Z.x, Cc.x, fmaf(Z.y, Cc.y, re));
                             im = fmaf(-Z.x, Cc.y, fmaf(-Z.y, Cc.x, im));
@@ -713,7 +732,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     const double th = C.b[3 * a] * p[0] + C.b[3 * a + 1] * p[1] + C.b[3 * a + 2] * p[2];
                     double sn, cs;
                     sincos((double)n * th, &sn, &cs);
-                    etab[e][a][n + K] = make_double2(cs, sn);
+                    etab[(e * 3 + a) * tw + n + K] = make_double2(cs, sn);
                 }
                 if (threadIdx.x < 2 * NS) eq[threadIdx.x] = C.sq[threadIdx.x % NS];
                 __syncthreads();
@@ -724,7 +743,8 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     if (n_new)  // added first (ewald_incremental_state.cc:107-111)
 #pragma unroll
                         for (int s = 0; s < NS; ++s) {
-                            const double2 A = etab[NS + s][0][n0], B = etab[NS + s][1][n1], Cc = etab[NS + s][2][n2];
+                            const double2 A = etab[((NS + s) * 3 + 0) * tw + n0], B = etab[((NS + s) * 3 + 1) * tw + n1],
+                                          Cc = etab[((NS + s) * 3 + 2) * tw + n2];
                             const double abr = A.x * B.x - A.y * B.y, abi = A.x * B.y + A.y * B.x;
                             re += eq[NS + s] * (abr * Cc.x - abi * Cc.y);
                             im += eq[NS + s] * (abr * Cc.y + abi * Cc.x);
@@ -732,7 +752,8 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     if (n_old)  // then removed (:112-116)
 #pragma unroll
                         for (int s = 0; s < NS; ++s) {
-                            const double2 A = etab[s][0][n0], B = etab[s][1][n1], Cc = etab[s][2][n2];
+                            const double2 A = etab[(s * 3 + 0) * tw + n0], B = etab[(s * 3 + 1) * tw + n1],
+                                          Cc = etab[(s * 3 + 2) * tw + n2];
                             const double abr = A.x * B.x - A.y * B.y, abi = A.x * B.y + A.y * B.x;
                             re -= eq[s] * (abr * Cc.x - abi * Cc.y);
                             im -= eq[s] * (abr * Cc.y + abi * Cc.x);
@@ -949,13 +970,15 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
 template <int NS>
 void launch_chains(unsigned n_chains, const GcmcConst& C, const GcmcPtrs& P, uint64_t steps,
                    cudaStream_t s) {
+    const size_t bytes = C.charged ? phase_bytes<NS>(C.kmax, C.f32 != 0) : 0;
     if (C.f32) {
-        const size_t bytes = C.charged ? f32_phase_bytes<NS>(C.kmax) : 0;
         ALEA_CUDA(cudaFuncSetAttribute(gcmc_kernel<NS, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
         gcmc_kernel<NS, true><<<n_chains, GT, bytes, s>>>(C, P, steps);
     } else {
-        gcmc_kernel<NS, false><<<n_chains, GT, 0, s>>>(C, P, steps);
+        ALEA_CUDA(cudaFuncSetAttribute(gcmc_kernel<NS, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        gcmc_kernel<NS, false><<<n_chains, GT, bytes, s>>>(C, P, steps);
     }
 }
 
@@ -1093,7 +1116,7 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
                     "MonteCarloEngine: GCMC species 0 is not individually charge-neutral");
             require(std::fabs(fwq) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
                     "MonteCarloEngine: framework is not charge-neutral");
-            require(ew->kmax <= KMAXC, ALEA_ERR_INVALID_ARGUMENT, "GCMC: kMax <= 20 supported");
+            require(ew->kmax <= KMAXC, ALEA_ERR_INVALID_ARGUMENT, "GCMC: kMax <= 64 supported");
             validate_cutoff(C.L, ew->real_space_cutoff, "MonteCarloEngine (Ewald real space)");
         }
         require_device();

@@ -147,3 +147,20 @@ def test_energy_grid_guards(lib):
         chains.set_grid(g_cell)
     chains.set_grid(None)
     chains.run(10)
+
+
+def test_large_kmax_chain_matches_oracle(lib, orc):
+    """kMax 24 (a cell of about 100 A needs about 35 for Ewald 1e-6): the phase
+    tables beyond the old limit of 20; same moves as the oracle."""
+    A, _ = lib
+    fw = W.cubic_framework(seed=12, charged=True)
+    fw.charge = fw.charge * 0.15
+    ew = dict(alpha=0.31, rc=12.0, kmax=24)
+    fug = orc.pr_fugacity(*W.CO2_CRITICAL, 298.0, 1e6)
+    gpu, cpu = _pair(A, orc, fw, W.co2_guest(fw), ew, fug, 3, 7)
+    for _ in range(3):
+        gpu.run(300)
+        cpu.run(300)
+        _compare(gpu, cpu, charged=True)
+    with pytest.raises(ValueError):
+        _pair(A, orc, fw, W.co2_guest(fw), dict(alpha=0.31, rc=12.0, kmax=65), fug, 3, 7)

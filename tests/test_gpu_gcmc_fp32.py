@@ -27,13 +27,15 @@ def _chains(A, fw, guest, ew, fugs, seeds, streams, precision, max_molecules=256
                         max_molecules=max_molecules, precision=precision)
 
 
-@pytest.mark.parametrize("charge_scale", [1.0, 0.15])
-def test_fp32_move_energies_track_fp64(lib, orc, charge_scale):
+@pytest.mark.parametrize("charge_scale,kmax", [(1.0, None), (0.15, None), (0.15, 36)])
+def test_fp32_move_energies_track_fp64(lib, orc, charge_scale, kmax):
+    """kmax None: the 1e-6 rule (10 here); 36: the FP32 form forms the
+    (n0, n1) phase products per term (its table would not fit)."""
     A, _ = lib
     fw = W.cubic_framework(seed=12, charged=True)
     fw.charge = fw.charge * charge_scale
-    alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
-    ew = A.Ewald(alpha, 12.0, kmax)
+    alpha, k_rule = W.ewald_parameters(fw.lattice, 12.0)
+    ew = A.Ewald(alpha, 12.0, k_rule if kmax is None else kmax)
     fug = orc.pr_fugacity(*W.CO2_CRITICAL, KT, 1e6)
     guest = W.co2_guest(fw)
     c64 = _chains(A, fw, guest, ew, [fug], [3], [7], A.FP64)
