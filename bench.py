@@ -543,6 +543,55 @@ def kernel_case(case):
     return 0
 
 
+def c5_isotherm_sample(A, torch, moves=1000, n=64):
+    """The large batched isotherm: the 4x4x4 triclinic supercell (27 008 charged
+    atoms), 64 rigid-CO2 chains at pressures log-spaced over 0.01-50 bar in one
+    launch, FP32 form, dispersion from the 0.2 A FP32 energy grid of the CO2
+    site types, Ewald at 1e-6 (alpha and kMax from the rule, rc 12 A, FP64
+    S(k) per chain), insertions from the learned proposal fitted on the
+    supercell's own Widom trials. A bounded sample: `moves` moves per chain
+    (the chains are not equilibrated); reported are the costs and the loadings
+    reached."""
+    from aleator_gb300 import workloads as W
+    T = 298.0
+    fw, guests = make_workload()
+    alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
+    ff = A.LennardJones(fw.eps, fw.sigma, CUTOFF, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    ew = A.Ewald(alpha, 12.0, kmax)
+    guest = W.co2_guest(fw)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    grid, t_grid = timed(lambda: A.FrameworkEnergyGrid(ff, p, fw.lattice, guests, SPACING, A.FP32))
+    widom = A.Widom(ff, p, fw.lattice, guest, T, ewald=ew, precision=A.FP32)
+    prop = A.Proposal(seed=2)
+    _, t_fit = timed(lambda: prop.fit(widom, n_samples=1 << 16, rounds=2, epochs=15, cells=64))
+    pressures = np.logspace(np.log10(0.01), np.log10(50.0), n)
+    fugs = [A.peng_robinson_fugacity(*W.CO2_CRITICAL, T, P * 1e5) for P in pressures]
+    ch, t_create = timed(lambda: A.GcmcChains(ff, p, fw.lattice, guest, T, fugs, list(range(n)),
+                                              list(range(n)), ewald=ew, max_molecules=4000,
+                                              precision=A.FP32))
+    ch.set_grid(grid)
+    ch.set_proposal(prop)
+    _, t_run = timed(lambda: ch.run(moves))
+    mol = [ch.molecules(c) for c in range(n)]
+    terms = int(A.EwaldIncrementalState(ew, p, fw.lattice).term_count())
+    return {"workload": f"4x4x4 triclinic supercell, {len(fw.x)} charged atoms, rigid CO2, {n} chains "
+                        f"at 0.01-50 bar, Ewald kMax {kmax} ({terms} terms), 0.2 A FP32 grid, learned "
+                        "proposal, FP32 form",
+            "grid_build_s": t_grid, "proposal_fit_s": t_fit, "chains_create_s": t_create,
+            "moves_per_chain": moves, "run_s": t_run,
+            "us_per_move_per_chain": t_run / moves * 1e6,
+            "chain_moves_per_s": n * moves / t_run,
+            "molecules_after": {f"{P:.3g} bar": m for P, m in list(zip(pressures, mol))[::9]}}
+
+
 def batched_screening(A, torch, n_frameworks=256, trials=100_000):
     """Batched screening: 256 uneven synthetic triclinic frameworks (a, b, c
     uniform in 10-40 A, angles in 60-120 deg, 50-2000 atoms, each replicated so
@@ -642,6 +691,7 @@ def extras(A, torch, peaks):
     gbs = algo_bytes / (ms * 1e-3) / 1e9
     out["interpolate_queries_per_s"] = n / (ms * 1e-3)
     out["batched_screening"] = batched_screening(A, torch)
+    out["c5_isotherm_sample"] = c5_isotherm_sample(A, torch)
     out["interpolate_roofline"] = {
         "bound": "fp64", "achieved": gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
         "frac": gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None, "bytes_per_query": 96,
