@@ -317,6 +317,14 @@ class Oracle:
                           fugacity_pa, seed, stream, max_translation, max_rotation, draw_order,
                           grid)
 
+    def gcmc_mixture(self, ff, ewald, m, x, y, z, q, species, guests, temperature, fugacities_pa,
+                     seed, stream, max_translation=1.5, max_rotation=0.5,
+                     draw_order=DRAWS_RIGHT_TO_LEFT):
+        """Several rigid species (the engine's mixture constructor)."""
+        return OracleGcmc(self, ff, ewald, m, x, y, z, q, species, list(guests), temperature,
+                          list(fugacities_pa), seed, stream, max_translation, max_rotation,
+                          draw_order)
+
 
 class OracleGcmc:
     """Single-species GCMC chain (MonteCarloEngine::run restated in C)."""
@@ -341,19 +349,33 @@ class OracleGcmc:
         L.orc_gcmc_ewald_energy.restype = ctypes.c_double
         L.orc_gcmc_ewald_energy.argtypes = [ctypes.c_void_p]
         L.orc_gcmc_counters.argtypes = [ctypes.c_void_p, _U64]
+        L.orc_gcmc_new_mixture.restype = ctypes.c_void_p
+        L.orc_gcmc_new_mixture.argtypes = [ctypes.POINTER(_LJ), ctypes.POINTER(_EwaldParams), _D,
+                                           ctypes.c_uint64, _D, _D, _D, _D, _U32, ctypes.c_uint32,
+                                           ctypes.POINTER(_Species), ctypes.c_double, _D,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                           ctypes.c_uint64, ctypes.c_int]
         lj, keep = orc._lj(ff)
         self._keep = keep
         ew = _EwaldParams(ewald["alpha"], ewald["rc"], ewald["kmax"]) if ewald else _EwaldParams(0, 0, 0)
-        g = {k: _f64(guest[k]) for k in ("x", "y", "z", "charge")}
-        gs = np.ascontiguousarray(guest["lj_species"], dtype=np.uint32)
-        sp = _Species(len(g["x"]), _dp(g["x"]), _dp(g["y"]), _dp(g["z"]), _u32(gs), _dp(g["charge"]))
+        guests = guest if isinstance(guest, list) else [guest]
+        self._gkeep = []
+        sps = (_Species * len(guests))()
+        for i, gd in enumerate(guests):
+            g = {k: _f64(gd[k]) for k in ("x", "y", "z", "charge")}
+            gs = np.ascontiguousarray(gd["lj_species"], dtype=np.uint32)
+            self._gkeep.append((g, gs))
+            sps[i] = _Species(len(g["x"]), _dp(g["x"]), _dp(g["y"]), _dp(g["z"]), _u32(gs),
+                              _dp(g["charge"]))
         x, y, z = _f64(x), _f64(y), _f64(z)
         q = _f64(q if q is not None else np.zeros(len(x)))
         fs = np.ascontiguousarray(species, dtype=np.uint32)
-        self.h = L.orc_gcmc_new(ctypes.byref(lj), ctypes.byref(ew), _dp(_mat(m)), len(x), _dp(x),
-                                _dp(y), _dp(z), _dp(q), _u32(fs), ctypes.byref(sp), temperature,
-                                fugacity_pa, max_translation, max_rotation, seed, stream,
-                                draw_order)
+        fug = _f64(np.atleast_1d(fugacity_pa))
+        self._fug = fug
+        self.h = L.orc_gcmc_new_mixture(ctypes.byref(lj), ctypes.byref(ew), _dp(_mat(m)), len(x),
+                                        _dp(x), _dp(y), _dp(z), _dp(q), _u32(fs), len(guests), sps,
+                                        temperature, _dp(fug), max_translation, max_rotation, seed,
+                                        stream, draw_order)
         if grid is not None:
             L.orc_gcmc_set_grid.argtypes = [ctypes.c_void_p, _I32, ctypes.c_uint32, _U32,
                                             ctypes.POINTER(_D)]
@@ -389,9 +411,15 @@ class OracleGcmc:
         return self.L.orc_gcmc_ewald_energy(self.h)
 
     def counters(self):
-        out = np.zeros(8, np.uint64)
+        """attempted[5] then accepted[5]: translate, rotate, insert, delete, swap"""
+        out = np.zeros(10, np.uint64)
         self.L.orc_gcmc_counters(self.h, _u64(out))
         return out
+
+    def molecules_of(self, species):
+        self.L.orc_gcmc_molecules_of.restype = ctypes.c_uint64
+        self.L.orc_gcmc_molecules_of.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
+        return int(self.L.orc_gcmc_molecules_of(self.h, species))
 
 
 class OracleEwaldState:
@@ -530,6 +558,15 @@ class Reference:
         L.ref_gcmc_create_grid.restype = ctypes.c_void_p
         L.ref_gcmc_create_grid.argtypes = L.ref_gcmc_create.argtypes + [ctypes.c_double,
                                                                           ctypes.c_uint32, _U32]
+        L.ref_gcmc_create_mixture.restype = ctypes.c_void_p
+        L.ref_gcmc_create_mixture.argtypes = [_D, ctypes.c_uint64, _D, _D, _D, _D, _U32,
+                                              ctypes.c_uint32, _D, _D, ctypes.c_double, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                              ctypes.c_int, ctypes.c_uint32, _U32, _D, _D, _D, _U32,
+                                              _D, _D, ctypes.c_double, ctypes.c_double,
+                                              ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64]
+        L.ref_gcmc_molecules_of.restype = ctypes.c_uint64
+        L.ref_gcmc_molecules_of.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
         L.ref_gcmc_run.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
         L.ref_gcmc_molecules.restype = ctypes.c_uint64
         L.ref_gcmc_molecules.argtypes = [ctypes.c_void_p]
@@ -672,6 +709,12 @@ class Reference:
         return ReferenceGcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature,
                              fugacity_pa, seed, stream, max_translation, max_rotation, grid)
 
+    def gcmc_mixture(self, ff, ewald, m, x, y, z, q, species, guests, temperature, fugacities_pa,
+                     seed, stream, max_translation=1.5, max_rotation=0.5):
+        """The engine's mixture constructor (several rigid species)."""
+        return ReferenceGcmc(self, ff, ewald, m, x, y, z, q, species, list(guests), temperature,
+                             list(fugacities_pa), seed, stream, max_translation, max_rotation)
+
 
 class ReferenceGcmc:
     """MonteCarloEngine (the reference's own class) driven through the shim."""
@@ -683,18 +726,34 @@ class ReferenceGcmc:
         x, y, z = _f64(x), _f64(y), _f64(z)
         q = _f64(q if q is not None else np.zeros(len(x)))
         sp = np.ascontiguousarray(species, dtype=np.uint32)
-        gx, gy, gz = _f64(guest["x"]), _f64(guest["y"]), _f64(guest["z"])
-        gs = np.ascontiguousarray(guest["lj_species"], dtype=np.uint32)
-        gq = _f64(guest["charge"])
+        mixture = isinstance(guest, list)
+        guests = guest if mixture else [guest]
+        gx = _f64(np.concatenate([np.asarray(g["x"], float) for g in guests]))
+        gy = _f64(np.concatenate([np.asarray(g["y"], float) for g in guests]))
+        gz = _f64(np.concatenate([np.asarray(g["z"], float) for g in guests]))
+        gs = np.ascontiguousarray(np.concatenate([np.asarray(g["lj_species"]) for g in guests]),
+                                  dtype=np.uint32)
+        gq = _f64(np.concatenate([np.asarray(g["charge"], float) for g in guests]))
+        per = np.array([len(g["x"]) for g in guests], dtype=np.uint32)
         alpha = ewald["alpha"] if ewald else 0.0
         erc = ewald["rc"] if ewald else 0.0
         kmax = ewald["kmax"] if ewald else 0
+        self._keep = (gx, gy, gz, gs, gq, per)
         args = [_dp(_mat(m)), len(x), _dp(x), _dp(y), _dp(z), _dp(q), _u32(sp), len(eps), _dp(eps),
                 _dp(sig), ff["cutoff"], ff.get("truncation", SHIFTED),
                 ff.get("mixing", LORENTZ_BERTHELOT), alpha, erc, kmax, len(gx), _dp(gx), _dp(gy),
                 _dp(gz), _u32(gs), _dp(gq), temperature, fugacity_pa, max_translation,
                 max_rotation, seed, stream]
-        if grid is None:
+        if mixture:
+            fug = _f64(np.asarray(fugacity_pa, float))
+            self._keep = self._keep + (fug,)
+            self.h = ref.lib.ref_gcmc_create_mixture(
+                _dp(_mat(m)), len(x), _dp(x), _dp(y), _dp(z), _dp(q), _u32(sp), len(eps), _dp(eps),
+                _dp(sig), ff["cutoff"], ff.get("truncation", SHIFTED),
+                ff.get("mixing", LORENTZ_BERTHELOT), alpha, erc, kmax, len(guests), _u32(per),
+                _dp(gx), _dp(gy), _dp(gz), _u32(gs), _dp(gq), _dp(fug), temperature,
+                max_translation, max_rotation, seed, stream)
+        elif grid is None:
             self.h = ref.lib.ref_gcmc_create(*args)
         else:
             ids = np.ascontiguousarray(grid["species"], dtype=np.uint32)
@@ -711,6 +770,9 @@ class ReferenceGcmc:
 
     def molecules(self):
         return int(self.ref.lib.ref_gcmc_molecules(self.h))
+
+    def molecules_of(self, species):
+        return int(self.ref.lib.ref_gcmc_molecules_of(self.h, species))
 
     def positions(self):
         n = self.ref.lib.ref_gcmc_particles(self.h, None, 0)

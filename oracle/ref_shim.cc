@@ -496,6 +496,42 @@ void* ref_gcmc_create_grid(const double* m, uint64_t n, const double* x, const d
     return g;
 }
 
+// The mixture constructor (monte_carlo_engine.hpp:143-151): nGuest species,
+// species k with nSitesPer[k] sites, their site arrays concatenated.
+void* ref_gcmc_create_mixture(const double* m, uint64_t n, const double* x, const double* y,
+                              const double* z, const double* q, const uint32_t* sp,
+                              uint32_t nSpecies, const double* eps, const double* sigma,
+                              double cutoff, int trunc, int mixing, double alpha, double ewaldRc,
+                              int kMax, uint32_t nGuest, const uint32_t* nSitesPer,
+                              const double* sx, const double* sy, const double* sz,
+                              const uint32_t* sLj, const double* sq, const double* fugacitiesPa,
+                              double temperature, double maxTrans, double maxRot, uint64_t seed,
+                              uint64_t stream) {
+    auto* g = new RefGcmc{latticeOf(m), nullptr};
+    const auto fw = particlesOf(n, x, y, z, q, sp);
+    auto lj = ljOf(nSpecies, eps, sigma, cutoff, trunc, mixing);
+    std::shared_ptr<forcefield::Ewald> ewald;
+    if (alpha > 0.0) ewald = std::make_shared<forcefield::Ewald>(alpha, ewaldRc, kMax);
+    std::vector<engines::MoleculeSpecies> list;
+    std::vector<double> fug;
+    uint32_t off = 0;
+    for (uint32_t k = 0; k < nGuest; ++k) {
+        list.push_back(speciesOf(nSitesPer[k], sx + off, sy + off, sz + off, sLj + off, sq + off));
+        fug.push_back(fugacitiesPa[k]);
+        off += nSitesPer[k];
+    }
+    auto rng = std::make_unique<core::Philox4x32Rng>();
+    rng->seed(seed, stream);
+    g->engine = std::make_unique<engines::MonteCarloEngine>(fw, g->lattice, lj, std::move(rng),
+                                                            temperature, list, fug, maxTrans,
+                                                            maxRot, ewald, nullptr);
+    return g;
+}
+
+uint64_t ref_gcmc_molecules_of(void* h, uint64_t species) {
+    return static_cast<RefGcmc*>(h)->engine->moleculeCountOfSpecies(species);
+}
+
 void ref_gcmc_run(void* h, uint64_t steps) { static_cast<RefGcmc*>(h)->engine->run(steps); }
 
 uint64_t ref_gcmc_molecules(void* h) { return static_cast<RefGcmc*>(h)->engine->moleculeCount(); }

@@ -29,8 +29,9 @@ def _compare(gpu, cpu, chain=0, charged=False):
     assert info["molecules"] == cpu.molecules()
     assert info["call_index"] == cpu.calls()
     ctr = cpu.counters()
-    assert list(info["attempted"]) == [int(v) for v in ctr[:4]]
-    assert list(info["accepted"]) == [int(v) for v in ctr[4:]]
+    n = len(info["attempted"])  # the oracle's counters: attempted[5], accepted[5]
+    assert list(info["attempted"]) == [int(v) for v in ctr[:n]]
+    assert list(info["accepted"]) == [int(v) for v in ctr[5:5 + n]]
     pg, pc = gpu.positions(chain), cpu.positions()
     assert pg.shape == pc.shape
     assert np.abs(pg - pc).max() <= 1e-9

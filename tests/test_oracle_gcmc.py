@@ -56,3 +56,36 @@ def test_chain_with_energy_grid_bit_identical_to_reference(orc, ref, charged):
         assert np.array_equal(a.positions(), b.positions())
         assert a.ewald_energy() == b.ewald_energy()
     assert a.molecules() > 0
+
+
+@pytest.mark.parametrize("charged", [False, True])
+def test_mixture_chain_bit_identical_to_reference(orc, ref, charged):
+    """The mixture constructor (monte_carlo_engine.hpp:143-151): CH4 and CO2,
+    20 % each of translate, rotate, insert, delete and identity swap
+    (monte_carlo_engine.cc:405-439, 673-792); bit-identical trajectories,
+    per-species counts and Ewald cache energies."""
+    fw = W.cubic_framework(seed=21, charged=charged)
+    if charged:
+        fw.charge = fw.charge * 0.15
+    ff = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.8, truncation=O.SHIFTED)
+    ew = dict(alpha=0.31, rc=12.0, kmax=5) if charged else None
+    ch4 = W.ch4_guest(fw)
+    ch4 = dict(ch4, charge=[0.0])
+    guests = [W.co2_guest(fw), ch4] if charged else [ch4, dict(W.co2_guest(fw), charge=[0.0] * 3)]
+    fugs = [ref.pr_fugacity(*W.CO2_CRITICAL, 298.0, 5e5), ref.pr_fugacity(*W.METHANE_CRITICAL, 298.0, 2e6)]
+    if not charged:
+        fugs = fugs[::-1]
+    a = ref.gcmc_mixture(ff, ew, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guests, 298.0,
+                         fugs, 9, 4)
+    b = orc.gcmc_mixture(ff, ew, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guests, 298.0,
+                         fugs, 9, 4)
+    for _ in range(5):
+        a.run(400)
+        b.run(400)
+        assert a.molecules() == b.molecules()
+        assert [a.molecules_of(k) for k in range(2)] == [b.molecules_of(k) for k in range(2)]
+        assert np.array_equal(a.positions(), b.positions())
+        assert a.ewald_energy() == b.ewald_energy()
+    ctr = b.counters()
+    assert ctr[9] > 0, ctr  # swaps accepted
+    assert min(a.molecules_of(k) for k in range(2)) > 0
