@@ -88,8 +88,9 @@ class _GridBatchStats(ctypes.Structure):
 class _ChainInfo(ctypes.Structure):
     _fields_ = [("molecules", ctypes.c_uint64), ("guest_sites", ctypes.c_uint64),
                 ("call_index", ctypes.c_uint64), ("steps", ctypes.c_uint64),
-                ("resyncs", ctypes.c_uint64), ("attempted", ctypes.c_uint64 * 4),
-                ("accepted", ctypes.c_uint64 * 4), ("sum_molecules", ctypes.c_double),
+                ("resyncs", ctypes.c_uint64), ("attempted", ctypes.c_uint64 * 5),
+                ("accepted", ctypes.c_uint64 * 5), ("species_molecules", ctypes.c_uint64 * 4),
+                ("sum_molecules", ctypes.c_double),
                 ("sum_molecules_sq", ctypes.c_double), ("last_du", ctypes.c_double),
                 ("last_kernel_ms", ctypes.c_float)]
 
@@ -200,6 +201,12 @@ _SIGNATURES = {
                                           ctypes.POINTER(_Species), ctypes.c_double, _D, _U64, _U64,
                                           ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_int32, ctypes.c_uint32, ctypes.POINTER(_VP)]),
+    "alea_gcmc_create_mixture": (ctypes.c_int32, [ctypes.POINTER(_LJ), ctypes.POINTER(_Ewald),
+                                                  ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
+                                                  ctypes.c_uint32, ctypes.POINTER(_Species),
+                                                  ctypes.c_double, _D, _U64, _U64, ctypes.c_uint32,
+                                                  ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                                  ctypes.c_uint32, ctypes.POINTER(_VP)]),
     "alea_gcmc_run": (ctypes.c_int32, [_VP, ctypes.c_uint64, _VP]),
     "alea_gcmc_chain_info_get": (ctypes.c_int32, [_VP, ctypes.c_uint32, ctypes.POINTER(_ChainInfo)]),
     "alea_gcmc_particles": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D, ctypes.c_uint64, _U64]),
@@ -957,36 +964,47 @@ class Proposal:
 
 
 class GcmcChains:
-    """MonteCarloEngine (monte_carlo_engine.hpp:76-83, single species) for many
-    independent chains advanced together on the GPU."""
+    """MonteCarloEngine (monte_carlo_engine.hpp:76-83, 143-151) for many
+    independent chains advanced together on the GPU. `guest` is one species
+    (a dict: the single-species engine, one fugacity per chain) or a list of
+    species (the mixture engine: per chain a list of fugacities)."""
 
-    def __init__(self, force_field: LennardJones, framework: ParticleData, lattice, guest: dict,
+    def __init__(self, force_field: LennardJones, framework: ParticleData, lattice, guest,
                  temperature: float, fugacities_pa, seeds, streams, ewald: Ewald | None = None,
                  max_translation=1.5, max_rotation=0.5, draw_order=ALEA_DRAWS_RIGHT_TO_LEFT,
                  max_molecules=256, precision=None):
         self._lib = library()
         self._h = _VP()
-        self._g = {k: (_f64(guest[k]) if k != "lj_species" else
-                       np.ascontiguousarray(guest[k], dtype=np.uint32))
-                   for k in ("x", "y", "z", "lj_species", "charge")}
-        sp = _Species(len(self._g["x"]), _dp(self._g["x"]), _dp(self._g["y"]), _dp(self._g["z"]),
-                      _u32p(self._g["lj_species"]), _dp(self._g["charge"]))
-        f = _f64(np.atleast_1d(fugacities_pa))
+        mixture = isinstance(guest, (list, tuple))
+        guests = list(guest) if mixture else [guest]
+        self._g = [{k: (_f64(gd[k]) if k != "lj_species" else
+                        np.ascontiguousarray(gd[k], dtype=np.uint32))
+                    for k in ("x", "y", "z", "lj_species", "charge")} for gd in guests]
+        sps = (_Species * len(guests))()
+        for i, gd in enumerate(self._g):
+            sps[i] = _Species(len(gd["x"]), _dp(gd["x"]), _dp(gd["y"]), _dp(gd["z"]),
+                              _u32p(gd["lj_species"]), _dp(gd["charge"]))
+        f = np.asarray(fugacities_pa, dtype=np.float64)
+        if mixture:
+            f = f.reshape(-1, len(guests))
+        else:
+            f = np.atleast_1d(f).reshape(-1, 1)
+        f = _f64(f.reshape(-1))
         se = np.ascontiguousarray(np.atleast_1d(seeds), dtype=np.uint64)
         st = np.ascontiguousarray(np.atleast_1d(streams), dtype=np.uint64)
-        self.n_chains = len(f)
+        self.n_chains = len(f) // len(guests)
+        self.n_species = len(guests)
         if len(se) != self.n_chains or len(st) != self.n_chains:
-            raise ValueError("one fugacity, seed and stream per chain")
+            raise ValueError("one fugacity (per species), seed and stream per chain")
         lj = force_field.c()
         p = framework.c()
         lat = _lattice(lattice)
         e = ewald.c() if ewald is not None else None
-        _check(self._lib.alea_gcmc_create(ctypes.byref(lj), ctypes.byref(e) if e else None,
-                                          ctypes.byref(p), ctypes.byref(lat), ctypes.byref(sp),
-                                          float(temperature), _dp(f), _u64p(se), _u64p(st),
-                                          self.n_chains, float(max_translation),
-                                          float(max_rotation), int(draw_order), int(max_molecules),
-                                          ctypes.byref(self._h)))
+        _check(self._lib.alea_gcmc_create_mixture(
+            ctypes.byref(lj), ctypes.byref(e) if e else None, ctypes.byref(p), ctypes.byref(lat),
+            len(guests), sps, float(temperature), _dp(f), _u64p(se), _u64p(st), self.n_chains,
+            float(max_translation), float(max_rotation), int(draw_order), int(max_molecules),
+            ctypes.byref(self._h)))
         if precision is not None:
             self.set_precision(precision)
 
@@ -1025,6 +1043,7 @@ class GcmcChains:
         d = {f: getattr(s, f) for f, _ in s._fields_}
         d["attempted"] = list(s.attempted)
         d["accepted"] = list(s.accepted)
+        d["species_molecules"] = list(s.species_molecules)
         return d
 
     def molecules(self, chain=0):

@@ -860,8 +860,38 @@ alea_status alea_gcmc_create(const alea_lennard_jones* lj, const alea_ewald* ewa
         *out = nullptr;
         auto* g = new alea_gcmc{nullptr};
         try {
-            g->impl = alea::gcmc_create(*lj, ewald, particles_or_empty(framework), *lattice, *species,
+            g->impl = alea::gcmc_create(*lj, ewald, particles_or_empty(framework), *lattice, 1, species,
                                         temperature, fugacity_pa, seeds, streams, n_chains,
+                                        max_translation, max_rotation, draw_order, max_molecules);
+        } catch (...) {
+            delete g;
+            throw;
+        }
+        *out = g;
+    });
+}
+
+alea_status alea_gcmc_create_mixture(const alea_lennard_jones* lj, const alea_ewald* ewald,
+                                     const alea_particles* framework, const alea_lattice* lattice,
+                                     uint32_t n_species, const alea_molecule_species* species,
+                                     double temperature, const double* fugacity_pa,
+                                     const uint64_t* seeds, const uint64_t* streams,
+                                     uint32_t n_chains, double max_translation,
+                                     double max_rotation, int32_t draw_order,
+                                     uint32_t max_molecules, alea_gcmc** out) {
+    return guarded([&] {
+        need(lj, "lj");
+        need(lattice, "lattice");
+        need(species, "species");
+        need(fugacity_pa, "fugacity_pa");
+        need(seeds, "seeds");
+        need(streams, "streams");
+        need(out, "out");
+        *out = nullptr;
+        auto* g = new alea_gcmc{nullptr};
+        try {
+            g->impl = alea::gcmc_create(*lj, ewald, particles_or_empty(framework), *lattice, n_species,
+                                        species, temperature, fugacity_pa, seeds, streams, n_chains,
                                         max_translation, max_rotation, draw_order, max_molecules);
         } catch (...) {
             delete g;
@@ -892,10 +922,11 @@ alea_status alea_gcmc_chain_info_get(const alea_gcmc* g, uint32_t chain, alea_gc
         out->call_index = c.call;
         out->steps = c.steps;
         out->resyncs = c.resyncs;
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < 5; ++i) {
             out->attempted[i] = c.attempted[i];
             out->accepted[i] = c.accepted[i];
         }
+        for (int i = 0; i < 4; ++i) out->species_molecules[i] = c.n_of[i];
         out->sum_molecules = c.sum_n;
         out->sum_molecules_sq = c.sum_n2;
         out->last_du = c.last_du;

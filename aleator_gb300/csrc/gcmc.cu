@@ -50,11 +50,19 @@ constexpr int KMAXC = 64;   // largest kMax the per-site phase tables hold
 constexpr size_t AB_TABLE_BUDGET = 160 * 1024;
 constexpr int RSTRIDE = 4 * MAXS + 1;
 
+constexpr int MAXGS = GCMC_MAX_SPECIES;
+constexpr int MAXROWS = 8;  // distinct LJ species among the guest sites
+
 struct GcmcConst {
     Lattice L;
-    int ns;
-    double sx[MAXS], sy[MAXS], sz[MAXS], sq[MAXS];
-    uint32_t slj[MAXS];
+    int ns;     // sites of the largest guest species (the kernel's NS)
+    int n_gsp;  // guest species (1: the single-species engine)
+    int sp_ns[MAXGS];
+    double spx[MAXGS][MAXS], spy[MAXGS][MAXS], spz[MAXGS][MAXS], spq[MAXGS][MAXS];
+    uint32_t splj[MAXGS][MAXS];
+    int sprow[MAXGS][MAXS];  // the site's row of the pair tables
+    int n_rows;
+    uint32_t row_lj[MAXROWS];  // distinct guest LJ species, one pair-table row each
     uint32_t n_species;
     double rc, rc2;
     int trunc;
@@ -74,10 +82,10 @@ struct GcmcConst {
     // learned insertion proposal (prop_cells == 0: the reference's uniform
     // insertion): the template centred on its centroid, and the table size
     int prop_cells;
-    double tc[MAXS][3];
+    double tc[MAXGS][MAXS][3];
     int f32;  // ALEA_FP32 form: FP32 pair and real-space terms, FP32 per-term S(k) deltas
     float lh[9], ll[9], linv[9];  // FP32 form: rows a_i as hi + lo; the inverse (f = d . inv)
-    double excl_tmpl;  // FP32 form: pairExclusionSum of the rigid template (any position)
+    double excl_tmpl[MAXGS];  // FP32 form: pairExclusionSum of each rigid template
     // the engine's frameworkEnergyGrid (grid == 0: none): a site's dispersion
     // is its species' interpolated table plus the LJ with the guests
     int grid, grid_fast;
@@ -109,11 +117,15 @@ struct GcmcPtrs {
     // S(k) (refreshed on every commit and resync), FP32 per-term deltas
     const float* w32;
     float *sre32, *sim32, *dre32, *dim32;
-    const double* gtab[MAXS];  // per site: its LJ species' grid table
+    const double* gtab[MAXROWS];  // per pair-table row: its LJ species' grid table
+    uint32_t* msp;                // per chain, per molecule: its species
 };
 
 struct StepShared {
     int move, valid, accept, do_resync;
+    int sp_old, sp_new;       // species of the old and the new sites
+    double sq_slot[2 * MAXS];  // charge per slot (old sites, then new)
+    int row_slot[2 * MAXS];    // pair-table row per slot
     uint32_t mi;
     int n_old, n_new;
     uint64_t ng;        // guest sites while the move is evaluated
@@ -219,11 +231,67 @@ __device__ __forceinline__ uint32_t proposal_cell(int cells, const double* f) {
     return (idx[2] * (uint32_t)cells + idx[1]) * (uint32_t)cells + idx[0];
 }
 
-// Learned-proposal insertion: the centroid from the tabulated density (a cell
-// from the CDF, a uniform point inside it; draws 1 and 2..4), a uniform
-// orientation (draws 5..7, in order), the template centred on its centroid.
+// A rotation q of a species' site (rotateByQuaternion, monte_carlo_engine.cc:
+// 68-72, non-contracted) about the origin of its template frame.
+__device__ __forceinline__ void rotate_site(const double* loc, const double* q, double* rot) {
+    const double qv[3] = {q[1], q[2], q[3]};
+    const double cr[3] = {sub_rn(mul_rn(qv[1], loc[2]), mul_rn(qv[2], loc[1])),
+                          sub_rn(mul_rn(qv[2], loc[0]), mul_rn(qv[0], loc[2])),
+                          sub_rn(mul_rn(qv[0], loc[1]), mul_rn(qv[1], loc[0]))};
+    const double t[3] = {mul_rn(cr[0], 2.0), mul_rn(cr[1], 2.0), mul_rn(cr[2], 2.0)};
+    const double c2[3] = {sub_rn(mul_rn(qv[1], t[2]), mul_rn(qv[2], t[1])),
+                          sub_rn(mul_rn(qv[2], t[0]), mul_rn(qv[0], t[2])),
+                          sub_rn(mul_rn(qv[0], t[1]), mul_rn(qv[1], t[0]))};
+    for (int i = 0; i < 3; ++i) rot[i] = add_rn(add_rn(loc[i], mul_rn(t[i], q[0])), c2[i]);
+}
+
+// randomUnitQuaternion (monte_carlo_engine.cc:56-63) over three draws taken
+// in the engine's argument order.
+__device__ __forceinline__ void draw_quaternion(const GcmcConst& C, ChainState& c, double* q,
+                                                bool swap_order) {
+    double v[3];
+    v[0] = u01(c);
+    v[1] = u01(c);
+    v[2] = u01(c);
+    if (swap_order) {
+        const double t = v[0];
+        v[0] = v[2];
+        v[2] = t;
+    }
+    const double r1 = __dsqrt_rn(sub_rn(1.0, v[0])), r2 = __dsqrt_rn(v[0]);
+    const double t1 = mul_rn(2.0 * kPi, v[1]), t2 = mul_rn(2.0 * kPi, v[2]);
+    double s1, c1, s2, c2;
+    sincos(t1, &s1, &c1);
+    sincos(t2, &s2, &c2);
+    q[0] = mul_rn(r2, c2);
+    q[1] = mul_rn(r1, s1);
+    q[2] = mul_rn(r1, c1);
+    q[3] = mul_rn(r2, s2);
+}
+
+// The new sites of species k at ref: the template (about its own origin, or
+// about its centroid when `centred`) rotated by q when it has several sites.
+__device__ __forceinline__ void place_new(const GcmcConst& C, int k, const double* ref,
+                                          const double* q, bool centred, StepShared& S) {
+    const int ns = C.sp_ns[k];
+    for (int s = 0; s < ns; ++s) {
+        const double loc[3] = {centred ? C.tc[k][s][0] : C.spx[k][s],
+                               centred ? C.tc[k][s][1] : C.spy[k][s],
+                               centred ? C.tc[k][s][2] : C.spz[k][s]};
+        double rot[3] = {loc[0], loc[1], loc[2]};
+        if (ns > 1) rotate_site(loc, q, rot);
+        for (int i = 0; i < 3; ++i) S.np_[s][i] = add_rn(ref[i], rot[i]);
+    }
+    S.n_new = ns;
+    S.sp_new = k;
+}
+
+// Learned-proposal insertion of species k: the centroid from the tabulated
+// density (a cell from the CDF, a uniform point inside it; draws 1 and 2..4),
+// a uniform orientation (draws 5..7, in order), the template centred on its
+// centroid.
 __device__ void plan_biased_insertion(const GcmcConst& C, const GcmcPtrs& P, ChainState& c,
-                                      StepShared& S) {
+                                      StepShared& S, int k) {
     const uint32_t cells = (uint32_t)C.prop_cells;
     const double uc = u01(c);
     uint32_t lo = 0, hi = cells * cells * cells - 1;
@@ -237,128 +305,23 @@ __device__ void plan_biased_insertion(const GcmcConst& C, const GcmcPtrs& P, Cha
     S.lq = P.plogp[lo];
     const double* M = C.L.m;
     double ref[3];
-    for (int k = 0; k < 3; ++k)
-        ref[k] = add_rn(add_rn(mul_rn(M[k], u[0]), mul_rn(M[3 + k], u[1])), mul_rn(M[6 + k], u[2]));
-    const int ns = C.ns;
+    for (int i = 0; i < 3; ++i)
+        ref[i] = add_rn(add_rn(mul_rn(M[i], u[0]), mul_rn(M[3 + i], u[1])), mul_rn(M[6 + i], u[2]));
     double q[4] = {1.0, 0.0, 0.0, 0.0};
-    if (ns > 1) {
-        const double v0 = u01(c), v1 = u01(c), v2 = u01(c);
-        const double r1 = __dsqrt_rn(sub_rn(1.0, v0)), r2 = __dsqrt_rn(v0);
-        const double t1 = mul_rn(2.0 * kPi, v1), t2 = mul_rn(2.0 * kPi, v2);
-        double s1, c1, s2, c2;
-        sincos(t1, &s1, &c1);
-        sincos(t2, &s2, &c2);
-        q[0] = mul_rn(r2, c2);
-        q[1] = mul_rn(r1, s1);
-        q[2] = mul_rn(r1, c1);
-        q[3] = mul_rn(r2, s2);
-    }
-    for (int s = 0; s < ns; ++s) {
-        const double* loc = C.tc[s];
-        double rot[3] = {loc[0], loc[1], loc[2]};
-        if (ns > 1) {
-            const double qv[3] = {q[1], q[2], q[3]};
-            const double cr[3] = {sub_rn(mul_rn(qv[1], loc[2]), mul_rn(qv[2], loc[1])),
-                                  sub_rn(mul_rn(qv[2], loc[0]), mul_rn(qv[0], loc[2])),
-                                  sub_rn(mul_rn(qv[0], loc[1]), mul_rn(qv[1], loc[0]))};
-            const double t[3] = {mul_rn(cr[0], 2.0), mul_rn(cr[1], 2.0), mul_rn(cr[2], 2.0)};
-            const double c2[3] = {sub_rn(mul_rn(qv[1], t[2]), mul_rn(qv[2], t[1])),
-                                  sub_rn(mul_rn(qv[2], t[0]), mul_rn(qv[0], t[2])),
-                                  sub_rn(mul_rn(qv[0], t[1]), mul_rn(qv[1], t[0]))};
-            for (int i = 0; i < 3; ++i) rot[i] = add_rn(add_rn(loc[i], mul_rn(t[i], q[0])), c2[i]);
-        }
-        for (int i = 0; i < 3; ++i) S.np_[s][i] = add_rn(ref[i], rot[i]);
-    }
-    S.n_new = ns;
+    if (C.sp_ns[k] > 1) draw_quaternion(C, c, q, false);
+    place_new(C, k, ref, q, true, S);
 }
 
-// The double-float copy of a guest site's position (the FP32 form's input).
-__device__ __forceinline__ void put_hilo(float4* ghi, float4* glo, uint32_t slot, const double* p,
-                                         double q) {
-    const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
-    ghi[slot] = make_float4(x.hi, y.hi, z.hi, (float)q);
-    glo[slot] = make_float4(x.lo, y.lo, z.lo, 0.f);
-}
-
-// Thread 0: the draws and trial geometry of one move.
-__device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, const double* gx,
-                          const double* gy, const double* gz, const uint32_t* mol, StepShared& S) {
-    const double pick = u01(c);
-    S.move = pick < 0.25 ? 0 : pick < 0.5 ? 1 : pick < 0.75 ? 2 : 3;
-    S.valid = 1;
-    S.accept = 0;
-    S.do_resync = 0;
-    S.n_old = S.n_new = 0;
-    S.ng = c.n_guest;
-    S.lq = 0.0;
-    const int ns = C.ns;
-    if (S.move == 2 && C.prop_cells > 0) {
-        plan_biased_insertion(C, P, c, S);
-        return;
-    }
-    if (S.move == 2) {  // monte_carlo_engine.cc:568-590
-        double u[3];
-        u[0] = u01(c);
-        u[1] = u01(c);
-        u[2] = u01(c);
-        if (C.draw_order == ALEA_DRAWS_RIGHT_TO_LEFT) {
-            const double t = u[0];
-            u[0] = u[2];
-            u[2] = t;
-        }
-        const double* M = C.L.m;
-        double ref[3];
-        for (int k = 0; k < 3; ++k)
-            ref[k] = add_rn(add_rn(mul_rn(M[k], u[0]), mul_rn(M[3 + k], u[1])), mul_rn(M[6 + k], u[2]));
-        double q[4] = {1.0, 0.0, 0.0, 0.0};
-        if (ns > 1) {
-            double v[3];
-            v[0] = u01(c);
-            v[1] = u01(c);
-            v[2] = u01(c);
-            if (C.draw_order == ALEA_DRAWS_RIGHT_TO_LEFT) {
-                const double t = v[0];
-                v[0] = v[2];
-                v[2] = t;
-            }
-            const double r1 = __dsqrt_rn(sub_rn(1.0, v[0])), r2 = __dsqrt_rn(v[0]);
-            const double t1 = mul_rn(2.0 * kPi, v[1]), t2 = mul_rn(2.0 * kPi, v[2]);
-            double s1, c1, s2, c2;
-            sincos(t1, &s1, &c1);
-            sincos(t2, &s2, &c2);
-            q[0] = mul_rn(r2, c2);
-            q[1] = mul_rn(r1, s1);
-            q[2] = mul_rn(r1, c1);
-            q[3] = mul_rn(r2, s2);
-        }
-        for (int s = 0; s < ns; ++s) {
-            const double loc[3] = {C.sx[s], C.sy[s], C.sz[s]};
-            double rot[3] = {loc[0], loc[1], loc[2]};
-            if (ns > 1) {
-                const double qv[3] = {q[1], q[2], q[3]};
-                const double cr[3] = {sub_rn(mul_rn(qv[1], loc[2]), mul_rn(qv[2], loc[1])),
-                                      sub_rn(mul_rn(qv[2], loc[0]), mul_rn(qv[0], loc[2])),
-                                      sub_rn(mul_rn(qv[0], loc[1]), mul_rn(qv[1], loc[0]))};
-                const double t[3] = {mul_rn(cr[0], 2.0), mul_rn(cr[1], 2.0), mul_rn(cr[2], 2.0)};
-                const double c2[3] = {sub_rn(mul_rn(qv[1], t[2]), mul_rn(qv[2], t[1])),
-                                      sub_rn(mul_rn(qv[2], t[0]), mul_rn(qv[0], t[2])),
-                                      sub_rn(mul_rn(qv[0], t[1]), mul_rn(qv[1], t[0]))};
-                for (int i = 0; i < 3; ++i) rot[i] = add_rn(add_rn(loc[i], mul_rn(t[i], q[0])), c2[i]);
-            }
-            for (int i = 0; i < 3; ++i) S.np_[s][i] = add_rn(ref[i], rot[i]);
-        }
-        S.n_new = ns;
-        return;
-    }
-    // nothing to act on, or a single-site rotation: no further draws
-    if (c.n_mol == 0 || (S.move == 1 && ns < 2)) {
-        S.valid = 0;
-        return;
-    }
-    const uint32_t mi = (uint32_t)(u01(c) * (double)c.n_mol);
+// The molecule `mi`'s sites as the old ones.
+__device__ __forceinline__ void take_old(const GcmcConst& C, const GcmcPtrs& P, const double* gx,
+                                         const double* gy, const double* gz, const uint32_t* mol,
+                                         const uint32_t* msp, uint32_t mi, StepShared& S) {
+    const int k = (int)msp[mi];
+    const int ns = C.sp_ns[k];
     S.mi = mi;
+    S.sp_old = k;
     for (int s = 0; s < ns; ++s) {
-        const uint32_t gi = mol[(size_t)mi * ns + s];
+        const uint32_t gi = mol[(size_t)mi * C.ns + s];
         S.ex[s] = gi;
         const uint32_t slot = gi - (uint32_t)C.n_fw;
         S.op[s][0] = gx[slot];
@@ -366,12 +329,89 @@ __device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, 
         S.op[s][2] = gz[slot];
     }
     S.n_old = ns;
-    if (S.move == 3) {
+}
+
+// The pick-th molecule of species k (index order): the engine's
+// moleculeIndicesOfSpecies(k)[pick].
+__device__ __forceinline__ uint32_t nth_of_species(const uint32_t* msp, uint64_t n_mol, int k,
+                                                   uint64_t pick) {
+    uint64_t seen = 0;
+    for (uint64_t m = 0; m < n_mol; ++m)
+        if ((int)msp[m] == k && seen++ == pick) return (uint32_t)m;
+    return 0;
+}
+
+// Thread 0: the draws and trial geometry of one move (run, monte_carlo_engine.cc:
+// 405-439: 25 % each of translate, rotate, insert, delete for one species; 20 %
+// each plus identity swap for several).
+__device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, const double* gx,
+                          const double* gy, const double* gz, const uint32_t* mol,
+                          const uint32_t* msp, StepShared& S) {
+    const double pick = u01(c);
+    const bool mixture = C.n_gsp >= 2;
+    if (!mixture)
+        S.move = pick < 0.25 ? 0 : pick < 0.5 ? 1 : pick < 0.75 ? 2 : 3;
+    else
+        S.move = pick < 0.2 ? 0 : pick < 0.4 ? 1 : pick < 0.6 ? 2 : pick < 0.8 ? 3 : 4;
+    S.valid = 1;
+    S.accept = 0;
+    S.do_resync = 0;
+    S.n_old = S.n_new = 0;
+    S.sp_old = S.sp_new = 0;
+    S.ng = c.n_guest;
+    S.lq = 0.0;
+    for (int s = 0; s < MAXS; ++s) S.ex[s] = 0xffffffffu;
+    const bool rl = C.draw_order == ALEA_DRAWS_RIGHT_TO_LEFT;
+    if (S.move == 2) {  // attemptInsertion (monte_carlo_engine.cc:556-619)
+        const int k = mixture ? (int)(u01(c) * (double)C.n_gsp) : 0;
+        if (C.prop_cells > 0) {
+            plan_biased_insertion(C, P, c, S, k);
+            return;
+        }
+        double u[3];
+        u[0] = u01(c);
+        u[1] = u01(c);
+        u[2] = u01(c);
+        if (rl) {
+            const double t = u[0];
+            u[0] = u[2];
+            u[2] = t;
+        }
+        const double* M = C.L.m;
+        double ref[3];
+        for (int i = 0; i < 3; ++i)
+            ref[i] = add_rn(add_rn(mul_rn(M[i], u[0]), mul_rn(M[3 + i], u[1])), mul_rn(M[6 + i], u[2]));
+        double q[4] = {1.0, 0.0, 0.0, 0.0};
+        if (C.sp_ns[k] > 1) draw_quaternion(C, c, q, rl);
+        place_new(C, k, ref, q, false, S);
+        return;
+    }
+    if (c.n_mol == 0) {  // nothing to act on: no further draws
+        S.valid = 0;
+        return;
+    }
+    if (S.move == 1 && !mixture && C.sp_ns[0] < 2) {  // single species, single site: no draw
+        S.valid = 0;
+        return;
+    }
+    if (S.move == 3) {  // attemptDeletion (:621-671)
+        uint32_t mi;
+        if (!mixture) {
+            mi = (uint32_t)(u01(c) * (double)c.n_mol);
+        } else {
+            const int k = (int)(u01(c) * (double)C.n_gsp);
+            if (c.n_of[k] == 0) {
+                S.valid = 0;
+                return;
+            }
+            mi = nth_of_species(msp, c.n_mol, k, (uint64_t)(u01(c) * (double)c.n_of[k]));
+        }
+        take_old(C, P, gx, gy, gz, mol, msp, mi, S);
         if (C.prop_cells > 0) {  // the proposal's density at the molecule's centroid
             double cen[3] = {0.0, 0.0, 0.0};
-            for (int s = 0; s < ns; ++s)
+            for (int s = 0; s < S.n_old; ++s)
                 for (int i = 0; i < 3; ++i) cen[i] += S.op[s][i];
-            for (int i = 0; i < 3; ++i) cen[i] /= (double)ns;
+            for (int i = 0; i < 3; ++i) cen[i] /= (double)S.n_old;
             double f[3];
             for (int a = 0; a < 3; ++a)
                 f[a] = cen[0] * C.L.inv[a] + cen[1] * C.L.inv[3 + a] + cen[2] * C.L.inv[6 + a];
@@ -379,6 +419,36 @@ __device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, 
         }
         return;
     }
+    if (S.move == 4) {  // attemptSwap (:673-792)
+        const int from = (int)(u01(c) * (double)C.n_gsp);
+        if (c.n_of[from] == 0) {
+            S.valid = 0;
+            return;
+        }
+        const uint32_t mi = nth_of_species(msp, c.n_mol, from, (uint64_t)(u01(c) * (double)c.n_of[from]));
+        int to = (int)(u01(c) * (double)(C.n_gsp - 1));
+        if (to >= from) ++to;
+        take_old(C, P, gx, gy, gz, mol, msp, mi, S);
+        // moleculeCentroid (:74-80)
+        double cen[3] = {0.0, 0.0, 0.0};
+        for (int s = 0; s < S.n_old; ++s)
+            for (int i = 0; i < 3; ++i) cen[i] = add_rn(cen[i], S.op[s][i]);
+        const double inv = 1.0 / (double)S.n_old;
+        for (int i = 0; i < 3; ++i) cen[i] = mul_rn(cen[i], inv);
+        double q[4] = {1.0, 0.0, 0.0, 0.0};
+        if (C.sp_ns[to] > 1) draw_quaternion(C, c, q, rl);
+        place_new(C, to, cen, q, false, S);
+        return;
+    }
+    // translate or rotate: any molecule
+    const uint32_t mi = (uint32_t)(u01(c) * (double)c.n_mol);
+    take_old(C, P, gx, gy, gz, mol, msp, mi, S);
+    const int ns = S.n_old;
+    if (S.move == 1 && ns < 2) {  // this molecule's species is single-site
+        S.valid = 0;
+        return;
+    }
+    S.sp_new = S.sp_old;
     if (S.move == 0) {  // braced initializer: left-to-right draws (:454-456)
         double d[3];
         for (int i = 0; i < 3; ++i) d[i] = mul_rn(sub_rn(mul_rn(2.0, u01(c)), 1.0), C.max_trans);
@@ -408,6 +478,30 @@ __device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, 
     S.n_new = ns;
 }
 
+// The double-float copy of a guest site's position (the FP32 form's input).
+__device__ __forceinline__ void put_hilo(float4* ghi, float4* glo, uint32_t slot, const double* p,
+                                         double q) {
+    const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
+    ghi[slot] = make_float4(x.hi, y.hi, z.hi, (float)q);
+    glo[slot] = make_float4(x.lo, y.lo, z.lo, 0.f);
+}
+
+// Per slot (old sites, then new): charge and pair-table row of its species' site.
+__device__ __forceinline__ void slot_tables(const GcmcConst& C, StepShared& S) {
+    for (int e = 0; e < 2 * MAXS; ++e) {
+        S.sq_slot[e] = 0.0;
+        S.row_slot[e] = 0;
+    }
+    for (int s = 0; s < S.n_old; ++s) {
+        S.sq_slot[s] = C.spq[S.sp_old][s];
+        S.row_slot[s] = C.sprow[S.sp_old][s];
+    }
+    for (int s = 0; s < S.n_new; ++s) {
+        S.sq_slot[C.ns + s] = C.spq[S.sp_new][s];
+        S.row_slot[C.ns + s] = C.sprow[S.sp_new][s];
+    }
+}
+
 // The grid's value at site slot e (old sites first, then new): its LJ
 // species' table interpolated at the site (frameworkEnergyGrid_->interpolate,
 // monte_carlo_engine.cc:353-356).
@@ -416,8 +510,9 @@ __device__ __forceinline__ double site_grid_energy(const GcmcConst& C, const Gcm
                                                    const StepShared& S, int e) {
     const int s = e < NS ? e : e - NS;
     const double* p = e < NS ? S.op[s] : S.np_[s];
-    return C.grid_fast ? grid_interp_fast(C.L, C.gn[0], C.gn[1], C.gn[2], P.gtab[s], p[0], p[1], p[2])
-                       : grid_interp_ref(C.L, C.gn[0], C.gn[1], C.gn[2], P.gtab[s], p[0], p[1], p[2]);
+    const double* tab = P.gtab[S.row_slot[e]];
+    return C.grid_fast ? grid_interp_fast(C.L, C.gn[0], C.gn[1], C.gn[2], tab, p[0], p[1], p[2])
+                       : grid_interp_ref(C.L, C.gn[0], C.gn[1], C.gn[2], tab, p[0], p[1], p[2]);
 }
 
 // Per-site phase tables in dynamic shared memory. FP64 form: e^{i n theta_a}
@@ -443,9 +538,9 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     __shared__ StepShared S;
     __shared__ double red[(GT / 32 + 1) * RSTRIDE];
     __shared__ double eq[2 * NS];
-    __shared__ PairParams srow[NS][64];
-    __shared__ PairF32 srow32[F32 ? NS : 1][64];
-    __shared__ PairCloseFF srowff[F32 ? NS : 1][64];
+    __shared__ PairParams srow[F32 ? 1 : MAXROWS][64];
+    __shared__ PairF32 srow32[F32 ? MAXROWS : 1][64];
+    __shared__ PairCloseFF srowff[F32 ? MAXROWS : 1][64];
     __shared__ float4 sph[F32 ? 2 * NS : 1], spl[F32 ? 2 * NS : 1];  // trial sites, hi + lo
     extern __shared__ __align__(16) unsigned char dyn[];
 
@@ -460,6 +555,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     float4* ghi = P.ghi + so;
     float4* glo = P.glo + so;
     uint32_t* mol = P.mol + (size_t)chain * C.max_mol * NS;
+    uint32_t* msp = P.msp + (size_t)chain * C.max_mol;
     double* sre = P.sre + (size_t)chain * C.nk;
     double* sim = P.sim + (size_t)chain * C.nk;
     double* dre = P.dre + (size_t)chain * C.nk;
@@ -469,17 +565,18 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     float* dre32 = F32 ? P.dre32 + (size_t)chain * C.nk : nullptr;
     float* dim32 = F32 ? P.dim32 + (size_t)chain * C.nk : nullptr;
     const int K = C.kmax;
-    for (int i = threadIdx.x; i < NS * (int)C.n_species; i += GT) {
-        const PairParams pp = P.table[(size_t)C.slj[i / C.n_species] * C.n_species + i % C.n_species];
-        srow[i / C.n_species][i % C.n_species] = pp;
-        if constexpr (F32) {
+    for (int i = threadIdx.x; i < C.n_rows * (int)C.n_species; i += GT) {
+        const int r = i / C.n_species, t = i % C.n_species;
+        const PairParams pp = P.table[(size_t)C.row_lj[r] * C.n_species + t];
+        if constexpr (!F32) {
+            srow[r][t] = pp;
+        } else {
             const double s2 = pp.sigma * pp.sigma, s6 = s2 * s2 * s2;
-            srow32[i / C.n_species][i % C.n_species] =
-                PairF32{(float)(4.0 * pp.eps * s6 * s6), (float)(4.0 * pp.eps * s6), (float)pp.shift,
-                        (float)pp.dvdrc, (float)s2};
+            srow32[r][t] = PairF32{(float)(4.0 * pp.eps * s6 * s6), (float)(4.0 * pp.eps * s6),
+                                   (float)pp.shift, (float)pp.dvdrc, (float)s2};
             const ff fs2 = ff_from(s2), fe4 = ff_from(4.0 * pp.eps), fsh = ff_from(pp.shift);
-            srowff[i / C.n_species][i % C.n_species] =
-                PairCloseFF{fs2.hi, fs2.lo, fe4.hi, fe4.lo, fsh.hi, fsh.lo, (float)pp.dvdrc, 0.f};
+            srowff[r][t] = PairCloseFF{fs2.hi, fs2.lo, fe4.hi, fe4.lo, fsh.hi, fsh.lo,
+                                       (float)pp.dvdrc, 0.f};
         }
     }
     const int tw = 2 * C.kmax + 1;
@@ -492,7 +589,8 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     for (uint64_t step = 0; step < steps; ++step) {
         if (threadIdx.x == 0) {
             if (c.err == 0) {
-                plan_move(C, P, c, gx, gy, gz, mol, S);
+                plan_move(C, P, c, gx, gy, gz, mol, msp, S);
+                slot_tables(C, S);
                 if constexpr (F32) {
                     for (int e = 0; e < 2 * NS; ++e) {
                         const double* p = e < NS ? S.op[e] : S.np_[e - NS];
@@ -549,7 +647,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
 #pragma unroll
                     for (int e = 0; e < 2 * NS; ++e) {
                         const bool is_old = e < NS;
-                        if (is_old ? (n_old == 0) : (n_new == 0)) continue;
+                        if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
                         const int s = is_old ? e : e - NS;
                         const float4 ph = sph[e], pl = spl[e];
                         ff dx = ff_add(ff{ah.x, al.x}, ff{-ph.x, -pl.x});
@@ -561,10 +659,10 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         const bool el_in = C.charged && r2 <= rce2f;
                         if (!lj_in && !el_in) continue;
                         if (lj_in) {
-                            const PairF32 q = srow32[s][ta];
+                            const PairF32 q = srow32[S.row_slot[e]][ta];
                             if (r2 < q.sig2) {
                                 const ff rr = ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
-                                closef[e] = ff_add(closef[e], lj_close_ff(srowff[s][ta], rr, rcf, C.trunc));
+                                closef[e] = ff_add(closef[e], lj_close_ff(srowff[S.row_slot[e]][ta], rr, rcf, C.trunc));
                             } else {
                                 const float ir2 = 1.0f / r2;
                                 const float ir6 = ir2 * ir2 * ir2;
@@ -589,7 +687,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 if (C.grid) {  // thread e adds site slot e's interpolated table
 #pragma unroll
                     for (int e = 0; e < 2 * NS; ++e)
-                        if (threadIdx.x == e && (e < NS ? n_old : n_new))
+                        if (threadIdx.x == e && (e < NS ? e < n_old : e - NS < n_new))
                             v[2 * e] = ff_add(v[2 * e], ff_from(site_grid_energy<NS>(C, P, S, e)));
                 }
                 block_sum_ff(v, 4 * NS, red);
@@ -616,7 +714,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
 #pragma unroll
                 for (int e = 0; e < 2 * NS; ++e) {
                     const bool is_old = e < NS;
-                    if (is_old ? (n_old == 0) : (n_new == 0)) continue;
+                    if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
                     const int s = is_old ? e : e - NS;
                     const double* p = is_old ? S.op[s] : S.np_[s];
                     double dx, dy, dz;
@@ -626,7 +724,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     const bool el_in = C.charged && r2 <= C.rc_ew2 * (1.0 + 1e-12);
                     if (!lj_in && !el_in) continue;
                     const double r = sqrt(r2);
-                    if (lj_in) acc[2 * e] += lj_pair_rt(C.trunc, r, C.rc, srow[s][ta]);
+                    if (lj_in) acc[2 * e] += lj_pair_rt(C.trunc, r, C.rc, srow[S.row_slot[e]][ta]);
                     if (el_in && r <= C.rc_ew) acc[2 * e + 1] += a.w * (erfc(C.alpha * r) / r);
                 }
             }
@@ -634,7 +732,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 if (C.grid) {
 #pragma unroll
                     for (int e = 0; e < 2 * NS; ++e)
-                        if (threadIdx.x == e && (e < NS ? n_old : n_new))
+                        if (threadIdx.x == e && (e < NS ? e < n_old : e - NS < n_new))
                             acc[2 * e] += site_grid_energy<NS>(C, P, S, e);
                 }
                 block_sum_n(acc, 4 * NS, red);
@@ -644,7 +742,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 for (int e = 0; e < 2 * NS; ++e) {
                     const int s = e < NS ? e : e - NS;
                     S.e_lj[e] = acc[2 * e];
-                    S.e_el[e] = (C.sq[s] * acc[2 * e + 1]) * kCoulomb;
+                    S.e_el[e] = (S.sq_slot[e] * acc[2 * e + 1]) * kCoulomb;
                 }
 
             // ---- reciprocal delta: removed = old sites, added = new sites
@@ -654,7 +752,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 for (int i = threadIdx.x; i < 2 * NS * 3 * tw; i += GT) {
                     const int e = i / (3 * tw), a = (i / tw) % 3, n = i % tw - K;
                     const bool is_old = e < NS;
-                    if (is_old ? (n_old == 0) : (n_new == 0)) continue;
+                    if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
                     const int s = is_old ? e : e - NS;
                     const double* p = is_old ? S.op[s] : S.np_[s];
                     const double th = C.b[3 * a] * p[0] + C.b[3 * a + 1] * p[1] + C.b[3 * a + 2] * p[2];
@@ -668,9 +766,9 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 for (int i = threadIdx.x; ab_table && i < 2 * NS * tw * tw; i += GT) {
                     const int e = i / (tw * tw), n0 = (i / tw) % tw, n1 = i % tw;
                     const bool is_old = e < NS;
-                    if (is_old ? (n_old == 0) : (n_new == 0)) continue;
+                    if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
                     const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1];
-                    const float q = (float)C.sq[is_old ? e : e - NS];
+                    const float q = (float)S.sq_slot[e];
                     ab32[i] = make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
                 }
                 __syncthreads();
@@ -685,12 +783,13 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     auto zq = [&](int e) -> float2 {
                         if (ab_table) return ab32[(e * tw + n0) * tw + n1];
                         const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1];
-                        const float q = (float)C.sq[e < NS ? e : e - NS];
+                        const float q = (float)S.sq_slot[e];
                         return make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
                     };
                     if (n_new)  // added first (ewald_incremental_state.cc:107-111)
 #pragma unroll
                         for (int s = 0; s < NS; ++s) {
+                            if (s >= n_new) break;  // a smaller species' unused slots hold stale phases
                             const float2 Z = zq(NS + s);
                             const float2 Cc = etab32[((NS + s) * 3 + 2) * tw + n2];
                             re = fmaf(Z.x, Cc.x, fmaf(-Z.y, Cc.y, re));
@@ -699,6 +798,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     if (n_old)  // then removed (:112-116)
 #pragma unroll
                         for (int s = 0; s < NS; ++s) {
+                            if (s >= n_old) break;
                             const float2 Z = zq(s);
                             const float2 Cc = etab32[(s * 3 + 2) * tw + n2];
                             re = fmaf(-Z.x, Cc.x, fmaf(Z.y, Cc.y, re));
@@ -715,18 +815,19 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 if (threadIdx.x == 0) {
                     S.rec_sum = C.rec_pref * red[(GT / 32) * RSTRIDE];
                     double q2a = 0.0, q2r = 0.0;
-                    for (int s = 0; s < n_new; ++s) q2a += C.sq[s] * C.sq[s];
-                    for (int s = 0; s < n_old; ++s) q2r += C.sq[s] * C.sq[s];
+                    for (int s = 0; s < n_new; ++s) q2a += S.sq_slot[NS + s] * S.sq_slot[NS + s];
+                    for (int s = 0; s < n_old; ++s) q2r += S.sq_slot[s] * S.sq_slot[s];
                     S.dself = C.self_pref * (q2a - q2r);
                     // a rigid molecule's exclusion sum is the template's
-                    S.dexcl = -kCoulomb * ((n_new ? C.excl_tmpl : 0.0) - (n_old ? C.excl_tmpl : 0.0));
+                    S.dexcl = -kCoulomb * ((n_new ? C.excl_tmpl[S.sp_new] : 0.0) -
+                                           (n_old ? C.excl_tmpl[S.sp_old] : 0.0));
                 }
               }
             } else if (C.charged) {
                 for (int i = threadIdx.x; i < 2 * NS * 3 * tw; i += GT) {
                     const int e = i / (3 * tw), a = (i / tw) % 3, n = i % tw - K;
                     const bool is_old = e < NS;
-                    if (is_old ? (n_old == 0) : (n_new == 0)) continue;
+                    if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
                     const int s = is_old ? e : e - NS;
                     const double* p = is_old ? S.op[s] : S.np_[s];
                     const double th = C.b[3 * a] * p[0] + C.b[3 * a + 1] * p[1] + C.b[3 * a + 2] * p[2];
@@ -734,7 +835,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     sincos((double)n * th, &sn, &cs);
                     etab[(e * 3 + a) * tw + n + K] = make_double2(cs, sn);
                 }
-                if (threadIdx.x < 2 * NS) eq[threadIdx.x] = C.sq[threadIdx.x % NS];
+                if (threadIdx.x < 2 * NS) eq[threadIdx.x] = S.sq_slot[threadIdx.x];
                 __syncthreads();
                 double racc = 0.0;
                 for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
@@ -743,6 +844,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     if (n_new)  // added first (ewald_incremental_state.cc:107-111)
 #pragma unroll
                         for (int s = 0; s < NS; ++s) {
+                            if (s >= n_new) break;  // a smaller species' unused slots hold stale phases
                             const double2 A = etab[((NS + s) * 3 + 0) * tw + n0], B = etab[((NS + s) * 3 + 1) * tw + n1],
                                           Cc = etab[((NS + s) * 3 + 2) * tw + n2];
                             const double abr = A.x * B.x - A.y * B.y, abi = A.x * B.y + A.y * B.x;
@@ -752,6 +854,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     if (n_old)  // then removed (:112-116)
 #pragma unroll
                         for (int s = 0; s < NS; ++s) {
+                            if (s >= n_old) break;
                             const double2 A = etab[(s * 3 + 0) * tw + n0], B = etab[(s * 3 + 1) * tw + n1],
                                           Cc = etab[(s * 3 + 2) * tw + n2];
                             const double abr = A.x * B.x - A.y * B.y, abi = A.x * B.y + A.y * B.x;
@@ -769,11 +872,11 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 if (threadIdx.x == 0) {
                     S.rec_sum = C.rec_pref * v[0];
                     double q2a = 0.0, q2r = 0.0;
-                    for (int s = 0; s < n_new; ++s) q2a += C.sq[s] * C.sq[s];
-                    for (int s = 0; s < n_old; ++s) q2r += C.sq[s] * C.sq[s];
+                    for (int s = 0; s < n_new; ++s) q2a += S.sq_slot[NS + s] * S.sq_slot[NS + s];
+                    for (int s = 0; s < n_old; ++s) q2r += S.sq_slot[s] * S.sq_slot[s];
                     S.dself = C.self_pref * (q2a - q2r);
-                    S.dexcl = -kCoulomb * (exclusion_sum(C.L, S.np_, C.sq, n_new, C.alpha) -
-                                           exclusion_sum(C.L, S.op, C.sq, n_old, C.alpha));
+                    S.dexcl = -kCoulomb * (exclusion_sum(C.L, S.np_, &S.sq_slot[NS], n_new, C.alpha) -
+                                           exclusion_sum(C.L, S.op, &S.sq_slot[0], n_old, C.alpha));
                 }
             }
 
@@ -796,19 +899,26 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     ratio = exp(-du / T);
                 } else if (S.move == 2) {
                     du = u_new + e_new + rec;
-                    ratio = (c.fugacity * C.volume / T) / (double)(c.n_mol + 1) * exp(-du / T);
+                    ratio = (c.fugacity[S.sp_new] * C.volume / T) / (double)(c.n_of[S.sp_new] + 1) *
+                            exp(-du / T);
                     // learned proposal: divided by its density (relative to uniform)
                     if (C.prop_cells > 0) ratio *= exp(-S.lq);
-                } else {
+                } else if (S.move == 3) {
                     du = -(u_old + e_old) + rec;
-                    ratio = (double)c.n_mol / (c.fugacity * C.volume / T) * exp(-du / T);
+                    ratio = (double)c.n_of[S.sp_old] / (c.fugacity[S.sp_old] * C.volume / T) *
+                            exp(-du / T);
                     // the reverse insertion's proposal density at this centroid
                     if (C.prop_cells > 0) ratio *= exp(S.lq);
+                } else {  // swapRatio (gcmc_acceptance.hpp:89-95)
+                    du = (u_new - u_old) + (e_new - e_old) + rec;
+                    ratio = (c.fugacity[S.sp_new] / c.fugacity[S.sp_old]) *
+                            ((double)c.n_of[S.sp_old] / (double)(c.n_of[S.sp_new] + 1)) * exp(-du / T);
                 }
                 c.attempted[S.move]++;
                 const double prob = ratio < 1.0 ? ratio : 1.0;
                 S.accept = u01(c) < prob ? 1 : 0;
-                if (S.accept && S.move == 2 && c.n_mol + 1 > C.max_mol) {
+                if (S.accept && ((S.move == 2 && c.n_mol + 1 > C.max_mol) ||
+                                 (S.move >= 2 && c.n_guest + S.n_new > C.max_sites))) {
                     c.err |= DEV_ERR_CAPACITY;  // the chain stops; the host reports it
                     S.accept = 0;
                 }
@@ -838,34 +948,10 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         c.self_e += S.dself;
                         c.excl_e += S.dexcl;
                     }
-                    if (S.move <= 1) {
-                        for (int s = 0; s < NS; ++s) {
-                            const uint32_t slot = S.ex[s] - (uint32_t)C.n_fw;
-                            gx[slot] = S.np_[s][0];
-                            gy[slot] = S.np_[s][1];
-                            gz[slot] = S.np_[s][2];
-                            put_hilo(ghi, glo, slot, S.np_[s], C.sq[s]);
-                        }
-                    } else if (S.move == 2) {
-                        for (int s = 0; s < NS; ++s) {
-                            const uint32_t slot = (uint32_t)c.n_guest + s;
-                            gx[slot] = S.np_[s][0];
-                            gy[slot] = S.np_[s][1];
-                            gz[slot] = S.np_[s][2];
-                            gq[slot] = C.sq[s];
-                            gt[slot] = C.slj[s];
-                            put_hilo(ghi, glo, slot, S.np_[s], C.sq[s]);
-                            mol[(size_t)c.n_mol * NS + s] = (uint32_t)C.n_fw + slot;
-                        }
-                        c.n_guest += NS;
-                        c.n_mol += 1;
-                    } else {
-                        uint32_t idx[NS];
-                        for (int s = 0; s < NS; ++s) idx[s] = S.ex[s];
-                        for (uint32_t m = S.mi; m + 1 < c.n_mol; ++m)
-                            for (int s = 0; s < NS; ++s) mol[(size_t)m * NS + s] = mol[(size_t)(m + 1) * NS + s];
-                        c.n_mol -= 1;
-                        for (int k = 0; k < NS; ++k) {
+                    // removeParticleIndices (monte_carlo_engine.cc:825-848):
+                    // swap-with-last, fixing the molecule records that held the last site
+                    auto remove_sites = [&](uint32_t* idx, int n) {
+                        for (int k = 0; k < n; ++k) {
                             const uint32_t site = idx[k];
                             const uint32_t last = (uint32_t)(C.n_fw + c.n_guest - 1);
                             if (site != last) {
@@ -877,13 +963,61 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                                 gt[ds] = gt[ls];
                                 ghi[ds] = ghi[ls];
                                 glo[ds] = glo[ls];
-                                for (uint64_t m = 0; m < (uint64_t)c.n_mol * NS; ++m)
-                                    if (mol[m] == last) mol[m] = site;
-                                for (int k2 = k + 1; k2 < NS; ++k2)
+                                for (uint64_t m = 0; m < c.n_mol; ++m) {
+                                    const int nsm = C.sp_ns[msp[m]];
+                                    for (int s2 = 0; s2 < nsm; ++s2)
+                                        if (mol[(size_t)m * NS + s2] == last) mol[(size_t)m * NS + s2] = site;
+                                }
+                                for (int k2 = k + 1; k2 < n; ++k2)
                                     if (idx[k2] == last) idx[k2] = site;
                             }
                             c.n_guest -= 1;
                         }
+                    };
+                    // the new sites appended after the guests (insertion, swap)
+                    auto append_new = [&](uint64_t mrec) {
+                        for (int s = 0; s < S.n_new; ++s) {
+                            const uint32_t slot = (uint32_t)c.n_guest + s;
+                            gx[slot] = S.np_[s][0];
+                            gy[slot] = S.np_[s][1];
+                            gz[slot] = S.np_[s][2];
+                            gq[slot] = S.sq_slot[NS + s];
+                            gt[slot] = C.splj[S.sp_new][s];
+                            put_hilo(ghi, glo, slot, S.np_[s], S.sq_slot[NS + s]);
+                            mol[(size_t)mrec * NS + s] = (uint32_t)C.n_fw + slot;
+                        }
+                        msp[mrec] = (uint32_t)S.sp_new;
+                        c.n_guest += S.n_new;
+                    };
+                    if (S.move <= 1) {
+                        for (int s = 0; s < S.n_new; ++s) {
+                            const uint32_t slot = S.ex[s] - (uint32_t)C.n_fw;
+                            gx[slot] = S.np_[s][0];
+                            gy[slot] = S.np_[s][1];
+                            gz[slot] = S.np_[s][2];
+                            put_hilo(ghi, glo, slot, S.np_[s], S.sq_slot[NS + s]);
+                        }
+                    } else if (S.move == 2) {
+                        append_new(c.n_mol);
+                        c.n_mol += 1;
+                        c.n_of[S.sp_new] += 1;
+                    } else if (S.move == 3) {  // removeMolecule (:814-823): erase, then remove
+                        uint32_t idx[MAXS];
+                        for (int s = 0; s < S.n_old; ++s) idx[s] = S.ex[s];
+                        for (uint32_t m = S.mi; m + 1 < c.n_mol; ++m) {
+                            for (int s = 0; s < NS; ++s) mol[(size_t)m * NS + s] = mol[(size_t)(m + 1) * NS + s];
+                            msp[m] = msp[m + 1];
+                        }
+                        c.n_mol -= 1;
+                        c.n_of[S.sp_old] -= 1;
+                        remove_sites(idx, S.n_old);
+                    } else {  // swap: the molecule becomes the new species, then the old sites go
+                        uint32_t idx[MAXS];
+                        for (int s = 0; s < S.n_old; ++s) idx[s] = S.ex[s];
+                        append_new(S.mi);
+                        c.n_of[S.sp_old] -= 1;
+                        c.n_of[S.sp_new] += 1;
+                        remove_sites(idx, S.n_old);
                     }
                     if (C.charged) {
                         c.moves_since_resync++;
@@ -935,19 +1069,20 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         for (uint64_t g = 0; g < ng; ++g) q2 += gq[g] * gq[g];
                         c.self_e = C.self_pref * q2;
                         double ex = 0.0;
-                        if constexpr (F32)
-                            ex = (double)c.n_mol * C.excl_tmpl;
-                        else
+                        if constexpr (F32) {
+                            for (uint32_t m = 0; m < c.n_mol; ++m) ex += C.excl_tmpl[msp[m]];
+                        } else
                         for (uint32_t m = 0; m < c.n_mol; ++m) {
+                            const int nsm = C.sp_ns[msp[m]];
                             double p[MAXS][3], q[MAXS];
-                            for (int s = 0; s < NS; ++s) {
+                            for (int s = 0; s < nsm; ++s) {
                                 const uint32_t slot = mol[(size_t)m * NS + s] - (uint32_t)C.n_fw;
                                 p[s][0] = gx[slot];
                                 p[s][1] = gy[slot];
                                 p[s][2] = gz[slot];
                                 q[s] = gq[slot];
                             }
-                            ex += exclusion_sum(C.L, p, q, NS, C.alpha);
+                            ex += exclusion_sum(C.L, p, q, nsm, C.alpha);
                         }
                         c.excl_e = -kCoulomb * ex;
                     }
@@ -1014,22 +1149,26 @@ struct GcmcImpl {
     DevBuf<unsigned> flags;
     DevBuf<double> pcdf, plogp;  // the chains' copy of a tabulated proposal
     DevBuf<float4> fwh, fwl, ghi, glo;  // FP32 form: double-float positions
+    DevBuf<uint32_t> msp;               // species of each molecule, per chain
     DevBuf<float> w32, sre32, sim32, dre32, dim32;  // FP32 form: S(k) copies and deltas
-    const double* gtab[MAXS] = {};  // the borrowed grid's tables, per site
+    const double* gtab[MAXROWS] = {};  // the borrowed grid's tables, per pair-table row
     float last_ms = 0.f;
 };
 
 GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const alea_particles& fw,
-                      const alea_lattice& lat, const alea_molecule_species& guest,
+                      const alea_lattice& lat, uint32_t n_gsp, const alea_molecule_species* guests,
                       double temperature, const double* fugacity_pa, const uint64_t* seeds,
                       const uint64_t* streams, uint32_t n_chains, double max_translation,
                       double max_rotation, int draw_order, uint32_t max_molecules) {
     require(n_chains >= 1, ALEA_ERR_INVALID_ARGUMENT, "GCMC: at least one chain");
-    require(guest.n_sites >= 1 && guest.n_sites <= MAXS, ALEA_ERR_INVALID_ARGUMENT,
-            "GCMC: the species needs 1..8 sites");
-    require(guest.n_sites == 1 || guest.n_sites == 2 || guest.n_sites == 3 || guest.n_sites == 4 ||
-                guest.n_sites == 5,
-            ALEA_ERR_INVALID_ARGUMENT, "GCMC: 1..5 sites per molecule are compiled");
+    require(n_gsp >= 1 && n_gsp <= (uint32_t)MAXGS, ALEA_ERR_INVALID_ARGUMENT,
+            "GCMC: 1..4 guest species");
+    int ns_max = 0;
+    for (uint32_t k = 0; k < n_gsp; ++k) {
+        require(guests[k].n_sites >= 1 && guests[k].n_sites <= 5, ALEA_ERR_INVALID_ARGUMENT,
+                "GCMC: 1..5 sites per molecule are compiled");
+        ns_max = std::max(ns_max, (int)guests[k].n_sites);
+    }
     require(temperature > 0.0, ALEA_ERR_INVALID_ARGUMENT,
             "MonteCarloEngine: temperatureKelvin must be positive");
     require(lj.cutoff > 0.0 && lj.n_species >= 1 && lj.n_species <= 64, ALEA_ERR_INVALID_ARGUMENT,
@@ -1039,48 +1178,66 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
             ALEA_ERR_INVALID_ARGUMENT, "GCMC: unknown draw order");
     require(fw.n == 0 || (fw.x && fw.y && fw.z), ALEA_ERR_INVALID_ARGUMENT,
             "GCMC: framework coordinates missing");
-    for (uint32_t c = 0; c < n_chains; ++c)
-        require(fugacity_pa[c] * (1.0 / (1.380649e-23 * 1.0e30)) > 0.0, ALEA_ERR_INVALID_ARGUMENT,
+    for (uint64_t i = 0; i < (uint64_t)n_chains * n_gsp; ++i)
+        require(fugacity_pa[i] * (1.0 / (1.380649e-23 * 1.0e30)) > 0.0, ALEA_ERR_INVALID_ARGUMENT,
                 "MonteCarloEngine: every fugacityPascal must be positive");
     auto* g = new GcmcImpl();
     try {
         GcmcConst& C = g->C;
         C.L = make_lattice(lat.m);
         validate_cutoff(C.L, lj.cutoff, "MonteCarloEngine (LJ)");
-        C.ns = (int)guest.n_sites;
-        double qs = 0.0;
-        for (uint32_t s = 0; s < guest.n_sites; ++s) {
-            require(guest.lj_species[s] < lj.n_species, ALEA_ERR_OUT_OF_RANGE,
-                    "GCMC: site LJ species out of range");
-            C.sx[s] = guest.x[s];
-            C.sy[s] = guest.y[s];
-            C.sz[s] = guest.z[s];
-            C.sq[s] = guest.charge ? guest.charge[s] : 0.0;
-            C.slj[s] = guest.lj_species[s];
-            C.tc[s][0] = guest.x[s];
-            C.tc[s][1] = guest.y[s];
-            C.tc[s][2] = guest.z[s];
-            qs += C.sq[s];
-        }
-        {  // pairExclusionSum of the template (ewald_incremental_state.cc:32-43): a rigid
-           // molecule's, wherever it is (its pairs are far shorter than half a cell)
+        C.ns = ns_max;
+        C.n_gsp = (int)n_gsp;
+        C.n_rows = 0;
+        for (uint32_t k = 0; k < n_gsp; ++k) {
+            const alea_molecule_species& guest = guests[k];
+            C.sp_ns[k] = (int)guest.n_sites;
+            double qs = 0.0;
+            for (uint32_t s = 0; s < guest.n_sites; ++s) {
+                require(guest.lj_species[s] < lj.n_species, ALEA_ERR_OUT_OF_RANGE,
+                        "GCMC: site LJ species out of range");
+                C.spx[k][s] = guest.x[s];
+                C.spy[k][s] = guest.y[s];
+                C.spz[k][s] = guest.z[s];
+                C.spq[k][s] = guest.charge ? guest.charge[s] : 0.0;
+                C.splj[k][s] = guest.lj_species[s];
+                int r = 0;
+                while (r < C.n_rows && C.row_lj[r] != guest.lj_species[s]) ++r;
+                if (r == C.n_rows) {
+                    require(C.n_rows < MAXROWS, ALEA_ERR_INVALID_ARGUMENT,
+                            "GCMC: at most 8 distinct LJ species among the guest sites");
+                    C.row_lj[C.n_rows++] = guest.lj_species[s];
+                }
+                C.sprow[k][s] = r;
+                C.tc[k][s][0] = guest.x[s];
+                C.tc[k][s][1] = guest.y[s];
+                C.tc[k][s][2] = guest.z[s];
+                qs += C.spq[k][s];
+            }
+            // monte_carlo_engine.cc:273-293
+            if (ew)
+                require(std::fabs(qs) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
+                        "MonteCarloEngine: GCMC species " + std::to_string(k) +
+                            " is not individually charge-neutral (total site charge = " +
+                            std::to_string(qs) + " e)");
+            // pairExclusionSum of the template (ewald_incremental_state.cc:32-43): a rigid
+            // molecule's, wherever it is (its pairs are far shorter than half a cell)
             double ex = 0.0;
             for (int i = 0; i < (int)guest.n_sites; ++i)
                 for (int j = i + 1; j < (int)guest.n_sites; ++j) {
                     const double dx = guest.x[j] - guest.x[i], dy = guest.y[j] - guest.y[i],
                                  dz = guest.z[j] - guest.z[i];
                     const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
-                    const double qq = C.sq[i] * C.sq[j];
+                    const double qq = C.spq[k][i] * C.spq[k][j];
                     if (ew) ex += qq * (r < 1e-8 ? 2.0 * ew->alpha / std::sqrt(kPi) : std::erf(ew->alpha * r) / r);
                 }
-            C.excl_tmpl = ex;
-        }
-        {  // the template about its centroid (the learned proposal's reference point)
+            C.excl_tmpl[k] = ex;
+            // the template about its centroid (the learned proposal's reference point)
             double m[3] = {0.0, 0.0, 0.0};
-            for (int s = 0; s < C.ns; ++s)
-                for (int i = 0; i < 3; ++i) m[i] += C.tc[s][i];
-            for (int s = 0; s < C.ns; ++s)
-                for (int i = 0; i < 3; ++i) C.tc[s][i] -= m[i] / C.ns;
+            for (int s = 0; s < C.sp_ns[k]; ++s)
+                for (int i = 0; i < 3; ++i) m[i] += C.tc[k][s][i];
+            for (int s = 0; s < C.sp_ns[k]; ++s)
+                for (int i = 0; i < 3; ++i) C.tc[k][s][i] -= m[i] / C.sp_ns[k];
         }
         C.n_species = lj.n_species;
         C.rc = lj.cutoff;
@@ -1092,7 +1249,7 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         C.draw_order = draw_order;
         C.n_fw = fw.n;
         C.max_mol = max_molecules;
-        C.max_sites = max_molecules * guest.n_sites;
+        C.max_sites = max_molecules * (uint32_t)C.ns;
         C.volume = std::fabs(C.L.volume);
         std::vector<double4> packed(fw.n);
         std::vector<uint32_t> types(fw.n, 0);
@@ -1112,8 +1269,6 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         EwaldStateImpl* ews = nullptr;
         if (ew) {
             // monte_carlo_engine.cc:273-293
-            require(std::fabs(qs) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
-                    "MonteCarloEngine: GCMC species 0 is not individually charge-neutral");
             require(std::fabs(fwq) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
                     "MonteCarloEngine: framework is not charge-neutral");
             require(ew->kmax <= KMAXC, ALEA_ERR_INVALID_ARGUMENT, "GCMC: kMax <= 64 supported");
@@ -1197,6 +1352,7 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         g->mol.alloc(sites);
         g->ghi.alloc(sites);
         g->glo.alloc(sites);
+        g->msp.alloc((size_t)max_molecules * n_chains);
         std::vector<ChainState> st(n_chains);
         const double self0 = ews ? ewald_state_view(ews).self_pref * fwq2 : 0.0;
         for (uint32_t c = 0; c < n_chains; ++c) {
@@ -1204,7 +1360,8 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
             s = ChainState{};
             s.seed = seeds[c];
             s.stream = streams[c];
-            s.fugacity = fugacity_pa[c] * (1.0 / (1.380649e-23 * 1.0e30));
+            for (uint32_t k = 0; k < n_gsp; ++k)
+                s.fugacity[k] = fugacity_pa[(size_t)c * n_gsp + k] * (1.0 / (1.380649e-23 * 1.0e30));
             s.self_e = self0;
         }
         if (ews) {
@@ -1254,7 +1411,8 @@ void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s) {
     P.ghi = g->ghi.p;
     P.glo = g->glo.p;
     P.w32 = g->w32.p;
-    for (int s = 0; s < MAXS; ++s) P.gtab[s] = g->gtab[s];
+    for (int r = 0; r < MAXROWS; ++r) P.gtab[r] = g->gtab[r];
+    P.msp = g->msp.p;
     P.sre32 = g->sre32.p;
     P.sim32 = g->sim32.p;
     P.dre32 = g->dre32.p;
@@ -1377,11 +1535,11 @@ void gcmc_set_grid(GcmcImpl* g, const GridImpl* grid) {
         g->C.grid = 0;
         return;
     }
-    const GridView v0 = grid_view(grid, g->C.slj[0]);
+    const GridView v0 = grid_view(grid, g->C.row_lj[0]);
     for (int i = 0; i < 9; ++i)
         require(v0.L.m[i] == g->C.L.m[i], ALEA_ERR_INVALID_ARGUMENT,
                 "GCMC: the energy grid is for another cell");
-    for (int s = 0; s < g->C.ns; ++s) g->gtab[s] = grid_view(grid, g->C.slj[s]).table;
+    for (int r = 0; r < g->C.n_rows; ++r) g->gtab[r] = grid_view(grid, g->C.row_lj[r]).table;
     for (int a = 0; a < 3; ++a) g->C.gn[a] = v0.n[a];
     g->C.grid_fast = v0.fast;
     g->C.grid = 1;

@@ -229,7 +229,7 @@ void widom_batch_destroy(WidomBatchImpl* b);
 struct GcmcImpl;
 struct ChainState;
 GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const alea_particles& fw,
-                      const alea_lattice& lat, const alea_molecule_species& guest,
+                      const alea_lattice& lat, uint32_t n_species, const alea_molecule_species* guests,
                       double temperature, const double* fugacity_pa, const uint64_t* seeds,
                       const uint64_t* streams, uint32_t n_chains, double max_translation,
                       double max_rotation, int draw_order, uint32_t max_molecules);

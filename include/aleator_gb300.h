@@ -436,6 +436,19 @@ alea_status alea_gcmc_create(const alea_lennard_jones* lj, const alea_ewald* ewa
                              const uint64_t* streams, uint32_t n_chains, double max_translation,
                              double max_rotation, int32_t draw_order, uint32_t max_molecules,
                              alea_gcmc** out);
+/* The mixture constructor (monte_carlo_engine.hpp:143-151): n_species rigid
+ * species (1..4), fugacity_pa holds n_chains x n_species values (chain-major).
+ * With two or more species the move set is the reference's 5-way split with
+ * identity swaps (monte_carlo_engine.cc:405-439, 673-792); with one it is
+ * alea_gcmc_create. */
+alea_status alea_gcmc_create_mixture(const alea_lennard_jones* lj, const alea_ewald* ewald,
+                                     const alea_particles* framework, const alea_lattice* lattice,
+                                     uint32_t n_species, const alea_molecule_species* species,
+                                     double temperature, const double* fugacity_pa,
+                                     const uint64_t* seeds, const uint64_t* streams,
+                                     uint32_t n_chains, double max_translation,
+                                     double max_rotation, int32_t draw_order,
+                                     uint32_t max_molecules, alea_gcmc** out);
 /* run(numSteps) (monte_carlo_engine.hpp:163, .cc:405-439) on every chain. */
 alea_status alea_gcmc_run(alea_gcmc* g, uint64_t steps, void* cuda_stream);
 typedef struct {
@@ -444,8 +457,9 @@ typedef struct {
     uint64_t call_index;     /* Philox draws consumed so far */
     uint64_t steps;
     uint64_t resyncs;        /* S(k) rebuilds (maybeResyncEwald) */
-    uint64_t attempted[4];   /* translate, rotate, insert, delete */
-    uint64_t accepted[4];
+    uint64_t attempted[5];   /* translate, rotate, insert, delete, swap */
+    uint64_t accepted[5];
+    uint64_t species_molecules[4]; /* moleculeCountOfSpecies(k) (monte_carlo_engine.hpp:179) */
     double sum_molecules;    /* sum over moves of the molecule count after the move */
     double sum_molecules_sq;
     double last_du;

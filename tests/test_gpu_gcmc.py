@@ -165,3 +165,34 @@ def test_large_kmax_chain_matches_oracle(lib, orc):
         _compare(gpu, cpu, charged=True)
     with pytest.raises(ValueError):
         _pair(A, orc, fw, W.co2_guest(fw), dict(alpha=0.31, rc=12.0, kmax=65), fug, 3, 7)
+
+
+@pytest.mark.parametrize("charged", [False, True])
+def test_mixture_chain_matches_oracle(lib, orc, charged):
+    """Two species (CH4 and CO2; the mixture constructor, monte_carlo_engine.hpp:
+    143-151): 20 % each of translate, rotate, insert, delete and identity swap.
+    Same moves, decisions, per-species counts and particle order as the oracle
+    (itself bit-identical to the reference's mixture engine)."""
+    A, _ = lib
+    fw = W.cubic_framework(seed=21, charged=charged)
+    if charged:
+        fw.charge = fw.charge * 0.15
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    ewd = dict(alpha=0.31, rc=12.0, kmax=5) if charged else None
+    ew = A.Ewald(0.31, 12.0, 5) if charged else None
+    ch4 = dict(W.ch4_guest(fw), charge=[0.0])
+    guests = [W.co2_guest(fw), ch4] if charged else [ch4, dict(W.co2_guest(fw), charge=[0.0] * 3)]
+    fugs = [orc.pr_fugacity(*W.CO2_CRITICAL, 298.0, 5e5), orc.pr_fugacity(*W.METHANE_CRITICAL, 298.0, 2e6)]
+    if not charged:
+        fugs = fugs[::-1]
+    gpu = A.GcmcChains(ff, p, fw.lattice, guests, 298.0, [fugs], [9], [4], ewald=ew)
+    od = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.8, truncation=O.SHIFTED)
+    cpu = orc.gcmc_mixture(od, ewd, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guests,
+                           298.0, fugs, 9, 4)
+    for _ in range(5):
+        gpu.run(400)
+        cpu.run(400)
+        _compare(gpu, cpu, charged=charged)
+        assert gpu.info()["species_molecules"][:2] == [cpu.molecules_of(k) for k in range(2)]
+    assert gpu.info()["accepted"][4] > 0  # swaps accepted

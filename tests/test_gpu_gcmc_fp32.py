@@ -126,3 +126,32 @@ def test_fp32_with_energy_grid_matches_fp64_loading(lib, orc):
     se = np.hypot(m64.std(ddof=1), m32.std(ddof=1)) / np.sqrt(n)
     assert m64.mean() > 1.0
     assert abs(m32.mean() - m64.mean()) <= 3 * se, (m32.mean(), m64.mean(), se)
+
+
+def test_fp32_mixture_loading_matches_fp64(lib, orc):
+    """CH4 + charged CO2 (field weakened to 0.15) with identity swaps: per
+    species, the mean loading of the FP32 chains within 3 combined standard
+    errors of the FP64 chains'."""
+    A, _ = lib
+    n = 64
+    fw = W.cubic_framework(seed=13, charged=True)
+    fw.charge = fw.charge * 0.15
+    ew = A.Ewald(0.31, 12.0, 6)
+    guests = [W.co2_guest(fw), W.ch4_guest(fw)]
+    fugs = [orc.pr_fugacity(*W.CO2_CRITICAL, KT, 5e5), orc.pr_fugacity(*W.METHANE_CRITICAL, KT, 2e6)]
+    out = {}
+    for prec in (A.FP64, A.FP32):
+        ch = _chains(A, fw, guests, ew, [fugs] * n, list(range(200, 200 + n)), [5] * n, prec)
+        ch.run(3000)
+        snaps = []
+        for _ in range(12):
+            ch.run(500)
+            snaps.append([ch.info(c)["species_molecules"][:2] for c in range(n)])
+        out[prec] = np.array(snaps, dtype=np.float64).mean(axis=0)  # chains x species
+        info = ch.info(0)
+        assert info["attempted"][4] > 0 and info["accepted"][4] > 0
+    for k in range(2):
+        m64, m32 = out[A.FP64][:, k], out[A.FP32][:, k]
+        se = np.hypot(m64.std(ddof=1), m32.std(ddof=1)) / np.sqrt(n)
+        assert m64.mean() > 0.5, (k, m64.mean())
+        assert abs(m32.mean() - m64.mean()) <= 3 * se, (k, m32.mean(), m64.mean(), se)
