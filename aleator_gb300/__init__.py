@@ -39,6 +39,7 @@ from ._lib import (  # noqa: F401
     lj_tail_correction,
     load_library,
     peng_robinson_fugacity,
+    peng_robinson_mixture,
     philox4x32_10,
     philox_u64,
     philox_uniform,

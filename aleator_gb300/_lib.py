@@ -243,6 +243,8 @@ _SIGNATURES = {
     "alea_swap_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                           ctypes.c_uint64, ctypes.c_double, ctypes.c_double]),
     "alea_peng_robinson_fugacity": (ctypes.c_int32, [ctypes.c_double] * 5 + [_D]),
+    "alea_peng_robinson_mixture": (ctypes.c_int32, [ctypes.c_uint32, _D, _D, _D, _D,
+                                                    ctypes.c_double, ctypes.c_double, _D, _D, _D]),
 }
 
 _LIB = None
@@ -1076,3 +1078,27 @@ def peng_robinson_fugacity(tc, pc, omega, t, p):
     v = ctypes.c_double()
     _check(library().alea_peng_robinson_fugacity(tc, pc, omega, t, p, ctypes.byref(v)))
     return v.value
+
+
+def peng_robinson_mixture(substances, t, p, mole_fractions, kij=None):
+    """PengRobinsonMixture(substances, kij): (compressibilityFactor,
+    fugacitiesPascal) at temperature t (K), total pressure p (Pa) and the mole
+    fractions; substances = [(tc, pc, omega), ...], kij an n x n matrix or None."""
+    n = len(substances)
+    tc, pc, om = (np.ascontiguousarray([s[i] for s in substances], dtype=np.float64)
+                  for i in range(3))
+    k = None  # the constructor's check comes before fugacitiesPascal's
+    if kij is not None:
+        k = np.ascontiguousarray(kij, dtype=np.float64)
+        if n >= 2 and k.shape != (n, n):
+            raise ValueError("PengRobinsonMixture: binaryInteractionKij must be substances.size() x "
+                             "substances.size()")
+    x = np.ascontiguousarray(mole_fractions, dtype=np.float64)
+    if n >= 2 and x.shape != (n,):
+        raise ValueError("PengRobinsonMixture: moleFractions.size() must equal the number of substances")
+    f = np.zeros(n)
+    z = ctypes.c_double()
+    _check(library().alea_peng_robinson_mixture(n, _dp(tc), _dp(pc), _dp(om),
+                                                None if k is None else _dp(k), t, p, _dp(x),
+                                                ctypes.byref(z), _dp(f)))
+    return z.value, f

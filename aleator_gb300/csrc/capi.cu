@@ -981,6 +981,30 @@ double alea_swap_ratio(double f_from, double f_to, uint64_t n_from, uint64_t n_t
     return (f_to / f_from) * ((double)n_from / (double)(n_to + 1)) * std::exp(-du / t);
 }
 
+// The gas-phase root of Z^3 - (1-B) Z^2 + (A - 3B^2 - 2B) Z - (AB - B^2 - B^3):
+// Newton from Z = 1, kept above B (peng_robinson.cc:62-100; the mixture's
+// solve, :236-276, is the same with the mixture's A and B).
+static double pr_gas_root(double A, double B, const char* who, double t, double p) {
+    const double c2 = -(1.0 - B), c1 = A - 3.0 * B * B - 2.0 * B, c0 = -(A * B - B * B - B * B * B);
+    double z = 1.0;
+    bool converged = false;
+    for (int it = 0; it < 100; ++it) {
+        const double fz = z * z * z + c2 * z * z + c1 * z + c0;
+        if (std::fabs(fz) < 1e-14) {
+            converged = true;
+            break;
+        }
+        const double fp = 3.0 * z * z + 2.0 * c2 * z + c1;
+        if (fp == 0.0) break;
+        z -= fz / fp;
+        if (!(z > B)) z = B + 0.5 * (1.0 - B > 0 ? 1.0 - B : 1.0);
+    }
+    if (!converged && std::fabs(z * z * z + c2 * z * z + c1 * z + c0) > 1e-8)
+        throw alea::Error(ALEA_ERR_RUNTIME, std::string(who) + ": Newton-Raphson did not converge for T=" +
+                                                std::to_string(t) + " K, P=" + std::to_string(p) + " Pa");
+    return z;
+}
+
 // PengRobinson (peng_robinson.cc:10-110): a scalar Newton solve, host side.
 alea_status alea_peng_robinson_fugacity(double tc, double pc, double omega, double t, double p,
                                         double* out) {
@@ -998,26 +1022,89 @@ alea_status alea_peng_robinson_fugacity(double tc, double pc, double omega, doub
         const double aa = a * (term * term);
         const double A = aa * p / (R * R * t * t);
         const double B = b * p / (R * t);
-        const double c2 = -(1.0 - B), c1 = A - 3.0 * B * B - 2.0 * B, c0 = -(A * B - B * B - B * B * B);
-        double z = 1.0;
-        bool converged = false;
-        for (int it = 0; it < 100; ++it) {
-            const double fz = z * z * z + c2 * z * z + c1 * z + c0;
-            if (std::fabs(fz) < 1e-14) {
-                converged = true;
-                break;
-            }
-            const double fp = 3.0 * z * z + 2.0 * c2 * z + c1;
-            if (fp == 0.0) break;
-            z -= fz / fp;
-            if (!(z > B)) z = B + 0.5 * (1.0 - B > 0 ? 1.0 - B : 1.0);
-        }
-        if (!converged && std::fabs(z * z * z + c2 * z * z + c1 * z + c0) > 1e-8)
-            throw alea::Error(ALEA_ERR_RUNTIME, "PengRobinson::compressibilityFactor: Newton-Raphson did not converge");
+        const double z = pr_gas_root(A, B, "PengRobinson::compressibilityFactor", t, p);
         const double s2 = 1.41421356237309504880;
         const double lnphi = (z - 1.0) - std::log(z - B) -
                              (A / (2.0 * s2 * B)) * std::log((z + (1.0 + s2) * B) / (z + (1.0 - s2) * B));
         *out = std::exp(lnphi) * p;
+    });
+}
+
+// PengRobinsonMixture (peng_robinson.cc:112-309): van der Waals one-fluid
+// mixing, a_ij = sqrt(a_i(T) a_j(T)) (1 - k_ij), a_mix = sum x_i x_j a_ij,
+// b_mix = sum x_i b_i; the mixture's Z from the pure form's cubic; per
+// component f_i = x_i phi_i P with ln phi_i = (b_i/b)(Z-1) - ln(Z-B)
+// - A/(2 sqrt2 B) [(2/a) sum_j x_j a_ij - b_i/b] ln[(Z+(1+sqrt2)B)/(Z+(1-sqrt2)B)].
+alea_status alea_peng_robinson_mixture(uint32_t n, const double* tc, const double* pc,
+                                       const double* omega, const double* kij, double t, double p,
+                                       const double* x, double* z_out, double* f_out) {
+    return guarded([&] {
+        auto bad = [](const std::string& m) { throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, m); };
+        if (n < 2) bad("PengRobinsonMixture: needs at least 2 substances (use PengRobinson for a pure component)");
+        need(tc, "tc");
+        need(pc, "pc");
+        need(omega, "omega");
+        need(x, "mole_fractions");
+        need(f_out, "out");
+        const double R = 8.31446261815324;
+        std::vector<double> a(n), b(n), kappa(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            if (!(tc[i] > 0.0)) bad("PengRobinsonMixture: criticalTemperatureKelvin must be positive");
+            if (!(pc[i] > 0.0)) bad("PengRobinsonMixture: criticalPressurePascal must be positive");
+            a[i] = 0.45724 * R * R * tc[i] * tc[i] / pc[i];
+            b[i] = 0.07780 * R * tc[i] / pc[i];
+            kappa[i] = 0.37464 + 1.54226 * omega[i] - 0.26992 * omega[i] * omega[i];
+        }
+        // k_ij: n x n, zero diagonal, symmetric (NULL: every k_ij = 0)
+        auto k = [&](uint32_t i, uint32_t j) { return kij ? kij[(size_t)i * n + j] : 0.0; };
+        if (kij)
+            for (uint32_t i = 0; i < n; ++i) {
+                if (kij[(size_t)i * n + i] != 0.0)
+                    bad("PengRobinsonMixture: binaryInteractionKij diagonal must be zero (k_ii = 0)");
+                for (uint32_t j = i + 1; j < n; ++j)
+                    if (kij[(size_t)i * n + j] != kij[(size_t)j * n + i])
+                        bad("PengRobinsonMixture: binaryInteractionKij must be symmetric (k_ij = k_ji)");
+            }
+        // fugacitiesPascal checks the mole fractions, then compressibilityFactor T and P
+        double sum = 0.0;
+        for (uint32_t i = 0; i < n; ++i) {
+            if (!(x[i] >= 0.0)) bad("PengRobinsonMixture: every mole fraction must be >= 0");
+            sum += x[i];
+        }
+        if (std::fabs(sum - 1.0) > 1e-9)
+            bad("PengRobinsonMixture: mole fractions must sum to 1 (got " + std::to_string(sum) + ")");
+        if (!(t > 0.0)) bad("PengRobinsonMixture: temperatureKelvin must be positive");
+        if (!(p > 0.0)) bad("PengRobinsonMixture: totalPressurePascal must be positive");
+        std::vector<double> aa(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            const double term = 1.0 + kappa[i] * (1.0 - std::sqrt(t / tc[i]));
+            aa[i] = a[i] * (term * term);
+        }
+        // a_mix as compressibilityFactor forms it (x_i x_j a_ij) and as
+        // fugacitiesPascal does ((x_i x_j sqrt(..)) (1 - k_ij)); their last bits can differ
+        double amix_z = 0.0, amix = 0.0, bmix = 0.0;
+        for (uint32_t i = 0; i < n; ++i) {
+            bmix += x[i] * b[i];
+            for (uint32_t j = 0; j < n; ++j) {
+                const double g = std::sqrt(aa[i] * aa[j]);
+                amix_z += x[i] * x[j] * (g * (1.0 - k(i, j)));
+                amix += x[i] * x[j] * g * (1.0 - k(i, j));
+            }
+        }
+        const double Az = amix_z * p / (R * R * t * t);
+        const double B = bmix * p / (R * t);
+        const double z = pr_gas_root(Az, B, "PengRobinsonMixture::compressibilityFactor", t, p);
+        const double A = amix * p / (R * R * t * t);
+        const double s2 = 1.41421356237309504880;
+        for (uint32_t i = 0; i < n; ++i) {
+            double sj = 0.0;
+            for (uint32_t j = 0; j < n; ++j) sj += x[j] * std::sqrt(aa[i] * aa[j]) * (1.0 - k(i, j));
+            const double lnphi = (b[i] / bmix) * (z - 1.0) - std::log(z - B) -
+                                 (A / (2.0 * s2 * B)) * ((2.0 / amix) * sj - b[i] / bmix) *
+                                     std::log((z + (1.0 + s2) * B) / (z + (1.0 - s2) * B));
+            f_out[i] = x[i] * std::exp(lnphi) * p;
+        }
+        if (z_out) *z_out = z;
     });
 }
 

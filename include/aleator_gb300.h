@@ -514,6 +514,15 @@ double alea_swap_ratio(double f_from, double f_to, uint64_t n_from, uint64_t n_t
 /* PengRobinson::fugacityPascal (engines/monte_carlo/peng_robinson.cc:108-110) */
 alea_status alea_peng_robinson_fugacity(double tc, double pc, double omega, double t, double p,
                                         double* out);
+/* PengRobinsonMixture(substances, binaryInteractionKij).fugacitiesPascal and
+ * .compressibilityFactor (engines/monte_carlo/peng_robinson.hpp:127-155,
+ * peng_robinson.cc:112-309): n >= 2 substances (tc, pc, omega), kij an n x n
+ * row-major matrix (symmetric, zero diagonal) or NULL for every k_ij = 0,
+ * mole fractions x summing to 1. f_out[i] = x_i phi_i P (Pa); z_out (may be
+ * NULL) the mixture's compressibility factor. */
+alea_status alea_peng_robinson_mixture(uint32_t n, const double* tc, const double* pc,
+                                       const double* omega, const double* kij, double t, double p,
+                                       const double* x, double* z_out, double* f_out);
 
 #ifdef __cplusplus
 }

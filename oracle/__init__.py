@@ -167,6 +167,9 @@ class Oracle:
                                 ctypes.c_uint64, ctypes.c_int, ctypes.c_int, _D]
         L.orc_pr_fugacity.restype = ctypes.c_double
         L.orc_pr_fugacity.argtypes = [ctypes.c_double] * 5
+        L.orc_pr_mixture.restype = ctypes.c_int
+        L.orc_pr_mixture.argtypes = [ctypes.c_uint32, _D, _D, _D, _D, ctypes.c_double,
+                                     ctypes.c_double, _D, _D, _D]
         L.orc_random_unit_quaternion.argtypes = [ctypes.c_double] * 3 + [_D]
         L.orc_rotate_by_quaternion.argtypes = [_D, _D, _D]
         self._keep = []
@@ -307,6 +310,21 @@ class Oracle:
 
     def pr_fugacity(self, tc, pc, omega, t, p):
         return self.lib.orc_pr_fugacity(tc, pc, omega, t, p)
+
+    def pr_mixture(self, substances, t, p, x, kij=None):
+        """(Z, [f_i]) of PengRobinsonMixture; substances = [(tc, pc, omega), ...]."""
+        tc, pc, om = (np.ascontiguousarray([s[i] for s in substances], dtype=np.float64)
+                      for i in range(3))
+        xs = np.ascontiguousarray(x, dtype=np.float64)
+        k = None if kij is None else np.ascontiguousarray(kij, dtype=np.float64)
+        f = np.zeros(len(substances))
+        z = ctypes.c_double()
+        rc = self.lib.orc_pr_mixture(len(substances), _dp(tc), _dp(pc), _dp(om),
+                                     None if k is None else _dp(k), t, p, _dp(xs),
+                                     ctypes.byref(z), _dp(f))
+        if rc != 0:
+            raise ValueError("PengRobinsonMixture: invalid argument")
+        return z.value, f
 
     def gcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature, fugacity_pa, seed,
              stream, max_translation=1.5, max_rotation=0.5, draw_order=DRAWS_RIGHT_TO_LEFT,
@@ -579,6 +597,9 @@ class Reference:
         L.ref_gcmc_destroy.argtypes = [ctypes.c_void_p]
         L.ref_pr_fugacity.restype = ctypes.c_double
         L.ref_pr_fugacity.argtypes = [ctypes.c_double] * 5
+        L.ref_pr_mixture.restype = ctypes.c_int
+        L.ref_pr_mixture.argtypes = [ctypes.c_uint32, _D, _D, _D, _D, ctypes.c_double,
+                                     ctypes.c_double, _D, _D, _D, ctypes.c_char_p, ctypes.c_size_t]
 
     def philox4x32_10(self, ctr, key):
         c = np.asarray(ctr, dtype=np.uint32)
@@ -701,6 +722,23 @@ class Reference:
 
     def pr_fugacity(self, tc, pc, omega, t, p):
         return self.lib.ref_pr_fugacity(tc, pc, omega, t, p)
+
+    def pr_mixture(self, substances, t, p, x, kij=None):
+        """(Z, [f_i]) from the reference's PengRobinsonMixture; its exception
+        message raised as ValueError."""
+        tc, pc, om = (np.ascontiguousarray([s[i] for s in substances], dtype=np.float64)
+                      for i in range(3))
+        xs = np.ascontiguousarray(x, dtype=np.float64)
+        k = None if kij is None else np.ascontiguousarray(kij, dtype=np.float64)
+        f = np.zeros(len(substances))
+        z = ctypes.c_double()
+        msg = ctypes.create_string_buffer(512)
+        rc = self.lib.ref_pr_mixture(len(substances), _dp(tc), _dp(pc), _dp(om),
+                                     None if k is None else _dp(k), t, p, _dp(xs),
+                                     ctypes.byref(z), _dp(f), msg, 512)
+        if rc != 0:
+            raise ValueError(msg.value.decode())
+        return z.value, f
 
     def gcmc(self, ff, ewald, m, x, y, z, q, species, guest, temperature, fugacity_pa, seed,
              stream, max_translation=1.5, max_rotation=0.5, grid=None):

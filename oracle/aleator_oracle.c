@@ -982,6 +982,72 @@ double orc_clamp_probability(double r) { return r < 1.0 ? r : 1.0; }
 
 /* ------------------------------------------------------------------ Peng-Robinson */
 
+/* the gas-phase Newton root shared by both forms (peng_robinson.cc:62-100, 236-276) */
+static double orc_pr_root(double A, double B) {
+    const double c2 = -(1.0 - B);
+    const double c1 = A - 3.0 * B * B - 2.0 * B;
+    const double c0 = -(A * B - B * B - B * B * B);
+    double zz = 1.0;
+    for (int iter = 0; iter < 100; ++iter) {
+        const double fz = zz * zz * zz + c2 * zz * zz + c1 * zz + c0;
+        if (fabs(fz) < 1e-14) break;
+        const double fp = 3.0 * zz * zz + 2.0 * c2 * zz + c1;
+        if (fp == 0.0) break;
+        zz -= fz / fp;
+        if (!(zz > B)) zz = B + 0.5 * (1.0 - B > 0 ? 1.0 - B : 1.0);
+    }
+    return zz;
+}
+
+/* PengRobinsonMixture (peng_robinson.cc:112-309): one-fluid mixing; Z from the
+ * mixture's A (a_mix summed as x_i x_j a_ij, :229-235) and B; the fugacities
+ * from a_mix summed as (x_i x_j sqrt(a_i a_j)) (1 - k_ij) (:288-295). */
+int orc_pr_mixture(uint32_t n, const double* tc, const double* pc, const double* omega,
+                   const double* kij, double t, double p, const double* x, double* z_out,
+                   double* f_out) {
+    const double R = 8.31446261815324;
+    if (n < 2 || n > 64) return -1;
+    double b[64], aa[64];
+    double sum = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!(tc[i] > 0.0) || !(pc[i] > 0.0) || !(x[i] >= 0.0)) return -1;
+        sum += x[i];
+    }
+    if (fabs(sum - 1.0) > 1e-9 || !(t > 0.0) || !(p > 0.0)) return -1;
+    for (uint32_t i = 0; i < n; ++i) {
+        const double a = 0.45724 * R * R * tc[i] * tc[i] / pc[i];
+        b[i] = 0.07780 * R * tc[i] / pc[i];
+        const double kappa = 0.37464 + 1.54226 * omega[i] - 0.26992 * omega[i] * omega[i];
+        const double term = 1.0 + kappa * (1.0 - sqrt(t / tc[i]));
+        aa[i] = a * (term * term);
+    }
+    double amix_z = 0.0, amix = 0.0, bmix = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        bmix += x[i] * b[i];
+        for (uint32_t j = 0; j < n; ++j) {
+            const double k = kij ? kij[(size_t)i * n + j] : 0.0;
+            const double aij = sqrt(aa[i] * aa[j]) * (1.0 - k);
+            amix_z += x[i] * x[j] * aij;
+            amix += x[i] * x[j] * sqrt(aa[i] * aa[j]) * (1.0 - k);
+        }
+    }
+    const double B = bmix * p / (R * t);
+    const double zz = orc_pr_root(amix_z * p / (R * R * t * t), B);
+    const double A = amix * p / (R * R * t * t);
+    const double sqrt2 = 1.41421356237309504880;
+    for (uint32_t i = 0; i < n; ++i) {
+        double sj = 0.0;
+        for (uint32_t j = 0; j < n; ++j)
+            sj += x[j] * sqrt(aa[i] * aa[j]) * (1.0 - (kij ? kij[(size_t)i * n + j] : 0.0));
+        const double lnphi = (b[i] / bmix) * (zz - 1.0) - log(zz - B) -
+                             (A / (2.0 * sqrt2 * B)) * ((2.0 / amix) * sj - b[i] / bmix) *
+                                 log((zz + (1.0 + sqrt2) * B) / (zz + (1.0 - sqrt2) * B));
+        f_out[i] = x[i] * exp(lnphi) * p;
+    }
+    if (z_out) *z_out = zz;
+    return 0;
+}
+
 /* peng_robinson.cc:10-110 (kGasConstant peng_robinson.hpp:46) */
 double orc_pr_fugacity(double tc, double pc, double omega, double t, double p) {
     const double R = 8.31446261815324;

@@ -155,6 +155,12 @@ double orc_clamp_probability(double r);
 
 /* ---- Peng-Robinson (peng_robinson.cc:10-110) ---- */
 double orc_pr_fugacity(double tc, double pc, double omega, double t, double p);
+/* PengRobinsonMixture::compressibilityFactor / fugacitiesPascal
+ * (peng_robinson.cc:112-309); kij n x n row-major or NULL. Returns 0, or -1
+ * for an argument the reference rejects. */
+int orc_pr_mixture(uint32_t n, const double* tc, const double* pc, const double* omega,
+                   const double* kij, double t, double p, const double* x, double* z_out,
+                   double* f_out);
 
 #ifdef __cplusplus
 }

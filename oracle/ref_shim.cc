@@ -13,6 +13,7 @@
 #include <array>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <filesystem>
 #include <memory>
@@ -560,6 +561,28 @@ void ref_gcmc_destroy(void* h) { delete static_cast<RefGcmc*>(h); }
 // ---------------------------------------------------------------- Peng-Robinson
 double ref_pr_fugacity(double tc, double pc, double omega, double t, double p) {
     return engines::PengRobinson({tc, pc, omega}).fugacityPascal(t, p);
+}
+
+// PengRobinsonMixture: 0, or -1 with the exception's message in msg
+int ref_pr_mixture(uint32_t n, const double* tc, const double* pc, const double* omega,
+                   const double* kij, double t, double p, const double* x, double* z_out,
+                   double* f_out, char* msg, size_t cap) {
+    try {
+        std::vector<engines::PengRobinsonSubstance> subs;
+        for (uint32_t i = 0; i < n; ++i) subs.push_back({tc[i], pc[i], omega[i]});
+        std::vector<std::vector<double>> k;
+        if (kij)
+            for (uint32_t i = 0; i < n; ++i) k.emplace_back(kij + (size_t)i * n, kij + (size_t)(i + 1) * n);
+        const engines::PengRobinsonMixture eos(std::move(subs), std::move(k));
+        const std::vector<double> xs(x, x + n);
+        const auto f = eos.fugacitiesPascal(t, p, xs);
+        for (uint32_t i = 0; i < n; ++i) f_out[i] = f[i];
+        *z_out = eos.compressibilityFactor(t, p, xs);
+        return 0;
+    } catch (const std::exception& e) {
+        std::snprintf(msg, cap, "%s", e.what());
+        return -1;
+    }
 }
 
 }  // extern "C"

@@ -237,6 +237,36 @@ def main():
         co2=np.array([ref.pr_fugacity(*W.CO2_CRITICAL, 298.0, p) for p in pressures]),
         ch4=np.array([ref.pr_fugacity(*W.METHANE_CRITICAL, 298.0, p) for p in pressures]))
 
+    # ---- PengRobinsonMixture: CO2 + CH4 (k_ij 0 and 0.09), CO2 + N2 + CH4, over
+    # pressures and compositions; critical constants as in the workloads
+    n2 = (126.19, 3.3958e6, 0.0372)  # the reference's mixture test substance
+    mix_cases = [([W.CO2_CRITICAL, W.METHANE_CRITICAL], None),
+                 ([W.CO2_CRITICAL, W.METHANE_CRITICAL], [[0.0, 0.09], [0.09, 0.0]]),
+                 ([W.CO2_CRITICAL, n2, W.METHANE_CRITICAL], None)]
+    rows, fails = [], []
+    for ci, (subs, kij) in enumerate(mix_cases):
+        for t in (250.0, 298.0, 350.0):
+            for p in (1e4, 1e6, 5e6):
+                for x0 in (0.1, 0.5, 0.85):
+                    x = [x0, 1.0 - x0] if len(subs) == 2 else [x0, (1.0 - x0) * 0.6, (1.0 - x0) * 0.4]
+                    try:
+                        z, f = ref.pr_mixture(subs, t, p, x, kij)
+                    except ValueError:  # the reference's Newton solve gives up (near condensation)
+                        fails.append([ci, t, p] + x + [0.0] * (3 - len(x)))
+                        continue
+                    rows.append([ci, t, p] + x + [0.0] * (3 - len(x)) + [z] + list(f) +
+                                [0.0] * (3 - len(f)))
+    fixtures["peng_robinson_mixture"] = dict(
+        tc=np.array([[s[0] for s in c] + [0.0] * (3 - len(c)) for c, _ in mix_cases]),
+        pc=np.array([[s[1] for s in c] + [1.0] * (3 - len(c)) for c, _ in mix_cases]),
+        omega=np.array([[s[2] for s in c] + [0.0] * (3 - len(c)) for c, _ in mix_cases]),
+        n=np.array([len(c) for c, _ in mix_cases]),
+        kij=np.array([np.zeros((3, 3)) if k is None else np.pad(np.array(k), ((0, 1), (0, 1)))
+                      for _, k in mix_cases]),
+        has_kij=np.array([k is not None for _, k in mix_cases]),
+        rows=np.array(rows),  # case, T, P, x0..x2, Z, f0..f2
+        fails=np.array(fails).reshape(-1, 6))  # case, T, P, x0..x2: the solve does not converge
+
     for name, data in fixtures.items():
         np.savez_compressed(OUT / f"{name}.npz", **data)
     (OUT / "MANIFEST.json").write_text(json.dumps(

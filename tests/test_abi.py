@@ -115,3 +115,47 @@ def test_no_device_is_reported_not_faked(so):
         A.FrameworkEnergyGrid(A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED),
                               A.ParticleData.from_framework(fw), fw.lattice, [4], 2.0)
     assert e.value.status == 5
+
+
+def test_peng_robinson_mixture(so):
+    """alea_peng_robinson_mixture (a host call) against the reference's values,
+    its identities (test_peng_robinson.cc:147-210) and its argument errors."""
+    import aleator_gb300 as A
+    from aleator_gb300 import workloads as W
+    from tests.test_oracle_golden import _pr_mixture_cases
+
+    g, cases = _pr_mixture_cases()
+    for row in g["rows"]:
+        n, subs, kij = cases[int(row[0])]
+        z, f = A.peng_robinson_mixture(subs, row[1], row[2], row[3:3 + n], kij)
+        assert z == row[6]
+        assert np.array_equal(f, row[7:7 + n])
+    for row in g["fails"]:  # where the reference's Newton solve gives up, so does this one
+        n, subs, kij = cases[int(row[0])]
+        with pytest.raises(RuntimeError, match="did not converge"):
+            A.peng_robinson_mixture(subs, row[1], row[2], row[3:3 + n], kij)
+    # two identical components: the pure substance split by mole fraction
+    ch4 = W.METHANE_CRITICAL
+    for t, p in [(298.15, 1e5), (298.15, 1e7), (350.0, 5e6)]:
+        fp = A.peng_robinson_fugacity(*ch4, t, p)
+        for x0 in (0.5, 0.1, 0.999):
+            _, f = A.peng_robinson_mixture([ch4, ch4], t, p, [x0, 1 - x0])
+            assert abs(f[0] - x0 * fp) <= 1e-10 * fp and abs(f[1] - (1 - x0) * fp) <= 1e-10 * fp
+    # ideal-gas limit
+    _, f = A.peng_robinson_mixture([W.CO2_CRITICAL, (126.19, 3.3958e6, 0.0372)], 298.15, 1.0, [0.3, 0.7])
+    assert abs(f[0] / 0.3 - 1) < 1e-6 and abs(f[1] / 0.7 - 1) < 1e-6
+    bad = [
+        (([ch4], 298.0, 1e5, [1.0], None), "needs at least 2 substances"),
+        (([ch4, (0.0, 1e6, 0.0)], 298.0, 1e5, [0.5, 0.5], None), "criticalTemperatureKelvin must be positive"),
+        (([ch4, ch4], 298.0, 1e5, [0.5, 0.5], [[0.1, 0.0], [0.0, 0.0]]), "diagonal must be zero"),
+        (([ch4, ch4], 298.0, 1e5, [0.5, 0.5], [[0.0, 0.1], [0.2, 0.0]]), "must be symmetric"),
+        (([ch4, ch4], 298.0, 1e5, [0.5, 0.5], [[0.0]]), "must be substances.size"),
+        (([ch4, ch4], 298.0, 1e5, [1.0], None), "moleFractions.size"),
+        (([ch4, ch4], 298.0, 1e5, [1.2, -0.2], None), "every mole fraction must be >= 0"),
+        (([ch4, ch4], 298.0, 1e5, [0.5, 0.6], None), "must sum to 1"),
+        (([ch4, ch4], -1.0, 1e5, [0.5, 0.5], None), "temperatureKelvin must be positive"),
+        (([ch4, ch4], 298.0, 0.0, [0.5, 0.5], None), "totalPressurePascal must be positive"),
+    ]
+    for args, msg in bad:
+        with pytest.raises(ValueError, match=msg):
+            A.peng_robinson_mixture(*args)

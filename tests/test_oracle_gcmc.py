@@ -89,3 +89,28 @@ def test_mixture_chain_bit_identical_to_reference(orc, ref, charged):
     ctr = b.counters()
     assert ctr[9] > 0, ctr  # swaps accepted
     assert min(a.molecules_of(k) for k in range(2)) > 0
+
+
+def test_peng_robinson_mixture_errors_match_reference(ref):
+    """The library's argument errors carry the reference's own exception text."""
+    import aleator_gb300 as A
+    from aleator_gb300.build import LIB, build
+
+    if not LIB.exists():
+        build()
+    ch4 = W.METHANE_CRITICAL
+    cases = [
+        ([ch4, (0.0, 1e6, 0.0)], 298.0, 1e5, [0.5, 0.5], None),
+        ([ch4, ch4], 298.0, 1e5, [0.5, 0.5], [[0.1, 0.0], [0.0, 0.0]]),
+        ([ch4, ch4], 298.0, 1e5, [0.5, 0.5], [[0.0, 0.1], [0.2, 0.0]]),
+        ([ch4, ch4], 298.0, 1e5, [1.2, -0.2], None),
+        ([ch4, ch4], 298.0, 1e5, [0.5, 0.6], None),
+        ([ch4, ch4], -1.0, 1e5, [0.5, 0.5], None),
+        ([ch4, ch4], 298.0, 0.0, [0.5, 0.5], None),
+    ]
+    for args in cases:
+        with pytest.raises(ValueError) as mine:
+            A.peng_robinson_mixture(*args)
+        with pytest.raises(ValueError) as theirs:
+            ref.pr_mixture(*args)
+        assert str(mine.value) == str(theirs.value)

@@ -198,3 +198,25 @@ def test_peng_robinson(orc):
     for i, P in enumerate(p["pressures"]):
         assert abs(orc.pr_fugacity(*W.CO2_CRITICAL, 298.0, P) / p["co2"][i] - 1) <= 1e-13
         assert abs(orc.pr_fugacity(*W.METHANE_CRITICAL, 298.0, P) / p["ch4"][i] - 1) <= 1e-13
+
+
+def _pr_mixture_cases():
+    g = golden("peng_robinson_mixture")
+    cases = []
+    for ci in range(len(g["n"])):
+        n = int(g["n"][ci])
+        subs = [(g["tc"][ci][i], g["pc"][ci][i], g["omega"][ci][i]) for i in range(n)]
+        kij = g["kij"][ci][:n, :n] if g["has_kij"][ci] else None
+        cases.append((n, subs, kij))
+    return g, cases
+
+
+def test_peng_robinson_mixture(orc):
+    """The oracle's PengRobinsonMixture against the reference's Z and partial
+    fugacities (two and three components, k_ij = 0 and 0.09)."""
+    g, cases = _pr_mixture_cases()
+    for row in g["rows"]:
+        n, subs, kij = cases[int(row[0])]
+        z, f = orc.pr_mixture(subs, row[1], row[2], row[3:3 + n], kij)
+        assert z == row[6]
+        assert np.array_equal(f, row[7:7 + n])
