@@ -1442,13 +1442,32 @@ __global__ void grid_interpolate_kernel(Lattice L, int nx, int ny, int nz,
 // fractional transform as multiplies by the inverse cell (no IEEE divisions)
 // and fused lerps: about 40 FP64 operations per query instead of about 100,
 // within ~1e-12 relative of the reference form's value (not bit-equal).
-__global__ void grid_interpolate_fast_kernel(Lattice L, int nx, int ny, int nz,
-                                             const double* __restrict__ table,
-                                             const double* __restrict__ xyz, uint64_t n,
-                                             double* __restrict__ out) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    out[i] = grid_interp_fast(L, nx, ny, nz, table, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+// FP32-form grids: a persistent grid-stride loop, one query per thread and
+// turn: locate in double-float, the eight corner loads issued together
+// (predicated, no early exit, so the warp's gathers stay in flight together),
+// then the blend; a query outside the double-float range goes to FP64.
+__global__ void __launch_bounds__(256)
+grid_interpolate_fast_kernel(Lattice L, InvFF inv, int nx, int ny, int nz,
+                             const double* __restrict__ table, const double* __restrict__ xyz,
+                             uint64_t n, double* __restrict__ out) {
+    const int cnt[3] = {nx, ny, nz};
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double px = xyz[3 * i], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
+        int i0[3], i1[3];
+        ff t[3];
+        const bool ok = grid_ff_locate(inv, cnt, px, py, pz, i0, i1, t);
+        double c[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int ix = (k & 1) ? i1[0] : i0[0], iy = (k & 2) ? i1[1] : i0[1],
+                      iz = (k & 4) ? i1[2] : i0[2];
+            c[k] = ok ? __ldg(&table[((size_t)iz * ny + iy) * nx + ix]) : 0.0;
+        }
+        double r;
+        if (!ok || !grid_ff_blend(c, t, r)) r = grid_interp_fast(L, nx, ny, nz, table, px, py, pz);
+        out[i] = r;
+    }
 }
 
 struct BuildArgs {
@@ -1812,10 +1831,20 @@ void grid_interpolate_device(const GridImpl* g, uint32_t species, const double* 
     if (n == 0) return;
     const unsigned blocks = (unsigned)((n + 255) / 256);
     // the FP64 form reproduces the reference's arithmetic bit for bit
-    if (g->precision == ALEA_FP32)
-        grid_interpolate_fast_kernel<<<blocks, 256, 0, s>>>(g->geo.L, g->geo.n[0], g->geo.n[1],
-                                                           g->geo.n[2], tab, xyz, n, out);
-    else
+    if (g->precision == ALEA_FP32) {
+        InvFF inv;
+        for (int k = 0; k < 9; ++k) {
+            const ff v = ff_from(g->geo.L.inv[k]);
+            inv.h[k] = v.hi;
+            inv.l[k] = v.lo;
+        }
+        int dev = 0, sms = 0;  // resident work for a persistent loop: 24 blocks per SM
+        ALEA_CUDA(cudaGetDevice(&dev));
+        ALEA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const unsigned fb = (unsigned)std::min<uint64_t>(blocks, (uint64_t)sms * 24);
+        grid_interpolate_fast_kernel<<<fb, 256, 0, s>>>(g->geo.L, inv, g->geo.n[0], g->geo.n[1],
+                                                       g->geo.n[2], tab, xyz, n, out);
+    } else
         grid_interpolate_kernel<<<blocks, 256, 0, s>>>(g->geo.L, g->geo.n[0], g->geo.n[1],
                                                       g->geo.n[2], tab, xyz, n, out);
     ALEA_CUDA(cudaGetLastError());

@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "ff.cuh"
 
 namespace alea {
 
@@ -83,6 +84,7 @@ __device__ __forceinline__ double grid_interp_fast(const Lattice& L, int nx, int
         int base = (int)g;  // g >= 0
         t[a] = g - (double)base;
         if (base >= cnt[a]) base -= cnt[a];  // f rounded up to 1
+        base = min(max(base, 0), cnt[a] - 1);  // NaN or infinite positions
         i0[a] = base;
         i1[a] = base + 1 == cnt[a] ? 0 : base + 1;
     }
@@ -95,6 +97,90 @@ __device__ __forceinline__ double grid_interp_fast(const Lattice& L, int nx, int
     const double c01 = lerp(V(i0[0], i0[1], i1[2]), V(i1[0], i0[1], i1[2]), t[0]);
     const double c11 = lerp(V(i0[0], i1[1], i1[2]), V(i1[0], i1[1], i1[2]), t[0]);
     return lerp(lerp(c00, c10, t[1]), lerp(c01, c11, t[1]), t[2]);
+}
+
+// hi + lo split of a double with integer operations only (no FP64
+// instruction): hi keeps the top 24 significant bits, lo the next 29 rounded
+// to 24, so hi + lo carries ~48 bits. False for subnormals and magnitudes
+// outside [2^-60, 2^100], which the caller handles in FP64; zero splits exactly.
+__device__ __forceinline__ bool ff_split_bits(double v, ff& out) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int e = (int)((b >> 52) & 0x7ffu);
+    const unsigned long long m = b & 0xfffffffffffffull;
+    if (e == 0) {
+        out = ff{__uint_as_float(sign), 0.f};
+        return m == 0;
+    }
+    const int ue = e - 1023;
+    if (ue < -60 || ue > 100) return false;
+    const float hi = __uint_as_float(sign | ((unsigned)(ue + 127) << 23) | (unsigned)(m >> 29));
+    const float scale = __uint_as_float((unsigned)(ue - 52 + 127) << 23);  // 2^(ue - 52)
+    const float lo = __uint_as_float(
+        __float_as_uint(__fmul_rn(__uint2float_rn((unsigned)(m & 0x1fffffffu)), scale)) | sign);
+    out = ff_fast(hi, lo);
+    return true;
+}
+
+// floor of a normalised double-float value with |hi| < 2^22 (so |lo| < 1/4)
+__device__ __forceinline__ float ff_floor(ff v) {
+    float f = floorf(v.hi);
+    if (v.hi == f && v.lo < 0.f) f -= 1.f;
+    return f;
+}
+
+// The inverse cell (f = c . inv) as double-float.
+struct InvFF {
+    float h[9], l[9];
+};
+
+// FP32-form grids: grid_interp_fast's fractional transform, wrap and
+// trilinear weights in double-float on the FP32 pipe, in two steps so that a
+// kernel can issue the eight corner loads between them. The position and the
+// corners are split by integer operations, so FP64 runs only to form the
+// result; a query whose operands fall outside the split's range (either step
+// returns false) is answered by grid_interp_fast. Agrees with
+// grid_interp_fast to ~48 bits of the position and of the corners.
+//
+// Step 1: the lower corner (i0), the upper one with wrap (i1) and the weights.
+__device__ __forceinline__ bool grid_ff_locate(const InvFF& inv, const int* cnt, double px,
+                                               double py, double pz, int* i0, int* i1, ff* t) {
+    ff p[3];
+    if (!ff_split_bits(px, p[0]) || !ff_split_bits(py, p[1]) || !ff_split_bits(pz, p[2]))
+        return false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        ff f = ff_add(ff_add(ff_mul(p[0], ff{inv.h[a], inv.l[a]}), ff_mul(p[1], ff{inv.h[3 + a], inv.l[3 + a]})),
+                      ff_mul(p[2], ff{inv.h[6 + a], inv.l[6 + a]}));
+        // ff_floor needs |lo| < 1: beyond 2^22 cells the image is answered in FP64
+        if (!(fabsf(f.hi) < 4194304.f)) return false;
+        f = ff_add_f(f, -ff_floor(f));  // [0, 1)
+        const ff g = ff_mul(f, ff{(float)cnt[a], 0.f});
+        const float fb = ff_floor(g);
+        t[a] = ff_add_f(g, -fb);
+        int base = (int)fb;
+        if (base >= cnt[a]) base -= cnt[a];
+        base = min(max(base, 0), cnt[a] - 1);  // in range whatever the rounding
+        i0[a] = base;
+        i1[a] = base + 1 == cnt[a] ? 0 : base + 1;
+    }
+    return true;
+}
+
+// Step 2: the trilinear blend of the corners c[k] (k = x + 2y + 4z, 0 lower,
+// 1 upper), the same lerp order as grid_interp_fast.
+__device__ __forceinline__ bool grid_ff_blend(const double* c, const ff* t, double& out) {
+    ff v[8];
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) ok &= ff_split_bits(c[k], v[k]);
+    if (!ok) return false;
+    auto lerp = [](ff a, ff b, ff w) { return ff_add(a, ff_mul(w, ff_add(b, ff{-a.hi, -a.lo}))); };
+    const ff c00 = lerp(v[0], v[1], t[0]), c10 = lerp(v[2], v[3], t[0]);
+    const ff c01 = lerp(v[4], v[5], t[0]), c11 = lerp(v[6], v[7], t[0]);
+    const ff r = lerp(lerp(c00, c10, t[1]), lerp(c01, c11, t[1]), t[2]);
+    out = (double)r.hi + (double)r.lo;
+    return true;
 }
 
 // One species' table of a grid, for kernels that interpolate it.

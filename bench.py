@@ -693,13 +693,15 @@ def extras(A, torch, peaks):
     out["batched_screening"] = batched_screening(A, torch)
     out["c5_isotherm_sample"] = c5_isotherm_sample(A, torch)
     out["interpolate_roofline"] = {
-        "bound": "fp64", "achieved": gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+        "bound": "hbm", "achieved": gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
         "frac": gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None, "bytes_per_query": 96,
         "note": "96 algorithmic bytes per query (8 corner loads of 8 B + 24 B in + 8 B out), random "
-                "queries over a 0.7 GB table of an FP32-form grid; achieved against the HBM copy "
-                "peak, but the bound is the FP64 pipe: ~40 FP64 operations per query (fractional "
-                "transform, floors, 7 lerps) at 1/64 of the FP32 rate; the FP64-form grids keep the "
-                "reference's ~100-operation arithmetic (3 IEEE divisions) for bit-equal values"}
+                "queries over a 0.7 GB table of an FP32-form grid, against the HBM copy peak. The "
+                "transform and lerps run in double-float on the FP32 pipe (operands split by integer "
+                "operations), so the kernel waits on random 32-byte-sector gathers: each query "
+                "touches ~4 sectors in 4 DRAM rows, ~130 B of DRAM traffic per query at a 41 % L2 "
+                "hit rate on the 2x2x2 grid, more on this one. The FP64-form grids keep the "
+                "reference's FP64 arithmetic (3 IEEE divisions) for bit-equal values"}
     return out
 
 
