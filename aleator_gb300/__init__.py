@@ -40,6 +40,8 @@ from ._lib import (  # noqa: F401
     load_library,
     peng_robinson_fugacity,
     peng_robinson_mixture,
+    read_cif,
+    Structure,
     philox4x32_10,
     philox_u64,
     philox_uniform,

@@ -243,6 +243,15 @@ _SIGNATURES = {
     "alea_swap_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                           ctypes.c_uint64, ctypes.c_double, ctypes.c_double]),
     "alea_peng_robinson_fugacity": (ctypes.c_int32, [ctypes.c_double] * 5 + [_D]),
+    "alea_read_cif": (ctypes.c_int32, [ctypes.c_char_p, ctypes.POINTER(_VP)]),
+    "alea_structure_sizes": (ctypes.c_int32, [_VP, _U64, _U32]),
+    "alea_structure_lattice": (ctypes.c_int32, [_VP, _D]),
+    "alea_structure_atoms": (ctypes.c_int32, [_VP, _D, _D, _D, _D, _D, _U32, _D]),
+    "alea_structure_species_symbol": (ctypes.c_int32, [_VP, ctypes.c_uint32, ctypes.c_char_p,
+                                                       ctypes.c_size_t]),
+    "alea_structure_source_label": (ctypes.c_int32, [_VP, ctypes.c_uint64, ctypes.c_char_p,
+                                                     ctypes.c_size_t]),
+    "alea_structure_destroy": (ctypes.c_int32, [_VP]),
     "alea_peng_robinson_mixture": (ctypes.c_int32, [ctypes.c_uint32, _D, _D, _D, _D,
                                                     ctypes.c_double, ctypes.c_double, _D, _D, _D]),
 }
@@ -1078,6 +1087,50 @@ def peng_robinson_fugacity(tc, pc, omega, t, p):
     v = ctypes.c_double()
     _check(library().alea_peng_robinson_fugacity(tc, pc, omega, t, p, ctypes.byref(v)))
     return v.value
+
+
+class Structure:
+    """readCif's StructureData (io/structure_io.hpp:18-40): `particles` (a
+    ParticleData: x, y, z, charge, species), `lattice` (3x3 rows a_i), `mass`,
+    `species_symbols` (element of each species id), `occupancy` and
+    `source_label` (the atom_site label each atom was expanded from)."""
+
+    def __init__(self, particles, lattice, mass, species_symbols, occupancy, source_label):
+        self.particles = particles
+        self.lattice = lattice
+        self.mass = mass
+        self.species_symbols = species_symbols
+        self.occupancy = occupancy
+        self.source_label = source_label
+
+
+def read_cif(path) -> Structure:
+    """readCif(file) (io/structure_io.hpp:51): a malformed file raises
+    RuntimeError with the reference's CifParseError message."""
+    lib = library()
+    h = _VP()
+    _check(lib.alea_read_cif(os.fsencode(str(path)), ctypes.byref(h)))
+    try:
+        n, ns = ctypes.c_uint64(), ctypes.c_uint32()
+        _check(lib.alea_structure_sizes(h, ctypes.byref(n), ctypes.byref(ns)))
+        m = np.zeros(9)
+        _check(lib.alea_structure_lattice(h, _dp(m)))
+        x, y, z, q, mass, occ = (np.zeros(n.value) for _ in range(6))
+        sp = np.zeros(n.value, np.uint32)
+        _check(lib.alea_structure_atoms(h, _dp(x), _dp(y), _dp(z), _dp(q), _dp(mass), _u32p(sp),
+                                        _dp(occ)))
+        buf = ctypes.create_string_buffer(4096)
+        symbols = []
+        for k in range(ns.value):
+            _check(lib.alea_structure_species_symbol(h, k, buf, 4096))
+            symbols.append(buf.value.decode())
+        labels = []
+        for i in range(n.value):
+            _check(lib.alea_structure_source_label(h, i, buf, 4096))
+            labels.append(buf.value.decode())
+    finally:
+        lib.alea_structure_destroy(h)
+    return Structure(ParticleData(x, y, z, q, sp), m.reshape(3, 3), mass, symbols, occ, labels)
 
 
 def peng_robinson_mixture(substances, t, p, mole_fractions, kij=None):

@@ -19,8 +19,8 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libaleator_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["common.cu", "philox.cu", "grid.cu", "grid_cache.cpp", "lj.cu", "ewald.cu", "widom.cu",
-           "gcmc.cu", "proposal.cu", "capi.cu", "probe.cu", "noalloc.cu"]
+SOURCES = ["common.cu", "philox.cu", "grid.cu", "grid_cache.cpp", "cif.cpp", "lj.cu", "ewald.cu",
+           "widom.cu", "gcmc.cu", "proposal.cu", "capi.cu", "probe.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:
@@ -39,7 +39,7 @@ def _stale(out: Path, deps) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "aleator_gb300.h"]
+    headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [PKG.parent / "include" / "aleator_gb300.h"]
     cc = nvcc()
     common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I", str(PKG.parent / "include")]
@@ -50,8 +50,9 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         if not force and not _stale(o, [s, *headers]):
             return o, ""
         cmd = [cc, *common, "-Xptxas", "-v", "-c", str(s), "-o", str(o)]
-        if src.endswith(".cpp"):
-            cmd = [cc, *common, "-x", "cu", "-c", str(s), "-o", str(o)]
+        if src.endswith(".cpp"):  # host code: the reference's IEEE sequence, no FMA contraction
+            cmd = [cc, *common, "-x", "cu", "-Xcompiler", "-ffp-contract=off", "-c", str(s), "-o",
+                   str(o)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

@@ -10,6 +10,7 @@
 #include "common.cuh"
 #include "gcmc.cuh"
 #include "grid.cuh"
+#include "cif.h"
 
 struct alea_grid {
     alea::GridImpl* impl;
@@ -306,6 +307,88 @@ alea_status alea_grid_cache_file_name(const alea_lennard_jones* lj, const alea_p
             throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, "alea_grid_cache_file_name: buffer too small");
         std::memcpy(out, s.c_str(), s.size() + 1);
     });
+}
+
+struct alea_structure {
+    alea::Structure s;
+};
+
+alea_status alea_read_cif(const char* path, alea_structure** out) {
+    return guarded([&] {
+        need(path, "path");
+        need(out, "out");
+        *out = nullptr;
+        auto* h = new alea_structure{alea::read_cif(path)};
+        *out = h;
+    });
+}
+
+alea_status alea_structure_sizes(const alea_structure* s, uint64_t* n_atoms, uint32_t* n_species) {
+    return guarded([&] {
+        need(s, "structure");
+        if (n_atoms) *n_atoms = s->s.x.size();
+        if (n_species) *n_species = (uint32_t)s->s.symbols.size();
+    });
+}
+
+alea_status alea_structure_lattice(const alea_structure* s, double m[9]) {
+    return guarded([&] {
+        need(s, "structure");
+        need(m, "m");
+        std::memcpy(m, s->s.m, sizeof s->s.m);
+    });
+}
+
+alea_status alea_structure_atoms(const alea_structure* s, double* x, double* y, double* z,
+                                 double* charge, double* mass, uint32_t* species,
+                                 double* occupancy) {
+    return guarded([&] {
+        need(s, "structure");
+        const alea::Structure& t = s->s;
+        const size_t n = t.x.size();
+        auto put = [n](auto* dst, const auto& src) {
+            if (dst && n) std::memcpy(dst, src.data(), n * sizeof(src[0]));
+        };
+        put(x, t.x);
+        put(y, t.y);
+        put(z, t.z);
+        put(charge, t.charge);
+        put(mass, t.mass);
+        put(species, t.species);
+        put(occupancy, t.occupancy);
+    });
+}
+
+static void copy_text(const std::string& v, char* out, size_t cap, const char* who) {
+    if (v.size() + 1 > cap)
+        throw alea::Error(ALEA_ERR_INVALID_ARGUMENT, std::string(who) + ": buffer too small");
+    std::memcpy(out, v.c_str(), v.size() + 1);
+}
+
+alea_status alea_structure_species_symbol(const alea_structure* s, uint32_t species, char* out,
+                                          size_t cap) {
+    return guarded([&] {
+        need(s, "structure");
+        need(out, "out");
+        if (species >= s->s.symbols.size())
+            throw alea::Error(ALEA_ERR_OUT_OF_RANGE, "alea_structure_species_symbol: species out of range");
+        copy_text(s->s.symbols[species], out, cap, "alea_structure_species_symbol");
+    });
+}
+
+alea_status alea_structure_source_label(const alea_structure* s, uint64_t atom, char* out,
+                                        size_t cap) {
+    return guarded([&] {
+        need(s, "structure");
+        need(out, "out");
+        if (atom >= s->s.labels.size())
+            throw alea::Error(ALEA_ERR_OUT_OF_RANGE, "alea_structure_source_label: atom out of range");
+        copy_text(s->s.labels[atom], out, cap, "alea_structure_source_label");
+    });
+}
+
+alea_status alea_structure_destroy(alea_structure* s) {
+    return guarded([&] { delete s; });
 }
 
 alea_status alea_grid_load_cache(const char* cache_dir, const alea_lennard_jones* lj,

@@ -192,6 +192,33 @@ alea_status alea_grid_load_cache(const char* cache_dir, const alea_lennard_jones
                                  alea_grid** out);
 alea_status alea_grid_destroy(alea_grid* g);
 
+/* ------------------------------------------------------------------ CIF structures */
+/* readCif (io/structure_io.hpp:51, io/structure_io.cc:177-245): the cell
+ * (a, b, c, alpha, beta, gamma; a along x, b in the xy plane), the symmetry
+ * operations (_symmetry_equiv_pos_as_xyz or _space_group_symop_operation_xyz,
+ * P1 when neither is present) and the _atom_site loop expanded through every
+ * operation with images within 1e-3 A merged. Particles equal the reference's
+ * bit for bit; a malformed file fails with ALEA_ERR_RUNTIME and the
+ * reference's CifParseError message. Host only (no device needed). */
+typedef struct alea_structure alea_structure;
+alea_status alea_read_cif(const char* path, alea_structure** out);
+/* particles.size(), speciesSymbols.size() */
+alea_status alea_structure_sizes(const alea_structure* s, uint64_t* n_atoms, uint32_t* n_species);
+/* lattice.matrix() rows a_i, row-major */
+alea_status alea_structure_lattice(const alea_structure* s, double m[9]);
+/* particles x, y, z, charge, mass, species and the per-atom occupancy, each
+ * n_atoms long; any pointer may be NULL. x, y, z, charge, species are
+ * alea_particles' arrays. */
+alea_status alea_structure_atoms(const alea_structure* s, double* x, double* y, double* z,
+                                 double* charge, double* mass, uint32_t* species,
+                                 double* occupancy);
+/* speciesSymbols[species], sourceLabel[atom]: NUL-terminated into out */
+alea_status alea_structure_species_symbol(const alea_structure* s, uint32_t species, char* out,
+                                          size_t cap);
+alea_status alea_structure_source_label(const alea_structure* s, uint64_t atom, char* out,
+                                        size_t cap);
+alea_status alea_structure_destroy(alea_structure* s);
+
 /* ------------------------------------------------------------------ batch of energy grids */
 /* No counterpart in the reference (one FrameworkEnergyGrid per framework,
  * framework_energy_grid.cc:193-249). n independent frameworks, each with its

@@ -26,6 +26,8 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 ORACLE_SO = BUILD / "liboracle.so"
 REF_SO = HERE / "_ref" / "libaleator_ref.so"
+# the reference source tree (its sources and test data), present only where it was checked out
+REFERENCE_ROOT = Path(os.environ.get("ALEA_REFERENCE_ROOT", "/root/reference"))
 
 DRAWS_RIGHT_TO_LEFT = 0
 DRAWS_LEFT_TO_RIGHT = 1
@@ -597,6 +599,18 @@ class Reference:
         L.ref_gcmc_destroy.argtypes = [ctypes.c_void_p]
         L.ref_pr_fugacity.restype = ctypes.c_double
         L.ref_pr_fugacity.argtypes = [ctypes.c_double] * 5
+        L.ref_read_cif.restype = ctypes.c_void_p
+        L.ref_read_cif.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
+        L.ref_structure_size.restype = ctypes.c_uint64
+        L.ref_structure_size.argtypes = [ctypes.c_void_p]
+        L.ref_structure_species.restype = ctypes.c_uint32
+        L.ref_structure_species.argtypes = [ctypes.c_void_p]
+        L.ref_structure_atoms.argtypes = [ctypes.c_void_p] + [_D] * 6 + [_U32, _D]
+        L.ref_structure_symbol.restype = ctypes.c_char_p
+        L.ref_structure_symbol.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
+        L.ref_structure_label.restype = ctypes.c_char_p
+        L.ref_structure_label.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.ref_structure_free.argtypes = [ctypes.c_void_p]
         L.ref_pr_mixture.restype = ctypes.c_int
         L.ref_pr_mixture.argtypes = [ctypes.c_uint32, _D, _D, _D, _D, ctypes.c_double,
                                      ctypes.c_double, _D, _D, _D, ctypes.c_char_p, ctypes.c_size_t]
@@ -722,6 +736,30 @@ class Reference:
 
     def pr_fugacity(self, tc, pc, omega, t, p):
         return self.lib.ref_pr_fugacity(tc, pc, omega, t, p)
+
+    def read_cif(self, path):
+        """The reference's readCif: a dict of lattice, x, y, z, charge, mass,
+        species, occupancy, symbols, labels; its exception message raised as
+        RuntimeError."""
+        L = self.lib
+        msg = ctypes.create_string_buffer(1024)
+        h = L.ref_read_cif(os.fsencode(str(path)), msg, 1024)
+        if not h:
+            raise RuntimeError(msg.value.decode())
+        try:
+            n = L.ref_structure_size(h)
+            m = np.zeros(9)
+            x, y, z, q, mass, occ = (np.zeros(n) for _ in range(6))
+            sp = np.zeros(n, np.uint32)
+            L.ref_structure_atoms(h, _dp(m), _dp(x), _dp(y), _dp(z), _dp(q), _dp(mass),
+                                  sp.ctypes.data_as(_U32), _dp(occ))
+            return dict(lattice=m.reshape(3, 3), x=x, y=y, z=z, charge=q, mass=mass, species=sp,
+                        occupancy=occ,
+                        symbols=[L.ref_structure_symbol(h, k).decode()
+                                 for k in range(L.ref_structure_species(h))],
+                        labels=[L.ref_structure_label(h, i).decode() for i in range(n)])
+        finally:
+            L.ref_structure_free(h)
 
     def pr_mixture(self, substances, t, p, x, kij=None):
         """(Z, [f_i]) from the reference's PengRobinsonMixture; its exception

@@ -29,6 +29,10 @@ TUS=(
   engines/monte_carlo/framework_energy_grid.cc
   engines/monte_carlo/monte_carlo_engine.cc
   engines/monte_carlo/peng_robinson.cc
+  io/cif_document.cc
+  io/symmetry_operation.cc
+  io/element_table.cc
+  io/structure_io.cc
 )
 # -ffp-contract=off keeps the reference's IEEE operation sequence on every
 # host (no fused multiply-add contraction), matching the C restatement.

@@ -32,6 +32,7 @@
 #include "forcefield/electrostatics/ewald.hpp"
 #include "forcefield/electrostatics/ewald_incremental_state.hpp"
 #include "forcefield/pairwise/lennard_jones.hpp"
+#include "io/structure_io.hpp"
 
 using namespace aleator;
 
@@ -562,6 +563,42 @@ void ref_gcmc_destroy(void* h) { delete static_cast<RefGcmc*>(h); }
 double ref_pr_fugacity(double tc, double pc, double omega, double t, double p) {
     return engines::PengRobinson({tc, pc, omega}).fugacityPascal(t, p);
 }
+
+// readCif: a handle, or NULL with the exception's message in msg
+void* ref_read_cif(const char* path, char* msg, size_t cap) {
+    try {
+        return new io::StructureData(io::readCif(path));
+    } catch (const std::exception& e) {
+        std::snprintf(msg, cap, "%s", e.what());
+        return nullptr;
+    }
+}
+uint64_t ref_structure_size(void* h) { return static_cast<io::StructureData*>(h)->particles.size(); }
+uint32_t ref_structure_species(void* h) {
+    return (uint32_t) static_cast<io::StructureData*>(h)->speciesSymbols.size();
+}
+void ref_structure_atoms(void* h, double* m9, double* x, double* y, double* z, double* q,
+                         double* mass, uint32_t* sp, double* occ) {
+    const auto& s = *static_cast<io::StructureData*>(h);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) m9[3 * i + j] = s.lattice.matrix()[i][j];
+    for (size_t i = 0; i < s.particles.size(); ++i) {
+        x[i] = s.particles.x[i];
+        y[i] = s.particles.y[i];
+        z[i] = s.particles.z[i];
+        q[i] = s.particles.charge[i];
+        mass[i] = s.particles.mass[i];
+        sp[i] = s.particles.species[i];
+        occ[i] = s.occupancy[i];
+    }
+}
+const char* ref_structure_symbol(void* h, uint32_t k) {
+    return static_cast<io::StructureData*>(h)->speciesSymbols[k].c_str();
+}
+const char* ref_structure_label(void* h, uint64_t i) {
+    return static_cast<io::StructureData*>(h)->sourceLabel[i].c_str();
+}
+void ref_structure_free(void* h) { delete static_cast<io::StructureData*>(h); }
 
 // PengRobinsonMixture: 0, or -1 with the exception's message in msg
 int ref_pr_mixture(uint32_t n, const double* tc, const double* pc, const double* omega,

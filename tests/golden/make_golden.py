@@ -267,6 +267,21 @@ def main():
         rows=np.array(rows),  # case, T, P, x0..x2, Z, f0..f2
         fails=np.array(fails).reshape(-1, 6))  # case, T, P, x0..x2: the solve does not converge
 
+    # ---- readCif on the synthetic CIF files of tests/golden/cif (written for
+    # these tests): the parsed structure, or the reference's error message
+    cif = {}
+    for f in sorted((OUT / "cif").glob("*.cif")):
+        try:
+            r = ref.read_cif(f)
+        except RuntimeError as e:
+            cif[f"{f.stem}__error"] = np.array(str(e))
+            continue
+        for k in ("lattice", "x", "y", "z", "charge", "mass", "species", "occupancy"):
+            cif[f"{f.stem}__{k}"] = r[k]
+        cif[f"{f.stem}__symbols"] = np.array(r["symbols"])
+        cif[f"{f.stem}__labels"] = np.array(r["labels"])
+    fixtures["cif_structures"] = cif
+
     for name, data in fixtures.items():
         np.savez_compressed(OUT / f"{name}.npz", **data)
     (OUT / "MANIFEST.json").write_text(json.dumps(

@@ -297,3 +297,28 @@ def test_edge_cases(lib):
     eps, sig = np.sqrt(fw.eps[4] * fw.eps[0]), 0.5 * (fw.sigma[4] + fw.sigma[0])
     raw = lambda r: 4 * eps * ((sig / r) ** 12 - (sig / r) ** 6)
     assert abs(g1.table(4)[0] - min(raw(d) - raw(12.0), 1e5)) <= 1e-10 * max(1, abs(raw(d)))
+
+
+def test_grid_from_cif_structure(lib, orc):
+    """A framework read from a CIF file (triclinic cell, symmetry-expanded),
+    replicated until the cutoff fits, through the FP64 energy grid: within
+    1e-10 of the oracle's grid on the same particles."""
+    A, _ = lib
+    from pathlib import Path
+    from aleator_gb300 import workloads as W
+    s = A.read_cif(Path(__file__).resolve().parent / "golden" / "cif" / "triclinic_symops.cif")
+    ns = len(s.species_symbols)
+    rng = np.random.default_rng(4)
+    eps = np.concatenate([rng.uniform(20, 100, ns), [148.0]])   # framework types, then the probe
+    sigma = np.concatenate([rng.uniform(2.5, 3.5, ns), [3.73]])
+    # shifted off the nodes: the atoms on special positions (the origin among
+    # them) would otherwise sit exactly on grid nodes, where r = 0
+    fw = W.Framework(lattice=np.asarray(s.lattice), x=s.particles.x + 0.0123,
+                     y=s.particles.y + 0.0456, z=s.particles.z + 0.0789,
+                     species=s.particles.species, charge=s.particles.charge, eps=eps, sigma=sigma)
+    fw = W.replicate(fw, W.minimum_replication(fw.lattice, 9.0))
+    ff = A.LennardJones(fw.eps, fw.sigma, 9.0, A.SHIFTED)
+    grid = A.FrameworkEnergyGrid(ff, A.ParticleData.from_framework(fw), fw.lattice, [ns], 1.0, A.FP64)
+    od = dict(eps=fw.eps, sigma=fw.sigma, cutoff=9.0, truncation=O.SHIFTED)
+    want = orc.grid_build(od, fw.lattice, fw.x, fw.y, fw.z, fw.species, ns, 1.0, threads=8)
+    assert rel_err(grid.table(ns), want).max() <= 1e-10
