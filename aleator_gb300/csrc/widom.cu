@@ -34,6 +34,15 @@ constexpr int WT = 128;        // trials per block
 constexpr int ATILE = 512;     // framework atoms per shared-memory tile
 constexpr int MAXS = 8;        // sites per guest molecule
 constexpr int MAXT = 64;       // LJ species
+// FP32 form, uncharged trials: pairs closer than CLOSE_SIGMA x sigma (and,
+// for plain truncation, pairs whose cutoff decision FP32 cannot make) are
+// listed per thread, up to CLOSE_MAX per tile and site, and redone in
+// double-float after the tile; the rest run on FP32 displacements from the
+// atoms' FP32 positions (the image then carries up to ~ulp(L) ~ 4e-6 A, which
+// beyond 1.25 sigma moves a pair energy by < 3e-4 K).
+constexpr int CLOSE_MAX = 16;
+constexpr float CLOSE_SIGMA2 = 1.25f * 1.25f;
+constexpr float CUT_BAND = 1e-5f;  // relative band of r^2 around rc^2 redone in double-float
 
 struct GuestSite {
     double x, y, z, q;
@@ -89,7 +98,9 @@ struct WidomPtrs {
 
 // One block of WT trials: trials first + block WT + threadIdx.x; writes the
 // block's (max, s1, s2) to partial[3 block ..].
-template <typename Real>
+// Q: the context may be charged (false: an LJ-only instantiation, compiled
+// without the electrostatic sums and with fewer registers).
+template <typename Real, bool Q>
 __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtrs& D, uint64_t block,
                                             uint64_t seed, uint64_t stream, uint64_t first,
                                             uint64_t n, int draw_order, double* __restrict__ per_trial,
@@ -109,6 +120,7 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
     __shared__ PairF32W ppf[sizeof(Real) == 4 ? MAXS * MAXT : 1];
     __shared__ PairCloseFF ppc[sizeof(Real) == 4 ? MAXS * MAXT : 1];
     __shared__ double red[WT];
+    __shared__ uint16_t closej[sizeof(Real) == 4 ? CLOSE_MAX * WT : 1];
 
     const int ns = P.n_sites;
     for (int i = threadIdx.x; i < ns * (int)P.n_species; i += WT) {
@@ -240,8 +252,70 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                     const double r2 = dx * dx + dy * dy + dz * dz;
                     const double r = sqrt(r2);
                     lj_acc += lj_pair_rt(P.trunc, r, P.rc, pp[s * MAXT + ttype[j]]);
-                    if (P.charged && r <= P.rc_ewald) es_acc += a.w * (erfc(P.alpha * r) / r);
+                    if ((Q && P.charged) && r <= P.rc_ewald) es_acc += a.w * (erfc(P.alpha * r) / r);
                 }
+            } else if (!(Q && P.charged)) {
+                // FP32 displacement (hi and lo parts subtracted apart: exact
+                // for nearby atoms) and image on the FP32 pipe; close pairs and
+                // cutoff-ambiguous ones listed and redone in double-float
+                const ff px = ff_from(sx[s]), py = ff_from(sy[s]), pz = ff_from(sz[s]);
+                const float rc2f = (float)P.rc2, rcf = (float)P.rc;
+                const float band = P.trunc == ALEA_TRUNCATED ? CUT_BAND * rc2f : 0.f;
+                const PairF32W* rowf = ppf + s * MAXT;
+                ff close_acc{0.f, 0.f};
+                uint16_t* mine = closej + threadIdx.x;  // stride WT: bank-conflict free
+                int nclose = 0;
+                // double-float energy of pair j (its cutoff decided in double-float)
+                auto redo = [&](int j) {
+                    const float4* t4 = reinterpret_cast<const float4*>(&tile[j]);
+                    const float4 ah = t4[0], al = t4[1];
+                    ff dx = ff_add(ff{ah.x, al.x}, ff{-px.hi, -px.lo});
+                    ff dy = ff_add(ff{ah.y, al.y}, ff{-py.hi, -py.lo});
+                    ff dz = ff_add(ff{ah.z, al.z}, ff{-pz.hi, -pz.lo});
+                    ff_min_image(P.lh, P.ll, P.linv, P.L.ortho, dx, dy, dz);
+                    const ff rr = ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
+                    const ff over = ff_add(rr, ff_from(-P.rc2));
+                    if (over.hi > 0.f || (over.hi == 0.f && over.lo > 0.f)) return;
+                    close_acc = ff_add(close_acc, lj_close_ff(ppc[s * MAXT + ttype[j]], rr, rcf, P.trunc));
+                };
+                for (int j = 0; j < cnt; ++j) {
+                    // hi parts only: a far pair tolerates the ~ulp(L) this leaves
+                    const float4 ah = reinterpret_cast<const float4*>(&tile[j])[0];
+                    float dx = __fsub_rn(__fsub_rn(ah.x, px.hi), px.lo);
+                    float dy = __fsub_rn(__fsub_rn(ah.y, py.hi), py.lo);
+                    float dz = __fsub_rn(__fsub_rn(ah.z, pz.hi), pz.lo);
+                    if (P.L.ortho) {
+                        dx = fmaf(-rintf(dx * P.linv[0]), P.lh[0], dx);
+                        dy = fmaf(-rintf(dy * P.linv[4]), P.lh[4], dy);
+                        dz = fmaf(-rintf(dz * P.linv[8]), P.lh[8], dz);
+                    } else {
+                        float n[3];
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+                            n[a] = rintf(fmaf(dx, P.linv[a], fmaf(dy, P.linv[3 + a], dz * P.linv[6 + a])));
+                        const float ex = fmaf(-n[0], P.lh[0], fmaf(-n[1], P.lh[3], -n[2] * P.lh[6]));
+                        const float ey = fmaf(-n[0], P.lh[1], fmaf(-n[1], P.lh[4], -n[2] * P.lh[7]));
+                        const float ez = fmaf(-n[0], P.lh[2], fmaf(-n[1], P.lh[5], -n[2] * P.lh[8]));
+                        dx += ex;
+                        dy += ey;
+                        dz += ez;
+                    }
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const PairF32W q = rowf[ttype[j]];
+                    const bool close = r2 < CLOSE_SIGMA2 * q.sig2 || fabsf(r2 - rc2f) <= band;
+                    if (close) {  // rare: listed
+                        if (nclose < CLOSE_MAX) mine[WT * nclose++] = (uint16_t)j;
+                        else redo(j);  // a crowded trial: at once
+                    }
+                    // every lane evaluates the term (no divergence); kept inside rc
+                    const float ir2 = __frcp_rn(r2);
+                    const float ir6 = ir2 * ir2 * ir2;
+                    float e = ir6 * fmaf(q.a, ir6, -q.b) - q.shift;
+                    if (P.trunc == ALEA_LINEAR_FORCE_SHIFTED) e -= (sqrtf(r2) - rcf) * q.dvdrc;
+                    lj_acc += (!close && r2 <= rc2f) ? e : 0.f;
+                }
+                for (int k = 0; k < nclose; ++k) redo(mine[WT * k]);
+                lj_close = (double)close_acc.hi + (double)close_acc.lo;
             } else {
                 // the displacement formed and brought to its image in
                 // double-float, rounded to FP32 once; FP32 pair terms
@@ -272,7 +346,7 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                         if (P.trunc == ALEA_LINEAR_FORCE_SHIFTED) e -= (sqrtf(r2) - rcf) * q.dvdrc;
                         lj_acc += e;
                     }
-                    if (P.charged && r2 <= rce2f) {
+                    if ((Q && P.charged) && r2 <= rce2f) {
                         const float rf = sqrtf(r2);
                         es_acc += ah.w * (erfcf(alphaf * rf) / rf);
                     }
@@ -288,7 +362,7 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
     for (int s = 0; s < MAXS; ++s)
         if (s < ns) du += lj_site[s];
 
-    if (P.charged) {
+    if ((Q && P.charged)) {
         double e = 0.0;
 #pragma unroll
         for (int s = 0; s < MAXS; ++s)
@@ -440,9 +514,9 @@ struct WidomItem {
     ProposalTable tab;
 };
 
-// FP32: 3 CTAs per SM (at most 170 registers a thread)
-template <typename Real>
-__global__ void __launch_bounds__(WT, sizeof(Real) == 4 ? 3 : 1)
+// FP32: 3 CTAs per SM when charged (at most 170 registers a thread), 4 for LJ only
+template <typename Real, bool Q>
+__global__ void __launch_bounds__(WT, sizeof(Real) == 4 ? (Q ? 3 : 4) : 1)
 widom_batch_kernel(const WidomItem* __restrict__ items, int n_items, int draw_order) {
     __shared__ WidomParams Ps;
     __shared__ int item;
@@ -462,7 +536,7 @@ widom_batch_kernel(const WidomItem* __restrict__ items, int n_items, int draw_or
     for (int i = threadIdx.x; i < (int)(sizeof(WidomParams) / 4); i += WT) dst[i] = src[i];
     __syncthreads();
     const WidomItem& it = items[item];
-    widom_block<Real>(Ps, it.D, work - it.block0, it.seed, it.stream, it.first, it.n, draw_order,
+    widom_block<Real, Q>(Ps, it.D, work - it.block0, it.seed, it.stream, it.first, it.n, draw_order,
                       it.per_trial, it.partial, it.tab, it.frac_out, it.samples_out);
 }
 
@@ -471,6 +545,14 @@ __global__ void widom_batch_combine_kernel(const WidomItem* __restrict__ items, 
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_items) return;
     combine_partials(items[i].partial, items[i].nblocks, items[i].result);
+}
+
+// The instantiation for a launch: FP32 or FP64, charged or LJ-only contexts.
+using WidomKernel = void (*)(const WidomItem*, int, int);
+WidomKernel widom_kernel_for(int precision, bool charged) {
+    if (precision == ALEA_FP32)
+        return charged ? widom_batch_kernel<float, true> : widom_batch_kernel<float, false>;
+    return charged ? widom_batch_kernel<double, true> : widom_batch_kernel<double, false>;
 }
 
 }  // namespace
@@ -644,7 +726,7 @@ static void widom_launch(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t 
     it.samples_out = samples_dev;
     it.tab = tab;
     ALEA_CUDA(cudaMemcpy(w->item.p, &it, sizeof(WidomItem), cudaMemcpyHostToDevice));
-    auto kern = w->precision == ALEA_FP32 ? widom_batch_kernel<float> : widom_batch_kernel<double>;
+    const WidomKernel kern = widom_kernel_for(w->precision, it.P.charged != 0);
     kern<<<(unsigned)nblocks, WT>>>(w->item.p, 1, draw_order);
     ALEA_CUDA(cudaGetLastError());
     widom_batch_combine_kernel<<<1, 32>>>(w->item.p, 1);
@@ -800,7 +882,9 @@ void widom_batch_run(WidomBatchImpl* b, const uint64_t* seeds, const uint64_t* s
         if (b->graph) cudaGraphDestroy(b->graph);
         b->exec = nullptr;
         b->graph = nullptr;
-        auto kern = b->precision == ALEA_FP32 ? widom_batch_kernel<float> : widom_batch_kernel<double>;
+        bool charged = false;
+        for (size_t i = 0; i < m; ++i) charged |= b->items_h[i].P.charged != 0;
+        const WidomKernel kern = widom_kernel_for(b->precision, charged);
         require(total < (1ull << 31), ALEA_ERR_INVALID_ARGUMENT, "Widom batch: too many trials");
         ALEA_CUDA(cudaStreamSynchronize(run));
         ALEA_CUDA(cudaStreamBeginCapture(b->own, cudaStreamCaptureModeThreadLocal));

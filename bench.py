@@ -592,14 +592,14 @@ def c5_isotherm_sample(A, torch, moves=1000, n=64):
             "molecules_after": {f"{P:.3g} bar": m for P, m in list(zip(pressures, mol))[::9]}}
 
 
-def batched_screening(A, torch, n_frameworks=256, trials=100_000):
+def batched_screening(A, torch, n_frameworks=256, trials=1_000_000):
     """Batched screening: 256 uneven synthetic triclinic frameworks (a, b, c
     uniform in 10-40 A, angles in 60-120 deg, 50-2000 atoms, each replicated so
     the cutoff fits; 978k atoms in all), CH4 probe. Their 0.3 A FP32 grids are
     built in one persistent launch replayed from a CUDA graph (the
     first build autotunes the launch shape and captures), then Widom insertions
     for every framework in one persistent launch (FP32 pair terms, FP64
-    accumulation), `trials` per framework: a bounded sample of 1e6."""
+    accumulation), `trials` (1e6) per framework."""
     from aleator_gb300 import workloads as W
     t0 = time.perf_counter()
     fws = W.random_triclinic_frameworks(n_frameworks)

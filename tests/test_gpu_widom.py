@@ -100,3 +100,31 @@ def test_large_run_statistics(lib, orc):
                    298.0, 42, 0, n, threads=16)
     assert abs(r["henry"] / kh - 1) <= 1e-9
     assert 0 < r["rel_std_error"] < 0.1
+
+
+@pytest.mark.parametrize("trunc", ["TRUNCATED", "SHIFTED", "LINEAR_FORCE_SHIFTED"])
+def test_fp32_uncharged_triclinic_vs_fp64(lib, trunc):
+    """FP32 form, uncharged probe (FP32 displacements and images, pairs within
+    1.25 sigma and, for plain truncation, pairs at the cutoff redone in
+    double-float) on triclinic cells of the batched-screening kind, every
+    truncation: per trial within 1e-5 x max(kT, |dU|) of the FP64 form (itself
+    pinned to the oracle) on trials with dU <= 1e4 K, and K_H within 1e-5."""
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    fws = W.random_triclinic_frameworks(8, seed=31)
+    checked = 0
+    for i, fw in enumerate(fws):
+        ff = A.LennardJones(fw.eps, fw.sigma, 12.8, getattr(A, trunc))
+        p = A.ParticleData.from_framework(fw)
+        guest = W.ch4_guest(fw)
+        r64, per64 = A.Widom(ff, p, fw.lattice, guest, 298.0).run(5, i, 20000, per_trial=True)
+        r32, per32 = A.Widom(ff, p, fw.lattice, guest, 298.0, precision=A.FP32).run(
+            5, i, 20000, per_trial=True)
+        keep = per64 <= 1e4
+        assert (per32[~keep] > 1e4 * (1 - 1e-5)).all()
+        if keep.sum() < 50:  # a dense cell: no trial carries Boltzmann weight
+            continue
+        checked += 1
+        assert rel_err(per32[keep], per64[keep], floor=KT).max() <= 1e-5, (i, trunc)
+        assert abs(r32["henry"] / r64["henry"] - 1) <= 1e-5
+    assert checked >= 2
