@@ -88,6 +88,7 @@ __device__ __forceinline__ void cross_rn(const double* a, const double* b, doubl
 // Device data of one Widom context.
 struct WidomPtrs {
     const double4* atoms;
+    const float4* atoms32;  // FP32 form: per atom {x, y, z hi, charge}, {x, y, z lo, 0}
     const uint32_t* types;
     const PairParams* table;
     const KRow* rows;
@@ -227,14 +228,12 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
         __syncthreads();
         const int cnt = (int)min((uint64_t)ATILE, P.n_atoms - base);
         for (int i = threadIdx.x; i < cnt; i += WT) {
-            const double4 a = atoms[base + i];
-            if (sizeof(Real) == 8) {
-                tile[i] = a;
-            } else {  // {x, y, z hi, charge}, {x, y, z lo, 0} as double-float
-                const ff x = ff_from(a.x), y = ff_from(a.y), z = ff_from(a.z);
+            if constexpr (sizeof(Real) == 8) {
+                tile[i] = atoms[base + i];
+            } else {  // {x, y, z hi, charge}, {x, y, z lo, 0}: split once at creation
                 float4* t4 = reinterpret_cast<float4*>(&tile[i]);
-                t4[0] = make_float4(x.hi, y.hi, z.hi, (float)a.w);
-                t4[1] = make_float4(x.lo, y.lo, z.lo, 0.f);
+                t4[0] = D.atoms32[2 * (base + i)];
+                t4[1] = D.atoms32[2 * (base + i) + 1];
             }
             ttype[i] = types[base + i];
         }
@@ -561,6 +560,7 @@ struct WidomImpl {
     WidomParams P{};
     int precision = ALEA_FP64;
     DevBuf<double4> atoms;
+    DevBuf<float4> atoms32;
     DevBuf<uint32_t> types;
     DevBuf<PairParams> table;
     DevBuf<KRow> rows;
@@ -626,6 +626,16 @@ WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
         w->atoms.alloc(std::max<size_t>(fw.n, 1));
         w->types.alloc(std::max<size_t>(fw.n, 1));
         w->atoms.upload(packed.data(), fw.n);
+        if (precision == ALEA_FP32) {  // the atoms as double-float, split here once
+            std::vector<float4> split(2 * fw.n);
+            for (uint64_t i = 0; i < fw.n; ++i) {
+                const ff x = ff_from(packed[i].x), y = ff_from(packed[i].y), z = ff_from(packed[i].z);
+                split[2 * i] = make_float4(x.hi, y.hi, z.hi, (float)packed[i].w);
+                split[2 * i + 1] = make_float4(x.lo, y.lo, z.lo, 0.f);
+            }
+            w->atoms32.alloc(std::max<size_t>(2 * fw.n, 2));
+            w->atoms32.upload(split.data(), 2 * fw.n);
+        }
         w->types.upload(types.data(), fw.n);
         std::vector<PairParams> table((size_t)lj.n_species * lj.n_species);
         mixed_table(lj, table.data());
@@ -712,7 +722,7 @@ static void widom_launch(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t 
         sre = v.sre;
         sim = v.sim;
     }
-    it.D = WidomPtrs{w->atoms.p, w->types.p, w->table.p, w->rows.p, wk, sre, sim};
+    it.D = WidomPtrs{w->atoms.p, w->atoms32.p, w->types.p, w->table.p, w->rows.p, wk, sre, sim};
     it.seed = seed;
     it.stream = stream;
     it.first = first;
@@ -860,7 +870,7 @@ void widom_batch_run(WidomBatchImpl* b, const uint64_t* seeds, const uint64_t* s
         }
         WidomItem& it = b->items_h[i];
         it.P = w->P;
-        it.D = WidomPtrs{w->atoms.p, w->types.p, w->table.p, w->rows.p, wk, sre, sim};
+        it.D = WidomPtrs{w->atoms.p, w->atoms32.p, w->types.p, w->table.p, w->rows.p, wk, sre, sim};
         it.seed = seeds[i];
         it.stream = streams[i];
         it.first = first;
