@@ -49,6 +49,7 @@ constexpr int KMAXC = 64;   // largest kMax the per-site phase tables hold
 // of dynamic shared memory; beyond, the products are formed per term
 constexpr size_t AB_TABLE_BUDGET = 160 * 1024;
 constexpr int RSTRIDE = 4 * MAXS + 1;
+constexpr int TU = 4;  // FP32 form: reciprocal terms per turn of a thread's loop
 
 constexpr int MAXGS = GCMC_MAX_SPECIES;
 constexpr int MAXROWS = 8;  // distinct LJ species among the guest sites
@@ -116,7 +117,11 @@ struct GcmcPtrs {
     // FP32 form: FP32 copies of the weights and of each chain's committed
     // S(k) (refreshed on every commit and resync), FP32 per-term deltas
     const float* w32;
-    float *sre32, *sim32, *dre32, *dim32;
+    // FP32 form: each chain's committed S(k) as double-float, {re, im} hi and
+    // lo per term (the term loop reads the hi pair), and the terms' (n0, n1, n2)
+    // packed as (n0+K) | (n1+K) << 8 | (n2+K) << 16
+    float2 *sk_hi, *sk_lo;
+    const uint32_t* npack;
     const double* gtab[MAXROWS];  // per pair-table row: its LJ species' grid table
     uint32_t* msp;                // per chain, per molecule: its species
 };
@@ -560,10 +565,8 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     double* sim = P.sim + (size_t)chain * C.nk;
     double* dre = P.dre + (size_t)chain * C.nk;
     double* dim = P.dim + (size_t)chain * C.nk;
-    float* sre32 = F32 ? P.sre32 + (size_t)chain * C.nk : nullptr;
-    float* sim32 = F32 ? P.sim32 + (size_t)chain * C.nk : nullptr;
-    float* dre32 = F32 ? P.dre32 + (size_t)chain * C.nk : nullptr;
-    float* dim32 = F32 ? P.dim32 + (size_t)chain * C.nk : nullptr;
+    float2* sk_hi = F32 ? P.sk_hi + (size_t)chain * C.nk : nullptr;
+    float2* sk_lo = F32 ? P.sk_lo + (size_t)chain * C.nk : nullptr;
     const int K = C.kmax;
     for (int i = threadIdx.x; i < C.n_rows * (int)C.n_species; i += GT) {
         const int r = i / C.n_species, t = i % C.n_species;
@@ -607,6 +610,38 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
         if (S.valid) {
             const int n_old = S.n_old, n_new = S.n_new;
             const uint64_t n_all = C.n_fw + S.ng;
+            // FP32 form: term t's S(k) delta, added sites first then removed
+            // (ewald_incremental_state.cc:107-116), from this move's phase tables
+            auto f32_delta = [&](uint32_t pk) -> float2 {
+                const int n0 = pk & 0xff, n1 = (pk >> 8) & 0xff, n2 = (pk >> 16) & 0xff;
+                float re = 0.f, im = 0.f;
+                // q e^{i(n0 th0 + n1 th1)} of slot e: from the table, or formed here
+                auto zq = [&](int e) -> float2 {
+                    if (ab_table) return ab32[(e * tw + n0) * tw + n1];
+                    const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1];
+                    const float q = (float)S.sq_slot[e];
+                    return make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
+                };
+                if (n_new)
+#pragma unroll
+                    for (int s = 0; s < NS; ++s) {
+                        if (s >= n_new) break;  // a smaller species' unused slots hold stale phases
+                        const float2 Z = zq(NS + s);
+                        const float2 Cc = etab32[((NS + s) * 3 + 2) * tw + n2];
+                        re = fmaf(Z.x, Cc.x, fmaf(-Z.y, Cc.y, re));
+                        im = fmaf(Z.x, Cc.y, fmaf(Z.y, Cc.x, im));
+                    }
+                if (n_old)
+#pragma unroll
+                    for (int s = 0; s < NS; ++s) {
+                        if (s >= n_old) break;
+                        const float2 Z = zq(s);
+                        const float2 Cc = etab32[(s * 3 + 2) * tw + n2];
+                        re = fmaf(-Z.x, Cc.x, fmaf(Z.y, Cc.y, re));
+                        im = fmaf(-Z.x, Cc.y, fmaf(-Z.y, Cc.x, im));
+                    }
+                return make_float2(re, im);
+            };
             // with a grid the framework's LJ comes from the tables: its atoms
             // are visited only for the real-space Ewald terms
             const uint64_t j0 = (C.grid && !C.charged) ? C.n_fw : 0;
@@ -772,43 +807,30 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     ab32[i] = make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
                 }
                 __syncthreads();
-                // per term w (2 S.delta + |delta|^2) in FP32 from the FP32
-                // copy of S; this thread's ~nk/256 terms summed in FP32, the
-                // block's partials in FP64
+                // per term w (2 S.delta + |delta|^2) in FP32 from the hi part of
+                // S; this thread's ~nk/256 terms summed in FP32, the block's
+                // partials in FP64. The delta is not stored: a commit forms it again.
+                // (four terms a turn: their global loads issued together; the
+                // terms are still added in the order t, t + GT, t + 2 GT, ...)
                 float racc = 0.f;
-                for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
-                    const int n0 = P.nidx[3 * t] + K, n1 = P.nidx[3 * t + 1] + K, n2 = P.nidx[3 * t + 2] + K;
-                    float re = 0.f, im = 0.f;
-                    // q e^{i(n0 th0 + n1 th1)} of slot e: from the table, or formed here
-                    auto zq = [&](int e) -> float2 {
-                        if (ab_table) return ab32[(e * tw + n0) * tw + n1];
-                        const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1];
-                        const float q = (float)S.sq_slot[e];
-                        return make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
-                    };
-                    if (n_new)  // added first (ewald_incremental_state.cc:107-111)
+                for (uint64_t t0 = threadIdx.x; t0 < C.nk; t0 += TU * GT) {
+                    uint32_t pk[TU];
+                    float2 o[TU];
+                    float wv[TU];
 #pragma unroll
-                        for (int s = 0; s < NS; ++s) {
-                            if (s >= n_new) break;  // a smaller species' unused slots hold stale phases
-                            const float2 Z = zq(NS + s);
-                            const float2 Cc = etab32[((NS + s) * 3 + 2) * tw + n2];
-                            re = fmaf(Z.x, Cc.x, fmaf(-Z.y, Cc.y, re));
-                            im = fmaf(Z.x, Cc.y, fmaf(Z.y, Cc.x, im));
-                        }
-                    if (n_old)  // then removed (:112-116)
+                    for (int u = 0; u < TU; ++u) {
+                        const uint64_t t = t0 + (uint64_t)u * GT;
+                        const bool in = t < C.nk;
+                        pk[u] = in ? P.npack[t] : 0u;  // 0: a valid table entry, weight 0
+                        o[u] = in ? sk_hi[t] : make_float2(0.f, 0.f);
+                        wv[u] = in ? P.w32[t] : 0.f;
+                    }
 #pragma unroll
-                        for (int s = 0; s < NS; ++s) {
-                            if (s >= n_old) break;
-                            const float2 Z = zq(s);
-                            const float2 Cc = etab32[(s * 3 + 2) * tw + n2];
-                            re = fmaf(-Z.x, Cc.x, fmaf(Z.y, Cc.y, re));
-                            im = fmaf(-Z.x, Cc.y, fmaf(-Z.y, Cc.x, im));
-                        }
-                    const float o_re = sre32[t], o_im = sim32[t];
-                    const float dot = fmaf(o_re, re, o_im * im);
-                    racc = fmaf(P.w32[t], fmaf(2.f, dot, fmaf(re, re, im * im)), racc);
-                    dre32[t] = re;
-                    dim32[t] = im;
+                    for (int u = 0; u < TU; ++u) {
+                        const float2 d = f32_delta(pk[u]);
+                        const float dot = fmaf(o[u].x, d.x, o[u].y * d.y);
+                        racc = fmaf(wv[u], fmaf(2.f, dot, fmaf(d.x, d.x, d.y * d.y)), racc);
+                    }
                 }
                 ff v[1] = {ff{racc, 0.f}};
                 block_sum_ff(v, 1, red);
@@ -928,12 +950,13 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
 
             if (S.accept) {
                 if (C.charged) {
-                    if constexpr (F32) {
+                    if constexpr (F32) {  // S += delta in double-float on the FP32 pipe
                         for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
-                            sre[t] += (double)dre32[t];
-                            sim[t] += (double)dim32[t];
-                            sre32[t] = (float)sre[t];
-                            sim32[t] = (float)sim[t];
+                            const float2 d = f32_delta(P.npack[t]);
+                            const float2 h = sk_hi[t], l = sk_lo[t];
+                            const ff re = ff_add_f(ff{h.x, l.x}, d.x), im = ff_add_f(ff{h.y, l.y}, d.y);
+                            sk_hi[t] = make_float2(re.hi, im.hi);
+                            sk_lo[t] = make_float2(re.lo, im.lo);
                         }
                     } else {
                         for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
@@ -1057,11 +1080,13 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                                 im += gq[g] * sn;
                             }
                         }
-                        sre[t] = re;
-                        sim[t] = im;
                         if constexpr (F32) {
-                            sre32[t] = (float)re;
-                            sim32[t] = (float)im;
+                            const ff fr = ff_from(re), fi = ff_from(im);
+                            sk_hi[t] = make_float2(fr.hi, fi.hi);
+                            sk_lo[t] = make_float2(fr.lo, fi.lo);
+                        } else {
+                            sre[t] = re;
+                            sim[t] = im;
                         }
                     }
                     if (threadIdx.x == 0) {
@@ -1117,19 +1142,38 @@ void launch_chains(unsigned n_chains, const GcmcConst& C, const GcmcPtrs& P, uin
     }
 }
 
-// Every chain's committed S(k) starts as the framework's (and its FP32 copy;
-// the weights' FP32 copy too).
+// The committed S(k) between the forms: FP64 to double-float (to_f32) or back.
+__global__ void convert_sk_kernel(uint64_t n, int to_f32, double* re, double* im, float2* hi,
+                                  float2* lo) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    if (to_f32) {
+        const ff fr = ff_from(re[t]), fi = ff_from(im[t]);
+        hi[t] = make_float2(fr.hi, fi.hi);
+        lo[t] = make_float2(fr.lo, fi.lo);
+    } else {
+        re[t] = (double)hi[t].x + (double)lo[t].x;
+        im[t] = (double)hi[t].y + (double)lo[t].y;
+    }
+}
+
+// Every chain's committed S(k) starts as the framework's, in FP64 and as
+// double-float; the weights' FP32 copy and the packed term indices too.
 __global__ void gather_sfw_kernel(uint64_t nk, const double* re, const double* im, const double* w,
-                                  double* out_re, double* out_im, float* out_re32, float* out_im32,
-                                  float* w32, unsigned n_chains) {
+                                  const int* nidx, int kmax, double* out_re, double* out_im,
+                                  float2* out_hi, float2* out_lo, float* w32, uint32_t* npack,
+                                  unsigned n_chains) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nk) return;
     w32[t] = (float)w[t];
+    npack[t] = (uint32_t)(nidx[3 * t] + kmax) | (uint32_t)(nidx[3 * t + 1] + kmax) << 8 |
+               (uint32_t)(nidx[3 * t + 2] + kmax) << 16;
+    const ff fr = ff_from(re[t]), fi = ff_from(im[t]);
     for (unsigned c = 0; c < n_chains; ++c) {
         out_re[(size_t)c * nk + t] = re[t];
         out_im[(size_t)c * nk + t] = im[t];
-        out_re32[(size_t)c * nk + t] = (float)re[t];
-        out_im32[(size_t)c * nk + t] = (float)im[t];
+        out_hi[(size_t)c * nk + t] = make_float2(fr.hi, fi.hi);
+        out_lo[(size_t)c * nk + t] = make_float2(fr.lo, fi.lo);
     }
 }
 
@@ -1150,7 +1194,9 @@ struct GcmcImpl {
     DevBuf<double> pcdf, plogp;  // the chains' copy of a tabulated proposal
     DevBuf<float4> fwh, fwl, ghi, glo;  // FP32 form: double-float positions
     DevBuf<uint32_t> msp;               // species of each molecule, per chain
-    DevBuf<float> w32, sre32, sim32, dre32, dim32;  // FP32 form: S(k) copies and deltas
+    DevBuf<float> w32;                  // FP32 form: the weights
+    DevBuf<float2> sk_hi, sk_lo;        // FP32 form: each chain's S(k) as double-float
+    DevBuf<uint32_t> npack;             // FP32 form: packed (n0, n1, n2) per term
     const double* gtab[MAXROWS] = {};  // the borrowed grid's tables, per pair-table row
     float last_ms = 0.f;
 };
@@ -1333,14 +1379,13 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         g->dre.alloc(nkc * n_chains);
         g->dim.alloc(nkc * n_chains);
         g->w32.alloc(nkc);
-        g->sre32.alloc(nkc * n_chains);
-        g->sim32.alloc(nkc * n_chains);
-        g->dre32.alloc(nkc * n_chains);
-        g->dim32.alloc(nkc * n_chains);
+        g->npack.alloc(nkc);
+        g->sk_hi.alloc(nkc * n_chains);
+        g->sk_lo.alloc(nkc * n_chains);
         if (ews) {
             gather_sfw_kernel<<<(unsigned)((nk + 255) / 256), 256>>>(
-                nk, g->sfw_re.p, g->sfw_im.p, g->w.p, g->sre.p, g->sim.p, g->sre32.p, g->sim32.p,
-                g->w32.p, n_chains);
+                nk, g->sfw_re.p, g->sfw_im.p, g->w.p, g->nidx.p, C.kmax, g->sre.p, g->sim.p,
+                g->sk_hi.p, g->sk_lo.p, g->w32.p, g->npack.p, n_chains);
             ALEA_CUDA(cudaGetLastError());
         }
         const size_t sites = (size_t)C.max_sites * n_chains;
@@ -1413,10 +1458,9 @@ void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s) {
     P.w32 = g->w32.p;
     for (int r = 0; r < MAXROWS; ++r) P.gtab[r] = g->gtab[r];
     P.msp = g->msp.p;
-    P.sre32 = g->sre32.p;
-    P.sim32 = g->sim32.p;
-    P.dre32 = g->dre32.p;
-    P.dim32 = g->dim32.p;
+    P.sk_hi = g->sk_hi.p;
+    P.sk_lo = g->sk_lo.p;
+    P.npack = g->npack.p;
     cudaEvent_t e0, e1;
     ALEA_CUDA(cudaEventCreate(&e0));
     ALEA_CUDA(cudaEventCreate(&e1));
@@ -1501,8 +1545,20 @@ double gcmc_ewald_energy(const GcmcImpl* g, uint32_t chain) {
     if (!g->C.charged) return 0.0;
     const uint64_t nk = g->C.nk;
     std::vector<double> re(nk), im(nk), w(nk);
-    ALEA_CUDA(cudaMemcpy(re.data(), g->sre.p + (size_t)chain * nk, nk * 8, cudaMemcpyDeviceToHost));
-    ALEA_CUDA(cudaMemcpy(im.data(), g->sim.p + (size_t)chain * nk, nk * 8, cudaMemcpyDeviceToHost));
+    if (g->C.f32) {  // the FP32 form keeps S(k) as double-float
+        std::vector<float2> hi(nk), lo(nk);
+        ALEA_CUDA(cudaMemcpy(hi.data(), g->sk_hi.p + (size_t)chain * nk, nk * sizeof(float2),
+                             cudaMemcpyDeviceToHost));
+        ALEA_CUDA(cudaMemcpy(lo.data(), g->sk_lo.p + (size_t)chain * nk, nk * sizeof(float2),
+                             cudaMemcpyDeviceToHost));
+        for (uint64_t t = 0; t < nk; ++t) {
+            re[t] = (double)hi[t].x + (double)lo[t].x;
+            im[t] = (double)hi[t].y + (double)lo[t].y;
+        }
+    } else {
+        ALEA_CUDA(cudaMemcpy(re.data(), g->sre.p + (size_t)chain * nk, nk * 8, cudaMemcpyDeviceToHost));
+        ALEA_CUDA(cudaMemcpy(im.data(), g->sim.p + (size_t)chain * nk, nk * 8, cudaMemcpyDeviceToHost));
+    }
     ALEA_CUDA(cudaMemcpy(w.data(), g->w.p, nk * 8, cudaMemcpyDeviceToHost));
     ChainState s;
     ALEA_CUDA(cudaMemcpy(&s, g->st.p + chain, sizeof s, cudaMemcpyDeviceToHost));
@@ -1549,7 +1605,15 @@ void gcmc_set_grid(GcmcImpl* g, const GridImpl* grid) {
 void gcmc_set_precision(GcmcImpl* g, int precision) {
     require(precision == ALEA_FP64 || precision == ALEA_FP32, ALEA_ERR_INVALID_ARGUMENT,
             "GCMC: precision must be ALEA_FP64 or ALEA_FP32");
-    g->C.f32 = precision == ALEA_FP32;
+    const int f32 = precision == ALEA_FP32;
+    const uint64_t n = g->C.nk * g->n_chains;
+    if (f32 != g->C.f32 && g->C.charged && n) {  // carry the committed S(k) across
+        convert_sk_kernel<<<(unsigned)((n + 255) / 256), 256>>>(n, f32, g->sre.p, g->sim.p,
+                                                                g->sk_hi.p, g->sk_lo.p);
+        ALEA_CUDA(cudaGetLastError());
+        ALEA_CUDA(cudaDeviceSynchronize());
+    }
+    g->C.f32 = f32;
 }
 
 unsigned gcmc_chains(const GcmcImpl* g) { return g->n_chains; }
