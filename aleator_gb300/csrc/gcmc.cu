@@ -130,6 +130,7 @@ struct StepShared {
     int move, valid, accept, do_resync;
     int sp_old, sp_new;       // species of the old and the new sites
     double sq_slot[2 * MAXS];  // charge per slot (old sites, then new)
+    float sq32[2 * MAXS];      // the same in FP32 (the FP32 form's phase products)
     int row_slot[2 * MAXS];    // pair-table row per slot
     uint32_t mi;
     int n_old, n_new;
@@ -505,6 +506,7 @@ __device__ __forceinline__ void slot_tables(const GcmcConst& C, StepShared& S) {
         S.sq_slot[C.ns + s] = C.spq[S.sp_new][s];
         S.row_slot[C.ns + s] = C.sprow[S.sp_new][s];
     }
+    for (int e = 0; e < 2 * MAXS; ++e) S.sq32[e] = (float)S.sq_slot[e];
 }
 
 // The grid's value at site slot e (old sites first, then new): its LJ
@@ -619,7 +621,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 auto zq = [&](int e) -> float2 {
                     if (ab_table) return ab32[(e * tw + n0) * tw + n1];
                     const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1];
-                    const float q = (float)S.sq_slot[e];
+                    const float q = S.sq32[e];
                     return make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
                 };
                 if (n_new)
@@ -803,7 +805,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     const bool is_old = e < NS;
                     if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
                     const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1];
-                    const float q = (float)S.sq_slot[e];
+                    const float q = S.sq32[e];
                     ab32[i] = make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
                 }
                 __syncthreads();
