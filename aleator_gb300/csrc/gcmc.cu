@@ -42,7 +42,7 @@ namespace alea {
 
 namespace {
 
-constexpr int GT = 256;     // threads per chain
+constexpr int GT = 512;     // threads per chain
 constexpr int MAXS = 8;     // sites per molecule
 constexpr int KMAXC = 64;   // largest kMax the per-site phase tables hold
 // the FP32 form's (n0, n1) product table is used while it fits this budget
