@@ -1,5 +1,5 @@
-// Single-species GCMC chains on sm_103a, one CTA per chain, every move of a
-// launch in one persistent loop.
+// GCMC chains (one rigid species, or a mixture of up to four) on sm_103a, one
+// 512-thread CTA per chain, every move of a launch in one persistent loop.
 //
 // Reference: MonteCarloEngine (engines/monte_carlo/monte_carlo_engine.cc):
 //   run                      :405-439   25 % each translate / rotate / insert / delete
