@@ -121,6 +121,7 @@ struct GcmcPtrs {
     // lo per term (the term loop reads the hi pair), and the terms' (n0, n1, n2)
     // packed as (n0+K) | (n1+K) << 8 | (n2+K) << 16
     float2 *sk_hi, *sk_lo;
+    const float2 *sfw_hi, *sfw_lo;  // FP32 form: the framework's S(k) as double-float
     const uint32_t* npack;
     const double* gtab[MAXROWS];  // per pair-table row: its LJ species' grid table
     uint32_t* msp;                // per chain, per molecule: its species
@@ -1057,36 +1058,57 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 __syncthreads();
                 if (S.do_resync) {
                     const uint64_t ng = S.ng_after;
-                    for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
-                        const double k0 = P.k[3 * t], k1 = P.k[3 * t + 1], k2 = P.k[3 * t + 2];
-                        double re = P.sfw_re[t], im = P.sfw_im[t];
-                        if constexpr (F32) {
-                            // FP32 phases from the angle reduced in FP64, summed in double-float
-                            ff rf{0.f, 0.f}, imf{0.f, 0.f};
-                            for (uint64_t g = 0; g < ng; ++g) {
-                                const double x = k0 * gx[g] + k1 * gy[g] + k2 * gz[g];
+                    if constexpr (F32) {
+                        // the framework's S(k), then the guest sites in chunks of 2 NS
+                        // through the phase tables (each site's angles reduced in FP64
+                        // once per n), products in FP32, each chunk's sum added in
+                        // double-float
+                        for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
+                            sk_hi[t] = P.sfw_hi[t];
+                            sk_lo[t] = P.sfw_lo[t];
+                        }
+                        for (uint64_t g0 = 0; g0 < ng; g0 += 2 * NS) {
+                            const int m = (int)min((uint64_t)(2 * NS), ng - g0);
+                            __syncthreads();  // the previous chunk's tables are read
+                            for (int i = threadIdx.x; i < m * 3 * tw; i += GT) {
+                                const int e = i / (3 * tw), a = (i / tw) % 3, n = i % tw - K;
+                                const uint64_t g = g0 + e;
+                                const double th = C.b[3 * a] * gx[g] + C.b[3 * a + 1] * gy[g] + C.b[3 * a + 2] * gz[g];
+                                const double x = (double)n * th;
                                 const double r = x - (2.0 * kPi) * rint(x * (0.5 / kPi));
                                 float sn, cs;
                                 sincosf((float)r, &sn, &cs);
-                                const float q = ghi[g].w;
-                                rf = ff_add_f(rf, q * cs);
-                                imf = ff_add_f(imf, q * sn);
+                                etab32[i] = make_float2(cs, sn);
                             }
-                            re += (double)rf.hi + (double)rf.lo;
-                            im += (double)imf.hi + (double)imf.lo;
-                        } else {
+                            __syncthreads();
+                            for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
+                                const uint32_t pk = P.npack[t];
+                                const int n0 = pk & 0xff, n1 = (pk >> 8) & 0xff, n2 = (pk >> 16) & 0xff;
+                                float re = 0.f, im = 0.f;
+                                for (int e = 0; e < m; ++e) {
+                                    const float q = ghi[g0 + e].w;
+                                    const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1],
+                                                 Cc = etab32[(e * 3 + 2) * tw + n2];
+                                    const float abr = A.x * B.x - A.y * B.y, abi = A.x * B.y + A.y * B.x;
+                                    re = fmaf(q, abr * Cc.x - abi * Cc.y, re);
+                                    im = fmaf(q, abr * Cc.y + abi * Cc.x, im);
+                                }
+                                const float2 h = sk_hi[t], l = sk_lo[t];
+                                const ff fr = ff_add_f(ff{h.x, l.x}, re), fi = ff_add_f(ff{h.y, l.y}, im);
+                                sk_hi[t] = make_float2(fr.hi, fi.hi);
+                                sk_lo[t] = make_float2(fr.lo, fi.lo);
+                            }
+                        }
+                    } else {
+                        for (uint64_t t = threadIdx.x; t < C.nk; t += GT) {
+                            const double k0 = P.k[3 * t], k1 = P.k[3 * t + 1], k2 = P.k[3 * t + 2];
+                            double re = P.sfw_re[t], im = P.sfw_im[t];
                             for (uint64_t g = 0; g < ng; ++g) {
                                 double sn, cs;
                                 sincos(k0 * gx[g] + k1 * gy[g] + k2 * gz[g], &sn, &cs);
                                 re += gq[g] * cs;
                                 im += gq[g] * sn;
                             }
-                        }
-                        if constexpr (F32) {
-                            const ff fr = ff_from(re), fi = ff_from(im);
-                            sk_hi[t] = make_float2(fr.hi, fi.hi);
-                            sk_lo[t] = make_float2(fr.lo, fi.lo);
-                        } else {
                             sre[t] = re;
                             sim[t] = im;
                         }
@@ -1163,14 +1185,16 @@ __global__ void convert_sk_kernel(uint64_t n, int to_f32, double* re, double* im
 // double-float; the weights' FP32 copy and the packed term indices too.
 __global__ void gather_sfw_kernel(uint64_t nk, const double* re, const double* im, const double* w,
                                   const int* nidx, int kmax, double* out_re, double* out_im,
-                                  float2* out_hi, float2* out_lo, float* w32, uint32_t* npack,
-                                  unsigned n_chains) {
+                                  float2* out_hi, float2* out_lo, float2* fw_hi, float2* fw_lo,
+                                  float* w32, uint32_t* npack, unsigned n_chains) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nk) return;
     w32[t] = (float)w[t];
     npack[t] = (uint32_t)(nidx[3 * t] + kmax) | (uint32_t)(nidx[3 * t + 1] + kmax) << 8 |
                (uint32_t)(nidx[3 * t + 2] + kmax) << 16;
     const ff fr = ff_from(re[t]), fi = ff_from(im[t]);
+    fw_hi[t] = make_float2(fr.hi, fi.hi);
+    fw_lo[t] = make_float2(fr.lo, fi.lo);
     for (unsigned c = 0; c < n_chains; ++c) {
         out_re[(size_t)c * nk + t] = re[t];
         out_im[(size_t)c * nk + t] = im[t];
@@ -1198,6 +1222,7 @@ struct GcmcImpl {
     DevBuf<uint32_t> msp;               // species of each molecule, per chain
     DevBuf<float> w32;                  // FP32 form: the weights
     DevBuf<float2> sk_hi, sk_lo;        // FP32 form: each chain's S(k) as double-float
+    DevBuf<float2> sfw_hi, sfw_lo;      // FP32 form: the framework's S(k) as double-float
     DevBuf<uint32_t> npack;             // FP32 form: packed (n0, n1, n2) per term
     const double* gtab[MAXROWS] = {};  // the borrowed grid's tables, per pair-table row
     float last_ms = 0.f;
@@ -1384,10 +1409,12 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         g->npack.alloc(nkc);
         g->sk_hi.alloc(nkc * n_chains);
         g->sk_lo.alloc(nkc * n_chains);
+        g->sfw_hi.alloc(nkc);
+        g->sfw_lo.alloc(nkc);
         if (ews) {
             gather_sfw_kernel<<<(unsigned)((nk + 255) / 256), 256>>>(
                 nk, g->sfw_re.p, g->sfw_im.p, g->w.p, g->nidx.p, C.kmax, g->sre.p, g->sim.p,
-                g->sk_hi.p, g->sk_lo.p, g->w32.p, g->npack.p, n_chains);
+                g->sk_hi.p, g->sk_lo.p, g->sfw_hi.p, g->sfw_lo.p, g->w32.p, g->npack.p, n_chains);
             ALEA_CUDA(cudaGetLastError());
         }
         const size_t sites = (size_t)C.max_sites * n_chains;
@@ -1462,6 +1489,8 @@ void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s) {
     P.msp = g->msp.p;
     P.sk_hi = g->sk_hi.p;
     P.sk_lo = g->sk_lo.p;
+    P.sfw_hi = g->sfw_hi.p;
+    P.sfw_lo = g->sfw_lo.p;
     P.npack = g->npack.p;
     cudaEvent_t e0, e1;
     ALEA_CUDA(cudaEventCreate(&e0));
