@@ -288,11 +288,8 @@ def main():
     h2d = st["images"] * 32 + (fw.n_atoms * (4 * 8 + 4))
     d2h = nodes * 8 * len(guests)
     e2e_steps = max(2, min(args.steps, 5))
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+
+    def e2e_step():
         g = A.FrameworkEnergyGrid(ff, parts, fw.lattice, guests, SPACING, A.FP32)
         for i, s in enumerate(guests):
             status = A.library().alea_grid_download(
@@ -300,6 +297,14 @@ def main():
             if status != 0:
                 raise RuntimeError(f"alea_grid_download failed with status {status}")
         del g
+
+    e2e_step()  # untimed warm-up: the first copy into freshly pinned pages runs at half speed
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if dist:
