@@ -1470,6 +1470,56 @@ grid_interpolate_fast_kernel(Lattice L, InvFF inv, int nx, int ny, int nz,
     }
 }
 
+// The corner blocks of an FP32-form table: node i's eight corners (k = x + 2y
+// + 4z, 0 the node, 1 the next node along that axis with wrap) as four
+// double2, grid_ff_blend's order.
+__global__ void grid_corners_kernel(int nx, int ny, int nz, const double* __restrict__ t,
+                                    double2* __restrict__ out) {
+    const uint64_t nodes = (uint64_t)nx * ny * nz;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nodes; i += stride) {
+        const int ix = (int)(i % nx);
+        const uint64_t r = i / nx;
+        const int iy = (int)(r % ny), iz = (int)(r / ny);
+        const int jx = ix + 1 == nx ? 0 : ix + 1, jy = iy + 1 == ny ? 0 : iy + 1,
+                  jz = iz + 1 == nz ? 0 : iz + 1;
+        auto V = [&](int x, int y, int z) { return __ldg(&t[((size_t)z * ny + y) * nx + x]); };
+        out[4 * i] = make_double2(V(ix, iy, iz), V(jx, iy, iz));
+        out[4 * i + 1] = make_double2(V(ix, jy, iz), V(jx, jy, iz));
+        out[4 * i + 2] = make_double2(V(ix, iy, jz), V(jx, iy, jz));
+        out[4 * i + 3] = make_double2(V(ix, jy, jz), V(jx, jy, jz));
+    }
+}
+
+// FP32-form grids with their corner blocks: as grid_interpolate_fast_kernel,
+// the eight corners read as one aligned 64-byte block (one DRAM row) instead
+// of four 16-byte pairs in four rows.
+__global__ void __launch_bounds__(256)
+grid_interpolate_corners_kernel(Lattice L, InvFF inv, int nx, int ny, int nz,
+                                const double2* __restrict__ corners,
+                                const double* __restrict__ table, const double* __restrict__ xyz,
+                                uint64_t n, double* __restrict__ out) {
+    const int cnt[3] = {nx, ny, nz};
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double px = xyz[3 * i], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
+        int i0[3], i1[3];
+        ff t[3];
+        const bool ok = grid_ff_locate(inv, cnt, px, py, pz, i0, i1, t);
+        const uint64_t node = ok ? ((uint64_t)i0[2] * ny + i0[1]) * nx + i0[0] : 0;
+        double c[8];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const double2 v = __ldg(&corners[4 * node + k]);
+            c[2 * k] = v.x;
+            c[2 * k + 1] = v.y;
+        }
+        double r;
+        if (!ok || !grid_ff_blend(c, t, r)) r = grid_interp_fast(L, nx, ny, nz, table, px, py, pz);
+        out[i] = r;
+    }
+}
+
 struct BuildArgs {
     const ImageRec* images;      // FP64 form
     const ImageRecF* images_f;   // FP32 form
@@ -1546,6 +1596,13 @@ struct GridImpl {
     uint64_t executed_pairs = 0;
     float last_ms = 0.f;
     int launches = 0;
+    // FP32-form grids: per species, the eight trilinear corners of every node
+    // stored together (64 B a node), made on the first device interpolation of
+    // that species and remade after a build (gen counts the builds)
+    uint64_t gen = 0;
+    std::vector<DevBuf<double2>> corners;
+    std::vector<uint64_t> corners_gen;
+    bool corners_off = false;  // their allocation failed once: the plain table serves
 };
 
 static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_particles& fw,
@@ -1750,6 +1807,7 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
 }
 
 static void run_build(GridImpl& g, cudaStream_t s) {
+    ++g.gen;
     const int ng = (int)g.species.size();
     const size_t nodes = (size_t)g.geo.n[0] * g.geo.n[1] * g.geo.n[2];
     const uint64_t nbricks = (uint64_t)g.geo.bricks[0] * g.geo.bricks[1] * g.geo.bricks[2];
@@ -1825,6 +1883,38 @@ GridView grid_view(const GridImpl* g, uint32_t species) {
     return v;
 }
 
+// The corner blocks of an FP32-form grid's species table, made (on stream s)
+// when missing or older than the table; null when they cannot be allocated.
+static const double2* grid_corners(GridImpl* g, uint32_t species, cudaStream_t s) {
+    if (g->corners_off) return nullptr;
+    const int k = table_index(g, species);
+    const size_t nodes = (size_t)g->geo.n[0] * g->geo.n[1] * g->geo.n[2];
+    if (g->corners.size() != g->species.size()) {
+        g->corners.resize(g->species.size());
+        g->corners_gen.assign(g->species.size(), 0);
+    }
+    if (!g->corners[k].p || g->corners_gen[k] != g->gen) {
+        if (!g->corners[k].p) {
+            try {
+                g->corners[k].alloc(4 * nodes);
+            } catch (const Error&) {
+                (void)cudaGetLastError();  // out of memory: not sticky
+                g->corners[k].release();
+                g->corners_off = true;
+                return nullptr;
+            }
+        }
+        int dev = 0, sms = 0;
+        ALEA_CUDA(cudaGetDevice(&dev));
+        ALEA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        grid_corners_kernel<<<(unsigned)sms * 8, 256, 0, s>>>(g->geo.n[0], g->geo.n[1], g->geo.n[2],
+                                                              grid_table(g, species), g->corners[k].p);
+        ALEA_CUDA(cudaGetLastError());
+        g->corners_gen[k] = g->gen;
+    }
+    return g->corners[k].p;
+}
+
 void grid_interpolate_device(const GridImpl* g, uint32_t species, const double* xyz, uint64_t n,
                              double* out, cudaStream_t s) {
     const double* tab = grid_table(g, species);
@@ -1842,8 +1932,14 @@ void grid_interpolate_device(const GridImpl* g, uint32_t species, const double* 
         ALEA_CUDA(cudaGetDevice(&dev));
         ALEA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         const unsigned fb = (unsigned)std::min<uint64_t>(blocks, (uint64_t)sms * 24);
-        grid_interpolate_fast_kernel<<<fb, 256, 0, s>>>(g->geo.L, inv, g->geo.n[0], g->geo.n[1],
-                                                       g->geo.n[2], tab, xyz, n, out);
+        const double2* cb = grid_corners(const_cast<GridImpl*>(g), species, s);
+        if (cb)
+            grid_interpolate_corners_kernel<<<fb, 256, 0, s>>>(g->geo.L, inv, g->geo.n[0],
+                                                              g->geo.n[1], g->geo.n[2], cb, tab,
+                                                              xyz, n, out);
+        else
+            grid_interpolate_fast_kernel<<<fb, 256, 0, s>>>(g->geo.L, inv, g->geo.n[0], g->geo.n[1],
+                                                           g->geo.n[2], tab, xyz, n, out);
     } else
         grid_interpolate_kernel<<<blocks, 256, 0, s>>>(g->geo.L, g->geo.n[0], g->geo.n[1],
                                                       g->geo.n[2], tab, xyz, n, out);

@@ -703,9 +703,9 @@ def extras(A, torch, peaks):
         "note": "96 algorithmic bytes per query (8 corner loads of 8 B + 24 B in + 8 B out), random "
                 "queries over a 0.7 GB table of an FP32-form grid, against the HBM copy peak. The "
                 "transform and lerps run in double-float on the FP32 pipe (operands split by integer "
-                "operations), so the kernel waits on random 32-byte-sector gathers: each query "
-                "touches ~4 sectors in 4 DRAM rows, ~130 B of DRAM traffic per query at a 41 % L2 "
-                "hit rate on the 2x2x2 grid, more on this one. The FP64-form grids keep the "
+                "operations); each query reads its eight corners as one aligned 64-byte block of a "
+                "per-node corner copy (made on the first interpolation after a build), so the "
+                "kernel is bound by random 64-byte DRAM reads. The FP64-form grids keep the "
                 "reference's FP64 arithmetic (3 IEEE divisions) for bit-equal values"}
     return out
 
