@@ -339,11 +339,11 @@ class Oracle:
 
     def gcmc_mixture(self, ff, ewald, m, x, y, z, q, species, guests, temperature, fugacities_pa,
                      seed, stream, max_translation=1.5, max_rotation=0.5,
-                     draw_order=DRAWS_RIGHT_TO_LEFT):
-        """Several rigid species (the engine's mixture constructor)."""
+                     draw_order=DRAWS_RIGHT_TO_LEFT, grid=None):
+        """Several rigid species (the engine's mixture constructor); grid as in gcmc()."""
         return OracleGcmc(self, ff, ewald, m, x, y, z, q, species, list(guests), temperature,
                           list(fugacities_pa), seed, stream, max_translation, max_rotation,
-                          draw_order)
+                          draw_order, grid)
 
 
 class OracleGcmc:
@@ -584,7 +584,8 @@ class Reference:
                                               ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                               ctypes.c_int, ctypes.c_uint32, _U32, _D, _D, _D, _U32,
                                               _D, _D, ctypes.c_double, ctypes.c_double,
-                                              ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64]
+                                              ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64,
+                                              ctypes.c_double, ctypes.c_uint32, _U32]
         L.ref_gcmc_molecules_of.restype = ctypes.c_uint64
         L.ref_gcmc_molecules_of.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
         L.ref_gcmc_run.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
@@ -786,10 +787,11 @@ class Reference:
                              fugacity_pa, seed, stream, max_translation, max_rotation, grid)
 
     def gcmc_mixture(self, ff, ewald, m, x, y, z, q, species, guests, temperature, fugacities_pa,
-                     seed, stream, max_translation=1.5, max_rotation=0.5):
-        """The engine's mixture constructor (several rigid species)."""
+                     seed, stream, max_translation=1.5, max_rotation=0.5, grid=None):
+        """The engine's mixture constructor (several rigid species); grid as in gcmc()."""
         return ReferenceGcmc(self, ff, ewald, m, x, y, z, q, species, list(guests), temperature,
-                             list(fugacities_pa), seed, stream, max_translation, max_rotation)
+                             list(fugacities_pa), seed, stream, max_translation, max_rotation,
+                             grid)
 
 
 class ReferenceGcmc:
@@ -822,13 +824,16 @@ class ReferenceGcmc:
                 max_rotation, seed, stream]
         if mixture:
             fug = _f64(np.asarray(fugacity_pa, float))
-            self._keep = self._keep + (fug,)
+            gids = np.ascontiguousarray(grid["species"] if grid is not None else [0], dtype=np.uint32)
+            gids = gids if grid is not None else gids[:0]
+            self._keep = self._keep + (fug, gids)
             self.h = ref.lib.ref_gcmc_create_mixture(
                 _dp(_mat(m)), len(x), _dp(x), _dp(y), _dp(z), _dp(q), _u32(sp), len(eps), _dp(eps),
                 _dp(sig), ff["cutoff"], ff.get("truncation", SHIFTED),
                 ff.get("mixing", LORENTZ_BERTHELOT), alpha, erc, kmax, len(guests), _u32(per),
                 _dp(gx), _dp(gy), _dp(gz), _u32(gs), _dp(gq), _dp(fug), temperature,
-                max_translation, max_rotation, seed, stream)
+                max_translation, max_rotation, seed, stream,
+                grid["spacing"] if grid is not None else 0.0, len(gids), _u32(gids))
         elif grid is None:
             self.h = ref.lib.ref_gcmc_create(*args)
         else:

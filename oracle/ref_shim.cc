@@ -499,7 +499,8 @@ void* ref_gcmc_create_grid(const double* m, uint64_t n, const double* x, const d
 }
 
 // The mixture constructor (monte_carlo_engine.hpp:143-151): nGuest species,
-// species k with nSitesPer[k] sites, their site arrays concatenated.
+// species k with nSitesPer[k] sites, their site arrays concatenated; with
+// nGrid > 0, the engine's FrameworkEnergyGrid of those species at `spacing`.
 void* ref_gcmc_create_mixture(const double* m, uint64_t n, const double* x, const double* y,
                               const double* z, const double* q, const uint32_t* sp,
                               uint32_t nSpecies, const double* eps, const double* sigma,
@@ -508,7 +509,8 @@ void* ref_gcmc_create_mixture(const double* m, uint64_t n, const double* x, cons
                               const double* sx, const double* sy, const double* sz,
                               const uint32_t* sLj, const double* sq, const double* fugacitiesPa,
                               double temperature, double maxTrans, double maxRot, uint64_t seed,
-                              uint64_t stream) {
+                              uint64_t stream, double spacing, uint32_t nGrid,
+                              const uint32_t* gridSpecies) {
     auto* g = new RefGcmc{latticeOf(m), nullptr};
     const auto fw = particlesOf(n, x, y, z, q, sp);
     auto lj = ljOf(nSpecies, eps, sigma, cutoff, trunc, mixing);
@@ -522,11 +524,16 @@ void* ref_gcmc_create_mixture(const double* m, uint64_t n, const double* x, cons
         fug.push_back(fugacitiesPa[k]);
         off += nSitesPer[k];
     }
+    std::shared_ptr<const engines::FrameworkEnergyGrid> grid;
+    if (nGrid > 0) {
+        const std::vector<uint32_t> ids(gridSpecies, gridSpecies + nGrid);
+        grid = std::make_shared<const engines::FrameworkEnergyGrid>(*lj, fw, g->lattice, ids, spacing);
+    }
     auto rng = std::make_unique<core::Philox4x32Rng>();
     rng->seed(seed, stream);
     g->engine = std::make_unique<engines::MonteCarloEngine>(fw, g->lattice, lj, std::move(rng),
                                                             temperature, list, fug, maxTrans,
-                                                            maxRot, ewald, nullptr);
+                                                            maxRot, ewald, grid);
     return g;
 }
 

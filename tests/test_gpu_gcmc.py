@@ -196,3 +196,33 @@ def test_mixture_chain_matches_oracle(lib, orc, charged):
         _compare(gpu, cpu, charged=charged)
         assert gpu.info()["species_molecules"][:2] == [cpu.molecules_of(k) for k in range(2)]
     assert gpu.info()["accepted"][4] > 0  # swaps accepted
+
+
+def test_mixture_with_energy_grid_matches_oracle(lib, orc):
+    """CH4 + charged CO2 with the engine's energy grid (one table per guest LJ
+    species: CH4, CO2's O and C): the same moves, decisions and positions as
+    the oracle's mixture engine with the same tables."""
+    A, _ = lib
+    fw = W.cubic_framework(seed=23, charged=True)
+    fw.charge = fw.charge * 0.15
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    ewd = dict(alpha=0.31, rc=12.0, kmax=5)
+    ew = A.Ewald(0.31, 12.0, 5)
+    guests = [W.co2_guest(fw), W.ch4_guest(fw)]
+    species = sorted({int(s) for g in guests for s in g["lj_species"]})
+    grid = A.FrameworkEnergyGrid(ff, p, fw.lattice, species, 0.5, A.FP64)
+    od = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.8, truncation=O.SHIFTED)
+    tables = {s: orc.grid_build(od, fw.lattice, fw.x, fw.y, fw.z, fw.species, s, 0.5, threads=8)
+              for s in species}
+    fugs = [orc.pr_fugacity(*W.CO2_CRITICAL, 298.0, 5e5), orc.pr_fugacity(*W.METHANE_CRITICAL, 298.0, 2e6)]
+    gpu = A.GcmcChains(ff, p, fw.lattice, guests, 298.0, [fugs], [13], [2], ewald=ew)
+    gpu.set_grid(grid)
+    cpu = orc.gcmc_mixture(od, ewd, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guests,
+                           298.0, fugs, 13, 2, grid={"counts": grid.point_counts(), "tables": tables})
+    for _ in range(4):
+        gpu.run(300)
+        cpu.run(300)
+        _compare(gpu, cpu, charged=True)
+        assert gpu.info()["species_molecules"][:2] == [cpu.molecules_of(k) for k in range(2)]
+    assert gpu.molecules() > 0
