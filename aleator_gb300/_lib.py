@@ -243,6 +243,10 @@ _SIGNATURES = {
     "alea_swap_ratio": (ctypes.c_double, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                           ctypes.c_uint64, ctypes.c_double, ctypes.c_double]),
     "alea_peng_robinson_fugacity": (ctypes.c_int32, [ctypes.c_double] * 5 + [_D]),
+    "alea_grid_build_to_host": (ctypes.c_int32, [ctypes.POINTER(_LJ), ctypes.POINTER(_Particles),
+                                                 ctypes.POINTER(_Lattice), _U32, ctypes.c_uint32,
+                                                 ctypes.c_double, ctypes.c_int32,
+                                                 ctypes.POINTER(_D), ctypes.POINTER(_VP)]),
     "alea_read_cif": (ctypes.c_int32, [ctypes.c_char_p, ctypes.POINTER(_VP)]),
     "alea_structure_sizes": (ctypes.c_int32, [_VP, _U64, _U32]),
     "alea_structure_lattice": (ctypes.c_int32, [_VP, _D]),
@@ -431,6 +435,30 @@ class FrameworkEnergyGrid:
                                              _u32p(self._guests), len(self._guests),
                                              float(spacing_angstrom), int(precision),
                                              ctypes.byref(self._h)))
+
+    @classmethod
+    def build_to_host(cls, force_field: LennardJones, framework: ParticleData, lattice,
+                      guest_species_ids, spacing_angstrom: float, precision: int, host_ptrs,
+                      keep: bool = True):
+        """The constructor with every table copied to host memory as the build
+        goes (alea_grid_build_to_host): host_ptrs[k] is the address of a host
+        array of point-count-product doubles for guest_species_ids[k] (pinned
+        memory lets the copies overlap the build). Returns the grid, or None
+        when keep is False."""
+        lib = library()
+        lj = force_field.c()
+        p = framework.c()
+        lat = _lattice(lattice)
+        guests = np.ascontiguousarray(guest_species_ids, dtype=np.uint32)
+        ptrs = (_D * len(guests))(*[ctypes.cast(int(a), _D) for a in host_ptrs])
+        h = _VP()
+        _check(lib.alea_grid_build_to_host(ctypes.byref(lj), ctypes.byref(p), ctypes.byref(lat),
+                                           _u32p(guests), len(guests), float(spacing_angstrom),
+                                           int(precision), ptrs, ctypes.byref(h) if keep else None))
+        if not keep:
+            return None
+        return cls(force_field, framework, lattice, guest_species_ids, spacing_angstrom, precision,
+                   _handle=h)
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -199,6 +199,28 @@ alea_status alea_grid_build(const alea_lennard_jones* lj, const alea_particles* 
     });
 }
 
+alea_status alea_grid_build_to_host(const alea_lennard_jones* lj, const alea_particles* framework,
+                                    const alea_lattice* lattice, const uint32_t* guest_species,
+                                    uint32_t n_guest, double spacing, int32_t precision,
+                                    double* const* host_tables, alea_grid** out) {
+    return guarded([&] {
+        need(lj, "lj");
+        need(lattice, "lattice");
+        need(host_tables, "host_tables");
+        if (n_guest) need(guest_species, "guest_species");
+        for (uint32_t k = 0; k < n_guest; ++k) need(host_tables[k], "host_tables[k]");
+        if (out) *out = nullptr;
+        alea::GridImpl* impl = alea::grid_build_to_host(*lj, particles_or_empty(framework), *lattice,
+                                                        guest_species, n_guest, spacing, precision,
+                                                        host_tables);
+        if (!out) {
+            alea::grid_destroy(impl);
+            return;
+        }
+        *out = new alea_grid{impl};
+    });
+}
+
 alea_status alea_grid_point_counts(const alea_grid* g, int32_t out[3]) {
     return guarded([&] {
         need(g, "grid");

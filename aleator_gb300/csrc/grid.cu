@@ -82,6 +82,7 @@ struct GridGeom {
     double rc, rc2;
     int bricks[3];
     int n_types;             // framework LJ species in the table
+    int brick0;              // first brick of a launch (a slab of a pipelined build)
 };
 
 // ---------------------------------------------------------------- PTX helpers
@@ -361,7 +362,7 @@ grid_build_f64_kernel(GridGeom geo, const ImageRec* __restrict__ images,
 
     const int tid = threadIdx.x;
     const int nx = geo.n[0], ny = geo.n[1], nz = geo.n[2];
-    const int brick = blockIdx.x;
+    const int brick = geo.brick0 + (int)blockIdx.x;
     const int bxn = geo.bricks[0], byn = geo.bricks[1];
     const int bx = brick % bxn, by = (brick / bxn) % byn, bz = brick / (bxn * byn);
     const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
@@ -1310,7 +1311,7 @@ grid_build_f32_kernel(GridGeom geo, F32GridArgs args, unsigned long long* __rest
     }
     __syncthreads();
     uint32_t tiles = 0;
-    sweep_brick<NG, TRUNC>(geo, args, (int)blockIdx.x, smem, bars, tiles, executed, flags);
+    sweep_brick<NG, TRUNC>(geo, args, geo.brick0 + (int)blockIdx.x, smem, bars, tiles, executed, flags);
 }
 
 template <int NG, int TRUNC>
@@ -1806,7 +1807,11 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
     ALEA_CUDA(cudaMemset(g.flags.p, 0, sizeof(unsigned)));
 }
 
-static void run_build(GridImpl& g, cudaStream_t s) {
+// host: null, or per table one host array the build's rows are copied into as
+// the build goes: the bricks run in z-slabs on s, and each finished slab's
+// rows (contiguous, z being the slowest index) are copied on a second stream
+// while the next slab computes.
+static void run_build(GridImpl& g, cudaStream_t s, double* const* host = nullptr) {
     ++g.gen;
     const int ng = (int)g.species.size();
     const size_t nodes = (size_t)g.geo.n[0] * g.geo.n[1] * g.geo.n[2];
@@ -1819,19 +1824,49 @@ static void run_build(GridImpl& g, cudaStream_t s) {
     cudaEvent_t ev[2];
     for (auto& e : ev) ALEA_CUDA(cudaEventCreate(&e));
     ALEA_CUDA(cudaEventRecord(ev[0], s));
-    for (int c = 0; c < chunks; ++c) {
-        const int g0 = c * MAX_NG;
-        const int cnt = std::min(MAX_NG, ng - g0);
-        dim3 grid((unsigned)nbricks);
-        const size_t pofs = (size_t)g0 * g.geo.n_types;
-        const BuildArgs args{g.images.p, g.images_f.p, g.bin_start.p, g.params.p, g.guests.p + g0,
-                             f32 ? g.pab.p + pofs : nullptr, f32 ? g.pff.p + pofs : nullptr,
-                             g.tables.p + (size_t)g0 * nodes, g.executed.p, g.flags.p};
-        launch_build(cnt, g.truncation, f32, grid, s, g.geo, args);
-        ALEA_CUDA(cudaGetLastError());
+    const int layers = g.geo.bricks[2];
+    const int slabs = host ? std::min(4, layers) : 1;
+    const uint64_t per_layer = (uint64_t)g.geo.bricks[0] * g.geo.bricks[1];
+    const size_t row = (size_t)g.geo.n[0] * g.geo.n[1];
+    cudaStream_t cs = nullptr;
+    std::vector<cudaEvent_t> done(slabs);
+    if (host) {
+        ALEA_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        for (auto& e : done) ALEA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    for (int sl = 0; sl < slabs; ++sl) {
+        const int z0 = (int)((int64_t)layers * sl / slabs), z1 = (int)((int64_t)layers * (sl + 1) / slabs);
+        GridGeom geo = g.geo;
+        geo.brick0 = (int)(per_layer * z0);
+        for (int c = 0; c < chunks; ++c) {
+            const int g0 = c * MAX_NG;
+            const int cnt = std::min(MAX_NG, ng - g0);
+            dim3 grid((unsigned)(per_layer * (z1 - z0)));
+            const size_t pofs = (size_t)g0 * g.geo.n_types;
+            const BuildArgs args{g.images.p, g.images_f.p, g.bin_start.p, g.params.p, g.guests.p + g0,
+                                 f32 ? g.pab.p + pofs : nullptr, f32 ? g.pff.p + pofs : nullptr,
+                                 g.tables.p + (size_t)g0 * nodes, g.executed.p, g.flags.p};
+            launch_build(cnt, g.truncation, f32, grid, s, geo, args);
+            ALEA_CUDA(cudaGetLastError());
+        }
+        if (host) {  // this slab's node rows z in [BZ z0, BZ z1) of every table
+            ALEA_CUDA(cudaEventRecord(done[sl], s));
+            ALEA_CUDA(cudaStreamWaitEvent(cs, done[sl], 0));
+            const size_t a = (size_t)BZ * z0 * row;
+            const size_t b = std::min((size_t)BZ * z1, (size_t)g.geo.n[2]) * row;
+            for (int k = 0; k < ng; ++k)
+                if (host[k] && b > a)
+                    ALEA_CUDA(cudaMemcpyAsync(host[k] + a, g.tables.p + (size_t)k * nodes + a,
+                                              (b - a) * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        }
     }
     ALEA_CUDA(cudaEventRecord(ev[1], s));
     ALEA_CUDA(cudaEventSynchronize(ev[1]));
+    if (host) {
+        ALEA_CUDA(cudaStreamSynchronize(cs));
+        for (auto& e : done) cudaEventDestroy(e);
+        cudaStreamDestroy(cs);
+    }
     float ms = 0.f;
     ALEA_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
     for (auto& e : ev) cudaEventDestroy(e);
@@ -1858,6 +1893,34 @@ GridImpl* grid_build(const alea_lennard_jones& lj, const alea_particles& fw,
 }
 
 void grid_rebuild(GridImpl* g, cudaStream_t s) { run_build(*g, s); }
+
+GridImpl* grid_build_to_host(const alea_lennard_jones& lj, const alea_particles& fw,
+                             const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
+                             double spacing, int precision, double* const* host) {
+    auto* g = new GridImpl();
+    try {
+        build_plan(*g, lj, fw, lat, guest, n_guest, spacing, precision, 2.0);
+        // host arrays in the order of `guest`, tables in the grid's (sorted) order
+        std::vector<double*> per_table(g->species.size(), nullptr);
+        for (uint32_t k = 0; k < n_guest; ++k) {
+            const size_t t = (size_t)(std::lower_bound(g->species.begin(), g->species.end(), guest[k]) -
+                                      g->species.begin());
+            if (!per_table[t]) per_table[t] = host[k];
+        }
+        run_build(*g, 0, per_table.data());
+        // a species listed twice: its other arrays get the copy made above
+        for (uint32_t k = 0; k < n_guest; ++k) {
+            const size_t t = (size_t)(std::lower_bound(g->species.begin(), g->species.end(), guest[k]) -
+                                      g->species.begin());
+            const size_t nodes = (size_t)g->geo.n[0] * g->geo.n[1] * g->geo.n[2];
+            if (host[k] != per_table[t]) std::memcpy(host[k], per_table[t], nodes * sizeof(double));
+        }
+    } catch (...) {
+        delete g;
+        throw;
+    }
+    return g;
+}
 void grid_destroy(GridImpl* g) { delete g; }
 
 static int table_index(const GridImpl* g, uint32_t species) {

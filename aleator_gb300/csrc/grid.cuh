@@ -16,6 +16,11 @@ GridImpl* grid_from_tables(const alea_lattice& lat, double spacing, const int32_
                            const std::vector<uint32_t>& species,
                            const std::vector<std::vector<double>>& tables);
 void grid_rebuild(GridImpl* g, cudaStream_t s);
+// grid_build whose tables are also copied into host[k] (one array per entry of
+// guest, nodes long; pinned memory lets the copies overlap the build).
+GridImpl* grid_build_to_host(const alea_lennard_jones& lj, const alea_particles& fw,
+                             const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
+                             double spacing, int precision, double* const* host);
 void grid_destroy(GridImpl* g);
 const double* grid_table(const GridImpl* g, uint32_t species);
 void grid_interpolate_device(const GridImpl* g, uint32_t species, const double* xyz, uint64_t n,

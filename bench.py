@@ -14,8 +14,9 @@ evaluations per second, counted as the reference's loop counts them
   (alea_grid_rebuild), L2 flushed between steps; CUDA events on the launching
   stream; max over ranks.
 * ``e2e``: the same metric through the public C-ABI call a user makes
-  (FrameworkEnergyGrid from host arrays, then both tables copied to pinned
-  host memory), host<->device copies inside the timed region.
+  (alea_grid_build_to_host: the grid from host arrays with both tables copied
+  into pinned host memory as the build's z-slabs finish), host<->device copies
+  inside the timed region.
 * ``roofline``: the build kernel against the FP32 FFMA peak measured in the
   same run (the kernel is FP32-pipe bound; the peaks file has no FP32 figure).
 * ``cpu_baseline``: the CPU restatement of the reference's grid loop on a
@@ -289,14 +290,9 @@ def main():
     d2h = nodes * 8 * len(guests)
     e2e_steps = max(2, min(args.steps, 5))
 
-    def e2e_step():
-        g = A.FrameworkEnergyGrid(ff, parts, fw.lattice, guests, SPACING, A.FP32)
-        for i, s in enumerate(guests):
-            status = A.library().alea_grid_download(
-                g._h, s, ctypes.cast(pinned[i].data_ptr(), ctypes.POINTER(ctypes.c_double)), nodes)
-            if status != 0:
-                raise RuntimeError(f"alea_grid_download failed with status {status}")
-        del g
+    def e2e_step():  # alea_grid_build_to_host: the build with the table copies overlapped
+        A.FrameworkEnergyGrid.build_to_host(ff, parts, fw.lattice, guests, SPACING, A.FP32,
+                                            [t.data_ptr() for t in pinned], keep=False)
 
     e2e_step()  # untimed warm-up: the first copy into freshly pinned pages runs at half speed
     if dist:

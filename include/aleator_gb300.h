@@ -178,6 +178,16 @@ alea_status alea_grid_serialize(const alea_grid* g, const char* path,
                                 const alea_lennard_jones* lj, const alea_particles* framework,
                                 const alea_lattice* lattice, const uint32_t* guest_species,
                                 uint32_t n_guest);
+/* The constructor followed by reading every table, pipelined: the build runs
+ * in z-slabs and each finished slab's node rows are copied to host_tables[k]
+ * (one array of point_counts' product doubles per entry of guest_species, in
+ * that order) while the next slab computes. Pinned host arrays
+ * (cudaHostAlloc) let the copies overlap; pageable ones still work. *out may
+ * be NULL when only the tables are wanted. */
+alea_status alea_grid_build_to_host(const alea_lennard_jones* lj, const alea_particles* framework,
+                                    const alea_lattice* lattice, const uint32_t* guest_species,
+                                    uint32_t n_guest, double spacing_angstrom, int32_t precision,
+                                    double* const* host_tables, alea_grid** out);
 /* cacheFilePath(cacheDirectory, key) (framework_energy_grid.cc:318-325). */
 alea_status alea_grid_cache_file_name(const alea_lennard_jones* lj,
                                       const alea_particles* framework,

@@ -322,3 +322,29 @@ def test_grid_from_cif_structure(lib, orc):
     od = dict(eps=fw.eps, sigma=fw.sigma, cutoff=9.0, truncation=O.SHIFTED)
     want = orc.grid_build(od, fw.lattice, fw.x, fw.y, fw.z, fw.species, ns, 1.0, threads=8)
     assert rel_err(grid.table(ns), want).max() <= 1e-10
+
+
+def test_build_to_host_equals_build(lib):
+    """alea_grid_build_to_host (slab-pipelined build with the copies overlapped)
+    hands back exactly the tables of a plain build, both forms, a species listed
+    twice included."""
+    A, _ = lib
+    import torch
+    from aleator_gb300 import workloads as W
+    fw = W.triclinic_supercell(reps=1)
+    ff = A.LennardJones(fw.eps, fw.sigma, 10.0, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    guests = [fw.guest_species["CO2_O"], fw.guest_species["CO2_C"], fw.guest_species["CO2_O"]]
+    for prec in (A.FP64, A.FP32):
+        ref = A.FrameworkEnergyGrid(ff, p, fw.lattice, guests, 0.4, prec)
+        nodes = int(np.prod(ref.point_counts()))
+        outs = [torch.full((nodes,), np.nan, dtype=torch.float64, pin_memory=True) for _ in guests]
+        g = A.FrameworkEnergyGrid.build_to_host(ff, p, fw.lattice, guests, 0.4, prec,
+                                                [o.data_ptr() for o in outs])
+        for s, o in zip(guests, outs):
+            assert np.array_equal(o.numpy(), ref.table(s))
+            assert np.array_equal(g.table(s), ref.table(s))
+        plain = np.full(nodes, np.nan)  # pageable memory and no grid kept
+        assert A.FrameworkEnergyGrid.build_to_host(ff, p, fw.lattice, guests[:1], 0.4, prec,
+                                                   [plain.ctypes.data], keep=False) is None
+        assert np.array_equal(plain, ref.table(guests[0]))
