@@ -1825,7 +1825,7 @@ static void run_build(GridImpl& g, cudaStream_t s, double* const* host = nullptr
     for (auto& e : ev) ALEA_CUDA(cudaEventCreate(&e));
     ALEA_CUDA(cudaEventRecord(ev[0], s));
     const int layers = g.geo.bricks[2];
-    const int slabs = host ? std::min(4, layers) : 1;
+    const int slabs = host ? std::min(8, layers) : 1;
     const uint64_t per_layer = (uint64_t)g.geo.bricks[0] * g.geo.bricks[1];
     const size_t row = (size_t)g.geo.n[0] * g.geo.n[1];
     cudaStream_t cs = nullptr;
