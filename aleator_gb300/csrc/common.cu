@@ -2,6 +2,8 @@
 // mixed LJ parameter tables, device error flags.
 #include <cmath>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -106,6 +108,64 @@ void require_device() {
     if (e != cudaSuccess || n == 0)
         throw Error(ALEA_ERR_NO_DEVICE, std::string("no CUDA device available: ") +
                                             (e != cudaSuccess ? cudaGetErrorString(e) : "count 0"));
+}
+
+// ---------------------------------------------------------------- device memory
+namespace {
+constexpr size_t kKeepMin = 64ull << 20;   // blocks this large are kept on release
+constexpr size_t kKeepMax = 16ull << 30;   // at most this much kept idle
+std::mutex g_mem_mu;
+std::multimap<size_t, void*> g_kept;       // idle blocks by size
+size_t g_kept_bytes = 0;
+
+void release_kept() {  // with g_mem_mu held
+    for (auto& kv : g_kept) cudaFree(kv.second);
+    g_kept.clear();
+    g_kept_bytes = 0;
+}
+}  // namespace
+
+void* dev_alloc(size_t bytes) {
+    if (bytes >= kKeepMin) {
+        std::lock_guard<std::mutex> lock(g_mem_mu);
+        const auto it = g_kept.find(bytes);
+        if (it != g_kept.end()) {
+            void* p = it->second;
+            g_kept.erase(it);
+            g_kept_bytes -= bytes;
+            return p;
+        }
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+        (void)cudaGetLastError();
+        {
+            std::lock_guard<std::mutex> lock(g_mem_mu);
+            release_kept();
+        }
+        e = cudaMalloc(&p, bytes);
+    }
+    ALEA_CUDA(e);
+    return p;
+}
+
+void dev_free(void* p, size_t bytes) {
+    if (!p) return;
+    if (bytes >= kKeepMin) {
+        std::lock_guard<std::mutex> lock(g_mem_mu);
+        if (g_kept_bytes + bytes <= kKeepMax && cudaDeviceSynchronize() == cudaSuccess) {
+            g_kept.emplace(bytes, p);
+            g_kept_bytes += bytes;
+            return;
+        }
+    }
+    cudaFree(p);
+}
+
+size_t dev_cached_bytes() {
+    std::lock_guard<std::mutex> lock(g_mem_mu);
+    return g_kept_bytes;
 }
 
 }  // namespace alea

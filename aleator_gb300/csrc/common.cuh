@@ -197,6 +197,15 @@ __device__ __forceinline__ double lj_pair_rt(int trunc, double r, double rc, con
 void mixed_table(const alea_lennard_jones& lj, PairParams* out);
 
 // ---------------------------------------------------------------- device buffers
+// Device memory for DevBuf: blocks of 64 MB and more are kept on release (up to
+// 16 GB) and handed out again for a request of the same size, so that objects
+// rebuilt step after step (a grid's tables) skip cudaMalloc/cudaFree. Keeping a
+// block synchronizes the device first, as cudaFree would; an allocation that
+// fails for memory releases the kept blocks and tries once more.
+void* dev_alloc(size_t bytes);
+void dev_free(void* p, size_t bytes);
+size_t dev_cached_bytes();
+
 template <typename T>
 struct DevBuf {
     T* p = nullptr;
@@ -222,11 +231,11 @@ struct DevBuf {
     ~DevBuf() { release(); }
     void alloc(size_t count) {
         release();
+        if (count) p = static_cast<T*>(dev_alloc(count * sizeof(T)));
         n = count;
-        if (count) ALEA_CUDA(cudaMalloc(&p, count * sizeof(T)));
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) dev_free(p, n * sizeof(T));
         p = nullptr;
         n = 0;
     }
