@@ -145,3 +145,44 @@ def test_fit_at_loading_keeps_the_loading(lib, orc):
     se = np.hypot(mu.std(ddof=1), ml.std(ddof=1)) / np.sqrt(n)
     assert mu.mean() > 0.5
     assert abs(ml.mean() - mu.mean()) <= 3 * se, (ml.mean(), mu.mean(), se)
+
+
+def test_ideal_gas_mixture_poisson_with_biased_proposal(lib):
+    """Two ideal-gas species (CH4 and a 3-site CO2, every epsilon and charge
+    zero) with identity swaps and a strongly non-uniform insertion density:
+    each species' count stays Poisson with mean f_k V / T (means within 3
+    standard errors over independent chains, variances within 10 %)."""
+    A, _ = lib
+    fw = W.cubic_framework(seed=11)
+    eps = np.zeros_like(fw.eps)
+    ff = A.LennardJones(eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData(fw.x, fw.y, fw.z, None, fw.species)
+    guests = [W.ch4_guest(fw), dict(W.co2_guest(fw), charge=[0.0, 0.0, 0.0])]
+    V = abs(np.linalg.det(np.asarray(fw.lattice).reshape(3, 3)))
+    lams = [8.0, 5.0]
+    fugs = [lam * T / V / O.PASCAL_TO_INTERNAL for lam in lams]
+    n = 128
+    chains = A.GcmcChains(ff, p, fw.lattice, guests, T, [fugs] * n, list(range(300, 300 + n)),
+                          [0] * n, max_molecules=200)
+    P = A.Proposal(seed=23)
+    rng = np.random.default_rng(7)
+    w = P.get_params()
+    P.set_params((rng.normal(0, 1, w.size) * 0.25).astype(np.float32))
+    P.tabulate(16, 0.1)
+    lp = P.log_density(PO.cell_centres(16))
+    assert np.exp(lp).max() / np.exp(lp).min() > 8.0
+    chains.set_proposal(P)
+    chains.run(10000)
+    snaps = []
+    for _ in range(100):
+        chains.run(500)
+        snaps.append([chains.info(c)["species_molecules"][:2] for c in range(n)])
+    counts = np.array(snaps, dtype=np.float64)  # snapshots x chains x species
+    info = chains.info(0)
+    assert info["accepted"][4] > 0  # swaps happened
+    for k, lam in enumerate(lams):
+        per_chain = counts[:, :, k].mean(axis=0)
+        se = per_chain.std(ddof=1) / np.sqrt(n)
+        assert abs(per_chain.mean() - lam) <= 3 * se + 1e-9, (k, per_chain.mean(), lam, se)
+        var = counts[:, :, k].var()
+        assert abs(var / lam - 1) <= 0.10, (k, var, lam)
