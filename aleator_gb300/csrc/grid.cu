@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <type_traits>
 #include <vector>
@@ -1604,6 +1605,7 @@ struct GridImpl {
     std::vector<DevBuf<double2>> corners;
     std::vector<uint64_t> corners_gen;
     bool corners_off = false;  // their allocation failed once: the plain table serves
+    std::mutex corners_mu;     // interpolations from several host threads share them
 };
 
 static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_particles& fw,
@@ -1949,6 +1951,7 @@ GridView grid_view(const GridImpl* g, uint32_t species) {
 // The corner blocks of an FP32-form grid's species table, made (on stream s)
 // when missing or older than the table; null when they cannot be allocated.
 static const double2* grid_corners(GridImpl* g, uint32_t species, cudaStream_t s) {
+    std::lock_guard<std::mutex> lock(g->corners_mu);
     if (g->corners_off) return nullptr;
     const int k = table_index(g, species);
     const size_t nodes = (size_t)g->geo.n[0] * g->geo.n[1] * g->geo.n[2];
