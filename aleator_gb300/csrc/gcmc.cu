@@ -52,6 +52,14 @@ constexpr int RSTRIDE = 4 * MAXS + 1;
 constexpr int TU = 4;  // FP32 form: reciprocal terms per turn of a thread's loop
 
 constexpr int MAXGS = GCMC_MAX_SPECIES;
+// FP32 form: pairs closer than NEAR_R (A) take the double-float displacement;
+// beyond, a pair energy (<= ~100 K of Coulomb at 6 A) moves by < 1e-4 K with
+// the FP32 one. Under plain truncation, pairs within CUT_BAND (relative, on
+// r^2) of the cutoff are decided in double-float too.
+constexpr float NEAR_R2 = 6.0f * 6.0f;
+// the near sphere under 1 % of the cell: 100 x (4/3) pi 6^3 A^3
+constexpr double FIXED_FAR_VOLUME = 100.0 * 4.0 / 3.0 * 3.14159265358979 * 216.0;
+constexpr float CUT_BAND = 1e-5f;
 constexpr int MAXROWS = 8;  // distinct LJ species among the guest sites
 
 struct GcmcConst {
@@ -85,6 +93,10 @@ struct GcmcConst {
     int prop_cells;
     double tc[MAXGS][MAXS][3];
     int f32;  // ALEA_FP32 form: FP32 pair and real-space terms, FP32 per-term S(k) deltas
+    // FP32 form: far pairs on the fixed-point displacement (cells above
+    // FIXED_FAR_VOLUME, where under 1 % of pairs are near, so that a warp
+    // rarely takes both paths)
+    int fixed_far;
     float lh[9], ll[9], linv[9];  // FP32 form: rows a_i as hi + lo; the inverse (f = d . inv)
     double excl_tmpl[MAXGS];  // FP32 form: pairExclusionSum of each rigid template
     // the engine's frameworkEnergyGrid (grid == 0: none): a site's dispersion
@@ -114,6 +126,10 @@ struct GcmcPtrs {
     const float4* fwh;
     const float4* fwl;
     float4 *ghi, *glo;
+    // FP32 form: fractional positions in 32-bit fixed point (x, y, z, 0): the
+    // wrapped displacement of a pair is an exact integer difference
+    const uint4* fwq;
+    uint4* gq4;
     // FP32 form: FP32 copies of the weights and of each chain's committed
     // S(k) (refreshed on every commit and resync), FP32 per-term deltas
     const float* w32;
@@ -485,12 +501,26 @@ __device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, 
     S.n_new = ns;
 }
 
-// The double-float copy of a guest site's position (the FP32 form's input).
-__device__ __forceinline__ void put_hilo(float4* ghi, float4* glo, uint32_t slot, const double* p,
-                                         double q) {
+// A position's fractional coordinates in 32-bit fixed point (f wrapped into
+// [0, 1), times 2^32, rounded; 1 wraps to 0).
+__host__ __device__ __forceinline__ uint4 fixed_frac(const Lattice& L, double x, double y, double z) {
+    uint32_t q[3];
+    for (int a = 0; a < 3; ++a) {
+        double f = x * L.inv[a] + y * L.inv[3 + a] + z * L.inv[6 + a];
+        f -= floor(f);
+        q[a] = (uint32_t)(uint64_t)(f * 4294967296.0 + 0.5);
+    }
+    return make_uint4(q[0], q[1], q[2], 0u);
+}
+
+// The double-float and fixed-point copies of a guest site's position (the FP32
+// form's inputs).
+__device__ __forceinline__ void put_hilo(const Lattice& L, float4* ghi, float4* glo, uint4* gq4,
+                                         uint32_t slot, const double* p, double q) {
     const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
     ghi[slot] = make_float4(x.hi, y.hi, z.hi, (float)q);
     glo[slot] = make_float4(x.lo, y.lo, z.lo, 0.f);
+    gq4[slot] = fixed_frac(L, p[0], p[1], p[2]);
 }
 
 // Per slot (old sites, then new): charge and pair-table row of its species' site.
@@ -540,7 +570,8 @@ size_t phase_bytes(int kmax, bool f32) {
     return 2 * NS * 3 * tw * sizeof(float2) + (ab <= AB_TABLE_BUDGET ? ab : 0);
 }
 
-template <int NS, bool F32>
+// FX (FP32 form, large cells): far pairs on the fixed-point displacement.
+template <int NS, bool F32, bool FX>
 __global__ void __launch_bounds__(GT)
 gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     __shared__ StepShared S;
@@ -550,6 +581,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     __shared__ PairF32 srow32[F32 ? MAXROWS : 1][64];
     __shared__ PairCloseFF srowff[F32 ? MAXROWS : 1][64];
     __shared__ float4 sph[F32 ? 2 * NS : 1], spl[F32 ? 2 * NS : 1];  // trial sites, hi + lo
+    __shared__ uint4 sfq[F32 ? 2 * NS : 1];                          // and in fixed point
     extern __shared__ __align__(16) unsigned char dyn[];
 
     const int chain = blockIdx.x;
@@ -561,6 +593,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     double* gq = P.gq + so;
     uint32_t* gt = P.gt + so;
     float4* ghi = P.ghi + so;
+    uint4* gq4 = P.gq4 + so;
     float4* glo = P.glo + so;
     uint32_t* mol = P.mol + (size_t)chain * C.max_mol * NS;
     uint32_t* msp = P.msp + (size_t)chain * C.max_mol;
@@ -603,6 +636,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
                         sph[e] = make_float4(x.hi, y.hi, z.hi, 0.f);
                         spl[e] = make_float4(x.lo, y.lo, z.lo, 0.f);
+                        if constexpr (FX) sfq[e] = fixed_frac(C.L, p[0], p[1], p[2]);
                     }
                 }
             } else {
@@ -670,15 +704,18 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         for (int x = 0; x < NS; ++x) skip |= (S.ex[x] == (uint32_t)j);
                     if (skip) continue;
                     float4 ah, al;
+                    uint4 aq = make_uint4(0u, 0u, 0u, 0u);
                     uint32_t ta;
                     if (j < C.n_fw) {
                         ah = P.fwh[j];
                         al = P.fwl[j];
+                        if constexpr (FX) aq = P.fwq[j];
                         ta = P.fw_type[j];
                     } else {
                         const uint64_t g = j - C.n_fw;
                         ah = ghi[g];
                         al = glo[g];
+                        if constexpr (FX) aq = gq4[g];
                         ta = gt[g];
                     }
                     const float qa = ah.w;
@@ -686,19 +723,39 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     for (int e = 0; e < 2 * NS; ++e) {
                         const bool is_old = e < NS;
                         if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
-                        const int s = is_old ? e : e - NS;
-                        const float4 ph = sph[e], pl = spl[e];
-                        ff dx = ff_add(ff{ah.x, al.x}, ff{-ph.x, -pl.x});
-                        ff dy = ff_add(ff{ah.y, al.y}, ff{-ph.y, -pl.y});
-                        ff dz = ff_add(ff{ah.z, al.z}, ff{-ph.z, -pl.z});
-                        ff_min_image(C.lh, C.ll, C.linv, C.L.ortho, dx, dy, dz);
-                        const float r2 = fmaf(dx.hi, dx.hi, fmaf(dy.hi, dy.hi, dz.hi * dz.hi));
+                        // large cells: the wrapped fractional displacement, exact in
+                        // fixed point, to Cartesian in FP32 (~2e-7 relative); pairs
+                        // within NEAR_R (and cutoff-ambiguous ones under plain
+                        // truncation) in double-float, the rest on that displacement
+                        float cx = 0.f, cy = 0.f, cz = 0.f, r2 = 0.f;
+                        bool near = true;
+                        if constexpr (FX) {
+                            const uint4 pq = sfq[e];
+                            const float fx = (float)(int32_t)(aq.x - pq.x) * 2.3283064365386963e-10f;
+                            const float fy = (float)(int32_t)(aq.y - pq.y) * 2.3283064365386963e-10f;
+                            const float fz = (float)(int32_t)(aq.z - pq.z) * 2.3283064365386963e-10f;
+                            cx = fmaf(fx, C.lh[0], fmaf(fy, C.lh[3], fz * C.lh[6]));
+                            cy = fmaf(fx, C.lh[1], fmaf(fy, C.lh[4], fz * C.lh[7]));
+                            cz = fmaf(fx, C.lh[2], fmaf(fy, C.lh[5], fz * C.lh[8]));
+                            r2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+                            near = r2 < NEAR_R2 ||
+                                   (C.trunc == ALEA_TRUNCATED && fabsf(r2 - rc2f) <= CUT_BAND * rc2f);
+                        }
+                        ff dx{cx, 0.f}, dy{cy, 0.f}, dz{cz, 0.f};
+                        if (near) {
+                            const float4 ph = sph[e], pl = spl[e];
+                            dx = ff_add(ff{ah.x, al.x}, ff{-ph.x, -pl.x});
+                            dy = ff_add(ff{ah.y, al.y}, ff{-ph.y, -pl.y});
+                            dz = ff_add(ff{ah.z, al.z}, ff{-ph.z, -pl.z});
+                            ff_min_image(C.lh, C.ll, C.linv, C.L.ortho, dx, dy, dz);
+                            r2 = fmaf(dx.hi, dx.hi, fmaf(dy.hi, dy.hi, dz.hi * dz.hi));
+                        }
                         const bool lj_in = !(C.grid && j < C.n_fw) && r2 <= rc2f;
                         const bool el_in = C.charged && r2 <= rce2f;
                         if (!lj_in && !el_in) continue;
                         if (lj_in) {
                             const PairF32 q = srow32[S.row_slot[e]][ta];
-                            if (r2 < q.sig2) {
+                            if (r2 < q.sig2) {  // r < sigma: only ever a near pair
                                 const ff rr = ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
                                 closef[e] = ff_add(closef[e], lj_close_ff(srowff[S.row_slot[e]][ta], rr, rcf, C.trunc));
                             } else {
@@ -989,6 +1046,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                                 gt[ds] = gt[ls];
                                 ghi[ds] = ghi[ls];
                                 glo[ds] = glo[ls];
+                                gq4[ds] = gq4[ls];
                                 for (uint64_t m = 0; m < c.n_mol; ++m) {
                                     const int nsm = C.sp_ns[msp[m]];
                                     for (int s2 = 0; s2 < nsm; ++s2)
@@ -1009,7 +1067,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                             gz[slot] = S.np_[s][2];
                             gq[slot] = S.sq_slot[NS + s];
                             gt[slot] = C.splj[S.sp_new][s];
-                            put_hilo(ghi, glo, slot, S.np_[s], S.sq_slot[NS + s]);
+                            put_hilo(C.L, ghi, glo, gq4, slot, S.np_[s], S.sq_slot[NS + s]);
                             mol[(size_t)mrec * NS + s] = (uint32_t)C.n_fw + slot;
                         }
                         msp[mrec] = (uint32_t)S.sp_new;
@@ -1021,7 +1079,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                             gx[slot] = S.np_[s][0];
                             gy[slot] = S.np_[s][1];
                             gz[slot] = S.np_[s][2];
-                            put_hilo(ghi, glo, slot, S.np_[s], S.sq_slot[NS + s]);
+                            put_hilo(C.L, ghi, glo, gq4, slot, S.np_[s], S.sq_slot[NS + s]);
                         }
                     } else if (S.move == 2) {
                         append_new(c.n_mol);
@@ -1156,13 +1214,13 @@ void launch_chains(unsigned n_chains, const GcmcConst& C, const GcmcPtrs& P, uin
                    cudaStream_t s) {
     const size_t bytes = C.charged ? phase_bytes<NS>(C.kmax, C.f32 != 0) : 0;
     if (C.f32) {
-        ALEA_CUDA(cudaFuncSetAttribute(gcmc_kernel<NS, true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-        gcmc_kernel<NS, true><<<n_chains, GT, bytes, s>>>(C, P, steps);
+        auto kern = C.fixed_far ? gcmc_kernel<NS, true, true> : gcmc_kernel<NS, true, false>;
+        ALEA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        kern<<<n_chains, GT, bytes, s>>>(C, P, steps);
     } else {
-        ALEA_CUDA(cudaFuncSetAttribute(gcmc_kernel<NS, false>,
+        ALEA_CUDA(cudaFuncSetAttribute(gcmc_kernel<NS, false, false>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-        gcmc_kernel<NS, false><<<n_chains, GT, bytes, s>>>(C, P, steps);
+        gcmc_kernel<NS, false, false><<<n_chains, GT, bytes, s>>>(C, P, steps);
     }
 }
 
@@ -1219,6 +1277,7 @@ struct GcmcImpl {
     DevBuf<unsigned> flags;
     DevBuf<double> pcdf, plogp;  // the chains' copy of a tabulated proposal
     DevBuf<float4> fwh, fwl, ghi, glo;  // FP32 form: double-float positions
+    DevBuf<uint4> fwq, gq4;             // FP32 form: fixed-point fractional positions
     DevBuf<uint32_t> msp;               // species of each molecule, per chain
     DevBuf<float> w32;                  // FP32 form: the weights
     DevBuf<float2> sk_hi, sk_lo;        // FP32 form: each chain's S(k) as double-float
@@ -1364,6 +1423,12 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
             g->fwl.alloc(std::max<size_t>(fw.n, 1));
             g->fwh.upload(h.data(), fw.n);
             g->fwl.upload(l.data(), fw.n);
+            std::vector<uint4> fq(fw.n);
+            for (uint64_t i = 0; i < fw.n; ++i)
+                fq[i] = fixed_frac(C.L, packed[i].x, packed[i].y, packed[i].z);
+            g->fwq.alloc(std::max<size_t>(fw.n, 1));
+            g->fwq.upload(fq.data(), fw.n);
+            C.fixed_far = std::fabs(C.L.volume) > FIXED_FAR_VOLUME;
             for (int i = 0; i < 9; ++i) {
                 const ff m = ff_from(C.L.m[i]);
                 C.lh[i] = m.hi;
@@ -1426,6 +1491,7 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         g->mol.alloc(sites);
         g->ghi.alloc(sites);
         g->glo.alloc(sites);
+        g->gq4.alloc(sites);
         g->msp.alloc((size_t)max_molecules * n_chains);
         std::vector<ChainState> st(n_chains);
         const double self0 = ews ? ewald_state_view(ews).self_pref * fwq2 : 0.0;
@@ -1483,6 +1549,8 @@ void gcmc_run(GcmcImpl* g, uint64_t steps, cudaStream_t s) {
     P.fwh = g->fwh.p;
     P.fwl = g->fwl.p;
     P.ghi = g->ghi.p;
+    P.gq4 = g->gq4.p;
+    P.fwq = g->fwq.p;
     P.glo = g->glo.p;
     P.w32 = g->w32.p;
     for (int r = 0; r < MAXROWS; ++r) P.gtab[r] = g->gtab[r];

@@ -155,3 +155,46 @@ def test_fp32_mixture_loading_matches_fp64(lib, orc):
         se = np.hypot(m64.std(ddof=1), m32.std(ddof=1)) / np.sqrt(n)
         assert m64.mean() > 0.5, (k, m64.mean())
         assert abs(m32.mean() - m64.mean()) <= 3 * se, (k, m32.mean(), m64.mean(), se)
+
+
+def test_fp32_far_pairs_in_fixed_point_large_cell(lib, orc):
+    """A cell above 100 x the 6 A near sphere (the 2x2x2 triclinic supercell,
+    3 376 charged atoms): far pairs take the fixed-point FP32 displacement,
+    near ones double-float. Move energies as in the small-cell test: insertion
+    and deletion dU within 1e-5 x max(kT, |dU|) of the FP64 form."""
+    A, _ = lib
+    fw = W.triclinic_supercell(reps=2)
+    assert abs(np.linalg.det(np.asarray(fw.lattice))) > 100 * 4 / 3 * np.pi * 6 ** 3
+    fw.charge = fw.charge * 0.15
+    alpha, _ = W.ewald_parameters(fw.lattice, 12.0)
+    ew = A.Ewald(alpha, 12.0, 8)
+    fug = orc.pr_fugacity(*W.CO2_CRITICAL, KT, 1e6)
+    guest = W.co2_guest(fw)
+    c64 = _chains(A, fw, guest, ew, [fug], [5], [3], A.FP64)
+    c32 = _chains(A, fw, guest, ew, [fug], [5], [3], A.FP32)
+    compared = {0: 0, 1: 0, 2: 0, 3: 0}
+    e_scale = 0.0
+    prev = c64.info()["attempted"]
+    for _ in range(900):
+        c64.run(1)
+        c32.run(1)
+        i64, i32 = c64.info(), c32.info()
+        if i64["call_index"] != i32["call_index"] or i64["molecules"] != i32["molecules"]:
+            break
+        step = np.array(i64["attempted"]) - np.array(prev)
+        prev = i64["attempted"]
+        if step.sum() == 0:
+            continue
+        move = int(np.argmax(step))
+        if i64["attempted"] == i32["attempted"] and np.isfinite(i64["last_du"]):
+            d64, d32 = i64["last_du"], i32["last_du"]
+            if abs(d64) > 1e5:
+                continue
+            if move >= 2:
+                e_scale = max(e_scale, abs(d64))
+                assert abs(d32 - d64) <= 1e-5 * max(KT, abs(d64)), (move, d32, d64)
+            else:
+                assert abs(d32 - d64) <= 1e-5 * max(KT, abs(d64), e_scale), (move, d32, d64, e_scale)
+            compared[move] += 1
+    assert sum(compared.values()) >= 150, compared
+    assert compared[2] >= 20, compared
