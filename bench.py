@@ -69,6 +69,23 @@ def _dist():
     return ws, rank
 
 
+def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
+    """The slowest rank's figure (every rank gets it): the replicas' job ends
+    when the last one does. dist is None for one process."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world: int, units_per_step: float, steps: int, seconds: float) -> float:
+    """Whole-job throughput of `world` independent replicas, each doing
+    units_per_step per step, timed by the slowest one."""
+    return world * units_per_step * steps / seconds
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -275,13 +292,9 @@ def main():
     kernel_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     step_ms = float(np.mean(kernel_ms))
     st = grid.stats()
-    total_ms = float(np.sum(kernel_ms))
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(np.sum(kernel_ms)), dist)
     pairs_step = st["algorithmic_pairs"]
-    value = ws * pairs_step * args.steps / (total_ms * 1e-3)
+    value = replica_value(ws, pairs_step, args.steps, total_ms * 1e-3)
 
     # e2e through the public call with host buffers (pinned host output)
     nodes = st["nodes"]
@@ -302,12 +315,8 @@ def main():
     for _ in range(e2e_steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = ws * pairs_step * e2e_steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e_value = replica_value(ws, pairs_step, e2e_steps, e2e_s)
 
     if rank == 0:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
