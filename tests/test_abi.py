@@ -159,3 +159,28 @@ def test_peng_robinson_mixture(so):
     for args, msg in bad:
         with pytest.raises(ValueError, match=msg):
             A.peng_robinson_mixture(*args)
+
+
+def test_build_to_host_checks_before_device(so):
+    """alea_grid_build_to_host: a null host array and the grid's own argument
+    errors are reported before any device work; without a GPU a valid call
+    reports ALEA_ERR_NO_DEVICE rather than building anything on the host."""
+    import ctypes
+    import torch
+    import aleator_gb300 as A
+
+    fw = _fw()
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    with pytest.raises(ValueError, match="host_tables"):
+        A.FrameworkEnergyGrid.build_to_host(ff, p, fw.lattice, [4], 2.0, A.FP32, [0])
+    buf = np.zeros(10)
+    with pytest.raises(ValueError, match="spacingAngstrom must be positive"):
+        A.FrameworkEnergyGrid.build_to_host(ff, p, fw.lattice, [4], -1.0, A.FP32,
+                                            [buf.ctypes.data])
+    if not torch.cuda.is_available():
+        with pytest.raises(A.AleatorError) as e:
+            A.FrameworkEnergyGrid.build_to_host(ff, p, fw.lattice, [4], 2.0, A.FP32,
+                                                [buf.ctypes.data], keep=False)
+        assert e.value.status == 5
+        assert not buf.any()
