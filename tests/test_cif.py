@@ -33,9 +33,9 @@ def A():
 def _same(s, r):
     assert np.array_equal(s.lattice, r["lattice"])
     for k in ("x", "y", "z", "charge", "species"):
-        assert np.array_equal(getattr(s.particles, k), r[k]), k
+        assert np.array_equal(getattr(s.particles, k), r[k], equal_nan=k != "species"), k
     assert np.array_equal(s.mass, r["mass"])
-    assert np.array_equal(s.occupancy, r["occupancy"])
+    assert np.array_equal(s.occupancy, r["occupancy"], equal_nan=True)
     assert list(s.species_symbols) == [str(v) for v in r["symbols"]]
     assert list(s.source_label) == [str(v) for v in r["labels"]]
 
@@ -90,3 +90,77 @@ def test_reference_structures_read_identically(A, ref):
         pytest.skip("the reference's structure files are not present")
     for f in files:
         _same(A.read_cif(f), ref.read_cif(f))
+
+
+def _cif_text(ops, coords, cell=("10.0", "11.0", "12.0", "90", "95.5", "100")):
+    lines = ["data_fuzz",
+             f"_cell_length_a {cell[0]}", f"_cell_length_b {cell[1]}", f"_cell_length_c {cell[2]}",
+             f"_cell_angle_alpha {cell[3]}", f"_cell_angle_beta {cell[4]}",
+             f"_cell_angle_gamma {cell[5]}", "loop_", "_symmetry_equiv_pos_as_xyz"]
+    lines += [f"'{op}'" for op in ops]
+    lines += ["loop_", "_atom_site_label", "_atom_site_fract_x", "_atom_site_fract_y",
+              "_atom_site_fract_z", "_atom_site_charge"]
+    for i, (x, y, z, q) in enumerate(coords):
+        lines.append(f"C{i} {x} {y} {z} {q}")
+    return "\n".join(lines) + "\n"
+
+
+def test_reader_fuzzed_against_reference(A, ref, tmp_path):
+    """Generated symmetry operations (signed terms, fractions, decimals, stray
+    characters) and coordinate tokens (esd suffixes, placeholders, exponents,
+    garbage): the library and the reference read the same particles or fail
+    with the same message. One pass draws from the valid grammar (most files
+    parse, so the particles are compared), one from anything."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    def ops_of(signs, numbers, variables, sizes):
+        term = st.builds(lambda a, b, c: a + b + c, st.sampled_from(signs), st.sampled_from(numbers),
+                         st.sampled_from(variables))
+        comp = st.lists(term, min_size=1, max_size=3).map("".join)
+        return st.lists(st.lists(comp, min_size=sizes[0], max_size=sizes[1]).map(",".join),
+                        min_size=1, max_size=4)
+
+    valid_ops = ops_of(["", "+", "-"], ["", "1", "1/2", "1/3", "2/3", "0.5", "3/4"],
+                       ["x", "y", "z", "X"], (3, 3))
+    any_ops = ops_of(["", "+", "-"], ["", "1", "2", "1/2", "0.5", "1/", ".25", "3/"],
+                     ["x", "y", "z", "", "w", "Y"], (1, 4))
+    valid_num = st.sampled_from(["0.1", "0.25(3)", "1e-3", ".5", "5.", "-0.75", "1.5", "0.333333",
+                                 "0.0", "1.0", "2(1)"])
+    any_num = st.sampled_from(["0.1", "?", ".", "abc", "nan", "1e400", "0.2(", "-"])
+    case = {"n": 0, "ok": 0}
+
+    def compare(ops, coords):
+        case["n"] += 1
+        f = tmp_path / f"f{case['n']}.cif"
+        f.write_text(_cif_text(ops, coords))
+        try:
+            r, rerr = ref.read_cif(f), None
+        except RuntimeError as e:
+            r, rerr = None, str(e)
+        try:
+            s, serr = A.read_cif(f), None
+        except RuntimeError as e:
+            s, serr = None, str(e)
+        assert rerr == serr, (ops, coords, rerr, serr)
+        if r is not None:
+            _same(s, r)
+            case["ok"] += 1
+
+    settings = hyp.settings(max_examples=150, deadline=None, database=None, derandomize=True)
+
+    @settings
+    @hyp.given(ops=valid_ops, coords=st.lists(st.tuples(valid_num, valid_num, valid_num, valid_num),
+                                              min_size=1, max_size=3))
+    def valid(ops, coords):
+        compare(ops, coords)
+
+    @settings
+    @hyp.given(ops=any_ops, coords=st.lists(st.tuples(any_num, valid_num, any_num, any_num),
+                                            min_size=1, max_size=3))
+    def anything(ops, coords):
+        compare(ops, coords)
+
+    valid()
+    assert case["ok"] >= 100, case  # the valid grammar parses: particles compared
+    anything()
