@@ -164,3 +164,58 @@ def test_reader_fuzzed_against_reference(A, ref, tmp_path):
     valid()
     assert case["ok"] >= 100, case  # the valid grammar parses: particles compared
     anything()
+
+
+def test_document_grammar_fuzzed_against_reference(A, ref, tmp_path):
+    """Random constructs between the sections of a valid file: comments, blank
+    lines, tags with bare, quoted and text-field values, extra loops whose rows
+    span lines (or fall short), unterminated quotes and text fields, stray
+    words, a second data block. Same particles or the same message (with the
+    same line number) from both readers."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    noise = st.sampled_from([
+        "# a comment line", "", "   ", "\t# indented comment",
+        "_extra_tag value", "_extra_tag 'two words'", '_extra_tag "it\'s quoted"',
+        "_extra_tag\n;\nfree text\nover lines\n;", "_extra_tag\n; one-liner\n;",
+        "_extra_tag\nnext_line_value", "_UPPER_Tag 3.5(2)",
+        "loop_\n_l_a\n_l_b\n1 2\n3\n4", "loop_\n_l_a\n_l_b\n'x y' \"z\"\n# c\n5 6",
+        "loop_\n_l_a\n_l_b\n1 2 3",                      # a short row
+        "loop_\n# no columns", "_bad_tag 'unterminated", "_text\n; never closed",
+        "stray words here", "data_second\n_cell_length_a 1", "_tag_at_end",
+    ])
+    head = ["data_grammar", "_cell_length_a 9.5", "_cell_length_b 10.5", "_cell_length_c 11.5",
+            "_cell_angle_alpha 88", "_cell_angle_beta 92", "_cell_angle_gamma 101"]
+    sym = ["loop_", "_symmetry_equiv_pos_as_xyz", "'x,y,z'", "'-x,-y,-z'"]
+    atoms = ["loop_", "_atom_site_label", "_atom_site_type_symbol", "_atom_site_fract_x",
+             "_atom_site_fract_y", "_atom_site_fract_z", "O1 O 0.1 0.2 0.3", "Si1 Si 0.5 0.5",
+             "0.5", "C2 C 0.0 0.0 0.0"]
+    sections = [head, sym, atoms]
+    case = {"n": 0, "ok": 0}
+
+    @hyp.settings(max_examples=200, deadline=None, database=None, derandomize=True)
+    @hyp.given(inserts=st.lists(st.lists(noise, max_size=2), min_size=4, max_size=4))
+    def check(inserts):
+        case["n"] += 1
+        parts = []
+        for k in range(3):
+            parts += inserts[k]
+            parts += sections[k]
+        parts += inserts[3]
+        f = tmp_path / f"g{case['n']}.cif"
+        f.write_text("\n".join(parts) + "\n")
+        try:
+            r, rerr = ref.read_cif(f), None
+        except RuntimeError as e:
+            r, rerr = None, str(e)
+        try:
+            s, serr = A.read_cif(f), None
+        except RuntimeError as e:
+            s, serr = None, str(e)
+        assert rerr == serr, (inserts, rerr, serr)
+        if r is not None:
+            _same(s, r)
+            case["ok"] += 1
+
+    check()
+    assert case["ok"] >= 30, case
