@@ -144,3 +144,45 @@ def test_mixture_with_grid_bit_identical_to_reference(ref, orc):
         assert np.array_equal(a.positions(), b.positions())
         assert a.ewald_energy() == b.ewald_energy()
     assert a.molecules() > 0
+
+
+def test_peng_robinson_mixture_fuzzed_against_reference(ref):
+    """Random substances (2-4), compositions, temperatures, pressures and k_ij:
+    the library's Z and partial fugacities equal the reference's bit for bit,
+    or both reject the input with the same message."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    import aleator_gb300 as A
+    from aleator_gb300.build import LIB, build
+
+    if not LIB.exists():
+        build()
+    sub = st.tuples(st.floats(80.0, 700.0), st.floats(1e6, 8e6), st.floats(-0.2, 0.6))
+
+    @hyp.settings(max_examples=200, deadline=None, database=None, derandomize=True)
+    @hyp.given(subs=st.lists(sub, min_size=2, max_size=4), t=st.floats(150.0, 600.0),
+               p=st.sampled_from([1.0, 1e3, 1e5, 1e6, 5e6, 2e7]),
+               w=st.lists(st.floats(0.0, 1.0), min_size=4, max_size=4), k=st.floats(-0.1, 0.2),
+               use_k=st.booleans())
+    def check(subs, t, p, w, k, use_k):
+        n = len(subs)
+        tot = sum(w[:n]) or 1.0
+        x = [v / tot for v in w[:n]]
+        kij = None
+        if use_k:
+            kij = [[0.0 if i == j else k for j in range(n)] for i in range(n)]
+        try:
+            zr, fr = ref.pr_mixture(subs, t, p, x, kij)
+            rerr = None
+        except ValueError as e:
+            rerr = str(e)
+        try:
+            zs, fs = A.peng_robinson_mixture(subs, t, p, x, kij)
+            serr = None
+        except (ValueError, RuntimeError) as e:
+            serr = str(e)
+        assert rerr == serr, (subs, t, p, x, kij, rerr, serr)
+        if rerr is None:
+            assert zs == zr and np.array_equal(fs, fr)
+
+    check()
