@@ -186,3 +186,55 @@ def test_peng_robinson_mixture_fuzzed_against_reference(ref):
             assert zs == zr and np.array_equal(fs, fr)
 
     check()
+
+
+def test_gcmc_oracle_fuzzed_against_reference(ref, orc):
+    """Random engines: seed and stream, pressure, CH4 / CO2 / their mixture,
+    charged or not, with or without the energy grid. The oracle's trajectory is
+    the reference engine's, bit for bit (positions, counts, Ewald energy)."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    fw = W.cubic_framework(seed=31, charged=True)
+    fw.charge = fw.charge * 0.15
+    ff = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.8, truncation=O.SHIFTED)
+    ew = dict(alpha=0.31, rc=12.0, kmax=4)
+    spacing = 1.0
+    all_species = sorted({int(s) for g in (W.co2_guest(fw), W.ch4_guest(fw)) for s in g["lj_species"]})
+    tables = {s: orc.grid_build(ff, fw.lattice, fw.x, fw.y, fw.z, fw.species, s, spacing, threads=8)
+              for s in all_species}
+    counts = orc.grid_point_counts(fw.lattice, spacing)
+
+    @hyp.settings(max_examples=12, deadline=None, database=None, derandomize=True)
+    @hyp.given(seed=st.integers(0, 2 ** 40), stream=st.integers(0, 1000),
+               bar=st.sampled_from([0.5, 5.0, 30.0]), kind=st.sampled_from(["ch4", "co2", "mix"]),
+               charged=st.booleans(), grid=st.booleans())
+    def check(seed, stream, bar, kind, charged, grid):
+        co2 = W.co2_guest(fw) if charged else dict(W.co2_guest(fw), charge=[0.0, 0.0, 0.0])
+        guests = {"ch4": [W.ch4_guest(fw)], "co2": [co2], "mix": [co2, W.ch4_guest(fw)]}[kind]
+        crit = {"ch4": [W.METHANE_CRITICAL], "co2": [W.CO2_CRITICAL],
+                "mix": [W.CO2_CRITICAL, W.METHANE_CRITICAL]}[kind]
+        fugs = [ref.pr_fugacity(*c, 298.0, bar * 1e5) for c in crit]
+        ewd = ew if charged else None
+        species = sorted({int(s) for g in guests for s in g["lj_species"]})
+        rg = {"spacing": spacing, "species": species} if grid else None
+        og = {"counts": counts, "tables": {s: tables[s] for s in species}} if grid else None
+        if kind == "mix":
+            a = ref.gcmc_mixture(ff, ewd, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guests,
+                                 298.0, fugs, seed, stream, grid=rg)
+            b = orc.gcmc_mixture(ff, ewd, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guests,
+                                 298.0, fugs, seed, stream, grid=og)
+        else:
+            a = ref.gcmc(ff, ewd, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guests[0], 298.0,
+                         fugs[0], seed, stream, grid=rg)
+            b = orc.gcmc(ff, ewd, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, guests[0], 298.0,
+                         fugs[0], seed, stream, grid=og)
+        for _ in range(2):
+            a.run(250)
+            b.run(250)
+            assert a.molecules() == b.molecules()
+            assert np.array_equal(a.positions(), b.positions())
+            assert a.ewald_energy() == b.ewald_energy()
+        if kind == "mix":
+            assert [a.molecules_of(k) for k in range(2)] == [b.molecules_of(k) for k in range(2)]
+
+    check()
