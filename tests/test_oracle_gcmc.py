@@ -238,3 +238,33 @@ def test_gcmc_oracle_fuzzed_against_reference(ref, orc):
             assert [a.molecules_of(k) for k in range(2)] == [b.molecules_of(k) for k in range(2)]
 
     check()
+
+
+def test_widom_oracle_fuzzed_against_reference(ref, orc):
+    """Random Widom runs (seed, stream, CH4 or CO2, charged or not, cubic or
+    triclinic cell, every truncation): the oracle's per-trial energies and K_H
+    equal the reference engine's."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    cells = {"cubic": W.cubic_framework(seed=41, charged=True),
+             "triclinic": W.triclinic_supercell(reps=1)}
+
+    @hyp.settings(max_examples=12, deadline=None, database=None, derandomize=True)
+    @hyp.given(seed=st.integers(0, 2 ** 40), stream=st.integers(0, 1000),
+               co2=st.booleans(), charged=st.booleans(), cell=st.sampled_from(["cubic", "triclinic"]),
+               trunc=st.sampled_from([O.TRUNCATED, O.SHIFTED, O.LINEAR_FORCE_SHIFTED]))
+    def check(seed, stream, co2, charged, cell, trunc):
+        fw = cells[cell]
+        rc = 12.8 if cell == "cubic" else 10.0
+        ff = dict(eps=fw.eps, sigma=fw.sigma, cutoff=rc, truncation=trunc)
+        ew = dict(alpha=0.33, rc=min(rc, 10.0), kmax=4) if charged else None
+        guest = W.co2_guest(fw) if co2 else W.ch4_guest(fw)
+        q = fw.charge if charged else None
+        kr, pr = ref.widom(ff, ew, fw.lattice, fw.x, fw.y, fw.z, q, fw.species, guest, 298.0, seed,
+                           stream, 150, per_trial=True)
+        ko, po = orc.widom(ff, ew, fw.lattice, fw.x, fw.y, fw.z, q, fw.species, guest, 298.0, seed,
+                           stream, 150, per_trial=True)
+        assert np.array_equal(pr, po)
+        assert kr[0] == ko
+
+    check()
