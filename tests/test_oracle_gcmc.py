@@ -268,3 +268,28 @@ def test_widom_oracle_fuzzed_against_reference(ref, orc):
         assert kr[0] == ko
 
     check()
+
+
+def test_grid_oracle_fuzzed_against_reference(ref, orc, tmp_path):
+    """Random triclinic frameworks (50-300 atoms, replicated to fit the cutoff),
+    spacings and truncations: the oracle's grid tables equal the reference's
+    FrameworkEnergyGrid (read back from its own cache file) node for node."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    from test_oracle_golden import _cache_tables
+
+    @hyp.settings(max_examples=6, deadline=None, database=None, derandomize=True)
+    @hyp.given(seed=st.integers(1, 10 ** 6), spacing=st.sampled_from([1.7, 2.3, 3.1]),
+               trunc=st.sampled_from([O.TRUNCATED, O.SHIFTED, O.LINEAR_FORCE_SHIFTED]))
+    def check(seed, spacing, trunc):
+        fw = W.random_triclinic_frameworks(1, seed=seed, cutoff=9.0, max_atoms=300)[0]
+        ff = dict(eps=fw.eps, sigma=fw.sigma, cutoff=9.0, truncation=trunc)
+        guest = fw.guest_species["CH4"]
+        g = ref.grid(ff, fw.lattice, fw.x, fw.y, fw.z, fw.species, [guest], spacing)
+        f = tmp_path / f"g{seed}.bin"
+        g.serialize(f)
+        _, tables = _cache_tables(np.frombuffer(f.read_bytes(), np.uint8))
+        mine = orc.grid_build(ff, fw.lattice, fw.x, fw.y, fw.z, fw.species, guest, spacing, threads=8)
+        assert np.array_equal(mine, tables[guest])
+
+    check()
