@@ -184,3 +184,60 @@ def test_build_to_host_checks_before_device(so):
                                                 [buf.ctypes.data], keep=False)
         assert e.value.status == 5
         assert not buf.any()
+
+
+C_PROGRAM = r"""
+#include <stdio.h>
+#include "aleator_gb300.h"
+int main(int argc, char** argv) {
+    alea_structure* s = NULL;
+    if (argc < 2 || alea_read_cif(argv[1], &s) != ALEA_OK) return 2;
+    uint64_t n = 0; uint32_t ns = 0;
+    alea_structure_sizes(s, &n, &ns);
+    double m[9];
+    alea_structure_lattice(s, m);
+    char sym[16];
+    alea_structure_species_symbol(s, 0, sym, sizeof sym);
+    alea_structure_destroy(s);
+    const double tc[2] = {304.1282, 190.564}, pc[2] = {7.3773e6, 4.5992e6}, om[2] = {0.22394, 0.01142};
+    const double x[2] = {0.4, 0.6};
+    double z = 0.0, f[2];
+    if (alea_peng_robinson_mixture(2, tc, pc, om, NULL, 298.0, 1e6, x, &z, f) != ALEA_OK) return 3;
+    char msg[256];
+    int bad = alea_read_cif("does/not/exist.cif", &s) == ALEA_ERR_RUNTIME;
+    alea_last_error(msg, sizeof msg);
+    printf("%llu %u %.3f %s %.6f %d %s\n", (unsigned long long)n, ns, m[0], sym, z, bad, msg);
+    return 0;
+}
+"""
+
+
+def test_plain_c_program_links_and_runs(so, tmp_path):
+    """The header is C (C99, -pedantic) and a C program linked against the
+    library runs its host entry points: the CIF reader, the Peng-Robinson
+    mixture and the error channel."""
+    import shutil
+    import aleator_gb300 as A
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "prog.c"
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "prog"
+    libdir = str(Path(so).parent)
+    inc = str(Path(__file__).resolve().parents[1] / "include")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", inc,
+                        str(src), "-o", str(exe), "-L", libdir, "-laleator_gb300",
+                        f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    cif = Path(__file__).resolve().parent / "golden" / "cif" / "triclinic_symops.cif"
+    out = subprocess.run([str(exe), str(cif)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    n, ns, a, sym, z, bad, *msg = out.stdout.split()
+    s = A.read_cif(cif)
+    assert int(n) == len(s.particles) and int(ns) == len(s.species_symbols) and sym == "Cu"
+    assert float(a) == pytest.approx(9.10)
+    z_py, _ = A.peng_robinson_mixture([(304.1282, 7.3773e6, 0.22394), (190.564, 4.5992e6, 0.01142)],
+                                      298.0, 1e6, [0.4, 0.6])
+    assert float(z) == pytest.approx(z_py, abs=1e-6)
+    assert bad == "1" and "could not open file" in " ".join(msg)
