@@ -33,3 +33,29 @@ def test_ewald_parameters():
     fw = W.cubic_framework()
     alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
     assert abs(alpha - 0.3097) < 1e-3 and kmax == 10
+
+
+def test_random_triclinic_frameworks_shape():
+    """The screening set's frameworks. Base cells (a cutoff small enough that
+    nothing is replicated): a, b, c in 10-40 A, angles in 60-120 degrees, 50-2000
+    atoms (fewer only where 8 A^3 per atom caps a small cell), framework types
+    0-3 plus the CH4 probe. At the 12.8 A cutoff every perpendicular width
+    exceeds 2 rc after replication (the reference's buildSupercell rule). The same
+    seed gives the same frameworks."""
+    for fw in W.random_triclinic_frameworks(12, seed=77, cutoff=1.0):
+        m = np.asarray(fw.lattice)
+        lengths = np.linalg.norm(m, axis=1)
+        assert ((lengths >= 10.0) & (lengths <= 40.0)).all(), lengths
+        cos = [m[1] @ m[2] / (lengths[1] * lengths[2]), m[0] @ m[2] / (lengths[0] * lengths[2]),
+               m[0] @ m[1] / (lengths[0] * lengths[1])]
+        ang = np.degrees(np.arccos(cos))
+        assert ((ang >= 60 - 1e-9) & (ang <= 120 + 1e-9)).all(), ang
+        vol = abs(np.linalg.det(m))
+        assert min(50, int(vol / 8.0)) <= fw.n_atoms <= 2000
+        assert fw.species.max() <= 3 and fw.guest_species == {"CH4": 4}
+    fws = W.random_triclinic_frameworks(12, seed=77)
+    for fw in fws:
+        assert (W.perpendicular_widths(np.asarray(fw.lattice)) > 2 * 12.8).all()
+    again = W.random_triclinic_frameworks(12, seed=77)
+    assert all(np.array_equal(a.x, b.x) and np.array_equal(a.lattice, b.lattice)
+               for a, b in zip(fws, again))
