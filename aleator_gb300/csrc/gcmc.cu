@@ -1351,7 +1351,9 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
                 require(std::fabs(qs) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
                         "MonteCarloEngine: GCMC species " + std::to_string(k) +
                             " is not individually charge-neutral (total site charge = " +
-                            std::to_string(qs) + " e)");
+                            std::to_string(qs) +
+                            " e); every insertion/deletion/swap would drift the system away from "
+                            "neutrality, which electrostatics requires");
             // pairExclusionSum of the template (ewald_incremental_state.cc:32-43): a rigid
             // molecule's, wherever it is (its pairs are far shorter than half a cell)
             double ex = 0.0;
@@ -1402,7 +1404,8 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         if (ew) {
             // monte_carlo_engine.cc:273-293
             require(std::fabs(fwq) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
-                    "MonteCarloEngine: framework is not charge-neutral");
+                    "MonteCarloEngine: framework is not charge-neutral (total charge = " +
+                        std::to_string(fwq) + " e)");
             require(ew->kmax <= KMAXC, ALEA_ERR_INVALID_ARGUMENT, "GCMC: kMax <= 64 supported");
             validate_cutoff(C.L, ew->real_space_cutoff, "MonteCarloEngine (Ewald real space)");
         }

@@ -612,6 +612,20 @@ WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
         P.trunc = lj.truncation;
         P.temperature = temperature;
         w->precision = precision;
+        if (ew) {  // engine ctor checks (monte_carlo_engine.cc:273-293), before any device work
+            double qs = 0.0;
+            for (uint32_t s = 0; s < guest.n_sites; ++s) qs += guest.charge ? guest.charge[s] : 0.0;
+            require(std::fabs(qs) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
+                    "MonteCarloEngine: GCMC species 0 is not individually charge-neutral (total "
+                    "site charge = " + std::to_string(qs) +
+                        " e); every insertion/deletion/swap would drift the system away from "
+                        "neutrality, which electrostatics requires");
+            double qf = 0.0;
+            for (uint64_t i = 0; i < fw.n; ++i) qf += fw.charge ? fw.charge[i] : 0.0;
+            require(std::fabs(qf) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
+                    "MonteCarloEngine: framework is not charge-neutral (total charge = " +
+                        std::to_string(qf) + " e)");
+        }
         require_device();
         std::vector<double4> packed(fw.n);
         std::vector<uint32_t> types(fw.n, 0);
@@ -643,15 +657,6 @@ WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
         w->table.upload(table.data(), table.size());
         std::vector<KRow> rows;
         if (ew) {
-            // engine ctor checks (monte_carlo_engine.cc:273-293)
-            double qs = 0.0;
-            for (uint32_t s = 0; s < guest.n_sites; ++s) qs += guest.charge ? guest.charge[s] : 0.0;
-            require(std::fabs(qs) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
-                    "MonteCarloEngine: GCMC species 0 is not individually charge-neutral");
-            double qf = 0.0;
-            for (uint64_t i = 0; i < fw.n; ++i) qf += fw.charge ? fw.charge[i] : 0.0;
-            require(std::fabs(qf) <= 1e-8, ALEA_ERR_INVALID_ARGUMENT,
-                    "MonteCarloEngine: framework is not charge-neutral");
             validate_cutoff(P.L, ew->real_space_cutoff, "MonteCarloEngine (Ewald real space)");
             w->ews = ewald_state_create(*ew, fw, lat);
             const EwaldDeviceView v = ewald_state_view(w->ews);

@@ -241,3 +241,39 @@ def test_plain_c_program_links_and_runs(so, tmp_path):
                                       298.0, 1e6, [0.4, 0.6])
     assert float(z) == pytest.approx(z_py, abs=1e-6)
     assert bad == "1" and "could not open file" in " ".join(msg)
+
+
+def test_neutrality_errors_match_reference_text(so):
+    """The engine constructor's neutrality checks (monte_carlo_engine.cc:273-293)
+    with the reference's message text, before any device work: a non-neutral
+    mixture species (GCMC), a non-neutral probe (Widom), a non-neutral framework."""
+    import aleator_gb300 as A
+    from aleator_gb300 import workloads as W
+
+    fw = W.cubic_framework(seed=5, charged=True)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    ew = A.Ewald(0.31, 12.0, 5)
+    bad = dict(W.co2_guest(fw), charge=[-0.35, 0.70, -0.30])  # +0.05 e
+    tail = ("; every insertion/deletion/swap would drift the system away from neutrality, which "
+            "electrostatics requires")
+    msg = "MonteCarloEngine: GCMC species 1 is not individually charge-neutral (total site charge = "
+    with pytest.raises(ValueError) as e:
+        A.GcmcChains(ff, p, fw.lattice, [W.ch4_guest(fw), bad], 298.0, [[1e5, 1e5]], [1], [1], ewald=ew)
+    qsum = 0.0
+    for c in bad["charge"]:  # summed in site order, formatted as std::to_string (%f)
+        qsum += c
+    assert str(e.value) == msg + f"{qsum:f} e)" + tail
+    with pytest.raises(ValueError) as e:
+        A.Widom(ff, p, fw.lattice, bad, 298.0, ewald=ew)
+    assert str(e.value).startswith("MonteCarloEngine: GCMC species 0 is not individually charge-neutral")
+    assert str(e.value).endswith(tail)
+    q = fw.charge.copy()
+    q[0] += 0.5
+    p2 = A.ParticleData(fw.x, fw.y, fw.z, q, fw.species)
+    for make in (lambda: A.Widom(ff, p2, fw.lattice, W.co2_guest(fw), 298.0, ewald=ew),
+                 lambda: A.GcmcChains(ff, p2, fw.lattice, W.co2_guest(fw), 298.0, [1e5], [1], [1],
+                                      ewald=ew)):
+        with pytest.raises(ValueError, match=r"^MonteCarloEngine: framework is not charge-neutral "
+                                             r"\(total charge = 0\.5\d* e\)$"):
+            make()
