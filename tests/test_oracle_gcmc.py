@@ -293,3 +293,52 @@ def test_grid_oracle_fuzzed_against_reference(ref, orc, tmp_path):
         assert np.array_equal(mine, tables[guest])
 
     check()
+
+
+def test_ewald_state_fuzzed_against_reference(ref, orc):
+    """Random propose/commit sequences on the EwaldIncrementalState (insertions,
+    deletions and moves of 1- to 3-site molecules at random charges, proposals
+    left uncommitted, cubic or triclinic cell, random alpha and kMax): the
+    oracle's deltas, energies and raw S(k) equal the reference's."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    cells = {"cubic": W.cubic_framework(seed=51, charged=True), "triclinic": W.triclinic_supercell(reps=1)}
+
+    @hyp.settings(max_examples=10, deadline=None, database=None, derandomize=True)
+    @hyp.given(seed=st.integers(0, 2 ** 31), cell=st.sampled_from(["cubic", "triclinic"]),
+               alpha=st.sampled_from([0.22, 0.3, 0.41]), kmax=st.integers(2, 6))
+    def check(seed, cell, alpha, kmax):
+        fw = cells[cell]
+        a = ref.ewald_state(fw.lattice, fw.x, fw.y, fw.z, fw.charge, alpha, kmax)
+        b = orc.ewald_state(fw.lattice, fw.x, fw.y, fw.z, fw.charge, alpha, kmax)
+        rng = np.random.default_rng(seed)
+        span = float(np.abs(np.asarray(fw.lattice)).sum(axis=0).max())
+        mols = []
+        for _ in range(40):
+            ns = int(rng.integers(1, 4))
+            q = rng.uniform(-1, 1, ns)
+            q -= q.mean()
+            new = np.column_stack([rng.uniform(-0.2 * span, 1.2 * span, (ns, 3)), q])
+            pick = rng.uniform()
+            if mols and pick < 0.35:
+                rem, add = mols[-1], np.zeros((0, 4))
+            elif mols and pick < 0.6:
+                rem = mols[-1]
+                add = rem.copy()
+                add[:, :3] += rng.uniform(-2, 2, 3)
+            else:
+                rem, add = np.zeros((0, 4)), new
+            assert a.propose(rem, add) == b.propose(rem, add)
+            if rng.uniform() < 0.7:
+                a.commit(rem, add)
+                b.commit(rem, add)
+                if len(rem) and len(add):
+                    mols[-1] = add
+                elif len(rem):
+                    mols.pop()
+                else:
+                    mols.append(add)
+            assert a.energy() == b.energy()
+        assert np.array_equal(a.raw(), b.raw())
+
+    check()
