@@ -107,6 +107,10 @@ _SIGNATURES = {
     "alea_version": (ctypes.c_int32, [_I32, _I32, _I32]),
     "alea_device_info": (ctypes.c_int32, [ctypes.c_char_p, ctypes.c_size_t, _I32, _I32, _I32]),
     "alea_probe_fp32_fma_tflops": (ctypes.c_int32, [_D]),
+    "alea_probe_fp32x2_fma_tflops": (ctypes.c_int32, [_D]),
+    "alea_cached_bytes": (ctypes.c_int32, [_U64]),
+    "alea_release_cached": (ctypes.c_int32, [_U64]),
+    "alea_test_block_cache": (ctypes.c_int32, []),
     "alea_philox4x32_10": (ctypes.c_int32, [_U32, _U32, _U32, ctypes.c_uint64]),
     "alea_philox_fill_u64": (ctypes.c_int32, [ctypes.c_uint64] * 4 + [_U64]),
     "alea_philox_fill_uniform": (ctypes.c_int32, [ctypes.c_uint64] * 4 + [_D]),
@@ -132,6 +136,10 @@ _SIGNATURES = {
                                                    ctypes.POINTER(_Lattice), _U32, ctypes.c_uint32,
                                                    ctypes.c_double, ctypes.c_char_p,
                                                    ctypes.c_size_t]),
+    "alea_test_grid_tile_wait_limit": (ctypes.c_int32, [ctypes.c_int64]),
+    "alea_grid_cache_hit": (ctypes.c_int32, [ctypes.c_char_p, ctypes.POINTER(_LJ),
+                                             ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
+                                             _U32, ctypes.c_uint32, ctypes.c_double, _I32]),
     "alea_grid_load_cache": (ctypes.c_int32, [ctypes.c_char_p, ctypes.POINTER(_LJ),
                                               ctypes.POINTER(_Particles), ctypes.POINTER(_Lattice),
                                               _U32, ctypes.c_uint32, ctypes.c_double,
@@ -404,10 +412,12 @@ def device_info():
     return {"name": name.value.decode(), "sm_count": sms.value, "cc": (ma.value, mi.value)}
 
 
-def fp32_fma_tflops():
-    """Sustained FP32 FFMA throughput measured on the current device."""
+def fp32_fma_tflops(packed: bool = False):
+    """Sustained FP32 FMA throughput measured on the current device: scalar
+    fmaf, or (packed=True) the two-lane fma.rn.f32x2 the grid sweep issues."""
     v = ctypes.c_double()
-    _check(library().alea_probe_fp32_fma_tflops(ctypes.byref(v)))
+    fn = library().alea_probe_fp32x2_fma_tflops if packed else library().alea_probe_fp32_fma_tflops
+    _check(fn(ctypes.byref(v)))
     return v.value
 
 
@@ -548,6 +558,36 @@ class FrameworkEnergyGrid:
         if not h:
             return None
         return cls(force_field, framework, lattice, g, spacing, _handle=h)
+
+    @staticmethod
+    def cache_hit(cache_dir, force_field, framework, lattice, guest_species_ids, spacing):
+        """cacheHit (framework_energy_grid.cc:326-352): True when the key's file
+        exists and matches, False when none is there; AleatorError (a
+        RuntimeError) when a file at that path has another version or key."""
+        g = np.ascontiguousarray(guest_species_ids, dtype=np.uint32)
+        lj = force_field.c()
+        p = framework.c()
+        lat = _lattice(lattice)
+        hit = ctypes.c_int32(0)
+        _check(library().alea_grid_cache_hit(str(cache_dir).encode(), ctypes.byref(lj),
+                                             ctypes.byref(p), ctypes.byref(lat), _u32p(g), len(g),
+                                             float(spacing), ctypes.byref(hit)))
+        return bool(hit.value)
+
+    @classmethod
+    def load_or_build(cls, cache_dir, force_field, framework, lattice, guest_species_ids,
+                      spacing, precision=FP64):
+        """loadOrBuildFrameworkEnergyGrid (framework_energy_grid.cc:411-435):
+        the cached grid when the key's file is there, else a fresh build written
+        to the cache. Returns (grid, was_hit)."""
+        grid = cls.load_from_cache(cache_dir, force_field, framework, lattice, guest_species_ids,
+                                   spacing)
+        if grid is not None:
+            return grid, True
+        grid = cls(force_field, framework, lattice, guest_species_ids, spacing, precision)
+        name = cls.cache_file_name(force_field, framework, lattice, guest_species_ids, spacing)
+        grid.serialize(os.path.join(str(cache_dir), name))
+        return grid, False
 
 
 # ---------------------------------------------------------------- LJ / Ewald free functions

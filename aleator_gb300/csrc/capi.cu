@@ -124,6 +124,51 @@ alea_status alea_device_info(char* name, size_t cap, int32_t* sm_count, int32_t*
     });
 }
 
+// ---------------------------------------------------------------- device block cache
+alea_status alea_cached_bytes(uint64_t* out) {
+    return guarded([&] {
+        need(out, "out");
+        *out = alea::dev_cached_bytes();
+    });
+}
+
+alea_status alea_release_cached(uint64_t* freed) {
+    return guarded([&] {
+        const size_t n = alea::dev_release_cached();
+        if (freed) *freed = n;
+    });
+}
+
+// Fake pointers only: the bookkeeping is checked without touching a device.
+alea_status alea_test_block_cache(void) {
+    return guarded([&] {
+        alea::KeptBlocks kb;
+        char a, b, c, d;
+        auto fail = [](const char* what) {
+            throw alea::Error(ALEA_ERR_RUNTIME, std::string("block cache keying: ") + what);
+        };
+        const size_t M = 64ull << 20, cap = 4 * M;
+        if (!kb.put(0, M, &a, cap) || !kb.put(1, M, &b, cap) || !kb.put(0, 2 * M, &c, cap))
+            fail("put under the cap refused");
+        if (kb.bytes() != 4 * M) fail("byte count after puts");
+        if (kb.put(1, M, &d, cap)) fail("put over the cap accepted");
+        if (kb.take(2, M) != nullptr) fail("a block handed to a device that never kept one");
+        if (kb.take(1, 2 * M) != nullptr) fail("a block of another device's size handed out");
+        if (kb.take(1, M) != &b) fail("device 1's block not returned to device 1");
+        if (kb.take(1, M) != nullptr) fail("device 1's block handed out twice");
+        if (kb.take(0, M) != &a) fail("device 0's block not returned to device 0");
+        if (kb.bytes() != 2 * M) fail("byte count after takes");
+        if (!kb.put(1, M, &d, cap)) fail("put after takes refused");
+        auto d0 = kb.drain(0);
+        if (d0.size() != 1 || d0[0].p != &c || d0[0].device != 0 || d0[0].bytes != 2 * M)
+            fail("drain of device 0");
+        if (kb.bytes() != M) fail("byte count after a device drain");
+        auto rest = kb.drain(-1);
+        if (rest.size() != 1 || rest[0].p != &d || rest[0].device != 1) fail("drain of all");
+        if (kb.bytes() != 0 || kb.take(1, M) != nullptr) fail("state after the full drain");
+    });
+}
+
 // ---------------------------------------------------------------- Philox
 alea_status alea_philox4x32_10(const uint32_t* ctr, const uint32_t* key, uint32_t* out, uint64_t n) {
     return guarded([&] {
@@ -411,6 +456,27 @@ alea_status alea_structure_source_label(const alea_structure* s, uint64_t atom, 
 
 alea_status alea_structure_destroy(alea_structure* s) {
     return guarded([&] { delete s; });
+}
+
+alea_status alea_test_grid_tile_wait_limit(int64_t limit) {
+    return guarded([&] { alea::grid_test_set_tile_wait_limit(limit); });
+}
+
+alea_status alea_grid_cache_hit(const char* cache_dir, const alea_lennard_jones* lj,
+                                const alea_particles* framework, const alea_lattice* lattice,
+                                const uint32_t* guest_species, uint32_t n_guest, double spacing,
+                                int32_t* hit) {
+    return guarded([&] {
+        need(cache_dir, "cache_dir");
+        need(lj, "lj");
+        need(lattice, "lattice");
+        need(hit, "hit");
+        if (n_guest) need(guest_species, "guest_species");
+        *hit = alea::grid_cache_hit(cache_dir, *lj, particles_or_empty(framework), *lattice,
+                                    guest_species, n_guest, spacing)
+                   ? 1
+                   : 0;
+    });
 }
 
 alea_status alea_grid_load_cache(const char* cache_dir, const alea_lennard_jones* lj,

@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <map>
+#include <vector>
 #include <mutex>
 #include <string>
 
@@ -115,57 +116,123 @@ namespace {
 constexpr size_t kKeepMin = 64ull << 20;   // blocks this large are kept on release
 constexpr size_t kKeepMax = 16ull << 30;   // at most this much kept idle
 std::mutex g_mem_mu;
-std::multimap<size_t, void*> g_kept;       // idle blocks by size
-size_t g_kept_bytes = 0;
+KeptBlocks g_kept;                          // idle blocks by (device, size)
 
-void release_kept() {  // with g_mem_mu held
-    for (auto& kv : g_kept) cudaFree(kv.second);
-    g_kept.clear();
-    g_kept_bytes = 0;
+void free_on_device(int dev, void* p) {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (cur != dev) cudaSetDevice(dev);
+    cudaFree(p);
+    if (cur != dev && cur >= 0) cudaSetDevice(cur);
+}
+
+void free_all(std::vector<KeptBlocks::Block>&& blocks) {
+    for (auto& b : blocks) free_on_device(b.device, b.p);
 }
 }  // namespace
 
+// ---- KeptBlocks: the idle-block bookkeeping, no CUDA calls (tested on CPU)
+void* KeptBlocks::take(int device, size_t bytes) {
+    const auto it = blocks_.find({device, bytes});
+    if (it == blocks_.end()) return nullptr;
+    void* p = it->second;
+    blocks_.erase(it);
+    bytes_ -= bytes;
+    return p;
+}
+
+bool KeptBlocks::put(int device, size_t bytes, void* p, size_t cap) {
+    if (bytes_ + bytes > cap) return false;
+    blocks_.emplace(std::make_pair(device, bytes), p);
+    bytes_ += bytes;
+    return true;
+}
+
+std::vector<KeptBlocks::Block> KeptBlocks::drain(int device) {
+    std::vector<Block> out;
+    for (auto it = blocks_.begin(); it != blocks_.end();) {
+        if (device < 0 || it->first.first == device) {
+            out.push_back({it->first.first, it->first.second, it->second});
+            bytes_ -= it->first.second;
+            it = blocks_.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    return out;
+}
+
 void* dev_alloc(size_t bytes) {
+    int dev = 0;
+    ALEA_CUDA(cudaGetDevice(&dev));
     if (bytes >= kKeepMin) {
         std::lock_guard<std::mutex> lock(g_mem_mu);
-        const auto it = g_kept.find(bytes);
-        if (it != g_kept.end()) {
-            void* p = it->second;
-            g_kept.erase(it);
-            g_kept_bytes -= bytes;
-            return p;
-        }
+        if (void* p = g_kept.take(dev, bytes)) return p;
     }
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, bytes);
     if (e == cudaErrorMemoryAllocation) {
         (void)cudaGetLastError();
+        std::vector<KeptBlocks::Block> idle;
         {
             std::lock_guard<std::mutex> lock(g_mem_mu);
-            release_kept();
+            idle = g_kept.drain(dev);
         }
-        e = cudaMalloc(&p, bytes);
+        if (!idle.empty()) {
+            free_all(std::move(idle));
+            e = cudaMalloc(&p, bytes);
+        }
     }
     ALEA_CUDA(e);
     return p;
 }
 
+// A kept block must not be handed out while kernels may still use it, so it
+// is kept only after its own device has finished its work (the ordering
+// cudaFree gives). The synchronisation runs outside the lock; a device that
+// cannot be synchronised (a stream of it being captured, say) gets the block
+// freed instead.
 void dev_free(void* p, size_t bytes) {
     if (!p) return;
-    if (bytes >= kKeepMin) {
-        std::lock_guard<std::mutex> lock(g_mem_mu);
-        if (g_kept_bytes + bytes <= kKeepMax && cudaDeviceSynchronize() == cudaSuccess) {
-            g_kept.emplace(bytes, p);
-            g_kept_bytes += bytes;
-            return;
+    int dev = -1;
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, p) == cudaSuccess && attr.type == cudaMemoryTypeDevice)
+        dev = attr.device;
+    else
+        (void)cudaGetLastError();
+    if (bytes >= kKeepMin && dev >= 0) {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (cur != dev) cudaSetDevice(dev);
+        const bool idle = cudaDeviceSynchronize() == cudaSuccess;
+        if (!idle) (void)cudaGetLastError();
+        if (cur != dev && cur >= 0) cudaSetDevice(cur);
+        if (idle) {
+            std::lock_guard<std::mutex> lock(g_mem_mu);
+            if (g_kept.put(dev, bytes, p, kKeepMax)) return;
         }
     }
-    cudaFree(p);
+    if (dev >= 0)
+        free_on_device(dev, p);
+    else
+        cudaFree(p);
 }
 
 size_t dev_cached_bytes() {
     std::lock_guard<std::mutex> lock(g_mem_mu);
-    return g_kept_bytes;
+    return g_kept.bytes();
+}
+
+size_t dev_release_cached() {
+    std::vector<KeptBlocks::Block> idle;
+    {
+        std::lock_guard<std::mutex> lock(g_mem_mu);
+        idle = g_kept.drain(-1);
+    }
+    size_t n = 0;
+    for (auto& b : idle) n += b.bytes;
+    free_all(std::move(idle));
+    return n;
 }
 
 }  // namespace alea

@@ -4,8 +4,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <stdexcept>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/aleator_gb300.h"
 
@@ -198,13 +201,36 @@ void mixed_table(const alea_lennard_jones& lj, PairParams* out);
 
 // ---------------------------------------------------------------- device buffers
 // Device memory for DevBuf: blocks of 64 MB and more are kept on release (up to
-// 16 GB) and handed out again for a request of the same size, so that objects
-// rebuilt step after step (a grid's tables) skip cudaMalloc/cudaFree. Keeping a
-// block synchronizes the device first, as cudaFree would; an allocation that
-// fails for memory releases the kept blocks and tries once more.
+// 16 GB idle, over all devices) and handed out again for a request of the same
+// size on the same device, so that objects rebuilt step after step (a grid's
+// tables) skip cudaMalloc/cudaFree. Keeping a block synchronizes the block's
+// own device first, as cudaFree would; an allocation that fails for memory
+// releases the device's kept blocks and tries once more; dev_release_cached
+// frees every idle block (alea_release_cached).
 void* dev_alloc(size_t bytes);
 void dev_free(void* p, size_t bytes);
 size_t dev_cached_bytes();
+size_t dev_release_cached();
+
+// The idle-block bookkeeping of the allocator: blocks keyed by (device, size),
+// at most `cap` bytes in total. No CUDA calls, so the keying is testable on any
+// host (alea_test_block_cache).
+class KeptBlocks {
+public:
+    struct Block {
+        int device;
+        size_t bytes;
+        void* p;
+    };
+    void* take(int device, size_t bytes);                    // null when none kept
+    bool put(int device, size_t bytes, void* p, size_t cap);  // false: over the cap
+    std::vector<Block> drain(int device);                     // device < 0: all devices
+    size_t bytes() const { return bytes_; }
+
+private:
+    std::multimap<std::pair<int, size_t>, void*> blocks_;
+    size_t bytes_ = 0;
+};
 
 template <typename T>
 struct DevBuf {

@@ -23,8 +23,10 @@
 // r^-6 (A r^-6 - B) with the shift terms applied per same-type run.
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <numeric>
 #include <type_traits>
@@ -127,8 +129,9 @@ __device__ __forceinline__ void fence_proxy_async() {
 
 // Waits for one phase of an mbarrier with an iteration limit; on timeout the
 // error flag is raised and false returned (the caller stops using the tile).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, unsigned* flags) {
-    for (unsigned it = 0; it < WAIT_LIMIT; ++it) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, unsigned* flags,
+                                                  unsigned limit = WAIT_LIMIT) {
+    for (unsigned it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if (it > 64) __nanosleep(64);
     }
@@ -927,7 +930,7 @@ template <int NG, int TRUNC>
 __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridArgs& A, int brick,
                                             unsigned char* smem, uint64_t* bars, uint32_t& tiles,
                                             unsigned long long* __restrict__ executed,
-                                            unsigned* flags) {
+                                            unsigned* flags, unsigned tile_wait = WAIT_LIMIT) {
     SmemCarve sc{smem};
     ImageRecF* raw = sc.take<ImageRecF>(TILE);         // the staged tile (TMA)
     ulonglong2* cxy = sc.take<ulonglong2>(2 * TILE);   // converted tiles: {x, x}, {y, y}
@@ -1042,7 +1045,7 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
         ulonglong2* cxy_t = cxy + (t & 1) * TILE;
         ulonglong2* czt_t = czt + (t & 1) * TILE;
         uint16_t* amask_t = amask + (t & 1) * TILE;
-        const bool got = mbar_wait_bounded(&bars[0], (T0 + t) & 1, flags);
+        const bool got = mbar_wait_bounded(&bars[0], (T0 + t) & 1, flags, tile_wait);
         static_assert(TILE == THREADS, "one record per thread in the conversion pass");
         static_assert(TILE <= 32768 && THREADS / 32 <= 8, "list entry and class-mask widths");
         if (got && (uint32_t)tid < cnt) {
@@ -1302,7 +1305,7 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
 template <int NG, int TRUNC>
 __global__ void __launch_bounds__(THREADS, NG <= 2 ? 4 : 3)
 grid_build_f32_kernel(GridGeom geo, F32GridArgs args, unsigned long long* __restrict__ executed,
-                      unsigned* flags) {
+                      unsigned* flags, unsigned tile_wait) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bars[2];
     if (threadIdx.x == 0) {
@@ -1312,7 +1315,8 @@ grid_build_f32_kernel(GridGeom geo, F32GridArgs args, unsigned long long* __rest
     }
     __syncthreads();
     uint32_t tiles = 0;
-    sweep_brick<NG, TRUNC>(geo, args, geo.brick0 + (int)blockIdx.x, smem, bars, tiles, executed, flags);
+    sweep_brick<NG, TRUNC>(geo, args, geo.brick0 + (int)blockIdx.x, smem, bars, tiles, executed, flags,
+                           tile_wait);
 }
 
 template <int NG, int TRUNC>
@@ -1533,6 +1537,7 @@ struct BuildArgs {
     double* tables;
     unsigned long long* executed;
     unsigned* flags;
+    unsigned tile_wait;          // FP32 form: polls before a tile wait gives up
 };
 
 template <int NG, int TRUNC>
@@ -1543,7 +1548,8 @@ void launch_one(bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo, const 
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f32_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
         const F32GridArgs fa{a.images_f, a.bins, a.pab, a.pff, a.tables};
-        grid_build_f32_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(geo, fa, a.executed, a.flags);
+        grid_build_f32_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(geo, fa, a.executed, a.flags,
+                                                                       a.tile_wait);
     } else {
         constexpr size_t bytes = f64_smem_bytes<NG>();
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f64_kernel<NG, TRUNC>,
@@ -1604,6 +1610,12 @@ struct GridImpl {
     uint64_t gen = 0;
     std::vector<DevBuf<double2>> corners;
     std::vector<uint64_t> corners_gen;
+    // recorded after each species' corner kernel: an interpolation on another
+    // stream waits on it before reading the blocks
+    struct EventDel {
+        void operator()(CUevent_st* e) const { cudaEventDestroy(e); }
+    };
+    std::vector<std::unique_ptr<CUevent_st, EventDel>> corners_ev;
     bool corners_off = false;  // their allocation failed once: the plain table serves
     std::mutex corners_mu;     // interpolations from several host threads share them
 };
@@ -1809,6 +1821,13 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
     ALEA_CUDA(cudaMemset(g.flags.p, 0, sizeof(unsigned)));
 }
 
+// Test support (alea_test_grid_tile_wait_limit): when set (>= 0), the poll limit
+// of every tile wait of the next FP32-form build, consumed by that build; the
+// wait for the copy still in flight when a CTA gives up keeps WAIT_LIMIT.
+static std::atomic<int64_t> g_next_tile_wait{-1};
+
+void grid_test_set_tile_wait_limit(int64_t limit) { g_next_tile_wait.store(limit); }
+
 // host: null, or per table one host array the build's rows are copied into as
 // the build goes: the bricks run in z-slabs on s, and each finished slab's
 // rows (contiguous, z being the slowest index) are copied on a second stream
@@ -1821,6 +1840,8 @@ static void run_build(GridImpl& g, cudaStream_t s, double* const* host = nullptr
     require(nbricks < (1ull << 31), ALEA_ERR_INVALID_ARGUMENT, "grid too large");
     ALEA_CUDA(cudaMemsetAsync(g.executed.p, 0, sizeof(unsigned long long), s));
     const bool f32 = g.precision == ALEA_FP32;
+    const int64_t knob = f32 ? g_next_tile_wait.exchange(-1) : -1;
+    const unsigned tile_wait = knob >= 0 ? (unsigned)std::min<int64_t>(knob, WAIT_LIMIT) : WAIT_LIMIT;
     // one launch per chunk of up to MAX_NG guests, timed by events on the stream
     const int chunks = (ng + MAX_NG - 1) / MAX_NG;
     cudaEvent_t ev[2];
@@ -1847,7 +1868,8 @@ static void run_build(GridImpl& g, cudaStream_t s, double* const* host = nullptr
             const size_t pofs = (size_t)g0 * g.geo.n_types;
             const BuildArgs args{g.images.p, g.images_f.p, g.bin_start.p, g.params.p, g.guests.p + g0,
                                  f32 ? g.pab.p + pofs : nullptr, f32 ? g.pff.p + pofs : nullptr,
-                                 g.tables.p + (size_t)g0 * nodes, g.executed.p, g.flags.p};
+                                 g.tables.p + (size_t)g0 * nodes, g.executed.p, g.flags.p,
+                                 tile_wait};
             launch_build(cnt, g.truncation, f32, grid, s, geo, args);
             ALEA_CUDA(cudaGetLastError());
         }
@@ -1950,6 +1972,8 @@ GridView grid_view(const GridImpl* g, uint32_t species) {
 
 // The corner blocks of an FP32-form grid's species table, made (on stream s)
 // when missing or older than the table; null when they cannot be allocated.
+// Every caller's stream s waits on the event recorded after the corner kernel,
+// so an interpolation on another stream never reads blocks still being made.
 static const double2* grid_corners(GridImpl* g, uint32_t species, cudaStream_t s) {
     std::lock_guard<std::mutex> lock(g->corners_mu);
     if (g->corners_off) return nullptr;
@@ -1958,6 +1982,7 @@ static const double2* grid_corners(GridImpl* g, uint32_t species, cudaStream_t s
     if (g->corners.size() != g->species.size()) {
         g->corners.resize(g->species.size());
         g->corners_gen.assign(g->species.size(), 0);
+        g->corners_ev.resize(g->species.size());
     }
     if (!g->corners[k].p || g->corners_gen[k] != g->gen) {
         if (!g->corners[k].p) {
@@ -1970,13 +1995,21 @@ static const double2* grid_corners(GridImpl* g, uint32_t species, cudaStream_t s
                 return nullptr;
             }
         }
+        if (!g->corners_ev[k]) {
+            cudaEvent_t ev = nullptr;
+            ALEA_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            g->corners_ev[k].reset(ev);
+        }
         int dev = 0, sms = 0;
         ALEA_CUDA(cudaGetDevice(&dev));
         ALEA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         grid_corners_kernel<<<(unsigned)sms * 8, 256, 0, s>>>(g->geo.n[0], g->geo.n[1], g->geo.n[2],
                                                               grid_table(g, species), g->corners[k].p);
         ALEA_CUDA(cudaGetLastError());
+        ALEA_CUDA(cudaEventRecord(g->corners_ev[k].get(), s));
         g->corners_gen[k] = g->gen;
+    } else {
+        ALEA_CUDA(cudaStreamWaitEvent(s, g->corners_ev[k].get(), 0));
     }
     return g->corners[k].p;
 }

@@ -206,6 +206,9 @@ void grid_batch_stats(const GridBatchImpl* b, alea_grid_batch_stats* out);
 const GridImpl* grid_batch_item(const GridBatchImpl* b, uint32_t i);
 void grid_batch_destroy(GridBatchImpl* b);
 
+// Test support: the tile-wait poll limit of the next FP32-form build (< 0: none).
+void grid_test_set_tile_wait_limit(int64_t limit);
+
 // grid_cache.cpp: the reference's on-disk cache format (version 1).
 void grid_cache_write(const char* path, const alea_lennard_jones& lj, const alea_particles& fw,
                       const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
@@ -214,6 +217,11 @@ void grid_cache_write(const char* path, const alea_lennard_jones& lj, const alea
 std::string grid_cache_file_name(const alea_lennard_jones& lj, const alea_particles& fw,
                                  const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
                                  double spacing);
+// cacheHit: false on a plain miss; throws Error(ALEA_ERR_RUNTIME) when a file at
+// the key's path has another version or stored key. Host only.
+bool grid_cache_hit(const char* dir, const alea_lennard_jones& lj, const alea_particles& fw,
+                    const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
+                    double spacing);
 // Returns false on a plain miss; throws Error(ALEA_ERR_RUNTIME) on a bad file.
 bool grid_cache_read(const char* dir, const alea_lennard_jones& lj, const alea_particles& fw,
                      const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,

@@ -17,7 +17,9 @@
 // (framework_energy_grid.cc:309). With libstdc++ and the few guest species a
 // grid carries (each in its own bucket, no rehash after the first insert)
 // that order is the reverse of insertion, i.e. descending species id, which
-// is the order written here.
+// is the order written here. That order is an accident of one standard
+// library, so the reader does not rely on it: it accepts the tables in any
+// order and sorts them by species id.
 
 #include <algorithm>
 #include <cstdio>
@@ -208,6 +210,39 @@ void grid_cache_write(const char* path, const alea_lennard_jones& lj, const alea
     }
     if (!out)
         throw Error(ALEA_ERR_RUNTIME, "FrameworkEnergyGrid::serialize: write failed for " + p.string());
+}
+
+// cacheHit (framework_energy_grid.cc:326-352): false when no file sits at the
+// key's content-addressed path; a file there whose version or stored key
+// differs is a hard error (never a miss, never a reuse). Reads the header only.
+bool grid_cache_hit(const char* dir, const alea_lennard_jones& lj, const alea_particles& fw,
+                    const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
+                    double spacing) {
+    const Key key = make_key(lj, fw, lat, guest, n_guest, spacing);
+    const std::filesystem::path path = std::filesystem::path(dir) / file_name(key);
+    if (!std::filesystem::exists(path)) return false;
+    std::ifstream in(path, std::ios::binary);
+    if (!in)
+        throw Error(ALEA_ERR_RUNTIME, "FrameworkEnergyGrid::cacheHit: could not open " + path.string());
+    const uint64_t limit = std::filesystem::file_size(path);
+    Reader r{in};
+    const uint32_t version = r.get<uint32_t>();
+    if (version != kVersion)
+        throw Error(ALEA_ERR_RUNTIME, "FrameworkEnergyGrid cache: " + path.string() +
+                                          " has format version " + std::to_string(version) +
+                                          ", this build expects " + std::to_string(kVersion) +
+                                          " -- refusing to reinterpret it. Delete the file (or the "
+                                          "cache directory) to force a rebuild.");
+    const Key stored = read_key(r, limit);
+    if (!in || !(stored == key))
+        throw Error(ALEA_ERR_RUNTIME,
+                    "FrameworkEnergyGrid cache: " + path.string() +
+                        " exists and has a matching content-hash filename, but its stored key does "
+                        "not exactly match the current inputs (framework/lattice/force-field/"
+                        "spacing) -- this is either a hash collision or a corrupted/foreign cache "
+                        "file, and refusing to silently reuse or silently rebuild over it is the "
+                        "only safe response. Delete the file if you are sure it is stale.");
+    return true;
 }
 
 // loadFromCache (framework_energy_grid.cc:354-409)

@@ -161,7 +161,10 @@ extern "C" alea_status alea_ewald_propose_no_alloc(const double* k, const double
         require(n_terms <= NA_MAX_TERMS, ALEA_ERR_INVALID_ARGUMENT,
                 "alea_ewald_propose_no_alloc: at most 262144 reciprocal terms (the size of its "
                 "fixed scratch array)");
-        require(n_removed + n_added <= (uint64_t)NA_MAX_SITES, ALEA_ERR_INVALID_ARGUMENT,
+        // each count on its own first: their sum could wrap around
+        require(n_removed <= (uint64_t)NA_MAX_SITES &&
+                    n_added <= (uint64_t)NA_MAX_SITES - n_removed,
+                ALEA_ERR_INVALID_ARGUMENT,
                 "alea_ewald_propose_no_alloc: at most 64 removed + added sites");
         require(n_terms == 0 || (k && weight && sre && sim), ALEA_ERR_INVALID_ARGUMENT,
                 "alea_ewald_propose_no_alloc: k, weight, sre and sim are required");

@@ -1,7 +1,8 @@
-// Measurement helper: sustained FP32 FFMA throughput of this device, the
-// roofline denominator for the FP32 pair kernels (the measured peaks file
-// carries HBM and tensor-core figures only). Eight independent FMA chains per
-// thread, every SM busy, timed with CUDA events.
+// Measurement helpers: sustained FP32 FMA throughput of this device, scalar
+// (fmaf) and packed two-lane (fma.rn.f32x2), the roofline denominators for the
+// FP32 pair kernels (the measured peaks file carries HBM and tensor-core
+// figures only). Eight independent FMA chains per thread, every SM busy, timed
+// with CUDA events; the best of five launches.
 #include "common.cuh"
 
 namespace alea {
@@ -19,35 +20,80 @@ __global__ void ffma_kernel(float* out, int iters, float a, float b) {
     for (int i = 0; i < 8; ++i) s += x[i];
     if (s == 1234.5f) out[0] = s;  // keeps the chains live
 }
+
+// The same with the packed two-lane FMA (fma.rn.f32x2, sm_100 family), the
+// instruction the FP32 grid sweep issues: 8 independent packed chains.
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b,
+                                                   unsigned long long c) {
+    unsigned long long d;
+    asm volatile("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
+    return (unsigned long long)__float_as_uint(lo) | ((unsigned long long)__float_as_uint(hi) << 32);
+}
+
+__global__ void ffma2_kernel(float* out, int iters, float a, float b) {
+    unsigned long long x[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = pack2(threadIdx.x * 1e-3f + i, threadIdx.x * 2e-3f - i);
+    const unsigned long long a2 = pack2(a, a), b2 = pack2(b, b);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) x[i] = fma2(x[i], a2, b2);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+        s += __uint_as_float((unsigned)x[i]) + __uint_as_float((unsigned)(x[i] >> 32));
+    if (s == 1234.5f) out[0] = s;  // keeps the chains live
+}
+
+template <typename K>
+double time_fma(K kernel, double flops_per_thread_iter) {
+    int dev = 0, sms = 0;
+    ALEA_CUDA(cudaGetDevice(&dev));
+    ALEA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    DevBuf<float> o(1);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    kernel<<<blocks, threads>>>(o.p, 64, 0.999f, 1e-3f);  // warm-up
+    ALEA_CUDA(cudaGetLastError());
+    cudaEvent_t e0, e1;
+    ALEA_CUDA(cudaEventCreate(&e0));
+    ALEA_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        ALEA_CUDA(cudaEventRecord(e0));
+        kernel<<<blocks, threads>>>(o.p, iters, 0.999f, 1e-3f);
+        ALEA_CUDA(cudaEventRecord(e1));
+        ALEA_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        ALEA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        best = ms < best ? ms : best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const double flops = flops_per_thread_iter * iters * (double)blocks * threads;
+    return flops / (best * 1e-3) / 1e12;
+}
 }  // namespace
 }  // namespace alea
+
+extern "C" alea_status alea_probe_fp32x2_fma_tflops(double* out) {
+    try {
+        alea::require_device();
+        *out = alea::time_fma(alea::ffma2_kernel, 2.0 * 2.0 * 8.0);
+        return ALEA_OK;
+    } catch (const alea::Error& e) {
+        return e.status;
+    }
+}
 
 extern "C" alea_status alea_probe_fp32_fma_tflops(double* out) {
     try {
         alea::require_device();
-        int dev = 0, sms = 0;
-        ALEA_CUDA(cudaGetDevice(&dev));
-        ALEA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        alea::DevBuf<float> o(1);
-        const int blocks = sms * 8, threads = 256, iters = 4096;
-        alea::ffma_kernel<<<blocks, threads>>>(o.p, 64, 0.999f, 1e-3f);  // warm-up
-        cudaEvent_t e0, e1;
-        ALEA_CUDA(cudaEventCreate(&e0));
-        ALEA_CUDA(cudaEventCreate(&e1));
-        float best = 1e30f;
-        for (int rep = 0; rep < 5; ++rep) {
-            ALEA_CUDA(cudaEventRecord(e0));
-            alea::ffma_kernel<<<blocks, threads>>>(o.p, iters, 0.999f, 1e-3f);
-            ALEA_CUDA(cudaEventRecord(e1));
-            ALEA_CUDA(cudaEventSynchronize(e1));
-            float ms = 0;
-            ALEA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            best = ms < best ? ms : best;
-        }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
-        *out = flops / (best * 1e-3) / 1e12;
+        *out = alea::time_fma(alea::ffma_kernel, 2.0 * 8.0);
         return ALEA_OK;
     } catch (const alea::Error& e) {
         return e.status;

@@ -171,11 +171,9 @@ def replicate(fw: Framework, n) -> Framework:
     for i in range(nx):
         for j in range(ny):
             for k in range(nz):
-                o = i * m[0] + j * m[1] + k * m[2]
                 ox = i * m[0][0] + j * m[1][0] + k * m[2][0]
                 oy = i * m[0][1] + j * m[1][1] + k * m[2][1]
                 oz = i * m[0][2] + j * m[1][2] + k * m[2][2]
-                del o
                 xs.append(fw.x + ox)
                 ys.append(fw.y + oy)
                 zs.append(fw.z + oz)

@@ -17,8 +17,11 @@ evaluations per second, counted as the reference's loop counts them
   (alea_grid_build_to_host: the grid from host arrays with both tables copied
   into pinned host memory as the build's z-slabs finish), host<->device copies
   inside the timed region.
-* ``roofline``: the build kernel against the FP32 FFMA peak measured in the
-  same run (the kernel is FP32-pipe bound; the peaks file has no FP32 figure).
+* ``roofline``: the build kernel against the FP32 FMA peak measured in the
+  same run, scalar and packed (the kernel is FP32-pipe bound; the peaks file
+  has no FP32 figure).
+* ``fp32_error``: every node of the timed FP32-form grid against the FP64 form
+  of the same grid, by node class (built after the timed region).
 * ``cpu_baseline``: the CPU restatement of the reference's grid loop on a
   bounded sample of the same nodes, on all host cores.
 * ``--impl reference``: the reference's CPU algorithm (the oracle port; the
@@ -61,6 +64,51 @@ KERNEL_FLOPS_PER_SPECIES = 4
 # DRAM bytes (read + write) of one sweep launch on this workload, from a
 # single-pass ncu capture of the full workload (profiles/grid_build_f32_c5_dram.md)
 SWEEP_DRAM_BYTES_PER_LAUNCH = 1347673088
+
+
+def fp32_error_stats(t32, t64, kt=298.0, cap=1e5):
+    """Error of an FP32-form grid table against the FP64 form of the same grid,
+    by node class: pure relative |dE|/|E|, against max(kT, |E|), and the nodes
+    above 1e-5 pure relative (with the largest |E| among them). Nodes at the
+    cap in the FP64 form are counted apart (the FP32 form must be capped too)."""
+    capped = t64 >= cap
+    live = ~capped
+    a, b = t32[live], t64[live]
+    d = np.abs(a - b)
+    mag = np.abs(b)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        pure = np.where(mag > 0, d / mag, np.where(d > 0, np.inf, 0.0))
+    floored = d / np.maximum(kt, mag)
+    big = mag >= kt
+    over = pure > 1e-5
+    hot = b > 1e4
+    return {
+        "nodes": int(t64.size),
+        "capped_nodes": int(capped.sum()),
+        "capped_equal": bool((t32[capped] >= cap).all()),
+        "max_abs_err_K": float(d.max()),
+        "max_pure_rel": float(pure.max()),
+        "max_rel_kT_floor": float(floored.max()),
+        "max_pure_rel_abs_E_ge_kT": float(pure[big].max()) if big.any() else 0.0,
+        "nodes_above_1e-5_pure_rel": int(over.sum()),
+        "max_abs_E_above_1e-5_pure_rel_K": float(mag[over].max()) if over.any() else 0.0,
+        "nodes_1e4_to_1e5_K": int(hot.sum()),
+        "max_pure_rel_1e4_to_1e5_K": float(pure[hot].max()) if hot.any() else 0.0,
+    }
+
+
+def fp32_error(A, ff, parts, fw, guests, grid32):
+    """The timed FP32-form grid against the FP64 form of the same grid, built
+    after the timed region (the FP64 form equals the reference's loop to
+    1e-10, tested)."""
+    t0 = time.perf_counter()
+    g64 = A.FrameworkEnergyGrid(ff, parts, fw.lattice, guests, SPACING, A.FP64)
+    build_s = time.perf_counter() - t0
+    out = {"kT_K": 298.0, "fp64_build_s": build_s, "reference": "FP64 form of the same grid"}
+    for s in guests:
+        out[f"guest_species_{s}"] = fp32_error_stats(grid32.table(s), g64.table(s))
+    del g64
+    return out
 
 
 def _dist():
@@ -321,7 +369,9 @@ def main():
     if rank == 0:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
             if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-        fp32_peak = A.fp32_fma_tflops()
+        scalar_peak = A.fp32_fma_tflops()
+        packed_peak = A.fp32_fma_tflops(packed=True)
+        fp32_peak = max(scalar_peak, packed_peak)  # the device's FP32 FMA peak
         ng = len(guests)
         node_image = st["executed_pairs"] / ng
         sweep = float(np.mean(sweep_ms))
@@ -340,7 +390,12 @@ def main():
             "roofline": {
                 "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak,
-                "peak_source": "FP32 FFMA loop measured in this run (alea_probe_fp32_fma_tflops)",
+                "peak_source": "the larger of two FP32 FMA loops measured in this run: scalar "
+                               "fmaf (alea_probe_fp32_fma_tflops) and packed fma.rn.f32x2 "
+                               "(alea_probe_fp32x2_fma_tflops), the instruction the sweep issues",
+                "peak_scalar_fma": scalar_peak, "peak_packed_fma": packed_peak,
+                "frac_vs_scalar_peak": achieved / scalar_peak,
+                "frac_vs_packed_peak": achieved / packed_peak,
                 "traffic": SWEEP_DRAM_BYTES_PER_LAUNCH if args.workload == "full" else None,
                 "kernel": "grid_build_f32_kernel<2,SHIFTED>",
                 "kernel_ms": sweep,
@@ -350,12 +405,15 @@ def main():
                     KERNEL_FLOPS_PER_NODE_IMAGE + KERNEL_FLOPS_PER_SPECIES * ng,
                 "kernel_issued_achieved": kachieved,
                 "kernel_issued_frac": kachieved / fp32_peak,
+                "kernel_issued_frac_vs_scalar_peak": kachieved / scalar_peak,
+                "kernel_issued_frac_vs_packed_peak": kachieved / packed_peak,
             },
             "e2e": {"value": e2e_value, "unit": "pair evals/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
             "clocks": clocks.summary(),
             "peaks_file": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops")},
         }
+        line["fp32_error"] = fp32_error(A, ff, parts, fw, guests, grid)
         if not args.no_cpu_baseline:
             rate, info = cpu_grid_rate(fw, guests, seconds_target=12.0)
             line["cpu_baseline"] = {"value": rate, "unit": "pair evals/s",

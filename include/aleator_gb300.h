@@ -111,6 +111,25 @@ alea_status alea_device_info(char* name, size_t cap, int32_t* sm_count, int32_t*
 /* Sustained FP32 FFMA throughput of the current device in TFLOP/s (a
  * measurement helper: the roofline denominator of the FP32 pair kernels). */
 alea_status alea_probe_fp32_fma_tflops(double* out);
+/* The same with the packed two-lane FMA (fma.rn.f32x2), the instruction the
+ * FP32 grid sweep issues; an FMA lane counts 2 FLOP. */
+alea_status alea_probe_fp32x2_fma_tflops(double* out);
+
+/* Device memory held idle by the library's block cache (no counterpart in the
+ * reference, which allocates on the host). Device blocks of 64 MB and more are
+ * kept on release, up to 16 GB idle over all devices, and handed out again for
+ * a request of the same size on the same device, so that a grid rebuilt step
+ * after step skips cudaMalloc/cudaFree. Keeping a block synchronizes its own
+ * device first, the ordering cudaFree gives. Other jobs on a shared GPU do not
+ * see the idle blocks as free: alea_release_cached gives them back (the freed
+ * bytes in *freed, which may be NULL); an allocation that fails for memory
+ * releases the device's idle blocks and tries once more. */
+alea_status alea_cached_bytes(uint64_t* out);
+alea_status alea_release_cached(uint64_t* freed);
+/* Test support for the block cache: runs a scripted take / put / drain
+ * sequence on its bookkeeping with fake pointers (no device call) and returns
+ * ALEA_OK when each step returned what keying by (device, size) requires. */
+alea_status alea_test_block_cache(void);
 
 /* ------------------------------------------------------------------ Philox4x32-10 */
 /* philox4x32_10 (core/math/counter_based_rng.hpp:43-44, .cc:42-54), evaluated
@@ -188,11 +207,28 @@ alea_status alea_grid_build_to_host(const alea_lennard_jones* lj, const alea_par
                                     const alea_lattice* lattice, const uint32_t* guest_species,
                                     uint32_t n_guest, double spacing_angstrom, int32_t precision,
                                     double* const* host_tables, alea_grid** out);
+/* Test support for the device-side bounded waits (no counterpart in the
+ * reference, which has no device code): the tile waits of the next FP32-form
+ * grid build or rebuild in this process give up after `limit` polls (0: at the
+ * first wait) instead of the usual ~2^20. The build then ends with
+ * ALEA_ERR_DEVICE_CHECK ("wait") after each CTA has waited, with the usual
+ * limit, for the copy it still had in flight; the device stays usable and the
+ * build after it runs normally. limit < 0 cancels a pending setting. */
+alea_status alea_test_grid_tile_wait_limit(int64_t limit);
 /* cacheFilePath(cacheDirectory, key) (framework_energy_grid.cc:318-325). */
 alea_status alea_grid_cache_file_name(const alea_lennard_jones* lj,
                                       const alea_particles* framework,
                                       const alea_lattice* lattice, const uint32_t* guest_species,
                                       uint32_t n_guest, double spacing, char* out, size_t cap);
+/* cacheHit(cacheDirectory, key) (framework_energy_grid.cc:326-352): *hit = 1
+ * when the file named by the key exists and its version and stored key match
+ * exactly, 0 when no file is there; ALEA_ERR_RUNTIME when a file at that path
+ * has another format version or another stored key (a collision or a foreign
+ * file: never a miss, never a reuse). Host only: reads the file's header. */
+alea_status alea_grid_cache_hit(const char* cache_dir, const alea_lennard_jones* lj,
+                                const alea_particles* framework, const alea_lattice* lattice,
+                                const uint32_t* guest_species, uint32_t n_guest, double spacing,
+                                int32_t* hit);
 /* loadFromCache (framework_energy_grid.cc:354-409): reads the file named by
  * the key in cache_dir; *out = NULL on a plain miss; ALEA_ERR_RUNTIME on a
  * version mismatch, key mismatch or truncated file. */

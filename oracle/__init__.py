@@ -26,8 +26,22 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 ORACLE_SO = BUILD / "liboracle.so"
 REF_SO = HERE / "_ref" / "libaleator_ref.so"
-# the reference source tree (its sources and test data), present only where it was checked out
-REFERENCE_ROOT = Path(os.environ.get("ALEA_REFERENCE_ROOT", "/root/reference"))
+
+
+def _reference_root() -> Path | None:
+    """The reference source tree (its sources and test data), present only
+    where it was checked out: ALEA_REFERENCE_ROOT, else the tree oracle/_ref
+    was last built from (recorded by build_ref.sh); None when neither is set."""
+    env = os.environ.get("ALEA_REFERENCE_ROOT")
+    if env:
+        return Path(env)
+    rec = HERE / "_ref" / "source_root"
+    if rec.exists():
+        return Path(rec.read_text().strip())
+    return None
+
+
+REFERENCE_ROOT = _reference_root()
 
 DRAWS_RIGHT_TO_LEFT = 0
 DRAWS_LEFT_TO_RIGHT = 1
@@ -52,13 +66,17 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_SO
 
 
-def build_reference(reference_root: str = "/root/reference") -> Path | None:
-    """Build oracle/_ref from the reference sources when they are present."""
-    if not Path(reference_root, "src").is_dir():
+def build_reference(reference_root: str | None = None) -> Path | None:
+    """Build oracle/_ref from the reference sources when they are present: the
+    tree given, else ALEA_REFERENCE_ROOT, else build_ref.sh's own default."""
+    global REFERENCE_ROOT
+    root = reference_root or os.environ.get("ALEA_REFERENCE_ROOT")
+    if root is not None and not Path(root, "src").is_dir():
         return REF_SO if REF_SO.exists() else None
-    subprocess.run(["bash", str(HERE / "build_ref.sh"), reference_root], check=True,
+    subprocess.run(["bash", str(HERE / "build_ref.sh"), *([root] if root else [])], check=True,
                    stdout=subprocess.DEVNULL)
-    return REF_SO
+    REFERENCE_ROOT = _reference_root()
+    return REF_SO if REF_SO.exists() else None
 
 
 _D = ctypes.POINTER(ctypes.c_double)

@@ -49,4 +49,6 @@ g++ "${CXXFLAGS[@]}" -c "$HERE/ref_shim.cc" -o "$OUT/obj/ref_shim.o" &
 pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 g++ -shared -o "$OUT/libaleator_ref.so" "${objs[@]}" "$OUT/obj/ref_shim.o"
+# where the tests find the reference's own data files (structure files)
+(cd "$REF" && pwd) > "$OUT/source_root"
 echo "build_ref: wrote $OUT/libaleator_ref.so"

@@ -277,3 +277,37 @@ def test_neutrality_errors_match_reference_text(so):
         with pytest.raises(ValueError, match=r"^MonteCarloEngine: framework is not charge-neutral "
                                              r"\(total charge = 0\.5\d* e\)$"):
             make()
+
+
+def test_block_cache_keying(so):
+    """The device block cache hands a kept block only to a request of the same
+    size on the same device (fake pointers, no device call); with no device
+    nothing is kept and the trim call frees nothing."""
+    import aleator_gb300 as A
+
+    lib = A.load_library()
+    assert lib.alea_test_block_cache() == 0
+    n = ctypes.c_uint64(7)
+    assert lib.alea_cached_bytes(ctypes.byref(n)) == 0 and n.value == 0
+    assert lib.alea_release_cached(ctypes.byref(n)) == 0 and n.value == 0
+    assert lib.alea_release_cached(None) == 0
+
+
+def test_no_alloc_site_counts_cannot_wrap(so):
+    """alea_ewald_propose_no_alloc checks each site count on its own, so a sum
+    that wraps around 2^64 is rejected before any site is copied."""
+    import aleator_gb300 as A
+    from aleator_gb300._lib import _lattice, _D
+
+    lib = A.load_library()
+    lat = _lattice(np.eye(3) * 30.0)
+    add = np.zeros(8)
+    for n_removed, n_added in ((2 ** 64 - 1, 2), (65, 0), (0, 65), (40, 25), (2, 2 ** 64 - 1)):
+        status = lib.alea_ewald_propose_no_alloc(None, None, None, None, 0, 0.3,
+                                                 ctypes.byref(lat), add.ctypes.data_as(_D),
+                                                 n_removed, add.ctypes.data_as(_D), n_added, 1,
+                                                 None)
+        assert status == 1, (n_removed, n_added)
+        buf = ctypes.create_string_buffer(256)
+        lib.alea_last_error(buf, 256)
+        assert b"at most 64 removed + added sites" in buf.value

@@ -85,7 +85,7 @@ def test_missing_file(A, ref):
 def test_reference_structures_read_identically(A, ref):
     """The reference's own structure files (MOF and zeolite cells, 30 to 576
     atoms after expansion) through both readers."""
-    files = sorted((O.REFERENCE_ROOT / "tests").rglob("*.cif"))
+    files = sorted((O.REFERENCE_ROOT / "tests").rglob("*.cif")) if O.REFERENCE_ROOT else []
     if not files:
         pytest.skip("the reference's structure files are not present")
     for f in files:

@@ -348,3 +348,29 @@ def test_build_to_host_equals_build(lib):
         assert A.FrameworkEnergyGrid.build_to_host(ff, p, fw.lattice, guests[:1], 0.4, prec,
                                                    [plain.ctypes.data], keep=False) is None
         assert np.array_equal(plain, ref.table(guests[0]))
+
+
+def test_bounded_tile_wait_gives_up_and_recovers(lib):
+    """The FP32 sweep's tile waits are bounded: with the test knob the next
+    build's waits give up at the first poll (no fault, no hang: each CTA still
+    waits, bounded, for the copy it has in flight, then returns). The build
+    reports ALEA_ERR_DEVICE_CHECK ("wait"), the knob is spent, and the next
+    build on the same context returns the normal tables."""
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    fw = W.cubic_framework(seed=5)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.0, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    grid = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4, 6], 0.8, A.FP32)
+    want = {s: grid.table(s) for s in (4, 6)}
+    lib_ = A.load_library()
+    assert lib_.alea_test_grid_tile_wait_limit(0) == 0
+    with pytest.raises(A.AleatorError) as e:
+        grid.rebuild()
+    assert e.value.status == 6 and "wait" in str(e.value)
+    grid.rebuild()  # the knob was consumed by the failed build
+    for s in (4, 6):
+        assert np.array_equal(grid.table(s), want[s])
+    again = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4, 6], 0.8, A.FP32)
+    for s in (4, 6):
+        assert np.array_equal(again.table(s), want[s])
