@@ -223,6 +223,8 @@ _SIGNATURES = {
     "alea_gcmc_set_proposal": (ctypes.c_int32, [_VP, _VP]),
     "alea_gcmc_set_precision": (ctypes.c_int32, [_VP, ctypes.c_int32]),
     "alea_gcmc_set_grid": (ctypes.c_int32, [_VP, _VP]),
+    "alea_gcmc_set_tail_correction": (ctypes.c_int32, [_VP, ctypes.c_int32]),
+    "alea_widom_set_tail_correction": (ctypes.c_int32, [_VP, ctypes.c_int32, _D]),
     "alea_gcmc_guest_sites": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D, ctypes.POINTER(ctypes.c_uint32),
                                                ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
     "alea_grid_batch_create": (ctypes.c_int32, [ctypes.c_uint32, ctypes.POINTER(_LJ),
@@ -792,6 +794,13 @@ class Widom:
         r = {f: getattr(res, f) for f, _ in res._fields_}
         return (r, out) if per_trial else r
 
+    def set_tail_correction(self, on=True):
+        """Opt-in: every trial's deltaU gains U_tail(framework + molecule) -
+        U_tail(framework); returns that constant (K)."""
+        v = ctypes.c_double()
+        _check(self._lib.alea_widom_set_tail_correction(self._h, 1 if on else 0, ctypes.byref(v)))
+        return v.value
+
     def henry_coefficient(self, seed, stream, n_trials, draw_order=ALEA_DRAWS_RIGHT_TO_LEFT):
         return self.run(seed, stream, n_trials, draw_order=draw_order)["henry"]
 
@@ -1093,6 +1102,11 @@ class GcmcChains:
         restores the direct scan."""
         _check(self._lib.alea_gcmc_set_grid(self._h, grid._h if grid is not None else None))
         self._grid = grid
+
+    def set_tail_correction(self, on=True):
+        """Opt-in: insertions, deletions and swaps add U_tail(after) - U_tail(before)
+        (the reference engine's moves leave the tail correction out)."""
+        _check(self._lib.alea_gcmc_set_tail_correction(self._h, 1 if on else 0))
 
     def set_precision(self, precision):
         """FP64 (the reference's arithmetic) or FP32 (FP32 pair terms and

@@ -892,6 +892,21 @@ alea_status alea_gcmc_set_grid(alea_gcmc* g, const alea_grid* grid) {
     });
 }
 
+alea_status alea_gcmc_set_tail_correction(alea_gcmc* g, int32_t on) {
+    return guarded([&] {
+        need(g, "gcmc");
+        alea::gcmc_set_tail_correction(g->impl, on);
+    });
+}
+
+alea_status alea_widom_set_tail_correction(alea_widom* w, int32_t on, double* du_tail) {
+    return guarded([&] {
+        need(w, "widom");
+        alea::widom_set_tail_correction(w->impl, on);
+        if (du_tail) *du_tail = alea::widom_tail_change(w->impl);
+    });
+}
+
 alea_status alea_gcmc_set_precision(alea_gcmc* g, int32_t precision) {
     return guarded([&] {
         need(g, "gcmc");

@@ -103,6 +103,16 @@ struct GcmcConst {
     // is its species' interpolated table plus the LJ with the guests
     int grid, grid_fast;
     int gn[3];
+    // opt-in tail correction of insertions, deletions and swaps (no
+    // counterpart in the reference engine): with T_b the particle count of LJ
+    // species b, U_tail = K sum_ab f_ab T_a T_b (lennard_jones.cc:217-257,
+    // K = 2 pi / V) is quadratic in the molecule counts n_s, so
+    //   U(n + e_s) - U(n) = lin(s) + tail_self[s],
+    //   lin(s) = tail_fw[s] + sum_s' n_s' tail_x[s][s']
+    int tail;
+    double tail_fw[MAXGS];         // 2K sum_ab f_ab d^s_a F_b (F: framework counts)
+    double tail_x[MAXGS][MAXGS];   // 2K sum_ab f_ab d^s_a d^s'_b
+    double tail_self[MAXGS];       // K sum_ab f_ab d^s_a d^s_b
 };
 
 struct GcmcPtrs {
@@ -976,23 +986,39 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 const double rec = C.charged ? (S.rec_sum + S.dself) + S.dexcl : 0.0;
                 const double T = C.temperature;
                 double du, ratio;
+                // opt-in: U_tail(after) - U_tail(before) of a change in the molecule counts
+                double dut = 0.0;
+                if (C.tail && S.move >= 2) {
+                    auto lin = [&](int s) {
+                        double v = C.tail_fw[s];
+                        for (int s2 = 0; s2 < C.n_gsp; ++s2) v += (double)c.n_of[s2] * C.tail_x[s][s2];
+                        return v;
+                    };
+                    if (S.move == 2)
+                        dut = lin(S.sp_new) + C.tail_self[S.sp_new];
+                    else if (S.move == 3)
+                        dut = C.tail_self[S.sp_old] - lin(S.sp_old);
+                    else
+                        dut = (lin(S.sp_new) - lin(S.sp_old)) +
+                              ((C.tail_self[S.sp_new] + C.tail_self[S.sp_old]) - C.tail_x[S.sp_old][S.sp_new]);
+                }
                 if (S.move <= 1) {
                     du = (u_new - u_old) + (e_new - e_old) + rec;
                     ratio = exp(-du / T);
                 } else if (S.move == 2) {
-                    du = u_new + e_new + rec;
+                    du = u_new + e_new + rec + dut;
                     ratio = (c.fugacity[S.sp_new] * C.volume / T) / (double)(c.n_of[S.sp_new] + 1) *
                             exp(-du / T);
                     // learned proposal: divided by its density (relative to uniform)
                     if (C.prop_cells > 0) ratio *= exp(-S.lq);
                 } else if (S.move == 3) {
-                    du = -(u_old + e_old) + rec;
+                    du = -(u_old + e_old) + rec + dut;
                     ratio = (double)c.n_of[S.sp_old] / (c.fugacity[S.sp_old] * C.volume / T) *
                             exp(-du / T);
                     // the reverse insertion's proposal density at this centroid
                     if (C.prop_cells > 0) ratio *= exp(S.lq);
                 } else {  // swapRatio (gcmc_acceptance.hpp:89-95)
-                    du = (u_new - u_old) + (e_new - e_old) + rec;
+                    du = (u_new - u_old) + (e_new - e_old) + rec + dut;
                     ratio = (c.fugacity[S.sp_new] / c.fugacity[S.sp_old]) *
                             ((double)c.n_of[S.sp_old] / (double)(c.n_of[S.sp_new] + 1)) * exp(-du / T);
                 }
@@ -1443,6 +1469,36 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         mixed_table(lj, table.data());
         g->table.alloc(table.size());
         g->table.upload(table.data(), table.size());
+        {  // the tail-correction constants (used when switched on)
+            const uint32_t nsp = lj.n_species;
+            const double rc = lj.cutoff, rc3 = rc * rc * rc;
+            std::vector<double> f((size_t)nsp * nsp), fw_n(nsp, 0.0);
+            for (uint32_t a = 0; a < nsp; ++a)
+                for (uint32_t b = 0; b < nsp; ++b) {  // tailEnergyCorrection's integral
+                    const PairParams& pp = table[(size_t)a * nsp + b];
+                    const double sr3 = pp.sigma * pp.sigma * pp.sigma;
+                    const double sr9 = sr3 * sr3 * sr3 / (rc3 * rc3 * rc3);
+                    f[(size_t)a * nsp + b] = pp.eps * sr3 * ((4.0 / 9.0) * sr9 - (4.0 / 3.0) * (sr3 / rc3));
+                }
+            for (uint64_t i = 0; i < fw.n; ++i) fw_n[types[i]] += 1.0;
+            std::vector<std::vector<double>> d(n_gsp, std::vector<double>(nsp, 0.0));
+            for (uint32_t k = 0; k < n_gsp; ++k)
+                for (int s = 0; s < C.sp_ns[k]; ++s) d[k][C.splj[k][s]] += 1.0;
+            const double K = 2.0 * kPi / C.volume;
+            auto form = [&](const std::vector<double>& u, const std::vector<double>& v) {
+                double t = 0.0;
+                for (uint32_t a = 0; a < nsp; ++a)
+                    if (u[a] != 0.0)
+                        for (uint32_t b = 0; b < nsp; ++b) t += u[a] * v[b] * f[(size_t)a * nsp + b];
+                return t;
+            };
+            for (uint32_t k = 0; k < n_gsp; ++k) {
+                C.tail_fw[k] = 2.0 * K * form(d[k], fw_n);
+                C.tail_self[k] = K * form(d[k], d[k]);
+                for (uint32_t k2 = 0; k2 < n_gsp; ++k2) C.tail_x[k][k2] = 2.0 * K * form(d[k], d[k2]);
+            }
+            C.tail = 0;
+        }
         uint64_t nk = 0;
         if (ew) {
             ews = ewald_state_create(*ew, fw, lat);
@@ -1702,6 +1758,10 @@ void gcmc_set_grid(GcmcImpl* g, const GridImpl* grid) {
     g->C.grid_fast = v0.fast;
     g->C.grid = 1;
 }
+
+// Opt-in: insertions, deletions and swaps of the next runs add the change of
+// the LJ tail correction (off: the reference engine's energies).
+void gcmc_set_tail_correction(GcmcImpl* g, int on) { g->C.tail = on ? 1 : 0; }
 
 // ALEA_FP64 (the parity form) or ALEA_FP32 for the next runs.
 void gcmc_set_precision(GcmcImpl* g, int precision) {

@@ -314,6 +314,8 @@ void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uin
 void widom_samples(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uint64_t n,
                    int draw_order, float* samples_dev, const ProposalTable* proposal);
 void widom_destroy(WidomImpl* w);
+void widom_set_tail_correction(WidomImpl* w, int on);
+double widom_tail_change(const WidomImpl* w);
 struct WidomBatchImpl;
 WidomBatchImpl* widom_batch_create(uint32_t n, const alea_lennard_jones* lj, const alea_ewald* ew,
                                    const alea_particles* fw, const alea_lattice* lat,
@@ -341,6 +343,7 @@ double gcmc_ewald_energy(const GcmcImpl* g, uint32_t chain);
 void gcmc_set_proposal(GcmcImpl* g, const ProposalTable* t);
 void gcmc_set_precision(GcmcImpl* g, int precision);
 void gcmc_set_grid(GcmcImpl* g, const GridImpl* grid);
+void gcmc_set_tail_correction(GcmcImpl* g, int on);
 unsigned gcmc_chains(const GcmcImpl* g);
 float gcmc_last_ms(const GcmcImpl* g);
 void gcmc_destroy(GcmcImpl* g);

@@ -568,6 +568,11 @@ struct WidomImpl {
     DevBuf<double> partial, result, per_trial, per_trial_frac;
     WidomItem item_h{};
     DevBuf<WidomItem> item;          // the context as a batch of one
+    // opt-in (no counterpart in the reference engine): every trial's deltaU
+    // gains U_tail(framework + molecule) - U_tail(framework), a constant of
+    // the context (tailEnergyCorrection, lennard_jones.cc:246-257)
+    bool tail = false;
+    double tail_du = 0.0;
     ~WidomImpl() {
         if (ews) ewald_state_destroy(ews);
     }
@@ -605,6 +610,36 @@ WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
                     "Widom: guest site LJ species out of range");
             P.site[s] = GuestSite{guest.x[s], guest.y[s], guest.z[s],
                                   guest.charge ? guest.charge[s] : 0.0, guest.lj_species[s]};
+        }
+        {  // the tail-correction change of one insertion into the framework
+            std::vector<double> cnt(lj.n_species, 0.0), mol(lj.n_species, 0.0);
+            for (uint64_t i = 0; i < fw.n; ++i) {
+                const uint32_t t = fw.species ? fw.species[i] : 0u;
+                require(t < lj.n_species, ALEA_ERR_OUT_OF_RANGE, "Widom: framework species out of range");
+                cnt[t] += 1.0;
+            }
+            for (uint32_t s = 0; s < guest.n_sites; ++s) mol[guest.lj_species[s]] += 1.0;
+            std::vector<PairParams> tab((size_t)lj.n_species * lj.n_species);
+            mixed_table(lj, tab.data());
+            const double rc3 = lj.cutoff * lj.cutoff * lj.cutoff;
+            auto u_tail = [&](const std::vector<double>& n) {
+                double total = 0.0;
+                for (uint32_t a = 0; a < lj.n_species; ++a) {
+                    if (n[a] == 0.0) continue;
+                    for (uint32_t b = 0; b < lj.n_species; ++b) {
+                        if (n[b] == 0.0) continue;
+                        const PairParams& pp = tab[(size_t)a * lj.n_species + b];
+                        const double sr3 = pp.sigma * pp.sigma * pp.sigma;
+                        const double sr9 = sr3 * sr3 * sr3 / (rc3 * rc3 * rc3);
+                        total += n[a] * n[b] *
+                                 (pp.eps * sr3 * ((4.0 / 9.0) * sr9 - (4.0 / 3.0) * (sr3 / rc3)));
+                    }
+                }
+                return (2.0 * kPi / std::fabs(P.L.volume)) * total;
+            };
+            std::vector<double> after(cnt);
+            for (uint32_t t = 0; t < lj.n_species; ++t) after[t] += mol[t];
+            w->tail_du = u_tail(after) - u_tail(cnt);
         }
         P.n_species = lj.n_species;
         P.rc = lj.cutoff;
@@ -799,7 +834,17 @@ void widom_run(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t first, uin
                              cudaMemcpyDeviceToHost));
     }
     summarise(r, n, w->P.temperature, ms, out);
+    if (w->tail) {  // a constant added to every trial's deltaU
+        const double shift = -w->tail_du / w->P.temperature;
+        out->log_mean_weight += shift;
+        out->henry *= std::exp(shift);
+        if (per_trial)
+            for (uint64_t i = 0; i < n; ++i) per_trial[i] += w->tail_du;
+    }
 }
+
+void widom_set_tail_correction(WidomImpl* w, int on) { w->tail = on != 0; }
+double widom_tail_change(const WidomImpl* w) { return w->tail_du; }
 
 void widom_destroy(WidomImpl* w) { delete w; }
 

@@ -576,6 +576,18 @@ alea_status alea_gcmc_set_precision(alea_gcmc* g, int32_t precision);
  * chains', with a table for every site species (else ALEA_ERR_OUT_OF_RANGE).
  * NULL restores the direct scan. */
 alea_status alea_gcmc_set_grid(alea_gcmc* g, const alea_grid* grid);
+/* Opt-in LJ tail correction of particle-number moves. The reference engine
+ * leaves it out of every move (its tailEnergyCorrection, lennard_jones.cc:
+ * 246-257, is a whole-system energy); with on != 0 each insertion, deletion
+ * and identity swap of the next runs adds U_tail(after) - U_tail(before) to
+ * its deltaU, U_tail being tailEnergyCorrection over every particle of the
+ * chain (framework and guests). Off by default. */
+alea_status alea_gcmc_set_tail_correction(alea_gcmc* g, int32_t on);
+/* The same for Widom insertions: every trial's deltaU gains the constant
+ * U_tail(framework + molecule) - U_tail(framework), written to *du_tail (may
+ * be NULL) whatever `on` is; K_H is multiplied by exp(-du_tail / T). Single
+ * contexts only (alea_widom_run, alea_widom_run_biased); off by default. */
+alea_status alea_widom_set_tail_correction(alea_widom* w, int32_t on, double* du_tail);
 
 /* ------------------------------------------------------------------ acceptance / EOS (host) */
 /* gcmc::insertionRatio ... clampToProbability (engines/monte_carlo/gcmc_acceptance.hpp:28-101) */

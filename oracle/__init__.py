@@ -454,6 +454,11 @@ class OracleGcmc:
         self.L.orc_gcmc_counters(self.h, _u64(out))
         return out
 
+    def set_tail(self, on=True):
+        """Opt-in: insertions, deletions and swaps add U_tail(after) - U_tail(before)."""
+        self.L.orc_gcmc_set_tail.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self.L.orc_gcmc_set_tail(self.h, 1 if on else 0)
+
     def molecules_of(self, species):
         self.L.orc_gcmc_molecules_of.restype = ctypes.c_uint64
         self.L.orc_gcmc_molecules_of.argtypes = [ctypes.c_void_p, ctypes.c_uint32]

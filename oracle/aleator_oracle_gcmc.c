@@ -360,6 +360,28 @@ static void attempt_rotation(orc_gcmc* g) {
     }
 }
 
+/* U_tail(after) - U_tail(before) as two tailEnergyCorrection evaluations
+ * (lennard_jones.cc:246-257): before = particles [0, n_before); after = the
+ * same without the n_rem sites rem[] plus the n_add sites at [n_before,
+ * n_before + n_add) (a trial's sites are appended to the arrays). */
+static double tail_change(const orc_gcmc* g, uint64_t n_before, const uint64_t* rem, uint32_t n_rem,
+                          uint32_t n_add) {
+    if (!g->tail) return 0.0;
+    const double before = orc_lj_tail(&g->lj, g->m, n_before, g->sp);
+    uint32_t* after = (uint32_t*)malloc(sizeof(uint32_t) * (n_before + n_add + 1));
+    uint64_t n = 0;
+    for (uint64_t i = 0; i < n_before + n_add; ++i) {
+        int gone = 0;
+        for (uint32_t r = 0; r < n_rem; ++r) gone |= rem[r] == i;
+        if (!gone) after[n++] = g->sp[i];
+    }
+    const double a = orc_lj_tail(&g->lj, g->m, n, after);
+    free(after);
+    return a - before;
+}
+
+void orc_gcmc_set_tail(orc_gcmc* g, int on) { g->tail = on; }
+
 static uint64_t count_of_species(const orc_gcmc* g, uint32_t k) {
     uint64_t c = 0;
     for (uint64_t mi = 0; mi < g->n_mol; ++mi) c += g->mol_sp[mi] == k;
@@ -395,7 +417,7 @@ static void attempt_insertion(orc_gcmc* g) {
         pack_sites(g, idx, sp->ns, new_s);
         rec = orc_ews_delta(&g->ews, NULL, 0, new_s, sp->ns, NULL, NULL, NULL, NULL);
     }
-    const double du = disp + elec + rec;
+    const double du = disp + elec + rec + tail_change(g, g->n - sp->ns, NULL, 0, sp->ns);
     g->last_du = du;
     const double volume = fabs(orc_volume(m));
     const uint64_t before = g->n_species == 1 ? g->n_mol : count_of_species(g, k);
@@ -472,7 +494,7 @@ static void attempt_deletion(orc_gcmc* g) {
         pack_sites(g, idx, ns, old_s);
         rec = orc_ews_delta(&g->ews, old_s, ns, NULL, 0, NULL, NULL, NULL, NULL);
     }
-    const double du = -(ui + ei) + rec;
+    const double du = -(ui + ei) + rec + tail_change(g, g->n, idx, ns, 0);
     g->last_du = du;
     const double volume = fabs(orc_volume(g->m));
     const double ratio =
@@ -537,7 +559,8 @@ static void attempt_swap(orc_gcmc* g) {
         pack_sites(g, new_idx, ts->ns, new_s);
         rec = orc_ews_delta(&g->ews, old_s, ns_old, new_s, ts->ns, NULL, NULL, NULL, NULL);
     }
-    const double du = (u_after - u_before) + (e_after - e_before) + rec;
+    const double du = (u_after - u_before) + (e_after - e_before) + rec +
+                      tail_change(g, g->n - ts->ns, old_idx, ns_old, ts->ns);
     g->last_du = du;
     const uint64_t count_to = count_of_species(g, to);
     const double ratio = orc_swap_ratio(g->spc[from].fugacity, ts->fugacity, count_from, count_to,

@@ -45,6 +45,10 @@ typedef struct {
     uint64_t moves_since_resync, resyncs, steps;
     uint64_t attempted[5], accepted[5]; /* translate, rotate, insert, delete, swap */
     double last_du;
+    /* opt-in (no counterpart in the reference engine): insertions, deletions
+     * and swaps add U_tail(after) - U_tail(before), tailEnergyCorrection over
+     * every particle (lennard_jones.cc:246-257) */
+    int tail;
     /* optional energy grid (tables borrowed, one per LJ species or NULL) */
     int grid;
     int gcounts[3];
@@ -82,6 +86,8 @@ void orc_gcmc_counters(const orc_gcmc* g, uint64_t* out10);
 /* MonteCarloEngine's frameworkEnergyGrid: per-species tables of a grid with
  * `counts` nodes on the chain's cell (borrowed; NULL entries for species
  * without a table); n_tables == 0 removes it. */
+/* the opt-in tail-correction change of insertions, deletions and swaps */
+void orc_gcmc_set_tail(orc_gcmc* g, int on);
 void orc_gcmc_set_grid(orc_gcmc* g, const int counts[3], uint32_t n_tables, const uint32_t* species,
                        const double* const* tables);
 
