@@ -2,7 +2,7 @@
 
 Run in a checkout that has the reference tree (default /root/reference):
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py [REFERENCE_ROOT] [--only=irmof1]
 
 It builds oracle/_ref (the reference's hot-path sources compiled by
 oracle/build_ref.sh), runs the reference code on seeded synthetic inputs and
@@ -61,10 +61,39 @@ def load_xyz(path: Path, with_type=False):
     return np.diag([lx, ly, lz]), xyz, types
 
 
+def irmof1_fixture(refroot: Path, ref) -> dict:
+    """The real IRMOF-1 cell as the reference's readCif reads it
+    (tests/validation/data/irmof1/IRMOF-1.cif), with the force field of the
+    reference's CH4/IRMOF-1 validation test: the UFF-derived GenericMOFs
+    parameters per element and the CH4 site, parsed from that test's source
+    (test_gcmc_ch4_irmof1_isotherm.cc:61-76, 98-101)."""
+    r = ref.read_cif(refroot / "tests/validation/data/irmof1/IRMOF-1.cif")
+    src = (refroot / "tests/validation/test_gcmc_ch4_irmof1_isotherm.cc").read_text()
+    table = dict((m[0], (float(m[1]), float(m[2]))) for m in
+                 re.findall(r'\{"(\w+)",\s*\{([\d.]+),\s*([\d.]+)\}\}', src))
+    ch4 = re.search(r"ljParameters\.push_back\(\{([\d.]+),\s*([\d.]+)\}\);\s*//\s*CH4", src)
+    cutoff = re.search(r"const double cutoff = ([\d.]+);", src)
+    eps = [table[s][0] for s in r["symbols"]] + [float(ch4.group(1))]
+    sigma = [table[s][1] for s in r["symbols"]] + [float(ch4.group(2))]
+    return dict(lattice=r["lattice"], x=r["x"], y=r["y"], z=r["z"], species=r["species"],
+                charge=r["charge"], symbols=np.array(r["symbols"]), eps=np.array(eps),
+                sigma=np.array(sigma), cutoff=np.array(float(cutoff.group(1))))
+
+
 def main():
-    refroot = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
+    refroot = Path(args[0] if args else "/root/reference")
     O.build_reference(str(refroot))
     ref = O.Reference()
+    if only == ["irmof1"]:  # regenerate this one fixture, keep the others
+        data = irmof1_fixture(refroot, ref)
+        np.savez_compressed(OUT / "irmof1.npz", **data)
+        man = json.loads((OUT / "MANIFEST.json").read_text())
+        man["irmof1"] = sorted(data.keys())
+        (OUT / "MANIFEST.json").write_text(json.dumps(man, indent=1) + "\n")
+        print("wrote irmof1 to", OUT)
+        return
     fixtures = {}
 
     # ---- Philox streams (counter_based_rng.cc:56-79)
@@ -281,6 +310,7 @@ def main():
         cif[f"{f.stem}__symbols"] = np.array(r["symbols"])
         cif[f"{f.stem}__labels"] = np.array(r["labels"])
     fixtures["cif_structures"] = cif
+    fixtures["irmof1"] = irmof1_fixture(refroot, ref)
 
     for name, data in fixtures.items():
         np.savez_compressed(OUT / f"{name}.npz", **data)

@@ -219,3 +219,21 @@ def test_document_grammar_fuzzed_against_reference(A, ref, tmp_path):
 
     check()
     assert case["ok"] >= 30, case
+
+
+def test_irmof1_fixture_is_the_readers_output(A):
+    """tests/golden/irmof1.npz (the real IRMOF-1 cell the GPU physics test
+    runs) equals this library's reader on the reference's IRMOF-1.cif, where
+    the reference tree is present."""
+    g = golden("irmof1")
+    if O.REFERENCE_ROOT is None:
+        pytest.skip("the reference tree is not present")
+    f = O.REFERENCE_ROOT / "tests/validation/data/irmof1/IRMOF-1.cif"
+    if not f.exists():
+        pytest.skip("the reference's IRMOF-1.cif is not present")
+    s = A.read_cif(f)
+    assert np.array_equal(np.asarray(s.lattice), g["lattice"])
+    for k in ("x", "y", "z", "species"):
+        assert np.array_equal(getattr(s.particles, k), g[k])
+    assert list(s.species_symbols) == [str(v) for v in g["symbols"]]
+    assert len(g["eps"]) == len(s.species_symbols) + 1
