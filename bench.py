@@ -282,6 +282,9 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--workload", default="full", choices=["full", "small"],
                     help="small: 2x2x2 supercell for profiler captures (not a bench line)")
+    ap.add_argument("--henry-judge", type=float, default=None, metavar="SECONDS",
+                    help="run the uniform-insertion judge of the learned Henry coefficient for "
+                         "SECONDS and print one JSON line (no bench line)")
     ap.add_argument("--kernel-case", default=None, choices=["gcmc", "widom", "interp", "ewald"],
                     help="one small case of a non-grid kernel for profiler captures, then exit "
                          "(no bench line)")
@@ -290,6 +293,12 @@ def main():
         return run_reference(args)
     if args.kernel_case:
         return kernel_case(args.kernel_case)
+    if args.henry_judge:
+        import torch
+        import aleator_gb300 as A
+        A.load_library()
+        print(json.dumps(henry_judge(A, torch, args.henry_judge)), flush=True)
+        return 0
 
     import torch
     import aleator_gb300 as A
@@ -427,75 +436,139 @@ def main():
     return 0
 
 
-def henry_time_to_1pct(A, torch, gcmc=True):
-    """The second half of the metric: wall time to a 1 % relative-error Henry
-    coefficient, learned proposal vs uniform insertion, on the charged 424-atom
-    cubic cell with rigid CO2 (Ewald at 1e-6: alpha and kMax from the rule,
-    rc 12 A; LJ shifted at 12.8 A), 298 K, FP64 energies for both.
+def combine_widom(chunks, temperature):
+    """K_H and its relative standard error over consecutive chunks of one
+    trial stream, from each chunk's (trials, log mean weight, relative s.e.):
+    the chunks' first and second moments of the weight, combined in log
+    space (the weights reach e^40 and more on this framework)."""
+    n = np.array([c["n_trials"] for c in chunks], dtype=np.float64)
+    lm = np.array([c["log_mean_weight"] for c in chunks])
+    rel = np.array([c["rel_std_error"] for c in chunks])
+    ln = np.log(n)
+    lm2 = 2.0 * lm + np.log1p(rel * rel * n)  # log E[w^2] of each chunk
+    big_n = n.sum()
 
-    Each time is extrapolated from a fixed run with the estimator's own
-    standard error, t_1% = t_run (rel_se / 0.01)^2. The learned time includes
-    fitting the proposal on the GPU (3 rounds of 2^18 Widom trials, 20 epochs,
-    64^3 cells). With this framework's deep electrostatic wells the uniform
-    estimator's standard error is itself underestimated at any affordable run
-    length (heavy tail), so its time is a lower bound and its K_H low."""
+    def lse(v):
+        m = v.max()
+        return m + np.log(np.exp(v - m).sum())
+
+    l1 = lse(lm + ln) - np.log(big_n)
+    l2 = lse(lm2 + ln) - np.log(big_n)
+    var_rel = max(np.expm1(l2 - 2.0 * l1), 0.0)
+    return {"trials": int(big_n), "henry": float(np.exp(l1) / temperature),
+            "log_mean_weight": float(l1), "rel_std_error": float(np.sqrt(var_rel / big_n))}
+
+
+def run_to_target(torch, run_chunk, temperature, target, cap_s, first_chunk, max_chunk):
+    """Consecutive chunks of one trial stream until the combined relative
+    standard error reaches the target or the time cap passes; wall time
+    measured (device synchronised)."""
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    chunks, first, size = [], 0, first_chunk
+    while True:
+        chunks.append(run_chunk(first, size))
+        first += size
+        comb = combine_widom(chunks, temperature)
+        torch.cuda.synchronize()
+        elapsed = time.perf_counter() - t0
+        if comb["rel_std_error"] <= target or elapsed >= cap_s:
+            break
+        size = min(2 * size, max_chunk)
+    comb.update(seconds=elapsed, reached=comb["rel_std_error"] <= target)
+    return comb
+
+
+def henry_setup(A):
+    """The C4 workload: the charged 424-atom cubic cell, rigid 3-site CO2,
+    Ewald for 1e-6 relative precision (alpha and kMax from the rule), rc 12 Å,
+    LJ shifted at 12.8 Å, 298 K."""
     from aleator_gb300 import workloads as W
     fw = W.cubic_framework(charged=True)
     alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
     ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
     p = A.ParticleData.from_framework(fw)
     ew = A.Ewald(alpha, 12.0, kmax)
-    guest = W.co2_guest(fw)
-    T = 298.0
-    widom = A.Widom(ff, p, fw.lattice, guest, T, ewald=ew)
+    return fw, ff, p, ew, W.co2_guest(fw), 298.0, alpha, kmax
+
+
+# the learned proposal's training budget: 2e6 Boltzmann-weighted Widom samples
+# over three adaptive rounds (each round's rows drawn from the previous table)
+TRAIN_SAMPLES = 2_000_000
+TRAIN_ROUNDS = 3
+
+
+def fit_proposal(A, widom, seed=2, stream=7, epochs=8):
+    prop = A.Proposal(seed=seed)
+    prop.fit(widom, n_samples=TRAIN_SAMPLES // TRAIN_ROUNDS, rounds=TRAIN_ROUNDS, epochs=epochs,
+             cells=64, stream=stream)
+    return prop
+
+
+def henry_time_to_1pct(A, torch, gcmc=True, cap_s=60.0):
+    """The second half of the metric: wall time to a 1 % relative-error Henry
+    coefficient, learned proposal against uniform insertion, on the C4
+    workload (henry_setup), both in the FP32 form (its per-trial energies are
+    within 1e-5 of the FP64 form's, tested).
+
+    Both arms are measured, not extrapolated: each runs consecutive chunks of
+    one trial stream until its relative standard error reaches 1 % or the time
+    cap passes. The learned arm's time includes fitting the proposal on the
+    GPU (2e6 training samples). Where uniform insertion does not reach 1 %
+    within the cap, the speed-up is a measured lower bound (cap over the
+    learned time). The uniform estimate's own standard error is unreliable on
+    this heavy-tailed weight distribution (rare deep electrostatic wells), so
+    the two estimates are also compared in combined standard errors."""
+    fw, ff, p, ew, guest, T, alpha, kmax = henry_setup(A)
+    widom = A.Widom(ff, p, fw.lattice, guest, T, ewald=ew, precision=A.FP32)
     widom.run(1, 0, 4096)  # warm-up
-
-    def timed(fn):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = fn()
-        torch.cuda.synchronize()
-        return r, time.perf_counter() - t0
-
-    n_u, n_b = 1 << 20, 1 << 18
-    u, t_u = timed(lambda: widom.run(42, 0, n_u))
-    prop = A.Proposal(seed=2)
-    _, t_fit = timed(lambda: prop.fit(widom, n_samples=1 << 18, rounds=3, epochs=20, cells=64))
-    b, t_b = timed(lambda: widom.run_biased(prop, 42, 0, n_b))
-    tu1 = t_u * (u["rel_std_error"] / 0.01) ** 2
-    tb1 = t_b * (b["rel_std_error"] / 0.01) ** 2
-    se = np.hypot(u["rel_std_error"] * u["henry"], b["rel_std_error"] * b["henry"])
-    # unbiasedness check: a second proposal (other seeds, 20 % uniform share,
-    # coarser table) and other trial draws estimate the same K_H; and a 16x
-    # longer uniform run, whose estimate climbs toward it as more trials land
-    # in the deep wells
-    prop2 = A.Proposal(seed=7)
-    prop2.fit(widom, n_samples=1 << 18, rounds=3, epochs=20, cells=48, uniform_share=0.2, seed=11,
-              stream=5)
-    b2 = widom.run_biased(prop2, 43, 1, n_b)
-    se2 = np.hypot(b["rel_std_error"] * b["henry"], b2["rel_std_error"] * b2["henry"])
-    n_ul = 1 << 24
-    ul, t_ul = timed(lambda: widom.run(43, 1, n_ul))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prop = fit_proposal(A, widom)
+    torch.cuda.synchronize()
+    t_fit = time.perf_counter() - t0
+    learned = run_to_target(torch, lambda f, n: widom.run_biased(prop, 42, 0, n, first_trial=f),
+                            T, 0.01, cap_s, 1 << 20, 1 << 24)
+    learned["fit_seconds"] = t_fit
+    learned["time_to_1pct_s"] = t_fit + learned["seconds"] if learned["reached"] else None
+    uniform = run_to_target(torch, lambda f, n: widom.run(42, 1, n, first_trial=f), T, 0.01, cap_s,
+                            1 << 22, 1 << 26)
+    uniform["time_to_1pct_s"] = uniform["seconds"] if uniform["reached"] else None
+    se = np.hypot(learned["rel_std_error"] * learned["henry"],
+                  uniform["rel_std_error"] * uniform["henry"])
+    tl = learned["time_to_1pct_s"]
     out = {
         "workload": "charged 424-atom cubic cell (25.832 A), rigid 3-site CO2, Ewald 1e-6 "
-                    f"(alpha {alpha:.4f}, kMax {kmax}), 298 K, FP64",
-        "uniform": {"trials": n_u, "seconds": t_u, "henry": u["henry"],
-                    "rel_std_error": u["rel_std_error"], "time_to_1pct_s": tu1},
-        "learned": {"trials": n_b, "seconds": t_b, "fit_seconds": t_fit, "henry": b["henry"],
-                    "rel_std_error": b["rel_std_error"], "time_to_1pct_s": t_fit + tb1,
-                    "time_to_1pct_excluding_fit_s": tb1},
-        "speedup_including_fit": tu1 / (t_fit + tb1),
-        "speedup_excluding_fit": tu1 / tb1,
-        "henry_difference_in_combined_se": abs(b["henry"] - u["henry"]) / se,
-        "note": "uniform rel_std_error is underestimated on this heavy-tailed weight distribution",
-        "second_proposal": {"henry": b2["henry"], "rel_std_error": b2["rel_std_error"],
-                            "difference_from_learned_in_combined_se": abs(b2["henry"] - b["henry"]) / se2},
-        "uniform_16x": {"trials": n_ul, "seconds": t_ul, "henry": ul["henry"],
-                        "rel_std_error": ul["rel_std_error"]},
+                    f"(alpha {alpha:.4f}, kMax {kmax}), 298 K, FP32 form; proposal trained on "
+                    f"{TRAIN_SAMPLES} Widom samples",
+        "learned": learned, "uniform": uniform, "uniform_cap_s": cap_s,
+        "speedup": (uniform["time_to_1pct_s"] / tl) if (tl and uniform["reached"]) else None,
+        "speedup_lower_bound": (uniform["seconds"] / tl) if (tl and not uniform["reached"]) else None,
+        "henry_difference_in_combined_se": abs(learned["henry"] - uniform["henry"]) / se,
     }
     if gcmc:
         out["gcmc_loading_10bar"] = gcmc_loading(A, torch, ff, p, fw, guest, ew, T)
     return out
+
+
+def henry_judge(A, torch, seconds):
+    """The plain method as the judge of the learned K_H: uniform insertion for
+    `seconds` of FP32 trials, and an independent learned run (another seed,
+    stream and proposal) to 0.5 %; one JSON line."""
+    fw, ff, p, ew, guest, T, alpha, kmax = henry_setup(A)
+    widom = A.Widom(ff, p, fw.lattice, guest, T, ewald=ew, precision=A.FP32)
+    prop = fit_proposal(A, widom, seed=5, stream=21)
+    learned = run_to_target(torch, lambda f, n: widom.run_biased(prop, 77, 3, n, first_trial=f),
+                            T, 0.005, 600.0, 1 << 22, 1 << 24)
+    uniform = run_to_target(torch, lambda f, n: widom.run(77, 4, n, first_trial=f), T, 0.0,
+                            seconds, 1 << 24, 1 << 27)
+    se = np.hypot(learned["rel_std_error"] * learned["henry"],
+                  uniform["rel_std_error"] * uniform["henry"])
+    return {"henry_judge": {"learned": learned, "uniform": uniform,
+                            "difference_in_combined_se": abs(learned["henry"] - uniform["henry"]) / se,
+                            "difference_in_uniform_se":
+                                abs(learned["henry"] - uniform["henry"]) /
+                                (uniform["rel_std_error"] * uniform["henry"])}}
 
 
 def gcmc_loading(A, torch, ff, p, fw, guest, ew, T, n=152, block=15000, blocks=20, refits=4):

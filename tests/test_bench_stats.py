@@ -1,0 +1,34 @@
+"""Host-side statistics of the benchmark: chunks of one Widom trial stream
+combine into the whole stream's K_H and relative standard error (the chunked
+runs to a 1 % target use this)."""
+import numpy as np
+
+import bench
+
+
+def _stats(lw, temperature):
+    """What one Widom call reports for log-weights lw: the log mean weight
+    and the relative standard error of the mean weight."""
+    m = lw.max()
+    s1 = np.exp(lw - m).sum()
+    s2 = np.exp(2 * (lw - m)).sum()
+    n = len(lw)
+    mean = s1 / n
+    var = s2 / n - mean * mean
+    return {"n_trials": n, "log_mean_weight": m + np.log(mean),
+            "rel_std_error": np.sqrt(max(var, 0.0) / n) / mean}
+
+
+def test_chunks_combine_to_the_whole_stream():
+    rng = np.random.default_rng(3)
+    # heavy-tailed log-weights reaching e^60, as on the charged framework
+    lw = np.concatenate([rng.normal(0.0, 3.0, 70_000), rng.normal(55.0, 2.0, 12)])
+    rng.shuffle(lw)
+    whole = _stats(lw, 298.0)
+    cuts = [0, 1000, 3000, 7000, 15_000, 31_000, 70_012]
+    chunks = [_stats(lw[a:b], 298.0) for a, b in zip(cuts[:-1], cuts[1:])]
+    comb = bench.combine_widom(chunks, 298.0)
+    assert comb["trials"] == len(lw)
+    assert abs(comb["log_mean_weight"] - whole["log_mean_weight"]) <= 1e-12 * abs(whole["log_mean_weight"])
+    assert abs(comb["henry"] / (np.exp(whole["log_mean_weight"]) / 298.0) - 1.0) <= 1e-12
+    assert abs(comb["rel_std_error"] / whole["rel_std_error"] - 1.0) <= 1e-9
