@@ -224,6 +224,7 @@ _SIGNATURES = {
     "alea_gcmc_set_precision": (ctypes.c_int32, [_VP, ctypes.c_int32]),
     "alea_gcmc_set_grid": (ctypes.c_int32, [_VP, _VP]),
     "alea_gcmc_set_tail_correction": (ctypes.c_int32, [_VP, ctypes.c_int32]),
+    "alea_gcmc_set_orientation_trials": (ctypes.c_int32, [_VP, ctypes.c_int32]),
     "alea_widom_set_tail_correction": (ctypes.c_int32, [_VP, ctypes.c_int32, _D]),
     "alea_gcmc_guest_sites": (ctypes.c_int32, [_VP, ctypes.c_uint32, _D, ctypes.POINTER(ctypes.c_uint32),
                                                ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
@@ -1102,6 +1103,11 @@ class GcmcChains:
         restores the direct scan."""
         _check(self._lib.alea_gcmc_set_grid(self._h, grid._h if grid is not None else None))
         self._grid = grid
+
+    def set_orientation_trials(self, k):
+        """Orientation-biased insertion and deletion with k trial orientations
+        (k = 1: the reference's single random orientation)."""
+        _check(self._lib.alea_gcmc_set_orientation_trials(self._h, int(k)))
 
     def set_tail_correction(self, on=True):
         """Opt-in: insertions, deletions and swaps add U_tail(after) - U_tail(before)

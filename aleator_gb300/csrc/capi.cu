@@ -899,6 +899,13 @@ alea_status alea_gcmc_set_tail_correction(alea_gcmc* g, int32_t on) {
     });
 }
 
+alea_status alea_gcmc_set_orientation_trials(alea_gcmc* g, int32_t k) {
+    return guarded([&] {
+        need(g, "gcmc");
+        alea::gcmc_set_orientation_trials(g->impl, k);
+    });
+}
+
 alea_status alea_widom_set_tail_correction(alea_widom* w, int32_t on, double* du_tail) {
     return guarded([&] {
         need(w, "widom");

@@ -61,6 +61,7 @@ constexpr float NEAR_R2 = 6.0f * 6.0f;
 constexpr double FIXED_FAR_VOLUME = 100.0 * 4.0 / 3.0 * 3.14159265358979 * 216.0;
 constexpr float CUT_BAND = 1e-5f;
 constexpr int MAXROWS = 8;  // distinct LJ species among the guest sites
+constexpr int MAXCB = 16;   // orientation trials of a biased insertion or deletion
 
 struct GcmcConst {
     Lattice L;
@@ -110,6 +111,9 @@ struct GcmcConst {
     //   U(n + e_s) - U(n) = lin(s) + tail_self[s],
     //   lin(s) = tail_fw[s] + sum_s' n_s' tail_x[s][s']
     int tail;
+    // orientation-biased insertion and deletion of multi-site molecules (no
+    // counterpart in the reference engine; 1: its single random orientation)
+    int orient;
     double tail_fw[MAXGS];         // 2K sum_ab f_ab d^s_a F_b (F: framework counts)
     double tail_x[MAXGS][MAXGS];   // 2K sum_ab f_ab d^s_a d^s'_b
     double tail_self[MAXGS];       // K sum_ab f_ab d^s_a d^s_b
@@ -169,6 +173,16 @@ struct StepShared {
     double e_lj[2 * MAXS], e_el[2 * MAXS];
     double rec_sum, dself, dexcl;
     double lq;  // learned proposal: log density at the inserted / deleted centroid
+    // orientation bias (C.orient > 1): cb 1 for an insertion, 2 for a
+    // deletion; cb_pass the energy pass being evaluated; cb_q the trial
+    // orientations about the centroid cb_ref; cb_lw their log weights -U/T;
+    // cb_logw log(W / k) of the trials (insertion) or of the molecule's own
+    // orientation and its k - 1 alternatives (deletion)
+    int cb, cb_pass, cb_more;
+    double cb_ref[3];
+    double cb_q[MAXCB][4];
+    double cb_lw[MAXCB];
+    double cb_u0, cb_logw, cb_du;
 };
 
 // FP32 form: a guest site's pair terms with one framework or guest type:
@@ -343,6 +357,8 @@ __device__ void plan_biased_insertion(const GcmcConst& C, const GcmcPtrs& P, Cha
     double q[4] = {1.0, 0.0, 0.0, 0.0};
     if (C.sp_ns[k] > 1) draw_quaternion(C, c, q, false);
     place_new(C, k, ref, q, true, S);
+    for (int i = 0; i < 3; ++i) S.cb_ref[i] = ref[i];
+    for (int i = 0; i < 4; ++i) S.cb_q[0][i] = q[i];
 }
 
 // The molecule `mi`'s sites as the old ones.
@@ -416,7 +432,11 @@ __device__ void plan_move(const GcmcConst& C, const GcmcPtrs& P, ChainState& c, 
             ref[i] = add_rn(add_rn(mul_rn(M[i], u[0]), mul_rn(M[3 + i], u[1])), mul_rn(M[6 + i], u[2]));
         double q[4] = {1.0, 0.0, 0.0, 0.0};
         if (C.sp_ns[k] > 1) draw_quaternion(C, c, q, rl);
-        place_new(C, k, ref, q, false, S);
+        // with orientation trials the drawn point is the molecule's centroid
+        // (the deletion's reverse move uses the centroid)
+        place_new(C, k, ref, q, C.orient > 1 && C.sp_ns[k] > 1, S);
+        for (int i = 0; i < 3; ++i) S.cb_ref[i] = ref[i];
+        for (int i = 0; i < 4; ++i) S.cb_q[0][i] = q[i];
         return;
     }
     if (c.n_mol == 0) {  // nothing to act on: no further draws
@@ -550,6 +570,125 @@ __device__ __forceinline__ void slot_tables(const GcmcConst& C, StepShared& S) {
     for (int e = 0; e < 2 * MAXS; ++e) S.sq32[e] = (float)S.sq_slot[e];
 }
 
+// ---- orientation-biased insertion and deletion (C.orient = k > 1; no
+// counterpart in the reference engine). The standard orientational
+// configurational-bias scheme for a rigid molecule: an insertion evaluates k
+// orientations about the drawn centroid, picks one with probability w_j / W
+// (w = exp(-U/T), W = sum w) and is accepted with the insertion ratio in
+// which exp(-dU/T) is replaced by W / k; a deletion evaluates the molecule's
+// own orientation and k - 1 random ones about its centroid and uses k / W in
+// place of exp(+U/T). Insertion and deletion are then each other's reverse
+// with the same proposal probabilities, so detailed balance holds. Energy
+// passes: insertion trial j (k passes, then the picked one again unless it
+// was the last); deletion: the molecule removed, then k - 1 rotations of it
+// (U_j = U_0 + dU_rotation), then the removal again. The extra draws (k - 1
+// quaternions, then the pick) follow the move's own draws.
+
+// Thread 0, after plan_move: sets up the passes (S.cb = 0: the plain move).
+__device__ void cbmc_begin(const GcmcConst& C, ChainState& c, StepShared& S) {
+    S.cb = 0;
+    S.cb_more = 0;
+    S.cb_pass = 0;
+    if (C.orient <= 1 || !S.valid) return;
+    if (S.move == 2 && C.sp_ns[S.sp_new] > 1) {
+        for (int j = 1; j < C.orient; ++j) draw_quaternion(C, c, S.cb_q[j], false);
+        S.cb = 1;
+    } else if (S.move == 3 && C.sp_ns[S.sp_old] > 1) {
+        for (int i = 0; i < 3; ++i) S.cb_ref[i] = 0.0;
+        for (int s = 0; s < S.n_old; ++s)
+            for (int i = 0; i < 3; ++i) S.cb_ref[i] += S.op[s][i];
+        for (int i = 0; i < 3; ++i) S.cb_ref[i] /= (double)S.n_old;
+        S.cb = 2;
+    }
+}
+
+// log(sum_j exp(lw_j) / k) over the k trials
+__device__ double cbmc_log_mean(const double* lw, int k) {
+    double m = lw[0];
+    for (int j = 1; j < k; ++j) m = fmax(m, lw[j]);
+    double s = 0.0;
+    for (int j = 0; j < k; ++j) s += exp(lw[j] - m);
+    return m + log(s / (double)k);
+}
+
+// Thread 0, after an energy pass of an orientation-biased move: records the
+// pass's energy and sets up the next pass (S.cb_more = 1) or ends (0).
+__device__ void cbmc_after_pass(const GcmcConst& C, ChainState& c, StepShared& S, int NS) {
+    S.cb_more = 0;
+    if (!S.cb) return;
+    const int k = C.orient;
+    double u_old = 0.0, u_new = 0.0, e_old = 0.0, e_new = 0.0;
+    for (int s = 0; s < S.n_old; ++s) {
+        u_old += S.e_lj[s];
+        e_old += S.e_el[s];
+    }
+    for (int s = 0; s < S.n_new; ++s) {
+        u_new += S.e_lj[NS + s];
+        e_new += S.e_el[NS + s];
+    }
+    const double rec = C.charged ? (S.rec_sum + S.dself) + S.dexcl : 0.0;
+    const double T = C.temperature;
+    const int p = S.cb_pass;
+    if (S.cb == 1) {  // insertion
+        if (p < k) S.cb_lw[p] = -(u_new + e_new + rec) / T;
+        if (p + 1 < k) {
+            place_new(C, S.sp_new, S.cb_ref, S.cb_q[p + 1], true, S);
+            S.cb_pass = p + 1;
+            S.cb_more = 1;
+            return;
+        }
+        if (p == k - 1) {  // pick a trial with probability w_j / W
+            S.cb_logw = cbmc_log_mean(S.cb_lw, k);
+            double m = S.cb_lw[0];
+            for (int j = 1; j < k; ++j) m = fmax(m, S.cb_lw[j]);
+            double tot = 0.0;
+            for (int j = 0; j < k; ++j) tot += exp(S.cb_lw[j] - m);
+            const double u = u01(c) * tot;
+            int pick = k - 1;
+            double cum = 0.0;
+            for (int j = 0; j < k; ++j) {
+                cum += exp(S.cb_lw[j] - m);
+                if (u < cum) {
+                    pick = j;
+                    break;
+                }
+            }
+            S.cb_du = -S.cb_lw[pick] * T;
+            if (pick != k - 1) {  // evaluate the picked trial again (its sites and S(k) delta)
+                place_new(C, S.sp_new, S.cb_ref, S.cb_q[pick], true, S);
+                S.cb_pass = k;
+                S.cb_more = 1;
+            }
+        }
+        return;
+    }
+    // deletion
+    if (p == 0) {
+        S.cb_u0 = (u_old + e_old) - rec;  // the molecule's energy: dU of removal is -U_0
+        S.cb_lw[0] = -S.cb_u0 / T;
+    } else if (p < k) {
+        S.cb_lw[p] = -(S.cb_u0 + ((u_new - u_old) + (e_new - e_old) + rec)) / T;
+    }
+    if (p + 1 < k) {  // the molecule in another orientation about its centroid
+        double q[4];
+        draw_quaternion(C, c, q, false);
+        S.sp_new = S.sp_old;
+        place_new(C, S.sp_old, S.cb_ref, q, true, S);
+        slot_tables(C, S);
+        S.cb_pass = p + 1;
+        S.cb_more = 1;
+        return;
+    }
+    if (p == k - 1) {  // the removal again, for its S(k) delta
+        S.cb_logw = cbmc_log_mean(S.cb_lw, k);
+        S.cb_du = -S.cb_u0;
+        S.n_new = 0;
+        slot_tables(C, S);
+        S.cb_pass = k;
+        S.cb_more = 1;
+    }
+}
+
 // The grid's value at site slot e (old sites first, then new): its LJ
 // species' table interpolated at the site (frameworkEnergyGrid_->interpolate,
 // monte_carlo_engine.cc:353-356).
@@ -578,6 +717,19 @@ size_t phase_bytes(int kmax, bool f32) {
     if (!f32) return 2 * NS * 3 * tw * sizeof(double2);
     const size_t ab = f32_ab_bytes<NS>(kmax);
     return 2 * NS * 3 * tw * sizeof(float2) + (ab <= AB_TABLE_BUDGET ? ab : 0);
+}
+
+// FP32 form: the trial sites as double-float (hi, lo) and fixed-point copies.
+template <int NS, bool FX>
+__device__ __forceinline__ void prep_sites_f32(const GcmcConst& C, const StepShared& S, float4* sph,
+                                               float4* spl, uint4* sfq) {
+    for (int e = 0; e < 2 * NS; ++e) {
+        const double* p = e < NS ? S.op[e] : S.np_[e - NS];
+        const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
+        sph[e] = make_float4(x.hi, y.hi, z.hi, 0.f);
+        spl[e] = make_float4(x.lo, y.lo, z.lo, 0.f);
+        if constexpr (FX) sfq[e] = fixed_frac(C.L, p[0], p[1], p[2]);
+    }
 }
 
 // FX (FP32 form, large cells): far pairs on the fixed-point displacement.
@@ -640,22 +792,15 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
             if (c.err == 0) {
                 plan_move(C, P, c, gx, gy, gz, mol, msp, S);
                 slot_tables(C, S);
-                if constexpr (F32) {
-                    for (int e = 0; e < 2 * NS; ++e) {
-                        const double* p = e < NS ? S.op[e] : S.np_[e - NS];
-                        const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
-                        sph[e] = make_float4(x.hi, y.hi, z.hi, 0.f);
-                        spl[e] = make_float4(x.lo, y.lo, z.lo, 0.f);
-                        if constexpr (FX) sfq[e] = fixed_frac(C.L, p[0], p[1], p[2]);
-                    }
-                }
+                cbmc_begin(C, c, S);
+                if constexpr (F32) prep_sites_f32<NS, FX>(C, S, sph, spl, sfq);
             } else {
                 S.valid = 0;
             }
         }
         __syncthreads();
         if (S.valid) {
-            const int n_old = S.n_old, n_new = S.n_new;
+            int n_old = S.n_old, n_new = S.n_new;  // this energy pass's site counts
             const uint64_t n_all = C.n_fw + S.ng;
             // FP32 form: term t's S(k) delta, added sites first then removed
             // (ewald_incremental_state.cc:107-116), from this move's phase tables
@@ -692,6 +837,9 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
             // with a grid the framework's LJ comes from the tables: its atoms
             // are visited only for the real-space Ewald terms
             const uint64_t j0 = (C.grid && !C.charged) ? C.n_fw : 0;
+            for (;;) {  // energy passes: one, or several for an orientation-biased move
+            n_old = S.n_old;
+            n_new = S.n_new;
             // ---- LJ and real-space sums of old sites (e < NS) and new sites (e >= NS)
             double acc[4 * NS];
 #pragma unroll
@@ -972,8 +1120,20 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 }
             }
 
+            if (!S.cb) break;
+            if (threadIdx.x == 0) {
+                cbmc_after_pass(C, c, S, NS);
+                if constexpr (F32)
+                    if (S.cb_more) prep_sites_f32<NS, FX>(C, S, sph, spl, sfq);
+            }
+            __syncthreads();
+            if (!S.cb_more) break;
+            }  // energy passes
+
             // ---- acceptance (gcmc_acceptance.hpp:28-101)
             if (threadIdx.x == 0) {
+                n_old = S.n_old;
+                n_new = S.n_new;
                 double u_old = 0.0, u_new = 0.0, e_old = 0.0, e_new = 0.0;
                 for (int s = 0; s < n_old; ++s) {
                     u_old += S.e_lj[s];
@@ -1002,7 +1162,17 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         dut = (lin(S.sp_new) - lin(S.sp_old)) +
                               ((C.tail_self[S.sp_new] + C.tail_self[S.sp_old]) - C.tail_x[S.sp_old][S.sp_new]);
                 }
-                if (S.move <= 1) {
+                if (S.cb == 1) {  // orientation-biased insertion: W / k for exp(-dU/T)
+                    du = S.cb_du + dut;
+                    ratio = (c.fugacity[S.sp_new] * C.volume / T) / (double)(c.n_of[S.sp_new] + 1) *
+                            exp(S.cb_logw - dut / T);
+                    if (C.prop_cells > 0) ratio *= exp(-S.lq);
+                } else if (S.cb == 2) {  // orientation-biased deletion: k / W for exp(+U/T)
+                    du = S.cb_du + dut;
+                    ratio = (double)c.n_of[S.sp_old] / (c.fugacity[S.sp_old] * C.volume / T) *
+                            exp(-S.cb_logw - dut / T);
+                    if (C.prop_cells > 0) ratio *= exp(S.lq);
+                } else if (S.move <= 1) {
                     du = (u_new - u_old) + (e_new - e_old) + rec;
                     ratio = exp(-du / T);
                 } else if (S.move == 2) {
@@ -1498,6 +1668,7 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
                 for (uint32_t k2 = 0; k2 < n_gsp; ++k2) C.tail_x[k][k2] = 2.0 * K * form(d[k], d[k2]);
             }
             C.tail = 0;
+            C.orient = 1;
         }
         uint64_t nk = 0;
         if (ew) {
@@ -1757,6 +1928,14 @@ void gcmc_set_grid(GcmcImpl* g, const GridImpl* grid) {
     for (int a = 0; a < 3; ++a) g->C.gn[a] = v0.n[a];
     g->C.grid_fast = v0.fast;
     g->C.grid = 1;
+}
+
+// Orientation trials of insertions and deletions of multi-site molecules in
+// the next runs (1: the reference's single random orientation).
+void gcmc_set_orientation_trials(GcmcImpl* g, int k) {
+    require(k >= 1 && k <= MAXCB, ALEA_ERR_INVALID_ARGUMENT,
+            "GCMC: orientation trials must be 1.." + std::to_string(MAXCB));
+    g->C.orient = k;
 }
 
 // Opt-in: insertions, deletions and swaps of the next runs add the change of

@@ -344,6 +344,7 @@ void gcmc_set_proposal(GcmcImpl* g, const ProposalTable* t);
 void gcmc_set_precision(GcmcImpl* g, int precision);
 void gcmc_set_grid(GcmcImpl* g, const GridImpl* grid);
 void gcmc_set_tail_correction(GcmcImpl* g, int on);
+void gcmc_set_orientation_trials(GcmcImpl* g, int k);
 unsigned gcmc_chains(const GcmcImpl* g);
 float gcmc_last_ms(const GcmcImpl* g);
 void gcmc_destroy(GcmcImpl* g);

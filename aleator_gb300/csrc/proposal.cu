@@ -8,8 +8,12 @@
 // s in [0, 1)^3 -> 2 n_freq periodic features (sin, cos)(2 pi k_j . s) with
 // integer wave vectors k_j -> depth hidden layers of `width` with SiLU ->
 // one output f(s), an unnormalised log-density. Weights are rounded to BF16
-// (the copy the kernels read) from FP32 master weights that Adam updates;
-// every product accumulates in FP32.
+// (the copy the kernels read) from FP32 master weights that Adam updates. The
+// hidden layers' products run on the tensor cores (mma.sync m16n8k16, BF16
+// operands, FP32 accumulation): the features, the post-SiLU activations and
+// the back-propagated pre-activation gradients are stored in BF16, the
+// pre-activations in FP32 (for SiLU'); the one-unit output layer, the loss and
+// Adam stay in FP32 on the CUDA cores.
 //
 // Training rows {s0, s1, s2, l, lq}: a position, its log-weight l = -dU/T and
 // the log density lq of the proposal it was drawn from (relative to uniform;
@@ -53,6 +57,12 @@ enum { EPI_STORE = 0, EPI_BIAS = 1, EPI_BIAS_SILU = 2, EPI_SILU_GRAD = 3 };
 
 __device__ __forceinline__ float to_f(float v) { return v; }
 __device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <typename T>
+__device__ __forceinline__ T from_f(float v);
+template <>
+__device__ __forceinline__ float from_f<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
 
 __device__ __forceinline__ float sigmoidf(float z) { return 1.0f / (1.0f + __expf(-z)); }
 
@@ -61,10 +71,10 @@ __device__ __forceinline__ float sigmoidf(float z) { return 1.0f / (1.0f + __exp
 // (k_chunk per slice): EPI_STORE slices write to C + z M ldc.
 // Epilogues: EPI_BIAS: C = acc + bias[n]; EPI_BIAS_SILU: aux = acc + bias[n]
 // (pre-activation), C = SiLU(aux); EPI_SILU_GRAD: C = acc SiLU'(aux).
-template <bool TA, bool TB, typename BT, int EPI>
+template <bool TA, bool TB, typename AT, typename BT, typename CT, int EPI>
 __global__ void __launch_bounds__(GTHREADS)
-gemm_kernel(int M, int N, int K, const float* __restrict__ A, int lda, const BT* __restrict__ B,
-            int ldb, float* __restrict__ C, int ldc, const float* __restrict__ bias,
+gemm_kernel(int M, int N, int K, const AT* __restrict__ A, int lda, const BT* __restrict__ B,
+            int ldb, CT* __restrict__ C, int ldc, const float* __restrict__ bias,
             float* __restrict__ aux, int k_chunk) {
     __shared__ float As[GK][GT + 4];
     __shared__ float Bs[GK][GT + 4];
@@ -79,7 +89,7 @@ gemm_kernel(int M, int N, int K, const float* __restrict__ A, int lda, const BT*
             int mm, kk;
             if (TA) { mm = e % GT; kk = e / GT; } else { kk = e % GK; mm = e / GK; }
             const int m = m0 + mm, k = k0 + kk;
-            As[kk][mm] = (m < M && k < ke) ? (TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k]) : 0.f;
+            As[kk][mm] = (m < M && k < ke) ? to_f(TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k]) : 0.f;
         }
         for (int e = tid; e < GT * GK; e += GTHREADS) {
             int nn, kk;
@@ -102,7 +112,7 @@ gemm_kernel(int M, int N, int K, const float* __restrict__ A, int lda, const BT*
         }
         __syncthreads();
     }
-    float* Cz = C + (EPI == EPI_STORE ? (size_t)blockIdx.z * M * ldc : 0);
+    CT* Cz = C + (EPI == EPI_STORE ? (size_t)blockIdx.z * M * ldc : 0);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int m = m0 + ty * 4 + i;
@@ -123,8 +133,122 @@ gemm_kernel(int M, int N, int K, const float* __restrict__ A, int lda, const BT*
                 const float z = aux[o], sg = sigmoidf(z);
                 v *= sg * (1.0f + z * (1.0f - sg));
             }
-            Cz[o] = v;
+            Cz[o] = from_f<CT>(v);
         }
+    }
+}
+
+// ---------------------------------------------------------------- tensor-core GEMM
+// C[M x N] = op(A) op(B), BF16 operands, FP32 accumulation, with the same op()
+// convention and epilogues as gemm_kernel. A 64 x 64 tile per CTA of 4 warps
+// (each 32 x 32: 2 x 4 mma.sync m16n8k16), k-steps of 32 staged in shared
+// memory as As[m][k] and Bs[n][k] (k contiguous, whatever the operands' global
+// layout) and read into fragments with ldmatrix. EPI_STORE writes split-K
+// partials to C + z M ldc; with bpart, the CTAs of the first column of tiles
+// also write the row sums of op(A) over their k-slice to bpart[z M + m] (the
+// bias gradient when op(A) = dz^T).
+constexpr int TC_T = 64, TC_K = 32, TC_PAD = 8, TC_THREADS = 128;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+template <bool TA, bool TB, typename CT, int EPI>
+__global__ void __launch_bounds__(TC_THREADS)
+tc_gemm_kernel(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
+               const __nv_bfloat16* __restrict__ B, int ldb, CT* __restrict__ C, int ldc,
+               const float* __restrict__ bias, float* __restrict__ aux, int k_chunk,
+               float* __restrict__ bpart) {
+    __shared__ __align__(16) __nv_bfloat16 As[TC_T][TC_K + TC_PAD];
+    __shared__ __align__(16) __nv_bfloat16 Bs[TC_T][TC_K + TC_PAD];
+    __shared__ float brow[TC_T];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp >> 1, wn = warp & 1;  // this warp's 32 x 32 quarter
+    const int m0 = blockIdx.y * TC_T, n0 = blockIdx.x * TC_T;
+    const int kb = blockIdx.z * k_chunk;
+    const int ke = min(K, kb + k_chunk);
+    const bool row_sums = bpart != nullptr && blockIdx.x == 0;
+    float acc[2][4][4] = {};
+    float rs = 0.f;  // row sum of op(A) (thread tid < 64 owns row tid)
+    const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
+    for (int k0 = kb; k0 < ke; k0 += TC_K) {
+        // stage op(A)[m0.., k0..] as As[m][k] and op(B)[k0.., n0..] as Bs[n][k]
+        for (int e = tid; e < TC_T * TC_K; e += TC_THREADS) {
+            int mm, kk;
+            if (TA) { mm = e % TC_T; kk = e / TC_T; } else { kk = e % TC_K; mm = e / TC_K; }
+            const int m = m0 + mm, k = k0 + kk;
+            As[mm][kk] = (m < M && k < ke) ? (TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k]) : zero;
+        }
+        for (int e = tid; e < TC_T * TC_K; e += TC_THREADS) {
+            int nn, kk;
+            if (TB) { kk = e % TC_K; nn = e / TC_K; } else { nn = e % TC_T; kk = e / TC_T; }
+            const int n = n0 + nn, k = k0 + kk;
+            Bs[nn][kk] = (n < N && k < ke) ? (TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n]) : zero;
+        }
+        __syncthreads();
+        if (row_sums && tid < TC_T)
+            for (int kk = 0; kk < TC_K; ++kk) rs += __bfloat162float(As[tid][kk]);
+#pragma unroll
+        for (int ks = 0; ks < TC_K; ks += 16) {
+            uint32_t a[2][4], b[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const __nv_bfloat16* pa = &As[wm * 32 + i * 16 + (lane & 15)][ks + (lane >> 4) * 8];
+                asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+                             : "=r"(a[i][0]), "=r"(a[i][1]), "=r"(a[i][2]), "=r"(a[i][3])
+                             : "r"(smem_u32(pa)));
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j += 2) {
+                // matrices: (n j8.., k ks), (n j8.., k ks+8), (n j8+8.., k ks), (n j8+8.., k ks+8)
+                const int r = wn * 32 + j * 8 + (lane & 7) + ((lane >> 4) << 3);
+                const __nv_bfloat16* pb = &Bs[r][ks + ((lane >> 3) & 1) * 8];
+                asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+                             : "=r"(b[j][0]), "=r"(b[j][1]), "=r"(b[j + 1][0]), "=r"(b[j + 1][1])
+                             : "r"(smem_u32(pb)));
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    asm volatile(
+                        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, "
+                        "{%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
+                        : "+f"(acc[i][j][0]), "+f"(acc[i][j][1]), "+f"(acc[i][j][2]), "+f"(acc[i][j][3])
+                        : "r"(a[i][0]), "r"(a[i][1]), "r"(a[i][2]), "r"(a[i][3]), "r"(b[j][0]),
+                          "r"(b[j][1]));
+        }
+        __syncthreads();
+    }
+    if (row_sums && tid < TC_T) brow[tid] = rs;
+    CT* Cz = C + (EPI == EPI_STORE ? (size_t)blockIdx.z * M * ldc : 0);
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                // C fragment: rows lane/4 (+8 for h >= 2), columns 2 (lane % 4) + (h & 1)
+                const int m = m0 + wm * 32 + i * 16 + (lane >> 2) + ((h >> 1) << 3);
+                const int n = n0 + wn * 32 + j * 8 + 2 * (lane & 3) + (h & 1);
+                if (m >= M || n >= N) continue;
+                const size_t o = (size_t)m * ldc + n;
+                float v = acc[i][j][h];
+                if (EPI == EPI_BIAS) {
+                    v += bias[n];
+                } else if (EPI == EPI_BIAS_SILU) {
+                    v += bias[n];
+                    aux[o] = v;
+                    v = v * sigmoidf(v);
+                } else if (EPI == EPI_SILU_GRAD) {
+                    const float z = aux[o], sg = sigmoidf(z);
+                    v *= sg * (1.0f + z * (1.0f - sg));
+                }
+                Cz[o] = from_f<CT>(v);
+            }
+    if (row_sums) {
+        __syncthreads();
+        if (tid < TC_T && m0 + tid < M) bpart[(size_t)blockIdx.z * M + m0 + tid] = brow[tid];
     }
 }
 
@@ -138,15 +262,34 @@ __global__ void reduce_slices_kernel(const float* __restrict__ part, int slices,
     out[i] = s;
 }
 
+// The weight and bias gradients of a layer from their split-K partials, in
+// slice order: out_w[i] = sum_z pw[z][i] (cnt entries), out_b[i] = sum_z pb[z][i].
+__global__ void reduce_wb_kernel(const float* __restrict__ pw, const float* __restrict__ pb,
+                                 int slices, size_t cnt, size_t nb, float* __restrict__ out_w,
+                                 float* __restrict__ out_b) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < cnt) {
+        float s = 0.f;
+        for (int z = 0; z < slices; ++z) s += pw[(size_t)z * cnt + i];
+        out_w[i] = s;
+    } else if (i < cnt + nb) {
+        const size_t j = i - cnt;
+        float s = 0.f;
+        for (int z = 0; z < slices; ++z) s += pb[(size_t)z * nb + j];
+        out_b[j] = s;
+    }
+}
+
 // Column sums of X [rows x cols] in a fixed order: per column, rows are
 // summed by slices of `chunk` into part[slice][col], then reduce_slices.
-__global__ void colsum_part_kernel(const float* __restrict__ X, int rows, int cols, int chunk,
+template <typename XT>
+__global__ void colsum_part_kernel(const XT* __restrict__ X, int rows, int cols, int chunk,
                                    float* __restrict__ part) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cols) return;
     const int r0 = blockIdx.y * chunk, r1 = min(rows, r0 + chunk);
     float s = 0.f;
-    for (int r = r0; r < r1; ++r) s += X[(size_t)r * cols + c];
+    for (int r = r0; r < r1; ++r) s += to_f(X[(size_t)r * cols + c]);
     part[(size_t)blockIdx.y * cols + c] = s;
 }
 
@@ -155,7 +298,8 @@ __global__ void colsum_part_kernel(const float* __restrict__ X, int rows, int co
 // idx (optional) gathers rows: sample = idx ? idx(i) : i.
 __global__ void features_kernel(const float* __restrict__ samples, int stride, uint64_t n,
                                 uint64_t perm_a, uint64_t perm_c, uint64_t pool,
-                                const float* __restrict__ kvec, int nf, float* __restrict__ phi) {
+                                const float* __restrict__ kvec, int nf,
+                                __nv_bfloat16* __restrict__ phi) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t src = pool ? (perm_a * i + perm_c) % pool : i;
@@ -164,8 +308,8 @@ __global__ void features_kernel(const float* __restrict__ samples, int stride, u
         const float t = kvec[3 * j] * s[0] + kvec[3 * j + 1] * s[1] + kvec[3 * j + 2] * s[2];
         float sn, cs;
         sincospif(2.0f * (t - floorf(t)), &sn, &cs);
-        phi[i * 2 * nf + j] = sn;
-        phi[i * 2 * nf + nf + j] = cs;
+        phi[i * 2 * nf + j] = __float2bfloat16_rn(sn);
+        phi[i * 2 * nf + nf + j] = __float2bfloat16_rn(cs);
     }
 }
 
@@ -316,8 +460,10 @@ struct ProposalImpl {
     uint64_t adam_t = 0;
     // batch workspace
     uint64_t cap = 0;
-    DevBuf<float> phi, f, gf, dz_a, dz_b, part;
-    std::vector<DevBuf<float>> z, h;  // per hidden layer
+    DevBuf<__nv_bfloat16> phi, dz_a, dz_b;  // features, back-propagated gradients (BF16)
+    DevBuf<float> f, gf, part, bpart;
+    std::vector<DevBuf<float>> z;               // per hidden layer: pre-activation
+    std::vector<DevBuf<__nv_bfloat16>> h;       // per hidden layer: SiLU output (BF16)
     DevBuf<double> lpart, stats;
     // tabulated proposal
     int cells = 0;
@@ -344,14 +490,25 @@ static void ensure_capacity(ProposalImpl& P, uint64_t n) {
     P.lpart.alloc(blocks_for(n, 256) * 5);
 }
 
-template <bool TA, bool TB, typename BT, int EPI>
-static void gemm(cudaStream_t s, int M, int N, int K, const float* A, int lda, const BT* B, int ldb,
-                 float* C, int ldc, const float* bias = nullptr, float* aux = nullptr,
+template <bool TA, bool TB, int EPI, typename AT, typename BT, typename CT>
+static void gemm(cudaStream_t s, int M, int N, int K, const AT* A, int lda, const BT* B, int ldb,
+                 CT* C, int ldc, const float* bias = nullptr, float* aux = nullptr,
                  int slices = 1) {
     const int chunk = slices > 1 ? ((K + slices - 1) / slices + GK - 1) / GK * GK : K;
     dim3 grid((unsigned)((N + GT - 1) / GT), (unsigned)((M + GT - 1) / GT), (unsigned)slices);
-    gemm_kernel<TA, TB, BT, EPI><<<grid, GTHREADS, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias,
-                                                          aux, chunk);
+    gemm_kernel<TA, TB, AT, BT, CT, EPI><<<grid, GTHREADS, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc,
+                                                                  bias, aux, chunk);
+    ALEA_CUDA(cudaGetLastError());
+}
+
+template <bool TA, bool TB, int EPI, typename CT>
+static void tc_gemm(cudaStream_t s, int M, int N, int K, const __nv_bfloat16* A, int lda,
+                    const __nv_bfloat16* B, int ldb, CT* C, int ldc, const float* bias = nullptr,
+                    float* aux = nullptr, int slices = 1, float* bpart = nullptr) {
+    const int chunk = slices > 1 ? ((K + slices - 1) / slices + TC_K - 1) / TC_K * TC_K : K;
+    dim3 grid((unsigned)((N + TC_T - 1) / TC_T), (unsigned)((M + TC_T - 1) / TC_T), (unsigned)slices);
+    tc_gemm_kernel<TA, TB, CT, EPI><<<grid, TC_THREADS, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc,
+                                                               bias, aux, chunk, bpart);
     ALEA_CUDA(cudaGetLastError());
 }
 
@@ -363,22 +520,22 @@ static void forward(ProposalImpl& P, const float* samples, uint64_t n, uint64_t 
     features_kernel<<<blocks_for(n, 256), 256, 0, s>>>(samples, ROW, n, pa, pc, pool, P.kvec.p, P.nf,
                                                        P.phi.p);
     ALEA_CUDA(cudaGetLastError());
-    const float* in = P.phi.p;
-    for (int l = 0; l < P.depth; ++l) {
-        gemm<false, true, __nv_bfloat16, EPI_BIAS_SILU>(s, (int)n, P.lout[l], P.lin[l], in, P.lin[l],
-                                                        P.wb.p + P.woff[l], P.lin[l], P.h[l].p,
-                                                        P.lout[l], P.w.p + P.boff[l], P.z[l].p);
+    const __nv_bfloat16* in = P.phi.p;
+    for (int l = 0; l < P.depth; ++l) {  // tensor cores: h_l = SiLU(h_{l-1} W_l^T + b_l)
+        tc_gemm<false, true, EPI_BIAS_SILU>(s, (int)n, P.lout[l], P.lin[l], in, P.lin[l],
+                                            P.wb.p + P.woff[l], P.lin[l], P.h[l].p, P.lout[l],
+                                            P.w.p + P.boff[l], P.z[l].p);
         in = P.h[l].p;
     }
     const int L = P.depth;
-    // output bias is read in FP32 (as every bias): biases are not rounded
-    gemm<false, true, __nv_bfloat16, EPI_BIAS>(s, (int)n, 1, P.width, in, P.width, P.wb.p + P.woff[L],
-                                               P.width, P.f.p, 1, P.w.p + P.boff[L]);
+    // the one-unit output layer on the CUDA cores; biases are read in FP32 (not rounded)
+    gemm<false, true, EPI_BIAS>(s, (int)n, 1, P.width, in, P.width, P.wb.p + P.woff[L], P.width,
+                                P.f.p, 1, P.w.p + P.boff[L]);
 }
 
 // Loss and gradient for a batch: fills P.g and returns the loss.
 static double loss_grad(ProposalImpl& P, const float* samples, uint64_t n, uint64_t pa, uint64_t pc,
-                        uint64_t pool, double tau, cudaStream_t s) {
+                        uint64_t pool, double tau, cudaStream_t s, bool want_loss = true) {
     forward(P, samples, n, pa, pc, pool, s);
     const unsigned nb = blocks_for(n, 256);
     loss_part_kernel<<<nb, 256, 0, s>>>(P.f.p, samples, ROW, n, pa, pc, pool, tau, P.lpart.p);
@@ -387,39 +544,48 @@ static double loss_grad(ProposalImpl& P, const float* samples, uint64_t n, uint6
     ALEA_CUDA(cudaGetLastError());
     const int W = P.width, L = P.depth;
     const int slices = (int)std::min<uint64_t>(64, std::max<uint64_t>(1, n / 1024));
-    auto wgrad = [&](int layer, const float* dz, const float* hin, int nout, int nin) {
-        // dW = dz^T hin (split over samples), db = column sums of dz
-        const size_t cnt = (size_t)nout * nin;
-        const size_t need = (size_t)slices * cnt;
-        if (need > P.part.n) P.part.alloc(need);
-        gemm<true, false, float, EPI_STORE>(s, nout, nin, (int)n, dz, nout, hin, nin, P.part.p, nin,
-                                            nullptr, nullptr, slices);
-        reduce_slices_kernel<<<blocks_for(cnt, 256), 256, 0, s>>>(P.part.p, slices, cnt,
-                                                                  P.g.p + P.woff[layer]);
-        const int chunk = (int)((n + slices - 1) / slices);
-        colsum_part_kernel<<<dim3(blocks_for(nout, 128), slices), 128, 0, s>>>(dz, (int)n, nout, chunk,
-                                                                               P.part.p);
-        reduce_slices_kernel<<<blocks_for(nout, 256), 256, 0, s>>>(P.part.p, slices, nout,
-                                                                   P.g.p + P.boff[layer]);
-        ALEA_CUDA(cudaGetLastError());
+    auto need_parts = [&](size_t cnt, size_t nb) {
+        if ((size_t)slices * cnt > P.part.n) P.part.alloc((size_t)slices * cnt);
+        if ((size_t)slices * nb > P.bpart.n) P.bpart.alloc((size_t)slices * nb);
     };
-    // output layer: dW_L = g^T h_{L-1}, db_L = sum g; dz_{L-1} = (g W_L) SiLU'(z_{L-1})
-    wgrad(L, P.gf.p, P.h[L - 1].p, 1, W);
-    float* dz = P.dz_a.p;
-    float* dz_next = P.dz_b.p;
-    gemm<false, false, __nv_bfloat16, EPI_SILU_GRAD>(s, (int)n, W, 1, P.gf.p, 1, P.wb.p + P.woff[L], W,
-                                                     dz, W, nullptr, P.z[L - 1].p);
+    // output layer (one unit, CUDA cores): dW_L = g^T h_{L-1}, db_L = sum g
+    {
+        const size_t cnt = (size_t)W;
+        need_parts(cnt, 1);
+        gemm<true, false, EPI_STORE>(s, 1, W, (int)n, P.gf.p, 1, P.h[L - 1].p, W, P.part.p, W,
+                                     nullptr, nullptr, slices);
+        const int chunk = (int)((n + slices - 1) / slices);
+        colsum_part_kernel<<<dim3(1, slices), 128, 0, s>>>(P.gf.p, (int)n, 1, chunk, P.bpart.p);
+        reduce_wb_kernel<<<blocks_for(cnt + 1, 256), 256, 0, s>>>(P.part.p, P.bpart.p, slices, cnt, 1,
+                                                                  P.g.p + P.woff[L], P.g.p + P.boff[L]);
+        ALEA_CUDA(cudaGetLastError());
+    }
+    // dz_{L-1} = (g W_L) SiLU'(z_{L-1}) (rank one, CUDA cores), stored in BF16
+    __nv_bfloat16* dz = P.dz_a.p;
+    __nv_bfloat16* dz_next = P.dz_b.p;
+    gemm<false, false, EPI_SILU_GRAD>(s, (int)n, W, 1, P.gf.p, 1, P.wb.p + P.woff[L], W, dz, W,
+                                      nullptr, P.z[L - 1].p);
     for (int l = L - 1; l >= 0; --l) {
-        const float* hin = l > 0 ? P.h[l - 1].p : P.phi.p;
-        wgrad(l, dz, hin, P.lout[l], P.lin[l]);
+        const __nv_bfloat16* hin = l > 0 ? P.h[l - 1].p : P.phi.p;
+        // tensor cores: dW_l = dz_l^T h_{l-1} split over samples, with the bias
+        // gradient (the row sums of dz_l^T) in the same launch; then both reduced
+        // in slice order by one launch
+        const size_t cnt = (size_t)P.lout[l] * P.lin[l];
+        need_parts(cnt, (size_t)P.lout[l]);
+        tc_gemm<true, false, EPI_STORE>(s, P.lout[l], P.lin[l], (int)n, dz, P.lout[l], hin, P.lin[l],
+                                        P.part.p, P.lin[l], nullptr, nullptr, slices, P.bpart.p);
+        reduce_wb_kernel<<<blocks_for(cnt + P.lout[l], 256), 256, 0, s>>>(
+            P.part.p, P.bpart.p, slices, cnt, (size_t)P.lout[l], P.g.p + P.woff[l], P.g.p + P.boff[l]);
+        ALEA_CUDA(cudaGetLastError());
         if (l > 0) {
-            // dz_{l-1} = (dz_l W_l) SiLU'(z_{l-1})
-            gemm<false, false, __nv_bfloat16, EPI_SILU_GRAD>(s, (int)n, P.lin[l], P.lout[l], dz,
-                                                             P.lout[l], P.wb.p + P.woff[l], P.lin[l],
-                                                             dz_next, P.lin[l], nullptr, P.z[l - 1].p);
+            // dz_{l-1} = (dz_l W_l) SiLU'(z_{l-1}) on the tensor cores
+            tc_gemm<false, false, EPI_SILU_GRAD>(s, (int)n, P.lin[l], P.lout[l], dz, P.lout[l],
+                                                 P.wb.p + P.woff[l], P.lin[l], dz_next, P.lin[l],
+                                                 nullptr, P.z[l - 1].p);
             std::swap(dz, dz_next);
         }
     }
+    if (!want_loss) return 0.0;
     double st[5];
     ALEA_CUDA(cudaMemcpyAsync(st, P.stats.p, sizeof(st), cudaMemcpyDeviceToHost, s));
     ALEA_CUDA(cudaStreamSynchronize(s));
@@ -558,7 +724,8 @@ double proposal_train(ProposalImpl* P, const float* samples_dev, uint64_t pool,
         const uint64_t cc = (uint64_t)(philox_uniform(c.seed, 3, call++) * (double)pool);
         for (uint64_t st = 0; st < steps; ++st) {
             const uint64_t pc = (cc + a * (st * batch % pool)) % pool;
-            loss = loss_grad(*P, samples_dev, batch, a, pc, pool, c.tau, s);
+            const bool last = e + 1 == c.epochs && st + 1 == steps;
+            loss = loss_grad(*P, samples_dev, batch, a, pc, pool, c.tau, s, last);
             ++P->adam_t;
             const float c1 = 1.f - std::pow((float)c.beta1, (float)P->adam_t);
             const float c2 = 1.f - std::pow((float)c.beta2, (float)P->adam_t);

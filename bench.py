@@ -285,6 +285,10 @@ def main():
     ap.add_argument("--henry-judge", type=float, default=None, metavar="SECONDS",
                     help="run the uniform-insertion judge of the learned Henry coefficient for "
                          "SECONDS and print one JSON line (no bench line)")
+    ap.add_argument("--loading", type=float, default=None, metavar="SECONDS",
+                    help="the C4 loading comparison at 0.1, 1, 10 and 30 bar, SECONDS per arm, "
+                         "one JSON line (no bench line)")
+    ap.add_argument("--orientation-trials", type=int, default=1)
     ap.add_argument("--kernel-case", default=None, choices=["gcmc", "widom", "interp", "ewald"],
                     help="one small case of a non-grid kernel for profiler captures, then exit "
                          "(no bench line)")
@@ -293,6 +297,13 @@ def main():
         return run_reference(args)
     if args.kernel_case:
         return kernel_case(args.kernel_case)
+    if args.loading:
+        import torch
+        import aleator_gb300 as A
+        A.load_library()
+        print(json.dumps(loading_comparison(A, torch, seconds=args.loading,
+                                            orient=args.orientation_trials)), flush=True)
+        return 0
     if args.henry_judge:
         import torch
         import aleator_gb300 as A
@@ -475,7 +486,9 @@ def run_to_target(torch, run_chunk, temperature, target, cap_s, first_chunk, max
         if comb["rel_std_error"] <= target or elapsed >= cap_s:
             break
         size = min(2 * size, max_chunk)
-    comb.update(seconds=elapsed, reached=comb["rel_std_error"] <= target)
+    comb.update(seconds=elapsed, reached=comb["rel_std_error"] <= target,
+                chunks=[(int(c["n_trials"]), float(c["log_mean_weight"]), float(c["rel_std_error"]))
+                        for c in chunks])
     return comb
 
 
@@ -547,7 +560,7 @@ def henry_time_to_1pct(A, torch, gcmc=True, cap_s=60.0):
         "henry_difference_in_combined_se": abs(learned["henry"] - uniform["henry"]) / se,
     }
     if gcmc:
-        out["gcmc_loading_10bar"] = gcmc_loading(A, torch, ff, p, fw, guest, ew, T)
+        out["gcmc_loading"] = loading_comparison(A, torch, pressures_bar=(10.0,), seconds=12.0)
     return out
 
 
@@ -571,67 +584,111 @@ def henry_judge(A, torch, seconds):
                                 (uniform["rel_std_error"] * uniform["henry"])}}
 
 
-def gcmc_loading(A, torch, ff, p, fw, guest, ew, T, n=152, block=15000, blocks=20, refits=4):
-    """GCMC loading of the same cell at 10 bar (the charged-CO2 GCMC state
-    point), uniform insertion against the learned proposal refitted at loading
-    (Widom trials in the framework plus 8 chains' current guests, before each
-    of the first `refits` blocks; fit time counted), FP32 form, one chain per
-    SM. Reported: the mean loading over chains after each block against wall
-    time, and the time each method needs to reach 95 % of the uniform run's
-    final loading (linear between blocks)."""
+def loading_run(A, torch, ff, p, fw, guest, ew, T, pressure_pa, learned, seconds, n=152,
+                block=5000, refits=3, proposal=None, orient=1, seed0=2000):
+    """One arm of the loading comparison: n FP32 chains of charged CO2 from an
+    empty cell at one pressure (Peng-Robinson fugacity), blocks of `block`
+    moves until `seconds` of wall time. The learned arm starts from `proposal`
+    (trained on the empty framework; its fit time is counted) and refits at
+    loading before each of its first `refits` blocks (timed). Returns the
+    per-block trajectory: (wall time, per-chain mean N over the block)."""
     from aleator_gb300 import workloads as W
-    fug = A.peng_robinson_fugacity(*W.CO2_CRITICAL, T, 1e6)
-    res = {}
-    for name in ("uniform", "learned"):
-        ch = A.GcmcChains(ff, p, fw.lattice, guest, T, [fug] * n, list(range(2000, 2000 + n)),
-                          [5] * n, ewald=ew, max_molecules=800, precision=A.FP32)
-        prop, t_total, fit_s, traj = None, 0.0, 0.0, []
-        prev = np.array([ch.info(c)["sum_molecules"] for c in range(n)])
-        for b in range(blocks):
-            if name == "learned" and b < refits:
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                prop = prop or A.Proposal(seed=2)
-                prop.fit_at_loading(ch, ff, p, fw.lattice, guest, T, ewald=ew, chain_ids=range(8),
-                                    n_samples=1 << 17, rounds=2 if b == 0 else 1, epochs=15,
-                                    cells=48, uniform_share=0.2, seed=100 + b, stream=10 * b)
-                ch.set_proposal(prop)
-                torch.cuda.synchronize()
-                dt = time.perf_counter() - t0
-                fit_s += dt
-                t_total += dt
+    fug = A.peng_robinson_fugacity(*W.CO2_CRITICAL, T, pressure_pa)
+    ch = A.GcmcChains(ff, p, fw.lattice, guest, T, [fug] * n, list(range(seed0, seed0 + n)),
+                      [7] * n, ewald=ew, max_molecules=800, precision=A.FP32)
+    if orient > 1:
+        ch.set_orientation_trials(orient)
+    prop, t_total, fit_s = None, 0.0, 0.0
+    if learned:
+        prop, fit_s = proposal
+        t_total += fit_s
+        ch.set_proposal(prop)
+    prev = np.array([ch.info(c)["sum_molecules"] for c in range(n)])
+    traj, b = [], 0
+    while t_total < seconds:
+        if learned and b < refits:
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            ch.run(block)
+            prop.fit_at_loading(ch, ff, p, fw.lattice, guest, T, ewald=ew, chain_ids=range(8),
+                                n_samples=1 << 17, rounds=1, epochs=10, cells=48,
+                                uniform_share=0.2, seed=100 + b, stream=10 * b)
+            ch.set_proposal(prop)
             torch.cuda.synchronize()
-            t_total += time.perf_counter() - t0
-            cur = np.array([ch.info(c)["sum_molecules"] for c in range(n)])
-            avg = (cur - prev) / block
-            prev = cur
-            traj.append((t_total, float(avg.mean()), float(avg.std(ddof=1) / np.sqrt(n))))
-        att = np.array([ch.info(c)["attempted"] for c in range(n)]).sum(0)
-        acc = np.array([ch.info(c)["accepted"] for c in range(n)]).sum(0)
-        res[name] = {"moves_per_chain": block * blocks, "seconds": t_total, "fit_seconds": fit_s,
-                     "us_per_move_per_chain": (t_total - fit_s) / (block * blocks) * 1e6,
-                     "final_loading": traj[-1][1], "final_se": traj[-1][2],
-                     "insert_acceptance": float(acc[2] / max(att[2], 1)),
-                     "trajectory_s_loading": [(round(t, 2), round(m, 2)) for t, m, _ in traj[::4]]}
-        res[name]["_traj"] = traj
-    target = 0.95 * res["uniform"]["final_loading"]
-    for name in ("uniform", "learned"):
-        traj = res[name].pop("_traj")
-        t_hit = None
-        for (t0, m0, _), (t1, m1, _) in zip([(0.0, 0.0, 0.0)] + traj[:-1], traj):
-            if m1 >= target:
-                t_hit = t0 + (t1 - t0) * (target - m0) / max(m1 - m0, 1e-12)
-                break
-        res[name]["time_to_95pct_of_uniform_final_s"] = t_hit
-    tu, tl = (res[k]["time_to_95pct_of_uniform_final_s"] for k in ("uniform", "learned"))
-    res["speedup_learned_vs_uniform"] = (tu / tl) if (tu and tl) else None
-    res["note"] = ("neither method equilibrates within the run (the loading still rises); at this "
-                   "loading an insertion is accepted for few orientations, which a position-only "
-                   "proposal cannot raise, so the learned proposal does not speed up the loading")
-    return res
+            dt = time.perf_counter() - t0
+            fit_s += dt
+            t_total += dt
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ch.run(block)
+        torch.cuda.synchronize()
+        t_total += time.perf_counter() - t0
+        cur = np.array([ch.info(c)["sum_molecules"] for c in range(n)])
+        traj.append((t_total, (cur - prev) / block))
+        prev = cur
+        b += 1
+    att = np.array([ch.info(c)["attempted"] for c in range(n)]).sum(0)
+    acc = np.array([ch.info(c)["accepted"] for c in range(n)]).sum(0)
+    return {"traj": traj, "fit_seconds": fit_s, "moves_per_chain": block * b,
+            "insert_acceptance": float(acc[2] / max(att[2], 1)),
+            "delete_acceptance": float(acc[3] / max(att[3], 1))}
+
+
+def loading_metrics(traj, ref, n):
+    """For each block end t: the loading estimate over the second half of the
+    blocks so far (the first half discarded as burn-in) and its standard error
+    over the independent chains. Time to 1 %: the first t at which the
+    estimate is within 1 % of the reference loading `ref` and its standard
+    error is at most 1 % of it."""
+    t_hit, est = None, None
+    for k in range(1, len(traj) + 1):
+        half = traj[k // 2:k]
+        per_chain = np.mean([m for _, m in half], axis=0)
+        est = float(per_chain.mean())
+        se = float(per_chain.std(ddof=1) / np.sqrt(n))
+        if t_hit is None and abs(est - ref) <= 0.01 * ref and se <= 0.01 * ref:
+            t_hit = traj[k - 1][0]
+    return t_hit, est
+
+
+def loading_comparison(A, torch, pressures_bar=(0.1, 1.0, 10.0, 30.0), seconds=30.0, n=152,
+                       orient=1):
+    """GCMC loading, learned proposal against uniform insertion, on the C4
+    workload at each pressure: both arms run for the same wall time from an
+    empty cell; the reference loading is the mean over both arms' last quarter
+    of blocks (their final estimates agree within their standard errors when
+    both have equilibrated); each arm's time to a 1 %-accurate loading with a
+    1 % standard error (loading_metrics) and the ratio."""
+    fw, ff, p, ew, guest, T, alpha, kmax = henry_setup(A)
+    widom = A.Widom(ff, p, fw.lattice, guest, T, ewald=ew, precision=A.FP32)
+    out = {"workload": "charged 424-atom cubic cell, rigid CO2, Ewald 1e-6, 298 K, FP32 chains, "
+                       f"{n} chains per arm from an empty cell, {seconds:.0f} s per arm",
+           "orientation_trials": orient}
+    for P_bar in pressures_bar:
+        res = {}
+        for learned in (False, True):
+            prop = None
+            if learned:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                pr = fit_proposal(A, widom)
+                torch.cuda.synchronize()
+                prop = (pr, time.perf_counter() - t0)
+            res["learned" if learned else "uniform"] = loading_run(
+                A, torch, ff, p, fw, guest, ew, T, P_bar * 1e5, learned, seconds, n=n,
+                proposal=prop, orient=orient)
+        tail = [m for arm in res.values() for _, m in arm["traj"][-max(1, len(arm["traj"]) // 4):]]
+        ref = float(np.mean(tail))
+        row = {"reference_loading": ref}
+        for name, arm in res.items():
+            t_hit, est = loading_metrics(arm["traj"], ref, n)
+            traj = arm.pop("traj")
+            arm.update(time_to_1pct_s=t_hit, final_estimate=est,
+                       trajectory=[(round(t, 2), round(float(m.mean()), 2)) for t, m in traj[::3]])
+            row[name] = arm
+        tu, tl = row["uniform"]["time_to_1pct_s"], row["learned"]["time_to_1pct_s"]
+        row["speedup"] = (tu / tl) if (tu and tl) else None
+        out[f"{P_bar:g} bar"] = row
+    return out
 
 
 def kernel_case(case):

@@ -583,6 +583,17 @@ alea_status alea_gcmc_set_grid(alea_gcmc* g, const alea_grid* grid);
  * its deltaU, U_tail being tailEnergyCorrection over every particle of the
  * chain (framework and guests). Off by default. */
 alea_status alea_gcmc_set_tail_correction(alea_gcmc* g, int32_t on);
+/* Orientation-biased insertion and deletion of multi-site molecules (no
+ * counterpart in the reference engine, which inserts with one random
+ * orientation, monte_carlo_engine.cc:572-579): with k > 1 an insertion
+ * evaluates k random orientations about the drawn centroid, keeps one with
+ * probability exp(-dU_j/T) / W and is accepted with W / k in place of
+ * exp(-dU/T) (gcmc_acceptance.hpp:28-44); a deletion evaluates the molecule's
+ * own orientation and k - 1 random ones about its centroid and uses k / W in
+ * place of exp(+U/T). Composes with the learned proposal (the centroid's
+ * density) and the tail correction. k = 1 (the default) is the reference's
+ * move; 1 <= k <= 16. */
+alea_status alea_gcmc_set_orientation_trials(alea_gcmc* g, int32_t k);
 /* The same for Widom insertions: every trial's deltaU gains the constant
  * U_tail(framework + molecule) - U_tail(framework), written to *du_tail (may
  * be NULL) whatever `on` is; K_H is multiplied by exp(-du_tail / T). Single

@@ -32,3 +32,22 @@ def test_chunks_combine_to_the_whole_stream():
     assert abs(comb["log_mean_weight"] - whole["log_mean_weight"]) <= 1e-12 * abs(whole["log_mean_weight"])
     assert abs(comb["henry"] / (np.exp(whole["log_mean_weight"]) / 298.0) - 1.0) <= 1e-12
     assert abs(comb["rel_std_error"] / whole["rel_std_error"] - 1.0) <= 1e-9
+
+
+def test_loading_time_to_one_percent():
+    """The running estimate (second half of the blocks so far) first within
+    1 % of the reference with a 1 % standard error: a chain set that fills
+    up over 10 blocks, then fluctuates about 100 molecules."""
+    rng = np.random.default_rng(0)
+    n = 64
+    traj = []
+    for b in range(60):
+        level = 100.0 * min(1.0, (b + 1) / 10.0)
+        traj.append((0.5 * (b + 1), level + rng.normal(0.0, 3.0, n)))
+    t_hit, est = bench.loading_metrics(traj, 100.0, n)
+    # 18 blocks: the second half (blocks 9-17) is all filled; 17 blocks still
+    # hold the 90 % block 8
+    assert t_hit == 9.0
+    assert abs(est - 100.0) <= 0.5
+    # never within 1 % of a wrong reference
+    assert bench.loading_metrics(traj, 120.0, n)[0] is None
