@@ -61,7 +61,13 @@ struct PairCloseFF {
 
 // pairEnergy (lennard_jones.cc:70-86) in double-float from r^2 (trunc: the
 // alea truncation code; the shift is 0 for plain truncation).
+// r^2 is clamped from below at 1e-4 sigma^2 (r >= 0.01 sigma): closer, (sigma/r)^12
+// would overflow FP32 and the double-float products turn inf - inf into NaN. The
+// clamped energy is still above 1e26 K, so its Boltzmann factor is 0 as the exact
+// one is, and every acceptance decision and weight is unchanged.
 __device__ __forceinline__ ff lj_close_ff(const PairCloseFF& q, ff rr, float rcf, int trunc) {
+    const float floor2 = 1e-4f * q.sig2h;
+    if (!(rr.hi >= floor2)) rr = ff{floor2, 0.f};
     const ff s2 = ff_mul(ff{q.sig2h, q.sig2l}, ff_rcp(rr));
     const ff s6 = ff_mul(ff_mul(s2, s2), s2);
     ff e = ff_mul(ff{q.eps4h, q.eps4l}, ff_mul(s6, ff_add(s6, ff{-1.f, 0.f})));

@@ -925,7 +925,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                             }
                         }
                         if (el_in) {
-                            const float r = sqrtf(r2);
+                            const float r = sqrtf(fmaxf(r2, 1e-12f));  // finite at coincidence
                             accf[2 * e + 1] += qa * (erfcf(alphaf * r) / r);
                         }
                     }

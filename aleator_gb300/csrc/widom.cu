@@ -346,7 +346,7 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                         lj_acc += e;
                     }
                     if ((Q && P.charged) && r2 <= rce2f) {
-                        const float rf = sqrtf(r2);
+                        const float rf = sqrtf(fmaxf(r2, 1e-12f));  // finite at coincidence
                         es_acc += ah.w * (erfcf(alphaf * rf) / rf);
                     }
                 }

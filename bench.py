@@ -288,7 +288,7 @@ def main():
     ap.add_argument("--loading", type=float, default=None, metavar="SECONDS",
                     help="the C4 loading comparison at 0.1, 1, 10 and 30 bar, SECONDS per arm, "
                          "one JSON line (no bench line)")
-    ap.add_argument("--orientation-trials", type=int, default=1)
+    ap.add_argument("--orientation-trials", type=int, default=6)
     ap.add_argument("--kernel-case", default=None, choices=["gcmc", "widom", "interp", "ewald"],
                     help="one small case of a non-grid kernel for profiler captures, then exit "
                          "(no bench line)")
@@ -302,7 +302,9 @@ def main():
         import aleator_gb300 as A
         A.load_library()
         print(json.dumps(loading_comparison(A, torch, seconds=args.loading,
-                                            orient=args.orientation_trials)), flush=True)
+                                            orient=args.orientation_trials,
+                                            arms=("uniform", "uniform_orient", "learned"))),
+              flush=True)
         return 0
     if args.henry_judge:
         import torch
@@ -560,7 +562,7 @@ def henry_time_to_1pct(A, torch, gcmc=True, cap_s=60.0):
         "henry_difference_in_combined_se": abs(learned["henry"] - uniform["henry"]) / se,
     }
     if gcmc:
-        out["gcmc_loading"] = loading_comparison(A, torch, pressures_bar=(10.0,), seconds=12.0)
+        out["gcmc_loading"] = loading_comparison(A, torch, pressures_bar=(10.0,), seconds=15.0)
     return out
 
 
@@ -651,13 +653,16 @@ def loading_metrics(traj, ref, n):
 
 
 def loading_comparison(A, torch, pressures_bar=(0.1, 1.0, 10.0, 30.0), seconds=30.0, n=152,
-                       orient=1):
-    """GCMC loading, learned proposal against uniform insertion, on the C4
-    workload at each pressure: both arms run for the same wall time from an
-    empty cell; the reference loading is the mean over both arms' last quarter
-    of blocks (their final estimates agree within their standard errors when
-    both have equilibrated); each arm's time to a 1 %-accurate loading with a
-    1 % standard error (loading_metrics) and the ratio."""
+                       orient=6, arms=("uniform", "learned")):
+    """GCMC loading on the C4 workload at each pressure, the learned form
+    (learned insertion proposal and `orient` orientation trials per insertion
+    and deletion) against the reference's moves (uniform insertion, one
+    orientation); arm "uniform_orient" adds the orientation trials alone. All
+    arms run for the same wall time from an empty cell; the reference loading
+    is the mean over the arms' last quarter of blocks (their final estimates
+    agree within their standard errors when they have equilibrated); each
+    arm's time to a 1 %-accurate loading with a 1 % standard error
+    (loading_metrics), and the ratio uniform / learned."""
     fw, ff, p, ew, guest, T, alpha, kmax = henry_setup(A)
     widom = A.Widom(ff, p, fw.lattice, guest, T, ewald=ew, precision=A.FP32)
     out = {"workload": "charged 424-atom cubic cell, rigid CO2, Ewald 1e-6, 298 K, FP32 chains, "
@@ -665,7 +670,8 @@ def loading_comparison(A, torch, pressures_bar=(0.1, 1.0, 10.0, 30.0), seconds=3
            "orientation_trials": orient}
     for P_bar in pressures_bar:
         res = {}
-        for learned in (False, True):
+        for arm in arms:
+            learned = arm == "learned"
             prop = None
             if learned:
                 torch.cuda.synchronize()
@@ -673,9 +679,8 @@ def loading_comparison(A, torch, pressures_bar=(0.1, 1.0, 10.0, 30.0), seconds=3
                 pr = fit_proposal(A, widom)
                 torch.cuda.synchronize()
                 prop = (pr, time.perf_counter() - t0)
-            res["learned" if learned else "uniform"] = loading_run(
-                A, torch, ff, p, fw, guest, ew, T, P_bar * 1e5, learned, seconds, n=n,
-                proposal=prop, orient=orient)
+            res[arm] = loading_run(A, torch, ff, p, fw, guest, ew, T, P_bar * 1e5, learned, seconds,
+                                   n=n, proposal=prop, orient=1 if arm == "uniform" else orient)
         tail = [m for arm in res.values() for _, m in arm["traj"][-max(1, len(arm["traj"]) // 4):]]
         ref = float(np.mean(tail))
         row = {"reference_loading": ref}
