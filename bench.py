@@ -289,7 +289,7 @@ def main():
                     help="the C4 loading comparison at 0.1, 1, 10 and 30 bar, SECONDS per arm, "
                          "one JSON line (no bench line)")
     ap.add_argument("--orientation-trials", type=int, default=6)
-    ap.add_argument("--kernel-case", default=None, choices=["gcmc", "widom", "interp", "ewald"],
+    ap.add_argument("--kernel-case", default=None, choices=["gcmc", "gcmc_c5", "widom", "widom_q32", "interp", "ewald"],
                     help="one small case of a non-grid kernel for profiler captures, then exit "
                          "(no bench line)")
     args = ap.parse_args()
@@ -705,6 +705,11 @@ def kernel_case(case):
               trials (kMax 10);
       interp: 2^24 random queries on the FP32-form grid of the 2x2x2 supercell
               (0.2 A, 174 MB table), then the same on its FP64-form grid;
+      widom_q32: charged CO2 in the charged 424-atom cell (kMax 10), FP32 form:
+              2^16 then 2^18 trials;
+      gcmc_c5: the large isotherm case (64 FP32 chains of charged CO2 in the
+              27 008-atom supercell with its 0.2 A grid, kMax 34), a 200-move
+              launch then a 100-move launch;
       ewald:  the EwaldIncrementalState of the charged 2x2x2 supercell (3 376
               atoms, alpha and kMax for 1e-6, rc 12 A): the S(k) build, then 8
               CO2 insertion proposals and commits (6 sites per move proposal)."""
@@ -731,6 +736,28 @@ def kernel_case(case):
         alpha, kmax = W.ewald_parameters(fq.lattice, 12.0)
         A.Widom(A.LennardJones(fq.eps, fq.sigma, 12.8, A.SHIFTED), A.ParticleData.from_framework(fq),
                 fq.lattice, W.co2_guest(fq), 298.0, ewald=A.Ewald(alpha, 12.0, kmax)).run(42, 0, 1 << 16)
+    elif case == "widom_q32":
+        fq = W.cubic_framework(charged=True)
+        alpha, kmax = W.ewald_parameters(fq.lattice, 12.0)
+        w = A.Widom(A.LennardJones(fq.eps, fq.sigma, 12.8, A.SHIFTED), A.ParticleData.from_framework(fq),
+                    fq.lattice, W.co2_guest(fq), 298.0, ewald=A.Ewald(alpha, 12.0, kmax),
+                    precision=A.FP32)
+        w.run(42, 0, 1 << 16)
+        w.run(42, 0, 1 << 18)
+    elif case == "gcmc_c5":
+        fw, guests = make_workload()
+        alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
+        ff = A.LennardJones(fw.eps, fw.sigma, CUTOFF, A.SHIFTED)
+        p = A.ParticleData.from_framework(fw)
+        grid = A.FrameworkEnergyGrid(ff, p, fw.lattice, guests, SPACING, A.FP32)
+        pressures = np.logspace(np.log10(0.01), np.log10(50.0), 64)
+        fugs = [A.peng_robinson_fugacity(*W.CO2_CRITICAL, 298.0, P * 1e5) for P in pressures]
+        ch = A.GcmcChains(ff, p, fw.lattice, W.co2_guest(fw), 298.0, fugs, list(range(64)),
+                          list(range(64)), ewald=A.Ewald(alpha, 12.0, kmax), max_molecules=4000,
+                          precision=A.FP32)
+        ch.set_grid(grid)
+        ch.run(200)
+        ch.run(100)
     elif case == "ewald":
         fw = W.triclinic_supercell(reps=2)
         alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
