@@ -31,6 +31,10 @@ namespace alea {
 namespace {
 
 constexpr int WT = 128;        // trials per block
+// FP32 form, charged trials: Coulomb pairs closer than 4.5 A are evaluated in
+// FP64 (closer, a pair's real-space term reaches 1e4-1e5 K, where FP32's ~1e-7
+// relative rounding would leave ~1e-2 K)
+constexpr float NEAR_COULOMB_R2 = 20.25f;
 constexpr int ATILE = 512;     // framework atoms per shared-memory tile
 constexpr int MAXS = 8;        // sites per guest molecule
 constexpr int MAXT = 64;       // LJ species
@@ -88,13 +92,14 @@ __device__ __forceinline__ void cross_rn(const double* a, const double* b, doubl
 // Device data of one Widom context.
 struct WidomPtrs {
     const double4* atoms;
-    const float4* atoms32;  // FP32 form: per atom {x, y, z hi, charge}, {x, y, z lo, 0}
+    const float4* atoms32;  // FP32 form: per atom {x, y, z, charge} hi, then lo
     const uint32_t* types;
     const PairParams* table;
     const KRow* rows;
     const double* w;
     const double* sre;
     const double* sim;
+    const float4* swk32;  // FP32 form: per term {w hi, w lo, Re S hi, lo}, {Im S hi, lo, 0, 0}
 };
 
 // One block of WT trials: trials first + block WT + threadIdx.x; writes the
@@ -242,7 +247,7 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
         for (int s = 0; s < MAXS; ++s) {
             if (s >= ns) break;
             Real lj_acc = 0, es_acc = 0;
-            double lj_close = 0.0;
+            double lj_close = 0.0, es_near = 0.0;
             if constexpr (sizeof(Real) == 8) {
                 for (int j = 0; j < cnt; ++j) {
                     const double4 a = tile[j];
@@ -346,14 +351,23 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                         lj_acc += e;
                     }
                     if ((Q && P.charged) && r2 <= rce2f) {
-                        const float rf = sqrtf(fmaxf(r2, 1e-12f));  // finite at coincidence
-                        es_acc += ah.w * (erfcf(alphaf * rf) / rf);
+                        if (r2 < NEAR_COULOMB_R2) {
+                            // a near pair: in FP64 from the double-float
+                            // displacement and charge
+                            const double ddx = (double)dx.hi + dx.lo, ddy = (double)dy.hi + dy.lo,
+                                         ddz = (double)dz.hi + dz.lo;
+                            const double rd = fmax(sqrt(ddx * ddx + ddy * ddy + ddz * ddz), 1e-6);
+                            es_near += ((double)ah.w + (double)al.w) * (erfc(P.alpha * rd) / rd);
+                        } else {
+                            const float rf = sqrtf(r2);
+                            es_acc += ah.w * (erfcf(alphaf * rf) / rf);
+                        }
                     }
                 }
                 lj_close = (double)close_acc.hi + (double)close_acc.lo;
             }
             lj_site[s] += (double)lj_acc + lj_close;
-            es_site[s] += (double)es_acc;
+            es_site[s] += (double)es_acc + es_near;
         }
     }
     double du = 0.0;
@@ -368,6 +382,97 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
             if (s < ns) e += (P.site[s].q * es_site[s]) * kCoulomb;
         du += e;
         // ---- reciprocal delta against the framework S(k)
+        double acc = 0.0;
+        if constexpr (sizeof(Real) == 4) {
+            // FP32 form: the trial's phases, the framework's S(k) and the
+            // weights as double-float (hi + lo FP32 pairs, ~48 bits) on the FP32
+            // pipe: each row's start phase and the step e^{i theta_2} from an
+            // FP64 sincos, one double-float complex rotation per term and site
+            // along the row; each row's terms summed in double-float, the rows
+            // in FP64. (Plain FP32 phases leave ~1e-7 relative per term, which
+            // the strongly charged frameworks' |S(k)| turns into ~1e-2 K.)
+            double th[MAXS][3];
+            ff qf[MAXS], c1f[MAXS], s1f[MAXS], c2f[MAXS], s2f[MAXS];
+            ff rc[MAXS], rs[MAXS];  // the previous row's start phase
+            const float4* __restrict__ swk = D.swk32;
+#pragma unroll
+            for (int s = 0; s < MAXS; ++s) {
+                if (s >= ns) break;
+                for (int i = 0; i < 3; ++i)
+                    th[s][i] = P.b[3 * i] * sx[s] + P.b[3 * i + 1] * sy[s] + P.b[3 * i + 2] * sz[s];
+                double sn, cs;
+                sincos(th[s][2], &sn, &cs);
+                s2f[s] = ff_from(sn);
+                c2f[s] = ff_from(cs);
+                sincos(th[s][1], &sn, &cs);
+                s1f[s] = ff_from(sn);
+                c1f[s] = ff_from(cs);
+                qf[s] = ff_from(P.site[s].q);
+            }
+            // (c, s) *= e^{i sign theta}, theta given by its (cos, sin)
+            auto rotate = [](ff& c, ff& s, const ff& ct, const ff& st, bool neg) {
+                const ff a = ff_mul(s, st), b = ff_mul(c, st);
+                const ff cc = ff_mul(c, ct), sc = ff_mul(s, ct);
+                c = neg ? ff_add(cc, a) : ff_add(cc, ff{-a.hi, -a.lo});
+                s = neg ? ff_add(sc, ff{-b.hi, -b.lo}) : ff_add(sc, b);
+            };
+            int prev_n0 = -(1 << 30), prev_n1 = 0, prev_m = 0;
+            for (int r = 0; r < P.n_rows; ++r) {
+                const KRow kr = rows[r];
+                ff pc[MAXS], ps[MAXS];
+                // the row's start phase n0 th0 + n1 th1 - m th2: from an FP64 sincos
+                // at the first row of each n0, else the previous row's advanced by
+                // e^{i th1} and (m - m_prev) steps of e^{-i th2}, in double-float
+                const bool chain = kr.n0 == prev_n0 && kr.n1 == prev_n1 + 1;
+#pragma unroll
+                for (int s = 0; s < MAXS; ++s) {
+                    if (s >= ns) break;
+                    if (!chain) {
+                        double sn, cs;
+                        sincos(kr.n0 * th[s][0] + kr.n1 * th[s][1] - kr.m * th[s][2], &sn, &cs);
+                        rs[s] = ff_from(sn);
+                        rc[s] = ff_from(cs);
+                    } else {
+                        rotate(rc[s], rs[s], c1f[s], s1f[s], false);
+                        for (int d = prev_m; d < kr.m; ++d) rotate(rc[s], rs[s], c2f[s], s2f[s], true);
+                        for (int d = kr.m; d < prev_m; ++d) rotate(rc[s], rs[s], c2f[s], s2f[s], false);
+                    }
+                    pc[s] = rc[s];
+                    ps[s] = rs[s];
+                }
+                prev_n0 = kr.n0;
+                prev_n1 = kr.n1;
+                prev_m = kr.m;
+                int t = kr.t0;
+                ff racc{0.f, 0.f};
+                for (int n2 = -kr.m; n2 <= kr.m; ++n2) {
+                    if (!(kr.n0 == 0 && kr.n1 == 0 && n2 == 0)) {
+                        ff re{0.f, 0.f}, im{0.f, 0.f};
+#pragma unroll
+                        for (int s = 0; s < MAXS; ++s) {
+                            if (s >= ns) break;
+                            re = ff_add(re, ff_mul(qf[s], pc[s]));
+                            im = ff_add(im, ff_mul(qf[s], ps[s]));
+                        }
+                        const float4 o1 = __ldg(&swk[2 * t]);      // {w, Re S} hi, lo
+                        const float4 o2 = __ldg(&swk[2 * t + 1]);  // {Im S} hi, lo
+                        const ff dot = ff_add(ff_mul(ff{o1.z, o1.w}, re), ff_mul(ff{o2.x, o2.y}, im));
+                        const ff d2 = ff_add(ff_mul(re, re), ff_mul(im, im));
+                        racc = ff_add(racc, ff_mul(ff{o1.x, o1.y}, ff_add(ff_add(dot, dot), d2)));
+                        ++t;
+                    }
+#pragma unroll
+                    for (int s = 0; s < MAXS; ++s) {
+                        if (s >= ns) break;
+                        const ff a = ff_mul(ps[s], s2f[s]);
+                        const ff c = ff_add(ff_mul(pc[s], c2f[s]), ff{-a.hi, -a.lo});
+                        ps[s] = ff_add(ff_mul(ps[s], c2f[s]), ff_mul(pc[s], s2f[s]));
+                        pc[s] = c;
+                    }
+                }
+                acc += (double)racc.hi + (double)racc.lo;
+            }
+        } else {
         double th[MAXS][3], cs2[MAXS], sn2[MAXS];
 #pragma unroll
         for (int s = 0; s < MAXS; ++s) {
@@ -376,7 +481,6 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                 th[s][i] = P.b[3 * i] * sx[s] + P.b[3 * i + 1] * sy[s] + P.b[3 * i + 2] * sz[s];
             sincos(th[s][2], &sn2[s], &cs2[s]);
         }
-        double acc = 0.0;
         for (int r = 0; r < P.n_rows; ++r) {
             const KRow kr = rows[r];
             double pc[MAXS], ps[MAXS];
@@ -410,6 +514,7 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                 }
             }
         }
+        }  // FP64 form
         double q2 = 0.0, ex = 0.0;
         for (int i = 0; i < ns; ++i) {
             q2 += P.site[i].q * P.site[i].q;
@@ -565,6 +670,7 @@ struct WidomImpl {
     DevBuf<PairParams> table;
     DevBuf<KRow> rows;
     EwaldStateImpl* ews = nullptr;
+    DevBuf<float4> swk32;            // FP32 form: per term {w, Re S} and {Im S} as hi, lo
     DevBuf<double> partial, result, per_trial, per_trial_frac;
     WidomItem item_h{};
     DevBuf<WidomItem> item;          // the context as a batch of one
@@ -678,9 +784,10 @@ WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
         if (precision == ALEA_FP32) {  // the atoms as double-float, split here once
             std::vector<float4> split(2 * fw.n);
             for (uint64_t i = 0; i < fw.n; ++i) {
-                const ff x = ff_from(packed[i].x), y = ff_from(packed[i].y), z = ff_from(packed[i].z);
-                split[2 * i] = make_float4(x.hi, y.hi, z.hi, (float)packed[i].w);
-                split[2 * i + 1] = make_float4(x.lo, y.lo, z.lo, 0.f);
+                const ff x = ff_from(packed[i].x), y = ff_from(packed[i].y), z = ff_from(packed[i].z),
+                         q = ff_from(packed[i].w);
+                split[2 * i] = make_float4(x.hi, y.hi, z.hi, q.hi);
+                split[2 * i + 1] = make_float4(x.lo, y.lo, z.lo, q.lo);
             }
             w->atoms32.alloc(std::max<size_t>(2 * fw.n, 2));
             w->atoms32.upload(split.data(), 2 * fw.n);
@@ -716,6 +823,20 @@ WidomImpl* widom_create(const alea_lennard_jones& lj, const alea_ewald* ew,
                 }
             require((uint64_t)t == v.nk, ALEA_ERR_RUNTIME, "Widom: k-row table mismatch");
             P.n_rows = (int)rows.size();
+            if (precision == ALEA_FP32 && v.nk) {
+                std::vector<double> hw(v.nk), hre(v.nk), him(v.nk);
+                ALEA_CUDA(cudaMemcpy(hw.data(), v.w, v.nk * sizeof(double), cudaMemcpyDeviceToHost));
+                ALEA_CUDA(cudaMemcpy(hre.data(), v.sre, v.nk * sizeof(double), cudaMemcpyDeviceToHost));
+                ALEA_CUDA(cudaMemcpy(him.data(), v.sim, v.nk * sizeof(double), cudaMemcpyDeviceToHost));
+                std::vector<float4> pk(2 * v.nk);
+                for (uint64_t i = 0; i < v.nk; ++i) {
+                    const ff a = ff_from(hw[i]), b = ff_from(hre[i]), c = ff_from(him[i]);
+                    pk[2 * i] = make_float4(a.hi, a.lo, b.hi, b.lo);
+                    pk[2 * i + 1] = make_float4(c.hi, c.lo, 0.f, 0.f);
+                }
+                w->swk32.alloc(2 * v.nk);
+                w->swk32.upload(pk.data(), 2 * v.nk);
+            }
         }
         w->rows.alloc(std::max<size_t>(rows.size(), 1));
         w->rows.upload(rows.data(), rows.size());
@@ -762,7 +883,8 @@ static void widom_launch(WidomImpl* w, uint64_t seed, uint64_t stream, uint64_t 
         sre = v.sre;
         sim = v.sim;
     }
-    it.D = WidomPtrs{w->atoms.p, w->atoms32.p, w->types.p, w->table.p, w->rows.p, wk, sre, sim};
+    it.D = WidomPtrs{w->atoms.p, w->atoms32.p, w->types.p, w->table.p, w->rows.p, wk, sre, sim,
+                     w->swk32.p};
     it.seed = seed;
     it.stream = stream;
     it.first = first;
@@ -920,7 +1042,8 @@ void widom_batch_run(WidomBatchImpl* b, const uint64_t* seeds, const uint64_t* s
         }
         WidomItem& it = b->items_h[i];
         it.P = w->P;
-        it.D = WidomPtrs{w->atoms.p, w->atoms32.p, w->types.p, w->table.p, w->rows.p, wk, sre, sim};
+        it.D = WidomPtrs{w->atoms.p, w->atoms32.p, w->types.p, w->table.p, w->rows.p, wk, sre, sim,
+                     w->swk32.p};
         it.seed = seeds[i];
         it.stream = streams[i];
         it.first = first;

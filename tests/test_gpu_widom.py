@@ -128,3 +128,28 @@ def test_fp32_uncharged_triclinic_vs_fp64(lib, trunc):
         assert rel_err(per32[keep], per64[keep], floor=KT).max() <= 1e-5, (i, trunc)
         assert abs(r32["henry"] / r64["henry"] - 1) <= 1e-5
     assert checked >= 2
+
+
+def test_fp32_charged_c4_per_trial_vs_fp64(lib):
+    """The FP32 form on the learned-proposal workload (charged 424-atom cell,
+    charges up to 1.2 e, rigid CO2, Ewald for 1e-6 with kMax 10), 65 536 trials:
+    per trial within 1e-5 x max(kT, |dU|) of the FP64 form on trials that carry
+    Boltzmann weight (dU <= 1e4 K), and K_H within 1e-5. Its reciprocal phases
+    are double-float and its Coulomb pairs within 4.5 A FP64: with FP32 phases
+    or FP32 near pairs this workload's errors reach ~5e-5 of kT."""
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    fw = W.cubic_framework(charged=True)
+    alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    ew = A.Ewald(alpha, 12.0, kmax)
+    out = {}
+    for prec in (A.FP64, A.FP32):
+        w = A.Widom(ff, p, fw.lattice, W.co2_guest(fw), 298.0, ewald=ew, precision=prec)
+        out[prec] = w.run(7, 3, 1 << 16, per_trial=True)
+    (r64, d64), (r32, d32) = out[A.FP64], out[A.FP32]
+    keep = d64 <= 1e4
+    assert keep.sum() > 1000
+    assert rel_err(d32[keep], d64[keep], floor=KT).max() <= 1e-5
+    assert abs(r32["henry"] / r64["henry"] - 1) <= 1e-5
