@@ -60,6 +60,9 @@ constexpr float NEAR_R2 = 6.0f * 6.0f;
 // the near sphere under 1 % of the cell: 100 x (4/3) pi 6^3 A^3
 constexpr double FIXED_FAR_VOLUME = 100.0 * 4.0 / 3.0 * 3.14159265358979 * 216.0;
 constexpr float CUT_BAND = 1e-5f;
+// FP32 form: Coulomb pairs closer than 4.5 A in FP64 (closer, a pair's
+// real-space term reaches 1e4-1e5 K, where FP32 rounding would leave ~1e-2 K)
+constexpr float NEAR_COULOMB_R2 = 20.25f;
 constexpr int MAXROWS = 8;  // distinct LJ species among the guest sites
 constexpr int MAXCB = 16;   // orientation trials of a biased insertion or deletion
 
@@ -547,9 +550,9 @@ __host__ __device__ __forceinline__ uint4 fixed_frac(const Lattice& L, double x,
 // form's inputs).
 __device__ __forceinline__ void put_hilo(const Lattice& L, float4* ghi, float4* glo, uint4* gq4,
                                          uint32_t slot, const double* p, double q) {
-    const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
-    ghi[slot] = make_float4(x.hi, y.hi, z.hi, (float)q);
-    glo[slot] = make_float4(x.lo, y.lo, z.lo, 0.f);
+    const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]), qq = ff_from(q);
+    ghi[slot] = make_float4(x.hi, y.hi, z.hi, qq.hi);
+    glo[slot] = make_float4(x.lo, y.lo, z.lo, qq.lo);
     gq4[slot] = fixed_frac(L, p[0], p[1], p[2]);
 }
 
@@ -849,10 +852,14 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 // few FP32 partials are added in FP64 by the block sum
                 float accf[4 * NS];
                 ff closef[2 * NS];  // pairs closer than sigma, double-float
+                double near_el[2 * NS];  // Coulomb pairs within 4.5 A, FP64
 #pragma unroll
                 for (int e = 0; e < 4 * NS; ++e) accf[e] = 0.f;
 #pragma unroll
-                for (int e = 0; e < 2 * NS; ++e) closef[e] = ff{0.f, 0.f};
+                for (int e = 0; e < 2 * NS; ++e) {
+                    closef[e] = ff{0.f, 0.f};
+                    near_el[e] = 0.0;
+                }
                 const float rc2f = (float)C.rc2, rcf = (float)C.rc, rce2f = (float)C.rc_ew2,
                             alphaf = (float)C.alpha;
                 for (uint64_t j = j0 + threadIdx.x; j < n_all; j += GT) {
@@ -925,8 +932,17 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                             }
                         }
                         if (el_in) {
-                            const float r = sqrtf(fmaxf(r2, 1e-12f));  // finite at coincidence
-                            accf[2 * e + 1] += qa * (erfcf(alphaf * r) / r);
+                            if (r2 < NEAR_COULOMB_R2) {
+                                // a near pair (its real-space term reaches 1e4-1e5 K):
+                                // in FP64 from the double-float displacement and charge
+                                const double ddx = (double)dx.hi + dx.lo, ddy = (double)dy.hi + dy.lo,
+                                             ddz = (double)dz.hi + dz.lo;
+                                const double rd = fmax(sqrt(ddx * ddx + ddy * ddy + ddz * ddz), 1e-6);
+                                near_el[e] += ((double)ah.w + (double)al.w) * (erfc(C.alpha * rd) / rd);
+                            } else {
+                                const float r = sqrtf(r2);
+                                accf[2 * e + 1] += qa * (erfcf(alphaf * r) / r);
+                            }
                         }
                     }
                 }
@@ -935,7 +951,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
 #pragma unroll
                 for (int e = 0; e < 2 * NS; ++e) {
                     v[2 * e] = ff_add_f(closef[e], accf[2 * e]);
-                    v[2 * e + 1] = ff{accf[2 * e + 1], 0.f};
+                    v[2 * e + 1] = ff_add(ff_from(near_el[e]), ff{accf[2 * e + 1], 0.f});
                 }
                 if (C.grid) {  // thread e adds site slot e's interpolated table
 #pragma unroll
@@ -1614,9 +1630,10 @@ GcmcImpl* gcmc_create(const alea_lennard_jones& lj, const alea_ewald* ew, const 
         {
             std::vector<float4> h(fw.n), l(fw.n);
             for (uint64_t i = 0; i < fw.n; ++i) {
-                const ff x = ff_from(packed[i].x), y = ff_from(packed[i].y), z = ff_from(packed[i].z);
-                h[i] = make_float4(x.hi, y.hi, z.hi, (float)packed[i].w);
-                l[i] = make_float4(x.lo, y.lo, z.lo, 0.f);
+                const ff x = ff_from(packed[i].x), y = ff_from(packed[i].y), z = ff_from(packed[i].z),
+                         q = ff_from(packed[i].w);
+                h[i] = make_float4(x.hi, y.hi, z.hi, q.hi);
+                l[i] = make_float4(x.lo, y.lo, z.lo, q.lo);
             }
             g->fwh.alloc(std::max<size_t>(fw.n, 1));
             g->fwl.alloc(std::max<size_t>(fw.n, 1));
