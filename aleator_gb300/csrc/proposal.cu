@@ -8,12 +8,11 @@
 // s in [0, 1)^3 -> 2 n_freq periodic features (sin, cos)(2 pi k_j . s) with
 // integer wave vectors k_j -> depth hidden layers of `width` with SiLU ->
 // one output f(s), an unnormalised log-density. Weights are rounded to BF16
-// (the copy the kernels read) from FP32 master weights that Adam updates. The
-// hidden layers' products run on the tensor cores (mma.sync m16n8k16, BF16
-// operands, FP32 accumulation): the features, the post-SiLU activations and
-// the back-propagated pre-activation gradients are stored in BF16, the
-// pre-activations in FP32 (for SiLU'); the one-unit output layer, the loss and
-// Adam stay in FP32 on the CUDA cores.
+// (the copy the kernels read) from FP32 master weights that Adam updates;
+// activations and gradients are FP32. The hidden layers' products run on the
+// tensor cores (mma.sync m16n8k16, BF16 operands, FP32 accumulation) with each
+// FP32 operand split into BF16 hi + lo parts (tc_gemm_kernel); the one-unit
+// output layer, the loss and Adam stay in FP32 on the CUDA cores.
 //
 // Training rows {s0, s1, s2, l, lq}: a position, its log-weight l = -dU/T and
 // the log density lq of the proposal it was drawn from (relative to uniform;
@@ -40,6 +39,7 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -139,28 +139,56 @@ gemm_kernel(int M, int N, int K, const AT* __restrict__ A, int lda, const BT* __
 }
 
 // ---------------------------------------------------------------- tensor-core GEMM
-// C[M x N] = op(A) op(B), BF16 operands, FP32 accumulation, with the same op()
-// convention and epilogues as gemm_kernel. A 64 x 64 tile per CTA of 4 warps
-// (each 32 x 32: 2 x 4 mma.sync m16n8k16), k-steps of 32 staged in shared
-// memory as As[m][k] and Bs[n][k] (k contiguous, whatever the operands' global
-// layout) and read into fragments with ldmatrix. EPI_STORE writes split-K
-// partials to C + z M ldc; with bpart, the CTAs of the first column of tiles
-// also write the row sums of op(A) over their k-slice to bpart[z M + m] (the
-// bias gradient when op(A) = dz^T).
+// C[M x N] = op(A) op(B) on the tensor cores (mma.sync m16n8k16, BF16 operands,
+// FP32 accumulation), with the same op() convention and epilogues as
+// gemm_kernel. An FP32 operand (the activations and gradients) is split into
+// BF16 hi + lo parts when it is staged, and its products are summed from
+// hi x hi, lo x hi and hi x lo MMAs: ~16 significant bits per operand, the
+// FP32 activations' precision for these sums; a BF16 operand (the weights,
+// which are BF16 by design) has no lo part. A 64 x 64 tile per CTA of 4 warps
+// (each 32 x 32: 2 x 4 MMA tiles), k-steps of 32 staged in shared memory as
+// As[m][k] and Bs[n][k] (k contiguous, whatever the global layout) and read
+// with ldmatrix. EPI_STORE writes split-K partials to C + z M ldc; with bpart,
+// the CTAs of the first column of tiles also write the row sums of op(A) over
+// their k-slice to bpart[z M + m] (the bias gradient when op(A) = dz^T).
 constexpr int TC_T = 64, TC_K = 32, TC_PAD = 8, TC_THREADS = 128;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-template <bool TA, bool TB, typename CT, int EPI>
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+    hi = __float2bfloat16_rn(x);
+    lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+__device__ __forceinline__ void split_bf16(__nv_bfloat16 x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+    hi = x;
+    lo = __float2bfloat16_rn(0.f);
+}
+
+__device__ __forceinline__ void ldm_x4(uint32_t (&r)[4], const __nv_bfloat16* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, "
+        "{%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+template <bool TA, bool TB, typename AT, typename BT, typename CT, int EPI>
 __global__ void __launch_bounds__(TC_THREADS)
-tc_gemm_kernel(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
-               const __nv_bfloat16* __restrict__ B, int ldb, CT* __restrict__ C, int ldc,
-               const float* __restrict__ bias, float* __restrict__ aux, int k_chunk,
-               float* __restrict__ bpart) {
-    __shared__ __align__(16) __nv_bfloat16 As[TC_T][TC_K + TC_PAD];
-    __shared__ __align__(16) __nv_bfloat16 Bs[TC_T][TC_K + TC_PAD];
+tc_gemm_kernel(int M, int N, int K, const AT* __restrict__ A, int lda, const BT* __restrict__ B,
+               int ldb, CT* __restrict__ C, int ldc, const float* __restrict__ bias,
+               float* __restrict__ aux, int k_chunk, float* __restrict__ bpart) {
+    constexpr bool SA = std::is_same<AT, float>::value;  // A has a lo part
+    constexpr bool SB = std::is_same<BT, float>::value;  // B has a lo part
+    __shared__ __align__(16) __nv_bfloat16 Ah[TC_T][TC_K + TC_PAD], Al[SA ? TC_T : 1][TC_K + TC_PAD];
+    __shared__ __align__(16) __nv_bfloat16 Bh[TC_T][TC_K + TC_PAD], Bl[SB ? TC_T : 1][TC_K + TC_PAD];
     __shared__ float brow[TC_T];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wm = warp >> 1, wn = warp & 1;  // this warp's 32 x 32 quarter
@@ -169,54 +197,66 @@ tc_gemm_kernel(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda
     const int ke = min(K, kb + k_chunk);
     const bool row_sums = bpart != nullptr && blockIdx.x == 0;
     float acc[2][4][4] = {};
-    float rs = 0.f;  // row sum of op(A) (thread tid < 64 owns row tid)
-    const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
+    float rs = 0.f;  // row sum of op(A) over the slice (thread tid < 64 owns row tid)
     for (int k0 = kb; k0 < ke; k0 += TC_K) {
-        // stage op(A)[m0.., k0..] as As[m][k] and op(B)[k0.., n0..] as Bs[n][k]
+        // stage op(A)[m0.., k0..] as A[m][k] and op(B)[k0.., n0..] as B[n][k]
         for (int e = tid; e < TC_T * TC_K; e += TC_THREADS) {
             int mm, kk;
             if (TA) { mm = e % TC_T; kk = e / TC_T; } else { kk = e % TC_K; mm = e / TC_K; }
             const int m = m0 + mm, k = k0 + kk;
-            As[mm][kk] = (m < M && k < ke) ? (TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k]) : zero;
+            const AT v = (m < M && k < ke) ? (TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k]) : AT(0.f);
+            __nv_bfloat16 hi, lo;
+            split_bf16(v, hi, lo);
+            Ah[mm][kk] = hi;
+            if constexpr (SA) Al[mm][kk] = lo;
         }
         for (int e = tid; e < TC_T * TC_K; e += TC_THREADS) {
             int nn, kk;
             if (TB) { kk = e % TC_K; nn = e / TC_K; } else { nn = e % TC_T; kk = e / TC_T; }
             const int n = n0 + nn, k = k0 + kk;
-            Bs[nn][kk] = (n < N && k < ke) ? (TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n]) : zero;
+            const BT v = (n < N && k < ke) ? (TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n]) : BT(0.f);
+            __nv_bfloat16 hi, lo;
+            split_bf16(v, hi, lo);
+            Bh[nn][kk] = hi;
+            if constexpr (SB) Bl[nn][kk] = lo;
         }
         __syncthreads();
-        if (row_sums && tid < TC_T)
-            for (int kk = 0; kk < TC_K; ++kk) rs += __bfloat162float(As[tid][kk]);
+        if (row_sums && tid < TC_T) {
+            const int m = m0 + tid;
+            if (m < M)
+                for (int k = k0; k < min(ke, k0 + TC_K); ++k)
+                    rs += to_f(TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k]);
+        }
 #pragma unroll
         for (int ks = 0; ks < TC_K; ks += 16) {
-            uint32_t a[2][4], b[4][2];
+            uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
-                const __nv_bfloat16* pa = &As[wm * 32 + i * 16 + (lane & 15)][ks + (lane >> 4) * 8];
-                asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
-                             : "=r"(a[i][0]), "=r"(a[i][1]), "=r"(a[i][2]), "=r"(a[i][3])
-                             : "r"(smem_u32(pa)));
+                const int r = wm * 32 + i * 16 + (lane & 15), c = ks + (lane >> 4) * 8;
+                ldm_x4(ah[i], &Ah[r][c]);
+                if constexpr (SA) ldm_x4(al[i], &Al[r][c]);
             }
 #pragma unroll
             for (int j = 0; j < 4; j += 2) {
                 // matrices: (n j8.., k ks), (n j8.., k ks+8), (n j8+8.., k ks), (n j8+8.., k ks+8)
                 const int r = wn * 32 + j * 8 + (lane & 7) + ((lane >> 4) << 3);
-                const __nv_bfloat16* pb = &Bs[r][ks + ((lane >> 3) & 1) * 8];
-                asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
-                             : "=r"(b[j][0]), "=r"(b[j][1]), "=r"(b[j + 1][0]), "=r"(b[j + 1][1])
-                             : "r"(smem_u32(pb)));
+                const int c = ks + ((lane >> 3) & 1) * 8;
+                uint32_t t[4];
+                ldm_x4(t, &Bh[r][c]);
+                bh[j][0] = t[0]; bh[j][1] = t[1]; bh[j + 1][0] = t[2]; bh[j + 1][1] = t[3];
+                if constexpr (SB) {
+                    ldm_x4(t, &Bl[r][c]);
+                    bl[j][0] = t[0]; bl[j][1] = t[1]; bl[j + 1][0] = t[2]; bl[j + 1][1] = t[3];
+                }
             }
 #pragma unroll
             for (int i = 0; i < 2; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    asm volatile(
-                        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, "
-                        "{%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
-                        : "+f"(acc[i][j][0]), "+f"(acc[i][j][1]), "+f"(acc[i][j][2]), "+f"(acc[i][j][3])
-                        : "r"(a[i][0]), "r"(a[i][1]), "r"(a[i][2]), "r"(a[i][3]), "r"(b[j][0]),
-                          "r"(b[j][1]));
+                for (int j = 0; j < 4; ++j) {
+                    mma_bf16(acc[i][j], ah[i], bh[j][0], bh[j][1]);
+                    if constexpr (SA) mma_bf16(acc[i][j], al[i], bh[j][0], bh[j][1]);
+                    if constexpr (SB) mma_bf16(acc[i][j], ah[i], bl[j][0], bl[j][1]);
+                }
         }
         __syncthreads();
     }
@@ -298,8 +338,7 @@ __global__ void colsum_part_kernel(const XT* __restrict__ X, int rows, int cols,
 // idx (optional) gathers rows: sample = idx ? idx(i) : i.
 __global__ void features_kernel(const float* __restrict__ samples, int stride, uint64_t n,
                                 uint64_t perm_a, uint64_t perm_c, uint64_t pool,
-                                const float* __restrict__ kvec, int nf,
-                                __nv_bfloat16* __restrict__ phi) {
+                                const float* __restrict__ kvec, int nf, float* __restrict__ phi) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t src = pool ? (perm_a * i + perm_c) % pool : i;
@@ -308,8 +347,8 @@ __global__ void features_kernel(const float* __restrict__ samples, int stride, u
         const float t = kvec[3 * j] * s[0] + kvec[3 * j + 1] * s[1] + kvec[3 * j + 2] * s[2];
         float sn, cs;
         sincospif(2.0f * (t - floorf(t)), &sn, &cs);
-        phi[i * 2 * nf + j] = __float2bfloat16_rn(sn);
-        phi[i * 2 * nf + nf + j] = __float2bfloat16_rn(cs);
+        phi[i * 2 * nf + j] = sn;
+        phi[i * 2 * nf + nf + j] = cs;
     }
 }
 
@@ -460,10 +499,8 @@ struct ProposalImpl {
     uint64_t adam_t = 0;
     // batch workspace
     uint64_t cap = 0;
-    DevBuf<__nv_bfloat16> phi, dz_a, dz_b;  // features, back-propagated gradients (BF16)
-    DevBuf<float> f, gf, part, bpart;
-    std::vector<DevBuf<float>> z;               // per hidden layer: pre-activation
-    std::vector<DevBuf<__nv_bfloat16>> h;       // per hidden layer: SiLU output (BF16)
+    DevBuf<float> phi, f, gf, dz_a, dz_b, part, bpart;
+    std::vector<DevBuf<float>> z, h;  // per hidden layer: pre-activation, SiLU output
     DevBuf<double> lpart, stats;
     // tabulated proposal
     int cells = 0;
@@ -501,13 +538,13 @@ static void gemm(cudaStream_t s, int M, int N, int K, const AT* A, int lda, cons
     ALEA_CUDA(cudaGetLastError());
 }
 
-template <bool TA, bool TB, int EPI, typename CT>
-static void tc_gemm(cudaStream_t s, int M, int N, int K, const __nv_bfloat16* A, int lda,
-                    const __nv_bfloat16* B, int ldb, CT* C, int ldc, const float* bias = nullptr,
-                    float* aux = nullptr, int slices = 1, float* bpart = nullptr) {
+template <bool TA, bool TB, int EPI, typename AT, typename BT, typename CT>
+static void tc_gemm(cudaStream_t s, int M, int N, int K, const AT* A, int lda, const BT* B, int ldb,
+                    CT* C, int ldc, const float* bias = nullptr, float* aux = nullptr,
+                    int slices = 1, float* bpart = nullptr) {
     const int chunk = slices > 1 ? ((K + slices - 1) / slices + TC_K - 1) / TC_K * TC_K : K;
     dim3 grid((unsigned)((N + TC_T - 1) / TC_T), (unsigned)((M + TC_T - 1) / TC_T), (unsigned)slices);
-    tc_gemm_kernel<TA, TB, CT, EPI><<<grid, TC_THREADS, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc,
+    tc_gemm_kernel<TA, TB, AT, BT, CT, EPI><<<grid, TC_THREADS, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc,
                                                                bias, aux, chunk, bpart);
     ALEA_CUDA(cudaGetLastError());
 }
@@ -520,7 +557,7 @@ static void forward(ProposalImpl& P, const float* samples, uint64_t n, uint64_t 
     features_kernel<<<blocks_for(n, 256), 256, 0, s>>>(samples, ROW, n, pa, pc, pool, P.kvec.p, P.nf,
                                                        P.phi.p);
     ALEA_CUDA(cudaGetLastError());
-    const __nv_bfloat16* in = P.phi.p;
+    const float* in = P.phi.p;
     for (int l = 0; l < P.depth; ++l) {  // tensor cores: h_l = SiLU(h_{l-1} W_l^T + b_l)
         tc_gemm<false, true, EPI_BIAS_SILU>(s, (int)n, P.lout[l], P.lin[l], in, P.lin[l],
                                             P.wb.p + P.woff[l], P.lin[l], P.h[l].p, P.lout[l],
@@ -560,13 +597,13 @@ static double loss_grad(ProposalImpl& P, const float* samples, uint64_t n, uint6
                                                                   P.g.p + P.woff[L], P.g.p + P.boff[L]);
         ALEA_CUDA(cudaGetLastError());
     }
-    // dz_{L-1} = (g W_L) SiLU'(z_{L-1}) (rank one, CUDA cores), stored in BF16
-    __nv_bfloat16* dz = P.dz_a.p;
-    __nv_bfloat16* dz_next = P.dz_b.p;
+    // dz_{L-1} = (g W_L) SiLU'(z_{L-1}) (rank one, CUDA cores)
+    float* dz = P.dz_a.p;
+    float* dz_next = P.dz_b.p;
     gemm<false, false, EPI_SILU_GRAD>(s, (int)n, W, 1, P.gf.p, 1, P.wb.p + P.woff[L], W, dz, W,
                                       nullptr, P.z[L - 1].p);
     for (int l = L - 1; l >= 0; --l) {
-        const __nv_bfloat16* hin = l > 0 ? P.h[l - 1].p : P.phi.p;
+        const float* hin = l > 0 ? P.h[l - 1].p : P.phi.p;
         // tensor cores: dW_l = dz_l^T h_{l-1} split over samples, with the bias
         // gradient (the row sums of dz_l^T) in the same launch; then both reduced
         // in slice order by one launch

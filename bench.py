@@ -289,6 +289,8 @@ def main():
                     help="the C4 loading comparison at 0.1, 1, 10 and 30 bar, SECONDS per arm, "
                          "one JSON line (no bench line)")
     ap.add_argument("--orientation-trials", type=int, default=6)
+    ap.add_argument("--c5-isotherm", type=float, default=None, metavar="SECONDS",
+                    help="run the C5 isotherm's 64 chains for SECONDS and print one JSON line")
     ap.add_argument("--kernel-case", default=None, choices=["gcmc", "gcmc_c5", "widom", "widom_q32", "interp", "ewald"],
                     help="one small case of a non-grid kernel for profiler captures, then exit "
                          "(no bench line)")
@@ -297,6 +299,12 @@ def main():
         return run_reference(args)
     if args.kernel_case:
         return kernel_case(args.kernel_case)
+    if args.c5_isotherm:
+        import torch
+        import aleator_gb300 as A
+        A.load_library()
+        print(json.dumps(c5_isotherm(A, torch, args.c5_isotherm)), flush=True)
+        return 0
     if args.loading:
         import torch
         import aleator_gb300 as A
@@ -839,6 +847,60 @@ def c5_isotherm_sample(A, torch, moves=1000, n=64):
             "us_per_move_per_chain": t_run / moves * 1e6,
             "chain_moves_per_s": n * moves / t_run,
             "molecules_after": {f"{P:.3g} bar": m for P, m in list(zip(pressures, mol))[::9]}}
+
+
+def c5_isotherm(A, torch, seconds, n=64, block=2000):
+    """The C5 isotherm itself: the 64 chains of c5_isotherm_sample (learned
+    proposal, 0.2 A FP32 grid, kMax 34, FP32 form) run in blocks of `block`
+    moves for `seconds` of wall time. Per pressure: the mean loading over the
+    second half of the blocks and its standard error from the block means
+    (blocks of 2000 moves; the chain is one replica per pressure), and the
+    drift between the two quarters of that half (an equilibration check)."""
+    from aleator_gb300 import workloads as W
+    T = 298.0
+    fw, guests = make_workload()
+    alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
+    ff = A.LennardJones(fw.eps, fw.sigma, CUTOFF, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    ew = A.Ewald(alpha, 12.0, kmax)
+    guest = W.co2_guest(fw)
+    grid = A.FrameworkEnergyGrid(ff, p, fw.lattice, guests, SPACING, A.FP32)
+    widom = A.Widom(ff, p, fw.lattice, guest, T, ewald=ew, precision=A.FP32)
+    prop = A.Proposal(seed=2)
+    prop.fit(widom, n_samples=1 << 18, rounds=2, epochs=10, cells=64)
+    pressures = np.logspace(np.log10(0.01), np.log10(50.0), n)
+    fugs = [A.peng_robinson_fugacity(*W.CO2_CRITICAL, T, P * 1e5) for P in pressures]
+    ch = A.GcmcChains(ff, p, fw.lattice, guest, T, fugs, list(range(n)), list(range(n)), ewald=ew,
+                      max_molecules=8000, precision=A.FP32)
+    ch.set_grid(grid)
+    ch.set_proposal(prop)
+    t0 = time.perf_counter()
+    prev = np.array([ch.info(c)["sum_molecules"] for c in range(n)])
+    means = []
+    while time.perf_counter() - t0 < seconds:
+        ch.run(block)
+        cur = np.array([ch.info(c)["sum_molecules"] for c in range(n)])
+        means.append((cur - prev) / block)
+        prev = cur
+    wall = time.perf_counter() - t0
+    m = np.array(means)  # blocks x chains
+    nb = len(m)
+    half = m[nb // 2:]
+    q1, q2 = half[:len(half) // 2], half[len(half) // 2:]
+    V = abs(np.linalg.det(np.asarray(fw.lattice)))
+    rows = []
+    for c in range(n):
+        mean = float(half[:, c].mean())
+        se = float(half[:, c].std(ddof=1) / np.sqrt(len(half))) if len(half) > 1 else None
+        rows.append({"bar": float(pressures[c]), "molecules": mean, "se": se,
+                     "drift": float(q2[:, c].mean() - q1[:, c].mean()) if len(q1) else None,
+                     "mmol_per_cm3": mean / V * 1e24 / 6.02214076e23 * 1e3})
+    info = [ch.info(c) for c in range(n)]
+    return {"workload": f"4x4x4 triclinic supercell, {fw.n_atoms} charged atoms, rigid CO2, {n} chains "
+                        f"at 0.01-50 bar, Ewald kMax {kmax}, 0.2 A FP32 grid, learned proposal, FP32",
+            "moves_per_chain": nb * block, "wall_s": wall,
+            "us_per_move_per_chain": wall / (nb * block) * 1e6,
+            "resyncs_max": int(max(i["resyncs"] for i in info)), "isotherm": rows}
 
 
 def batched_screening(A, torch, n_frameworks=256, trials=1_000_000):

@@ -9,9 +9,6 @@ definition the kernels implement:
 * features phi(s) = [sin(2 pi k_j . s), cos(2 pi k_j . s)] for integer k_j;
 * layers h_l = SiLU(W_l h_{l-1} + b_l), output f = W_L h_{L-1} + b_L, with the
   weights W rounded to BF16 (round to nearest even) and the biases in FP32;
-  the kernels' tensor-core products take BF16 operands, so the features, the
-  hidden activations h_l and the back-propagated gradients dz_l (of the hidden
-  pre-activations) are rounded to BF16 where the kernels store them;
 * loss L = -sum_i softmax(tau l - lq)_i f_i + log mean_i exp(f_i - lq_i) and its
   gradient (lq: log density of the proposal a row was drawn from, 0 if uniform);
 * the tabulated density P_c = (1 - u) softmax(f(centre_c)) + u / N.
@@ -36,7 +33,6 @@ class MLP:
     W [out x in] row-major, then b [out]."""
 
     def __init__(self, kvec, params, width=128, depth=3, round_bf16=True):
-        self.round = round_bf16
         self.k = np.asarray(kvec, dtype=np.float64).reshape(-1, 3)
         self.nf = len(self.k)
         self.width, self.depth = width, depth
@@ -64,16 +60,12 @@ class MLP:
         t = t - np.floor(t)
         return np.concatenate([np.sin(2 * np.pi * t), np.cos(2 * np.pi * t)], axis=1)
 
-    def _act(self, x):
-        """An activation as the kernels store it (BF16) when rounding."""
-        return bf16_round(x).astype(np.float64) if self.round else x
-
     def forward(self, s, keep=False):
-        h = self._act(self.features(s))
+        h = self.features(s)
         zs, hs = [], [h]
         for layer in range(self.depth):
             z = h @ self.W[layer].T + self.b[layer]
-            h = self._act(z / (1.0 + np.exp(-z)))
+            h = z / (1.0 + np.exp(-z))
             zs.append(z)
             hs.append(h)
         f = (h @ self.W[-1].T + self.b[-1])[:, 0]
@@ -102,7 +94,7 @@ class MLP:
                 dh = dz @ self.W[layer]
                 z = zs[layer - 1]
                 sg = 1.0 / (1.0 + np.exp(-z))
-                dz = self._act(dh * sg * (1.0 + z * (1.0 - sg)))
+                dz = dh * sg * (1.0 + z * (1.0 - sg))
         flat = np.concatenate([np.concatenate([gw.ravel(), gb]) for gw, gb in grads])
         return loss, flat
 
