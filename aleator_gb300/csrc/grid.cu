@@ -346,6 +346,133 @@ __device__ void drain_tiles(uint32_t failed_tile, uint32_t n_tiles, uint64_t* ba
     __syncthreads();
 }
 
+// ---------------------------------------------------------------- large cutoffs
+// A cutoff above half a perpendicular width (rc > L_perp/2): the reference's
+// constructor does not check this (framework_energy_grid.cc:193-249) and sums,
+// per node and atom, pairEnergy of the single minimum-image displacement
+// (Lattice::minimumImageDisplacement, lattice.cc:185-255: per axis for an
+// orthorhombic cell, else the best of the 125 lattice translations around the
+// nearest one in the greedily reduced basis, lattice.cc:70-101). Beyond L_perp/2
+// an atom can have several images within rc but only that one counts, so the
+// image-list kernels (which add every image within rc) would differ; this
+// FP64 kernel restates the reference's loop instead: a thread per node, the
+// atoms in index order through shared-memory tiles.
+struct MiGeom {
+    double m[9];     // lattice rows
+    int ortho;
+    double r[9];     // the reduced basis, rows
+    double t0[3], t1[3], t2[3];  // r1 x r2, r2 x r0, r0 x r1
+    double rvol;     // r0 . (r1 x r2)
+    int n[3];
+    double rc;
+    int trunc;
+    uint32_t n_species;
+};
+
+// lattice.cc:70-101 (greedyReduce): size reduction of each vector against the
+// others, then the three sorted by squared length, until nothing changes.
+static void reduced_basis(const double* m, double* out) {
+    double v[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c) v[i][c] = m[3 * i + c];
+    auto n2 = [](const double* a) { return a[0] * a[0] + a[1] * a[1] + a[2] * a[2]; };
+    for (int iter = 0; iter < 50; ++iter) {
+        bool changed = false;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                if (i == j) continue;
+                const double nj2 = n2(v[j]);
+                if (nj2 < 1e-10) continue;
+                const double t = std::round((v[i][0] * v[j][0] + v[i][1] * v[j][1] + v[i][2] * v[j][2]) / nj2);
+                if (t != 0.0) {
+                    for (int c = 0; c < 3; ++c) v[i][c] = v[i][c] - v[j][c] * t;
+                    changed = true;
+                }
+            }
+        for (int i = 1; i < 3; ++i) {  // three elements: an insertion sort on the squared length
+            double tmp[3] = {v[i][0], v[i][1], v[i][2]};
+            const double key = n2(tmp);
+            int j = i - 1;
+            while (j >= 0 && key < n2(v[j])) {
+                for (int c = 0; c < 3; ++c) v[j + 1][c] = v[j][c];
+                --j;
+            }
+            for (int c = 0; c < 3; ++c) v[j + 1][c] = tmp[c];
+        }
+        if (!changed) break;
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c) out[3 * i + c] = v[i][c];
+}
+
+__device__ __forceinline__ void mi_reference(const MiGeom& G, const double* d, double* out) {
+    if (G.ortho) {
+        for (int a = 0; a < 3; ++a) {
+            const double len = G.m[4 * a];
+            out[a] = d[a] - len * round(d[a] / len);
+        }
+        return;
+    }
+    const double f0 = (d[0] * G.t0[0] + d[1] * G.t0[1] + d[2] * G.t0[2]) / G.rvol;
+    const double f1 = (d[0] * G.t1[0] + d[1] * G.t1[1] + d[2] * G.t1[2]) / G.rvol;
+    const double f2 = (d[0] * G.t2[0] + d[1] * G.t2[1] + d[2] * G.t2[2]) / G.rvol;
+    const double n0 = round(f0), n1 = round(f1), n2 = round(f2);
+    out[0] = d[0];
+    out[1] = d[1];
+    out[2] = d[2];
+    double best2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    for (int a = -2; a <= 2; ++a)
+        for (int b = -2; b <= 2; ++b)
+            for (int c = -2; c <= 2; ++c) {
+                const double c0 = n0 + a, c1 = n1 + b, c2 = n2 + c;
+                double cand[3];
+                for (int k = 0; k < 3; ++k) cand[k] = d[k] - ((G.r[k] * c0 + G.r[3 + k] * c1) + G.r[6 + k] * c2);
+                const double cn2 = cand[0] * cand[0] + cand[1] * cand[1] + cand[2] * cand[2];
+                if (cn2 < best2) {
+                    best2 = cn2;
+                    out[0] = cand[0];
+                    out[1] = cand[1];
+                    out[2] = cand[2];
+                }
+            }
+}
+
+constexpr int MI_THREADS = 128;
+
+__global__ void __launch_bounds__(MI_THREADS)
+grid_build_mi_kernel(MiGeom G, const ImageRec* __restrict__ atoms, uint64_t n_atoms,
+                     const PairParams* __restrict__ params, const uint32_t* __restrict__ guests,
+                     int ng, double* __restrict__ tables) {
+    __shared__ ImageRec tile[MI_THREADS];
+    const uint64_t nodes = (uint64_t)G.n[0] * G.n[1] * G.n[2];
+    const uint64_t idx = (uint64_t)blockIdx.x * MI_THREADS + threadIdx.x;
+    const bool on = idx < nodes;
+    const int ix = (int)(idx % G.n[0]), iy = (int)((idx / G.n[0]) % G.n[1]), iz = (int)(idx / ((uint64_t)G.n[0] * G.n[1]));
+    const double f[3] = {(double)ix / G.n[0], (double)iy / G.n[1], (double)iz / G.n[2]};
+    double cart[3];
+    for (int c = 0; c < 3; ++c) cart[c] = (f[0] * G.m[c] + f[1] * G.m[3 + c]) + f[2] * G.m[6 + c];
+    for (int g = 0; g < ng; ++g) {
+        const PairParams* row = params + (size_t)guests[g] * G.n_species;
+        double e = 0.0;
+        for (uint64_t base = 0; base < n_atoms; base += MI_THREADS) {
+            __syncthreads();
+            if (base + threadIdx.x < n_atoms) tile[threadIdx.x] = atoms[base + threadIdx.x];
+            __syncthreads();
+            const int cnt = (int)min((uint64_t)MI_THREADS, n_atoms - base);
+            if (!on) continue;
+            for (int j = 0; j < cnt; ++j) {
+                const ImageRec a = tile[j];
+                const double d[3] = {a.x - cart[0], a.y - cart[1], a.z - cart[2]};
+                double o[3];
+                mi_reference(G, d, o);
+                const double r = sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
+                e += lj_pair_rt(G.trunc, r, G.rc, row[a.type]);
+            }
+        }
+        if (on) tables[(size_t)g * nodes + idx] = (kEnergyCap < e) ? kEnergyCap : e;  // capped()
+    }
+}
+
 // ---------------------------------------------------------------- FP64 build kernel
 // The parity form: the reference's node positions and pairEnergy in FP64 on
 // global Cartesian coordinates, candidates in a fixed order.
@@ -1602,6 +1729,8 @@ struct GridImpl {
     DevBuf<unsigned> flags;
     uint64_t n_images = 0;
     uint64_t executed_pairs = 0;
+    bool min_image = false;  // rc > L_perp/2: the reference's minimum-image loop (MiGeom)
+    MiGeom mg{};
     float last_ms = 0.f;
     int launches = 0;
     // FP32-form grids: per species, the eight trilinear corners of every node
@@ -1635,8 +1764,10 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
     require(fw.n == 0 || (fw.x && fw.y && fw.z), ALEA_ERR_INVALID_ARGUMENT,
             "alea_grid_build: framework coordinates missing");
     g.geo.L = make_lattice(lat.m);
-    validate_cutoff(g.geo.L, lj.cutoff, "FrameworkEnergyGrid");
-    g.precision = precision;
+    // the reference's constructor takes any cutoff: above L_perp/2 its
+    // minimum-image sum is restated by grid_build_mi_kernel (FP64)
+    for (int a = 0; a < 3; ++a) g.min_image |= lj.cutoff > 0.5 * g.geo.L.perp[a];
+    g.precision = g.min_image ? ALEA_FP64 : precision;
     g.truncation = lj.truncation;
     g.spacing = spacing;
     g.n_atoms = fw.n;
@@ -1656,6 +1787,42 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
     g.species = sp;
     const int ng = (int)sp.size();
     require_device();  // every check above runs without a GPU
+    if (g.min_image) {
+        MiGeom& G = g.mg;
+        for (int i = 0; i < 9; ++i) G.m[i] = g.geo.L.m[i];
+        G.ortho = g.geo.L.ortho;
+        reduced_basis(G.m, G.r);
+        auto cross = [](const double* a, const double* b, double* o) {
+            o[0] = a[1] * b[2] - a[2] * b[1];
+            o[1] = a[2] * b[0] - a[0] * b[2];
+            o[2] = a[0] * b[1] - a[1] * b[0];
+        };
+        cross(G.r + 3, G.r + 6, G.t0);
+        cross(G.r + 6, G.r, G.t1);
+        cross(G.r, G.r + 3, G.t2);
+        G.rvol = G.r[0] * G.t0[0] + G.r[1] * G.t0[1] + G.r[2] * G.t0[2];
+        for (int a = 0; a < 3; ++a) G.n[a] = g.geo.n[a];
+        G.rc = lj.cutoff;
+        G.trunc = lj.truncation;
+        G.n_species = lj.n_species;
+        std::vector<ImageRec> at(fw.n);
+        for (uint64_t i = 0; i < fw.n; ++i)
+            at[i] = ImageRec{fw.x[i], fw.y[i], fw.z[i], fw.species ? fw.species[i] : 0u, 0u};
+        g.images.alloc(std::max<size_t>(fw.n, 1));
+        g.images.upload(at.data(), fw.n);
+        g.n_images = fw.n;
+        std::vector<PairParams> tab((size_t)lj.n_species * lj.n_species);
+        mixed_table(lj, tab.data());
+        g.params.alloc(tab.size());
+        g.params.upload(tab.data(), tab.size());
+        g.guests.alloc(std::max(ng, 1));
+        g.guests.upload(sp.data(), sp.size());
+        g.tables.alloc((size_t)g.geo.n[0] * g.geo.n[1] * g.geo.n[2] * std::max(ng, 1));
+        g.executed.alloc(1);
+        g.flags.alloc(1);
+        ALEA_CUDA(cudaMemset(g.flags.p, 0, sizeof(unsigned)));
+        return;
+    }
 
     // metric tensor and extents
     const double* m = g.geo.L.m;
@@ -1834,6 +2001,31 @@ void grid_test_set_tile_wait_limit(int64_t limit) { g_next_tile_wait.store(limit
 // while the next slab computes.
 static void run_build(GridImpl& g, cudaStream_t s, double* const* host = nullptr) {
     ++g.gen;
+    if (g.min_image) {  // rc > L_perp/2: the reference's loop, every node x atom
+        const size_t nodes = (size_t)g.geo.n[0] * g.geo.n[1] * g.geo.n[2];
+        cudaEvent_t e0, e1;
+        ALEA_CUDA(cudaEventCreate(&e0));
+        ALEA_CUDA(cudaEventCreate(&e1));
+        ALEA_CUDA(cudaEventRecord(e0, s));
+        grid_build_mi_kernel<<<(unsigned)((nodes + MI_THREADS - 1) / MI_THREADS), MI_THREADS, 0, s>>>(
+            g.mg, g.images.p, g.n_images, g.params.p, g.guests.p, (int)g.species.size(), g.tables.p);
+        ALEA_CUDA(cudaGetLastError());
+        ALEA_CUDA(cudaEventRecord(e1, s));
+        ALEA_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        ALEA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        g.last_ms = ms;
+        g.launches = 1;
+        g.executed_pairs = (uint64_t)nodes * g.n_atoms;
+        if (host)
+            for (size_t k = 0; k < g.species.size(); ++k)
+                if (host[k])
+                    ALEA_CUDA(cudaMemcpy(host[k], g.tables.p + k * nodes, nodes * sizeof(double),
+                                         cudaMemcpyDeviceToHost));
+        return;
+    }
     const int ng = (int)g.species.size();
     const size_t nodes = (size_t)g.geo.n[0] * g.geo.n[1] * g.geo.n[2];
     const uint64_t nbricks = (uint64_t)g.geo.bricks[0] * g.geo.bricks[1] * g.geo.bricks[2];
@@ -2117,6 +2309,8 @@ GridBatchImpl* grid_batch_create(uint32_t n, const alea_lennard_jones* lj, const
         for (uint32_t i = 0; i < n; ++i) {
             auto* g = new GridImpl();
             b->grids.push_back(g);
+            // the batched kernel sums image lists: every cutoff must fit (rc <= L_perp/2)
+            validate_cutoff(make_lattice(lat[i].m), lj[i].cutoff, "alea_grid_batch_create");
             build_plan(*g, lj[i], fw[i], lat[i], guests + (size_t)i * n_guest, n_guest, spacing,
                        ALEA_FP32, 2.0);
             if (i == 0) {

@@ -16,11 +16,14 @@
  * Lattices are row-major double[9], row i = lattice vector a_i
  * (core/geometry/lattice.hpp:21-30).
  *
- * Every energy routine here requires cutoff <= L_perp/2 on every axis
- * (Lattice::validateCutoff, core/geometry/lattice.cc:286-300): under that
- * condition at most one periodic image of an atom lies within the cutoff,
- * which is what makes the device kernels' image handling equal to the
- * reference's minimum-image search.
+ * The engines (Widom, GCMC, the Ewald state) require cutoff <= L_perp/2 on
+ * every axis, as the reference's do (Lattice::validateCutoff,
+ * core/geometry/lattice.cc:286-300): under that condition at most one
+ * periodic image of an atom lies within the cutoff, which is what makes the
+ * device kernels' image handling equal to the reference's minimum-image
+ * search. The energy grid accepts any cutoff, as the reference's constructor
+ * does; above L_perp/2 it sums the reference's single minimum image per atom
+ * (an FP64 kernel, whatever precision is asked for).
  */
 #ifndef ALEATOR_GB300_H
 #define ALEATOR_GB300_H

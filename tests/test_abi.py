@@ -52,6 +52,11 @@ def _fw():
     return W.cubic_framework(seed=5)
 
 
+def W_ch4(fw):
+    from aleator_gb300 import workloads as W
+    return W.ch4_guest(fw)
+
+
 def test_host_side_errors_match_reference_exceptions(so):
     import aleator_gb300 as A
 
@@ -61,9 +66,11 @@ def test_host_side_errors_match_reference_exceptions(so):
     # framework_energy_grid.cc:199-201: spacing must be positive -> invalid_argument
     with pytest.raises(ValueError, match="spacingAngstrom must be positive"):
         A.FrameworkEnergyGrid(lj, p, fw.lattice, [4], 0.0)
-    # Lattice::validateCutoff message shape
+    # Lattice::validateCutoff message shape (the engines check it; the grid
+    # constructor does not, as the reference's)
+    big = A.LennardJones(fw.eps, fw.sigma, 13.5, A.SHIFTED)
     with pytest.raises(ValueError, match="exceeds half the perpendicular width"):
-        A.FrameworkEnergyGrid(A.LennardJones(fw.eps, fw.sigma, 13.5, A.SHIFTED), p, fw.lattice, [4], 0.5)
+        A.Widom(big, p, fw.lattice, W_ch4(fw), 298.0)
     with pytest.raises(IndexError):
         A.FrameworkEnergyGrid(lj, p, fw.lattice, [99], 0.5)
     with pytest.raises(ValueError, match="alpha must be positive"):

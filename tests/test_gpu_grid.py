@@ -374,3 +374,25 @@ def test_bounded_tile_wait_gives_up_and_recovers(lib):
     again = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4, 6], 0.8, A.FP32)
     for s in (4, 6):
         assert np.array_equal(again.table(s), want[s])
+
+
+@pytest.mark.parametrize("cell", ["cubic", "triclinic"])
+def test_cutoff_beyond_half_width_is_the_reference_minimum_image(lib, orc, cell):
+    """rc > L_perp/2, which the reference's grid constructor accepts: one
+    minimum image per atom (lattice.cc:185-255), as the oracle computes it,
+    within 1e-10 (1 K floor); a request for the FP32 form gets the same FP64
+    tables."""
+    A, _ = lib
+    from aleator_gb300 import workloads as W
+    if cell == "cubic":
+        fw, rc = W.cubic_framework(seed=99, charged=True), 13.5
+    else:
+        fw, rc = W.triclinic_supercell(reps=1, seed=31), 11.5
+    ff = A.LennardJones(fw.eps, fw.sigma, rc, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    sid = fw.guest_species["CH4"]
+    od = dict(eps=fw.eps, sigma=fw.sigma, cutoff=rc, truncation=O.SHIFTED)
+    want = orc.grid_build(od, fw.lattice, fw.x, fw.y, fw.z, fw.species, sid, 1.0, threads=8)
+    for prec in (A.FP64, A.FP32):
+        g = A.FrameworkEnergyGrid(ff, p, fw.lattice, [sid], 1.0, prec)
+        assert rel_err(g.table(sid), want).max() <= 1e-10

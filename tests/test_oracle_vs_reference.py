@@ -69,3 +69,20 @@ def test_ewald_state_bit_exact(orc, ref, fw):
         b.commit(rem, add)
         assert a.energy() == b.energy()
     assert np.array_equal(a.raw(), b.raw())
+
+
+@pytest.mark.parametrize("cell", ["cubic", "triclinic"])
+def test_grid_bit_exact_beyond_half_width(orc, ref, fw, cell):
+    """The reference's constructor takes a cutoff above L_perp/2 and sums one
+    minimum image per atom; the restatement does the same (bit-exact
+    interpolations of its tables)."""
+    if cell == "cubic":
+        f, rc = fw, 13.5  # L/2 = 12.916
+    else:
+        f, rc = W.triclinic_supercell(reps=1, seed=31), 11.5  # L_perp/2 ~ 10.9
+    ff = dict(eps=f.eps, sigma=f.sigma, cutoff=rc, truncation=O.SHIFTED)
+    sid = f.guest_species["CH4"]
+    g = ref.grid(ff, f.lattice, f.x, f.y, f.z, f.species, [sid], 2.0)
+    pts = np.random.default_rng(4).uniform(0, 24, (64, 3))
+    mine = orc.grid_build(ff, f.lattice, f.x, f.y, f.z, f.species, sid, 2.0, threads=4)
+    assert np.array_equal(orc.grid_interpolate(f.lattice, g.counts, mine, pts), g.interpolate(sid, pts))
