@@ -16,8 +16,13 @@
 // Kernel: one CTA per brick of 16x8x8 nodes (256 threads, 4 nodes each). The
 // CTA culls candidate bins against its brick with a lower bound on the
 // parallelepiped distance, merges each bin row into one contiguous atom
-// range, and streams the ranges through shared memory in 256-record tiles
-// with cp.async.bulk (TMA) copies completed on an mbarrier, double-buffered.
+// range, and streams the ranges through shared memory in 256-record tiles.
+// The FP64 form stages a tile with cp.async.bulk (TMA) copies, one per row
+// range, completed on an mbarrier and double-buffered. The FP32 form gathers
+// a tile with per-thread cp.async copies (record t*256 + tid by thread tid,
+// issued one tile ahead): its bins are 4 A wide and a brick's ~100 row ranges
+// hold ~7 records each, too short for bulk copies (issued one after another,
+// they cost more than the sweep of the tile they fetch).
 // The FP32 form then groups each tile by framework type, skips per warp the
 // atoms beyond reach of the warp's 8x4x4 sub-box, and evaluates the rest as
 // r^-6 (A r^-6 - B) with the shift terms applied per same-type run.
@@ -336,6 +341,34 @@ __device__ void issue_tile(uint32_t t, uint32_t n_cand, int nr, const uint32_t* 
     }
 }
 
+// Per-thread asynchronous global->shared copies (16 bytes, L2 only), waited
+// for by the issuing thread.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// FP32 form: candidate t * TILE + tid of the brick's concatenated list into
+// this thread's 32-byte slot of dst (the thread that later converts it).
+__device__ __forceinline__ void gather_tile(uint32_t t, uint32_t n_cand, int nr, const uint32_t* row_begin,
+                                            const uint32_t* row_off, const unsigned char* images,
+                                            unsigned char* dst) {
+    constexpr uint32_t REC = 32;
+    const uint32_t c = t * TILE + threadIdx.x;
+    if (c < n_cand) {
+        int lo = 0, hi = nr - 1;  // last row with row_off[r] <= c: the row holding c
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (row_off[mid] <= c) lo = mid; else hi = mid - 1;
+        }
+        const unsigned char* src = images + (size_t)(row_begin[lo] + (c - row_off[lo])) * REC;
+        cp_async16(dst + threadIdx.x * REC, src);
+        cp_async16(dst + threadIdx.x * REC + 16, src + 16);
+    }
+    cp_async_commit();
+}
+
 // After a timed-out wait: tiles failed_tile and failed_tile + 1 are the only
 // ones issued and not consumed; wait for each (again bounded) before exit.
 __device__ void drain_tiles(uint32_t failed_tile, uint32_t n_tiles, uint64_t* bars) {
@@ -481,7 +514,8 @@ __global__ void __launch_bounds__(THREADS, 2)
 grid_build_f64_kernel(GridGeom geo, const ImageRec* __restrict__ images,
                       const uint32_t* __restrict__ bin_start, const PairParams* __restrict__ params,
                       const uint32_t* __restrict__ guests, double* __restrict__ tables,
-                      unsigned long long* __restrict__ executed, unsigned* flags) {
+                      unsigned long long* __restrict__ executed, unsigned* flags,
+                      unsigned tile_wait) {
     extern __shared__ __align__(128) unsigned char smem[];
     SmemCarve sc{smem};
     ImageRec* raw = sc.take<ImageRec>(2 * TILE);
@@ -549,7 +583,7 @@ grid_build_f64_kernel(GridGeom geo, const ImageRec* __restrict__ images,
         const int buf = t & 1;
         const uint32_t cnt = min((uint32_t)TILE, n_cand - t * TILE);
         // block-wide vote so that every thread takes the same path on a timeout
-        const bool got = mbar_wait_bounded(&bars[buf], (t >> 1) & 1, flags);
+        const bool got = mbar_wait_bounded(&bars[buf], (t >> 1) & 1, flags, tile_wait);
         if (!__syncthreads_and(got)) {
             drain_tiles(t, n_tiles, bars);
             return;
@@ -1049,17 +1083,15 @@ __device__ __forceinline__ void fix_flagged(const GridGeom& geo, const F32GridAr
     }
 }
 
-// One brick of the sweep (the body of the sweep kernels). `tiles` counts the
-// tiles this CTA has staged so far: the two mbarriers alternate by it, so
-// their phases run on across bricks. Returns false when the CTA must stop (a
-// bounded wait ran out; the error flag is raised).
+// One brick of the sweep (the body of the sweep kernels). Every thread of the
+// block calls it; no copy of this CTA is in flight when it returns.
 template <int NG, int TRUNC>
-__device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridArgs& A, int brick,
-                                            unsigned char* smem, uint64_t* bars, uint32_t& tiles,
+__device__ __forceinline__ void sweep_brick(const GridGeom& geo, const F32GridArgs& A, int brick,
+                                            unsigned char* smem,
                                             unsigned long long* __restrict__ executed,
-                                            unsigned* flags, unsigned tile_wait = WAIT_LIMIT) {
+                                            unsigned* flags) {
     SmemCarve sc{smem};
-    ImageRecF* raw = sc.take<ImageRecF>(TILE);         // the staged tile (TMA)
+    ImageRecF* raw = sc.take<ImageRecF>(TILE);         // the gathered tile (cp.async)
     ulonglong2* cxy = sc.take<ulonglong2>(2 * TILE);   // converted tiles: {x, x}, {y, y}
     ulonglong2* czt = sc.take<ulonglong2>(2 * TILE);   // {z, z}, {type, 0}
     uint32_t* row_begin = sc.take<uint32_t>(MAX_ROWS);
@@ -1089,7 +1121,7 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     load_f32_params(P, A.pab, A.pff, geo.n_types, rcf);
     const int nr = plan_rows(geo, geo.hf, geo.keep2f, bin_start, x0, y0, z0, row_begin, row_off,
                              warp_tot, flags);
-    if (nr < 0) return true;  // capacity flag raised; the other bricks go on
+    if (nr < 0) return;  // capacity flag raised; the other bricks go on
     const uint32_t n_cand = row_off[nr];
 
     int tx, ty, tz0;
@@ -1137,7 +1169,7 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) r2max = fmaxf(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
         const float rad = sqrtf(r2max) + 1e-3f;
-        if ((tid & 31) == 0) {  // read after the first tile's barrier
+        if ((tid & 31) == 0) {
             wsph[w] = make_float4(wcx, wcy, wcz, (geo.rcf + rad) * (geo.rcf + rad) * (1.0f + 1e-5f));
             // near: within sigma_max of some node; inner: every node within the cutoff
             const float in = geo.rcf - rad;
@@ -1145,6 +1177,8 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
                                   in > 0.f ? in * in * (1.0f - 1e-5f) : -1.f);
         }
     }
+    // every warp's sphere is read by every thread in the conversion of tile 0
+    __syncthreads();
 
     float ce[NG][NPT];               // FP32 close-pair estimates
     uint32_t has_close = 0;  // bit k: node k has a close pair; bit NPT + k: a pair at rc (truncated)
@@ -1161,21 +1195,21 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     const unsigned char* img = reinterpret_cast<const unsigned char*>(images);
     unsigned char* rawb = reinterpret_cast<unsigned char*>(raw);
     const uint32_t n_tiles = (n_cand + TILE - 1) / TILE;
-    const uint32_t T0 = tiles;  // tile t of this brick is the CTA's tile T0 + t
-    // One staging buffer (bars[0]; its k-th phase is the CTA's tile k) and two
-    // converted-tile buffers: the conversion of tile t writes buffer t & 1,
-    // last read by the main loop of tile t - 2, which every warp finished
-    // before the barrier of tile t - 1; so one barrier per tile.
-    if (tid == 0 && n_tiles > 0) issue_tile(0, n_cand, nr, row_begin, row_off, img, rawb, &bars[0]);
+    // One staging buffer, in which thread tid's slot holds the record that
+    // thread tid gathered and converts, and two converted-tile buffers: the
+    // conversion of tile t writes buffer t & 1, last read by the main loop of
+    // tile t - 2, which every warp finished before the barrier of tile t - 1;
+    // so one barrier per tile.
+    if (n_tiles > 0) gather_tile(0, n_cand, nr, row_begin, row_off, img, rawb);
     for (uint32_t t = 0; t < n_tiles; ++t) {
         const uint32_t cnt = min((uint32_t)TILE, n_cand - t * TILE);
         ulonglong2* cxy_t = cxy + (t & 1) * TILE;
         ulonglong2* czt_t = czt + (t & 1) * TILE;
         uint16_t* amask_t = amask + (t & 1) * TILE;
-        const bool got = mbar_wait_bounded(&bars[0], (T0 + t) & 1, flags, tile_wait);
+        cp_async_wait_all();  // this thread's record of tile t
         static_assert(TILE == THREADS, "one record per thread in the conversion pass");
         static_assert(TILE <= 32768 && THREADS / 32 <= 8, "list entry and class-mask widths");
-        if (got && (uint32_t)tid < cnt) {
+        if ((uint32_t)tid < cnt) {
             ff v[3];
             const ImageRecF r = raw[tid];
             atom_local(r, org, v);
@@ -1195,19 +1229,9 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
             }
             amask_t[tid] = (uint16_t)m;
         }
-        // block-wide vote so that every thread takes the same path on a timeout
-        if (!__syncthreads_and(got)) {
-            if (tid == 0)  // the timed-out tile is the only one in flight
-                for (unsigned it = 0; it < WAIT_LIMIT && !mbar_try_wait(&bars[0], (T0 + t) & 1); ++it)
-                    __nanosleep(64);
-            __syncthreads();
-            return false;
-        }
-        // the staging buffer is free again: stage tile t + 1 while computing
-        if (tid == 0 && t + 1 < n_tiles) {
-            fence_proxy_async();
-            issue_tile(t + 1, n_cand, nr, row_begin, row_off, img, rawb, &bars[0]);
-        }
+        __syncthreads();
+        // the staging buffer is free again: gather tile t + 1 while computing
+        if (t + 1 < n_tiles) gather_tile(t + 1, n_cand, nr, row_begin, row_off, img, rawb);
         // this warp's atoms: inner ones from the front of its list (tile
         // order), the others from the back; the shift sum over both (every
         // lane of the warp needs the same sum)
@@ -1364,7 +1388,6 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
                 acc_lo(g, 2 * q + 1) = sb.lo;
             }
     }
-    tiles = T0 + n_tiles;
 
     // per node and guest: sweep sum, cap, sweep sum + FP32 estimate, or the
     // sweep sum flagged for the double-float correction
@@ -1425,25 +1448,15 @@ __device__ __forceinline__ bool sweep_brick(const GridGeom& geo, const F32GridAr
     fix_flagged<NG, TRUNC>(geo, A, P, org, x0, y0, z0, gm, smem, reinterpret_cast<ParamFF*>(accs),
                            row_begin, row_off, warp_tot, flags);
     __syncthreads();  // shared memory is reused by the next brick
-    return true;
 }
 
 // 4 CTAs per SM fit in shared memory up to two guests, 3 beyond
 template <int NG, int TRUNC>
 __global__ void __launch_bounds__(THREADS, NG <= 2 ? 4 : 3)
 grid_build_f32_kernel(GridGeom geo, F32GridArgs args, unsigned long long* __restrict__ executed,
-                      unsigned* flags, unsigned tile_wait) {
+                      unsigned* flags) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bars[2];
-    if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    uint32_t tiles = 0;
-    sweep_brick<NG, TRUNC>(geo, args, geo.brick0 + (int)blockIdx.x, smem, bars, tiles, executed, flags,
-                           tile_wait);
+    sweep_brick<NG, TRUNC>(geo, args, geo.brick0 + (int)blockIdx.x, smem, executed, flags);
 }
 
 template <int NG, int TRUNC>
@@ -1499,24 +1512,14 @@ grid_build_f32_batch_kernel(const BatchItem* __restrict__ items, int n_items, ui
                             unsigned long long* next, unsigned long long* __restrict__ executed,
                             unsigned* flags) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bars[2];
     __shared__ unsigned long long work;
     __shared__ int item;
     GridGeom& geo = *reinterpret_cast<GridGeom*>(smem);
     unsigned char* body = smem + carve(sizeof(GridGeom));
     static_assert(sizeof(GridGeom) % 4 == 0, "geometry copied as words");
-    if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    uint32_t tiles = 0;
     while (next_item(items, n_items, total, next, work, item, geo)) {
         const BatchItem& it = items[item];
-        if (!sweep_brick<NG, TRUNC>(geo, it.args, (int)(work - it.brick0), body, bars, tiles,
-                                    executed, flags))
-            return;
+        sweep_brick<NG, TRUNC>(geo, it.args, (int)(work - it.brick0), body, executed, flags);
         __syncthreads();  // work, item and geo are rewritten next
     }
 }
@@ -1664,7 +1667,7 @@ struct BuildArgs {
     double* tables;
     unsigned long long* executed;
     unsigned* flags;
-    unsigned tile_wait;          // FP32 form: polls before a tile wait gives up
+    unsigned tile_wait;          // FP64 form: polls before a tile wait gives up
 };
 
 template <int NG, int TRUNC>
@@ -1675,14 +1678,13 @@ void launch_one(bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo, const 
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f32_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
         const F32GridArgs fa{a.images_f, a.bins, a.pab, a.pff, a.tables};
-        grid_build_f32_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(geo, fa, a.executed, a.flags,
-                                                                       a.tile_wait);
+        grid_build_f32_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(geo, fa, a.executed, a.flags);
     } else {
         constexpr size_t bytes = f64_smem_bytes<NG>();
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f64_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
         grid_build_f64_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(
-            geo, a.images, a.bins, a.params, a.guests, a.tables, a.executed, a.flags);
+            geo, a.images, a.bins, a.params, a.guests, a.tables, a.executed, a.flags, a.tile_wait);
     }
 }
 
@@ -1748,6 +1750,13 @@ struct GridImpl {
     bool corners_off = false;  // their allocation failed once: the plain table serves
     std::mutex corners_mu;     // interpolations from several host threads share them
 };
+
+// Initial bin width (A). The FP64 kernel evaluates every candidate against
+// every node of its brick, so narrow bins (fewer candidates) pay; the FP32
+// sweep culls per warp and gathers each record on its own, so its cost is per
+// bin row (planning, list building) and wider bins pay: 4 A bins build the
+// 4x4x4 supercell's 0.2 A grid in 19.4 ms against 21.9 ms with 2 A bins.
+static double bin_width(int precision) { return precision == ALEA_FP32 ? 4.0 : 2.0; }
 
 static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_particles& fw,
                        const alea_lattice& lat, const uint32_t* guest, uint32_t n_guest,
@@ -1989,8 +1998,9 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
 }
 
 // Test support (alea_test_grid_tile_wait_limit): when set (>= 0), the poll limit
-// of every tile wait of the next FP32-form build, consumed by that build; the
-// wait for the copy still in flight when a CTA gives up keeps WAIT_LIMIT.
+// of every tile wait of the next FP64-form build, consumed by that build; the
+// waits for the copies still in flight when a CTA gives up keep WAIT_LIMIT.
+// (The FP32 form's gathers complete on cp.async.wait_all: no polled wait.)
 static std::atomic<int64_t> g_next_tile_wait{-1};
 
 void grid_test_set_tile_wait_limit(int64_t limit) { g_next_tile_wait.store(limit); }
@@ -2032,7 +2042,7 @@ static void run_build(GridImpl& g, cudaStream_t s, double* const* host = nullptr
     require(nbricks < (1ull << 31), ALEA_ERR_INVALID_ARGUMENT, "grid too large");
     ALEA_CUDA(cudaMemsetAsync(g.executed.p, 0, sizeof(unsigned long long), s));
     const bool f32 = g.precision == ALEA_FP32;
-    const int64_t knob = f32 ? g_next_tile_wait.exchange(-1) : -1;
+    const int64_t knob = f32 ? -1 : g_next_tile_wait.exchange(-1);
     const unsigned tile_wait = knob >= 0 ? (unsigned)std::min<int64_t>(knob, WAIT_LIMIT) : WAIT_LIMIT;
     // one launch per chunk of up to MAX_NG guests, timed by events on the stream
     const int chunks = (ng + MAX_NG - 1) / MAX_NG;
@@ -2099,7 +2109,7 @@ GridImpl* grid_build(const alea_lennard_jones& lj, const alea_particles& fw,
                      double spacing, int precision) {
     auto* g = new GridImpl();
     try {
-        build_plan(*g, lj, fw, lat, guest, n_guest, spacing, precision, 2.0);
+        build_plan(*g, lj, fw, lat, guest, n_guest, spacing, precision, bin_width(precision));
         run_build(*g, 0);
     } catch (...) {
         delete g;
@@ -2115,7 +2125,7 @@ GridImpl* grid_build_to_host(const alea_lennard_jones& lj, const alea_particles&
                              double spacing, int precision, double* const* host) {
     auto* g = new GridImpl();
     try {
-        build_plan(*g, lj, fw, lat, guest, n_guest, spacing, precision, 2.0);
+        build_plan(*g, lj, fw, lat, guest, n_guest, spacing, precision, bin_width(precision));
         // host arrays in the order of `guest`, tables in the grid's (sorted) order
         std::vector<double*> per_table(g->species.size(), nullptr);
         for (uint32_t k = 0; k < n_guest; ++k) {
@@ -2312,7 +2322,7 @@ GridBatchImpl* grid_batch_create(uint32_t n, const alea_lennard_jones* lj, const
             // the batched kernel sums image lists: every cutoff must fit (rc <= L_perp/2)
             validate_cutoff(make_lattice(lat[i].m), lj[i].cutoff, "alea_grid_batch_create");
             build_plan(*g, lj[i], fw[i], lat[i], guests + (size_t)i * n_guest, n_guest, spacing,
-                       ALEA_FP32, 2.0);
+                       ALEA_FP32, bin_width(ALEA_FP32));
             if (i == 0) {
                 b->ng = (int)g->species.size();
                 b->truncation = g->truncation;

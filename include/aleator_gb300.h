@@ -211,9 +211,10 @@ alea_status alea_grid_build_to_host(const alea_lennard_jones* lj, const alea_par
                                     uint32_t n_guest, double spacing_angstrom, int32_t precision,
                                     double* const* host_tables, alea_grid** out);
 /* Test support for the device-side bounded waits (no counterpart in the
- * reference, which has no device code): the tile waits of the next FP32-form
+ * reference, which has no device code): the tile waits of the next FP64-form
  * grid build or rebuild in this process give up after `limit` polls (0: at the
- * first wait) instead of the usual ~2^20. The build then ends with
+ * first wait) instead of the usual ~2^20 (the FP32 form's tiles complete on
+ * cp.async.wait_all, with no polled wait). The build then ends with
  * ALEA_ERR_DEVICE_CHECK ("wait") after each CTA has waited, with the usual
  * limit, for the copy it still had in flight; the device stays usable and the
  * build after it runs normally. limit < 0 cancels a pending setting. */

@@ -351,17 +351,18 @@ def test_build_to_host_equals_build(lib):
 
 
 def test_bounded_tile_wait_gives_up_and_recovers(lib):
-    """The FP32 sweep's tile waits are bounded: with the test knob the next
-    build's waits give up at the first poll (no fault, no hang: each CTA still
-    waits, bounded, for the copy it has in flight, then returns). The build
-    reports ALEA_ERR_DEVICE_CHECK ("wait"), the knob is spent, and the next
-    build on the same context returns the normal tables."""
+    """The FP64 build's tile waits (TMA copies on an mbarrier) are bounded:
+    with the test knob the next build's waits give up at the first poll (no
+    fault, no hang: each CTA still waits, bounded, for the copies it has in
+    flight, then returns). The build reports ALEA_ERR_DEVICE_CHECK ("wait"),
+    the knob is spent, and the next build on the same context returns the
+    normal tables. An FP32 build is not affected by the knob."""
     A, _ = lib
     from aleator_gb300 import workloads as W
     fw = W.cubic_framework(seed=5)
     ff = A.LennardJones(fw.eps, fw.sigma, 12.0, A.SHIFTED)
     p = A.ParticleData.from_framework(fw)
-    grid = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4, 6], 0.8, A.FP32)
+    grid = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4, 6], 0.8, A.FP64)
     want = {s: grid.table(s) for s in (4, 6)}
     lib_ = A.load_library()
     assert lib_.alea_test_grid_tile_wait_limit(0) == 0
@@ -371,9 +372,16 @@ def test_bounded_tile_wait_gives_up_and_recovers(lib):
     grid.rebuild()  # the knob was consumed by the failed build
     for s in (4, 6):
         assert np.array_equal(grid.table(s), want[s])
-    again = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4, 6], 0.8, A.FP32)
+    again = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4, 6], 0.8, A.FP64)
     for s in (4, 6):
         assert np.array_equal(again.table(s), want[s])
+    # the FP32 build leaves a pending knob alone; the next FP64 build takes it
+    f32 = A.FrameworkEnergyGrid(ff, p, fw.lattice, [4, 6], 0.8, A.FP32)
+    assert lib_.alea_test_grid_tile_wait_limit(0) == 0
+    f32.rebuild()
+    with pytest.raises(A.AleatorError):
+        grid.rebuild()
+    grid.rebuild()
 
 
 @pytest.mark.parametrize("cell", ["cubic", "triclinic"])
