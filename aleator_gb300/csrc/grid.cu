@@ -832,7 +832,38 @@ struct F32GridArgs {
     const ParamAB* pab;  // [guest of this launch][type]
     const ParamFF* pff;  // [guest of this launch][type]
     double* tables;
+    // the bricks' row plans made by grid_plan_kernel (stride words a brick:
+    // nr, row_begin[nr], row_off[nr + 1]), or null: each brick plans itself
+    const uint32_t* plans;
+    uint32_t plan_stride;
 };
+
+// The row plan of every brick of a launch (plan_rows), ahead of the sweep: a
+// light kernel (small registers and shared memory, so many CTAs a SM hide
+// the bin loads and the per-row bin tests), where in the sweep each brick's
+// planning held its CTA's warps from the pair loop. nr = ~0u: the brick
+// touches more rows than a plan holds (the error flag is raised).
+__global__ void __launch_bounds__(THREADS)
+grid_plan_kernel(GridGeom geo, const uint32_t* __restrict__ bin_start, uint32_t* __restrict__ plans,
+                 uint32_t stride, unsigned* flags) {
+    __shared__ uint32_t row_begin[MAX_ROWS], row_off[MAX_ROWS + 1], warp_tot[THREADS / 32];
+    const int brick = geo.brick0 + (int)blockIdx.x;
+    const int bxn = geo.bricks[0], byn = geo.bricks[1];
+    const int bx = brick % bxn, by = (brick / bxn) % byn, bz = brick / (bxn * byn);
+    uint32_t* out = plans + (size_t)brick * stride;
+    const int nr = plan_rows(geo, geo.hf, geo.keep2f, bin_start, bx * BX, by * BY, bz * BZ, row_begin,
+                             row_off, warp_tot, flags);
+    if (nr < 0 || 2 * (uint32_t)nr + 2 > stride) {
+        if (threadIdx.x == 0) {
+            if (nr >= 0) flag_error(flags, DEV_ERR_CAPACITY);
+            out[0] = ~0u;
+        }
+        return;
+    }
+    if (threadIdx.x == 0) out[0] = (uint32_t)nr;
+    for (int i = threadIdx.x; i < nr; i += THREADS) out[1 + i] = row_begin[i];
+    for (int i = threadIdx.x; i <= nr; i += THREADS) out[1 + nr + i] = row_off[i];
+}
 
 // ---------------------------------------------------------------- FP32 close-pair correction
 // For the nodes the sweep flagged: the pairs closer than sigma_t, exactly as
@@ -1119,9 +1150,20 @@ __device__ __forceinline__ void sweep_brick(const GridGeom& geo, const F32GridAr
     auto acc_lo = [&](int g, int k) -> float& { return accs[((g * NPT + k) * 2 + 1) * THREADS + tid]; };
 
     load_f32_params(P, A.pab, A.pff, geo.n_types, rcf);
-    const int nr = plan_rows(geo, geo.hf, geo.keep2f, bin_start, x0, y0, z0, row_begin, row_off,
-                             warp_tot, flags);
-    if (nr < 0) return;  // capacity flag raised; the other bricks go on
+    int nr;
+    if (A.plans) {  // the brick's plan, made ahead by grid_plan_kernel
+        const uint32_t* __restrict__ pl = A.plans + (size_t)brick * A.plan_stride;
+        const uint32_t n = pl[0];
+        if (n == ~0u) return;  // capacity flag raised; the other bricks go on
+        nr = (int)n;
+        for (int i = tid; i < nr; i += THREADS) row_begin[i] = pl[1 + i];
+        for (int i = tid; i <= nr; i += THREADS) row_off[i] = pl[1 + nr + i];
+        __syncthreads();
+    } else {
+        nr = plan_rows(geo, geo.hf, geo.keep2f, bin_start, x0, y0, z0, row_begin, row_off, warp_tot,
+                       flags);
+        if (nr < 0) return;  // capacity flag raised; the other bricks go on
+    }
     const uint32_t n_cand = row_off[nr];
 
     int tx, ty, tz0;
@@ -1243,6 +1285,7 @@ __device__ __forceinline__ void sweep_brick(const GridGeom& geo, const F32GridAr
             const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
             for (int g = 0; g < NG; ++g) shift_sum[g] = 0.f;
+#pragma unroll 4  // the class loads and ballots of several chunks in flight
             for (uint32_t c0 = 0; c0 < cnt; c0 += 32) {
                 const uint32_t j = c0 + lane;
                 const uint32_t cls = j < cnt ? (amask_t[j] >> (2 * w)) & 3u : 0u;
@@ -1668,6 +1711,8 @@ struct BuildArgs {
     unsigned long long* executed;
     unsigned* flags;
     unsigned tile_wait;          // FP64 form: polls before a tile wait gives up
+    const uint32_t* plans;       // FP32 form: the row plans of grid_plan_kernel
+    uint32_t plan_stride;
 };
 
 template <int NG, int TRUNC>
@@ -1677,7 +1722,7 @@ void launch_one(bool f32, dim3 grid, cudaStream_t s, const GridGeom& geo, const 
         // opt in to more than 48 KB of dynamic shared memory (per device, cheap)
         ALEA_CUDA(cudaFuncSetAttribute(grid_build_f32_kernel<NG, TRUNC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-        const F32GridArgs fa{a.images_f, a.bins, a.pab, a.pff, a.tables};
+        const F32GridArgs fa{a.images_f, a.bins, a.pab, a.pff, a.tables, a.plans, a.plan_stride};
         grid_build_f32_kernel<NG, TRUNC><<<grid, THREADS, bytes, s>>>(geo, fa, a.executed, a.flags);
     } else {
         constexpr size_t bytes = f64_smem_bytes<NG>();
@@ -1724,6 +1769,8 @@ struct GridImpl {
     DevBuf<ParamAB> pab;         // FP32 form, [guest][type]
     DevBuf<ParamFF> pff;
     DevBuf<uint32_t> bin_start;
+    DevBuf<uint32_t> plans;      // FP32 form: the bricks' row plans (grid_plan_kernel)
+    uint32_t plan_stride = 0;    // words a brick: 2 + 2 x the most rows a brick can touch
     DevBuf<PairParams> params;
     DevBuf<uint32_t> guests;
     DevBuf<double> tables;
@@ -1856,8 +1903,8 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
         }
     }
     // widen the bins until no brick can touch more than MAX_ROWS bin rows
+    int span_bins[3] = {0, 0, 0};
     for (int attempt = 0; attempt < 64; ++attempt) {
-        int span_bins[3];
         for (int a = 0; a < 3; ++a) {
             const double h = lj.cutoff / g.geo.L.perp[a];
             const double span = (double)(g.geo.n[a] - 1) / g.geo.n[a] + 2 * h + 2e-7;
@@ -1869,6 +1916,9 @@ static void build_plan(GridImpl& g, const alea_lennard_jones& lj, const alea_par
         if (span_bins[1] * span_bins[2] <= MAX_ROWS) break;
         bin_width *= 1.25;
     }
+    // plan_rows spans at most span_bins[a] bins on axes 1 and 2 (its margins
+    // are a bin narrower than the 4 added here)
+    g.plan_stride = 2 + 2 * (uint32_t)std::min(span_bins[1] * span_bins[2], MAX_ROWS);
     for (int a = 0; a < 3; ++a) {
         const double h = lj.cutoff / g.geo.L.perp[a];
         g.geo.lo[a] = -h - 1e-7;
@@ -2059,10 +2109,16 @@ static void run_build(GridImpl& g, cudaStream_t s, double* const* host = nullptr
         ALEA_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         for (auto& e : done) ALEA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
+    if (f32 && !g.plans.p) g.plans.alloc((size_t)per_layer * layers * g.plan_stride);
     for (int sl = 0; sl < slabs; ++sl) {
         const int z0 = (int)((int64_t)layers * sl / slabs), z1 = (int)((int64_t)layers * (sl + 1) / slabs);
         GridGeom geo = g.geo;
         geo.brick0 = (int)(per_layer * z0);
+        if (f32 && z1 > z0) {  // the slab's row plans, shared by its guest chunks
+            grid_plan_kernel<<<(unsigned)(per_layer * (z1 - z0)), THREADS, 0, s>>>(
+                geo, g.bin_start.p, g.plans.p, g.plan_stride, g.flags.p);
+            ALEA_CUDA(cudaGetLastError());
+        }
         for (int c = 0; c < chunks; ++c) {
             const int g0 = c * MAX_NG;
             const int cnt = std::min(MAX_NG, ng - g0);
@@ -2071,7 +2127,7 @@ static void run_build(GridImpl& g, cudaStream_t s, double* const* host = nullptr
             const BuildArgs args{g.images.p, g.images_f.p, g.bin_start.p, g.params.p, g.guests.p + g0,
                                  f32 ? g.pab.p + pofs : nullptr, f32 ? g.pff.p + pofs : nullptr,
                                  g.tables.p + (size_t)g0 * nodes, g.executed.p, g.flags.p,
-                                 tile_wait};
+                                 tile_wait, g.plans.p, g.plan_stride};
             launch_build(cnt, g.truncation, f32, grid, s, geo, args);
             ALEA_CUDA(cudaGetLastError());
         }
@@ -2097,7 +2153,7 @@ static void run_build(GridImpl& g, cudaStream_t s, double* const* host = nullptr
     ALEA_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
     for (auto& e : ev) cudaEventDestroy(e);
     g.last_ms = ms;
-    g.launches = chunks;
+    g.launches = slabs * chunks + (f32 ? slabs : 0);
     unsigned long long ex = 0;
     ALEA_CUDA(cudaMemcpy(&ex, g.executed.p, sizeof(ex), cudaMemcpyDeviceToHost));
     g.executed_pairs = ex;
@@ -2335,7 +2391,7 @@ GridBatchImpl* grid_batch_create(uint32_t n, const alea_lennard_jones* lj, const
             (void)nodes;
             items[i].geo = g->geo;
             items[i].args = F32GridArgs{g->images_f.p, g->bin_start.p, g->pab.p, g->pff.p,
-                                        g->tables.p};
+                                        g->tables.p, nullptr, 0u};
             items[i].brick0 = b->total;
             b->total += (uint64_t)g->geo.bricks[0] * g->geo.bricks[1] * g->geo.bricks[2];
         }

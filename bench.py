@@ -426,7 +426,8 @@ def main():
                 "frac_vs_scalar_peak": achieved / scalar_peak,
                 "frac_vs_packed_peak": achieved / packed_peak,
                 "traffic": SWEEP_DRAM_BYTES_PER_LAUNCH if args.workload == "full" else None,
-                "kernel": "grid_build_f32_kernel<2,SHIFTED>",
+                "kernel": "grid_build_f32_kernel<2,SHIFTED>, timed with the grid_plan_kernel "
+                          "launch before it (the bricks' row plans, ~1 % of the time)",
                 "kernel_ms": sweep,
                 "flops_per_pair": FLOPS_PER_PAIR,
                 "executed_pairs_per_step": int(st["executed_pairs"]),
