@@ -63,6 +63,7 @@ constexpr float CUT_BAND = 1e-5f;
 // FP32 form: Coulomb pairs closer than 4.5 A in FP64 (closer, a pair's
 // real-space term reaches 1e4-1e5 K, where FP32 rounding would leave ~1e-2 K)
 constexpr float NEAR_COULOMB_R2 = 20.25f;
+constexpr int NEAR_W = 64;  // FP32 form: near-Coulomb pairs a warp defers in one energy pass
 constexpr int MAXROWS = 8;  // distinct LJ species among the guest sites
 constexpr int MAXCB = 16;   // orientation trials of a biased insertion or deletion
 
@@ -747,6 +748,8 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     __shared__ PairCloseFF srowff[F32 ? MAXROWS : 1][64];
     __shared__ float4 sph[F32 ? 2 * NS : 1], spl[F32 ? 2 * NS : 1];  // trial sites, hi + lo
     __shared__ uint4 sfq[F32 ? 2 * NS : 1];                          // and in fixed point
+    __shared__ uint32_t nearq[F32 ? GT / 32 : 1][NEAR_W];  // deferred near-Coulomb pairs (j << 4 | slot)
+    __shared__ uint32_t nearn[GT / 32];
     extern __shared__ __align__(16) unsigned char dyn[];
 
     const int chain = blockIdx.x;
@@ -862,12 +865,45 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 }
                 const float rc2f = (float)C.rc2, rcf = (float)C.rc, rce2f = (float)C.rc_ew2,
                             alphaf = (float)C.alpha;
-                for (uint64_t j = j0 + threadIdx.x; j < n_all; j += GT) {
-                    bool skip = false;
-                    if (n_old)
+                const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+                // atom j's records and its FP64 real-space Coulomb term with site
+                // slot e (a near pair: within 4.5 A, where the term reaches 1e4-1e5
+                // K), from the double-float displacement and charge
+                auto near_coulomb = [&](uint64_t j, int e) -> double {
+                    float4 ah, al;
+                    if (j < C.n_fw) {
+                        ah = P.fwh[j];
+                        al = P.fwl[j];
+                    } else {
+                        ah = ghi[j - C.n_fw];
+                        al = glo[j - C.n_fw];
+                    }
+                    const float4 ph = sph[e], pl = spl[e];
+                    ff dx = ff_add(ff{ah.x, al.x}, ff{-ph.x, -pl.x});
+                    ff dy = ff_add(ff{ah.y, al.y}, ff{-ph.y, -pl.y});
+                    ff dz = ff_add(ff{ah.z, al.z}, ff{-ph.z, -pl.z});
+                    ff_min_image(C.lh, C.ll, C.linv, C.L.ortho, dx, dy, dz);
+                    const double ddx = (double)dx.hi + dx.lo, ddy = (double)dy.hi + dy.lo,
+                                 ddz = (double)dz.hi + dz.lo;
+                    const double rd = fmax(sqrt(ddx * ddx + ddy * ddy + ddz * ddz), 1e-6);
+                    return ((double)ah.w + (double)al.w) * (erfc(C.alpha * rd) / rd);
+                };
+                // Warp-uniform chunks of 32 atoms (lane l: atom jb + l). The near
+                // Coulomb pairs are not evaluated where they are found: FP64 issues
+                // at a small fraction of the FP32 rate and a warp pays a whole FP64
+                // instruction for one lane, so a chunk's near pairs are appended to
+                // the warp's list in (lane, slot) order and evaluated after the loop
+                // by all threads, one pair a thread (a warp whose list is full
+                // evaluates them in place).
+                uint32_t nq = 0;  // entries in this warp's list (the same on every lane)
+                for (uint64_t jb = j0 + (uint64_t)(threadIdx.x & ~31); jb < n_all; jb += GT) {
+                    const uint64_t j = jb + (uint64_t)lane;
+                    uint32_t nm = 0;  // slots whose Coulomb pair with atom j is near
+                    bool skip = j >= n_all;
+                    if (!skip && n_old)
 #pragma unroll
                         for (int x = 0; x < NS; ++x) skip |= (S.ex[x] == (uint32_t)j);
-                    if (skip) continue;
+                    if (!skip) {
                     float4 ah, al;
                     uint4 aq = make_uint4(0u, 0u, 0u, 0u);
                     uint32_t ta;
@@ -933,18 +969,47 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         }
                         if (el_in) {
                             if (r2 < NEAR_COULOMB_R2) {
-                                // a near pair (its real-space term reaches 1e4-1e5 K):
-                                // in FP64 from the double-float displacement and charge
-                                const double ddx = (double)dx.hi + dx.lo, ddy = (double)dy.hi + dy.lo,
-                                             ddz = (double)dz.hi + dz.lo;
-                                const double rd = fmax(sqrt(ddx * ddx + ddy * ddy + ddz * ddz), 1e-6);
-                                near_el[e] += ((double)ah.w + (double)al.w) * (erfc(C.alpha * rd) / rd);
+                                nm |= 1u << e;  // (NEAR_COULOMB_R2 < NEAR_R2: dx, dy, dz are double-float)
                             } else {
                                 const float r = sqrtf(r2);
                                 accf[2 * e + 1] += qa * (erfcf(alphaf * r) / r);
                             }
                         }
                     }
+                    }
+                    // append the chunk's near pairs: lane order, then slot order
+                    const uint32_t cnt = (uint32_t)__popc(nm);
+                    uint32_t pre = cnt;  // inclusive prefix over the lanes
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, pre, o);
+                        if (lane >= o) pre += y;
+                    }
+                    const uint32_t tot = __shfl_sync(0xffffffffu, pre, 31);
+                    if (nq + tot <= NEAR_W) {
+                        uint32_t at = nq + pre - cnt;
+                        for (uint32_t m = nm; m; m &= m - 1)
+                            nearq[wid][at++] = ((uint32_t)j << 4) | (uint32_t)(__ffs(m) - 1);
+                        nq += tot;
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 2 * NS; ++e)
+                            if ((nm >> e) & 1u) near_el[e] += near_coulomb(j, e);
+                    }
+                }
+                if (lane == 0) nearn[wid] = nq;
+                __syncthreads();
+                // the warps' lists in warp order, entry i on thread i mod GT
+                for (uint32_t i = threadIdx.x;; i += GT) {
+                    uint32_t w = 0, base = 0;
+                    while (w < GT / 32 && base + nearn[w] <= i) base += nearn[w++];
+                    if (w == GT / 32) break;
+                    const uint32_t code = nearq[w][i - base];
+                    const int e = (int)(code & 15u);
+                    const double val = near_coulomb(code >> 4, e);
+#pragma unroll
+                    for (int e2 = 0; e2 < 2 * NS; ++e2)
+                        if (e == e2) near_el[e2] += val;
                 }
                 // this thread's sums as double-float, added over the block
                 ff v[4 * NS];
