@@ -108,6 +108,7 @@ _SIGNATURES = {
     "alea_device_info": (ctypes.c_int32, [ctypes.c_char_p, ctypes.c_size_t, _I32, _I32, _I32]),
     "alea_probe_fp32_fma_tflops": (ctypes.c_int32, [_D]),
     "alea_probe_fp32x2_fma_tflops": (ctypes.c_int32, [_D]),
+    "alea_test_ff_near": (ctypes.c_int32, [ctypes.c_int32, _D, _D, ctypes.c_uint64, ctypes.c_double]),
     "alea_cached_bytes": (ctypes.c_int32, [_U64]),
     "alea_release_cached": (ctypes.c_int32, [_U64]),
     "alea_test_block_cache": (ctypes.c_int32, []),

@@ -60,12 +60,17 @@ constexpr float NEAR_R2 = 6.0f * 6.0f;
 // the near sphere under 1 % of the cell: 100 x (4/3) pi 6^3 A^3
 constexpr double FIXED_FAR_VOLUME = 100.0 * 4.0 / 3.0 * 3.14159265358979 * 216.0;
 constexpr float CUT_BAND = 1e-5f;
-// FP32 form: Coulomb pairs closer than 4.5 A in FP64 (closer, a pair's
-// real-space term reaches 1e4-1e5 K, where FP32 rounding would leave ~1e-2 K)
-constexpr float NEAR_COULOMB_R2 = 20.25f;
-constexpr int NEAR_W = 64;  // FP32 form: near-Coulomb pairs a warp defers in one energy pass
+// FP32 form: Coulomb pairs closer than 6 A in double-float (ff.cuh
+// near_coulomb_ff; closer, a pair's real-space term reaches 1e2-1e5 K, where
+// FP32 rounding would leave up to ~1e-2 K)
+constexpr float NEAR_COULOMB_R2 = 36.0f;
+constexpr int NEAR_W = 128;  // FP32 form: near-Coulomb pairs a warp defers in one energy pass
 constexpr int MAXROWS = 8;  // distinct LJ species among the guest sites
 constexpr int MAXCB = 16;   // orientation trials of a biased insertion or deletion
+// FP32 form: up to FUSE_MAX orientation trials are evaluated in one energy
+// pass (all trial sites against every atom and reciprocal term at once);
+// more, one pass each as in the FP64 form
+constexpr int FUSE_MAX = 8;
 
 struct GcmcConst {
     Lattice L;
@@ -187,6 +192,11 @@ struct StepShared {
     double cb_q[MAXCB][4];
     double cb_lw[MAXCB];
     double cb_u0, cb_logw, cb_du;
+    // trial orientations 1..cb_ndraw drawn by warp 0's lanes at once, from
+    // the consecutive Philox calls that begin at cb_call0 (three each)
+    uint64_t cb_call0;
+    int cb_ndraw;
+    double cb_e[MAXCB];  // exp(lw_j - max lw), formed by warp 0's lanes
 };
 
 // FP32 form: a guest site's pair terms with one framework or guest type:
@@ -298,6 +308,7 @@ __device__ __forceinline__ void rotate_site(const double* loc, const double* q, 
 
 // randomUnitQuaternion (monte_carlo_engine.cc:56-63) over three draws taken
 // in the engine's argument order.
+__device__ __forceinline__ void quaternion_from(const double* v, double* q);
 __device__ __forceinline__ void draw_quaternion(const GcmcConst& C, ChainState& c, double* q,
                                                 bool swap_order) {
     double v[3];
@@ -309,6 +320,10 @@ __device__ __forceinline__ void draw_quaternion(const GcmcConst& C, ChainState& 
         v[0] = v[2];
         v[2] = t;
     }
+    quaternion_from(v, q);
+}
+// The quaternion of three draws (already in the engine's argument order).
+__device__ __forceinline__ void quaternion_from(const double* v, double* q) {
     const double r1 = __dsqrt_rn(sub_rn(1.0, v[0])), r2 = __dsqrt_rn(v[0]);
     const double t1 = mul_rn(2.0 * kPi, v[1]), t2 = mul_rn(2.0 * kPi, v[2]);
     double s1, c1, s2, c2;
@@ -593,15 +608,26 @@ __device__ void cbmc_begin(const GcmcConst& C, ChainState& c, StepShared& S) {
     S.cb = 0;
     S.cb_more = 0;
     S.cb_pass = 0;
+    S.cb_ndraw = 0;
     if (C.orient <= 1 || !S.valid) return;
     if (S.move == 2 && C.sp_ns[S.sp_new] > 1) {
-        for (int j = 1; j < C.orient; ++j) draw_quaternion(C, c, S.cb_q[j], false);
+        // trials 1..k-1 take the next 3 (k - 1) calls; warp 0 forms them
+        S.cb_call0 = c.call;
+        S.cb_ndraw = C.orient - 1;
+        c.call += 3 * (uint64_t)(C.orient - 1);
         S.cb = 1;
     } else if (S.move == 3 && C.sp_ns[S.sp_old] > 1) {
         for (int i = 0; i < 3; ++i) S.cb_ref[i] = 0.0;
         for (int s = 0; s < S.n_old; ++s)
             for (int i = 0; i < 3; ++i) S.cb_ref[i] += S.op[s][i];
         for (int i = 0; i < 3; ++i) S.cb_ref[i] /= (double)S.n_old;
+        // one pass for every trial (FP32 form): the rotations drawn now, in the
+        // order the pass-by-pass scheme draws them between its passes
+        if (C.f32 && C.orient <= FUSE_MAX) {
+            S.cb_call0 = c.call;
+            S.cb_ndraw = C.orient - 1;
+            c.call += 3 * (uint64_t)(C.orient - 1);
+        }
         S.cb = 2;
     }
 }
@@ -613,6 +639,28 @@ __device__ double cbmc_log_mean(const double* lw, int k) {
     double s = 0.0;
     for (int j = 0; j < k; ++j) s += exp(lw[j] - m);
     return m + log(s / (double)k);
+}
+
+// Thread 0, an insertion's k trial weights known: log(W / k), one draw picks
+// trial j with probability w_j / W; its energy becomes the move's.
+__device__ int cbmc_pick(ChainState& c, StepShared& S, int k, double T) {
+    S.cb_logw = cbmc_log_mean(S.cb_lw, k);
+    double m = S.cb_lw[0];
+    for (int j = 1; j < k; ++j) m = fmax(m, S.cb_lw[j]);
+    double tot = 0.0;
+    for (int j = 0; j < k; ++j) tot += exp(S.cb_lw[j] - m);
+    const double u = u01(c) * tot;
+    int pick = k - 1;
+    double cum = 0.0;
+    for (int j = 0; j < k; ++j) {
+        cum += exp(S.cb_lw[j] - m);
+        if (u < cum) {
+            pick = j;
+            break;
+        }
+    }
+    S.cb_du = -S.cb_lw[pick] * T;
+    return pick;
 }
 
 // Thread 0, after an energy pass of an orientation-biased move: records the
@@ -642,22 +690,7 @@ __device__ void cbmc_after_pass(const GcmcConst& C, ChainState& c, StepShared& S
             return;
         }
         if (p == k - 1) {  // pick a trial with probability w_j / W
-            S.cb_logw = cbmc_log_mean(S.cb_lw, k);
-            double m = S.cb_lw[0];
-            for (int j = 1; j < k; ++j) m = fmax(m, S.cb_lw[j]);
-            double tot = 0.0;
-            for (int j = 0; j < k; ++j) tot += exp(S.cb_lw[j] - m);
-            const double u = u01(c) * tot;
-            int pick = k - 1;
-            double cum = 0.0;
-            for (int j = 0; j < k; ++j) {
-                cum += exp(S.cb_lw[j] - m);
-                if (u < cum) {
-                    pick = j;
-                    break;
-                }
-            }
-            S.cb_du = -S.cb_lw[pick] * T;
+            const int pick = cbmc_pick(c, S, k, T);
             if (pick != k - 1) {  // evaluate the picked trial again (its sites and S(k) delta)
                 place_new(C, S.sp_new, S.cb_ref, S.cb_q[pick], true, S);
                 S.cb_pass = k;
@@ -716,24 +749,27 @@ __host__ __device__ size_t f32_ab_bytes(int kmax) {
     return 2 * NS * tw * tw * sizeof(float2);
 }
 template <int NS>
-size_t phase_bytes(int kmax, bool f32) {
+__host__ __device__ size_t phase_bytes(int kmax, bool f32) {
     const size_t tw = 2 * (size_t)kmax + 1;
     if (!f32) return 2 * NS * 3 * tw * sizeof(double2);
     const size_t ab = f32_ab_bytes<NS>(kmax);
     return 2 * NS * 3 * tw * sizeof(float2) + (ab <= AB_TABLE_BUDGET ? ab : 0);
 }
 
-// FP32 form: the trial sites as double-float (hi, lo) and fixed-point copies.
+// FP32 form: slot e's site as double-float (hi, lo) and fixed-point copies.
+template <int NS, bool FX>
+__device__ __forceinline__ void prep_site_f32(const GcmcConst& C, const StepShared& S, int e,
+                                              float4* sph, float4* spl, uint4* sfq) {
+    const double* p = e < NS ? S.op[e] : S.np_[e - NS];
+    const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
+    sph[e] = make_float4(x.hi, y.hi, z.hi, 0.f);
+    spl[e] = make_float4(x.lo, y.lo, z.lo, 0.f);
+    if constexpr (FX) sfq[e] = fixed_frac(C.L, p[0], p[1], p[2]);
+}
 template <int NS, bool FX>
 __device__ __forceinline__ void prep_sites_f32(const GcmcConst& C, const StepShared& S, float4* sph,
                                                float4* spl, uint4* sfq) {
-    for (int e = 0; e < 2 * NS; ++e) {
-        const double* p = e < NS ? S.op[e] : S.np_[e - NS];
-        const ff x = ff_from(p[0]), y = ff_from(p[1]), z = ff_from(p[2]);
-        sph[e] = make_float4(x.hi, y.hi, z.hi, 0.f);
-        spl[e] = make_float4(x.lo, y.lo, z.lo, 0.f);
-        if constexpr (FX) sfq[e] = fixed_frac(C.L, p[0], p[1], p[2]);
-    }
+    for (int e = 0; e < 2 * NS; ++e) prep_site_f32<NS, FX>(C, S, e, sph, spl, sfq);
 }
 
 // FX (FP32 form, large cells): far pairs on the fixed-point displacement.
@@ -749,6 +785,10 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     __shared__ float4 sph[F32 ? 2 * NS : 1], spl[F32 ? 2 * NS : 1];  // trial sites, hi + lo
     __shared__ uint4 sfq[F32 ? 2 * NS : 1];                          // and in fixed point
     __shared__ uint32_t nearq[F32 ? GT / 32 : 1][NEAR_W];  // deferred near-Coulomb pairs (j << 4 | slot)
+    // FP32 form, orientation trials in one pass: the trial sites (FP64, hi + lo, fixed point)
+    __shared__ double tpos[F32 ? FUSE_MAX * NS : 1][3];
+    __shared__ float4 tph[F32 ? FUSE_MAX * NS : 1], tpl[F32 ? FUSE_MAX * NS : 1];
+    __shared__ uint4 tfq[F32 ? FUSE_MAX * NS : 1];
     __shared__ uint32_t nearn[GT / 32];
     extern __shared__ __align__(16) unsigned char dyn[];
 
@@ -790,7 +830,9 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
     double2* etab = reinterpret_cast<double2*>(dyn);               // FP64 form: [2NS][3][tw]
     float2* etab32 = reinterpret_cast<float2*>(dyn);               // FP32 form: [2NS][3][tw]
     float2* ab32 = etab32 + (size_t)2 * NS * 3 * tw;                // [2NS][tw][tw]
+    float2* ftab32 = reinterpret_cast<float2*>(dyn + phase_bytes<NS>(C.kmax, true));  // [trial sites][3][tw]
     const bool ab_table = F32 && f32_ab_bytes<NS>(C.kmax) <= AB_TABLE_BUDGET;
+    const ff alpha_ff = ff_from(C.alpha);
     __syncthreads();
 
     for (uint64_t step = 0; step < steps; ++step) {
@@ -799,13 +841,27 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 plan_move(C, P, c, gx, gy, gz, mol, msp, S);
                 slot_tables(C, S);
                 cbmc_begin(C, c, S);
-                if constexpr (F32) prep_sites_f32<NS, FX>(C, S, sph, spl, sfq);
             } else {
                 S.valid = 0;
             }
         }
         __syncthreads();
         if (S.valid) {
+            // the move's parallel set-up: trial orientations 1..cb_ndraw, one a
+            // lane of warp 0 (the same draws and arithmetic as one after the
+            // other on thread 0), and (FP32 form) the slots' FP32 copies, one a
+            // thread of warp 1
+            if (threadIdx.x < S.cb_ndraw) {
+                const uint64_t c0 = S.cb_call0 + 3 * (uint64_t)threadIdx.x;
+                const double v[3] = {philox_uniform(c.seed, c.stream, c0),
+                                     philox_uniform(c.seed, c.stream, c0 + 1),
+                                     philox_uniform(c.seed, c.stream, c0 + 2)};
+                quaternion_from(v, S.cb_q[threadIdx.x + 1]);
+            }
+            if constexpr (F32)
+                if (threadIdx.x >= 32 && threadIdx.x < 32 + 2 * NS)
+                    prep_site_f32<NS, FX>(C, S, (int)threadIdx.x - 32, sph, spl, sfq);
+            __syncthreads();
             int n_old = S.n_old, n_new = S.n_new;  // this energy pass's site counts
             const uint64_t n_all = C.n_fw + S.ng;
             // FP32 form: term t's S(k) delta, added sites first then removed
@@ -843,6 +899,386 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
             // with a grid the framework's LJ comes from the tables: its atoms
             // are visited only for the real-space Ewald terms
             const uint64_t j0 = (C.grid && !C.charged) ? C.n_fw : 0;
+            // FP32 form: the slots' phase tables, e^{i n theta_a} in FP32 (the
+            // angle reduced to [-pi, pi] in FP64 first), then (when it fits)
+            // q e^{i (n0 theta_0 + n1 theta_1)}; every thread calls it
+            auto tables_f32 = [&]() {
+                for (int i = threadIdx.x; i < 2 * NS * 3 * tw; i += GT) {
+                    const int e = i / (3 * tw), a = (i / tw) % 3, n = i % tw - K;
+                    const bool is_old = e < NS;
+                    if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
+                    const int s = is_old ? e : e - NS;
+                    const double* p = is_old ? S.op[s] : S.np_[s];
+                    const double th = C.b[3 * a] * p[0] + C.b[3 * a + 1] * p[1] + C.b[3 * a + 2] * p[2];
+                    const double x = (double)n * th;
+                    const double r = x - (2.0 * kPi) * rint(x * (0.5 / kPi));
+                    float sn, cs;
+                    sincosf((float)r, &sn, &cs);
+                    etab32[i] = make_float2(cs, sn);
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; ab_table && i < 2 * NS * tw * tw; i += GT) {
+                    const int e = i / (tw * tw), n0 = (i / tw) % tw, n1 = i % tw;
+                    const bool is_old = e < NS;
+                    if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
+                    const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1];
+                    const float q = S.sq32[e];
+                    ab32[i] = make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
+                }
+                __syncthreads();
+            };
+            // FP32 form, orientation-biased move with k <= FUSE_MAX trials: every
+            // trial in one energy pass. Trial t's site s is trial site t ns + s:
+            // insertion, the species' template about its centroid cb_ref rotated
+            // by cb_q[t]; deletion, trial 0 is the molecule itself (its energy
+            // U_0 from its removal) and trial t > 0 the template rotated by
+            // cb_q[t] about the molecule's centroid, inserted into the chain
+            // without the molecule. Per trial: LJ and real-space sums over the
+            // atoms (the molecule's own sites excluded in a deletion) and the
+            // reciprocal change against S(k); thread 0 then forms the Rosenbluth
+            // weights as the pass-by-pass scheme does, picks (insertion), and
+            // leaves the move's final sites for the acceptance and the commit.
+            const bool fused = F32 && S.cb != 0 && C.orient <= FUSE_MAX;
+            if (fused) {
+                const int k = C.orient;
+                const bool ins = S.cb == 1;
+                const int sp = ins ? S.sp_new : S.sp_old;
+                const int ns = C.sp_ns[sp];
+                const int nt = k * ns;
+                for (int i = threadIdx.x; i < nt; i += GT) {
+                    const int t = i / ns, s = i % ns;
+                    double pos[3];
+                    if (!ins && t == 0) {
+                        for (int a = 0; a < 3; ++a) pos[a] = S.op[s][a];
+                    } else {
+                        const double loc[3] = {C.tc[sp][s][0], C.tc[sp][s][1], C.tc[sp][s][2]};
+                        double rot[3];
+                        rotate_site(loc, S.cb_q[t], rot);
+                        for (int a = 0; a < 3; ++a) pos[a] = add_rn(S.cb_ref[a], rot[a]);
+                    }
+                    for (int a = 0; a < 3; ++a) tpos[i][a] = pos[a];
+                    const ff x = ff_from(pos[0]), y = ff_from(pos[1]), z = ff_from(pos[2]);
+                    tph[i] = make_float4(x.hi, y.hi, z.hi, 0.f);
+                    tpl[i] = make_float4(x.lo, y.lo, z.lo, 0.f);
+                    if constexpr (FX) tfq[i] = fixed_frac(C.L, pos[0], pos[1], pos[2]);
+                }
+                __syncthreads();
+                float qs32[NS];
+                double qs64[NS];
+                int rows[NS];
+#pragma unroll
+                for (int s = 0; s < NS; ++s) {
+                    qs64[s] = s < ns ? C.spq[sp][s] : 0.0;
+                    qs32[s] = (float)qs64[s];
+                    rows[s] = s < ns ? C.sprow[sp][s] : 0;
+                }
+                // per trial, in double-float: LJ (close pairs and far terms), the
+                // far real-space terms times the site charges (a trial's sites'
+                // terms cancel in part, which one FP32 sum would not resolve);
+                // the near pairs' FP64 terms
+                ff lj_t[FUSE_MAX], el_t[FUSE_MAX];
+                double near_t[FUSE_MAX];
+#pragma unroll
+                for (int t = 0; t < FUSE_MAX; ++t) {
+                    lj_t[t] = el_t[t] = ff{0.f, 0.f};
+                    near_t[t] = 0.0;
+                }
+                const float rc2f = (float)C.rc2, rcf = (float)C.rc, rce2f = (float)C.rc_ew2,
+                            alphaf = (float)C.alpha;
+                const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+                // atom a's displacement from trial site i, double-float
+                auto disp_ff = [&](const float4& ah, const float4& al, int i, ff& dx, ff& dy, ff& dz) {
+                    const float4 ph = tph[i], pl = tpl[i];
+                    dx = ff_add(ff{ah.x, al.x}, ff{-ph.x, -pl.x});
+                    dy = ff_add(ff{ah.y, al.y}, ff{-ph.y, -pl.y});
+                    dz = ff_add(ff{ah.z, al.z}, ff{-ph.z, -pl.z});
+                    ff_min_image(C.lh, C.ll, C.linv, C.L.ortho, dx, dy, dz);
+                };
+                // the real-space term of near pair (atom a, trial site i) times
+                // the site's charge, in double-float (FP64 beyond the series)
+                auto near_term = [&](uint64_t a, int i) -> double {
+                    float4 ah, al;
+                    if (a < C.n_fw) {
+                        ah = P.fwh[a];
+                        al = P.fwl[a];
+                    } else {
+                        ah = ghi[a - C.n_fw];
+                        al = glo[a - C.n_fw];
+                    }
+                    ff dx, dy, dz;
+                    disp_ff(ah, al, i, dx, dy, dz);
+                    double v;
+                    if (near_coulomb_ff(dx, dy, dz, ff{ah.w, al.w}, alpha_ff, v)) return C.spq[sp][i % ns] * v;
+                    const double ddx = (double)dx.hi + dx.lo, ddy = (double)dy.hi + dy.lo,
+                                 ddz = (double)dz.hi + dz.lo;
+                    const double rd = fmax(sqrt(ddx * ddx + ddy * ddy + ddz * ddz), 1e-6);
+                    return C.spq[sp][i % ns] * (((double)ah.w + (double)al.w) * (erfc(C.alpha * rd) / rd));
+                };
+                uint32_t nq = 0;
+                for (uint64_t jb = j0 + (uint64_t)(threadIdx.x & ~31); jb < n_all; jb += GT) {
+                    const uint64_t j = jb + (uint64_t)lane;
+                    uint64_t nm = 0;  // trial sites whose Coulomb pair with atom j is near
+                    bool skip = j >= n_all;
+                    if (!skip && !ins)
+#pragma unroll
+                        for (int x = 0; x < NS; ++x) skip |= (S.ex[x] == (uint32_t)j);
+                    if (!skip) {
+                        float4 ah, al;
+                        uint4 aq = make_uint4(0u, 0u, 0u, 0u);
+                        uint32_t ta;
+                        if (j < C.n_fw) {
+                            ah = P.fwh[j];
+                            al = P.fwl[j];
+                            if constexpr (FX) aq = P.fwq[j];
+                            ta = P.fw_type[j];
+                        } else {
+                            const uint64_t g = j - C.n_fw;
+                            ah = ghi[g];
+                            al = glo[g];
+                            if constexpr (FX) aq = gq4[g];
+                            ta = gt[g];
+                        }
+#pragma unroll
+                        for (int t = 0; t < FUSE_MAX; ++t) {
+                            if (t >= k) break;
+#pragma unroll
+                            for (int s = 0; s < NS; ++s) {
+                                if (s >= ns) break;
+                                const int i = t * ns + s;
+                                float cx = 0.f, cy = 0.f, cz = 0.f, r2 = 0.f;
+                                bool near = true;
+                                if constexpr (FX) {
+                                    const uint4 pq = tfq[i];
+                                    const float fx = (float)(int32_t)(aq.x - pq.x) * 2.3283064365386963e-10f;
+                                    const float fy = (float)(int32_t)(aq.y - pq.y) * 2.3283064365386963e-10f;
+                                    const float fz = (float)(int32_t)(aq.z - pq.z) * 2.3283064365386963e-10f;
+                                    cx = fmaf(fx, C.lh[0], fmaf(fy, C.lh[3], fz * C.lh[6]));
+                                    cy = fmaf(fx, C.lh[1], fmaf(fy, C.lh[4], fz * C.lh[7]));
+                                    cz = fmaf(fx, C.lh[2], fmaf(fy, C.lh[5], fz * C.lh[8]));
+                                    r2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+                                    near = r2 < NEAR_R2 ||
+                                           (C.trunc == ALEA_TRUNCATED && fabsf(r2 - rc2f) <= CUT_BAND * rc2f);
+                                }
+                                ff dx{cx, 0.f}, dy{cy, 0.f}, dz{cz, 0.f};
+                                if (near) {
+                                    disp_ff(ah, al, i, dx, dy, dz);
+                                    r2 = fmaf(dx.hi, dx.hi, fmaf(dy.hi, dy.hi, dz.hi * dz.hi));
+                                }
+                                const bool lj_in = !(C.grid && j < C.n_fw) && r2 <= rc2f;
+                                const bool el_in = C.charged && r2 <= rce2f;
+                                if (lj_in) {
+                                    const PairF32 q = srow32[rows[s]][ta];
+                                    if (r2 < q.sig2) {
+                                        const ff rr = ff_add(ff_add(ff_mul(dx, dx), ff_mul(dy, dy)), ff_mul(dz, dz));
+                                        lj_t[t] = ff_add(lj_t[t], lj_close_ff(srowff[rows[s]][ta], rr, rcf, C.trunc));
+                                    } else {
+                                        const float ir2 = 1.0f / r2;
+                                        const float ir6 = ir2 * ir2 * ir2;
+                                        float v = ir6 * fmaf(q.a, ir6, -q.b) - q.shift;
+                                        if (C.trunc == ALEA_LINEAR_FORCE_SHIFTED) v -= (sqrtf(r2) - rcf) * q.dvdrc;
+                                        lj_t[t] = ff_add_f(lj_t[t], v);
+                                    }
+                                }
+                                if (el_in) {
+                                    if (r2 < NEAR_COULOMB_R2) {
+                                        nm |= 1ull << i;
+                                    } else {
+                                        const float r = sqrtf(r2);
+                                        el_t[t] = ff_add_f(el_t[t], qs32[s] * (ah.w * (erfcf(alphaf * r) / r)));
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    // the chunk's near pairs into the warp's list (lane order,
+                    // then trial-site order), or at once when it is full
+                    const uint32_t cnt = (uint32_t)__popcll(nm);
+                    uint32_t pre = cnt;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, pre, o);
+                        if (lane >= o) pre += y;
+                    }
+                    const uint32_t tot = __shfl_sync(0xffffffffu, pre, 31);
+                    if (nq + tot <= NEAR_W) {
+                        uint32_t at = nq + pre - cnt;
+                        for (uint64_t m = nm; m; m &= m - 1)
+                            nearq[wid][at++] = ((uint32_t)j << 8) | (uint32_t)(__ffsll((long long)m) - 1);
+                        nq += tot;
+                    } else {
+                        for (uint64_t m = nm; m; m &= m - 1) {
+                            const int i = __ffsll((long long)m) - 1;
+                            const double v = near_term(j, i);
+#pragma unroll
+                            for (int t = 0; t < FUSE_MAX; ++t)
+                                if (i / ns == t) near_t[t] += v;
+                        }
+                    }
+                }
+                if (lane == 0) nearn[wid] = nq;
+                __syncthreads();
+                for (uint32_t e = threadIdx.x;; e += GT) {
+                    uint32_t w = 0, base = 0;
+                    while (w < GT / 32 && base + nearn[w] <= e) base += nearn[w++];
+                    if (w == GT / 32) break;
+                    const uint32_t code = nearq[w][e - base];
+                    const int i = (int)(code & 255u);
+                    const double v = near_term(code >> 8, i);
+#pragma unroll
+                    for (int t = 0; t < FUSE_MAX; ++t)
+                        if (i / ns == t) near_t[t] += v;
+                }
+                if (C.grid) {  // thread i adds trial site i's interpolated table
+                    if (threadIdx.x < nt) {
+                        const int i = threadIdx.x;
+                        const double* tab = P.gtab[C.sprow[sp][i % ns]];
+                        const double g = C.grid_fast
+                            ? grid_interp_fast(C.L, C.gn[0], C.gn[1], C.gn[2], tab, tpos[i][0], tpos[i][1], tpos[i][2])
+                            : grid_interp_ref(C.L, C.gn[0], C.gn[1], C.gn[2], tab, tpos[i][0], tpos[i][1], tpos[i][2]);
+#pragma unroll
+                        for (int t = 0; t < FUSE_MAX; ++t)
+                            if (i / ns == t) lj_t[t] = ff_add(lj_t[t], ff_from(g));
+                    }
+                }
+                ff v[2 * FUSE_MAX];
+#pragma unroll
+                for (int t = 0; t < FUSE_MAX; ++t) {
+                    v[2 * t] = lj_t[t];
+                    v[2 * t + 1] = ff_add(ff_from(near_t[t]), el_t[t]);
+                }
+                static_assert(2 * FUSE_MAX < RSTRIDE, "fused sums fit a reduction row");
+                block_sum_ff(v, 2 * FUSE_MAX, red);
+                double pair_u[FUSE_MAX];  // per trial: LJ + real-space Coulomb
+                if (threadIdx.x == 0)
+#pragma unroll
+                    for (int t = 0; t < FUSE_MAX; ++t)
+                        pair_u[t] = red[(GT / 32) * RSTRIDE + 2 * t] +
+                                    red[(GT / 32) * RSTRIDE + 2 * t + 1] * kCoulomb;
+                __syncthreads();
+                double rec_t[FUSE_MAX];  // per trial: the reciprocal change
+#pragma unroll
+                for (int t = 0; t < FUSE_MAX; ++t) rec_t[t] = 0.0;
+                if (C.charged) {
+                    // the trial sites' FP32 phases (angles reduced in FP64)
+                    for (int i = threadIdx.x; i < nt * 3 * tw; i += GT) {
+                        const int e = i / (3 * tw), a = (i / tw) % 3, n = i % tw - K;
+                        const double th = C.b[3 * a] * tpos[e][0] + C.b[3 * a + 1] * tpos[e][1] +
+                                          C.b[3 * a + 2] * tpos[e][2];
+                        const double x = (double)n * th;
+                        const double r = x - (2.0 * kPi) * rint(x * (0.5 / kPi));
+                        float sn, cs;
+                        sincosf((float)r, &sn, &cs);
+                        ftab32[i] = make_float2(cs, sn);
+                    }
+                    __syncthreads();
+                    // per term and trial: its sites' delta d_t; insertion
+                    // w (2 S.d_t + |d_t|^2); deletion x = -d_0 for trial 0 and
+                    // d_t - d_0 for the rotations, w (2 S.x + |x|^2)
+                    float racc[FUSE_MAX];
+#pragma unroll
+                    for (int t = 0; t < FUSE_MAX; ++t) racc[t] = 0.f;
+                    for (uint64_t tt = threadIdx.x; tt < C.nk; tt += GT) {
+                        const uint32_t pk = P.npack[tt];
+                        const int n0 = pk & 0xff, n1 = (pk >> 8) & 0xff, n2 = (pk >> 16) & 0xff;
+                        const float2 o = sk_hi[tt];
+                        const float wv = P.w32[tt];
+                        float d0r = 0.f, d0i = 0.f;
+#pragma unroll
+                        for (int t = 0; t < FUSE_MAX; ++t) {
+                            if (t >= k) break;
+                            float re = 0.f, im = 0.f;
+#pragma unroll
+                            for (int s = 0; s < NS; ++s) {
+                                if (s >= ns) break;
+                                const int e = t * ns + s;
+                                const float2 A = ftab32[(e * 3 + 0) * tw + n0], B = ftab32[(e * 3 + 1) * tw + n1],
+                                             Cc = ftab32[(e * 3 + 2) * tw + n2];
+                                const float zr = qs32[s] * (A.x * B.x - A.y * B.y),
+                                            zi = qs32[s] * (A.x * B.y + A.y * B.x);
+                                re = fmaf(zr, Cc.x, fmaf(-zi, Cc.y, re));
+                                im = fmaf(zr, Cc.y, fmaf(zi, Cc.x, im));
+                            }
+                            float xr = re, xi = im;
+                            if (!ins) {
+                                if (t == 0) {
+                                    d0r = re;
+                                    d0i = im;
+                                    xr = -re;
+                                    xi = -im;
+                                } else {
+                                    xr = re - d0r;
+                                    xi = im - d0i;
+                                }
+                            }
+                            const float dot = fmaf(o.x, xr, o.y * xi);
+                            racc[t] = fmaf(wv, fmaf(2.f, dot, fmaf(xr, xr, xi * xi)), racc[t]);
+                        }
+                    }
+                    ff rv[FUSE_MAX];
+#pragma unroll
+                    for (int t = 0; t < FUSE_MAX; ++t) rv[t] = ff{racc[t], 0.f};
+                    block_sum_ff(rv, FUSE_MAX, red);
+#pragma unroll
+                    for (int t = 0; t < FUSE_MAX; ++t) rec_t[t] = C.rec_pref * red[(GT / 32) * RSTRIDE + t];
+                }
+                const double T = C.temperature;
+                if (threadIdx.x == 0) {
+                    double q2 = 0.0;
+                    for (int s = 0; s < ns; ++s) q2 += C.spq[sp][s] * C.spq[sp][s];
+                    // an insertion's self and exclusion terms (a removal's are their negatives)
+                    const double dself = C.charged ? C.self_pref * q2 : 0.0;
+                    const double dexcl = C.charged ? -kCoulomb * C.excl_tmpl[sp] : 0.0;
+                    if (ins) {
+                        for (int t = 0; t < k; ++t) S.cb_lw[t] = -(pair_u[t] + ((rec_t[t] + dself) + dexcl)) / T;
+                    } else {
+                        S.cb_u0 = pair_u[0] - ((rec_t[0] - dself) - dexcl);
+                        S.cb_lw[0] = -S.cb_u0 / T;
+                        for (int t = 1; t < k; ++t)
+                            S.cb_lw[t] = -(S.cb_u0 + ((pair_u[t] - pair_u[0]) + rec_t[t])) / T;
+                    }
+                }
+                // the weights exp(lw_j - max lw), one a lane of warp 0; thread 0
+                // then sums them in order (cbmc_log_mean and cbmc_pick's values)
+                if (threadIdx.x < 32) {
+                    __syncwarp();
+                    double m = S.cb_lw[0];
+                    for (int t = 1; t < k; ++t) m = fmax(m, S.cb_lw[t]);
+                    if (threadIdx.x < k) S.cb_e[threadIdx.x] = exp(S.cb_lw[threadIdx.x] - m);
+                    __syncwarp();
+                    if (threadIdx.x == 0) {
+                        double tot = 0.0;
+                        for (int t = 0; t < k; ++t) tot += S.cb_e[t];
+                        S.cb_logw = m + log(tot / (double)k);
+                        if (ins) {
+                            const double u = u01(c) * tot;
+                            int pick = k - 1;
+                            double cum = 0.0;
+                            for (int t = 0; t < k; ++t) {
+                                cum += S.cb_e[t];
+                                if (u < cum) {
+                                    pick = t;
+                                    break;
+                                }
+                            }
+                            S.cb_du = -S.cb_lw[pick] * T;
+                            // the picked trial's sites (place_new's values)
+                            for (int s = 0; s < ns; ++s)
+                                for (int a = 0; a < 3; ++a) S.np_[s][a] = tpos[pick * ns + s][a];
+                            S.n_new = ns;
+                            S.sp_new = sp;
+                        } else {
+                            S.cb_du = -S.cb_u0;
+                            S.n_new = 0;
+                        }
+                        slot_tables(C, S);
+                    }
+                }
+                __syncthreads();
+                n_old = S.n_old;
+                n_new = S.n_new;
+                // the final sites' phase tables, for the commit
+                if (C.charged) tables_f32();
+            } else
             for (;;) {  // energy passes: one, or several for an orientation-biased move
             n_old = S.n_old;
             n_new = S.n_new;
@@ -866,9 +1302,9 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                 const float rc2f = (float)C.rc2, rcf = (float)C.rc, rce2f = (float)C.rc_ew2,
                             alphaf = (float)C.alpha;
                 const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-                // atom j's records and its FP64 real-space Coulomb term with site
-                // slot e (a near pair: within 4.5 A, where the term reaches 1e4-1e5
-                // K), from the double-float displacement and charge
+                // atom j's records and its real-space Coulomb term with site slot e
+                // (a near pair, within 6 A) from the double-float displacement and
+                // charge, in double-float (FP64 beyond the erfc series)
                 auto near_coulomb = [&](uint64_t j, int e) -> double {
                     float4 ah, al;
                     if (j < C.n_fw) {
@@ -883,6 +1319,8 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                     ff dy = ff_add(ff{ah.y, al.y}, ff{-ph.y, -pl.y});
                     ff dz = ff_add(ff{ah.z, al.z}, ff{-ph.z, -pl.z});
                     ff_min_image(C.lh, C.ll, C.linv, C.L.ortho, dx, dy, dz);
+                    double v;
+                    if (near_coulomb_ff(dx, dy, dz, ff{ah.w, al.w}, alpha_ff, v)) return v;
                     const double ddx = (double)dx.hi + dx.lo, ddy = (double)dy.hi + dy.lo,
                                  ddz = (double)dz.hi + dz.lo;
                     const double rd = fmax(sqrt(ddx * ddx + ddy * ddy + ddz * ddz), 1e-6);
@@ -969,7 +1407,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
                         }
                         if (el_in) {
                             if (r2 < NEAR_COULOMB_R2) {
-                                nm |= 1u << e;  // (NEAR_COULOMB_R2 < NEAR_R2: dx, dy, dz are double-float)
+                                nm |= 1u << e;  // (NEAR_COULOMB_R2 <= NEAR_R2: dx, dy, dz are double-float)
                             } else {
                                 const float r = sqrtf(r2);
                                 accf[2 * e + 1] += qa * (erfcf(alphaf * r) / r);
@@ -1082,30 +1520,7 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
             // ---- reciprocal delta: removed = old sites, added = new sites
             if constexpr (F32) {
               if (C.charged) {
-                // FP32 phases (the angle reduced to [-pi, pi] in FP64 first)
-                for (int i = threadIdx.x; i < 2 * NS * 3 * tw; i += GT) {
-                    const int e = i / (3 * tw), a = (i / tw) % 3, n = i % tw - K;
-                    const bool is_old = e < NS;
-                    if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
-                    const int s = is_old ? e : e - NS;
-                    const double* p = is_old ? S.op[s] : S.np_[s];
-                    const double th = C.b[3 * a] * p[0] + C.b[3 * a + 1] * p[1] + C.b[3 * a + 2] * p[2];
-                    const double x = (double)n * th;
-                    const double r = x - (2.0 * kPi) * rint(x * (0.5 / kPi));
-                    float sn, cs;
-                    sincosf((float)r, &sn, &cs);
-                    etab32[i] = make_float2(cs, sn);
-                }
-                __syncthreads();
-                for (int i = threadIdx.x; ab_table && i < 2 * NS * tw * tw; i += GT) {
-                    const int e = i / (tw * tw), n0 = (i / tw) % tw, n1 = i % tw;
-                    const bool is_old = e < NS;
-                    if (is_old ? (e >= n_old) : (e - NS >= n_new)) continue;
-                    const float2 A = etab32[(e * 3 + 0) * tw + n0], B = etab32[(e * 3 + 1) * tw + n1];
-                    const float q = S.sq32[e];
-                    ab32[i] = make_float2(q * (A.x * B.x - A.y * B.y), q * (A.x * B.y + A.y * B.x));
-                }
-                __syncthreads();
+                tables_f32();
                 // per term w (2 S.delta + |delta|^2) in FP32 from the hi part of
                 // S; this thread's ~nk/256 terms summed in FP32, the block's
                 // partials in FP64. The delta is not stored: a commit forms it again.
@@ -1489,7 +1904,9 @@ gcmc_kernel(const GcmcConst C, const GcmcPtrs P, uint64_t steps) {
 template <int NS>
 void launch_chains(unsigned n_chains, const GcmcConst& C, const GcmcPtrs& P, uint64_t steps,
                    cudaStream_t s) {
-    const size_t bytes = C.charged ? phase_bytes<NS>(C.kmax, C.f32 != 0) : 0;
+    size_t bytes = C.charged ? phase_bytes<NS>(C.kmax, C.f32 != 0) : 0;
+    if (C.charged && C.f32 && C.orient > 1 && C.orient <= FUSE_MAX)  // the trial sites' tables
+        bytes = phase_bytes<NS>(C.kmax, true) + (size_t)C.orient * NS * 3 * (2 * C.kmax + 1) * sizeof(float2);
     if (C.f32) {
         auto kern = C.fixed_far ? gcmc_kernel<NS, true, true> : gcmc_kernel<NS, true, false>;
         ALEA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -2029,6 +2446,9 @@ void gcmc_set_precision(GcmcImpl* g, int precision) {
     require(precision == ALEA_FP64 || precision == ALEA_FP32, ALEA_ERR_INVALID_ARGUMENT,
             "GCMC: precision must be ALEA_FP64 or ALEA_FP32");
     const int f32 = precision == ALEA_FP32;
+    // the FP32 form lists near pairs as (atom << 8 | trial site) in 32 bits
+    require(!f32 || g->C.n_fw + g->C.max_sites < (1ull << 24), ALEA_ERR_INVALID_ARGUMENT,
+            "GCMC (FP32 form): framework atoms + max_molecules x sites must be below 2^24");
     const uint64_t n = g->C.nk * g->n_chains;
     if (f32 != g->C.f32 && g->C.charged && n) {  // carry the committed S(k) across
         convert_sk_kernel<<<(unsigned)((n + 255) / 256), 256>>>(n, f32, g->sre.p, g->sim.p,

@@ -4,6 +4,7 @@
 // figures only). Eight independent FMA chains per thread, every SM busy, timed
 // with CUDA events; the best of five launches.
 #include "common.cuh"
+#include "ff.cuh"
 
 namespace alea {
 namespace {
@@ -77,8 +78,43 @@ double time_fma(K kernel, double flops_per_thread_iter) {
     const double flops = flops_per_thread_iter * iters * (double)blocks * threads;
     return flops / (best * 1e-3) / 1e12;
 }
+// Test support: the FP32 forms' double-float near-pair arithmetic, element by
+// element. mode 0: erfc(x) (ff_erfc, x within its series); mode 1: q erfc(alpha
+// r) / r of displacement (a, b, c) and charge q (near_coulomb_ff; NaN where it
+// defers to FP64).
+__global__ void ff_check_kernel(int mode, const double* in, double* out, uint64_t n, double alpha) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (mode == 0) {
+        const ff r = ff_erfc(ff_from(in[i]));
+        out[i] = (double)r.hi + (double)r.lo;
+    } else {
+        double v;
+        const double* d = in + 4 * i;
+        out[i] = near_coulomb_ff(ff_from(d[0]), ff_from(d[1]), ff_from(d[2]), ff_from(d[3]),
+                                 ff_from(alpha), v) ? v : __longlong_as_double(0x7ff8000000000000ll);
+    }
+}
 }  // namespace
 }  // namespace alea
+
+extern "C" alea_status alea_test_ff_near(int32_t mode, const double* in, double* out, uint64_t n,
+                                         double alpha) {
+    try {
+        alea::require_device();
+        alea::require(mode == 0 || mode == 1, ALEA_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
+        if (n == 0) return ALEA_OK;
+        const uint64_t w = mode == 0 ? 1 : 4;
+        alea::DevBuf<double> din(n * w), dout(n);
+        din.upload(in, n * w);
+        alea::ff_check_kernel<<<(unsigned)((n + 255) / 256), 256>>>(mode, din.p, dout.p, n, alpha);
+        ALEA_CUDA(cudaGetLastError());
+        ALEA_CUDA(cudaMemcpy(out, dout.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+        return ALEA_OK;
+    } catch (const alea::Error& e) {
+        return e.status;
+    }
+}
 
 extern "C" alea_status alea_probe_fp32x2_fma_tflops(double* out) {
     try {

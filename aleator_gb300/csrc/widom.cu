@@ -31,10 +31,11 @@ namespace alea {
 namespace {
 
 constexpr int WT = 128;        // trials per block
-// FP32 form, charged trials: Coulomb pairs closer than 4.5 A are evaluated in
-// FP64 (closer, a pair's real-space term reaches 1e4-1e5 K, where FP32's ~1e-7
-// relative rounding would leave ~1e-2 K)
-constexpr float NEAR_COULOMB_R2 = 20.25f;
+// FP32 form, charged trials: Coulomb pairs closer than 6 A are evaluated in
+// double-float (ff.cuh near_coulomb_ff; closer, a pair's real-space term
+// reaches 1e2-1e5 K, where FP32's ~1e-7 relative rounding would leave up to
+// ~1e-2 K)
+constexpr float NEAR_COULOMB_R2 = 36.0f;
 constexpr int ATILE = 512;     // framework atoms per shared-memory tile
 constexpr int MAXS = 8;        // sites per guest molecule
 constexpr int MAXT = 64;       // LJ species
@@ -45,6 +46,11 @@ constexpr int MAXT = 64;       // LJ species
 // atoms' FP32 positions (the image then carries up to ~ulp(L) ~ 4e-6 A, which
 // beyond 1.25 sigma moves a pair energy by < 3e-4 K).
 constexpr int CLOSE_MAX = 16;
+// FP32 form, charged: a thread's near-Coulomb pairs (within 6 A) of one site
+// and tile are listed, up to NEAR_MAX, and evaluated after the tile's loop:
+// evaluated where found, a warp paid the whole double-float sequence for each
+// atom that was near any one of its 32 trials.
+constexpr int NEAR_MAX = 80;
 constexpr float CLOSE_SIGMA2 = 1.25f * 1.25f;
 constexpr float CUT_BAND = 1e-5f;  // relative band of r^2 around rc^2 redone in double-float
 
@@ -127,6 +133,7 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
     __shared__ PairCloseFF ppc[sizeof(Real) == 4 ? MAXS * MAXT : 1];
     __shared__ double red[WT];
     __shared__ uint16_t closej[sizeof(Real) == 4 ? CLOSE_MAX * WT : 1];
+    __shared__ uint16_t nearj[(sizeof(Real) == 4 && Q) ? NEAR_MAX * WT : 1];
 
     const int ns = P.n_sites;
     for (int i = threadIdx.x; i < ns * (int)P.n_species; i += WT) {
@@ -328,6 +335,25 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                             rce2f = (float)(P.rc_ewald * P.rc_ewald);
                 const PairF32W* rowf = ppf + s * MAXT;
                 ff close_acc{0.f, 0.f};
+                const ff alpha_ff = ff_from(P.alpha);
+                // the term of a near pair from the double-float displacement
+                // and charge, in double-float (FP64 beyond the erfc series)
+                auto near_term = [&](int j) -> double {
+                    const float4* t4 = reinterpret_cast<const float4*>(&tile[j]);
+                    const float4 ah = t4[0], al = t4[1];
+                    ff dx = ff_add(ff{ah.x, al.x}, ff{-px.hi, -px.lo});
+                    ff dy = ff_add(ff{ah.y, al.y}, ff{-py.hi, -py.lo});
+                    ff dz = ff_add(ff{ah.z, al.z}, ff{-pz.hi, -pz.lo});
+                    ff_min_image(P.lh, P.ll, P.linv, P.L.ortho, dx, dy, dz);
+                    double v;
+                    if (near_coulomb_ff(dx, dy, dz, ff{ah.w, al.w}, alpha_ff, v)) return v;
+                    const double ddx = (double)dx.hi + dx.lo, ddy = (double)dy.hi + dy.lo,
+                                 ddz = (double)dz.hi + dz.lo;
+                    const double rd = fmax(sqrt(ddx * ddx + ddy * ddy + ddz * ddz), 1e-6);
+                    return ((double)ah.w + (double)al.w) * (erfc(P.alpha * rd) / rd);
+                };
+                uint16_t* nl = nearj + threadIdx.x;  // stride WT: bank-conflict free
+                int nnear = 0;
                 for (int j = 0; j < cnt; ++j) {
                     const float4* t4 = reinterpret_cast<const float4*>(&tile[j]);
                     const float4 ah = t4[0], al = t4[1];
@@ -351,19 +377,16 @@ __device__ __forceinline__ void widom_block(const WidomParams& P, const WidomPtr
                         lj_acc += e;
                     }
                     if ((Q && P.charged) && r2 <= rce2f) {
-                        if (r2 < NEAR_COULOMB_R2) {
-                            // a near pair: in FP64 from the double-float
-                            // displacement and charge
-                            const double ddx = (double)dx.hi + dx.lo, ddy = (double)dy.hi + dy.lo,
-                                         ddz = (double)dz.hi + dz.lo;
-                            const double rd = fmax(sqrt(ddx * ddx + ddy * ddy + ddz * ddz), 1e-6);
-                            es_near += ((double)ah.w + (double)al.w) * (erfc(P.alpha * rd) / rd);
+                        if (r2 < NEAR_COULOMB_R2) {  // a near pair: listed
+                            if (nnear < NEAR_MAX) nl[WT * nnear++] = (uint16_t)j;
+                            else es_near += near_term(j);  // a crowded trial: at once
                         } else {
                             const float rf = sqrtf(r2);
                             es_acc += ah.w * (erfcf(alphaf * rf) / rf);
                         }
                     }
                 }
+                for (int k = 0; k < nnear; ++k) es_near += near_term(nl[WT * k]);
                 lj_close = (double)close_acc.hi + (double)close_acc.lo;
             }
             lj_site[s] += (double)lj_acc + lj_close;

@@ -575,7 +575,8 @@ def henry_time_to_1pct(A, torch, gcmc=True, cap_s=60.0):
         "henry_difference_in_combined_se": abs(learned["henry"] - uniform["henry"]) / se,
     }
     if gcmc:
-        out["gcmc_loading"] = loading_comparison(A, torch, pressures_bar=(10.0,), seconds=15.0)
+        out["gcmc_loading"] = loading_comparison(A, torch, pressures_bar=(10.0,), seconds=15.0,
+                                                 arms=("uniform", "uniform_orient", "learned"))
     return out
 
 
@@ -705,6 +706,9 @@ def loading_comparison(A, torch, pressures_bar=(0.1, 1.0, 10.0, 30.0), seconds=3
             row[name] = arm
         tu, tl = row["uniform"]["time_to_1pct_s"], row["learned"]["time_to_1pct_s"]
         row["speedup"] = (tu / tl) if (tu and tl) else None
+        if "uniform_orient" in row:  # the orientation trials alone
+            to = row["uniform_orient"]["time_to_1pct_s"]
+            row["speedup_orientation_trials"] = (tu / to) if (tu and to) else None
         out[f"{P_bar:g} bar"] = row
     return out
 

@@ -117,6 +117,13 @@ alea_status alea_probe_fp32_fma_tflops(double* out);
 /* The same with the packed two-lane FMA (fma.rn.f32x2), the instruction the
  * FP32 grid sweep issues; an FMA lane counts 2 FLOP. */
 alea_status alea_probe_fp32x2_fma_tflops(double* out);
+/* Test support for the FP32 forms' double-float near-pair arithmetic (no
+ * counterpart in the reference): n values from host arrays. mode 0: out[i] =
+ * erfc(in[i]) for 0 <= in[i] <= 2; mode 1: in holds n records (dx, dy, dz, q)
+ * and out[i] = q erfc(alpha r) / r, or NaN where alpha r is beyond the series
+ * (the kernels then take the FP64 form). */
+alea_status alea_test_ff_near(int32_t mode, const double* in, double* out, uint64_t n,
+                              double alpha);
 
 /* Device memory held idle by the library's block cache (no counterpart in the
  * reference, which allocates on the host). Device blocks of 64 MB and more are

@@ -37,8 +37,9 @@ def _loading(chains, n, equil, prod):
     return mean, sq
 
 
-@pytest.mark.parametrize("with_proposal", [False, True])
-def test_orientation_trials_ideal_gas_poisson(lib, with_proposal):
+@pytest.mark.parametrize("with_proposal,fp32", [(False, False), (True, False), (False, True)])
+def test_orientation_trials_ideal_gas_poisson(lib, with_proposal, fp32):
+    """(fp32: the FP32 form, which evaluates all k trials in one pass.)"""
     A, _ = lib
     fw = W.cubic_framework(seed=11)
     ff = A.LennardJones(np.zeros_like(fw.eps), fw.sigma, 12.8, A.SHIFTED)
@@ -49,7 +50,7 @@ def test_orientation_trials_ideal_gas_poisson(lib, with_proposal):
     f_pa = lam * T / V / O.PASCAL_TO_INTERNAL
     n = 128
     chains = A.GcmcChains(ff, p, fw.lattice, guest, T, [f_pa] * n, list(range(300, 300 + n)),
-                          [2] * n, max_molecules=200)
+                          [2] * n, max_molecules=200, precision=A.FP32 if fp32 else A.FP64)
     chains.set_orientation_trials(6)
     if with_proposal:
         P = A.Proposal(seed=23)
@@ -120,3 +121,68 @@ def test_one_orientation_trial_is_the_reference_move(lib, orc):
     _compare(gpu, cpu, charged=True)
     with pytest.raises(ValueError):
         gpu.set_orientation_trials(17)
+
+
+@pytest.mark.parametrize("k", [3, 6])
+def test_fused_trials_follow_the_pass_by_pass_form(lib, k):
+    """The FP32 form evaluates all k <= 8 trial orientations of a biased
+    insertion or deletion in one pass; the FP64 form evaluates them one pass
+    each. From the same seeds the two take the same draws, so move by move
+    they make the same decisions, and each move's energy change agrees as the
+    FP32 form's does for plain moves (test_gpu_gcmc_fp32.py): a biased
+    insertion's (the picked trial's energy) or deletion's (minus the
+    molecule's own) within 1e-5 x max(kT, |dU|); a translation's or
+    rotation's, a difference of two molecule energies, within 1e-5 x max(kT,
+    |dU|, E), E the largest molecule energy met. A decision can flip where a
+    ratio falls within that error of its uniform draw; each chain is compared
+    up to such a point, which must lie beyond most of the run."""
+    A, _ = lib
+    fw = W.cubic_framework(seed=12, charged=True)
+    fw.charge = fw.charge * 0.3
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    guest = W.co2_guest(fw)
+    alpha, kmax = W.ewald_parameters(fw.lattice, 12.0)
+    ew = A.Ewald(alpha, 12.0, kmax)
+    fug = A.peng_robinson_fugacity(*W.CO2_CRITICAL, T, 10e5)
+    n = 4
+    pair = []
+    for prec in (A.FP64, A.FP32):
+        ch = A.GcmcChains(ff, p, fw.lattice, guest, T, [fug] * n, list(range(40, 40 + n)),
+                          [5] * n, ewald=ew, max_molecules=300, precision=prec)
+        ch.set_orientation_trials(k)
+        pair.append(ch)
+    g64, g32 = pair
+    live = [True] * n
+    prev = [g64.info(c)["attempted"] for c in range(n)]
+    e_scale = [0.0] * n
+    compared = {0: 0, 1: 0, 2: 0, 3: 0}
+    moves = 600
+    for step in range(moves):
+        g64.run(1)
+        g32.run(1)
+        for c in range(n):
+            a, b = g64.info(c), g32.info(c)
+            took = np.array(a["attempted"]) - np.array(prev[c])
+            prev[c] = a["attempted"]
+            if not live[c]:
+                continue
+            if a["call_index"] != b["call_index"] or a["molecules"] != b["molecules"] or \
+                    a["accepted"] != b["accepted"] or a["attempted"] != b["attempted"]:
+                live[c] = False  # a decision flipped: the chains part here
+                continue
+            if took.sum() == 0 or not np.isfinite(a["last_du"]):
+                continue  # nothing to act on: no energy evaluated
+            move = int(np.argmax(took))
+            du64, du32 = a["last_du"], b["last_du"]
+            if abs(du64) > 1e5:  # an overlapping trial: both reject whatever its size
+                continue
+            if move >= 2:
+                e_scale[c] = max(e_scale[c], abs(du64))
+                assert abs(du32 - du64) <= 1e-5 * max(T, abs(du64)), (step, c, move, du64, du32)
+            else:
+                assert abs(du32 - du64) <= 1e-5 * max(T, abs(du64), e_scale[c]), \
+                    (step, c, move, du64, du32, e_scale[c])
+            compared[move] += 1
+    assert sum(compared.values()) >= 0.6 * n * moves, compared
+    assert compared[2] >= 100 and compared[3] >= 20, compared
