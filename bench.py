@@ -284,6 +284,8 @@ def main():
                     help="leave out the learned-vs-uniform half (profiling runs of the grid)")
     ap.add_argument("--workload", default="full", choices=["full", "small"],
                     help="small: 2x2x2 supercell for profiler captures (not a bench line)")
+    ap.add_argument("--henry-scatter", action="store_true",
+                    help="the learned K_H over six proposal seeds and three uniform shares")
     ap.add_argument("--henry-judge", type=float, default=None, metavar="SECONDS",
                     help="run the uniform-insertion judge of the learned Henry coefficient for "
                          "SECONDS and print one JSON line (no bench line)")
@@ -315,6 +317,12 @@ def main():
                                             orient=args.orientation_trials,
                                             arms=("uniform", "uniform_orient", "learned"))),
               flush=True)
+        return 0
+    if args.henry_scatter:
+        import torch
+        import aleator_gb300 as A
+        A.load_library()
+        henry_scatter(A, torch)
         return 0
     if args.henry_judge:
         import torch
@@ -601,6 +609,30 @@ def henry_judge(A, torch, seconds):
                             "difference_in_uniform_se":
                                 abs(learned["henry"] - uniform["henry"]) /
                                 (uniform["rel_std_error"] * uniform["henry"])}}
+
+
+def henry_scatter(A, torch, seeds=(1, 3, 5, 8, 13, 21), shares=(0.05, 0.2, 0.4)):
+    """The learned K_H across proposals: for each proposal seed (training
+    stream 100 + seed) and uniform share, a run to 1 % (trial seed 900 + seed,
+    stream 3) and a run of 2^25 trials (seed 500 + seed, stream 5). One JSON
+    line per run."""
+    fw, ff, p, ew, guest, T, alpha, kmax = henry_setup(A)
+    widom = A.Widom(ff, p, fw.lattice, guest, T, ewald=ew, precision=A.FP32)
+    for seed in seeds:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prop = fit_proposal(A, widom, seed=seed, stream=100 + seed)
+        torch.cuda.synchronize()
+        fit_s = time.perf_counter() - t0
+        for share in shares:
+            prop.tabulate(128, share)
+            r = run_to_target(torch, lambda f, n: widom.run_biased(prop, 900 + seed, 3, n, first_trial=f),
+                              T, 0.01, 20.0, 1 << 20, 1 << 22)
+            big = widom.run_biased(prop, 500 + seed, 5, 1 << 25)
+            print(json.dumps({"seed": seed, "share": share, "fit_s": fit_s,
+                              "to1pct_trials": r["trials"], "to1pct_s": r["seconds"],
+                              "to1pct_henry": r["henry"], "to1pct_se": r["rel_std_error"],
+                              "big_henry": big["henry"], "big_se": big["rel_std_error"]}), flush=True)
 
 
 def loading_run(A, torch, ff, p, fw, guest, ew, T, pressure_pa, learned, seconds, n=152,
