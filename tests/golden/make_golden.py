@@ -1,6 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a checkout that has the reference tree (default /root/reference):
+Run where the reference tree is present, naming its root as the argument or
+in ALEA_REFERENCE_ROOT:
 
     python tests/golden/make_golden.py [REFERENCE_ROOT] [--only=irmof1]
 
@@ -15,6 +16,7 @@ test_ewald_spce_water.cc:134-147). Nothing here runs at test time.
 from __future__ import annotations
 
 import json
+import os
 import re
 import sys
 import tempfile
@@ -83,7 +85,10 @@ def irmof1_fixture(refroot: Path, ref) -> dict:
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
-    refroot = Path(args[0] if args else "/root/reference")
+    root = args[0] if args else os.environ.get("ALEA_REFERENCE_ROOT")
+    if not root:
+        sys.exit("make_golden.py: name the reference root (argument or ALEA_REFERENCE_ROOT)")
+    refroot = Path(root)
     O.build_reference(str(refroot))
     ref = O.Reference()
     if only == ["irmof1"]:  # regenerate this one fixture, keep the others
