@@ -574,10 +574,13 @@ struct alea_proposal;
 alea_status alea_gcmc_set_proposal(alea_gcmc* g, const struct alea_proposal* p);
 /* The chains' energy form from the next run on: ALEA_FP64 (default; the
  * reference's arithmetic, trajectories equal to the reference's) or ALEA_FP32
- * (LJ and real-space pair terms in FP32 after an FP64 minimum image, pairs
- * closer than sigma in FP64, per-term S(k) deltas from FP32 phases; every sum,
- * S(k), the self and exclusion terms and the acceptance in FP64). No
- * counterpart in the reference. */
+ * (LJ and real-space pair terms in FP32 after a double-float minimum image,
+ * pairs closer than sigma and Coulomb pairs within 6 A in double-float,
+ * per-term S(k) deltas from FP32 phases; the sums and S(k) in double-float or
+ * FP64, the self and exclusion terms and the acceptance in FP64; up to 8
+ * orientation trials of a biased move in one energy pass). ALEA_FP32 needs
+ * framework atoms + max_molecules x sites below 2^24 (else
+ * ALEA_ERR_INVALID_ARGUMENT). No counterpart in the reference. */
 alea_status alea_gcmc_set_precision(alea_gcmc* g, int32_t precision);
 /* MonteCarloEngine's frameworkEnergyGrid (monte_carlo_engine.hpp:76-83,
  * .cc:341-374): from the next run on, a site's dispersion energy is its LJ
