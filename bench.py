@@ -103,7 +103,12 @@ def fp32_error(A, ff, parts, fw, guests, grid32):
     t0 = time.perf_counter()
     g64 = A.FrameworkEnergyGrid(ff, parts, fw.lattice, guests, SPACING, A.FP64)
     build_s = time.perf_counter() - t0
-    out = {"kT_K": 298.0, "fp64_build_s": build_s, "reference": "FP64 form of the same grid"}
+    st64 = g64.stats()
+    out = {"kT_K": 298.0, "fp64_build_s": build_s, "reference": "FP64 form of the same grid",
+           # the parity form's own rate on this workload (its one build, CUDA-event timed)
+           "fp64_form_kernel_ms": float(st64["last_kernel_ms"]),
+           "fp64_form_pair_evals_per_s":
+               float(st64["algorithmic_pairs"]) / (float(st64["last_kernel_ms"]) * 1e-3)}
     for s in guests:
         out[f"guest_species_{s}"] = fp32_error_stats(grid32.table(s), g64.table(s))
     del g64
