@@ -459,6 +459,12 @@ class OracleGcmc:
         self.L.orc_gcmc_set_tail.argtypes = [ctypes.c_void_p, ctypes.c_int]
         self.L.orc_gcmc_set_tail(self.h, 1 if on else 0)
 
+    def set_orientation_trials(self, k):
+        """Opt-in: orientation-biased insertion and deletion with k trials, in
+        the GPU chains' FP64 draw order (no reference counterpart)."""
+        self.L.orc_gcmc_set_orientation_trials.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self.L.orc_gcmc_set_orientation_trials(self.h, int(k))
+
     def molecules_of(self, species):
         self.L.orc_gcmc_molecules_of.restype = ctypes.c_uint64
         self.L.orc_gcmc_molecules_of.argtypes = [ctypes.c_void_p, ctypes.c_uint32]

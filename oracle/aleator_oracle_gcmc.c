@@ -75,7 +75,21 @@ int orc_gcmc_create(orc_gcmc* g, const orc_lj* lj, const orc_ewald_params* ew, c
             sp->q[s] = guests[k].charge[s];
         }
         sp->fugacity = fugacity_pa[k] * ORC_PASCAL_TO_INTERNAL; /* monte_carlo_engine.cc:212-219 */
+        /* the template about its centroid: per axis the sum over the sites in
+         * order, then each site less the sum / ns */
+        double c[3] = {0.0, 0.0, 0.0};
+        for (uint32_t s = 0; s < sp->ns; ++s) {
+            c[0] += sp->x[s];
+            c[1] += sp->y[s];
+            c[2] += sp->z[s];
+        }
+        for (uint32_t s = 0; s < sp->ns; ++s) {
+            sp->cx[s] = sp->x[s] - c[0] / (double)sp->ns;
+            sp->cy[s] = sp->y[s] - c[1] / (double)sp->ns;
+            sp->cz[s] = sp->z[s] - c[2] / (double)sp->ns;
+        }
     }
+    g->orient = 1;
     g->temperature = temperature;
     g->max_translation = max_translation;
     g->max_rotation = max_rotation;
@@ -381,6 +395,190 @@ static double tail_change(const orc_gcmc* g, uint64_t n_before, const uint64_t* 
 }
 
 void orc_gcmc_set_tail(orc_gcmc* g, int on) { g->tail = on; }
+void orc_gcmc_set_orientation_trials(orc_gcmc* g, int k) { g->orient = k < 1 ? 1 : k > 16 ? 16 : k; }
+
+/* ---- orientation-biased insertion and deletion (no reference counterpart):
+ * the standard orientational configurational-bias scheme, in the draw order
+ * and arithmetic of the GPU chains' FP64 form. An insertion draws its point
+ * as the molecule's centroid and a first orientation (the move's own draws),
+ * then k - 1 orientations (three calls each, the engine's argument order),
+ * evaluates the energy U_j of each trial, picks one with probability w_j / W
+ * (one call; w = exp(-U / T)) and accepts with W / k in place of exp(-dU/T).
+ * A deletion evaluates the molecule's energy U_0 (minus its removal's dU),
+ * then k - 1 random orientations of it about its centroid, each drawn just
+ * before its evaluation (U_j = U_0 + dU of that rotation), and accepts with
+ * k / W in place of exp(+U_0 / T). */
+#define ORC_MAXCB 16
+
+static uint64_t count_of_species(const orc_gcmc* g, uint32_t k);
+
+static void draw_trial_orientation(orc_gcmc* g, double quat[4]) {
+    double v[3];
+    v[0] = u01(g);
+    v[1] = u01(g);
+    v[2] = u01(g);
+    orc_random_unit_quaternion(v[0], v[1], v[2], quat);
+}
+
+/* the centred template of species k rotated by quat, about ref, into pos */
+static void trial_sites(const orc_gcmc* g, uint32_t k, const double ref[3], const double quat[4],
+                        double* pos) {
+    const orc_gcmc_species* sp = &g->spc[k];
+    for (uint32_t s = 0; s < sp->ns; ++s) {
+        const double local[3] = {sp->cx[s], sp->cy[s], sp->cz[s]};
+        double rot[3];
+        orc_rotate_by_quaternion(local, quat, rot);
+        pos[3 * s] = ref[0] + rot[0];
+        pos[3 * s + 1] = ref[1] + rot[1];
+        pos[3 * s + 2] = ref[2] + rot[2];
+    }
+}
+
+/* log(sum_j exp(lw_j) / k) and, when pick is non-NULL, one draw picking j
+ * with probability exp(lw_j) / sum */
+static double rosenbluth(orc_gcmc* g, const double* lw, int k, int* pick) {
+    double m = lw[0];
+    for (int j = 1; j < k; ++j) m = fmax(m, lw[j]);
+    double tot = 0.0;
+    for (int j = 0; j < k; ++j) tot += exp(lw[j] - m);
+    const double logw = m + log(tot / (double)k);
+    if (pick) {
+        const double u = u01(g) * tot;
+        *pick = k - 1;
+        double cum = 0.0;
+        for (int j = 0; j < k; ++j) {
+            cum += exp(lw[j] - m);
+            if (u < cum) {
+                *pick = j;
+                break;
+            }
+        }
+    }
+    return logw;
+}
+
+static void insertion_trials(orc_gcmc* g, uint32_t k, const double ref[3], const double q0[4]) {
+    const orc_gcmc_species* sp = &g->spc[k];
+    const int kt = g->orient < ORC_MAXCB ? g->orient : ORC_MAXCB;
+    const double T = g->temperature;
+    double quat[ORC_MAXCB][4];
+    memcpy(quat[0], q0, sizeof(double) * 4);
+    for (int j = 1; j < kt; ++j) draw_trial_orientation(g, quat[j]);
+    double lw[ORC_MAXCB] = {0.0}, pos[ORC_MAXCB][3 * ORC_MOLW];
+    uint64_t idx[ORC_MOLW];
+    for (int j = 0; j < kt; ++j) {
+        trial_sites(g, k, ref, quat[j], pos[j]);
+        place_sites(g, k, ref, quat[j], idx); /* the sites appended, then set to the trial's */
+        for (uint32_t s = 0; s < sp->ns; ++s) {
+            g->x[idx[s]] = pos[j][3 * s];
+            g->y[idx[s]] = pos[j][3 * s + 1];
+            g->z[idx[s]] = pos[j][3 * s + 2];
+        }
+        const double disp = dispersion(g, idx, sp->ns, NULL, 0);
+        const double elec = electro_real(g, idx, sp->ns, NULL, 0);
+        double rec = 0.0;
+        if (g->charged) {
+            double new_s[4 * ORC_MOLW];
+            pack_sites(g, idx, sp->ns, new_s);
+            rec = orc_ews_delta(&g->ews, NULL, 0, new_s, sp->ns, NULL, NULL, NULL, NULL);
+        }
+        lw[j] = -((disp + elec) + rec) / T;
+        g->n -= sp->ns;
+    }
+    int pick = kt - 1;
+    const double logw = rosenbluth(g, lw, kt, &pick);
+    const double cb_du = -lw[pick] * T;
+    place_sites(g, k, ref, quat[pick], idx);
+    for (uint32_t s = 0; s < sp->ns; ++s) {
+        g->x[idx[s]] = pos[pick][3 * s];
+        g->y[idx[s]] = pos[pick][3 * s + 1];
+        g->z[idx[s]] = pos[pick][3 * s + 2];
+    }
+    const double dut = tail_change(g, g->n - sp->ns, NULL, 0, sp->ns);
+    g->last_du = cb_du + dut;
+    const double volume = fabs(orc_volume(g->m));
+    const uint64_t before = g->n_species == 1 ? g->n_mol : count_of_species(g, k);
+    const double ratio = (sp->fugacity * volume / T) / (double)(before + 1) * exp(logw - dut / T);
+    if (accept(g, ratio)) {
+        if (g->charged) {
+            double new_s[4 * ORC_MOLW];
+            pack_sites(g, idx, sp->ns, new_s);
+            orc_ews_commit(&g->ews, NULL, 0, new_s, sp->ns);
+        }
+        ensure_mol_capacity(g, g->n_mol + 1);
+        memcpy(g->mol + g->n_mol * ORC_MOLW, idx, sizeof(uint64_t) * sp->ns);
+        g->mol_sp[g->n_mol] = k;
+        g->n_mol++;
+        maybe_resync(g);
+        g->accepted[2]++;
+        return;
+    }
+    g->n -= sp->ns;
+}
+
+/* the deletion of molecule mi (species k, count_before of it) with trials;
+ * returns 1 when accepted (the caller removes the molecule) */
+static int deletion_trials(orc_gcmc* g, uint64_t mi, uint32_t k, uint64_t count_before) {
+    const uint32_t ns = g->spc[k].ns;
+    const int kt = g->orient < ORC_MAXCB ? g->orient : ORC_MAXCB;
+    const double T = g->temperature;
+    uint64_t idx[ORC_MOLW];
+    memcpy(idx, g->mol + mi * ORC_MOLW, sizeof(uint64_t) * ns);
+    const double u_old = dispersion(g, idx, ns, NULL, 0);
+    const double e_old = electro_real(g, idx, ns, NULL, 0);
+    double old_s[4 * ORC_MOLW], orig[3 * ORC_MOLW];
+    double rec0 = 0.0;
+    if (g->charged) {
+        pack_sites(g, idx, ns, old_s);
+        rec0 = orc_ews_delta(&g->ews, old_s, ns, NULL, 0, NULL, NULL, NULL, NULL);
+    }
+    const double u0 = (u_old + e_old) - rec0;
+    double lw[ORC_MAXCB];
+    lw[0] = -u0 / T;
+    double ref[3] = {0.0, 0.0, 0.0};
+    for (uint32_t s = 0; s < ns; ++s) {
+        ref[0] += g->x[idx[s]];
+        ref[1] += g->y[idx[s]];
+        ref[2] += g->z[idx[s]];
+    }
+    for (int a = 0; a < 3; ++a) ref[a] /= (double)ns;
+    for (uint32_t s = 0; s < ns; ++s) {
+        orig[3 * s] = g->x[idx[s]];
+        orig[3 * s + 1] = g->y[idx[s]];
+        orig[3 * s + 2] = g->z[idx[s]];
+    }
+    for (int j = 1; j < kt; ++j) {
+        double quat[4], pos[3 * ORC_MOLW];
+        draw_trial_orientation(g, quat);
+        trial_sites(g, k, ref, quat, pos);
+        for (uint32_t s = 0; s < ns; ++s) {
+            g->x[idx[s]] = pos[3 * s];
+            g->y[idx[s]] = pos[3 * s + 1];
+            g->z[idx[s]] = pos[3 * s + 2];
+        }
+        const double u_new = dispersion(g, idx, ns, NULL, 0);
+        const double e_new = electro_real(g, idx, ns, NULL, 0);
+        double rec = 0.0;
+        if (g->charged) {
+            double new_s[4 * ORC_MOLW];
+            pack_sites(g, idx, ns, new_s);
+            rec = orc_ews_delta(&g->ews, old_s, ns, new_s, ns, NULL, NULL, NULL, NULL);
+        }
+        lw[j] = -(u0 + ((u_new - u_old) + (e_new - e_old) + rec)) / T;
+        for (uint32_t s = 0; s < ns; ++s) {
+            g->x[idx[s]] = orig[3 * s];
+            g->y[idx[s]] = orig[3 * s + 1];
+            g->z[idx[s]] = orig[3 * s + 2];
+        }
+    }
+    const double logw = rosenbluth(g, lw, kt, NULL);
+    const double dut = tail_change(g, g->n, idx, ns, 0);
+    g->last_du = -u0 + dut;
+    const double volume = fabs(orc_volume(g->m));
+    const double ratio =
+        (double)count_before / (g->spc[k].fugacity * volume / T) * exp(-logw - dut / T);
+    return accept(g, ratio);
+}
 
 static uint64_t count_of_species(const orc_gcmc* g, uint32_t k) {
     uint64_t c = 0;
@@ -407,6 +605,10 @@ static void attempt_insertion(orc_gcmc* g) {
     for (int c = 0; c < 3; ++c) ref[c] = (m[c] * u[0] + m[3 + c] * u[1]) + m[6 + c] * u[2];
     double quat[4] = {1.0, 0.0, 0.0, 0.0};
     if (sp->ns > 1) draw_orientation(g, quat);
+    if (g->orient > 1 && sp->ns > 1) {  /* orientation trials about the drawn centroid */
+        insertion_trials(g, k, ref, quat);
+        return;
+    }
     uint64_t idx[ORC_MOLW];
     place_sites(g, k, ref, quat, idx);
     const double disp = dispersion(g, idx, sp->ns, NULL, 0);
@@ -486,6 +688,23 @@ static void attempt_deletion(orc_gcmc* g) {
     const uint32_t ns = g->spc[k].ns;
     uint64_t idx[ORC_MOLW];
     memcpy(idx, g->mol + mi * ORC_MOLW, sizeof(uint64_t) * ns);
+    if (g->orient > 1 && ns > 1) {
+        if (deletion_trials(g, mi, k, count_before)) {
+            if (g->charged) {
+                double old_s[4 * ORC_MOLW];
+                pack_sites(g, idx, ns, old_s);
+                orc_ews_commit(&g->ews, old_s, ns, NULL, 0);
+            }
+            memmove(g->mol + mi * ORC_MOLW, g->mol + (mi + 1) * ORC_MOLW,
+                    sizeof(uint64_t) * (g->n_mol - mi - 1) * ORC_MOLW);
+            memmove(g->mol_sp + mi, g->mol_sp + mi + 1, sizeof(uint32_t) * (g->n_mol - mi - 1));
+            g->n_mol--;
+            remove_particle_indices(g, idx, ns);
+            maybe_resync(g);
+            g->accepted[3]++;
+        }
+        return;
+    }
     const double ui = dispersion(g, idx, ns, NULL, 0);
     const double ei = electro_real(g, idx, ns, NULL, 0);
     double old_s[4 * ORC_MOLW];

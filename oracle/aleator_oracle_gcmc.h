@@ -18,6 +18,7 @@ extern "C" {
 typedef struct {
     uint32_t ns;
     double x[ORC_MOLW], y[ORC_MOLW], z[ORC_MOLW], q[ORC_MOLW];
+    double cx[ORC_MOLW], cy[ORC_MOLW], cz[ORC_MOLW]; /* the template about its centroid */
     uint32_t lj[ORC_MOLW];
     double fugacity; /* K / Å^3 */
 } orc_gcmc_species;
@@ -49,6 +50,10 @@ typedef struct {
      * and swaps add U_tail(after) - U_tail(before), tailEnergyCorrection over
      * every particle (lennard_jones.cc:246-257) */
     int tail;
+    /* opt-in (no counterpart in the reference engine): orientation-biased
+     * insertion and deletion with `orient` trial orientations (1: the
+     * reference's moves) */
+    int orient;
     /* optional energy grid (tables borrowed, one per LJ species or NULL) */
     int grid;
     int gcounts[3];
@@ -88,6 +93,8 @@ void orc_gcmc_counters(const orc_gcmc* g, uint64_t* out10);
  * without a table); n_tables == 0 removes it. */
 /* the opt-in tail-correction change of insertions, deletions and swaps */
 void orc_gcmc_set_tail(orc_gcmc* g, int on);
+/* orientation-biased insertion and deletion with k trials (1 <= k <= 16) */
+void orc_gcmc_set_orientation_trials(orc_gcmc* g, int k);
 void orc_gcmc_set_grid(orc_gcmc* g, const int counts[3], uint32_t n_tables, const uint32_t* species,
                        const double* const* tables);
 

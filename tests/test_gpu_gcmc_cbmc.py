@@ -186,3 +186,31 @@ def test_fused_trials_follow_the_pass_by_pass_form(lib, k):
             compared[move] += 1
     assert sum(compared.values()) >= 0.6 * n * moves, compared
     assert compared[2] >= 100 and compared[3] >= 20, compared
+
+
+@pytest.mark.parametrize("k", [3, 6])
+def test_orientation_trials_follow_the_oracle(lib, orc, k):
+    """The FP64 form's orientation-biased insertions and deletions against
+    the oracle's restatement of them (the same draws, in the same order, and
+    the same arithmetic): move for move the same counters, particle order and
+    positions (1e-9), and the same Ewald energy (1e-10)."""
+    A, _ = lib
+    fw = W.cubic_framework(seed=12, charged=True)
+    fw.charge = fw.charge * 0.15
+    ew = dict(alpha=0.31, rc=12.0, kmax=5)
+    fug = orc.pr_fugacity(*W.CO2_CRITICAL, T, 1e6)
+    ff = A.LennardJones(fw.eps, fw.sigma, 12.8, A.SHIFTED)
+    p = A.ParticleData.from_framework(fw)
+    gpu = A.GcmcChains(ff, p, fw.lattice, W.co2_guest(fw), T, [fug], [3], [7],
+                       ewald=A.Ewald(0.31, 12.0, 5))
+    gpu.set_orientation_trials(k)
+    od = dict(eps=fw.eps, sigma=fw.sigma, cutoff=12.8, truncation=O.SHIFTED)
+    cpu = orc.gcmc(od, ew, fw.lattice, fw.x, fw.y, fw.z, fw.charge, fw.species, W.co2_guest(fw),
+                   T, fug, 3, 7)
+    cpu.set_orientation_trials(k)
+    for _ in range(3):
+        gpu.run(400)
+        cpu.run(400)
+        _compare(gpu, cpu, charged=True)
+    acc = gpu.info()["accepted"]
+    assert acc[2] > 0 and acc[3] > 0, acc
