@@ -742,13 +742,21 @@ def loading_comparison(A, torch, pressures_bar=(0.1, 1.0, 10.0, 30.0), seconds=3
             t_hit, est = loading_metrics(arm["traj"], ref, n)
             traj = arm.pop("traj")
             arm.update(time_to_1pct_s=t_hit, final_estimate=est,
+                       wall_s=float(traj[-1][0]) if traj else 0.0,
                        trajectory=[(round(t, 2), round(float(m.mean()), 2)) for t, m in traj[::3]])
             row[name] = arm
         tu, tl = row["uniform"]["time_to_1pct_s"], row["learned"]["time_to_1pct_s"]
-        row["speedup"] = (tu / tl) if (tu and tl) else None
+        wu = row["uniform"]["wall_s"]
+
+        def ratio(t_other):  # uniform's time over the arm's; a lower bound when uniform never got there
+            if not t_other:
+                return None, None
+            return (tu / t_other, None) if tu else (None, wu / t_other)
+
+        row["speedup"], row["speedup_lower_bound"] = ratio(tl)
         if "uniform_orient" in row:  # the orientation trials alone
-            to = row["uniform_orient"]["time_to_1pct_s"]
-            row["speedup_orientation_trials"] = (tu / to) if (tu and to) else None
+            row["speedup_orientation_trials"], row["speedup_orientation_trials_lower_bound"] = \
+                ratio(row["uniform_orient"]["time_to_1pct_s"])
         out[f"{P_bar:g} bar"] = row
     return out
 

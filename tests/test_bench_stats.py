@@ -51,3 +51,33 @@ def test_loading_time_to_one_percent():
     assert abs(est - 100.0) <= 0.5
     # never within 1 % of a wrong reference
     assert bench.loading_metrics(traj, 120.0, n)[0] is None
+
+
+def test_loading_comparison_reports_a_lower_bound_when_uniform_never_gets_there(monkeypatch):
+    """The comparison's bookkeeping on stand-in trajectories (no GPU): arms
+    that reach a 1 % loading get their time; the uniform arm that does not
+    makes each speed-up a lower bound, its wall time over the arm's time."""
+    import types
+    import bench
+
+    def fake_run(A, torch, ff, p, fw, guest, ew, T, P, learned, seconds, n=152, proposal=None,
+                 orient=1):
+        rng = np.random.default_rng(orient + 10 * learned)
+        tau = 0.3 if (orient > 1 and not learned) else (0.5 if learned else 3.0)
+        traj = [(1.25 * (b + 1), 100.0 * (1 - np.exp(-1.25 * (b + 1) / tau)) + rng.normal(0, 0.3, n))
+                for b in range(12)]
+        return {"fit_seconds": 0.0, "traj": traj, "moves_per_chain": 1}
+
+    monkeypatch.setattr(bench, "loading_run", fake_run)
+    monkeypatch.setattr(bench, "henry_setup",
+                        lambda A: (types.SimpleNamespace(lattice=None), None, None, None, None,
+                                   298.0, 0.3, 10))
+    monkeypatch.setattr(bench, "fit_proposal", lambda A, w: None)
+    A = types.SimpleNamespace(Widom=lambda *a, **k: None, FP32=1)
+    torch = types.SimpleNamespace(cuda=types.SimpleNamespace(synchronize=lambda: None))
+    row = bench.loading_comparison(A, torch, pressures_bar=(10.0,), seconds=15.0, n=32,
+                                   arms=("uniform", "uniform_orient", "learned"))["10 bar"]
+    assert row["uniform"]["time_to_1pct_s"] is None and row["uniform"]["wall_s"] == 15.0
+    assert row["uniform_orient"]["time_to_1pct_s"] == 2.5
+    assert row["speedup"] is None and row["speedup_lower_bound"] == 15.0 / 2.5
+    assert row["speedup_orientation_trials_lower_bound"] == 15.0 / 2.5
