@@ -25,6 +25,15 @@
 // removal). Every 100 accepted moves S(k) is rebuilt as the framework's S(k)
 // plus the guest sites in index order, the reference's summation order.
 //
+// The FP32 form (alea_gcmc_set_precision) keeps that draw order and
+// bookkeeping and moves the per-pair and per-term work to the FP32 pipe:
+// pair terms in FP32 from double-float displacements; Coulomb pairs within
+// 6 A deferred to per-warp lists and evaluated after the pair loop, one a
+// thread, in double-float (ff.cuh near_coulomb_ff); S(k) committed as
+// double-float. An orientation-biased insertion or deletion (no reference
+// counterpart) evaluates its k <= 8 trials in one pass in this form, one pass
+// a trial in the FP64 form; both take the same draws.
+//
 // Layout in HBM: read-only framework (x, y, z, q as double4 + LJ type), mixed
 // LJ table, k-term table (k, weight, index triple, framework S(k)); per chain:
 // guest sites SoA (x, y, z, q, type), molecule -> particle index table, the
